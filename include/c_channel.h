@@ -1,0 +1,151 @@
+/*
+ * c_channel -- GB300 drop-in for the C entry points of the shadow-channel
+ * SWIG module (channel/channel.i) plus batched additions.
+ *
+ * Plain C ABI: complex numbers are {double re, im} (the layout of FFTW-2's
+ * fftw_complex, channel/mcomplex.h:19-22), arrays are caller-owned,
+ * C-contiguous and updated in place exactly as the SWIG INPLACE_ARRAY4
+ * typemaps do.  The dimension arguments that follow each array are the ones
+ * SWIG passes; a mismatch aborts the process like the reference's assert().
+ *
+ * Shapes: coefficients [Nz][2][Ny-2][Nx/2]; flow [3][3Nx/2][qpts][3Nz/2],
+ * qpts = 3Ny/2.  All arithmetic is FP64 on the GPU; the host only moves data.
+ *
+ * One global instance per process, as in the reference (channel/main.h
+ * keeps all state in globals; channel/__init__.py:80-82 enforces one init).
+ */
+#ifndef SHADOW_CHANNEL_GB300_C_CHANNEL_H
+#define SHADOW_CHANNEL_GB300_C_CHANNEL_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    double re, im;
+} chn_complex;
+
+/* ---- reference entry points (channel/channel.i) ---------------------- */
+
+/* channel.i:18-22 -> channel.c:207 init().  Returns 0, or 1 (EXIT_FAILURE)
+   for Nx % 4 != 0, Nz % 2 != 0, Ny <= 4, an unsupported FFT length or an
+   allocation failure.  flux is 2*meanU as the Python layer passes it. */
+int c_init(int Nx, int Ny, int Nz, double Lx, double Lz, double Re,
+           double flux, double dt, int nsteps);
+
+/* channel.i:27-30 -> channel.c:52 destroy() */
+void c_destroy(void);
+
+/* channel.i:38-52 -> channel.c:399 primal().  A zero-sized array (all four
+   dims 0) starts from the laminar profile plus a rand() perturbation. */
+void c_primal(int ru_steps, chn_complex *C_given, int Nz_dup, int Nvar_dup,
+              int Ny_dup, int Nx_dup);
+
+/* channel.i:60-70 -> channel.c:486 tangent() */
+void c_tangent(int start_step, int end_step, chn_complex *IC_given,
+               int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup, int inhomo);
+
+/* channel.i:78-88 -> channel.c:596 adjoint() */
+void c_adjoint(int start_step, int end_step, chn_complex *AC_given,
+               int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup, int inhomo,
+               double strength);
+
+/* channel.i:96-105 -> channel.c:704 ddt_project() */
+double c_ddt_project(int i_step, chn_complex *IC_given, int Nz_dup,
+                     int Nvar_dup, int Ny_dup, int Nx_dup);
+
+/* channel.i:115-125 / 133-142: pointer to the stored (incremental) solution
+   at step i_step.  The pointer refers to a library-owned host mirror that
+   is refreshed by every call; it stays valid until c_destroy(). */
+void c_getsoln(int i_step, chn_complex **MC_ptr, int *Nz_ptr, int *Nvar_ptr,
+               int *Ny_ptr, int *Nx_ptr);
+void c_getincresoln(int i_step, chn_complex **MIC_ptr, int *Nz_ptr,
+                    int *Nvar_ptr, int *Ny_ptr, int *Nx_ptr);
+
+/* channel.i:152-170 -> spec2phys.c:10 spec2phys() */
+void c_spec2phys(chn_complex *C_ptr, int Nz_dup, int Nvar_dup, int Ny_dup,
+                 int Nx_dup, double *flow_ptr, int Nd_flow, int Nx_flow,
+                 int Ny_flow, int Nz_flow);
+
+/* channel.i:178-205 -> channel.c:791/889.  HDF5 is not part of this build;
+   these write / read the same datasets (alpha, beta as [dimR][Nz][Nx/2]
+   {real, imaginary} records, Nx, Ny, Nz, dt, 1/Re, mpg) in a raw
+   little-endian container described in INTEGRATION.md. */
+void c_read_solution(char *filename, chn_complex *C_ptr, int Nz_dup,
+                     int Nvar_dup, int Ny_dup, int Nx_dup);
+void c_save_solution(char *filename, chn_complex *C_ptr, int Nz_dup,
+                     int Nvar_dup, int Ny_dup, int Nx_dup);
+
+/* channel.i:212-219: quadrature points and weights (library-owned) */
+void c_quad(double **y_ptr, int *qpts_ptr1, double **w_ptr, int *qpts_ptr2);
+
+/* channel.i:222-229 */
+int c_qpts(void);
+int c_dimR(void);
+int c_dimQ(void);
+int c_Nx(void);
+int c_Nz(void);
+int c_nsteps(void);
+
+/* ---- additions (no counterpart in the reference) --------------------- */
+
+/* Status of the last call: 0 ok; bit 0 = the CFL limit stopped the time loop
+   (the reference prints and returns silently, channel/pass1.c:133-137);
+   bit 1 = non-finite values seen; negative = CUDA or argument error. */
+int c_last_error(void);
+const char *c_last_error_message(void);
+/* largest CFL number seen by the last primal/tangent call */
+double c_last_cfl(void);
+
+/* Batched segments: nseg independent trajectories on the c_init grid, each
+   with ntan tangents; the adjoint couples (strength != 0) to the stored
+   trajectory of tangent `couple`.  Host arrays, segment-major. */
+int c_batch_init(int nseg, int ntan, int couple);
+int c_batch_destroy(void);
+/* primal trajectories for all segments; C [nseg][Nz][2][dimR][Nx/2] in/out */
+int c_batch_primal(int ru_steps, chn_complex *C);
+/* tangents on stored primal trajectories; IC [nseg][ntan][...] in/out;
+   inhomo[ntan] selects the mean-flux forcing per tangent */
+int c_batch_tangent(int start_step, int end_step, chn_complex *IC,
+                    const int *inhomo);
+/* primal and tangents advanced together from C (fused forward sweep) */
+int c_batch_forward(int start_step, int end_step, chn_complex *C,
+                    chn_complex *IC, const int *inhomo);
+/* adjoints; AC [nseg][...] in/out */
+int c_batch_adjoint(int start_step, int end_step, chn_complex *AC,
+                    double strength);
+/* MC / MIC of one segment at step i_step into out [Nz][2][dimR][Nx/2] */
+int c_batch_getsoln(int seg, int i_step, chn_complex *out);
+int c_batch_getincresoln(int seg, int i_step, chn_complex *out);
+
+/* The same batched calls on device-resident arrays (CUDA device pointers,
+   same layouts); no host copies.  stream 0 = the library's stream. */
+int c_batch_forward_dev(int start_step, int end_step, chn_complex *C,
+                        chn_complex *IC, const int *inhomo);
+int c_batch_adjoint_dev(int start_step, int end_step, chn_complex *AC,
+                        double strength);
+int c_batch_primal_dev(int ru_steps, chn_complex *C);
+int c_batch_tangent_dev(int start_step, int end_step, chn_complex *IC,
+                        const int *inhomo);
+
+/* wait for all queued device work of the library */
+int c_synchronize(void);
+/* kernel launches issued by the library since c_init (for bookkeeping) */
+long long c_launch_count(void);
+/* FP64 fused-multiply-add throughput of this GPU in TFLOP/s (2 flop/FMA),
+   measured with a register-only kernel; used as the roofline peak. */
+double c_fp64_peak_tflops(void);
+
+/* The time-invariant setup tables on the host (no GPU needed): which =
+   0 Q, 1 Q', 2 Q'', 3 R, 4 R' (values at the quadrature points, [qpts][n]),
+   5..9 the same weighted and transposed ([n][qpts]), 10 <Q,Q>, 11 <Q',Q'>,
+   12 <Q'',Q''> ([Ny-4][9] bands), 13 <R,R>, 14 <R',R'> ([Ny-2][5] bands),
+   15 quadrature points, 16 weights.  Writes when n is large enough; returns
+   the table size, or -1 for bad arguments. */
+int c_setup_table(int Nx, int Ny, int Nz, double Lx, double Lz, double Re,
+                  double flux, double dt, int which, double *out, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,194 @@
+"""Channel-flow DNS with tangent and adjoint solvers on a GB300.
+
+Python 3 counterpart of the reference package ``channel`` (channel/__init__.py):
+same module parameters, same functions, same array shapes.  The work happens
+in libc_channel.so (FP64 CUDA kernels for sm_103a) through ``c_channel``.
+
+Coefficient arrays are complex128 [Nz, 2, Ny-2, Nx/2]; physical fields are
+float64 [3, 3Nx/2, qpts, 3Nz/2] with qpts = 3Ny/2.
+"""
+import numpy as np
+
+from . import c_channel
+
+# global lock (per process), channel/__init__.py:6
+__is_initialized__ = False
+
+# default parameters, channel/__init__.py:10-26
+Nx = 16
+Ny = 33
+Nz = 16
+Lx = 1.6
+Lz = 1.6
+dt = .01
+meanU = 1.
+Re = 5000
+
+
+def _shape():
+    return (c_channel.c_Nz(), 2, c_channel.c_dimR(), c_channel.c_Nx() // 2)
+
+
+def quad():
+    y, w = c_channel.c_quad()
+    return y.copy(), w.copy()
+
+
+def save_solution(filename, C):
+    """Save the solution C (and the last tangent) to ``filename`` (raw
+    container).  Must be called after init()."""
+    if not filename.endswith('.hd5'):
+        filename += '.hd5'
+    assert C.shape == _shape()
+    c_channel.c_save_solution(filename, C)
+
+
+def read_solution(filename):
+    """Read a solution written by save_solution; returns complex [Nz, 2, dimR, Nx/2]."""
+    if not filename.endswith('.hd5'):
+        filename += '.hd5'
+    C = np.zeros(_shape(), complex)
+    c_channel.c_read_solution(str(filename), C)
+    return C
+
+
+def get_solution(i_step, copy=True):
+    """Primal solution at step i_step (not counting run-up steps)."""
+    C = c_channel.c_getsoln(int(i_step))
+    assert C.shape == _shape()
+    if copy:
+        C = C.copy()
+    return C
+
+
+def init(n_steps, ru_steps=0, restart=None):
+    """Must be called before any other call of this module; runs the primal.
+    restart: None (perturbed laminar start) or a solution file name."""
+    global __is_initialized__
+    assert not __is_initialized__
+    __is_initialized__ = True
+    assert n_steps >= 0 and ru_steps >= 0
+    rc = c_channel.c_init(int(Nx), int(Ny), int(Nz), float(Lx), float(Lz), float(Re),
+                          float(meanU * 2), float(dt), int(n_steps))
+    if rc != 0:
+        __is_initialized__ = False
+        raise RuntimeError("c_init failed: " + c_channel.c_last_error_message())
+    if restart is None:
+        c_channel.c_primal(int(ru_steps), np.zeros([0, 0, 0, 0], complex))
+    else:
+        C = read_solution(restart)
+        assert C.shape == _shape()
+        c_channel.c_primal(int(ru_steps), C)
+
+
+def para_init(n_steps, C):
+    """Like init, but from the given coefficient array (parallel LSS)."""
+    global __is_initialized__
+    assert not __is_initialized__
+    __is_initialized__ = True
+    assert n_steps >= 0
+    rc = c_channel.c_init(int(Nx), int(Ny), int(Nz), float(Lx), float(Lz), float(Re),
+                          float(meanU * 2), float(dt), int(n_steps))
+    if rc != 0:
+        __is_initialized__ = False
+        raise RuntimeError("c_init failed: " + c_channel.c_last_error_message())
+    assert C.shape == _shape()
+    c_channel.c_primal(0, C)
+
+
+def destroy():
+    global __is_initialized__
+    assert __is_initialized__
+    __is_initialized__ = False
+    c_channel.c_destroy()
+
+
+def primal(C_init):
+    """Run the primal from C_init for nsteps; C_init holds the final state after."""
+    assert C_init.shape == _shape()
+    c_channel.c_primal(0, C_init)
+
+
+def tangent(start_step, end_step, IC_init, inhomo):
+    """Tangent from start_step to end_step; IC_init updated in place.
+    inhomo != 0 adds the mean-flux (meanU) forcing (channel/increproject0.c:209-214)."""
+    assert IC_init.shape == _shape()
+    assert 0 <= start_step <= end_step <= c_channel.c_nsteps()
+    c_channel.c_tangent(int(start_step), int(end_step), IC_init, int(inhomo))
+
+
+def adjoint(start_step, end_step, AC_init, inhomo, strength):
+    assert AC_init.shape == _shape()
+    assert 0 <= end_step <= start_step <= c_channel.c_nsteps()
+    c_channel.c_adjoint(int(start_step), int(end_step), AC_init, int(inhomo), float(strength))
+
+
+def spec2phys(solution):
+    if isinstance(solution, str):
+        solution = read_solution(solution)
+    if isinstance(solution, int):
+        solution = get_solution(solution, copy=False)
+    assert solution.dtype == complex
+    assert solution.shape == _shape()
+    flow = np.zeros([3, int(c_channel.c_Nx() * 3 // 2), c_channel.c_qpts(),
+                     int(c_channel.c_Nz() * 3 // 2)], np.float64)
+    c_channel.c_spec2phys(np.ascontiguousarray(solution), flow)
+    return flow
+
+
+def ddt_project(i_step, v):
+    """Project v against the primal time derivative at i_step; v updated in
+    place; returns the removed component (channel/channel.c:704-780)."""
+    return c_channel.c_ddt_project(int(i_step), v)
+
+
+def vel(i_step):
+    """Streamwise velocity field at step i_step."""
+    return spec2phys(get_solution(i_step, copy=True))[0]
+
+
+def velAvg(start_step, end_step, T, profile=True):
+    """Time-averaged streamwise velocity profile (or its centreline value)."""
+    uavg = np.zeros(c_channel.c_qpts()) if profile else 0.0
+    assert 0 <= start_step <= end_step <= c_channel.c_nsteps()
+    for i in range(start_step, end_step):
+        u = vel(i).mean(2).mean(0)
+        if not profile:
+            u = u[c_channel.c_qpts() // 2 + 1]
+        uavg = uavg + (dt / T) * u
+    return uavg
+
+
+def Ivel(i_step, project=False):
+    """Incremental (tangent) streamwise velocity at step i_step."""
+    IC = c_channel.c_getincresoln(int(i_step)).copy()
+    assert IC.shape == _shape()
+    if project:
+        ddt_project(i_step, IC)
+    return spec2phys(IC)[0]
+
+
+def IvelAvg(start_step, end_step, T, profile=True):
+    vavg = np.zeros(c_channel.c_qpts()) if profile else 0.0
+    assert 0 <= start_step <= end_step <= c_channel.c_nsteps()
+    for i in range(start_step, end_step):
+        v = Ivel(i, project=False).mean(2).mean(0)
+        if not profile:
+            v = v[c_channel.c_qpts() // 2 + 1]
+        vavg = vavg + (dt / T) * v
+    return vavg
+
+
+def uavgGrad(n_chunk, chunk_bounds, T, uavg, zeta, profile=True):
+    """Time-averaged sensitivity of the mean streamwise profile to the mass
+    flux, with the LSS time-dilation terms zeta (channel/__init__.py:275-299)."""
+    grad = np.zeros(c_channel.c_qpts()) if profile else 0.0
+    for i in range(n_chunk):
+        start_step = chunk_bounds[i]
+        end_step = chunk_bounds[i + 1]
+        vavg = IvelAvg(start_step, end_step, T, profile)
+        uEnd = vel(end_step).mean(2).mean(0)
+        if not profile:
+            uEnd = uEnd[c_channel.c_qpts() // 2 + 1]
+        grad = grad + vavg + (1. / T) * zeta[i] * (uEnd - uavg)
+    return grad

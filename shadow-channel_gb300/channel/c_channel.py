@@ -1,0 +1,231 @@
+"""ctypes binding of libc_channel.so with the call signatures of the SWIG
+module ``c_channel`` (channel/channel.i), so code written against the
+reference's extension keeps working:
+
+    c_init(Nx, Ny, Nz, Lx, Lz, Re, flux, dt, nsteps) -> int
+    c_primal(ru_steps, C)                  C: complex128 [Nz, 2, Ny-2, Nx/2], in place
+    c_tangent(start, end, IC, inhomo)
+    c_adjoint(start, end, AC, inhomo, strength)
+    c_ddt_project(i_step, IC) -> float
+    c_getsoln(i_step) / c_getincresoln(i_step) -> ndarray (library-owned buffer)
+    c_spec2phys(C, flow)                   flow: float64 [3, 3Nx/2, qpts, 3Nz/2]
+    c_read_solution(filename, C) / c_save_solution(filename, C)
+    c_quad() -> (y, w)
+    c_qpts(), c_dimR(), c_dimQ(), c_Nx(), c_Nz(), c_nsteps()
+
+SWIG's INPLACE_ARRAY4 typemaps reject arrays that are not C-contiguous
+complex128; so does this module (TypeError).  The library has no CPU code
+path: if the shared library is missing this module raises ImportError.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent.parent
+_LIBPATH = Path(os.environ.get("CHN_LIBRARY", _PKG / "libc_channel.so"))
+
+if not _LIBPATH.exists():
+    raise ImportError(f"libc_channel.so not found at {_LIBPATH}; build it with "
+                      f"`python shadow-channel_gb300/build.py` (needs nvcc, sm_103a)")
+
+_lib = ctypes.CDLL(str(_LIBPATH))
+
+_i, _d, _vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+_pp = ctypes.POINTER(ctypes.c_void_p)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+_lib.c_init.argtypes = [_i, _i, _i, _d, _d, _d, _d, _d, _i]
+_lib.c_init.restype = _i
+_lib.c_destroy.argtypes = []
+_lib.c_destroy.restype = None
+_lib.c_primal.argtypes = [_i, _vp, _i, _i, _i, _i]
+_lib.c_primal.restype = None
+_lib.c_tangent.argtypes = [_i, _i, _vp, _i, _i, _i, _i, _i]
+_lib.c_tangent.restype = None
+_lib.c_adjoint.argtypes = [_i, _i, _vp, _i, _i, _i, _i, _i, _d]
+_lib.c_adjoint.restype = None
+_lib.c_ddt_project.argtypes = [_i, _vp, _i, _i, _i, _i]
+_lib.c_ddt_project.restype = _d
+_lib.c_getsoln.argtypes = [_i, _pp, _ip, _ip, _ip, _ip]
+_lib.c_getsoln.restype = None
+_lib.c_getincresoln.argtypes = [_i, _pp, _ip, _ip, _ip, _ip]
+_lib.c_getincresoln.restype = None
+_lib.c_spec2phys.argtypes = [_vp, _i, _i, _i, _i, _vp, _i, _i, _i, _i]
+_lib.c_spec2phys.restype = None
+_lib.c_read_solution.argtypes = [ctypes.c_char_p, _vp, _i, _i, _i, _i]
+_lib.c_read_solution.restype = None
+_lib.c_save_solution.argtypes = [ctypes.c_char_p, _vp, _i, _i, _i, _i]
+_lib.c_save_solution.restype = None
+_lib.c_quad.argtypes = [ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), _ip,
+                        ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), _ip]
+_lib.c_quad.restype = None
+for _n in ("c_qpts", "c_dimR", "c_dimQ", "c_Nx", "c_Nz", "c_nsteps", "c_last_error",
+           "c_batch_destroy", "c_synchronize"):
+    getattr(_lib, _n).argtypes = []
+    getattr(_lib, _n).restype = _i
+_lib.c_last_error_message.argtypes = []
+_lib.c_last_error_message.restype = ctypes.c_char_p
+_lib.c_last_cfl.argtypes = []
+_lib.c_last_cfl.restype = _d
+_lib.c_launch_count.argtypes = []
+_lib.c_launch_count.restype = ctypes.c_longlong
+_lib.c_fp64_peak_tflops.argtypes = []
+_lib.c_fp64_peak_tflops.restype = _d
+_lib.c_batch_init.argtypes = [_i, _i, _i]
+_lib.c_batch_init.restype = _i
+_lib.c_batch_primal.argtypes = [_i, _vp]
+_lib.c_batch_primal.restype = _i
+_lib.c_batch_tangent.argtypes = [_i, _i, _vp, _vp]
+_lib.c_batch_tangent.restype = _i
+_lib.c_batch_forward.argtypes = [_i, _i, _vp, _vp, _vp]
+_lib.c_batch_forward.restype = _i
+_lib.c_batch_adjoint.argtypes = [_i, _i, _vp, _d]
+_lib.c_batch_adjoint.restype = _i
+_lib.c_batch_getsoln.argtypes = [_i, _i, _vp]
+_lib.c_batch_getsoln.restype = _i
+_lib.c_batch_getincresoln.argtypes = [_i, _i, _vp]
+_lib.c_batch_getincresoln.restype = _i
+for _n in ("c_batch_primal_dev",):
+    getattr(_lib, _n).argtypes = [_i, _vp]
+    getattr(_lib, _n).restype = _i
+_lib.c_batch_tangent_dev.argtypes = [_i, _i, _vp, _vp]
+_lib.c_batch_tangent_dev.restype = _i
+_lib.c_batch_forward_dev.argtypes = [_i, _i, _vp, _vp, _vp]
+_lib.c_batch_forward_dev.restype = _i
+_lib.c_batch_adjoint_dev.argtypes = [_i, _i, _vp, _d]
+_lib.c_batch_adjoint_dev.restype = _i
+
+LIBRARY_PATH = str(_LIBPATH)
+lib = _lib
+
+
+def _inplace4(a, dtype, name):
+    if not isinstance(a, np.ndarray) or a.dtype != dtype or a.ndim != 4 or not a.flags["C_CONTIGUOUS"] \
+            or not a.flags["WRITEABLE"]:
+        raise TypeError(f"{name}: expected a writeable C-contiguous {np.dtype(dtype).name} array of rank 4")
+    return a.ctypes.data, a.shape
+
+
+def c_init(Nx, Ny, Nz, Lx, Lz, Re, flux, dt, nstep):
+    return _lib.c_init(int(Nx), int(Ny), int(Nz), float(Lx), float(Lz), float(Re), float(flux),
+                       float(dt), int(nstep))
+
+
+def c_destroy():
+    _lib.c_destroy()
+
+
+def c_primal(ru_steps, C_given):
+    p, s = _inplace4(C_given, np.complex128, "c_primal")
+    _lib.c_primal(int(ru_steps), p if C_given.size else None, *s)
+
+
+def c_tangent(start_step, end_step, IC_given, inhomo):
+    p, s = _inplace4(IC_given, np.complex128, "c_tangent")
+    _lib.c_tangent(int(start_step), int(end_step), p, *s, int(inhomo))
+
+
+def c_adjoint(start_step, end_step, AC_given, inhomo, strength):
+    p, s = _inplace4(AC_given, np.complex128, "c_adjoint")
+    _lib.c_adjoint(int(start_step), int(end_step), p, *s, int(inhomo), float(strength))
+
+
+def c_ddt_project(i_step, IC_given):
+    p, s = _inplace4(IC_given, np.complex128, "c_ddt_project")
+    return _lib.c_ddt_project(int(i_step), p, *s)
+
+
+def _traj(fn, i_step):
+    ptr = ctypes.c_void_p()
+    d = [ctypes.c_int() for _ in range(4)]
+    fn(int(i_step), ctypes.byref(ptr), *[ctypes.byref(v) for v in d])
+    shape = tuple(v.value for v in d)
+    n = int(np.prod(shape))
+    buf = (ctypes.c_double * (2 * n)).from_address(ptr.value)
+    return np.frombuffer(buf, dtype=np.complex128).reshape(shape)
+
+
+def c_getsoln(i_step):
+    return _traj(_lib.c_getsoln, i_step)
+
+
+def c_getincresoln(i_step):
+    return _traj(_lib.c_getincresoln, i_step)
+
+
+def c_spec2phys(C_ptr, flow_ptr):
+    pc, sc = _inplace4(C_ptr, np.complex128, "c_spec2phys")
+    pf, sf = _inplace4(flow_ptr, np.float64, "c_spec2phys")
+    _lib.c_spec2phys(pc, *sc, pf, *sf)
+
+
+def c_read_solution(filename, C_ptr):
+    p, s = _inplace4(C_ptr, np.complex128, "c_read_solution")
+    _lib.c_read_solution(str(filename).encode(), p, *s)
+
+
+def c_save_solution(filename, C_ptr):
+    p, s = _inplace4(C_ptr, np.complex128, "c_save_solution")
+    _lib.c_save_solution(str(filename).encode(), p, *s)
+
+
+def c_quad():
+    y = ctypes.POINTER(ctypes.c_double)()
+    w = ctypes.POINTER(ctypes.c_double)()
+    n1, n2 = ctypes.c_int(), ctypes.c_int()
+    _lib.c_quad(ctypes.byref(y), ctypes.byref(n1), ctypes.byref(w), ctypes.byref(n2))
+    return (np.ctypeslib.as_array(y, shape=(n1.value,)), np.ctypeslib.as_array(w, shape=(n2.value,)))
+
+
+def c_qpts():
+    return _lib.c_qpts()
+
+
+def c_dimR():
+    return _lib.c_dimR()
+
+
+def c_dimQ():
+    return _lib.c_dimQ()
+
+
+def c_Nx():
+    return _lib.c_Nx()
+
+
+def c_Nz():
+    return _lib.c_Nz()
+
+
+def c_nsteps():
+    return _lib.c_nsteps()
+
+
+# ---- additions ---------------------------------------------------------------
+
+def c_last_error():
+    return _lib.c_last_error()
+
+
+def c_last_error_message():
+    return _lib.c_last_error_message().decode()
+
+
+def c_last_cfl():
+    return _lib.c_last_cfl()
+
+
+def c_launch_count():
+    return _lib.c_launch_count()
+
+
+def c_fp64_peak_tflops():
+    return _lib.c_fp64_peak_tflops()
+
+
+def c_synchronize():
+    return _lib.c_synchronize()

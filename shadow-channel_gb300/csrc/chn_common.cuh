@@ -1,0 +1,98 @@
+// Shared device-side definitions for the GB300 channel-flow step.
+//
+// Layouts (all complex numbers are {double re, im}, FP64 throughout):
+//   coefficients  C[Nz][2][R][X]            R = Ny-2, X = Nx/2, [..][0] alpha, [..][1] beta
+//   velocity      U[Nz][5][Q][X]            Q = 3Ny/2 quadrature planes
+//                 slots 0..4 = u, v, w, du/dy, dw/dy (channel/minChnl.h:44-49)
+//   nonlinear     H[Nz][5][Q][X]            slot 0 Hz, 1 Hx, 2 Hy; adjoint adds 3 Sx, 4 Sz
+//                                           (channel/minChnl.h:50-52, pass2.c:474-566)
+//   physical      P[f][Q][pz][px]           pz = 3Nz/2, px = 3Nx/2, reals
+//                 f = 0 u, 1 v, 2 w, 3 wz, 4 wx, 5 wy (the reference's CT slot order)
+//   flow (spec2phys output) flow[3][px][Q][pz] (channel/spec2phys.c:80-86)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace chn {
+
+struct cpx {
+  double re, im;
+};
+
+// RK3 coefficient tables, forward (channel/project.c:44-47) and adjoint
+// (channel/adjproject.c:34-37).  The implicit-side coefficient b takes three
+// distinct values {1/6, 2/3, 0}; LHS factorizations are stored per distinct
+// value (index below), explicit matrices per distinct a in {1/3, -1/2}.
+struct RK {
+  double a[3], b[3], c[3], d[3];
+  int bidx[3];       // index of b[k] among {1/6, 2/3, 0}
+  int aidx_next[3];  // index of a[k+1] among {1/3, -1/2} (k < 2)
+};
+
+// Status bits of the per-instance device status word.
+enum : uint32_t {
+  ST_CFL = 1u,        // pass1: CFL number >= 2.8, loop stopped (channel/pass1.c:116-138)
+  ST_NONFINITE = 2u,  // a non-finite value was seen in a physical field (diagnostic only)
+};
+
+// Grid description plus device tables; passed by value to every kernel.
+struct Grid {
+  int Nx, Ny, Nz, X, Q, R, D, pz, px, Qh;  // Qh = (Q+1)/2 plane pairs
+  double dt, re, flux, norm, cfl1, cfl3;
+  const double* Kx;      // [X]
+  const double* Kz;      // [Nz]
+  const double* K2;      // [Nz][X]
+  const double* kxK2;    // [Nz][X]  kx/K2 (0 for the mean mode)
+  const double* kzK2;    // [Nz][X]  kz/K2
+  const double* cfl2;    // [Q]
+  const double* W;       // [Q] quadrature weights
+  // basis values at the quadrature points, row-major [Q][D] / [Q][R]
+  const double* Bq;      // Q   (1-y^2)^2 P_j
+  const double* Bqp;     // Q'
+  const double* Bqpp;    // Q''
+  const double* Br;      // R   (1-y^2) P_j
+  const double* Brp;     // R'
+  // weighted transposes [D][Q] / [R][Q]: Xw[i][j] = w_j X[j][i]
+  const double* Wq;      // Qw
+  const double* Wqp;     // Qpw
+  const double* Wqpp;    // Qppw
+  const double* Wr;      // Rw
+  const double* Wrp;     // Rpw
+  // banded systems, per (z, x): no-pivot LU factors of the LHS, and the
+  // explicit right-hand-side matrices; 9 every-other diagonals for the v
+  // (alpha) system, 5 for the g (beta) system, centre column 4 / 2.
+  const double* luA;     // [3][Nz][X][D][9]
+  const double* luB;     // [3][Nz][X][R][5]
+  const double* exA;     // [2][Nz][X][D][9]
+  const double* exB;     // [2][Nz][X][R][5]
+  // mean-flow (kx,kz) = (0,0) systems on the R basis
+  const double* lu0;     // [3][R][5]   Rs + re b dt Rps, LU factors
+  const double* ex0;     // [2][R][5]   Rs - re a dt Rps
+  const double* add0;    // [4][R]      flux-correction vectors: [0] forward, [1+bidx] adjoint
+  const double* rwsum;   // [R]         sum_j Rw[i][j]
+  // FFT twiddles exp(-2 pi i k/N), k < N, for N = pz and N = px
+  const cpx* twz;
+  const cpx* twx;
+};
+
+__host__ __device__ inline size_t coef_size(const Grid& g) { return (size_t)g.Nz * 2 * g.R * g.X; }
+__host__ __device__ inline size_t u_size(const Grid& g) { return (size_t)g.Nz * 5 * g.Q * g.X; }
+__host__ __device__ inline size_t plane_size(const Grid& g) { return (size_t)g.pz * g.px; }
+
+// One batched array: instance i lives at base + i * stride (elements).
+template <typename T>
+struct Batch {
+  T* base;
+  long long stride;
+  __host__ __device__ T* at(int i) const { return base + (long long)i * stride; }
+};
+
+__device__ __forceinline__ cpx cmul(cpx a, cpx b) {
+  cpx r;
+  r.re = fma(a.re, b.re, -a.im * b.im);
+  r.im = fma(a.re, b.im, a.im * b.re);
+  return r;
+}
+
+}  // namespace chn

@@ -1,0 +1,1140 @@
+// Host orchestration and the C ABI (include/c_channel.h).
+//
+// One substage of every solver is a short fixed pipeline of batched kernels
+// (reconstruct -> physical transforms -> products -> implicit solve); one
+// time step is three substages.  The trajectory slot each kernel touches is
+// derived on the device from a step counter that the last kernel of the step
+// advances, so a step is captured once into a CUDA graph and replayed for
+// every time step of a call.
+//
+// The reference keeps one solver per process in globals (channel/main.h:81-201)
+// and the Python layer enforces a single init (channel/__init__.py:80-82);
+// this library keeps one Engine per process likewise.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/c_channel.h"
+#include "chn_common.cuh"
+#include "kernels.h"
+#include "setup.h"
+
+namespace chn {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+
+static int g_status = 0;
+static std::string g_msg;
+static double g_cfl = 0.0;
+static long long g_launches = 0;
+
+static void set_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_status = code;
+  g_msg = buf;
+}
+
+#define CK(call)                                                                   \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) {                                                       \
+      set_error(-1, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return false;                                                                \
+    }                                                                              \
+  } while (0)
+
+#define LK(call)            \
+  do {                      \
+    ++g_launches;           \
+    CK(call);               \
+  } while (0)
+
+// the reference asserts shapes and aborts (channel/channel.i:45-48)
+static void shape_assert(bool ok, const char* what) {
+  if (!ok) {
+    fprintf(stderr, "c_channel: assertion failed: %s\n", what);
+    fflush(stderr);
+    abort();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// device tables
+// ---------------------------------------------------------------------------
+
+struct DevTables {
+  HostTables ht;
+  Grid g{};
+  std::vector<void*> ptrs;
+  double* luQs = nullptr;
+  double* luRs = nullptr;
+
+  template <typename T>
+  bool up(const std::vector<T>& v, const T** out) {
+    void* p = nullptr;
+    size_t n = v.size() * sizeof(T);
+    if (n == 0) n = sizeof(T);
+    CK(cudaMalloc(&p, n));
+    ptrs.push_back(p);
+    if (!v.empty()) CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *out = reinterpret_cast<const T*>(p);
+    return true;
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+};
+
+static bool fft_length_ok(int n) {
+  if (n % 3) return false;
+  int m = n / 3;
+  for (int f : {4, 2, 3, 5, 7})
+    while (m % f == 0) m /= f;
+  return m == 1;
+}
+
+static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx, double Lz, double Re,
+                                double flux, double dt) {
+  const char* err = nullptr;
+  if (!build_tables(Nx, Ny, Nz, Lx, Lz, Re, flux, dt, T.ht, &err)) {
+    set_error(1, "%s", err);
+    return false;
+  }
+  HostTables& h = T.ht;
+  if (!fft_length_ok(h.pz) || !fft_length_ok(h.px)) {
+    set_error(1, "unsupported transform length (3Nx/2 = %d, 3Nz/2 = %d): Nx/2 and Nz/2 must factor into 2, 3, 5, 7",
+              h.px, h.pz);
+    return false;
+  }
+  Grid& g = T.g;
+  g.Nx = h.Nx; g.Ny = h.Ny; g.Nz = h.Nz; g.X = h.X; g.Q = h.Q; g.R = h.R; g.D = h.D;
+  g.pz = h.pz; g.px = h.px; g.Qh = (h.Q + 1) / 2;
+  g.dt = dt; g.re = h.re; g.flux = flux;
+  g.norm = 1.0 / ((3. * Nx / 2.) * (3. * Nz / 2.));
+  g.cfl1 = h.cfl1; g.cfl3 = h.cfl3;
+  bool ok = T.up(h.Kx, &g.Kx) && T.up(h.Kz, &g.Kz) && T.up(h.K2, &g.K2) && T.up(h.kxK2, &g.kxK2) &&
+            T.up(h.kzK2, &g.kzK2) && T.up(h.cfl2, &g.cfl2) && T.up(h.w, &g.W) && T.up(h.Bq, &g.Bq) &&
+            T.up(h.Bqp, &g.Bqp) && T.up(h.Bqpp, &g.Bqpp) && T.up(h.Br, &g.Br) && T.up(h.Brp, &g.Brp) &&
+            T.up(h.Wq, &g.Wq) && T.up(h.Wqp, &g.Wqp) && T.up(h.Wqpp, &g.Wqpp) && T.up(h.Wr, &g.Wr) &&
+            T.up(h.Wrp, &g.Wrp) && T.up(h.luA, &g.luA) && T.up(h.luB, &g.luB) && T.up(h.exA, &g.exA) &&
+            T.up(h.exB, &g.exB) && T.up(h.lu0, &g.lu0) && T.up(h.ex0, &g.ex0) && T.up(h.add0, &g.add0) &&
+            T.up(h.rwsum, &g.rwsum);
+  if (!ok) return false;
+  const double* tz;
+  const double* tx;
+  if (!T.up(h.twz, &tz) || !T.up(h.twx, &tx)) return false;
+  g.twz = reinterpret_cast<const cpx*>(tz);
+  g.twx = reinterpret_cast<const cpx*>(tx);
+  std::vector<double> qs(h.Qs), rs(h.Rs);
+  band_lu(qs.data(), 9, 4, 4, h.D);
+  band_lu(rs.data(), 5, 2, 2, h.R);
+  const double *a, *b;
+  if (!T.up(qs, &a) || !T.up(rs, &b)) return false;
+  T.luQs = const_cast<double*>(a);
+  T.luRs = const_cast<double*>(b);
+  prepare_kernels(g);
+  CK(cudaGetLastError());
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// per-run working set: nseg segments, ntan tangents each
+// ---------------------------------------------------------------------------
+
+struct Work {
+  int nseg = 0, ntan = 0, nsteps = 0, couple = 0;
+  size_t csz = 0, usz = 0, psz = 0;   // coefficient, velocity, physical (6 fields) sizes
+  long long traj = 0;                 // elements per stored trajectory
+  cpx *MC = nullptr, *MIC = nullptr;
+  cpx *Cp = nullptr, *Sp = nullptr, *Ct = nullptr, *St = nullptr, *Ca = nullptr, *Sa = nullptr;
+  cpx *Up = nullptr, *Ut = nullptr, *Uprev = nullptr, *Ul = nullptr, *dC = nullptr, *io = nullptr;
+  double *Pp = nullptr, *Pt = nullptr, *Pprev = nullptr, *Pl = nullptr, *flow = nullptr;
+  double *part = nullptr, *r = nullptr, *cflmax = nullptr;
+  uint32_t* status = nullptr;
+  int* step = nullptr;
+  std::vector<void*> ptrs;
+  static constexpr int kDotBlocks = 64;
+
+  template <typename T>
+  bool alloc(T** p, size_t n) {
+    void* q = nullptr;
+    CK(cudaMalloc(&q, n * sizeof(T) + 16));
+    CK(cudaMemset(q, 0, n * sizeof(T) + 16));
+    ptrs.push_back(q);
+    *p = reinterpret_cast<T*>(q);
+    return true;
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+    *this = Work();
+  }
+  bool create(const Grid& g, int nseg_, int ntan_, int nsteps_, int couple_) {
+    nseg = nseg_; ntan = ntan_; nsteps = nsteps_; couple = couple_;
+    csz = coef_size(g);
+    usz = u_size(g);
+    psz = (size_t)6 * g.Q * plane_size(g);
+    traj = (long long)(3 * (long long)nsteps + 1) * (long long)csz;
+    const size_t nt = (size_t)nseg * (ntan > 0 ? ntan : 1);
+    return alloc(&MC, (size_t)nseg * traj) && alloc(&MIC, (size_t)nseg * traj) && alloc(&Cp, nseg * csz) &&
+           alloc(&Sp, nseg * csz) && alloc(&Ct, nt * csz) && alloc(&St, nt * csz) && alloc(&Ca, nseg * csz) &&
+           alloc(&Sa, nseg * csz) && alloc(&Up, nseg * usz) && alloc(&Ut, nt * usz) &&
+           alloc(&Uprev, nseg * usz) && alloc(&Ul, nseg * usz) && alloc(&dC, nseg * csz) &&
+           alloc(&io, nt * csz) && alloc(&Pp, nseg * psz) && alloc(&Pt, nt * psz) &&
+           alloc(&Pprev, nseg * psz) && alloc(&Pl, nseg * psz) && alloc(&flow, (size_t)3 * g.Q * plane_size(g)) &&
+           alloc(&part, (size_t)nseg * kDotBlocks * 2) && alloc(&r, nseg) && alloc(&cflmax, nseg) &&
+           alloc(&status, nseg) && alloc(&step, 4);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// engine
+// ---------------------------------------------------------------------------
+
+struct Engine {
+  DevTables T;
+  Work single;     // the reference API: one segment, one tangent
+  Work batch;      // c_batch_*
+  bool have_batch = false;
+  cudaStream_t st = nullptr;
+  int nsteps = 0;
+  std::vector<double> qy, qw;
+  cpx* host_mc = nullptr;   // pinned mirrors for c_getsoln / c_getincresoln
+  cpx* host_mic = nullptr;
+  std::vector<cpx> last_ic;  // the reference's global IC after the last tangent call
+};
+
+static Engine* E = nullptr;
+
+// sizes and shorthands
+static inline Batch<const cpx> cb(const cpx* p, long long s) { return Batch<const cpx>{p, s}; }
+static inline Batch<cpx> mb(cpx* p, long long s) { return Batch<cpx>{p, s}; }
+static inline Batch<const double> cbd(const double* p, long long s) { return Batch<const double>{p, s}; }
+static inline Batch<double> mbd(double* p, long long s) { return Batch<double>{p, s}; }
+static inline SlotRef noslot() { return SlotRef{nullptr, 0, 0, 0}; }
+
+// ---------------------------------------------------------------------------
+// stage pipelines
+// ---------------------------------------------------------------------------
+
+struct FwdOpts {
+  bool adv_primal;      // advance the primal (and store MC) or read it from MC
+  bool tangents;        // advance the tangents (store MIC of tangent `couple`)
+  int ru;               // run-up steps of the primal (MC slot offset)
+  uint32_t forced_mask; // tangents with the mean-flux forcing
+  bool raw_u_first;     // the primal velocity of substage 0 is already in Up
+};
+
+static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
+  const Grid& g = e.T.g;
+  cudaStream_t st = e.st;
+  const int nt = w.nseg * w.ntan;
+  for (int k = 0; k < 3; ++k) {
+    ReconArgs rp{};
+    rp.ninst = w.nseg;
+    rp.U = mb(w.Up, w.usz);
+    rp.status = w.status;
+    rp.sdiv = 1;
+    if (o.adv_primal) {
+      rp.C = cb(w.Sp, w.csz);
+      rp.slot = noslot();
+    } else {
+      rp.C = cb(w.MC, w.traj);
+      rp.slot = SlotRef{w.step, 3, k, (long long)w.csz};  // state before substage k: MC[3n + k]
+    }
+    if (!(o.raw_u_first && k == 0)) LK(launch_recon(g, rp, st));
+    if (o.tangents) {
+      ReconArgs rt{};
+      rt.ninst = nt;
+      rt.C = cb(w.St, w.csz);
+      rt.slot = noslot();
+      rt.U = mb(w.Ut, w.usz);
+      rt.status = w.status;
+      rt.sdiv = w.ntan;
+      LK(launch_recon(g, rt, st));
+    }
+    PhysArgs pp{};
+    pp.U = cb(w.Up, w.usz);
+    pp.P = mbd(w.Pp, w.psz);
+    pp.nfields = 6;
+    pp.ninst = w.nseg;
+    pp.status = w.status;
+    pp.sdiv = 1;
+    pp.cflmax = w.cflmax;
+    pp.cfl_check = k == 0;  // channel/pass1.c:117
+    pp.skip_blocked = 1;
+    LK(launch_phys_inverse(g, pp, st));
+    if (o.tangents) {
+      PhysArgs pt = pp;
+      pt.U = cb(w.Ut, w.usz);
+      pt.P = mbd(w.Pt, w.psz);
+      pt.ninst = nt;
+      pt.sdiv = w.ntan;
+      pt.cflmax = nullptr;
+      pt.cfl_check = 0;
+      LK(launch_phys_inverse(g, pt, st));
+      ProdArgs ap{};
+      ap.Pp = cbd(w.Pp, w.psz);
+      ap.pdiv = w.ntan;
+      ap.Pt = cbd(w.Pt, w.psz);
+      ap.H = mb(w.Ut, w.usz);
+      ap.ninst = nt;
+      ap.status = w.status;
+      ap.sdiv = w.ntan;
+      LK(launch_products_fwd(g, ap, st));
+    }
+    if (o.adv_primal) {
+      ProdArgs ap{};
+      ap.Pp = cbd(w.Pp, w.psz);
+      ap.pdiv = 1;
+      ap.Pt = cbd(nullptr, 0);
+      ap.H = mb(w.Up, w.usz);
+      ap.ninst = w.nseg;
+      ap.status = w.status;
+      ap.sdiv = 1;
+      LK(launch_products_fwd(g, ap, st));
+    }
+    if (o.tangents) {
+      SolveArgs sa{};
+      sa.H = cb(w.Ut, w.usz);
+      sa.Hprev = cb(nullptr, 0);
+      sa.Cc = mb(w.Ct, w.csz);
+      sa.Sout = mb(w.St, w.csz);
+      sa.T = mb(w.MIC, w.traj);
+      sa.tdiv = w.ntan;
+      sa.tsel = w.couple;
+      sa.slot = SlotRef{w.step, 3, k + 1, (long long)w.csz};  // MIC[3n + k + 1]
+      sa.k = k;
+      sa.adjoint = 0;
+      sa.mean_mode = MEAN_TAN_HOMOG;
+      sa.forced_mask = o.forced_mask;
+      sa.mdiv = w.ntan;
+      sa.ninst = nt;
+      sa.status = w.status;
+      sa.sdiv = w.ntan;
+      LK(launch_solve(g, sa, st));
+    }
+    if (o.adv_primal) {
+      SolveArgs sa{};
+      sa.H = cb(w.Up, w.usz);
+      sa.Hprev = cb(nullptr, 0);
+      sa.Cc = mb(w.Cp, w.csz);
+      sa.Sout = mb(w.Sp, w.csz);
+      sa.T = mb(w.MC, w.traj);
+      sa.tdiv = 1;
+      sa.tsel = 0;
+      sa.slot = SlotRef{w.step, 3, k + 1 - 3 * o.ru, (long long)w.csz};  // MC[3(n - ru) + k + 1]
+      sa.k = k;
+      sa.adjoint = 0;
+      sa.mean_mode = MEAN_PRIMAL;
+      sa.forced_mask = 0;
+      sa.mdiv = 1;
+      sa.ninst = w.nseg;
+      sa.status = w.status;
+      sa.sdiv = 1;
+      LK(launch_solve(g, sa, st));
+    }
+  }
+  LK(launch_step_advance(w.step, +1, st));
+  return true;
+}
+
+// spec2phys of nseg coefficient arrays (optionally at a trajectory slot) into P (3 fields)
+static bool enqueue_spec2phys(Engine& e, Work& w, Batch<const cpx> C, SlotRef slot, cpx* U, double* P, int nseg) {
+  const Grid& g = e.T.g;
+  ReconArgs ra{};
+  ra.C = C;
+  ra.slot = slot;
+  ra.U = mb(U, w.usz);
+  ra.ninst = nseg;
+  ra.status = nullptr;
+  ra.sdiv = 1;
+  LK(launch_recon(g, ra, e.st));
+  PhysArgs pa{};
+  pa.U = cb(U, w.usz);
+  pa.P = mbd(P, w.psz);
+  pa.nfields = 3;
+  pa.ninst = nseg;
+  pa.status = nullptr;
+  pa.sdiv = 1;
+  LK(launch_phys_inverse(g, pa, e.st));
+  return true;
+}
+
+// adjoint coupling to the stored tangent at i_step = *step + add
+// (channel/channel.c:624-631 and 682-689 with ddt_project, channel.c:704-780)
+static bool enqueue_coupling(Engine& e, Work& w, int add, double coef) {
+  const Grid& g = e.T.g;
+  DdtArgs d{w.MC, w.traj, w.step, add, w.nseg};
+  LK(launch_ddt_diff(g, d, w.dC, e.st));
+  if (!enqueue_spec2phys(e, w, cb(w.dC, w.csz), noslot(), w.Uprev, w.Pprev, w.nseg)) return false;
+  const SlotRef icslot{w.step, 3, 3 * add, (long long)w.csz};
+  if (!enqueue_spec2phys(e, w, cb(w.MIC, w.traj), icslot, w.Ul, w.Pl, w.nseg)) return false;
+  LK(launch_ddt_dots(g, cbd(w.Pprev, w.psz), cbd(w.Pl, w.psz), w.part, Work::kDotBlocks, w.nseg, e.st));
+  LK(launch_ddt_apply(g, w.part, Work::kDotBlocks, w.nseg, cb(w.MIC, w.traj), icslot, mb(nullptr, 0),
+                      cb(w.dC, w.csz), w.r, mb(w.Ca, w.csz), coef, e.st));
+  return true;
+}
+
+static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt) {
+  const Grid& g = e.T.g;
+  cudaStream_t st = e.st;
+  const double coef = 0.5 * strength_dt;
+  if (strength_dt != 0.0 && !enqueue_coupling(e, w, 0, coef)) return false;
+  for (int k = 0; k < 3; ++k) {
+    // primal at the current substage: MC[3n - k - 1]; previous: MC[3n - k - 2]
+    ReconArgs r{};
+    r.ninst = w.nseg;
+    r.status = nullptr;
+    r.sdiv = 1;
+    r.C = cb(w.MC, w.traj);
+    r.slot = SlotRef{w.step, 3, -k - 1, (long long)w.csz};
+    r.U = mb(w.Up, w.usz);
+    LK(launch_recon(g, r, st));
+    if (k < 2) {
+      r.slot = SlotRef{w.step, 3, -k - 2, (long long)w.csz};
+      r.U = mb(w.Uprev, w.usz);
+      LK(launch_recon(g, r, st));
+    }
+    r.C = cb(w.Sa, w.csz);
+    r.slot = noslot();
+    r.U = mb(w.Ul, w.usz);
+    LK(launch_recon(g, r, st));
+    PhysArgs p{};
+    p.nfields = 6;
+    p.ninst = w.nseg;
+    p.status = nullptr;
+    p.sdiv = 1;
+    p.U = cb(w.Up, w.usz);
+    p.P = mbd(w.Pp, w.psz);
+    LK(launch_phys_inverse(g, p, st));
+    if (k < 2) {
+      p.U = cb(w.Uprev, w.usz);
+      p.P = mbd(w.Pprev, w.psz);
+      LK(launch_phys_inverse(g, p, st));
+    }
+    p.nfields = 3;
+    p.U = cb(w.Ul, w.usz);
+    p.P = mbd(w.Pl, w.psz);
+    LK(launch_phys_inverse(g, p, st));
+    ProdArgs a{};
+    a.pdiv = 1;
+    a.ninst = w.nseg;
+    a.status = nullptr;
+    a.sdiv = 1;
+    a.Pp = cbd(w.Pp, w.psz);
+    a.Pt = cbd(w.Pl, w.psz);
+    a.H = mb(w.Up, w.usz);
+    LK(launch_products_adj(g, a, st));
+    if (k < 2) {
+      a.Pp = cbd(w.Pprev, w.psz);
+      a.H = mb(w.Uprev, w.usz);
+      LK(launch_products_adj(g, a, st));
+    }
+    SolveArgs s{};
+    s.H = cb(w.Up, w.usz);
+    s.Hprev = cb(w.Uprev, w.usz);
+    s.Cc = mb(w.Ca, w.csz);
+    s.Sout = mb(w.Sa, w.csz);
+    s.T = mb(nullptr, 0);
+    s.tdiv = 1;
+    s.tsel = 0;
+    s.slot = noslot();
+    s.k = k;
+    s.adjoint = 1;
+    s.mean_mode = MEAN_ADJOINT;
+    s.mdiv = 1;
+    s.ninst = w.nseg;
+    s.status = nullptr;
+    s.sdiv = 1;
+    LK(launch_solve(g, s, st));
+  }
+  if (strength_dt != 0.0 && !enqueue_coupling(e, w, -1, coef)) return false;
+  LK(launch_step_advance(w.step, -1, st));
+  return true;
+}
+
+// capture one step into a graph and replay it nsteps times
+template <typename F>
+static bool run_steps(Engine& e, int nsteps, F&& enqueue) {
+  if (nsteps <= 0) return true;
+  if (nsteps == 1) return enqueue();
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  CK(cudaStreamBeginCapture(e.st, cudaStreamCaptureModeThreadLocal));
+  const long long before = g_launches;
+  bool ok = enqueue();
+  cudaError_t ce = cudaStreamEndCapture(e.st, &graph);
+  if (!ok) {
+    if (graph) cudaGraphDestroy(graph);
+    return false;
+  }
+  CK(ce);
+  const long long per_step = g_launches - before;
+  cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CK(ie);
+  for (int n = 0; n < nsteps; ++n) {
+    cudaError_t le = cudaGraphLaunch(exec, e.st);
+    if (le != cudaSuccess) {
+      cudaGraphExecDestroy(exec);
+      set_error(-1, "cudaGraphLaunch: %s", cudaGetErrorString(le));
+      return false;
+    }
+  }
+  g_launches += per_step * (nsteps - 1);
+  CK(cudaGraphExecDestroy(exec));
+  return true;
+}
+
+static bool set_step(Engine& e, Work& w, int n) {
+  CK(cudaMemcpyAsync(w.step, &n, sizeof(int), cudaMemcpyHostToDevice, e.st));
+  return true;
+}
+
+static bool reset_status(Engine& e, Work& w) {
+  CK(cudaMemsetAsync(w.status, 0, sizeof(uint32_t) * w.nseg, e.st));
+  CK(cudaMemsetAsync(w.cflmax, 0, sizeof(double) * w.nseg, e.st));
+  return true;
+}
+
+static bool collect_status(Engine& e, Work& w) {
+  std::vector<uint32_t> s(w.nseg);
+  std::vector<double> c(w.nseg);
+  CK(cudaMemcpyAsync(s.data(), w.status, sizeof(uint32_t) * w.nseg, cudaMemcpyDeviceToHost, e.st));
+  CK(cudaMemcpyAsync(c.data(), w.cflmax, sizeof(double) * w.nseg, cudaMemcpyDeviceToHost, e.st));
+  CK(cudaStreamSynchronize(e.st));
+  uint32_t any = 0;
+  double cm = 0.0;
+  for (int i = 0; i < w.nseg; ++i) {
+    any |= s[i];
+    cm = std::fmax(cm, c[i]);
+  }
+  g_cfl = cm;
+  g_status = (int)any;
+  if (any & ST_CFL) g_msg = "CFL condition violated: time loop stopped (channel/pass1.c:133-137)";
+  else if (any & ST_NONFINITE) g_msg = "non-finite values in the physical fields";
+  else g_msg.clear();
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// operations shared by the single and batched APIs (device pointers in/out)
+// ---------------------------------------------------------------------------
+
+// primal from C (device, nseg arrays) or, when C == nullptr, the laminar start
+static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
+  const size_t csz = w.csz;
+  CK(cudaMemsetAsync(w.MC, 0, sizeof(cpx) * (size_t)w.nseg * w.traj, e.st));
+  if (C) {
+    CK(cudaMemcpy2DAsync(w.Cp, csz * sizeof(cpx), C, csz * sizeof(cpx), csz * sizeof(cpx), w.nseg,
+                         cudaMemcpyDeviceToDevice, e.st));
+  } else {
+    // channel/channel.c:409-422: laminar (1 - y^2) flux 3/4 plus rand() noise on
+    // (kz, kx) = (1, 1), then the Gram projection of initAlphaBeta()
+    const Grid& g = e.T.g;
+    std::vector<cpx> U(w.usz, cpx{0.0, 0.0});
+    for (int i = 0; i < g.Q; ++i)
+      U[((size_t)0 * 5 + 0) * g.Q * g.X + (size_t)i * g.X + 0] =
+          cpx{(1.0 - e.qy[i] * e.qy[i]) * g.flux * 3. / 4, 0.0};
+    for (int i = 0; i < g.Q; ++i) {
+      const double re = (rand() / (double)RAND_MAX - 0.5);
+      const double im = (rand() / (double)RAND_MAX - 0.5);
+      U[((size_t)1 * 5 + 0) * g.Q * g.X + (size_t)i * g.X + 1] = cpx{re, im};
+    }
+    CK(cudaMemcpyAsync(w.Ul, U.data(), sizeof(cpx) * w.usz, cudaMemcpyHostToDevice, e.st));
+    // the projection overwrites alpha rows < Ny-4 and beta; other rows keep the carried array
+    for (int s = 0; s < w.nseg; ++s) {
+      LK(launch_project_init(g, w.Ul, w.Cp + (size_t)s * csz, e.T.luQs, e.T.luRs, e.st));
+      // the first substage runs on these samples, not on their projection:
+      // the reference never rebuilds U after initAlphaBeta() (channel/channel.c:409-422)
+      CK(cudaMemcpyAsync(w.Up + (size_t)s * w.usz, w.Ul, sizeof(cpx) * w.usz, cudaMemcpyDeviceToDevice, e.st));
+    }
+  }
+  CK(cudaMemcpyAsync(w.Sp, w.Cp, sizeof(cpx) * csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
+  CK(cudaMemcpy2DAsync(w.MC, w.traj * sizeof(cpx), w.Cp, csz * sizeof(cpx), csz * sizeof(cpx), w.nseg,
+                       cudaMemcpyDeviceToDevice, e.st));
+  if (!reset_status(e, w) || !set_step(e, w, 0)) return false;
+  FwdOpts o{true, false, ru, 0u, false};
+  int todo = w.nsteps + ru;
+  if (!C && todo > 0) {
+    FwdOpts first = o;
+    first.raw_u_first = true;
+    if (!enqueue_forward_step(e, w, first)) return false;
+    --todo;
+  }
+  return run_steps(e, todo, [&] { return enqueue_forward_step(e, w, o); });
+}
+
+// tangents (and optionally the primal) from start to end; IC device [nseg*ntan]
+static bool op_forward(Engine& e, Work& w, int start, int end, const cpx* C, const cpx* IC, uint32_t forced_mask,
+                       bool adv_primal) {
+  const size_t csz = w.csz;
+  const int nt = w.nseg * w.ntan;
+  if (adv_primal) {
+    if (C) {
+      CK(cudaMemcpy2DAsync(w.Cp, csz * sizeof(cpx), C, csz * sizeof(cpx), csz * sizeof(cpx), w.nseg,
+                           cudaMemcpyDeviceToDevice, e.st));
+    } else {
+      CK(cudaMemcpy2DAsync(w.Cp, csz * sizeof(cpx), w.MC + (size_t)3 * start * csz, w.traj * sizeof(cpx),
+                           csz * sizeof(cpx), w.nseg, cudaMemcpyDeviceToDevice, e.st));
+    }
+    CK(cudaMemcpyAsync(w.Sp, w.Cp, sizeof(cpx) * csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
+    CK(cudaMemcpy2DAsync(w.MC + (size_t)3 * start * csz, w.traj * sizeof(cpx), w.Cp, csz * sizeof(cpx),
+                         csz * sizeof(cpx), w.nseg, cudaMemcpyDeviceToDevice, e.st));
+  }
+  if (w.ntan > 0) {
+    CK(cudaMemcpyAsync(w.Ct, IC, sizeof(cpx) * csz * nt, cudaMemcpyDeviceToDevice, e.st));
+    CK(cudaMemcpyAsync(w.St, IC, sizeof(cpx) * csz * nt, cudaMemcpyDeviceToDevice, e.st));
+    // MIC[3 start] = IC of the coupled tangent (channel/channel.c:525-527)
+    CK(cudaMemcpy2DAsync(w.MIC + (size_t)3 * start * csz, w.traj * sizeof(cpx), IC + (size_t)w.couple * csz,
+                         (size_t)w.ntan * csz * sizeof(cpx), csz * sizeof(cpx), w.nseg, cudaMemcpyDeviceToDevice,
+                         e.st));
+  }
+  if (!reset_status(e, w) || !set_step(e, w, start)) return false;
+  FwdOpts o{adv_primal, w.ntan > 0, 0, forced_mask, false};
+  return run_steps(e, end - start, [&] { return enqueue_forward_step(e, w, o); });
+}
+
+static bool op_adjoint(Engine& e, Work& w, int start, int end, const cpx* AC, double strength) {
+  CK(cudaMemcpyAsync(w.Ca, AC, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
+  CK(cudaMemcpyAsync(w.Sa, AC, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
+  if (!reset_status(e, w) || !set_step(e, w, start)) return false;
+  const double sdt = strength * e.T.g.dt;  // channel/channel.c:619
+  return run_steps(e, start - end, [&] { return enqueue_adjoint_step(e, w, sdt); });
+}
+
+// ---------------------------------------------------------------------------
+// helpers for the host-array API
+// ---------------------------------------------------------------------------
+
+static bool need_init(const char* fn) {
+  if (!E) {
+    set_error(-2, "%s called before c_init", fn);
+    fprintf(stderr, "c_channel: %s called before c_init\n", fn);
+    return false;
+  }
+  return true;
+}
+
+static void check_coef_dims(const Grid& g, int Nz_, int Nvar, int Ny_, int Nx_) {
+  shape_assert(Nx_ == g.Nx / 2, "Nx_dup == Nx / 2");
+  shape_assert(Ny_ == g.R, "Ny_dup == dimR");
+  shape_assert(Nz_ == g.Nz, "Nz_dup == Nz");
+  shape_assert(Nvar == 2, "Nvar_dup == 2");
+}
+
+static bool h2d(Engine& e, void* d, const void* h, size_t bytes) {
+  CK(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, e.st));
+  return true;
+}
+
+static bool d2h(Engine& e, void* h, const void* d, size_t bytes) {
+  CK(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, e.st));
+  CK(cudaStreamSynchronize(e.st));
+  return true;
+}
+
+static double ddt_project_single(Engine& e, int i_step, cpx* IC_host) {
+  Work& w = e.single;
+  const Grid& g = e.T.g;
+  const size_t bytes = sizeof(cpx) * w.csz;
+  if (!h2d(e, w.io, IC_host, bytes)) return NAN;
+  DdtArgs d{w.MC, w.traj, nullptr, i_step, 1};
+  ++g_launches;
+  if (launch_ddt_diff(g, d, w.dC, e.st) != cudaSuccess) return NAN;
+  if (!enqueue_spec2phys(e, w, cb(w.dC, w.csz), noslot(), w.Uprev, w.Pprev, 1)) return NAN;
+  if (!enqueue_spec2phys(e, w, cb(w.io, w.csz), noslot(), w.Ul, w.Pl, 1)) return NAN;
+  ++g_launches;
+  if (launch_ddt_dots(g, cbd(w.Pprev, w.psz), cbd(w.Pl, w.psz), w.part, Work::kDotBlocks, 1, e.st) != cudaSuccess)
+    return NAN;
+  ++g_launches;
+  if (launch_ddt_apply(g, w.part, Work::kDotBlocks, 1, cb(w.io, w.csz), noslot(), mb(w.io, w.csz), cb(w.dC, w.csz),
+                       w.r, mb(nullptr, 0), 0.0, e.st) != cudaSuccess)
+    return NAN;
+  double r = NAN;
+  if (!d2h(e, IC_host, w.io, bytes)) return NAN;
+  if (!d2h(e, &r, w.r, sizeof(double))) return NAN;
+  g_status = 0;
+  g_msg.clear();
+  return r;
+}
+
+}  // namespace chn
+
+using namespace chn;
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+int c_init(int Nx, int Ny, int Nz, double Lx, double Lz, double Re, double flux, double dt, int nsteps) {
+  printf("Nx,Ny,Nz,Lx  |  Lz,dt,nsteps  |  flux,Re\n%d %d %d %f  |  %f %f %d |  %f %f\n", Nx, Ny, Nz, Lx, Lz, dt,
+         nsteps, flux, Re);
+  if (E) c_destroy();
+  if (nsteps < 0) {
+    set_error(1, "nsteps must be >= 0");
+    return 1;
+  }
+  Engine* e = new Engine();
+  if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error(-1, "no CUDA device available");
+    delete e;
+    return 1;
+  }
+  if (!build_device_tables(e->T, Nx, Ny, Nz, Lx, Lz, Re, flux, dt)) {
+    e->T.release();
+    cudaStreamDestroy(e->st);
+    delete e;
+    return 1;
+  }
+  e->nsteps = nsteps;
+  e->qy = e->T.ht.y;
+  e->qw = e->T.ht.w;
+  if (!e->single.create(e->T.g, 1, 1, nsteps, 0)) {
+    e->single.release();
+    e->T.release();
+    cudaStreamDestroy(e->st);
+    delete e;
+    return 1;
+  }
+  e->last_ic.assign(e->single.csz, cpx{0.0, 0.0});
+  E = e;
+  g_status = 0;
+  g_msg.clear();
+  return 0;
+}
+
+void c_destroy(void) {
+  if (!E) return;
+  cudaStreamSynchronize(E->st);
+  E->single.release();
+  if (E->have_batch) E->batch.release();
+  if (E->host_mc) cudaFreeHost(E->host_mc);
+  if (E->host_mic) cudaFreeHost(E->host_mic);
+  E->T.release();
+  cudaStreamDestroy(E->st);
+  delete E;
+  E = nullptr;
+}
+
+void c_primal(int ru_steps, chn_complex* C_given, int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup) {
+  if (!need_init("c_primal")) return;
+  Engine& e = *E;
+  Work& w = e.single;
+  const bool empty = (Nx_dup == 0 && Ny_dup == 0 && Nz_dup == 0 && Nvar_dup == 0);
+  if (!empty) check_coef_dims(e.T.g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
+  const size_t bytes = sizeof(cpx) * w.csz;
+  if (!empty && !h2d(e, w.io, C_given, bytes)) return;
+  if (!op_primal(e, w, ru_steps, empty ? nullptr : w.io)) return;
+  if (!collect_status(e, w)) return;
+  if (g_status & ST_CFL) printf("Pass1 failure\n");
+  if (!empty) d2h(e, C_given, w.Cp, bytes);
+}
+
+void c_tangent(int start_step, int end_step, chn_complex* IC_given, int Nz_dup, int Nvar_dup, int Ny_dup,
+               int Nx_dup, int inhomo) {
+  if (!need_init("c_tangent")) return;
+  Engine& e = *E;
+  Work& w = e.single;
+  check_coef_dims(e.T.g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
+  shape_assert(end_step > start_step, "end_step > start_step");
+  shape_assert(start_step >= 0, "start_step >= 0");
+  shape_assert(end_step <= e.nsteps, "end_step <= nsteps");
+  shape_assert(IC_given != nullptr, "IC_given != 0");
+  const size_t bytes = sizeof(cpx) * w.csz;
+  if (!h2d(e, w.io, IC_given, bytes)) return;
+  if (!op_forward(e, w, start_step, end_step, nullptr, w.io, inhomo ? 1u : 0u, false)) return;
+  if (!collect_status(e, w)) return;
+  if (g_status & ST_CFL) printf("Pass1 failure\n");
+  d2h(e, IC_given, w.Ct, bytes);
+  memcpy(e.last_ic.data(), IC_given, bytes);
+}
+
+void c_adjoint(int start_step, int end_step, chn_complex* AC_given, int Nz_dup, int Nvar_dup, int Ny_dup,
+               int Nx_dup, int inhomo, double strength) {
+  (void)inhomo;  // unused by the reference too (channel/channel.c:596-696)
+  if (!need_init("c_adjoint")) return;
+  Engine& e = *E;
+  Work& w = e.single;
+  check_coef_dims(e.T.g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
+  shape_assert(end_step < start_step, "end_step < start_step");
+  shape_assert(end_step >= 0, "end_step >= 0");
+  shape_assert(start_step <= e.nsteps, "start_step <= nsteps");
+  shape_assert(AC_given != nullptr, "AC_given != 0");
+  const size_t bytes = sizeof(cpx) * w.csz;
+  if (!h2d(e, w.io, AC_given, bytes)) return;
+  if (!op_adjoint(e, w, start_step, end_step, w.io, strength)) return;
+  if (!collect_status(e, w)) return;
+  d2h(e, AC_given, w.Ca, bytes);
+}
+
+double c_ddt_project(int i_step, chn_complex* IC_given, int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup) {
+  if (!need_init("c_ddt_project")) return NAN;
+  check_coef_dims(E->T.g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
+  return ddt_project_single(*E, i_step, reinterpret_cast<cpx*>(IC_given));
+}
+
+static void get_traj(bool inc, int i_step, chn_complex** ptr, int* Nz_ptr, int* Nvar_ptr, int* Ny_ptr, int* Nx_ptr) {
+  Engine& e = *E;
+  Work& w = e.single;
+  shape_assert(i_step >= 0 && i_step <= e.nsteps, "i_step >= 0 && i_step <= nsteps");
+  cpx*& mirror = inc ? e.host_mic : e.host_mc;
+  if (!mirror) {
+    if (cudaMallocHost(&mirror, sizeof(cpx) * w.csz * (size_t)(e.nsteps + 1)) != cudaSuccess) {
+      set_error(-1, "cudaMallocHost failed for the trajectory mirror");
+      *ptr = nullptr;
+      return;
+    }
+  }
+  cpx* dst = mirror + (size_t)i_step * w.csz;
+  const cpx* src = (inc ? w.MIC : w.MC) + (size_t)3 * i_step * w.csz;
+  d2h(e, dst, src, sizeof(cpx) * w.csz);
+  *ptr = reinterpret_cast<chn_complex*>(dst);
+  *Nz_ptr = e.T.g.Nz;
+  *Nvar_ptr = 2;
+  *Ny_ptr = e.T.g.R;
+  *Nx_ptr = e.T.g.Nx / 2;
+}
+
+void c_getsoln(int i_step, chn_complex** MC_ptr, int* Nz_ptr, int* Nvar_ptr, int* Ny_ptr, int* Nx_ptr) {
+  if (!need_init("c_getsoln")) return;
+  get_traj(false, i_step, MC_ptr, Nz_ptr, Nvar_ptr, Ny_ptr, Nx_ptr);
+}
+
+void c_getincresoln(int i_step, chn_complex** MIC_ptr, int* Nz_ptr, int* Nvar_ptr, int* Ny_ptr, int* Nx_ptr) {
+  if (!need_init("c_getincresoln")) return;
+  get_traj(true, i_step, MIC_ptr, Nz_ptr, Nvar_ptr, Ny_ptr, Nx_ptr);
+}
+
+void c_spec2phys(chn_complex* C_ptr, int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup, double* flow_ptr, int Nd_flow,
+                 int Nx_flow, int Ny_flow, int Nz_flow) {
+  if (!need_init("c_spec2phys")) return;
+  Engine& e = *E;
+  Work& w = e.single;
+  const Grid& g = e.T.g;
+  check_coef_dims(g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
+  shape_assert(Nd_flow == 3, "Nd_flow == 3");
+  shape_assert(Nx_flow == 3 * g.Nx / 2, "Nx_flow == 3 * Nx / 2");
+  shape_assert(Ny_flow == g.Q, "Ny_flow == qpts");
+  shape_assert(Nz_flow == 3 * g.Nz / 2, "Nz_flow == 3 * Nz / 2");
+  if (!h2d(e, w.io, C_ptr, sizeof(cpx) * w.csz)) return;
+  if (!enqueue_spec2phys(e, w, cb(w.io, w.csz), noslot(), w.Ul, w.Pl, 1)) return;
+  ++g_launches;
+  if (launch_flow_out(g, w.Pl, w.flow, e.st) != cudaSuccess) return;
+  d2h(e, flow_ptr, w.flow, sizeof(double) * 3 * (size_t)g.Q * plane_size(g));
+  g_status = 0;
+  g_msg.clear();
+}
+
+// Raw solution container: "SCHNRAW1", int32 Nx, Ny, Nz, 0, double dt, 1/Re,
+// mpg, then alpha, beta, ialpha, ibeta as [dimR][Nz][Nx/2] {re, im} doubles
+// (the datasets of channel/channel.c:889-1028).
+void c_save_solution(char* filename, chn_complex* C_ptr, int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup) {
+  if (!need_init("c_save_solution")) return;
+  Engine& e = *E;
+  const Grid& g = e.T.g;
+  check_coef_dims(g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
+  FILE* f = fopen(filename, "wb");
+  if (!f) {
+    set_error(-3, "cannot open %s for writing", filename);
+    return;
+  }
+  const char magic[8] = {'S', 'C', 'H', 'N', 'R', 'A', 'W', '1'};
+  const int dims[4] = {g.Nx, g.Ny, g.Nz, 0};
+  const double sc[3] = {g.dt, g.re, 0.0};
+  fwrite(magic, 1, 8, f);
+  fwrite(dims, sizeof(int), 4, f);
+  fwrite(sc, sizeof(double), 3, f);
+  const cpx* C = reinterpret_cast<const cpx*>(C_ptr);
+  const cpx* IC = e.last_ic.data();
+  for (int src = 0; src < 2; ++src)
+    for (int v = 0; v < 2; ++v)
+      for (int r = 0; r < g.R; ++r)
+        for (int z = 0; z < g.Nz; ++z)
+          for (int x = 0; x < g.X; ++x) {
+            const cpx* A = src ? IC : C;
+            fwrite(&A[(((size_t)z * 2 + v) * g.R + r) * g.X + x], sizeof(cpx), 1, f);
+          }
+  fclose(f);
+  g_status = 0;
+  g_msg.clear();
+}
+
+void c_read_solution(char* filename, chn_complex* C_ptr, int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup) {
+  if (!need_init("c_read_solution")) return;
+  Engine& e = *E;
+  const Grid& g = e.T.g;
+  check_coef_dims(g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
+  FILE* f = fopen(filename, "rb");
+  shape_assert(f != nullptr, "solution file opens");
+  char magic[8];
+  int dims[4];
+  double sc[3];
+  bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "SCHNRAW1", 8) == 0 && fread(dims, sizeof(int), 4, f) == 4 &&
+            fread(sc, sizeof(double), 3, f) == 3 && dims[0] == g.Nx && dims[1] == g.Ny && dims[2] == g.Nz;
+  shape_assert(ok, "solution file header matches the grid");
+  cpx* C = reinterpret_cast<cpx*>(C_ptr);
+  for (int src = 0; src < 2; ++src)
+    for (int v = 0; v < 2; ++v)
+      for (int r = 0; r < g.R; ++r)
+        for (int z = 0; z < g.Nz; ++z)
+          for (int x = 0; x < g.X; ++x) {
+            cpx* A = src ? e.last_ic.data() : C;
+            ok = ok && fread(&A[(((size_t)z * 2 + v) * g.R + r) * g.X + x], sizeof(cpx), 1, f) == 1;
+          }
+  fclose(f);
+  shape_assert(ok, "solution file complete");
+  g_status = 0;
+  g_msg.clear();
+}
+
+void c_quad(double** y_ptr, int* qpts_ptr1, double** w_ptr, int* qpts_ptr2) {
+  if (!need_init("c_quad")) return;
+  *y_ptr = E->qy.data();
+  *w_ptr = E->qw.data();
+  *qpts_ptr1 = *qpts_ptr2 = E->T.g.Q;
+}
+
+int c_qpts(void) { return E ? E->T.g.Q : 0; }
+int c_dimR(void) { return E ? E->T.g.R : 0; }
+int c_dimQ(void) { return E ? E->T.g.D : 0; }
+int c_Nx(void) { return E ? E->T.g.Nx : 0; }
+int c_Nz(void) { return E ? E->T.g.Nz : 0; }
+int c_nsteps(void) { return E ? E->nsteps : 0; }
+
+int c_last_error(void) { return g_status; }
+const char* c_last_error_message(void) { return g_msg.c_str(); }
+double c_last_cfl(void) { return g_cfl; }
+
+int c_batch_init(int nseg, int ntan, int couple) {
+  if (!need_init("c_batch_init")) return -2;
+  if (nseg <= 0 || ntan < 0 || ntan > 32 || (ntan > 0 && (couple < 0 || couple >= ntan))) {
+    set_error(-4, "c_batch_init: need nseg > 0, 0 <= ntan <= 32, 0 <= couple < ntan");
+    return -4;
+  }
+  Engine& e = *E;
+  if (e.have_batch) {
+    cudaStreamSynchronize(e.st);
+    e.batch.release();
+    e.have_batch = false;
+  }
+  if (!e.batch.create(e.T.g, nseg, ntan, e.nsteps, couple)) {
+    e.batch.release();
+    return g_status;
+  }
+  e.have_batch = true;
+  g_status = 0;
+  return 0;
+}
+
+int c_batch_destroy(void) {
+  if (!E || !E->have_batch) return 0;
+  cudaStreamSynchronize(E->st);
+  E->batch.release();
+  E->have_batch = false;
+  return 0;
+}
+
+static bool batch_ready(const char* fn) {
+  if (!need_init(fn)) return false;
+  if (!E->have_batch) {
+    set_error(-4, "%s: call c_batch_init first", fn);
+    return false;
+  }
+  return true;
+}
+
+static uint32_t mask_of(const int* inhomo, int ntan) {
+  uint32_t m = 0;
+  for (int t = 0; t < ntan; ++t)
+    if (inhomo && inhomo[t]) m |= 1u << t;
+  return m;
+}
+
+int c_batch_primal_dev(int ru_steps, chn_complex* C) {
+  if (!batch_ready("c_batch_primal_dev")) return g_status;
+  Work& w = E->batch;
+  if (!op_primal(*E, w, ru_steps, reinterpret_cast<cpx*>(C))) return g_status;
+  if (C && cudaMemcpyAsync(C, w.Cp, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, E->st) != cudaSuccess)
+    return -1;
+  return collect_status(*E, w) ? g_status : -1;
+}
+
+int c_batch_tangent_dev(int start_step, int end_step, chn_complex* IC, const int* inhomo) {
+  if (!batch_ready("c_batch_tangent_dev")) return g_status;
+  Work& w = E->batch;
+  if (!(end_step > start_step && start_step >= 0 && end_step <= E->nsteps) || w.ntan == 0) {
+    set_error(-4, "c_batch_tangent: need 0 <= start < end <= nsteps and ntan > 0");
+    return -4;
+  }
+  if (!op_forward(*E, w, start_step, end_step, nullptr, reinterpret_cast<cpx*>(IC), mask_of(inhomo, w.ntan), false))
+    return g_status;
+  if (cudaMemcpyAsync(IC, w.Ct, sizeof(cpx) * w.csz * w.nseg * w.ntan, cudaMemcpyDeviceToDevice, E->st) != cudaSuccess)
+    return -1;
+  return collect_status(*E, w) ? g_status : -1;
+}
+
+int c_batch_forward_dev(int start_step, int end_step, chn_complex* C, chn_complex* IC, const int* inhomo) {
+  if (!batch_ready("c_batch_forward_dev")) return g_status;
+  Work& w = E->batch;
+  if (!(end_step > start_step && start_step >= 0 && end_step <= E->nsteps)) {
+    set_error(-4, "c_batch_forward: need 0 <= start < end <= nsteps");
+    return -4;
+  }
+  if (!op_forward(*E, w, start_step, end_step, reinterpret_cast<cpx*>(C), reinterpret_cast<cpx*>(IC),
+                  mask_of(inhomo, w.ntan), true))
+    return g_status;
+  if (C && cudaMemcpyAsync(C, w.Cp, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, E->st) != cudaSuccess)
+    return -1;
+  if (w.ntan > 0 &&
+      cudaMemcpyAsync(IC, w.Ct, sizeof(cpx) * w.csz * w.nseg * w.ntan, cudaMemcpyDeviceToDevice, E->st) != cudaSuccess)
+    return -1;
+  return collect_status(*E, w) ? g_status : -1;
+}
+
+int c_batch_adjoint_dev(int start_step, int end_step, chn_complex* AC, double strength) {
+  if (!batch_ready("c_batch_adjoint_dev")) return g_status;
+  Work& w = E->batch;
+  if (!(end_step < start_step && end_step >= 0 && start_step <= E->nsteps)) {
+    set_error(-4, "c_batch_adjoint: need 0 <= end < start <= nsteps");
+    return -4;
+  }
+  if (!op_adjoint(*E, w, start_step, end_step, reinterpret_cast<cpx*>(AC), strength)) return g_status;
+  if (cudaMemcpyAsync(AC, w.Ca, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, E->st) != cudaSuccess)
+    return -1;
+  return collect_status(*E, w) ? g_status : -1;
+}
+
+// host-array variants: stage through a temporary device buffer
+int c_batch_primal(int ru_steps, chn_complex* C) {
+  if (!batch_ready("c_batch_primal")) return g_status;
+  Work& w = E->batch;
+  cpx* d = nullptr;
+  const size_t bytes = sizeof(cpx) * w.csz * w.nseg;
+  if (C) {
+    if (cudaMalloc(&d, bytes) != cudaSuccess) { set_error(-1, "cudaMalloc"); return -1; }
+    cudaMemcpyAsync(d, C, bytes, cudaMemcpyHostToDevice, E->st);
+  }
+  int rc = c_batch_primal_dev(ru_steps, reinterpret_cast<chn_complex*>(d));
+  if (C) {
+    cudaMemcpyAsync(C, d, bytes, cudaMemcpyDeviceToHost, E->st);
+    cudaStreamSynchronize(E->st);
+    cudaFree(d);
+  }
+  return rc;
+}
+
+int c_batch_tangent(int start_step, int end_step, chn_complex* IC, const int* inhomo) {
+  if (!batch_ready("c_batch_tangent")) return g_status;
+  Work& w = E->batch;
+  const size_t bytes = sizeof(cpx) * w.csz * w.nseg * (w.ntan > 0 ? w.ntan : 1);
+  cpx* d = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) { set_error(-1, "cudaMalloc"); return -1; }
+  cudaMemcpyAsync(d, IC, bytes, cudaMemcpyHostToDevice, E->st);
+  int rc = c_batch_tangent_dev(start_step, end_step, reinterpret_cast<chn_complex*>(d), inhomo);
+  cudaMemcpyAsync(IC, d, bytes, cudaMemcpyDeviceToHost, E->st);
+  cudaStreamSynchronize(E->st);
+  cudaFree(d);
+  return rc;
+}
+
+int c_batch_forward(int start_step, int end_step, chn_complex* C, chn_complex* IC, const int* inhomo) {
+  if (!batch_ready("c_batch_forward")) return g_status;
+  Work& w = E->batch;
+  const size_t bc = sizeof(cpx) * w.csz * w.nseg;
+  const size_t bt = sizeof(cpx) * w.csz * w.nseg * (w.ntan > 0 ? w.ntan : 1);
+  cpx *dc = nullptr, *dt = nullptr;
+  if (cudaMalloc(&dc, bc) != cudaSuccess || cudaMalloc(&dt, bt) != cudaSuccess) {
+    set_error(-1, "cudaMalloc");
+    return -1;
+  }
+  cudaMemcpyAsync(dc, C, bc, cudaMemcpyHostToDevice, E->st);
+  if (w.ntan > 0) cudaMemcpyAsync(dt, IC, bt, cudaMemcpyHostToDevice, E->st);
+  int rc = c_batch_forward_dev(start_step, end_step, reinterpret_cast<chn_complex*>(dc),
+                               reinterpret_cast<chn_complex*>(dt), inhomo);
+  cudaMemcpyAsync(C, dc, bc, cudaMemcpyDeviceToHost, E->st);
+  if (w.ntan > 0) cudaMemcpyAsync(IC, dt, bt, cudaMemcpyDeviceToHost, E->st);
+  cudaStreamSynchronize(E->st);
+  cudaFree(dc);
+  cudaFree(dt);
+  return rc;
+}
+
+int c_batch_adjoint(int start_step, int end_step, chn_complex* AC, double strength) {
+  if (!batch_ready("c_batch_adjoint")) return g_status;
+  Work& w = E->batch;
+  const size_t bytes = sizeof(cpx) * w.csz * w.nseg;
+  cpx* d = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) { set_error(-1, "cudaMalloc"); return -1; }
+  cudaMemcpyAsync(d, AC, bytes, cudaMemcpyHostToDevice, E->st);
+  int rc = c_batch_adjoint_dev(start_step, end_step, reinterpret_cast<chn_complex*>(d), strength);
+  cudaMemcpyAsync(AC, d, bytes, cudaMemcpyDeviceToHost, E->st);
+  cudaStreamSynchronize(E->st);
+  cudaFree(d);
+  return rc;
+}
+
+int c_batch_getsoln(int seg, int i_step, chn_complex* out) {
+  if (!batch_ready("c_batch_getsoln")) return g_status;
+  Work& w = E->batch;
+  if (seg < 0 || seg >= w.nseg || i_step < 0 || i_step > E->nsteps) return -4;
+  return d2h(*E, out, w.MC + (size_t)seg * w.traj + (size_t)3 * i_step * w.csz, sizeof(cpx) * w.csz) ? 0 : -1;
+}
+
+int c_batch_getincresoln(int seg, int i_step, chn_complex* out) {
+  if (!batch_ready("c_batch_getincresoln")) return g_status;
+  Work& w = E->batch;
+  if (seg < 0 || seg >= w.nseg || i_step < 0 || i_step > E->nsteps) return -4;
+  return d2h(*E, out, w.MIC + (size_t)seg * w.traj + (size_t)3 * i_step * w.csz, sizeof(cpx) * w.csz) ? 0 : -1;
+}
+
+int c_synchronize(void) {
+  if (!E) return 0;
+  return cudaStreamSynchronize(E->st) == cudaSuccess ? 0 : -1;
+}
+
+long long c_launch_count(void) { return g_launches; }
+
+double c_fp64_peak_tflops(void) {
+  cudaStream_t st = E ? E->st : nullptr;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int threads = 256, blocks = sms * 8, iters = 4096;
+  double* buf = nullptr;
+  if (cudaMalloc(&buf, sizeof(double) * threads * blocks) != cudaSuccess) return NAN;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  launch_fp64_probe(buf, blocks, threads, iters, st);  // warm-up
+  cudaEventRecord(a, st);
+  for (int r = 0; r < 3; ++r) launch_fp64_probe(buf, blocks, threads, iters, st);
+  cudaEventRecord(b, st);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(buf);
+  g_launches += 4;
+  const double flop = 3.0 * blocks * threads * (double)iters * 8 * 2;
+  return flop / (ms * 1e-3) / 1e12;
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+// Kernel argument blocks and launchers (host-callable).
+#pragma once
+
+#include "chn_common.cuh"
+
+namespace chn {
+
+// A trajectory slot chosen on the device: slot = mul * (*ptr) + add (ptr may
+// be null: slot = add).  Lets one captured CUDA graph serve every time step.
+struct SlotRef {
+  const int* ptr;
+  int mul, add;
+  long long stride;  // elements between consecutive slots
+  __device__ __forceinline__ int slot() const { return ptr ? mul * (*ptr) + add : add; }
+};
+
+// coefficients -> velocity U (channel/initAlphaBeta2.c:12-240)
+struct ReconArgs {
+  Batch<const cpx> C;   // [inst] -> coefficient array (plus slot offset when slot.stride != 0)
+  SlotRef slot;
+  Batch<cpx> U;         // [inst] -> U[Nz][5][Q][X]
+  int ninst;
+  const uint32_t* status;
+  int sdiv;
+};
+
+struct PhysArgs {
+  Batch<const cpx> U;
+  Batch<double> P;      // [inst] -> P[nf][Q][pz][px]
+  int nfields;          // 3: u, v, w;  6: plus wz, wx, wy
+  int ninst;
+  uint32_t* status;     // per-segment status word (instance i -> status[i / sdiv])
+  int sdiv;
+  double* cflmax;       // per-segment largest CFL number seen (nullable)
+  int cfl_check;
+  int skip_blocked;
+};
+
+struct ProdArgs {
+  Batch<const double> Pp;  // primal physical fields, instance i -> Pp.base + (i / pdiv) * Pp.stride
+  int pdiv;
+  Batch<const double> Pt;  // tangent fields (forward) / lambda (adjoint); base == nullptr: primal H
+  Batch<cpx> H;            // [inst] -> H[Nz][5][Q][X]
+  int ninst;
+  const uint32_t* status;
+  int sdiv;
+};
+
+// mean-mode variants (channel/project0.c:153-168, increproject0.c:209-214, adjproject0.c:153-167)
+enum MeanMode : int { MEAN_PRIMAL = 0, MEAN_TAN_FORCED = 1, MEAN_TAN_HOMOG = 2, MEAN_ADJOINT = 3 };
+
+// One RK3 substage of the implicit Galerkin solve, one block per (instance, kz line, kx tile).
+// channel/project.c:24-405, project0.c:22-271, increproject*.c, adjproject*.c:10-550
+struct SolveArgs {
+  Batch<const cpx> H;       // nonlinear terms of this stage
+  Batch<const cpx> Hprev;   // adjoint: previous-stage terms for the next right-hand side
+  Batch<cpx> Cc;            // carried right-hand side / state (in place)
+  Batch<cpx> Sout;          // solved state output (scratch for the next reconstruction)
+  // trajectory store of instance i (only when i % tdiv == tsel):
+  //   T.base + (i / tdiv) * T.stride + slot * slot.stride, skipped for slot < 0
+  Batch<cpx> T;
+  int tdiv, tsel;
+  SlotRef slot;
+  int k;                    // RK substage 0..2
+  int adjoint;              // 0 forward coefficients, 1 adjoint coefficients
+  int mean_mode;            // for tangents: MEAN_TAN_HOMOG, or MEAN_TAN_FORCED where
+  uint32_t forced_mask;     //   bit (i % mdiv) of forced_mask is set
+  int mdiv;
+  int ninst;
+  const uint32_t* status;
+  int sdiv;
+};
+
+// one ddt_project / adjoint coupling for nseg segments (channel/channel.c:704-780)
+struct DdtArgs {
+  const cpx* MC;            // segment s trajectory: MC + s * traj_stride
+  long long traj_stride;
+  const int* step_ptr;      // i_step = *step_ptr + step_add (or step_add when null)
+  int step_add;
+  int nseg;
+};
+
+void prepare_kernels(const Grid& g);  // function attributes; call once, outside graph capture
+
+cudaError_t launch_recon(const Grid& g, const ReconArgs& a, cudaStream_t st);
+cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t st);
+cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t st);
+cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st);
+cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st);
+
+size_t recon_smem_bytes(const Grid& g);
+size_t phys_smem_bytes(const Grid& g, bool with_cfl);
+size_t prod_adj_smem_bytes(const Grid& g);
+size_t solve_smem_bytes(const Grid& g);
+
+// flow[d][xp][y][zp] <- P[d][y][zp][xp]
+cudaError_t launch_flow_out(const Grid& g, const double* P, double* flow, cudaStream_t st);
+// dC[s] = (MC[s][i+] - MC[s][i-]) / dt
+cudaError_t launch_ddt_diff(const Grid& g, const DdtArgs& d, cpx* dC, cudaStream_t st);
+// per-segment partial sums of sum a*b*W[y], sum a*a*W[y] over 3 fields: part[s][nblk][2]
+cudaError_t launch_ddt_dots(const Grid& g, Batch<const double> Pa, Batch<const double> Pb, double* part,
+                            int nblk, int nseg, cudaStream_t st);
+// r = num/den; IC' = IC - r dC (written to ICdst when non-null); AC -= coef * IC'
+cudaError_t launch_ddt_apply(const Grid& g, const double* part, int nblk, int nseg, Batch<const cpx> ICsrc,
+                             SlotRef icslot, Batch<cpx> ICdst, Batch<const cpx> dC, double* r_out,
+                             Batch<cpx> AC, double coef, cudaStream_t st);
+cudaError_t launch_project_init(const Grid& g, const cpx* Uinit, cpx* C, const double* luQs,
+                                const double* luRs, cudaStream_t st);
+cudaError_t launch_step_advance(int* ctr, int delta, cudaStream_t st);
+cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
+
+}  // namespace chn

@@ -1,0 +1,660 @@
+// Legendre-direction kernels.
+//
+//   k_recon  coefficients -> velocity at every quadrature plane
+//            (channel/initAlphaBeta2.c:12-240, same arithmetic as the
+//            reconstruction tail of channel/project.c:231-332)
+//   k_solve  one RK3 substage of the implicit Galerkin step for a kz line:
+//            quadrature right-hand side, banded solve, trajectory store and
+//            next-substage right-hand side (channel/project.c:24-405,
+//            project0.c:22-271, increproject*.c, adjproject*.c)
+//
+// Both exploit the parity of the Legendre bases on the symmetric Gauss
+// points: Q_n, Q_n'', R_n are even/odd as (-1)^n and Q_n', R_n' as
+// (-1)^(n+1), so for the plane pair (y, -y) a contraction splits into an
+// even-index sum E and an odd-index sum O with values E +- O.  This halves
+// the FP64 multiply-adds of every quadrature and reconstruction.
+#include "chn_common.cuh"
+#include "kernels.h"
+
+namespace chn {
+
+static constexpr int kThreads = 256;
+static constexpr int kTile = 16;   // kx columns per block
+
+__device__ __forceinline__ bool blocked(const uint32_t* status, int sdiv, int inst) {
+  return status != nullptr && (status[inst / sdiv] & ST_CFL) != 0;
+}
+
+__device__ __forceinline__ void cfma(double w, const cpx& a, double& re, double& im) {
+  re = fma(w, a.re, re);
+  im = fma(w, a.im, im);
+}
+
+// ---------------------------------------------------------------------------
+// reconstruction
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kThreads) k_recon(Grid g, ReconArgs a) {
+  const int ntx = (g.X + kTile - 1) / kTile;
+  const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
+  const int inst = blockIdx.y;
+  if (z == g.Nz / 2) return;  // never read (channel/pass1.c:51-85 skips it)
+  if (blocked(a.status, a.sdiv, inst)) return;
+  const int x0 = tx * kTile;
+  const int nx = min(kTile, g.X - x0);
+  extern __shared__ __align__(16) unsigned char smem[];
+  cpx* cs = reinterpret_cast<cpx*>(smem);  // [2][R][kTile]
+  const cpx* __restrict__ C = a.C.at(inst);
+  if (a.slot.stride) C += (long long)a.slot.slot() * a.slot.stride;
+  for (int i = threadIdx.x; i < 2 * g.R * kTile; i += blockDim.x) {
+    const int v = i / (g.R * kTile), r = (i / kTile) % g.R, x = i % kTile;
+    cpx val = {0.0, 0.0};
+    if (x < nx) val = C[(((size_t)z * 2 + v) * g.R + r) * g.X + x0 + x];
+    cs[i] = val;
+  }
+  __syncthreads();
+  const int lx = threadIdx.x % kTile, grp = threadIdx.x / kTile;
+  const int ngrp = blockDim.x / kTile;
+  if (lx >= nx) return;
+  const int x = x0 + lx;
+  cpx* __restrict__ U = a.U.at(inst);
+  const cpx* al = cs;                     // alpha_j at al[j*kTile + lx]
+  const cpx* be = cs + g.R * kTile;       // beta_j
+  const bool mean = (z == 0 && x == 0);
+  const double ax = g.kxK2[z * g.X + x], az = g.kzK2[z * g.X + x];
+  for (int yp = grp; yp < g.Qh; yp += ngrp) {
+    const int y1 = yp, y2 = g.Q - 1 - yp;
+    // E/O sums: [0] Q alpha (v), [1] Q' alpha, [2] Q'' alpha, [3] R beta, [4] R' beta
+    double er[5] = {0, 0, 0, 0, 0}, ei[5] = {0, 0, 0, 0, 0};
+    double orr[5] = {0, 0, 0, 0, 0}, oi[5] = {0, 0, 0, 0, 0};
+    if (!mean) {
+      const double* bq = g.Bq + (size_t)y1 * g.D;
+      const double* bqp = g.Bqp + (size_t)y1 * g.D;
+      const double* bqpp = g.Bqpp + (size_t)y1 * g.D;
+      int j = 0;
+      for (; j + 1 < g.D; j += 2) {
+        const cpx c0 = al[j * kTile + lx], c1 = al[(j + 1) * kTile + lx];
+        const double q0 = __ldg(bq + j), q1 = __ldg(bq + j + 1);
+        const double p0 = __ldg(bqp + j), p1 = __ldg(bqp + j + 1);
+        const double s0 = __ldg(bqpp + j), s1 = __ldg(bqpp + j + 1);
+        cfma(q0, c0, er[0], ei[0]); cfma(q1, c1, orr[0], oi[0]);
+        cfma(p0, c0, er[1], ei[1]); cfma(p1, c1, orr[1], oi[1]);
+        cfma(s0, c0, er[2], ei[2]); cfma(s1, c1, orr[2], oi[2]);
+      }
+      if (j < g.D) {
+        const cpx c0 = al[j * kTile + lx];
+        cfma(__ldg(bq + j), c0, er[0], ei[0]);
+        cfma(__ldg(bqp + j), c0, er[1], ei[1]);
+        cfma(__ldg(bqpp + j), c0, er[2], ei[2]);
+      }
+    }
+    {
+      const double* br = g.Br + (size_t)y1 * g.R;
+      const double* brp = g.Brp + (size_t)y1 * g.R;
+      // mean mode: R a and R' a land in slots 1/2 (u, du), R b and R' b in 3/4
+      const cpx* src0 = mean ? al : be;
+      int j = 0;
+      for (; j + 1 < g.R; j += 2) {
+        const double r0 = __ldg(br + j), r1 = __ldg(br + j + 1);
+        const double p0 = __ldg(brp + j), p1 = __ldg(brp + j + 1);
+        const cpx b0 = be[j * kTile + lx], b1 = be[(j + 1) * kTile + lx];
+        cfma(r0, b0, er[3], ei[3]); cfma(r1, b1, orr[3], oi[3]);
+        cfma(p0, b0, er[4], ei[4]); cfma(p1, b1, orr[4], oi[4]);
+        if (mean) {
+          const cpx c0 = src0[j * kTile + lx], c1 = src0[(j + 1) * kTile + lx];
+          cfma(r0, c0, er[1], ei[1]); cfma(r1, c1, orr[1], oi[1]);
+          cfma(p0, c0, er[2], ei[2]); cfma(p1, c1, orr[2], oi[2]);
+        }
+      }
+      if (j < g.R) {
+        const double r0 = __ldg(br + j), p0 = __ldg(brp + j);
+        const cpx b0 = be[j * kTile + lx];
+        cfma(r0, b0, er[3], ei[3]);
+        cfma(p0, b0, er[4], ei[4]);
+        if (mean) {
+          const cpx c0 = src0[j * kTile + lx];
+          cfma(r0, c0, er[1], ei[1]);
+          cfma(p0, c0, er[2], ei[2]);
+        }
+      }
+    }
+    for (int side = 0; side < 2; ++side) {
+      if (side == 1 && y2 == y1) break;
+      const int y = side ? y2 : y1;
+      // even-parity bases: E + O / E - O;  odd-parity (Q', R'): E + O / -(E - O)
+      auto val = [&](int c, bool odd_basis) {
+        cpx r;
+        if (!side) { r.re = er[c] + orr[c]; r.im = ei[c] + oi[c]; }
+        else if (!odd_basis) { r.re = er[c] - orr[c]; r.im = ei[c] - oi[c]; }
+        else { r.re = orr[c] - er[c]; r.im = oi[c] - ei[c]; }
+        return r;
+      };
+      cpx u, v, w, du, dw;
+      if (mean) {
+        // (kx,kz) = (0,0): u = R a, du = R' a, v = 0, w = R b, dw = R' b
+        u = val(1, false); du = val(2, true); w = val(3, false); dw = val(4, true);
+        v.re = 0.0; v.im = 0.0;
+      } else {
+        v = val(0, false);
+        const cpx qp = val(1, true);          // Q' alpha, f = -Q' alpha
+        const cpx qpp = val(2, false);
+        const cpx g_ = val(3, false);         // g = R beta
+        const cpx rp = val(4, true);
+        const cpx f = {-qp.re, -qp.im};
+        // u = (kx Im f + kz Im g)/K2 - i (kx Re f + kz Re g)/K2, etc.
+        u.re = fma(ax, f.im, az * g_.im);
+        u.im = -fma(ax, f.re, az * g_.re);
+        w.re = fma(-ax, g_.im, az * f.im);
+        w.im = fma(ax, g_.re, -az * f.re);
+        du.re = fma(-ax, qpp.im, az * rp.im);
+        du.im = fma(ax, qpp.re, -az * rp.re);
+        dw.re = -fma(ax, rp.im, az * qpp.im);
+        dw.im = fma(ax, rp.re, az * qpp.re);
+      }
+      cpx* out = U + ((size_t)z * 5 * g.Q + y) * g.X + x;
+      const size_t cs_ = (size_t)g.Q * g.X;
+      out[0] = u;
+      out[cs_] = v;
+      out[2 * cs_] = w;
+      out[3 * cs_] = du;
+      out[4 * cs_] = dw;
+    }
+  }
+}
+
+size_t recon_smem_bytes(const Grid& g) { return (size_t)2 * g.R * kTile * sizeof(cpx); }
+
+cudaError_t launch_recon(const Grid& g, const ReconArgs& a, cudaStream_t st) {
+  if (a.ninst <= 0) return cudaSuccess;
+  const int ntx = (g.X + kTile - 1) / kTile;
+  k_recon<<<dim3(g.Nz * ntx, a.ninst), kThreads, recon_smem_bytes(g), st>>>(g, a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// implicit solve
+// ---------------------------------------------------------------------------
+
+struct RKc {
+  double b, c, dnext;
+  int bidx, aidx0, aidx_next;
+};
+
+__device__ __forceinline__ RKc rk_coeffs(int k, int adjoint) {
+  // forward  a = {1/3,-1/2,1/3}, b = {1/6,2/3,0}, c = {1/2,1/3,1}, d = {0,-1/6,-2/3}
+  // adjoint  a = {1/3,-1/2,1/3}, b = {2/3,1/6,0}, c = {1,1/3,1/2}, d = {0,-2/3,-1/6}
+  RKc r;
+  if (!adjoint) {
+    r.bidx = k;
+    r.c = k == 0 ? 1. / 2 : (k == 1 ? 1. / 3. : 1.);
+    r.dnext = k == 0 ? -1. / 6 : (k == 1 ? -2. / 3 : 0.0);
+  } else {
+    r.bidx = k == 0 ? 1 : (k == 1 ? 0 : 2);
+    r.c = k == 0 ? 1. : (k == 1 ? 1. / 3. : 1. / 2.);
+    r.dnext = k == 0 ? -2. / 3 : (k == 1 ? -1. / 6 : 0.0);
+  }
+  r.b = r.bidx == 0 ? 1. / 6 : (r.bidx == 1 ? 2. / 3 : 0.);
+  r.aidx0 = 0;                         // a[0] = 1/3
+  r.aidx_next = (k == 0) ? 1 : 0;      // a[1] = -1/2, a[2] = 1/3
+  return r;
+}
+
+struct SolveSmem {
+  cpx* hc;    // [Qh][kTile][6] parity-combined inputs
+  cpx* Fa;    // [D][kTile]
+  cpx* Fb;    // [R][kTile]
+  cpx* ra;    // [R][kTile] alpha right-hand side / solution
+  cpx* rb;    // [R][kTile]
+  double* m0; // mean-mode scratch
+};
+
+size_t solve_smem_bytes(const Grid& g) {
+  size_t n = (size_t)g.Qh * kTile * 6 + (size_t)g.D * kTile + 3 * (size_t)g.R * kTile;
+  return n * sizeof(cpx) + (size_t)8 * g.R * sizeof(double);
+}
+
+__device__ inline SolveSmem carve_solve(const Grid& g, unsigned char* base) {
+  SolveSmem s;
+  cpx* p = reinterpret_cast<cpx*>(base);
+  s.hc = p; p += (size_t)g.Qh * kTile * 6;
+  s.Fa = p; p += (size_t)g.D * kTile;
+  s.Fb = p; p += (size_t)g.R * kTile;
+  s.ra = p; p += (size_t)g.R * kTile;
+  s.rb = p; p += (size_t)g.R * kTile;
+  s.m0 = reinterpret_cast<double*>(p);
+  return s;
+}
+
+// Quadrature right-hand side for columns x0..x0+nx-1 of line z from terms H:
+//   Fa = Qpw . i(kx Hx + kz Hz) - K2 Qw . Hy  [+ Qppw . -i(kz Sx - kx Sz)]
+//   Fb = Rw . i(kz Hx - kx Hz)                [+ Rpw  .  i(kz Sz + kx Sx)]
+// (channel/project.c:97-115, 177-191; channel/adjproject.c:113-134, 218-234)
+__device__ void quad_rhs(const Grid& g, const cpx* __restrict__ H, int z, int x0, int nx, bool adj,
+                         SolveSmem& s) {
+  const int lx = threadIdx.x % kTile, grp = threadIdx.x / kTile, ngrp = blockDim.x / kTile;
+  const double kz = g.Kz[z];
+  const size_t cs = (size_t)g.Q * g.X;
+  const cpx* Hz_ = H + (size_t)z * 5 * cs;  // slot c at Hz_ + c*cs + y*X + x
+  for (int phase = 0; phase < 2; ++phase) {
+    // phase 0: inputs of Fa (P, Hy, Sa); phase 1: inputs of Fb (G, Sb)
+    const int nin = phase == 0 ? (adj ? 3 : 2) : (adj ? 2 : 1);
+    for (int i = threadIdx.x; i < g.Qh * kTile; i += blockDim.x) {
+      const int yp = i / kTile, l = i - yp * kTile;
+      cpx* dst = s.hc + (size_t)i * 6;
+      if (l >= nx) continue;
+      const int x = x0 + l;
+      const double kx = g.Kx[x];
+      const int ya = yp, yb = g.Q - 1 - yp;
+      cpx in[2][3];
+      for (int side = 0; side < 2; ++side) {
+        const int y = side ? yb : ya;
+        const cpx hz = Hz_[0 * cs + (size_t)y * g.X + x];
+        const cpx hx = Hz_[1 * cs + (size_t)y * g.X + x];
+        if (phase == 0) {
+          const cpx hy = Hz_[2 * cs + (size_t)y * g.X + x];
+          in[side][0].re = -kx * hx.im - kz * hz.im;   // P = i(kx Hx + kz Hz)
+          in[side][0].im = kx * hx.re + kz * hz.re;
+          in[side][1] = hy;
+          if (adj) {
+            const cpx sx = Hz_[3 * cs + (size_t)y * g.X + x], sz = Hz_[4 * cs + (size_t)y * g.X + x];
+            in[side][2].re = kz * sx.im - kx * sz.im;  // Sa = -i(kz Sx - kx Sz)
+            in[side][2].im = -kz * sx.re + kx * sz.re;
+          }
+        } else {
+          in[side][0].re = -kz * hx.im + kx * hz.im;   // G = i(kz Hx - kx Hz)
+          in[side][0].im = kz * hx.re - kx * hz.re;
+          if (adj) {
+            const cpx sx = Hz_[3 * cs + (size_t)y * g.X + x], sz = Hz_[4 * cs + (size_t)y * g.X + x];
+            in[side][1].re = -kz * sz.im - kx * sx.im;  // Sb = i(kz Sz + kx Sx)
+            in[side][1].im = kz * sz.re + kx * sx.re;
+          }
+        }
+      }
+      for (int q = 0; q < nin; ++q) {
+        if (ya == yb) {  // centre plane of an odd point count
+          dst[2 * q] = in[0][q];
+          dst[2 * q + 1] = in[0][q];
+        } else {
+          dst[2 * q].re = in[0][q].re + in[1][q].re;      // "+" combination
+          dst[2 * q].im = in[0][q].im + in[1][q].im;
+          dst[2 * q + 1].re = in[0][q].re - in[1][q].re;  // "-" combination
+          dst[2 * q + 1].im = in[0][q].im - in[1][q].im;
+        }
+      }
+    }
+    __syncthreads();
+    if (lx < nx) {
+      const int x = x0 + lx;
+      const double k2 = g.K2[z * g.X + x];
+      const int N = phase == 0 ? g.D : g.R;
+      // rows i = grp, grp + ngrp, ... share the parity of grp (ngrp is even)
+      constexpr int MAXR = 8;
+      for (int ib = grp; ib < N; ib += ngrp * MAXR) {
+        double sr[MAXR][3], si[MAXR][3];
+#pragma unroll
+        for (int m = 0; m < MAXR; ++m)
+#pragma unroll
+          for (int q = 0; q < 3; ++q) { sr[m][q] = 0.0; si[m][q] = 0.0; }
+        const bool even = (ib & 1) == 0;
+        for (int yp = 0; yp < g.Qh; ++yp) {
+          const cpx* src = s.hc + ((size_t)yp * kTile + lx) * 6;
+          if (phase == 0) {
+            // even rows: Qpw (odd basis) pairs with "-", Qw and Qppw with "+"
+            const cpx P = src[even ? 1 : 0];
+            const cpx Hy = src[even ? 2 : 3];
+            const cpx Sa = adj ? src[even ? 4 : 5] : cpx{0.0, 0.0};
+#pragma unroll
+            for (int m = 0; m < MAXR; ++m) {
+              const int i = ib + m * ngrp;
+              if (i < N) {
+                const size_t o = (size_t)i * g.Q + yp;
+                cfma(__ldg(g.Wqp + o), P, sr[m][0], si[m][0]);
+                cfma(__ldg(g.Wq + o), Hy, sr[m][1], si[m][1]);
+                if (adj) cfma(__ldg(g.Wqpp + o), Sa, sr[m][2], si[m][2]);
+              }
+            }
+          } else {
+            // even rows: Rw with "+", Rpw (odd basis) with "-"
+            const cpx G = src[even ? 0 : 1];
+            const cpx Sb = adj ? src[even ? 3 : 2] : cpx{0.0, 0.0};
+#pragma unroll
+            for (int m = 0; m < MAXR; ++m) {
+              const int i = ib + m * ngrp;
+              if (i < N) {
+                const size_t o = (size_t)i * g.Q + yp;
+                cfma(__ldg(g.Wr + o), G, sr[m][0], si[m][0]);
+                if (adj) cfma(__ldg(g.Wrp + o), Sb, sr[m][1], si[m][1]);
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int m = 0; m < MAXR; ++m) {
+          const int i = ib + m * ngrp;
+          if (i >= N) continue;
+          cpx f;
+          if (phase == 0) {
+            f.re = fma(-k2, sr[m][1], sr[m][0]) + sr[m][2];
+            f.im = fma(-k2, si[m][1], si[m][0]) + si[m][2];
+            s.Fa[i * kTile + lx] = f;
+          } else {
+            f.re = sr[m][0] + sr[m][1];
+            f.im = si[m][0] + si[m][1];
+            s.Fb[i * kTile + lx] = f;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// out[i] = sum_j A[i][j] y[i + 2(j - dl)] over the valid band (channel/mvOps.c:198-220)
+__device__ __forceinline__ cpx band_matvec_row(const double* __restrict__ A, int w, int dl, int du, int N,
+                                               const cpx* y, int ystride, int i) {
+  int j0 = dl - i / 2;
+  if (j0 < 0) j0 = 0;
+  int j1 = (N - i + 1) / 2 + dl;
+  if (j1 > dl + du + 1) j1 = dl + du + 1;
+  double re = 0.0, im = 0.0;
+  for (int j = j0; j < j1; ++j) {
+    const double a = __ldg(A + (size_t)i * w + j);
+    const cpx v = y[(i - 2 * (dl - j)) * ystride];
+    re = fma(a, v.re, re);
+    im = fma(a, v.im, im);
+  }
+  return cpx{re, im};
+}
+
+// one elimination chain (fixed parity, real or imaginary part) of the
+// no-pivot every-other-diagonal LU solve (channel/mvOps.c:29-91)
+__device__ void band_solve_chain(const double* __restrict__ LU, int w, int dl, int du, int N, int par,
+                                 double* b, int bstride) {
+  for (int i = par; i < N; i += 2) {
+    if (i < 2) continue;
+    int j0 = dl - i / 2;
+    if (j0 < 0) j0 = 0;
+    double acc = b[i * bstride];
+    for (int j = j0; j < dl; ++j) acc = fma(-__ldg(LU + (size_t)i * w + j), b[(i - 2 * (dl - j)) * bstride], acc);
+    b[i * bstride] = acc;
+  }
+  // back substitution: the last row of this parity first
+  int ilast = ((N - 1 - par) % 2 == 0) ? N - 1 : N - 2;
+  for (int i = ilast; i >= 0; i -= 2) {
+    double acc = b[i * bstride];
+    if (i <= N - 3) {
+      int jm = (N - i + 1) / 2 - 1;
+      if (jm > du) jm = du;
+      for (int j = 1; j <= jm; ++j) acc = fma(-__ldg(LU + (size_t)i * w + dl + j), b[(i + 2 * j) * bstride], acc);
+    }
+    b[i * bstride] = acc / __ldg(LU + (size_t)i * w + dl);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_solve(Grid g, SolveArgs a) {
+  const int ntx = (g.X + kTile - 1) / kTile;
+  const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
+  const int inst = blockIdx.y;
+  if (blocked(a.status, a.sdiv, inst)) return;
+  const int x0 = tx * kTile;
+  const int nx = min(kTile, g.X - x0);
+  const size_t csz = coef_size(g);
+  cpx* __restrict__ Cc = a.Cc.at(inst);
+  cpx* __restrict__ So = a.Sout.at(inst);
+  cpx* Tst = nullptr;
+  if (a.T.base && (inst % a.tdiv) == a.tsel) {
+    const int slot = a.slot.slot();
+    if (slot >= 0) Tst = a.T.base + (long long)(inst / a.tdiv) * a.T.stride + (long long)slot * a.slot.stride;
+  }
+  int mean_mode = a.mean_mode;
+  if (mean_mode == MEAN_TAN_HOMOG && ((a.forced_mask >> (inst % a.mdiv)) & 1u)) mean_mode = MEAN_TAN_FORCED;
+  auto cidx = [&](int v, int r, int x) { return (((size_t)z * 2 + v) * g.R + r) * g.X + x; };
+  if (z == g.Nz / 2) {
+    // the Nz/2 line is zeroed every substage and never stored (channel/channel.c:460-467)
+    for (int i = threadIdx.x; i < 2 * g.R * nx; i += blockDim.x) {
+      const int v = i / (g.R * nx), r = (i / nx) % g.R, x = x0 + i % nx;
+      Cc[cidx(v, r, x)] = cpx{0.0, 0.0};
+      So[cidx(v, r, x)] = cpx{0.0, 0.0};
+    }
+    return;
+  }
+  extern __shared__ __align__(16) unsigned char smem[];
+  SolveSmem s = carve_solve(g, smem);
+  const RKc rk = rk_coeffs(a.k, a.adjoint);
+  const bool adj = a.adjoint != 0;
+  const cpx* __restrict__ H = a.H.at(inst);
+  quad_rhs(g, H, z, x0, nx, adj, s);
+  const double dt = g.dt;
+  const int xfirst = (z == 0 && x0 == 0) ? 1 : 0;  // the mean mode has its own system
+  // right-hand sides (channel/project.c:60-81, 125-130, 143-163, 202-207)
+  for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+    const int r = i / kTile, l = i - r * kTile;
+    if (l >= nx || l < xfirst) continue;
+    const int x = x0 + l;
+    const size_t zx = (size_t)z * g.X + x;
+    cpx va, vb;
+    if (r < g.D) {
+      if (a.k == 0) {
+        const double* E = g.exA + ((size_t)rk.aidx0 * g.Nz * g.X + zx) * g.D * 9;
+        va = band_matvec_row(E, 9, 4, 4, g.D, Cc + cidx(0, 0, x), g.X, r);
+      } else {
+        va = Cc[cidx(0, r, x)];
+      }
+      const cpx f = s.Fa[r * kTile + l];
+      va.re += dt * rk.c * f.re;
+      va.im += dt * rk.c * f.im;
+    } else {
+      va = Cc[cidx(0, r, x)];  // alpha rows >= Ny-4 ride along unchanged
+    }
+    if (a.k == 0) {
+      const double* E = g.exB + ((size_t)rk.aidx0 * g.Nz * g.X + zx) * g.R * 5;
+      vb = band_matvec_row(E, 5, 2, 2, g.R, Cc + cidx(1, 0, x), g.X, r);
+    } else {
+      vb = Cc[cidx(1, r, x)];
+    }
+    const cpx f = s.Fb[r * kTile + l];
+    vb.re += dt * rk.c * f.re;
+    vb.im += dt * rk.c * f.im;
+    s.ra[r * kTile + l] = va;
+    s.rb[r * kTile + l] = vb;
+  }
+  __syncthreads();
+  // banded solves: per column 4 chains for alpha, 4 for beta (parity x re/im)
+  if (threadIdx.x < 8 * kTile) {
+    const int l = threadIdx.x / 8, ch = threadIdx.x % 8;
+    if (l < nx && l >= xfirst) {
+      const int x = x0 + l;
+      const size_t zx = (size_t)z * g.X + x;
+      const int par = ch & 1, part = (ch >> 1) & 1;
+      if (ch < 4) {
+        const double* LU = g.luA + ((size_t)rk.bidx * g.Nz * g.X + zx) * g.D * 9;
+        band_solve_chain(LU, 9, 4, 4, g.D, par, reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
+      } else {
+        const double* LU = g.luB + ((size_t)rk.bidx * g.Nz * g.X + zx) * g.R * 5;
+        band_solve_chain(LU, 5, 2, 2, g.R, par, reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
+      }
+    }
+  }
+  __syncthreads();
+  // mean mode (channel/project0.c, increproject0.c, adjproject0.c), warp 0
+  if (xfirst == 1 && threadIdx.x < 32) {
+    double* fa = s.m0;                 // [R]
+    double* fb = s.m0 + g.R;           // [R]
+    cpx* ca = reinterpret_cast<cpx*>(s.m0 + 2 * g.R);  // [R]
+    cpx* cb = ca + g.R;                                // [R]
+    const int lane = threadIdx.x;
+    const size_t cs = (size_t)g.Q * g.X;
+    const cpx* H0 = H;  // z = 0, x = 0
+    for (int i = lane; i < g.R; i += 32) {
+      double sa = 0.0, sb = 0.0;
+      for (int y = 0; y < g.Q; ++y) {
+        const double rw = __ldg(g.Wr + (size_t)i * g.Q + y);
+        sa = fma(rw, H0[1 * cs + (size_t)y * g.X].re, sa);
+        sb = fma(rw, H0[0 * cs + (size_t)y * g.X].re, sb);
+        if (adj) {
+          const double rpw = __ldg(g.Wrp + (size_t)i * g.Q + y);
+          sa = fma(rpw, H0[4 * cs + (size_t)y * g.X].re, sa);
+          sb = fma(-rpw, H0[3 * cs + (size_t)y * g.X].re, sb);
+        }
+      }
+      fa[i] = sa;
+      fb[i] = sb;
+      cpx va, vb;
+      if (a.k == 0) {
+        const double* E = g.ex0 + (size_t)rk.aidx0 * g.R * 5;
+        va = band_matvec_row(E, 5, 2, 2, g.R, Cc + cidx(0, 0, 0), g.X, i);
+        vb = band_matvec_row(E, 5, 2, 2, g.R, Cc + cidx(1, 0, 0), g.X, i);
+      } else {
+        va = Cc[cidx(0, i, 0)];
+        vb = Cc[cidx(1, i, 0)];
+      }
+      va.re += dt * rk.c * sa;
+      vb.re += dt * rk.c * sb;
+      ca[i] = va;
+      cb[i] = vb;
+    }
+    __syncwarp();
+    if (lane < 8) {
+      const double* LU = g.lu0 + (size_t)rk.bidx * g.R * 5;
+      const int par = lane & 1, part = (lane >> 1) & 1;
+      cpx* vec = (lane < 4) ? ca : cb;
+      band_solve_chain(LU, 5, 2, 2, g.R, par, reinterpret_cast<double*>(vec) + part, 2);
+    }
+    __syncwarp();
+    // constant mass flux: a += 0.5 * flux_t * add (channel/project0.c:153-168)
+    double part = 0.0;
+    for (int i = lane; i < g.R; i += 32) part = fma(g.rwsum[i], ca[i].re, part);
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    double flux_t;
+    if (mean_mode == MEAN_PRIMAL) flux_t = g.flux - part;
+    else if (mean_mode == MEAN_TAN_FORCED) flux_t = 2.0 - part;
+    else flux_t = -part;
+    const double* add = g.add0 + (size_t)(adj ? 1 + rk.bidx : 0) * g.R;
+    __syncwarp();
+    for (int i = lane; i < g.R; i += 32) ca[i].re = ca[i].re + flux_t * add[i] * 0.5;
+    __syncwarp();
+    for (int i = lane; i < g.R; i += 32) {
+      So[cidx(0, i, 0)] = ca[i];
+      So[cidx(1, i, 0)] = cb[i];
+      if (Tst) {
+        Tst[cidx(0, i, 0)] = ca[i];
+        Tst[cidx(1, i, 0)] = cb[i];
+      }
+    }
+  }
+  // state rows: alpha from the solve (rows >= Ny-4 carried), beta from the solve
+  for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+    const int r = i / kTile, l = i - r * kTile;
+    if (l >= nx || l < xfirst) continue;
+    const int x = x0 + l;
+    const cpx va = s.ra[r * kTile + l], vb = s.rb[r * kTile + l];
+    So[cidx(0, r, x)] = va;
+    So[cidx(1, r, x)] = vb;
+    if (Tst) {
+      Tst[cidx(0, r, x)] = va;
+      Tst[cidx(1, r, x)] = vb;
+    }
+  }
+  __syncthreads();
+  if (a.k == 2) {
+    // the carried array is the state after the last substage
+    for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+      const int r = i / kTile, l = i - r * kTile;
+      if (l >= nx) continue;
+      const int x = x0 + l;
+      Cc[cidx(0, r, x)] = So[cidx(0, r, x)];
+      Cc[cidx(1, r, x)] = So[cidx(1, r, x)];
+    }
+    return;
+  }
+  // next-substage right-hand side: M(a[k+1]) state + dt d[k+1] F
+  // (channel/project.c:352-404; adjoint F from the previous-stage terms,
+  //  channel/adjproject.c:393-549)
+  if (adj) {
+    __syncthreads();
+    quad_rhs(g, a.Hprev.at(inst), z, x0, nx, true, s);
+    if (xfirst == 1 && threadIdx.x < 32) {
+      // mean mode fa/fb from the previous-stage terms (channel/adjproject0.c:254-294)
+      const cpx* H0 = a.Hprev.at(inst);
+      const size_t cs = (size_t)g.Q * g.X;
+      for (int i = threadIdx.x; i < g.R; i += 32) {
+        double sa = 0.0, sb = 0.0;
+        for (int y = 0; y < g.Q; ++y) {
+          const double rw = __ldg(g.Wr + (size_t)i * g.Q + y);
+          const double rpw = __ldg(g.Wrp + (size_t)i * g.Q + y);
+          sa = fma(rw, H0[1 * cs + (size_t)y * g.X].re, sa);
+          sa = fma(rpw, H0[4 * cs + (size_t)y * g.X].re, sa);
+          sb = fma(rw, H0[0 * cs + (size_t)y * g.X].re, sb);
+          sb = fma(-rpw, H0[3 * cs + (size_t)y * g.X].re, sb);
+        }
+        s.m0[i] = sa;
+        s.m0[g.R + i] = sb;
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+    const int r = i / kTile, l = i - r * kTile;
+    if (l >= nx || l < xfirst) continue;
+    const int x = x0 + l;
+    const size_t zx = (size_t)z * g.X + x;
+    cpx va, vb;
+    if (r < g.D) {
+      const double* E = g.exA + ((size_t)rk.aidx_next * g.Nz * g.X + zx) * g.D * 9;
+      va = band_matvec_row(E, 9, 4, 4, g.D, So + cidx(0, 0, x), g.X, r);
+      const cpx f = s.Fa[r * kTile + l];
+      va.re += dt * rk.dnext * f.re;
+      va.im += dt * rk.dnext * f.im;
+    } else {
+      va = So[cidx(0, r, x)];
+    }
+    const double* E = g.exB + ((size_t)rk.aidx_next * g.Nz * g.X + zx) * g.R * 5;
+    vb = band_matvec_row(E, 5, 2, 2, g.R, So + cidx(1, 0, x), g.X, r);
+    const cpx f = s.Fb[r * kTile + l];
+    vb.re += dt * rk.dnext * f.re;
+    vb.im += dt * rk.dnext * f.im;
+    s.ra[r * kTile + l] = va;
+    s.rb[r * kTile + l] = vb;
+  }
+  if (xfirst == 1 && threadIdx.x < 32) {
+    const double* E = g.ex0 + (size_t)rk.aidx_next * g.R * 5;
+    cpx* ca = reinterpret_cast<cpx*>(s.m0 + 2 * g.R);
+    cpx* cb = ca + g.R;
+    for (int i = threadIdx.x; i < g.R; i += 32) {
+      cpx va = band_matvec_row(E, 5, 2, 2, g.R, So + cidx(0, 0, 0), g.X, i);
+      cpx vb = band_matvec_row(E, 5, 2, 2, g.R, So + cidx(1, 0, 0), g.X, i);
+      va.re += dt * rk.dnext * s.m0[i];
+      vb.re += dt * rk.dnext * s.m0[g.R + i];
+      ca[i] = va;
+      cb[i] = vb;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+    const int r = i / kTile, l = i - r * kTile;
+    if (l >= nx) continue;
+    const int x = x0 + l;
+    if (l < xfirst) {
+      const cpx* ca = reinterpret_cast<const cpx*>(s.m0 + 2 * g.R);
+      Cc[cidx(0, r, x)] = ca[r];
+      Cc[cidx(1, r, x)] = ca[g.R + r];
+    } else {
+      Cc[cidx(0, r, x)] = s.ra[r * kTile + l];
+      Cc[cidx(1, r, x)] = s.rb[r * kTile + l];
+    }
+  }
+}
+
+cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st) {
+  if (a.ninst <= 0) return cudaSuccess;
+  const int ntx = (g.X + kTile - 1) / kTile;
+  k_solve<<<dim3(g.Nz * ntx, a.ninst), kThreads, solve_smem_bytes(g), st>>>(g, a);
+  return cudaGetLastError();
+}
+
+void prepare_recon_solve(const Grid& g) {
+  cudaFuncSetAttribute(k_recon, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)recon_smem_bytes(g));
+  cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)solve_smem_bytes(g));
+}
+
+}  // namespace chn

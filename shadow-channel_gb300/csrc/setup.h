@@ -1,0 +1,38 @@
+// Host-side construction of the time-invariant tables of the Legendre-Galerkin
+// channel discretisation: quadrature, basis values, banded Gram matrices, and
+// the LU factors of every implicit operator the RK3 step can ask for.
+#pragma once
+
+#include <vector>
+
+namespace chn {
+
+struct HostTables {
+  int Nx, Ny, Nz, X, Q, R, D, pz, px;
+  double Lx, Lz, Re, re, flux, dt;
+  std::vector<double> y, w;                 // quadrature points (ascending) and weights
+  std::vector<double> Bq, Bqp, Bqpp;        // [Q][D]
+  std::vector<double> Br, Brp;              // [Q][R]
+  std::vector<double> Wq, Wqp, Wqpp;        // [D][Q]
+  std::vector<double> Wr, Wrp;              // [R][Q]
+  std::vector<double> Qs, Qps, Qpps;        // [D][9]
+  std::vector<double> Rs, Rps;              // [R][5]
+  std::vector<double> Kx, Kz, K2, kxK2, kzK2, cfl2;
+  double cfl1, cfl3;
+  std::vector<double> luA, luB, exA, exB;   // see Grid in chn_common.cuh
+  std::vector<double> lu0, ex0, add0, rwsum;
+  std::vector<double> twz, twx;             // interleaved re,im
+};
+
+// Returns false (with a message in err) for parameters the reference rejects
+// (channel/channel.c:301-312: Nx % 4, Nz % 2, Ny > 4).
+bool build_tables(int Nx, int Ny, int Nz, double Lx, double Lz, double Re, double flux,
+                  double dt, HostTables& t, const char** err);
+
+// No-pivot LU of a banded matrix whose nonzeros sit on even offsets only, in
+// place, rows of pitch w with the diagonal in column dl (the reference's
+// elimination order, channel/mvOps.c:35-65): L multipliers left of column
+// dl, the pivots in column dl, U to the right.
+void band_lu(double* A, int w, int dl, int du, int N);
+
+}  // namespace chn

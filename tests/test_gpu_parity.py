@@ -1,0 +1,210 @@
+"""GPU parity: the product (libc_channel.so, FP64 CUDA) against the CPU oracle.
+
+Every call goes through the C ABI via the c_channel ctypes module, exactly
+like the reference's SWIG module is driven by channel/__init__.py.  The
+oracle is the C restatement (oracle/chan_port.c), itself pinned bit-exact to
+the reference (tests/test_oracle_pin.py), and the golden fixtures made from
+the reference (tests/golden).
+
+Tolerances (FP64, summation order and FFT algorithm differ from the
+reference): relative L2 error <= 1e-12 per time step for states, 1e-12 for
+physical fields; see each test.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import has_gpu
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def rel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def cc():
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+    from channel import c_channel
+    return c_channel
+
+
+def _init_both(cc, args):
+    Nx, Ny, Nz, Lx, Lz, Re, flux, dt, n = args
+    assert cc.c_init(Nx, Ny, Nz, Lx, Lz, Re, flux, dt, n) == 0, cc.c_last_error_message()
+    return O.PortChannel(*args)
+
+
+CFG_TINY = (8, 9, 8, 2 * np.pi, np.pi, 500.0, 2.0, 0.01, 4)
+CFG0 = (16, 33, 16, 2 * np.pi, np.pi, 2000.0, 2.0, 0.01, 10)
+
+
+@pytest.mark.parametrize("args", [CFG_TINY, CFG0])
+def test_quadrature_and_spec2phys(cc, args):
+    ref = _init_both(cc, args)
+    y, w = cc.c_quad()
+    yr, wr = ref.quad()
+    assert np.abs(y - yr).max() <= 4e-16 and np.abs(w - wr).max() <= 1e-15
+    C = O.synthetic_state(*args[:3], seed=7)
+    flow = np.zeros(ref.flow_shape)
+    cc.c_spec2phys(C, flow)
+    assert rel(flow, ref.spec2phys(C)) <= TOL
+
+
+@pytest.mark.parametrize("args", [CFG_TINY, CFG0])
+def test_primal_per_step(cc, args):
+    """Per-step relative L2 error <= 1e-12 over every stored step (10 at config 0)."""
+    ref = _init_both(cc, args)
+    n = args[-1]
+    C0 = O.synthetic_state(*args[:3], seed=0)
+    Cg, Cr = C0.copy(), C0.copy()
+    cc.c_primal(0, Cg)
+    assert cc.c_last_error() == 0, cc.c_last_error_message()
+    ref.primal(0, Cr)
+    for i in range(n + 1):
+        assert rel(cc.c_getsoln(i), ref.getsoln(i)) <= TOL * max(1, i), i
+    assert rel(Cg, Cr) <= TOL * n
+
+
+def test_primal_matches_golden(cc):
+    g = dict(np.load(O.HERE.parent / "tests" / "golden" / "golden_cfg0.npz"))
+    args = tuple(g["args"])
+    args = tuple(int(a) if i in (0, 1, 2, 8) else float(a) for i, a in enumerate(args))
+    assert cc.c_init(*args) == 0
+    C = g["C0"].copy()
+    cc.c_primal(0, C)
+    assert rel(C, g["C"]) <= TOL * args[-1]
+    IC = g["IC0"].copy()
+    cc.c_tangent(0, args[-1], IC, 1)
+    assert rel(IC, g["IC_inh"]) <= 1e-11
+    AC = g["AC0b"].copy()
+    cc.c_adjoint(args[-1], 1, AC, 0, 0.0)
+    assert rel(AC, g["ACb"]) <= 1e-11
+
+
+@pytest.mark.parametrize("inhomo", [0, 1])
+def test_tangent(cc, inhomo):
+    args = CFG0
+    ref = _init_both(cc, args)
+    n = args[-1]
+    C0 = O.synthetic_state(*args[:3], seed=0)
+    cc.c_primal(0, C0.copy())
+    ref.primal(0, C0.copy())
+    IC0 = O.synthetic_state(*args[:3], seed=3, laminar=False)
+    ICg, ICr = IC0.copy(), IC0.copy()
+    cc.c_tangent(2, n, ICg, inhomo)
+    ref.tangent(2, n, ICr, inhomo)
+    assert rel(ICg, ICr) <= 1e-11
+    for i in range(2, n + 1):
+        assert rel(cc.c_getincresoln(i), ref.getincresoln(i)) <= 1e-11, i
+
+
+@pytest.mark.parametrize("strength", [0.0, 0.8])
+def test_adjoint(cc, strength):
+    args = CFG0
+    ref = _init_both(cc, args)
+    n = args[-1]
+    C0 = O.synthetic_state(*args[:3], seed=0)
+    cc.c_primal(0, C0.copy())
+    ref.primal(0, C0.copy())
+    IC0 = O.synthetic_state(*args[:3], seed=3, laminar=False)
+    cc.c_tangent(0, n, IC0.copy(), 1)
+    ref.tangent(0, n, IC0.copy(), 1)
+    AC0 = O.synthetic_state(*args[:3], seed=4, laminar=False)
+    ACg, ACr = AC0.copy(), AC0.copy()
+    cc.c_adjoint(n, 1, ACg, 0, strength)
+    ref.adjoint(n, 1, ACr, 0, strength)
+    assert rel(ACg, ACr) <= 1e-11
+
+
+def test_ddt_project(cc):
+    args = CFG0
+    ref = _init_both(cc, args)
+    C0 = O.synthetic_state(*args[:3], seed=0)
+    cc.c_primal(0, C0.copy())
+    ref.primal(0, C0.copy())
+    for i in (0, 3):
+        V0 = O.synthetic_state(*args[:3], seed=9 + i, laminar=False)
+        Vg, Vr = V0.copy(), V0.copy()
+        rg = cc.c_ddt_project(i, Vg)
+        rr = ref.ddt_project(i, Vr)
+        assert abs(rg - rr) <= 1e-11 * max(1.0, abs(rr))
+        assert rel(Vg, Vr) <= TOL
+
+
+def test_laminar_start_with_rand(cc):
+    args = CFG_TINY
+    ref = O.PortChannel(*args)
+    O.libc_srand(1)
+    ref.primal(0, None)
+    assert cc.c_init(*args) == 0
+    O.libc_srand(1)
+    cc.c_primal(0, np.zeros((0, 0, 0, 0), complex))
+    for i in range(args[-1] + 1):
+        assert rel(cc.c_getsoln(i), ref.getsoln(i)) <= TOL * max(1, i), i
+
+
+def test_cfl_stop(cc):
+    """A step too large for the CFL limit stops the loop with the state kept,
+    like channel/pass1.c:133-137 + channel/channel.c:448-452."""
+    args = (8, 9, 8, 2 * np.pi, np.pi, 500.0, 2.0, 0.5, 3)
+    ref = _init_both(cc, args)
+    C0 = O.synthetic_state(*args[:3], seed=1)
+    Cg, Cr = C0.copy(), C0.copy()
+    cc.c_primal(0, Cg)
+    assert cc.c_last_error() & 1
+    assert cc.c_last_cfl() >= 2.8
+    assert ref.primal(0, Cr) == -1
+    assert rel(Cg, Cr) <= TOL
+    for i in range(args[-1] + 1):
+        assert rel(cc.c_getsoln(i), ref.getsoln(i)) <= TOL
+
+
+def test_deterministic_rerun(cc):
+    args = CFG_TINY
+    assert cc.c_init(*args) == 0
+    C0 = O.synthetic_state(*args[:3], seed=5)
+    a, b = C0.copy(), C0.copy()
+    cc.c_primal(0, a)
+    cc.c_primal(0, b)
+    assert np.array_equal(a, b)
+
+
+def test_dot_product_terms_match_reference(cc):
+    """testAdj.py pattern (drivers/testAdj.py:22-56): <lambda_0, T v_0> and
+    <T* lambda_0, v_0> in the physical quadrature inner product.  The
+    reference's adjoint (reversed RK coefficients, channel/adjproject.c:34-38)
+    is not the exact transpose of its tangent: the two sides differ by ~2e-4
+    relative at this size.  The drop-in must reproduce both sides."""
+    args = (16, 33, 16, 2 * np.pi, np.pi, 2000.0, 2.0, 0.01, 6)
+    ref = _init_both(cc, args)
+    n = args[-1]
+    C0 = O.synthetic_state(*args[:3], seed=0)
+    cc.c_primal(0, C0.copy())
+    ref.primal(0, C0.copy())
+    y, w = cc.c_quad()
+
+    def sides(T, A, P):
+        IC = O.synthetic_state(*args[:3], seed=22, laminar=False)
+        IC0 = IC.copy()
+        T(1, n - 1, IC, 0)
+        AC = O.synthetic_state(*args[:3], seed=23, laminar=False)
+        AC0 = AC.copy()
+        A(n - 1, 1, AC, 0, 0.0)
+        return (P(AC0) * P(IC) * w[:, None]).sum(), (P(AC) * P(IC0) * w[:, None]).sum()
+
+    def gphys(C):
+        f = np.zeros(ref.flow_shape)
+        cc.c_spec2phys(np.ascontiguousarray(C), f)
+        return f
+
+    lg, rg = sides(cc.c_tangent, cc.c_adjoint, gphys)
+    lr, rr = sides(ref.tangent, ref.adjoint, ref.spec2phys)
+    assert abs(lg - lr) <= 1e-10 * abs(lr)
+    assert abs(rg - rr) <= 1e-10 * abs(rr)
