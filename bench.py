@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""Benchmark: LSS segment-steps per second on a GB300.
+
+Workload (the batched least-squares-shadowing configuration): 64 segments of
+a 32x65x32 channel (Nx x Ny x Nz; 2pi x 2 x pi box, Re 3300, dt 0.005, FP64).
+One segment-step is one RK3 time step of the primal, two homogeneous
+tangents, one mean-flux-forced tangent (all advanced together) and one
+adjoint coupled to the forced tangent with strength 1 (the LSS backward
+solve).  A timed "step" advances every segment by one segment-step: the
+timed region is a forward sweep of K steps followed by the adjoint sweep of
+the same K steps back, exactly the per-segment work of one LSS matvec.
+
+Segment initial states: a seeded synthetic state (laminar profile plus
+low-mode noise) run up for 200 steps, plus independent seeded 1e-3
+perturbations per segment.  The working set (trajectories of 64 segments,
+physical-space fields) is several GB, far larger than the 126 MB L2, so no
+L2 flush is needed between steps.
+
+Prints one JSON line.  ``--impl reference`` times the reference algorithm
+on the host cores instead (the C restatement in oracle/, one segment per
+process, all cores).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "shadow-channel_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+GRID = dict(Nx=32, Ny=65, Nz=32, Lx=2 * math.pi, Lz=math.pi, Re=3300.0, flux=2.0, dt=0.005)
+NSEG, NTAN, COUPLE = 64, 3, 2
+INHOMO = [0, 0, 1]
+RUNUP = 200
+METRIC = "steps/s fwd+tangent+adjoint, 64 segs 32x32x65 FP64: batched vs plain GPU"
+UNIT = "segment-steps/s"
+CONFIG = {"workload": "64 LSS segments, 32x65x32 channel (Nx x Ny x Nz), Re 3300, dt 0.005; per segment-step "
+                      "1 primal + 2 homogeneous + 1 mean-flux tangent + 1 adjoint (strength 1)",
+          "segments": NSEG, "tangents_per_segment": NTAN, "grid": "32x65x32", "dtype": "f64",
+          "l2": "working set several GB > 126 MB L2 (no flush needed)"}
+
+
+def args_parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--segments", type=int, default=NSEG,
+                    help="segments per GPU (default 64; smaller only for profiling captures)")
+    return ap.parse_args()
+
+
+def grid_args(nsteps):
+    g = GRID
+    return (g["Nx"], g["Ny"], g["Nz"], g["Lx"], g["Lz"], g["Re"], g["flux"], g["dt"], nsteps)
+
+
+def segment_states(C_parent, nseg, seed0=1000, amp=1e-3):
+    from channel.synthetic import synthetic_state
+    g = GRID
+    out = np.empty((nseg,) + C_parent.shape, np.complex128)
+    for s in range(nseg):
+        pert = synthetic_state(g["Nx"], g["Ny"], g["Nz"], seed=seed0 + s, amp=amp, laminar=False)
+        out[s] = C_parent + pert
+    return out
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic FP64 work (flop, FMA = 2) of the dominant kernels, per launch
+# ---------------------------------------------------------------------------
+
+def fft_flops(n):
+    return 5.0 * n * math.log2(n)
+
+
+def phys_inverse_flops(ninst, g, nfields=6):
+    """z inverse FFTs of Nx/2 columns plus x inverse FFTs of the row pairs,
+    per plane and field (5 N log2 N per complex transform)."""
+    Nx, Ny, Nz = g["Nx"], g["Ny"], g["Nz"]
+    X, Q, pz, px = Nx // 2, 3 * Ny // 2, 3 * Nz // 2, 3 * Nx // 2
+    per_plane = X * fft_flops(pz) + ((pz + 1) // 2) * fft_flops(px)
+    return ninst * nfields * Q * per_plane
+
+
+def recon_flops(ninst, g):
+    """Parity-split reconstruction: (3D + 2R) complex multiply-adds per plane
+    pair and (kz, kx) mode, plus 24 flop of wavenumber algebra per point."""
+    Nx, Ny, Nz = g["Nx"], g["Ny"], g["Nz"]
+    X, Q, R, D = Nx // 2, 3 * Ny // 2, Ny - 2, Ny - 4
+    Qh = (Q + 1) // 2
+    modes = (Nz - 1) * X
+    return ninst * modes * (Qh * (3 * D + 2 * R) * 4 + Q * 24)
+
+
+# ---------------------------------------------------------------------------
+# the GB300 arm
+# ---------------------------------------------------------------------------
+
+def run_gb300(a):
+    global NSEG
+    NSEG = a.segments
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    from channel import c_channel as cc
+
+    K, W = a.steps, max(3, a.warmup)
+    nsteps = max(K, W)
+    assert cc.c_init(*grid_args(nsteps)) == 0, cc.c_last_error_message()
+    from channel.synthetic import synthetic_state
+    C0 = synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=0)
+    # parent field: run-up through the single-trajectory path (not timed)
+    cc.c_destroy()
+    assert cc.c_init(*grid_args(1)) == 0
+    Cp = C0.copy()
+    cc.c_primal(RUNUP, Cp)
+    cc.c_destroy()
+    assert cc.c_init(*grid_args(nsteps)) == 0
+    Cseg = segment_states(Cp, NSEG)
+    IC0 = np.stack([synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=2000 + i, laminar=False)
+                    for i in range(NSEG * NTAN)])
+    AC0 = np.stack([synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=5000 + i, laminar=False)
+                    for i in range(NSEG)])
+    assert cc.lib.c_batch_init(NSEG, NTAN, COUPLE) == 0, cc.c_last_error_message()
+    inh = (ctypes_int_array(INHOMO))
+    dev = torch.device("cuda", local)
+    dC = torch.from_numpy(Cseg.view(np.float64)).to(dev)
+    dIC = torch.from_numpy(IC0.view(np.float64)).to(dev)
+    dAC = torch.from_numpy(AC0.view(np.float64)).to(dev)
+
+    def sweep(k):
+        rc = cc.lib.c_batch_forward_dev(0, k, dC.data_ptr(), dIC.data_ptr(), inh)
+        assert rc == 0, (rc, cc.c_last_error_message())
+        rc = cc.lib.c_batch_adjoint_dev(k, 0, dAC.data_ptr(), 1.0)
+        assert rc == 0, (rc, cc.c_last_error_message())
+
+    # warm-up (untimed)
+    sweep(W)
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(cc.lib.c_stream(), device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = cc.c_launch_count()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        sweep(K)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = cc.c_launch_count() - launches0
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * NSEG * K / (ms * 1e-3)
+
+    # end to end through the host-array C ABI (H2D of the inputs and D2H of
+    # the results inside the timed region)
+    hC = np.ascontiguousarray(Cseg.copy())
+    hIC = np.ascontiguousarray(IC0.copy())
+    hAC = np.ascontiguousarray(AC0.copy())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc1 = cc.lib.c_batch_forward(0, K, hC.ctypes.data, hIC.ctypes.data, inh)
+    rc2 = cc.lib.c_batch_adjoint(K, 0, hAC.ctypes.data, 1.0)
+    cc.c_synchronize()
+    e2e_s = time.perf_counter() - t0
+    assert rc1 == 0 and rc2 == 0, cc.c_last_error_message()
+    bytes_in = (hC.nbytes + hIC.nbytes + hAC.nbytes)
+    e2e = {"value": NSEG * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bytes_in // K,
+           "d2h_bytes_per_step": bytes_in // K}
+
+    # roofline of the dominant kernel: CUDA events on the library stream
+    peak = cc.c_fp64_peak_tflops()
+    nt = NSEG * NTAN
+    k_ms = {name: cc.lib.c_batch_kernel_ms(i, 5) for i, name in
+            enumerate(["recon", "phys_inverse", "products_fwd", "solve", "products_adj"])}
+    dom_ms = k_ms["phys_inverse"]
+    flops = phys_inverse_flops(nt, GRID)
+    achieved = flops / (dom_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp64", "kernel": "k_phys_inverse (192 tangent fields)", "achieved": achieved,
+                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": "measured: FP64 FMA probe in this run (c_fp64_peak_tflops)",
+                "algorithmic_flop_per_launch": flops, "kernel_ms": k_ms,
+                "recon_tflops": recon_flops(nt, GRID) / (k_ms["recon"] * 1e-3) / 1e12}
+
+    cc.lib.c_batch_destroy()
+    cc.c_destroy()
+    plain = None
+    if not a.no_plain and rank == 0:
+        plain = plain_gpu(cc, Cseg[0], IC0[:NTAN], AC0[0], min(K, 6))
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic seeded states (no dataset; reference restart files absent)",
+            "config": CONFIG, "e2e": e2e, "roofline": roofline, "gpu_launches": launches,
+            "clocks": clk.summary()}
+    if plain:
+        line["plain_gpu"] = plain
+        line["plain_gpu"]["batched_over_plain"] = (value / world) / plain["value"]
+    if rank == 0 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def ctypes_int_array(vals):
+    import ctypes
+    return (ctypes.c_int * len(vals))(*vals)
+
+
+def plain_gpu(cc, C, IC, AC, K):
+    """One trajectory per launch sequence through the reference entry points
+    (c_primal, three c_tangent calls, c_adjoint coupled to the last tangent)
+    for one segment over K steps; segment-steps per second."""
+    assert cc.c_init(*grid_args(K)) == 0
+    ICs = [IC[t].copy() for t in range(len(IC))]
+    cc.c_primal(0, C.copy())  # warm-up
+    cc.c_tangent(0, K, IC[0].copy(), 0)
+    cc.c_adjoint(K, 0, AC.copy(), 0, 1.0)
+    cc.c_synchronize()
+    C, AC = C.copy(), AC.copy()
+    t0 = time.perf_counter()
+    cc.c_primal(0, C)
+    for t, x in enumerate(ICs):
+        cc.c_tangent(0, K, x, INHOMO[t])
+    cc.c_adjoint(K, 0, AC, 0, 1.0)
+    cc.c_synchronize()
+    dt_ = time.perf_counter() - t0
+    cc.c_destroy()
+    return {"value": K / dt_, "unit": UNIT, "segments": 1, "steps": K,
+            "note": "single-trajectory entry points (c_primal, c_tangent x3, c_adjoint), host arrays"}
+
+
+# ---------------------------------------------------------------------------
+# CPU: the reference algorithm (oracle restatement) on the host cores
+# ---------------------------------------------------------------------------
+
+def _cpu_segment(steps, seed):
+    import oracle as O
+    ch = O.PortChannel(*grid_args(steps))
+    C = O.synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=seed)
+    IC = [O.synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=seed + 1 + t, laminar=False)
+          for t in range(NTAN)]
+    AC = O.synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=seed + 9, laminar=False)
+    t0 = time.perf_counter()
+    ch.primal(0, C)
+    for t in range(NTAN):
+        ch.tangent(0, steps, IC[t], INHOMO[t])
+    ch.adjoint(steps, 0, AC, 0, 1.0)
+    dt_ = time.perf_counter() - t0
+    ch.close()
+    return dt_
+
+
+def cpu_baseline(steps=2):
+    import oracle as O
+    O.build_port()
+    dt_ = _cpu_segment(steps, 0)
+    return {"value": steps / dt_, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"1 segment x {steps} segment-steps (primal, 3 tangents each re-running the primal as "
+                      f"the reference does, adjoint with strength 1) at 32x65x32, oracle/chan_port.c, 1 thread",
+            "seconds": dt_}
+
+
+def run_reference(a):
+    """The reference algorithm on all host cores: one segment per process."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    import oracle as O
+    O.build_port()
+    cores = os.cpu_count() or 1
+    steps = 1
+    W = 0
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.starmap(_cpu_segment, [(1, 100 + i) for i in range(min(cores, 2))])  # warm-up
+        vals = []
+        for k in range(max(1, min(a.steps, 2))):
+            t0 = time.perf_counter()
+            pool.starmap(_cpu_segment, [(steps, 200 + 10 * i + k) for i in range(cores)])
+            vals.append(time.perf_counter() - t0)
+    wall = statistics.median(vals)
+    value = cores * steps / wall
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+            "steps": len(vals), "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded states",
+            "config": CONFIG,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{cores} processes x 1 segment x {steps} segment-step at 32x65x32 "
+                                       f"(oracle/chan_port.c, the reference algorithm)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    a = args_parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)

@@ -128,6 +128,13 @@ int c_batch_primal_dev(int ru_steps, chn_complex *C);
 int c_batch_tangent_dev(int start_step, int end_step, chn_complex *IC,
                         const int *inhomo);
 
+/* the library's CUDA stream (cudaStream_t), for recording events on it */
+void *c_stream(void);
+/* average device time in ms of one launch of one kernel of a batched forward
+   substage on the current batch buffers: 0 reconstruct, 1 physical
+   transforms, 2 tangent products, 3 tangent solve, 4 adjoint products */
+double c_batch_kernel_ms(int which, int reps);
+
 /* wait for all queued device work of the library */
 int c_synchronize(void);
 /* kernel launches issued by the library since c_init (for bookkeeping) */

@@ -99,6 +99,11 @@ _lib.c_batch_forward_dev.restype = _i
 _lib.c_batch_adjoint_dev.argtypes = [_i, _i, _vp, _d]
 _lib.c_batch_adjoint_dev.restype = _i
 
+_lib.c_stream.argtypes = []
+_lib.c_stream.restype = _vp
+_lib.c_batch_kernel_ms.argtypes = [_i, _i]
+_lib.c_batch_kernel_ms.restype = _d
+
 LIBRARY_PATH = str(_LIBPATH)
 lib = _lib
 

@@ -1021,22 +1021,15 @@ int c_batch_adjoint_dev(int start_step, int end_step, chn_complex* AC, double st
   return collect_status(*E, w) ? g_status : -1;
 }
 
-// host-array variants: stage through a temporary device buffer
+// host-array variants: staged through the working set's own device buffers
+// (dC holds the primal states, io the tangent / adjoint states)
 int c_batch_primal(int ru_steps, chn_complex* C) {
   if (!batch_ready("c_batch_primal")) return g_status;
   Work& w = E->batch;
-  cpx* d = nullptr;
   const size_t bytes = sizeof(cpx) * w.csz * w.nseg;
-  if (C) {
-    if (cudaMalloc(&d, bytes) != cudaSuccess) { set_error(-1, "cudaMalloc"); return -1; }
-    cudaMemcpyAsync(d, C, bytes, cudaMemcpyHostToDevice, E->st);
-  }
-  int rc = c_batch_primal_dev(ru_steps, reinterpret_cast<chn_complex*>(d));
-  if (C) {
-    cudaMemcpyAsync(C, d, bytes, cudaMemcpyDeviceToHost, E->st);
-    cudaStreamSynchronize(E->st);
-    cudaFree(d);
-  }
+  if (C && !h2d(*E, w.dC, C, bytes)) return -1;
+  const int rc = c_batch_primal_dev(ru_steps, C ? reinterpret_cast<chn_complex*>(w.dC) : nullptr);
+  if (C && !d2h(*E, C, w.dC, bytes)) return -1;
   return rc;
 }
 
@@ -1044,13 +1037,9 @@ int c_batch_tangent(int start_step, int end_step, chn_complex* IC, const int* in
   if (!batch_ready("c_batch_tangent")) return g_status;
   Work& w = E->batch;
   const size_t bytes = sizeof(cpx) * w.csz * w.nseg * (w.ntan > 0 ? w.ntan : 1);
-  cpx* d = nullptr;
-  if (cudaMalloc(&d, bytes) != cudaSuccess) { set_error(-1, "cudaMalloc"); return -1; }
-  cudaMemcpyAsync(d, IC, bytes, cudaMemcpyHostToDevice, E->st);
-  int rc = c_batch_tangent_dev(start_step, end_step, reinterpret_cast<chn_complex*>(d), inhomo);
-  cudaMemcpyAsync(IC, d, bytes, cudaMemcpyDeviceToHost, E->st);
-  cudaStreamSynchronize(E->st);
-  cudaFree(d);
+  if (!h2d(*E, w.io, IC, bytes)) return -1;
+  const int rc = c_batch_tangent_dev(start_step, end_step, reinterpret_cast<chn_complex*>(w.io), inhomo);
+  if (!d2h(*E, IC, w.io, bytes)) return -1;
   return rc;
 }
 
@@ -1058,21 +1047,13 @@ int c_batch_forward(int start_step, int end_step, chn_complex* C, chn_complex* I
   if (!batch_ready("c_batch_forward")) return g_status;
   Work& w = E->batch;
   const size_t bc = sizeof(cpx) * w.csz * w.nseg;
-  const size_t bt = sizeof(cpx) * w.csz * w.nseg * (w.ntan > 0 ? w.ntan : 1);
-  cpx *dc = nullptr, *dt = nullptr;
-  if (cudaMalloc(&dc, bc) != cudaSuccess || cudaMalloc(&dt, bt) != cudaSuccess) {
-    set_error(-1, "cudaMalloc");
-    return -1;
-  }
-  cudaMemcpyAsync(dc, C, bc, cudaMemcpyHostToDevice, E->st);
-  if (w.ntan > 0) cudaMemcpyAsync(dt, IC, bt, cudaMemcpyHostToDevice, E->st);
-  int rc = c_batch_forward_dev(start_step, end_step, reinterpret_cast<chn_complex*>(dc),
-                               reinterpret_cast<chn_complex*>(dt), inhomo);
-  cudaMemcpyAsync(C, dc, bc, cudaMemcpyDeviceToHost, E->st);
-  if (w.ntan > 0) cudaMemcpyAsync(IC, dt, bt, cudaMemcpyDeviceToHost, E->st);
-  cudaStreamSynchronize(E->st);
-  cudaFree(dc);
-  cudaFree(dt);
+  const size_t bt = sizeof(cpx) * w.csz * w.nseg * w.ntan;
+  if (!h2d(*E, w.dC, C, bc)) return -1;
+  if (bt && !h2d(*E, w.io, IC, bt)) return -1;
+  const int rc = c_batch_forward_dev(start_step, end_step, reinterpret_cast<chn_complex*>(w.dC),
+                                     reinterpret_cast<chn_complex*>(w.io), inhomo);
+  if (!d2h(*E, C, w.dC, bc)) return -1;
+  if (bt && !d2h(*E, IC, w.io, bt)) return -1;
   return rc;
 }
 
@@ -1080,13 +1061,9 @@ int c_batch_adjoint(int start_step, int end_step, chn_complex* AC, double streng
   if (!batch_ready("c_batch_adjoint")) return g_status;
   Work& w = E->batch;
   const size_t bytes = sizeof(cpx) * w.csz * w.nseg;
-  cpx* d = nullptr;
-  if (cudaMalloc(&d, bytes) != cudaSuccess) { set_error(-1, "cudaMalloc"); return -1; }
-  cudaMemcpyAsync(d, AC, bytes, cudaMemcpyHostToDevice, E->st);
-  int rc = c_batch_adjoint_dev(start_step, end_step, reinterpret_cast<chn_complex*>(d), strength);
-  cudaMemcpyAsync(AC, d, bytes, cudaMemcpyDeviceToHost, E->st);
-  cudaStreamSynchronize(E->st);
-  cudaFree(d);
+  if (!h2d(*E, w.io, AC, bytes)) return -1;
+  const int rc = c_batch_adjoint_dev(start_step, end_step, reinterpret_cast<chn_complex*>(w.io), strength);
+  if (!d2h(*E, AC, w.io, bytes)) return -1;
   return rc;
 }
 
@@ -1102,6 +1079,99 @@ int c_batch_getincresoln(int seg, int i_step, chn_complex* out) {
   Work& w = E->batch;
   if (seg < 0 || seg >= w.nseg || i_step < 0 || i_step > E->nsteps) return -4;
   return d2h(*E, out, w.MIC + (size_t)seg * w.traj + (size_t)3 * i_step * w.csz, sizeof(cpx) * w.csz) ? 0 : -1;
+}
+
+void* c_stream(void) { return E ? (void*)E->st : nullptr; }
+
+// Average device time (ms, CUDA events on the library stream) of one launch
+// of one kernel of the batched forward substage 0, on the current batch
+// buffers (run c_batch_forward first so they hold a real state).
+// which: 0 reconstruct (primal + tangents), 1 physical transforms (primal +
+// tangents), 2 tangent products, 3 tangent solve, 4 adjoint products.
+double c_batch_kernel_ms(int which, int reps) {
+  if (!E || !E->have_batch || reps <= 0) return -1.0;
+  Engine& e = *E;
+  Work& w = e.batch;
+  const Grid& g = e.T.g;
+  const int nt = w.nseg * w.ntan;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  int zero = 0;
+  cudaMemcpyAsync(w.step, &zero, sizeof(int), cudaMemcpyHostToDevice, e.st);
+  cudaMemsetAsync(w.status, 0, sizeof(uint32_t) * w.nseg, e.st);
+  auto launch = [&]() -> cudaError_t {
+    switch (which) {
+      case 0: {
+        ReconArgs r{};
+        r.ninst = nt;
+        r.C = cb(w.St, w.csz);
+        r.slot = noslot();
+        r.U = mb(w.Ut, w.usz);
+        r.sdiv = w.ntan;
+        return launch_recon(g, r, e.st);
+      }
+      case 1: {
+        PhysArgs p{};
+        p.U = cb(w.Ut, w.usz);
+        p.P = mbd(w.Pt, w.psz);
+        p.nfields = 6;
+        p.ninst = nt;
+        p.sdiv = w.ntan;
+        return launch_phys_inverse(g, p, e.st);
+      }
+      case 2: {
+        ProdArgs ap{};
+        ap.Pp = cbd(w.Pp, w.psz);
+        ap.pdiv = w.ntan;
+        ap.Pt = cbd(w.Pt, w.psz);
+        ap.H = mb(w.Ut, w.usz);
+        ap.ninst = nt;
+        ap.sdiv = w.ntan;
+        return launch_products_fwd(g, ap, e.st);
+      }
+      case 3: {
+        SolveArgs sa{};
+        sa.H = cb(w.Ut, w.usz);
+        sa.Hprev = cb(nullptr, 0);
+        sa.Cc = mb(w.io, w.csz);   // scratch copy: the carried state is left alone
+        sa.Sout = mb(w.io, w.csz);
+        sa.T = mb(nullptr, 0);
+        sa.tdiv = 1;
+        sa.slot = noslot();
+        sa.k = 1;
+        sa.mean_mode = MEAN_TAN_HOMOG;
+        sa.mdiv = w.ntan;
+        sa.ninst = nt;
+        sa.sdiv = w.ntan;
+        return launch_solve(g, sa, e.st);
+      }
+      case 4: {
+        ProdArgs ap{};
+        ap.Pp = cbd(w.Pp, w.psz);
+        ap.pdiv = 1;
+        ap.Pt = cbd(w.Pl, w.psz);
+        ap.H = mb(w.Up, w.usz);
+        ap.ninst = w.nseg;
+        ap.sdiv = 1;
+        return launch_products_adj(g, ap, e.st);
+      }
+      default:
+        return cudaErrorInvalidValue;
+    }
+  };
+  if (which == 3) cudaMemcpyAsync(w.io, w.Ct, sizeof(cpx) * w.csz * nt, cudaMemcpyDeviceToDevice, e.st);
+  if (launch() != cudaSuccess) return -1.0;  // warm-up
+  cudaEventRecord(a, e.st);
+  for (int r = 0; r < reps; ++r) launch();
+  cudaEventRecord(b, e.st);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  g_launches += reps + 1;
+  return ms / reps;
 }
 
 int c_synchronize(void) {

@@ -6,9 +6,13 @@ oracle is the C restatement (oracle/chan_port.c), itself pinned bit-exact to
 the reference (tests/test_oracle_pin.py), and the golden fixtures made from
 the reference (tests/golden).
 
-Tolerances (FP64, summation order and FFT algorithm differ from the
-reference): relative L2 error <= 1e-12 per time step for states, 1e-12 for
-physical fields; see each test.
+Tolerances.  Two valid FP64 evaluations of the reference's own algorithm
+(its C built with and without FMA contraction) differ by up to ~7e-12 per
+step at 16x33x16 and ~1.3e-11 at 32x65x32 for the primal, ~1e-11 for the
+adjoint at 16x33x16 (tests/test_oracle_noise_floor.py measures this): the
+implicit fourth-order operators amplify rounding.  The GPU path is held to
+that floor: per-step primal error <= 5e-12 (16x33x16) and 2e-11 (32x65x32),
+tangent 1e-11, adjoint 3e-11, physical fields 1e-12.
 """
 import numpy as np
 import pytest
@@ -18,7 +22,10 @@ from conftest import has_gpu
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-12
+TOL = 1e-12          # physical fields, quadrature
+TOL_STEP = {16: 5e-12, 32: 2e-11, 8: 5e-12}   # primal, per time step (see module docstring)
+TOL_TAN = 1e-11
+TOL_ADJ = 3e-11
 
 
 def rel(a, b):
@@ -57,19 +64,24 @@ def test_quadrature_and_spec2phys(cc, args):
     assert rel(flow, ref.spec2phys(C)) <= TOL
 
 
-@pytest.mark.parametrize("args", [CFG_TINY, CFG0])
+CFG1 = (32, 65, 32, 2 * np.pi, np.pi, 3300.0, 2.0, 0.005, 10)
+
+
+@pytest.mark.parametrize("args", [CFG_TINY, CFG0, CFG1])
 def test_primal_per_step(cc, args):
-    """Per-step relative L2 error <= 1e-12 over every stored step (10 at config 0)."""
+    """Per-step relative L2 error at the FP64 floor over every stored step (10 steps)."""
     ref = _init_both(cc, args)
     n = args[-1]
+    tol = TOL_STEP[args[0]]
     C0 = O.synthetic_state(*args[:3], seed=0)
     Cg, Cr = C0.copy(), C0.copy()
     cc.c_primal(0, Cg)
     assert cc.c_last_error() == 0, cc.c_last_error_message()
     ref.primal(0, Cr)
-    for i in range(n + 1):
-        assert rel(cc.c_getsoln(i), ref.getsoln(i)) <= TOL * max(1, i), i
-    assert rel(Cg, Cr) <= TOL * n
+    assert np.array_equal(cc.c_getsoln(0), ref.getsoln(0))
+    for i in range(1, n + 1):
+        assert rel(cc.c_getsoln(i), ref.getsoln(i)) <= tol, i
+    assert rel(Cg, Cr) <= tol
 
 
 def test_primal_matches_golden(cc):
@@ -79,13 +91,13 @@ def test_primal_matches_golden(cc):
     assert cc.c_init(*args) == 0
     C = g["C0"].copy()
     cc.c_primal(0, C)
-    assert rel(C, g["C"]) <= TOL * args[-1]
+    assert rel(C, g["C"]) <= TOL_STEP[16]
     IC = g["IC0"].copy()
     cc.c_tangent(0, args[-1], IC, 1)
-    assert rel(IC, g["IC_inh"]) <= 1e-11
+    assert rel(IC, g["IC_inh"]) <= TOL_TAN
     AC = g["AC0b"].copy()
     cc.c_adjoint(args[-1], 1, AC, 0, 0.0)
-    assert rel(AC, g["ACb"]) <= 1e-11
+    assert rel(AC, g["ACb"]) <= TOL_ADJ
 
 
 @pytest.mark.parametrize("inhomo", [0, 1])
@@ -100,9 +112,9 @@ def test_tangent(cc, inhomo):
     ICg, ICr = IC0.copy(), IC0.copy()
     cc.c_tangent(2, n, ICg, inhomo)
     ref.tangent(2, n, ICr, inhomo)
-    assert rel(ICg, ICr) <= 1e-11
+    assert rel(ICg, ICr) <= TOL_TAN
     for i in range(2, n + 1):
-        assert rel(cc.c_getincresoln(i), ref.getincresoln(i)) <= 1e-11, i
+        assert rel(cc.c_getincresoln(i), ref.getincresoln(i)) <= TOL_TAN, i
 
 
 @pytest.mark.parametrize("strength", [0.0, 0.8])
@@ -120,7 +132,7 @@ def test_adjoint(cc, strength):
     ACg, ACr = AC0.copy(), AC0.copy()
     cc.c_adjoint(n, 1, ACg, 0, strength)
     ref.adjoint(n, 1, ACr, 0, strength)
-    assert rel(ACg, ACr) <= 1e-11
+    assert rel(ACg, ACr) <= TOL_ADJ
 
 
 def test_ddt_project(cc):
@@ -134,8 +146,8 @@ def test_ddt_project(cc):
         Vg, Vr = V0.copy(), V0.copy()
         rg = cc.c_ddt_project(i, Vg)
         rr = ref.ddt_project(i, Vr)
-        assert abs(rg - rr) <= 1e-11 * max(1.0, abs(rr))
-        assert rel(Vg, Vr) <= TOL
+        assert abs(rg - rr) <= 1e-12 * max(1.0, abs(rr))
+        assert rel(Vg, Vr) <= 1e-10   # V - r dC/dt cancels; floor 3.5e-11 (noise-floor test)
 
 
 def test_laminar_start_with_rand(cc):
@@ -147,7 +159,7 @@ def test_laminar_start_with_rand(cc):
     O.libc_srand(1)
     cc.c_primal(0, np.zeros((0, 0, 0, 0), complex))
     for i in range(args[-1] + 1):
-        assert rel(cc.c_getsoln(i), ref.getsoln(i)) <= TOL * max(1, i), i
+        assert rel(cc.c_getsoln(i), ref.getsoln(i)) <= TOL_STEP[8], i
 
 
 def test_cfl_stop(cc):
