@@ -143,6 +143,22 @@ long long c_launch_count(void);
    measured with a register-only kernel; used as the roofline peak. */
 double c_fp64_peak_tflops(void);
 
+/* spec2phys without allocating: no counterpart in the reference.  For
+   callers that cannot call cudaMalloc when they need a physical field (code
+   running while a stream is captured into a graph, real-time loops that must
+   not touch the allocator).  C_dev (complex [Nz][2][dimR][Nx/2]) and flow_dev
+   (double [3][3Nx/2][qpts][3Nz/2]) are CUDA device arrays owned by the
+   caller; the intermediate arrays live in fixed device arrays of the library
+   (16 MiB on every GPU that loads it, kept until exit), so grids needing more
+   than 2^19 complex velocity or 2^20 physical scratch elements (beyond
+   32x65x32) are rejected with -5 and a message.  Requires c_init.  The first
+   call on a device looks up the scratch addresses; make that first call
+   before any stream capture.  The work is queued on the library stream
+   (c_stream); c_synchronize before reading flow_dev.  All calls share the
+   scratch, so calls that overlap on the GPU race.  Returns 0 or a negative
+   error (c_last_error_message). */
+int c_spec2phys_noalloc(const chn_complex *C_dev, double *flow_dev);
+
 /* The time-invariant setup tables on the host (no GPU needed): which =
    0 Q, 1 Q', 2 Q'', 3 R, 4 R' (values at the quadrature points, [qpts][n]),
    5..9 the same weighted and transposed ([n][qpts]), 10 <Q,Q>, 11 <Q',Q'>,

@@ -104,6 +104,9 @@ _lib.c_stream.restype = _vp
 _lib.c_batch_kernel_ms.argtypes = [_i, _i]
 _lib.c_batch_kernel_ms.restype = _d
 
+_lib.c_spec2phys_noalloc.argtypes = [_vp, _vp]
+_lib.c_spec2phys_noalloc.restype = _i
+
 LIBRARY_PATH = str(_LIBPATH)
 lib = _lib
 

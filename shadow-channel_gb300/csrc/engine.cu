@@ -673,6 +673,16 @@ static double ddt_project_single(Engine& e, int i_step, cpx* IC_host) {
   return r;
 }
 
+// access for the allocation-free entry point (noalloc.cu)
+bool engine_grid_stream(const Grid** g, cudaStream_t* st) {
+  if (!E) return false;
+  *g = &E->T.g;
+  *st = E->st;
+  return true;
+}
+void engine_set_error(int code, const char* msg) { set_error(code, "%s", msg); }
+void engine_count_launches(int n) { g_launches += n; }
+
 }  // namespace chn
 
 using namespace chn;
