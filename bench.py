@@ -59,6 +59,8 @@ def args_parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--segments", type=int, default=NSEG,
                     help="segments per GPU (default 64; smaller only for profiling captures)")
+    ap.add_argument("--runup", type=int, default=RUNUP,
+                    help="run-up steps of the parent field (default 200; 0 only for profiling captures)")
     return ap.parse_args()
 
 
@@ -187,7 +189,8 @@ def run_gb300(a):
     cc.c_destroy()
     assert cc.c_init(*grid_args(1)) == 0
     Cp = C0.copy()
-    cc.c_primal(RUNUP, Cp)
+    if a.runup > 0:
+        cc.c_primal(a.runup, Cp)
     cc.c_destroy()
     assert cc.c_init(*grid_args(nsteps)) == 0
     Cseg = segment_states(Cp, NSEG)

@@ -165,7 +165,42 @@ struct Work {
   double *part = nullptr, *r = nullptr, *cflmax = nullptr;
   uint32_t* status = nullptr;
   int* step = nullptr;
+  // Primal physical-field cache: the six physical fields of the primal state
+  // before every substage of the stored trajectory, [seg][3 nsteps][6][Q][pz][px].
+  // Tangent and adjoint sweeps read them instead of rebuilding them from MC.
+  // Allocated only when it fits in half of the free device memory.
+  double* Pc = nullptr;
+  long long cstride = 0;       // elements per segment in Pc
+  std::vector<char> slot_ok;   // slot c of Pc holds the fields of MC[c]
+  // Velocity cache of the coupled tangent: u, v, w of MIC[3i] for every step
+  // i, [seg][nsteps][3][Q][pz][px], written by the forward sweep at substage
+  // 0; the adjoint coupling (ddt_project) reads it with the primal cache.
+  double* Pv = nullptr;
+  long long vslot = 0, vstride = 0;
+  std::vector<char> vel_ok;    // slot i of Pv holds the fields of MIC[3i]
+  cpx* icp = nullptr;          // projected IC' of the last coupling, per segment
+  bool raw_start = false;      // MC came from a laminar start without run-up
   std::vector<void*> ptrs;
+  void mark(int c0, int c1, bool ok) {
+    for (int c = c0; c < c1 && c < (int)slot_ok.size(); ++c)
+      if (c >= 0) slot_ok[c] = ok;
+  }
+  bool cached(int c0, int c1) const {
+    if (!Pc || c0 < 0 || c1 > (int)slot_ok.size()) return false;
+    for (int c = c0; c < c1; ++c)
+      if (!slot_ok[c]) return false;
+    return true;
+  }
+  // the coupling at step i can take its fields from the caches
+  bool coupling_cached(int i) const {
+    if (!Pv || i < 0 || i >= (int)vel_ok.size() || !vel_ok[i]) return false;
+    const int ip = i == 0 ? 3 : 3 * i, im = i == 0 ? 0 : 3 * (i - 1);
+    return cached(ip, ip + 1) && cached(im, im + 1);
+  }
+  void mark_vel(int i0, int i1, bool ok) {
+    for (int i = i0; i < i1 && i < (int)vel_ok.size(); ++i)
+      if (i >= 0) vel_ok[i] = ok;
+  }
   static constexpr int kDotBlocks = 64;
 
   template <typename T>
@@ -196,7 +231,39 @@ struct Work {
            alloc(&io, nt * csz) && alloc(&Pp, nseg * psz) && alloc(&Pt, nt * psz) &&
            alloc(&Pprev, nseg * psz) && alloc(&Pl, nseg * psz) && alloc(&flow, (size_t)3 * g.Q * plane_size(g)) &&
            alloc(&part, (size_t)nseg * kDotBlocks * 2) && alloc(&r, nseg) && alloc(&cflmax, nseg) &&
-           alloc(&status, nseg) && alloc(&step, 4);
+           alloc(&status, nseg) && alloc(&step, 4) && alloc(&icp, nseg * csz) && alloc_cache(g);
+  }
+  bool alloc_cache(const Grid& g) {
+    Pc = nullptr;
+    Pv = nullptr;
+    slot_ok.assign(3 * (size_t)(nsteps > 0 ? nsteps : 0), 0);
+    vel_ok.assign((size_t)(nsteps > 0 ? nsteps : 0), 0);
+    const char* off = getenv("CHN_NO_FIELD_CACHE");
+    if ((off && off[0] == '1') || nsteps <= 0) return true;
+    cstride = (long long)3 * nsteps * (long long)psz;
+    vslot = (long long)3 * g.Q * (long long)plane_size(g);
+    vstride = (ntan > 0) ? (long long)nsteps * vslot : 0;
+    const size_t need_c = (size_t)nseg * (size_t)cstride * sizeof(double);
+    const size_t need_v = (size_t)nseg * (size_t)vstride * sizeof(double);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || need_c + need_v > free_b / 2) return true;
+    void* q = nullptr;
+    if (cudaMalloc(&q, need_c) != cudaSuccess) {
+      cudaGetLastError();
+      return true;
+    }
+    ptrs.push_back(q);
+    Pc = reinterpret_cast<double*>(q);
+    if (need_v) {
+      q = nullptr;
+      if (cudaMalloc(&q, need_v) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+      }
+      ptrs.push_back(q);
+      Pv = reinterpret_cast<double*>(q);
+    }
+    return true;
   }
 };
 
@@ -236,26 +303,41 @@ struct FwdOpts {
   int ru;               // run-up steps of the primal (MC slot offset)
   uint32_t forced_mask; // tangents with the mean-flux forcing
   bool raw_u_first;     // the primal velocity of substage 0 is already in Up
+  bool cache;           // adv_primal: write the primal fields to the cache;
+                        // otherwise: read them from the (valid) cache
+  bool store = true;    // adv_primal: store the primal states in MC
 };
 
 static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
   const Grid& g = e.T.g;
   cudaStream_t st = e.st;
   const int nt = w.nseg * w.ntan;
+  const bool use_cache = o.cache && w.Pc != nullptr;
   for (int k = 0; k < 3; ++k) {
-    ReconArgs rp{};
-    rp.ninst = w.nseg;
-    rp.U = mb(w.Up, w.usz);
-    rp.status = w.status;
-    rp.sdiv = 1;
-    if (o.adv_primal) {
-      rp.C = cb(w.Sp, w.csz);
-      rp.slot = noslot();
-    } else {
-      rp.C = cb(w.MC, w.traj);
-      rp.slot = SlotRef{w.step, 3, k, (long long)w.csz};  // state before substage k: MC[3n + k]
+    // where this substage's primal physical fields live
+    Batch<const double> Pprim = cbd(w.Pp, w.psz);
+    SlotRef pslot = noslot();
+    if (use_cache) {
+      Pprim = cbd(w.Pc, w.cstride);
+      // state before substage k: 3(n - ru) + k when advancing, 3n + k otherwise
+      pslot = SlotRef{w.step, 3, k - (o.adv_primal ? 3 * o.ru : 0), (long long)w.psz};
     }
-    if (!(o.raw_u_first && k == 0)) LK(launch_recon(g, rp, st));
+    const bool need_primal_fields = o.adv_primal || !use_cache;
+    if (need_primal_fields) {
+      ReconArgs rp{};
+      rp.ninst = w.nseg;
+      rp.U = mb(w.Up, w.usz);
+      rp.status = w.status;
+      rp.sdiv = 1;
+      if (o.adv_primal) {
+        rp.C = cb(w.Sp, w.csz);
+        rp.slot = noslot();
+      } else {
+        rp.C = cb(w.MC, w.traj);
+        rp.slot = SlotRef{w.step, 3, k, (long long)w.csz};  // state before substage k: MC[3n + k]
+      }
+      if (!(o.raw_u_first && k == 0)) LK(launch_recon(g, rp, st));
+    }
     if (o.tangents) {
       ReconArgs rt{};
       rt.ninst = nt;
@@ -266,29 +348,38 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
       rt.sdiv = w.ntan;
       LK(launch_recon(g, rt, st));
     }
-    PhysArgs pp{};
-    pp.U = cb(w.Up, w.usz);
-    pp.P = mbd(w.Pp, w.psz);
-    pp.nfields = 6;
-    pp.ninst = w.nseg;
-    pp.status = w.status;
-    pp.sdiv = 1;
-    pp.cflmax = w.cflmax;
-    pp.cfl_check = k == 0;  // channel/pass1.c:117
-    pp.skip_blocked = 1;
-    LK(launch_phys_inverse(g, pp, st));
+    if (need_primal_fields) {
+      PhysArgs pp{};
+      pp.U = cb(w.Up, w.usz);
+      pp.P = Batch<double>{const_cast<double*>(Pprim.base), Pprim.stride};
+      pp.pslot = pslot;
+      pp.nfields = 6;
+      pp.ninst = w.nseg;
+      pp.status = w.status;
+      pp.sdiv = 1;
+      pp.cflmax = w.cflmax;
+      pp.cfl_check = k == 0;  // channel/pass1.c:117
+      pp.skip_blocked = 1;
+      LK(launch_phys_inverse(g, pp, st));
+    }
     if (o.tangents) {
-      PhysArgs pt = pp;
+      PhysArgs pt{};
       pt.U = cb(w.Ut, w.usz);
       pt.P = mbd(w.Pt, w.psz);
+      pt.pslot = noslot();
+      pt.nfields = 6;
       pt.ninst = nt;
+      pt.status = w.status;
       pt.sdiv = w.ntan;
-      pt.cflmax = nullptr;
-      pt.cfl_check = 0;
+      pt.skip_blocked = 1;
       LK(launch_phys_inverse(g, pt, st));
+      if (k == 0 && w.Pv)
+        LK(launch_cache_velocity(g, w.Pt, w.psz, w.ntan, w.couple, w.Pv, w.vstride, w.vslot, w.step, 0, w.status,
+                                 w.nseg, st));
       ProdArgs ap{};
-      ap.Pp = cbd(w.Pp, w.psz);
+      ap.Pp = Pprim;
       ap.pdiv = w.ntan;
+      ap.pslot = pslot;
       ap.Pt = cbd(w.Pt, w.psz);
       ap.H = mb(w.Ut, w.usz);
       ap.ninst = nt;
@@ -298,8 +389,9 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     }
     if (o.adv_primal) {
       ProdArgs ap{};
-      ap.Pp = cbd(w.Pp, w.psz);
+      ap.Pp = Pprim;
       ap.pdiv = 1;
+      ap.pslot = pslot;
       ap.Pt = cbd(nullptr, 0);
       ap.H = mb(w.Up, w.usz);
       ap.ninst = w.nseg;
@@ -333,7 +425,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
       sa.Hprev = cb(nullptr, 0);
       sa.Cc = mb(w.Cp, w.csz);
       sa.Sout = mb(w.Sp, w.csz);
-      sa.T = mb(w.MC, w.traj);
+      sa.T = o.store ? mb(w.MC, w.traj) : mb(nullptr, 0);
       sa.tdiv = 1;
       sa.tsel = 0;
       sa.slot = SlotRef{w.step, 3, k + 1 - 3 * o.ru, (long long)w.csz};  // MC[3(n - ru) + k + 1]
@@ -374,73 +466,113 @@ static bool enqueue_spec2phys(Engine& e, Work& w, Batch<const cpx> C, SlotRef sl
   return true;
 }
 
-// adjoint coupling to the stored tangent at i_step = *step + add
-// (channel/channel.c:624-631 and 682-689 with ddt_project, channel.c:704-780)
-static bool enqueue_coupling(Engine& e, Work& w, int add, double coef) {
+// Adjoint coupling to the stored tangent at i_step = *step + add
+// (channel/channel.c:624-631 and 682-689 with ddt_project, channel.c:704-780):
+// IC' = ddt_project(i_step, MIC[3 i_step]) into w.icp, then AC -= coef * IC'
+// (coef == 0: projection only).  With `cached` the inner products read the
+// primal and velocity caches instead of transforming dCdt and MIC[3 i_step].
+static bool enqueue_coupling(Engine& e, Work& w, int add, double coef, bool cached) {
   const Grid& g = e.T.g;
   DdtArgs d{w.MC, w.traj, w.step, add, w.nseg};
   LK(launch_ddt_diff(g, d, w.dC, e.st));
-  if (!enqueue_spec2phys(e, w, cb(w.dC, w.csz), noslot(), w.Uprev, w.Pprev, w.nseg)) return false;
   const SlotRef icslot{w.step, 3, 3 * add, (long long)w.csz};
-  if (!enqueue_spec2phys(e, w, cb(w.MIC, w.traj), icslot, w.Ul, w.Pl, w.nseg)) return false;
-  LK(launch_ddt_dots(g, cbd(w.Pprev, w.psz), cbd(w.Pl, w.psz), w.part, Work::kDotBlocks, w.nseg, e.st));
-  LK(launch_ddt_apply(g, w.part, Work::kDotBlocks, w.nseg, cb(w.MIC, w.traj), icslot, mb(nullptr, 0),
-                      cb(w.dC, w.csz), w.r, mb(w.Ca, w.csz), coef, e.st));
+  if (cached) {
+    LK(launch_ddt_dots_cached(g, d, w.Pc, w.cstride, w.psz, w.Pv, w.vstride, w.vslot, w.part, Work::kDotBlocks,
+                              e.st));
+  } else {
+    if (!enqueue_spec2phys(e, w, cb(w.dC, w.csz), noslot(), w.Uprev, w.Pprev, w.nseg)) return false;
+    if (!enqueue_spec2phys(e, w, cb(w.MIC, w.traj), icslot, w.Ul, w.Pl, w.nseg)) return false;
+    LK(launch_ddt_dots(g, cbd(w.Pprev, w.psz), cbd(w.Pl, w.psz), w.part, Work::kDotBlocks, w.nseg, e.st));
+  }
+  LK(launch_ddt_apply(g, w.part, Work::kDotBlocks, w.nseg, cb(w.MIC, w.traj), icslot, mb(w.icp, w.csz),
+                      cb(w.dC, w.csz), w.r, coef != 0.0 ? mb(w.Ca, w.csz) : mb(nullptr, 0), coef, e.st));
   return true;
 }
 
-static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt) {
+// One adjoint step n = *step.  The reference couples to step n at the start
+// and to step n - 1 at the end of every step, so each interior projection is
+// applied twice with nothing in between; it is computed once, at the end of
+// step n + 1 (or before the first step), and carried in w.icp.
+static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool cached, bool cpl_cached) {
   const Grid& g = e.T.g;
   cudaStream_t st = e.st;
   const double coef = 0.5 * strength_dt;
-  if (strength_dt != 0.0 && !enqueue_coupling(e, w, 0, coef)) return false;
+  if (strength_dt != 0.0) LK(launch_sub_scaled(g, cb(w.icp, w.csz), mb(w.Ca, w.csz), coef, w.nseg, st));
+  // Without the cache the primal fields of substage k's previous state are the
+  // current state of substage k + 1, so they are computed once: buffers A/B
+  // alternate (cur: A, B, A; prev: B, A).
+  double* PA = w.Pp;
+  double* PB = w.Pprev;
   for (int k = 0; k < 3; ++k) {
-    // primal at the current substage: MC[3n - k - 1]; previous: MC[3n - k - 2]
-    ReconArgs r{};
-    r.ninst = w.nseg;
-    r.status = nullptr;
-    r.sdiv = 1;
-    r.C = cb(w.MC, w.traj);
-    r.slot = SlotRef{w.step, 3, -k - 1, (long long)w.csz};
-    r.U = mb(w.Up, w.usz);
-    LK(launch_recon(g, r, st));
-    if (k < 2) {
-      r.slot = SlotRef{w.step, 3, -k - 2, (long long)w.csz};
-      r.U = mb(w.Uprev, w.usz);
-      LK(launch_recon(g, r, st));
+    Batch<const double> Pcur, Pprv;
+    SlotRef scur = noslot(), sprv = noslot();
+    if (cached) {
+      Pcur = Pprv = cbd(w.Pc, w.cstride);
+      scur = SlotRef{w.step, 3, -k - 1, (long long)w.psz};  // MC[3n - k - 1]
+      sprv = SlotRef{w.step, 3, -k - 2, (long long)w.psz};  // MC[3n - k - 2]
+    } else {
+      double* cur = (k == 1) ? PB : PA;
+      double* prv = (k == 1) ? PA : PB;
+      Pcur = cbd(cur, w.psz);
+      Pprv = cbd(prv, w.psz);
+      ReconArgs r{};
+      r.ninst = w.nseg;
+      r.status = nullptr;
+      r.sdiv = 1;
+      r.C = cb(w.MC, w.traj);
+      PhysArgs p{};
+      p.nfields = 6;
+      p.ninst = w.nseg;
+      p.status = nullptr;
+      p.sdiv = 1;
+      p.pslot = noslot();
+      if (k == 0) {
+        r.slot = SlotRef{w.step, 3, -1, (long long)w.csz};
+        r.U = mb(w.Up, w.usz);
+        LK(launch_recon(g, r, st));
+        p.U = cb(w.Up, w.usz);
+        p.P = mbd(cur, w.psz);
+        LK(launch_phys_inverse(g, p, st));
+      }
+      if (k < 2) {
+        r.slot = SlotRef{w.step, 3, -k - 2, (long long)w.csz};
+        r.U = mb(w.Uprev, w.usz);
+        LK(launch_recon(g, r, st));
+        p.U = cb(w.Uprev, w.usz);
+        p.P = mbd(prv, w.psz);
+        LK(launch_phys_inverse(g, p, st));
+      }
     }
-    r.C = cb(w.Sa, w.csz);
-    r.slot = noslot();
-    r.U = mb(w.Ul, w.usz);
-    LK(launch_recon(g, r, st));
-    PhysArgs p{};
-    p.nfields = 6;
-    p.ninst = w.nseg;
-    p.status = nullptr;
-    p.sdiv = 1;
-    p.U = cb(w.Up, w.usz);
-    p.P = mbd(w.Pp, w.psz);
-    LK(launch_phys_inverse(g, p, st));
-    if (k < 2) {
-      p.U = cb(w.Uprev, w.usz);
-      p.P = mbd(w.Pprev, w.psz);
-      LK(launch_phys_inverse(g, p, st));
-    }
-    p.nfields = 3;
-    p.U = cb(w.Ul, w.usz);
-    p.P = mbd(w.Pl, w.psz);
-    LK(launch_phys_inverse(g, p, st));
+    ReconArgs rl{};
+    rl.ninst = w.nseg;
+    rl.status = nullptr;
+    rl.sdiv = 1;
+    rl.C = cb(w.Sa, w.csz);
+    rl.slot = noslot();
+    rl.U = mb(w.Ul, w.usz);
+    LK(launch_recon(g, rl, st));
+    PhysArgs pl{};
+    pl.nfields = 3;
+    pl.ninst = w.nseg;
+    pl.status = nullptr;
+    pl.sdiv = 1;
+    pl.pslot = noslot();
+    pl.U = cb(w.Ul, w.usz);
+    pl.P = mbd(w.Pl, w.psz);
+    LK(launch_phys_inverse(g, pl, st));
     ProdArgs a{};
     a.pdiv = 1;
     a.ninst = w.nseg;
     a.status = nullptr;
     a.sdiv = 1;
-    a.Pp = cbd(w.Pp, w.psz);
     a.Pt = cbd(w.Pl, w.psz);
+    a.Pp = Pcur;
+    a.pslot = scur;
     a.H = mb(w.Up, w.usz);
     LK(launch_products_adj(g, a, st));
     if (k < 2) {
-      a.Pp = cbd(w.Pprev, w.psz);
+      a.Pp = Pprv;
+      a.pslot = sprv;
       a.H = mb(w.Uprev, w.usz);
       LK(launch_products_adj(g, a, st));
     }
@@ -462,7 +594,7 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt) {
     s.sdiv = 1;
     LK(launch_solve(g, s, st));
   }
-  if (strength_dt != 0.0 && !enqueue_coupling(e, w, -1, coef)) return false;
+  if (strength_dt != 0.0 && !enqueue_coupling(e, w, -1, coef, cpl_cached)) return false;
   LK(launch_step_advance(w.step, -1, st));
   return true;
 }
@@ -568,15 +700,50 @@ static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
   CK(cudaMemcpy2DAsync(w.MC, w.traj * sizeof(cpx), w.Cp, csz * sizeof(cpx), csz * sizeof(cpx), w.nseg,
                        cudaMemcpyDeviceToDevice, e.st));
   if (!reset_status(e, w) || !set_step(e, w, 0)) return false;
-  FwdOpts o{true, false, ru, 0u, false};
-  int todo = w.nsteps + ru;
-  if (!C && todo > 0) {
-    FwdOpts first = o;
-    first.raw_u_first = true;
-    if (!enqueue_forward_step(e, w, first)) return false;
-    --todo;
+  w.mark(0, 3 * w.nsteps, false);
+  w.raw_start = !C && ru == 0;
+  // run-up steps are not stored, so their fields are not cached
+  FwdOpts o{true, false, ru, 0u, false, false};
+  int n = 0;
+  auto run_range = [&](int n1, bool cache) -> bool {
+    FwdOpts oo = o;
+    oo.cache = cache;
+    if (n == 0 && !C && n < n1) {
+      FwdOpts first = oo;
+      first.raw_u_first = true;
+      if (!enqueue_forward_step(e, w, first)) return false;
+      ++n;
+    }
+    const int cnt = n1 - n;
+    n = n1;
+    return run_steps(e, cnt, [&] { return enqueue_forward_step(e, w, oo); });
+  };
+  if (!run_range(ru, false) || !run_range(ru + w.nsteps, true)) return false;
+  if (!C && ru == 0 && w.Pc && w.nsteps > 0) {
+    // cache slot 0 holds the fields of the raw laminar samples that the first
+    // substage ran on; the tangent and adjoint sweeps rebuild MC[0] instead
+    // (channel/channel.c:496-514), so slot 0 gets the fields of MC[0]
+    ReconArgs r{};
+    r.C = cb(w.MC, w.traj);
+    r.slot = noslot();
+    r.U = mb(w.Up, w.usz);
+    r.ninst = w.nseg;
+    r.status = nullptr;
+    r.sdiv = 1;
+    LK(launch_recon(e.T.g, r, e.st));
+    PhysArgs p{};
+    p.U = cb(w.Up, w.usz);
+    p.P = mbd(w.Pc, w.cstride);
+    p.pslot = noslot();
+    p.nfields = 6;
+    p.ninst = w.nseg;
+    p.status = nullptr;
+    p.sdiv = 1;
+    LK(launch_phys_inverse(e.T.g, p, e.st));
   }
-  return run_steps(e, todo, [&] { return enqueue_forward_step(e, w, o); });
+  if (!collect_status(e, w)) return false;
+  w.mark(0, 3 * w.nsteps, w.Pc != nullptr && (g_status & ST_CFL) == 0);
+  return true;
 }
 
 // tangents (and optionally the primal) from start to end; IC device [nseg*ntan]
@@ -604,9 +771,35 @@ static bool op_forward(Engine& e, Work& w, int start, int end, const cpx* C, con
                          (size_t)w.ntan * csz * sizeof(cpx), csz * sizeof(cpx), w.nseg, cudaMemcpyDeviceToDevice,
                          e.st));
   }
+  // The reference's tangent re-advances the primal from MC[3 start] rebuilt
+  // into velocity (channel/channel.c:496-514, 557-571).  That reproduces the
+  // stored trajectory except after a laminar start without run-up, whose
+  // first substage ran on the raw samples: then the primal is re-advanced
+  // here too, without storing it.
+  const bool readvance = !adv_primal && w.raw_start && start == 0;
+  if (readvance) {
+    CK(cudaMemcpy2DAsync(w.Cp, csz * sizeof(cpx), w.MC, w.traj * sizeof(cpx), csz * sizeof(cpx), w.nseg,
+                         cudaMemcpyDeviceToDevice, e.st));
+    CK(cudaMemcpyAsync(w.Sp, w.Cp, sizeof(cpx) * csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
+  }
   if (!reset_status(e, w) || !set_step(e, w, start)) return false;
-  FwdOpts o{adv_primal, w.ntan > 0, 0, forced_mask, false};
-  return run_steps(e, end - start, [&] { return enqueue_forward_step(e, w, o); });
+  const bool cache = adv_primal ? true : (!readvance && w.cached(3 * start, 3 * end));
+  if (adv_primal) w.mark(3 * start, 3 * end + 1, false);
+  FwdOpts o{adv_primal || readvance, w.ntan > 0, 0, forced_mask, false, cache && !readvance, !readvance};
+  if (!run_steps(e, end - start, [&] { return enqueue_forward_step(e, w, o); })) return false;
+  const bool with_vel = w.ntan > 0 && w.Pv != nullptr;
+  if (adv_primal || with_vel) {
+    if (!collect_status(e, w)) return false;
+  }
+  const bool clean = (g_status & ST_CFL) == 0;
+  // the fused sweep rewrote MC[3 start + 1 .. 3 end] and cache slots [3 start, 3 end)
+  if (adv_primal) w.mark(3 * start, 3 * end, w.Pc != nullptr && clean);
+  if (w.ntan > 0) {
+    // MIC[3 start .. 3 end] were rewritten and velocity slots [start, end) with them
+    w.mark_vel(start, end, with_vel && clean);
+    w.mark_vel(end, end + 1, false);
+  }
+  return true;
 }
 
 static bool op_adjoint(Engine& e, Work& w, int start, int end, const cpx* AC, double strength) {
@@ -614,7 +807,11 @@ static bool op_adjoint(Engine& e, Work& w, int start, int end, const cpx* AC, do
   CK(cudaMemcpyAsync(w.Sa, AC, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
   if (!reset_status(e, w) || !set_step(e, w, start)) return false;
   const double sdt = strength * e.T.g.dt;  // channel/channel.c:619
-  return run_steps(e, start - end, [&] { return enqueue_adjoint_step(e, w, sdt); });
+  const bool cached = w.cached(3 * end, 3 * start);
+  bool cpl_cached = true;
+  for (int i = end; i < start; ++i) cpl_cached = cpl_cached && w.coupling_cached(i);
+  if (sdt != 0.0 && start > end && !enqueue_coupling(e, w, 0, 0.0, w.coupling_cached(start))) return false;
+  return run_steps(e, start - end, [&] { return enqueue_adjoint_step(e, w, sdt, cached, cpl_cached); });
 }
 
 // ---------------------------------------------------------------------------

@@ -26,7 +26,8 @@ struct ReconArgs {
 
 struct PhysArgs {
   Batch<const cpx> U;
-  Batch<double> P;      // [inst] -> P[nf][Q][pz][px]
+  Batch<double> P;      // [inst] -> P[nf][Q][pz][px] (plus a slot offset when pslot.stride != 0)
+  SlotRef pslot;
   int nfields;          // 3: u, v, w;  6: plus wz, wx, wy
   int ninst;
   uint32_t* status;     // per-segment status word (instance i -> status[i / sdiv])
@@ -38,7 +39,8 @@ struct PhysArgs {
 
 struct ProdArgs {
   Batch<const double> Pp;  // primal physical fields, instance i -> Pp.base + (i / pdiv) * Pp.stride
-  int pdiv;
+  int pdiv;                //   (plus a slot offset when pslot.stride != 0)
+  SlotRef pslot;
   Batch<const double> Pt;  // tangent fields (forward) / lambda (adjoint); base == nullptr: primal H
   Batch<cpx> H;            // [inst] -> H[Nz][5][Q][X]
   int ninst;
@@ -104,6 +106,19 @@ cudaError_t launch_ddt_dots(const Grid& g, Batch<const double> Pa, Batch<const d
 cudaError_t launch_ddt_apply(const Grid& g, const double* part, int nblk, int nseg, Batch<const cpx> ICsrc,
                              SlotRef icslot, Batch<cpx> ICdst, Batch<const cpx> dC, double* r_out,
                              Batch<cpx> AC, double coef, cudaStream_t st);
+// the same partial sums from field caches: dCdt's fields from primal cache
+// slots i+ and i- ([seg][slot][6][Q][pz][px]), the tangent's from velocity
+// cache slot i ([seg][step][3][Q][pz][px])
+cudaError_t launch_ddt_dots_cached(const Grid& g, const DdtArgs& d, const double* Pc, long long cstride,
+                                   long long psz, const double* Pv, long long vstride, long long vslot,
+                                   double* part, int nblk, cudaStream_t st);
+// velocity cache slot (*step + add) of segment s <- fields 0..2 of P instance s * div + sel
+cudaError_t launch_cache_velocity(const Grid& g, const double* P, long long pstride, int div, int sel, double* Pv,
+                                  long long vstride, long long vslot, const int* step, int add,
+                                  const uint32_t* status, int nseg, cudaStream_t st);
+// AC[s] -= coef * src[s]
+cudaError_t launch_sub_scaled(const Grid& g, Batch<const cpx> src, Batch<cpx> ac, double coef, int nseg,
+                              cudaStream_t st);
 cudaError_t launch_project_init(const Grid& g, const cpx* Uinit, cpx* C, const double* luQs,
                                 const double* luRs, cudaStream_t st);
 cudaError_t launch_step_advance(int* ctr, int delta, cudaStream_t st);

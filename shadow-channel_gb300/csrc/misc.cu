@@ -83,6 +83,99 @@ cudaError_t launch_ddt_dots(const Grid& g, Batch<const double> Pa, Batch<const d
   return cudaGetLastError();
 }
 
+// The same partial sums with both fields taken from physical-field caches:
+// dudt = (P(MC[i+]) - P(MC[i-])) / dt from the primal cache (the transform is
+// linear, so this is spec2phys of the finite difference), v from the cache of
+// the coupled tangent's fields at stage 0 of step i (spec2phys(MIC[3i])).
+__global__ void k_ddt_dots_cached(Grid g, DdtArgs d, const double* __restrict__ Pc, long long cstride,
+                                  long long psz, const double* __restrict__ Pv, long long vstride,
+                                  long long vslot, double* __restrict__ part) {
+  const int s = blockIdx.y;
+  const int i_step = d.step_ptr ? *d.step_ptr + d.step_add : d.step_add;
+  const int ip = i_step == 0 ? 3 : 3 * i_step;
+  const int im = i_step == 0 ? 0 : 3 * (i_step - 1);
+  const double* A = Pc + (long long)s * cstride + (long long)ip * psz;
+  const double* B = Pc + (long long)s * cstride + (long long)im * psz;
+  const double* V = Pv + (long long)s * vstride + (long long)i_step * vslot;
+  const size_t plane = (size_t)g.pz * g.px;
+  const size_t n = (size_t)3 * g.Q * plane;
+  const double rdt = 1.0 / g.dt;
+  double num = 0.0, den = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)((i / plane) % g.Q);
+    const double a = rdt * (A[i] - B[i]), w = g.W[y];
+    num = fma(a * V[i], w, num);
+    den = fma(a * a, w, den);
+  }
+  __shared__ double sn[256], sd[256];
+  sn[threadIdx.x] = num;
+  sd[threadIdx.x] = den;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) {
+      sn[threadIdx.x] += sn[threadIdx.x + k];
+      sd[threadIdx.x] += sd[threadIdx.x + k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[((size_t)s * gridDim.x + blockIdx.x) * 2] = sn[0];
+    part[((size_t)s * gridDim.x + blockIdx.x) * 2 + 1] = sd[0];
+  }
+}
+
+cudaError_t launch_ddt_dots_cached(const Grid& g, const DdtArgs& d, const double* Pc, long long cstride,
+                                   long long psz, const double* Pv, long long vstride, long long vslot,
+                                   double* part, int nblk, cudaStream_t st) {
+  k_ddt_dots_cached<<<dim3(nblk, d.nseg), 256, 0, st>>>(g, d, Pc, cstride, psz, Pv, vstride, vslot, part);
+  return cudaGetLastError();
+}
+
+// copy the first 3 physical fields (u, v, w) of instance (s * div + sel) of P
+// into slot (*step + add) of segment s of a field cache
+// (skipped for a segment whose time loop has stopped, like the solve that
+// would have stored the matching trajectory slot)
+__global__ void k_cache_velocity(size_t n, const double* __restrict__ P, long long pstride, int div, int sel,
+                                 double* __restrict__ Pv, long long vstride, long long vslot, const int* step,
+                                 int add, const uint32_t* __restrict__ status) {
+  const int s = blockIdx.y;
+  if (status && (status[s] & ST_CFL)) return;
+  const double* src = P + (long long)(s * div + sel) * pstride;
+  double* dst = Pv + (long long)s * vstride + (long long)(*step + add) * vslot;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+cudaError_t launch_cache_velocity(const Grid& g, const double* P, long long pstride, int div, int sel, double* Pv,
+                                  long long vstride, long long vslot, const int* step, int add,
+                                  const uint32_t* status, int nseg, cudaStream_t st) {
+  const size_t n = (size_t)3 * g.Q * plane_size(g);
+  k_cache_velocity<<<dim3(256, nseg), 256, 0, st>>>(n, P, pstride, div, sel, Pv, vstride, vslot, step, add,
+                                                     status);
+  return cudaGetLastError();
+}
+
+// AC -= coef * IC' for an IC' projected earlier (the same update as k_ddt_apply)
+__global__ void k_sub_scaled(size_t n, const cpx* __restrict__ src, long long sstride, cpx* __restrict__ ac,
+                             long long astride, double coef) {
+  const int s = blockIdx.y;
+  const cpx* v_ = src + (long long)s * sstride;
+  cpx* a_ = ac + (long long)s * astride;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const cpx v = v_[i];
+    a_[i].re -= coef * v.re;
+    a_[i].im -= coef * v.im;
+  }
+}
+
+cudaError_t launch_sub_scaled(const Grid& g, Batch<const cpx> src, Batch<cpx> ac, double coef, int nseg,
+                              cudaStream_t st) {
+  const size_t n = coef_size(g);
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  k_sub_scaled<<<dim3(nb < 512 ? nb : 512, nseg), 256, 0, st>>>(n, src.base, src.stride, ac.base, ac.stride, coef);
+  return cudaGetLastError();
+}
+
 // IC' = IC - (num/den) dCdt (channel/channel.c:769-772), then the adjoint's
 // AC -= 0.5*strength*dt*IC' (channel/channel.c:628-631, 686-689)
 __global__ void k_ddt_apply(size_t n, const double* __restrict__ part, int nblk, Batch<const cpx> ICsrc,

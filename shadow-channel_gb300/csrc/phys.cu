@@ -97,6 +97,7 @@ __global__ void __launch_bounds__(kThreads) k_phys_inverse(Grid g, PhysArgs a) {
   load_tw(g, s);
   const cpx* __restrict__ U = a.U.at(inst);
   double* __restrict__ P = a.P.at(inst);
+  if (a.pslot.stride) P += (long long)a.pslot.slot() * a.pslot.stride;
   const FftPlan pz_plan = make_plan(g.pz, true);
   const FftPlan px_plan = make_plan(g.px, true);
   const int npair = (g.pz + 1) / 2;
@@ -221,7 +222,8 @@ __global__ void __launch_bounds__(kThreads) k_products_fwd(Grid g, ProdArgs a) {
   PhysSmem s = carve(g, smem, false);
   load_tw(g, s);
   const size_t plane = (size_t)g.pz * g.px, fs = (size_t)g.Q * plane;
-  const double* __restrict__ Pp = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane;
+  const double* __restrict__ Pp = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane +
+                                  (a.pslot.stride ? (long long)a.pslot.slot() * a.pslot.stride : 0LL);
   const double* __restrict__ Pt = a.Pt.base ? a.Pt.at(inst) + (size_t)y * plane : nullptr;
   cpx* __restrict__ H = a.H.at(inst);
   const FftPlan pxF = make_plan(g.px, false);
@@ -261,7 +263,8 @@ __global__ void __launch_bounds__(kThreads) k_products_adj(Grid g, ProdArgs a) {
   cpx* keep = reinterpret_cast<cpx*>(smem + phys_smem_hd(g, false));  // [6][Nz][X]
   load_tw(g, s);
   const size_t plane = (size_t)g.pz * g.px, fs = (size_t)g.Q * plane;
-  const double* __restrict__ P = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane;
+  const double* __restrict__ P = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane +
+                                 (a.pslot.stride ? (long long)a.pslot.slot() * a.pslot.stride : 0LL);
   const double* __restrict__ L = a.Pt.at(inst) + (size_t)y * plane;  // lambda: 3 fields
   cpx* __restrict__ H = a.H.at(inst);
   const FftPlan pxF = make_plan(g.px, false);

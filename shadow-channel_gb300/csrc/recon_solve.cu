@@ -200,27 +200,33 @@ __device__ __forceinline__ RKc rk_coeffs(int k, int adjoint) {
 }
 
 struct SolveSmem {
-  cpx* hc;    // [Qh][kTile][6] parity-combined inputs
+  cpx* hc;    // [Qh][kTile][6] parity-combined inputs (live during a quadrature)
+  cpx* ra;    // [R][kTile] alpha right-hand side / solution (aliases hc: live between quadratures)
+  cpx* rb;    // [R][kTile]
   cpx* Fa;    // [D][kTile]
   cpx* Fb;    // [R][kTile]
-  cpx* ra;    // [R][kTile] alpha right-hand side / solution
-  cpx* rb;    // [R][kTile]
   double* m0; // mean-mode scratch
 };
 
+__host__ __device__ inline size_t solve_hc_elems(const Grid& g) {
+  size_t hc = (size_t)g.Qh * kTile * 6, r = 2 * (size_t)g.R * kTile;
+  return hc > r ? hc : r;
+}
+
 size_t solve_smem_bytes(const Grid& g) {
-  size_t n = (size_t)g.Qh * kTile * 6 + (size_t)g.D * kTile + 3 * (size_t)g.R * kTile;
+  size_t n = solve_hc_elems(g) + (size_t)g.D * kTile + (size_t)g.R * kTile;
   return n * sizeof(cpx) + (size_t)8 * g.R * sizeof(double);
 }
 
 __device__ inline SolveSmem carve_solve(const Grid& g, unsigned char* base) {
   SolveSmem s;
   cpx* p = reinterpret_cast<cpx*>(base);
-  s.hc = p; p += (size_t)g.Qh * kTile * 6;
+  s.hc = p;
+  s.ra = p;
+  s.rb = p + (size_t)g.R * kTile;
+  p += solve_hc_elems(g);
   s.Fa = p; p += (size_t)g.D * kTile;
   s.Fb = p; p += (size_t)g.R * kTile;
-  s.ra = p; p += (size_t)g.R * kTile;
-  s.rb = p; p += (size_t)g.R * kTile;
   s.m0 = reinterpret_cast<double*>(p);
   return s;
 }
@@ -288,7 +294,7 @@ __device__ void quad_rhs(const Grid& g, const cpx* __restrict__ H, int z, int x0
       const double k2 = g.K2[z * g.X + x];
       const int N = phase == 0 ? g.D : g.R;
       // rows i = grp, grp + ngrp, ... share the parity of grp (ngrp is even)
-      constexpr int MAXR = 8;
+      constexpr int MAXR = 4;
       for (int ib = grp; ib < N; ib += ngrp * MAXR) {
         double sr[MAXR][3], si[MAXR][3];
 #pragma unroll
@@ -391,7 +397,7 @@ __device__ void band_solve_chain(const double* __restrict__ LU, int w, int dl, i
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_solve(Grid g, SolveArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
   const int ntx = (g.X + kTile - 1) / kTile;
   const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
   const int inst = blockIdx.y;

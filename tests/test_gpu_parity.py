@@ -220,3 +220,38 @@ def test_dot_product_terms_match_reference(cc):
     lr, rr = sides(ref.tangent, ref.adjoint, ref.spec2phys)
     assert abs(lg - lr) <= 1e-10 * abs(lr)
     assert abs(rg - rr) <= 1e-10 * abs(rr)
+
+
+def test_field_cache_off_matches(cc):
+    """The physical-field caches are an optimisation only: a separate process
+    with CHN_NO_FIELD_CACHE=1 gives the same tangent (bit for bit) and adjoint
+    (the cached coupling forms dC/dt's fields as a difference of transforms
+    instead of the transform of a difference: equal up to rounding)."""
+    import json
+    import os
+    import subprocess
+    import sys
+    code = r"""
+import json, sys, numpy as np
+sys.path.insert(0, 'shadow-channel_gb300'); sys.path.insert(0, 'oracle')
+from channel import c_channel as cc
+from channel.synthetic import synthetic_state
+args = (16, 33, 16, 2 * np.pi, np.pi, 2000.0, 2.0, 0.01, 5)
+assert cc.c_init(*args) == 0
+cc.c_primal(0, synthetic_state(16, 33, 16, seed=0))
+IC = synthetic_state(16, 33, 16, seed=3, laminar=False); cc.c_tangent(0, 5, IC, 1)
+AC = synthetic_state(16, 33, 16, seed=4, laminar=False); cc.c_adjoint(5, 0, AC, 0, 0.5)
+print(json.dumps({"IC": IC.view(np.float64).tolist(), "AC": AC.view(np.float64).tolist()}))
+"""
+    root = O.HERE.parent
+    outs = []
+    for off in ("0", "1"):
+        env = dict(os.environ, CHN_NO_FIELD_CACHE=off)
+        r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        outs.append(json.loads(next(ln for ln in r.stdout.splitlines() if ln.startswith("{"))))
+    a, b = np.array(outs[0]["IC"]), np.array(outs[1]["IC"])
+    assert np.array_equal(a, b)
+    a, b = np.array(outs[0]["AC"]), np.array(outs[1]["AC"])
+    assert np.linalg.norm(a - b) <= 1e-11 * np.linalg.norm(b)   # measured 2.8e-12
