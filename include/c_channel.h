@@ -70,7 +70,8 @@ void c_spec2phys(chn_complex *C_ptr, int Nz_dup, int Nvar_dup, int Ny_dup,
 /* channel.i:178-205 -> channel.c:791/889.  HDF5 is not part of this build;
    these write / read the same datasets (alpha, beta as [dimR][Nz][Nx/2]
    {real, imaginary} records, Nx, Ny, Nz, dt, 1/Re, mpg) in a raw
-   little-endian container described in INTEGRATION.md. */
+   little-endian container: 8 bytes "SCHNRAW1", int32 Nx, Ny, Nz, 0,
+   double dt, 1/Re, mpg, then alpha, beta, ialpha, ibeta. */
 void c_read_solution(char *filename, chn_complex *C_ptr, int Nz_dup,
                      int Nvar_dup, int Ny_dup, int Nx_dup);
 void c_save_solution(char *filename, chn_complex *C_ptr, int Nz_dup,
@@ -101,6 +102,9 @@ double c_last_cfl(void);
    with ntan tangents; the adjoint couples (strength != 0) to the stored
    trajectory of tangent `couple`.  Host arrays, segment-major. */
 int c_batch_init(int nseg, int ntan, int couple);
+/* the same with a trajectory length of the batch's own (<= any length; the
+   reference's nsteps of c_init is not used by the batch) */
+int c_batch_init_steps(int nseg, int ntan, int couple, int nsteps);
 int c_batch_destroy(void);
 /* primal trajectories for all segments; C [nseg][Nz][2][dimR][Nx/2] in/out */
 int c_batch_primal(int ru_steps, chn_complex *C);
@@ -117,6 +121,18 @@ int c_batch_adjoint(int start_step, int end_step, chn_complex *AC,
 /* MC / MIC of one segment at step i_step into out [Nz][2][dimR][Nx/2] */
 int c_batch_getsoln(int seg, int i_step, chn_complex *out);
 int c_batch_getincresoln(int seg, int i_step, chn_complex *out);
+
+/* Segments as consecutive windows of one trajectory, each window_steps long
+   (LSS time segments, drivers/wrapper.py): ddt_project at a window start
+   takes dC/dt across the boundary from the previous segment, as the
+   reference does on its single global trajectory (channel/channel.c:729-740).
+   0 turns it off. */
+int c_batch_set_chain(int window_steps);
+/* ddt_project (channel.i:96-105 -> channel/channel.c:704-780) of one vector
+   per segment at the segment's step i_step, in place; r[nseg] receives the
+   projection coefficients (nullable).  Host arrays / device arrays. */
+int c_batch_ddt_project(int i_step, chn_complex *V, double *r);
+int c_batch_ddt_project_dev(int i_step, chn_complex *V, double *r);
 
 /* The same batched calls on device-resident arrays (CUDA device pointers,
    same layouts); no host copies.  stream 0 = the library's stream. */
@@ -158,6 +174,20 @@ double c_fp64_peak_tflops(void);
    scratch, so calls that overlap on the GPU race.  Returns 0 or a negative
    error (c_last_error_message). */
 int c_spec2phys_noalloc(const chn_complex *C_dev, double *flow_dev);
+
+/* Least-squares shadowing on the device (no reference C counterpart: the
+   reference does this in Python, drivers/wrapper.py:5-54 and
+   drivers/pariter.py:63-125).  Needs a chained batch with ntan = 1.
+   x, y: device arrays of 2*nseg - 1 coefficient arrays [v_0..v_{n-1},
+   w_0..w_{n-2}]; y = KKT x (the reference's Wrapper.matvec); zeta[nseg]
+   (device, nullable) = minus the window-end projection coefficients. */
+int c_lss_matvec_dev(const chn_complex *x, chn_complex *y, int inhomo, double *zeta);
+/* Euclidean dot product of two device arrays of n doubles (deterministic) */
+int c_lss_dot_dev(long long n, const double *a, const double *b, double *out);
+/* MINRES (pariter.par_minres) for KKT x = b from the x given; returns 0 when
+   |eta|/|b - A x0| < tol, 1 after maxiter iterations, < 0 on error */
+int c_lss_minres_dev(const chn_complex *b, chn_complex *x, double tol, int maxiter, int *iters,
+                     double *rel_residual);
 
 /* The time-invariant setup tables on the host (no GPU needed): which =
    0 Q, 1 Q', 2 Q'', 3 R, 4 R' (values at the quadrature points, [qpts][n]),

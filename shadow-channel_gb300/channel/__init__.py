@@ -36,7 +36,7 @@ def quad():
 
 def save_solution(filename, C):
     """Save the solution C (and the last tangent) to ``filename`` (raw
-    container).  Must be called after init()."""
+    container "SCHNRAW1", not HDF5).  Must be called after init()."""
     if not filename.endswith('.hd5'):
         filename += '.hd5'
     assert C.shape == _shape()

@@ -107,6 +107,21 @@ _lib.c_batch_kernel_ms.restype = _d
 _lib.c_spec2phys_noalloc.argtypes = [_vp, _vp]
 _lib.c_spec2phys_noalloc.restype = _i
 
+_lib.c_batch_init_steps.argtypes = [_i, _i, _i, _i]
+_lib.c_batch_init_steps.restype = _i
+_lib.c_batch_set_chain.argtypes = [_i]
+_lib.c_batch_set_chain.restype = _i
+_lib.c_batch_ddt_project.argtypes = [_i, _vp, _vp]
+_lib.c_batch_ddt_project.restype = _i
+_lib.c_batch_ddt_project_dev.argtypes = [_i, _vp, _vp]
+_lib.c_batch_ddt_project_dev.restype = _i
+_lib.c_lss_matvec_dev.argtypes = [_vp, _vp, _i, _vp]
+_lib.c_lss_matvec_dev.restype = _i
+_lib.c_lss_dot_dev.argtypes = [ctypes.c_longlong, _vp, _vp, _vp]
+_lib.c_lss_dot_dev.restype = _i
+_lib.c_lss_minres_dev.argtypes = [_vp, _vp, _d, _i, _ip, ctypes.POINTER(_d)]
+_lib.c_lss_minres_dev.restype = _i
+
 LIBRARY_PATH = str(_LIBPATH)
 lib = _lib
 

@@ -180,6 +180,7 @@ struct Work {
   std::vector<char> vel_ok;    // slot i of Pv holds the fields of MIC[3i]
   cpx* icp = nullptr;          // projected IC' of the last coupling, per segment
   bool raw_start = false;      // MC came from a laminar start without run-up
+  int chain = 0;               // > 0: segments are consecutive windows of one trajectory (DdtArgs::chain)
   std::vector<void*> ptrs;
   void mark(int c0, int c1, bool ok) {
     for (int c = c0; c < c1 && c < (int)slot_ok.size(); ++c)
@@ -195,6 +196,7 @@ struct Work {
   bool coupling_cached(int i) const {
     if (!Pv || i < 0 || i >= (int)vel_ok.size() || !vel_ok[i]) return false;
     const int ip = i == 0 ? 3 : 3 * i, im = i == 0 ? 0 : 3 * (i - 1);
+    if (i == 0 && chain > 0 && !cached(3 * (chain - 1), 3 * (chain - 1) + 1)) return false;
     return cached(ip, ip + 1) && cached(im, im + 1);
   }
   void mark_vel(int i0, int i1, bool ok) {
@@ -473,7 +475,7 @@ static bool enqueue_spec2phys(Engine& e, Work& w, Batch<const cpx> C, SlotRef sl
 // primal and velocity caches instead of transforming dCdt and MIC[3 i_step].
 static bool enqueue_coupling(Engine& e, Work& w, int add, double coef, bool cached) {
   const Grid& g = e.T.g;
-  DdtArgs d{w.MC, w.traj, w.step, add, w.nseg};
+  DdtArgs d{w.MC, w.traj, w.step, add, w.nseg, w.chain};
   LK(launch_ddt_diff(g, d, w.dC, e.st));
   const SlotRef icslot{w.step, 3, 3 * add, (long long)w.csz};
   if (cached) {
@@ -850,7 +852,7 @@ static double ddt_project_single(Engine& e, int i_step, cpx* IC_host) {
   const Grid& g = e.T.g;
   const size_t bytes = sizeof(cpx) * w.csz;
   if (!h2d(e, w.io, IC_host, bytes)) return NAN;
-  DdtArgs d{w.MC, w.traj, nullptr, i_step, 1};
+  DdtArgs d{w.MC, w.traj, nullptr, i_step, 1, 0};
   ++g_launches;
   if (launch_ddt_diff(g, d, w.dC, e.st) != cudaSuccess) return NAN;
   if (!enqueue_spec2phys(e, w, cb(w.dC, w.csz), noslot(), w.Uprev, w.Pprev, 1)) return NAN;
@@ -879,6 +881,31 @@ bool engine_grid_stream(const Grid** g, cudaStream_t* st) {
 }
 void engine_set_error(int code, const char* msg) { set_error(code, "%s", msg); }
 void engine_count_launches(int n) { g_launches += n; }
+// the batch working set's shape (lss.cu)
+bool engine_batch_shape(int* nseg, int* ntan, int* chain, size_t* csz, int* nsteps) {
+  if (!E || !E->have_batch) return false;
+  *nseg = E->batch.nseg;
+  *ntan = E->batch.ntan;
+  *chain = E->batch.chain;
+  *csz = E->batch.csz;
+  *nsteps = E->batch.nsteps;
+  return true;
+}
+int engine_status() { return g_status; }
+
+// ddt_project of one vector per segment against the segment's own stored
+// primal (channel/channel.c:704-780), in place; r[s] = num/den
+static bool batch_ddt_project(Engine& e, Work& w, int i_step, cpx* V, double* r) {
+  const Grid& g = e.T.g;
+  DdtArgs d{w.MC, w.traj, nullptr, i_step, w.nseg, w.chain};
+  LK(launch_ddt_diff(g, d, w.dC, e.st));
+  if (!enqueue_spec2phys(e, w, cb(w.dC, w.csz), noslot(), w.Uprev, w.Pprev, w.nseg)) return false;
+  if (!enqueue_spec2phys(e, w, cb(V, w.csz), noslot(), w.Ul, w.Pl, w.nseg)) return false;
+  LK(launch_ddt_dots(g, cbd(w.Pprev, w.psz), cbd(w.Pl, w.psz), w.part, Work::kDotBlocks, w.nseg, e.st));
+  LK(launch_ddt_apply(g, w.part, Work::kDotBlocks, w.nseg, cb(V, w.csz), noslot(), mb(V, w.csz), cb(w.dC, w.csz),
+                      r ? r : w.r, mb(nullptr, 0), 0.0, e.st));
+  return true;
+}
 
 }  // namespace chn
 
@@ -1131,8 +1158,13 @@ double c_last_cfl(void) { return g_cfl; }
 
 int c_batch_init(int nseg, int ntan, int couple) {
   if (!need_init("c_batch_init")) return -2;
-  if (nseg <= 0 || ntan < 0 || ntan > 32 || (ntan > 0 && (couple < 0 || couple >= ntan))) {
-    set_error(-4, "c_batch_init: need nseg > 0, 0 <= ntan <= 32, 0 <= couple < ntan");
+  return c_batch_init_steps(nseg, ntan, couple, E->nsteps);
+}
+
+int c_batch_init_steps(int nseg, int ntan, int couple, int nsteps) {
+  if (!need_init("c_batch_init_steps")) return -2;
+  if (nseg <= 0 || ntan < 0 || ntan > 32 || (ntan > 0 && (couple < 0 || couple >= ntan)) || nsteps < 0) {
+    set_error(-4, "c_batch_init: need nseg > 0, 0 <= ntan <= 32, 0 <= couple < ntan, nsteps >= 0");
     return -4;
   }
   Engine& e = *E;
@@ -1141,7 +1173,7 @@ int c_batch_init(int nseg, int ntan, int couple) {
     e.batch.release();
     e.have_batch = false;
   }
-  if (!e.batch.create(e.T.g, nseg, ntan, e.nsteps, couple)) {
+  if (!e.batch.create(e.T.g, nseg, ntan, nsteps, couple)) {
     e.batch.release();
     return g_status;
   }
@@ -1186,7 +1218,7 @@ int c_batch_primal_dev(int ru_steps, chn_complex* C) {
 int c_batch_tangent_dev(int start_step, int end_step, chn_complex* IC, const int* inhomo) {
   if (!batch_ready("c_batch_tangent_dev")) return g_status;
   Work& w = E->batch;
-  if (!(end_step > start_step && start_step >= 0 && end_step <= E->nsteps) || w.ntan == 0) {
+  if (!(end_step > start_step && start_step >= 0 && end_step <= E->batch.nsteps) || w.ntan == 0) {
     set_error(-4, "c_batch_tangent: need 0 <= start < end <= nsteps and ntan > 0");
     return -4;
   }
@@ -1200,7 +1232,7 @@ int c_batch_tangent_dev(int start_step, int end_step, chn_complex* IC, const int
 int c_batch_forward_dev(int start_step, int end_step, chn_complex* C, chn_complex* IC, const int* inhomo) {
   if (!batch_ready("c_batch_forward_dev")) return g_status;
   Work& w = E->batch;
-  if (!(end_step > start_step && start_step >= 0 && end_step <= E->nsteps)) {
+  if (!(end_step > start_step && start_step >= 0 && end_step <= E->batch.nsteps)) {
     set_error(-4, "c_batch_forward: need 0 <= start < end <= nsteps");
     return -4;
   }
@@ -1218,7 +1250,7 @@ int c_batch_forward_dev(int start_step, int end_step, chn_complex* C, chn_comple
 int c_batch_adjoint_dev(int start_step, int end_step, chn_complex* AC, double strength) {
   if (!batch_ready("c_batch_adjoint_dev")) return g_status;
   Work& w = E->batch;
-  if (!(end_step < start_step && end_step >= 0 && start_step <= E->nsteps)) {
+  if (!(end_step < start_step && end_step >= 0 && start_step <= E->batch.nsteps)) {
     set_error(-4, "c_batch_adjoint: need 0 <= end < start <= nsteps");
     return -4;
   }
@@ -1274,17 +1306,50 @@ int c_batch_adjoint(int start_step, int end_step, chn_complex* AC, double streng
   return rc;
 }
 
+int c_batch_set_chain(int window_steps) {
+  if (!batch_ready("c_batch_set_chain")) return g_status;
+  if (window_steps < 0 || window_steps > E->batch.nsteps) {
+    set_error(-4, "c_batch_set_chain: need 0 <= window_steps <= nsteps");
+    return -4;
+  }
+  E->batch.chain = window_steps;
+  g_status = 0;
+  return 0;
+}
+
+int c_batch_ddt_project_dev(int i_step, chn_complex* V, double* r) {
+  if (!batch_ready("c_batch_ddt_project_dev")) return g_status;
+  if (i_step < 0 || i_step > E->batch.nsteps || !V) {
+    set_error(-4, "c_batch_ddt_project: need 0 <= i_step <= nsteps and a vector array");
+    return -4;
+  }
+  g_status = 0;
+  return batch_ddt_project(*E, E->batch, i_step, reinterpret_cast<cpx*>(V), r) ? 0 : g_status;
+}
+
+int c_batch_ddt_project(int i_step, chn_complex* V, double* r) {
+  if (!batch_ready("c_batch_ddt_project")) return g_status;
+  Work& w = E->batch;
+  const size_t bytes = sizeof(cpx) * w.csz * w.nseg;
+  if (!V || !h2d(*E, w.io, V, bytes)) return -4;
+  const int rc = c_batch_ddt_project_dev(i_step, reinterpret_cast<chn_complex*>(w.io), nullptr);
+  if (rc != 0) return rc;
+  if (!d2h(*E, V, w.io, bytes)) return -1;
+  if (r && !d2h(*E, r, w.r, sizeof(double) * w.nseg)) return -1;
+  return 0;
+}
+
 int c_batch_getsoln(int seg, int i_step, chn_complex* out) {
   if (!batch_ready("c_batch_getsoln")) return g_status;
   Work& w = E->batch;
-  if (seg < 0 || seg >= w.nseg || i_step < 0 || i_step > E->nsteps) return -4;
+  if (seg < 0 || seg >= w.nseg || i_step < 0 || i_step > E->batch.nsteps) return -4;
   return d2h(*E, out, w.MC + (size_t)seg * w.traj + (size_t)3 * i_step * w.csz, sizeof(cpx) * w.csz) ? 0 : -1;
 }
 
 int c_batch_getincresoln(int seg, int i_step, chn_complex* out) {
   if (!batch_ready("c_batch_getincresoln")) return g_status;
   Work& w = E->batch;
-  if (seg < 0 || seg >= w.nseg || i_step < 0 || i_step > E->nsteps) return -4;
+  if (seg < 0 || seg >= w.nseg || i_step < 0 || i_step > E->batch.nsteps) return -4;
   return d2h(*E, out, w.MIC + (size_t)seg * w.traj + (size_t)3 * i_step * w.csz, sizeof(cpx) * w.csz) ? 0 : -1;
 }
 

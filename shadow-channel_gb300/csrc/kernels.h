@@ -80,6 +80,10 @@ struct DdtArgs {
   const int* step_ptr;      // i_step = *step_ptr + step_add (or step_add when null)
   int step_add;
   int nseg;
+  // > 0: the segments are consecutive windows of one trajectory, each chain
+  // steps long; at i_step 0 segment s > 0 takes its earlier state from
+  // segment s - 1, step chain - 1 (the reference's global step before the window)
+  int chain;
 };
 
 void prepare_kernels(const Grid& g);  // function attributes; call once, outside graph capture

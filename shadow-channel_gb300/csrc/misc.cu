@@ -27,10 +27,11 @@ cudaError_t launch_flow_out(const Grid& g, const double* P, double* flow, cudaSt
 __global__ void k_ddt_diff(size_t n, double rdt, DdtArgs d, cpx* __restrict__ dC) {
   const int s = blockIdx.y;
   const int i_step = d.step_ptr ? *d.step_ptr + d.step_add : d.step_add;
-  const int ip = i_step == 0 ? 3 : 3 * i_step;
-  const int im = i_step == 0 ? 0 : 3 * (i_step - 1);
+  const bool cross = i_step == 0 && d.chain > 0 && s > 0;
+  const int ip = cross ? 0 : (i_step == 0 ? 3 : 3 * i_step);
+  const int im = cross ? 3 * (d.chain - 1) : (i_step == 0 ? 0 : 3 * (i_step - 1));
   const cpx* A = d.MC + (long long)s * d.traj_stride + (long long)ip * n;
-  const cpx* B = d.MC + (long long)s * d.traj_stride + (long long)im * n;
+  const cpx* B = d.MC + (long long)(cross ? s - 1 : s) * d.traj_stride + (long long)im * n;
   cpx* out = dC + (long long)s * n;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     out[i].re = rdt * (A[i].re - B[i].re);
@@ -92,10 +93,11 @@ __global__ void k_ddt_dots_cached(Grid g, DdtArgs d, const double* __restrict__ 
                                   long long vslot, double* __restrict__ part) {
   const int s = blockIdx.y;
   const int i_step = d.step_ptr ? *d.step_ptr + d.step_add : d.step_add;
-  const int ip = i_step == 0 ? 3 : 3 * i_step;
-  const int im = i_step == 0 ? 0 : 3 * (i_step - 1);
+  const bool cross = i_step == 0 && d.chain > 0 && s > 0;
+  const int ip = cross ? 0 : (i_step == 0 ? 3 : 3 * i_step);
+  const int im = cross ? 3 * (d.chain - 1) : (i_step == 0 ? 0 : 3 * (i_step - 1));
   const double* A = Pc + (long long)s * cstride + (long long)ip * psz;
-  const double* B = Pc + (long long)s * cstride + (long long)im * psz;
+  const double* B = Pc + (long long)(cross ? s - 1 : s) * cstride + (long long)im * psz;
   const double* V = Pv + (long long)s * vstride + (long long)i_step * vslot;
   const size_t plane = (size_t)g.pz * g.px;
   const size_t n = (size_t)3 * g.Q * plane;
