@@ -175,6 +175,28 @@ double c_fp64_peak_tflops(void);
    error (c_last_error_message). */
 int c_spec2phys_noalloc(const chn_complex *C_dev, double *flow_dev);
 
+/* Objectives and statistics of the stored trajectories, computed on the
+   device from the coefficients (no reference C counterpart: the reference
+   averages spec2phys output in Python, channel/__init__.py:217-299 and
+   drivers/sensitivities.py).  inc 0: primal MC, 1: tangent MIC; comp 0 u,
+   1 v, 2 w; steps start..end-1.
+   c_mean_profile: x-z mean of the component at each quadrature point,
+     out [end-start][qpts];
+   c_wall_shear: dU/dy and dW/dy of the mean flow at y = -1 (the reference's
+     Uxb, Uzb of channel/project0.c:224-234), out [end-start][2];
+   c_mean_product: x-z mean of comp_a (of inc_a) times comp_b (of inc_b) at
+     each quadrature point, out [end-start][qpts].
+   Batch variants: the same for every segment, out [nseg][end-start][...]. */
+int c_mean_profile(int inc, int comp, int start_step, int end_step, double *out);
+int c_wall_shear(int inc, int start_step, int end_step, double *out);
+int c_mean_product(int inc_a, int comp_a, int inc_b, int comp_b, int start_step,
+                   int end_step, double *out);
+int c_batch_mean_profile(int inc, int comp, int start_step, int end_step, double *out);
+int c_batch_mean_profile_dev(int inc, int comp, int start_step, int end_step, double *out);
+int c_batch_wall_shear_dev(int inc, int start_step, int end_step, double *out);
+int c_batch_mean_product_dev(int inc_a, int comp_a, int inc_b, int comp_b,
+                             int start_step, int end_step, double *out);
+
 /* Least-squares shadowing on the device (no reference C counterpart: the
    reference does this in Python, drivers/wrapper.py:5-54 and
    drivers/pariter.py:63-125).  Needs a chained batch with ntan = 1.

@@ -147,16 +147,36 @@ def vel(i_step):
     return spec2phys(get_solution(i_step, copy=True))[0]
 
 
+def _centre(profile_values):
+    return profile_values[..., c_channel.c_qpts() // 2 + 1]
+
+
 def velAvg(start_step, end_step, T, profile=True):
-    """Time-averaged streamwise velocity profile (or its centreline value)."""
-    uavg = np.zeros(c_channel.c_qpts()) if profile else 0.0
+    """Time-averaged streamwise velocity profile (or its value at quadrature
+    point qpts/2 + 1), channel/__init__.py:217-236.  The x-z average of each
+    step's field is the mean Fourier mode, computed on the device from the
+    stored coefficients (c_mean_profile) instead of spec2phys per step."""
     assert 0 <= start_step <= end_step <= c_channel.c_nsteps()
-    for i in range(start_step, end_step):
-        u = vel(i).mean(2).mean(0)
-        if not profile:
-            u = u[c_channel.c_qpts() // 2 + 1]
-        uavg = uavg + (dt / T) * u
+    uavg = np.zeros(c_channel.c_qpts()) if profile else 0.0
+    if end_step > start_step:
+        prof = c_channel.c_mean_profile(0, 0, start_step, end_step)
+        for u in prof:
+            uavg = uavg + (dt / T) * (u if profile else _centre(u))
     return uavg
+
+
+def wallShear(start_step, end_step):
+    """dU/dy of the mean streamwise flow at the wall y = -1 for each step in
+    start_step..end_step-1 (the reference's Uxb, channel/project0.c:224-234)."""
+    return c_channel.c_wall_shear(0, start_step, end_step)[:, 0].copy()
+
+
+def wallShearAvg(start_step, end_step, T):
+    """Time-averaged wall shear dU/dy(-1) over steps start_step..end_step-1."""
+    tau = 0.0
+    for t in wallShear(start_step, end_step):
+        tau = tau + (dt / T) * t
+    return tau
 
 
 def Ivel(i_step, project=False):
@@ -169,13 +189,14 @@ def Ivel(i_step, project=False):
 
 
 def IvelAvg(start_step, end_step, T, profile=True):
-    vavg = np.zeros(c_channel.c_qpts()) if profile else 0.0
+    """Time-averaged mean tangent streamwise velocity (channel/__init__.py:253-273),
+    from the stored tangent trajectory on the device."""
     assert 0 <= start_step <= end_step <= c_channel.c_nsteps()
-    for i in range(start_step, end_step):
-        v = Ivel(i, project=False).mean(2).mean(0)
-        if not profile:
-            v = v[c_channel.c_qpts() // 2 + 1]
-        vavg = vavg + (dt / T) * v
+    vavg = np.zeros(c_channel.c_qpts()) if profile else 0.0
+    if end_step > start_step:
+        prof = c_channel.c_mean_profile(1, 0, start_step, end_step)
+        for v in prof:
+            vavg = vavg + (dt / T) * (v if profile else _centre(v))
     return vavg
 
 
@@ -187,8 +208,8 @@ def uavgGrad(n_chunk, chunk_bounds, T, uavg, zeta, profile=True):
         start_step = chunk_bounds[i]
         end_step = chunk_bounds[i + 1]
         vavg = IvelAvg(start_step, end_step, T, profile)
-        uEnd = vel(end_step).mean(2).mean(0)
+        uEnd = c_channel.c_mean_profile(0, 0, end_step, end_step + 1)[0]
         if not profile:
-            uEnd = uEnd[c_channel.c_qpts() // 2 + 1]
+            uEnd = _centre(uEnd)
         grad = grad + vavg + (1. / T) * zeta[i] * (uEnd - uavg)
     return grad

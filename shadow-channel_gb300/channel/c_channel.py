@@ -107,6 +107,22 @@ _lib.c_batch_kernel_ms.restype = _d
 _lib.c_spec2phys_noalloc.argtypes = [_vp, _vp]
 _lib.c_spec2phys_noalloc.restype = _i
 
+_lib.c_mean_profile.argtypes = [_i, _i, _i, _i, _vp]
+_lib.c_mean_profile.restype = _i
+_lib.c_wall_shear.argtypes = [_i, _i, _i, _vp]
+_lib.c_wall_shear.restype = _i
+_lib.c_mean_product.argtypes = [_i, _i, _i, _i, _i, _i, _vp]
+_lib.c_mean_product.restype = _i
+_lib.c_batch_mean_profile.argtypes = [_i, _i, _i, _i, _vp]
+_lib.c_batch_mean_profile.restype = _i
+for _n in ("c_batch_mean_profile_dev",):
+    getattr(_lib, _n).argtypes = [_i, _i, _i, _i, _vp]
+    getattr(_lib, _n).restype = _i
+_lib.c_batch_wall_shear_dev.argtypes = [_i, _i, _i, _vp]
+_lib.c_batch_wall_shear_dev.restype = _i
+_lib.c_batch_mean_product_dev.argtypes = [_i, _i, _i, _i, _i, _i, _vp]
+_lib.c_batch_mean_product_dev.restype = _i
+
 _lib.c_batch_init_steps.argtypes = [_i, _i, _i, _i]
 _lib.c_batch_init_steps.restype = _i
 _lib.c_batch_set_chain.argtypes = [_i]
@@ -194,6 +210,34 @@ def c_read_solution(filename, C_ptr):
 def c_save_solution(filename, C_ptr):
     p, s = _inplace4(C_ptr, np.complex128, "c_save_solution")
     _lib.c_save_solution(str(filename).encode(), p, *s)
+
+
+def c_mean_profile(inc, comp, start_step, end_step):
+    """x-z mean of velocity component comp (0 u, 1 v, 2 w) of MC (inc 0) or
+    MIC (inc 1) at steps start..end-1: float64 [end-start, qpts]."""
+    out = np.zeros((end_step - start_step, c_qpts()))
+    _check(_lib.c_mean_profile(int(inc), int(comp), int(start_step), int(end_step), out.ctypes.data))
+    return out
+
+
+def c_wall_shear(inc, start_step, end_step):
+    """dU/dy, dW/dy of the mean flow at y = -1 per step: float64 [end-start, 2]."""
+    out = np.zeros((end_step - start_step, 2))
+    _check(_lib.c_wall_shear(int(inc), int(start_step), int(end_step), out.ctypes.data))
+    return out
+
+
+def c_mean_product(inc_a, comp_a, inc_b, comp_b, start_step, end_step):
+    """x-z mean of the product of two velocity components per step: [end-start, qpts]."""
+    out = np.zeros((end_step - start_step, c_qpts()))
+    _check(_lib.c_mean_product(int(inc_a), int(comp_a), int(inc_b), int(comp_b), int(start_step),
+                               int(end_step), out.ctypes.data))
+    return out
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError(c_last_error_message())
 
 
 def c_quad():

@@ -892,6 +892,17 @@ bool engine_batch_shape(int* nseg, int* ntan, int* chain, size_t* csz, int* nste
   return true;
 }
 int engine_status() { return g_status; }
+// stored trajectories for the statistics (stats.cu): MC (inc 0) or MIC (inc 1)
+// of the single-trajectory working set (batch 0) or of the batch (batch 1)
+bool engine_traj(int batch, int inc, const cpx** base, long long* traj_stride, int* nseg, int* nsteps) {
+  if (!E || (batch && !E->have_batch)) return false;
+  const Work& w = batch ? E->batch : E->single;
+  *base = inc ? w.MIC : w.MC;
+  *traj_stride = w.traj;
+  *nseg = w.nseg;
+  *nsteps = w.nsteps;
+  return true;
+}
 
 // ddt_project of one vector per segment against the segment's own stored
 // primal (channel/channel.c:704-780), in place; r[s] = num/den
