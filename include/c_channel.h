@@ -46,6 +46,16 @@ void c_tangent(int start_step, int end_step, chn_complex *IC_given,
                int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup, int inhomo);
 
 /* channel.i:78-88 -> channel.c:596 adjoint() */
+/* c_tangent with a choice of forcing (no reference entry point; the
+   reference's c_tangent is forcing = inhomo != 0): 0 none, 1 mean flux
+   (meanU sensitivity, channel/increproject0.c:209-214), 2 Re sensitivity
+   with the reference's forcing reconnected (channel/tangent_forcing.c,
+   tangent_forcing0.c, increproject.c:61-104, disconnected at
+   channel/channel.c:521; first order in dt), 3 Re sensitivity, exact
+   derivative of the discrete RK3 step.  The mean flux is held fixed for 2, 3. */
+void c_tangent_forcing(int start_step, int end_step, chn_complex *IC_given,
+                       int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup,
+                       int forcing);
 void c_adjoint(int start_step, int end_step, chn_complex *AC_given,
                int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup, int inhomo,
                double strength);
@@ -109,7 +119,8 @@ int c_batch_destroy(void);
 /* primal trajectories for all segments; C [nseg][Nz][2][dimR][Nx/2] in/out */
 int c_batch_primal(int ru_steps, chn_complex *C);
 /* tangents on stored primal trajectories; IC [nseg][ntan][...] in/out;
-   inhomo[ntan] selects the mean-flux forcing per tangent */
+   inhomo[ntan] selects the forcing per tangent (the values of
+   c_tangent_forcing: 0 none, 1 mean flux, 2 / 3 Re) */
 int c_batch_tangent(int start_step, int end_step, chn_complex *IC,
                     const int *inhomo);
 /* primal and tangents advanced together from C (fused forward sweep) */

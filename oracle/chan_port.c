@@ -62,6 +62,7 @@ struct cport {
     double *Qy, *W, *Q, *Qp, *Qpp, *R, *Rp, *Qw, *Qpw, *Qppw, *Rw, *Rpw;
     double *Qs, *Qps, *Qpps, *Rs, *Rps;
     cpx *C, *IC, *AC, *U, *IU, *AU, *IAU, *LU, *MC, *MIC;
+    double *MFT;   /* primal flux correction flux_t of each stored substage (not in the reference) */
     cpx *CT, *ICT;
     double *M, *MZ;
     cpx *Fa, *Fb, *TM, *fa, *fb, *tm, *add;
@@ -850,6 +851,106 @@ static void rhs_fb(cport *s, const cpx *H, int z, int x0, int adj)
             }
 }
 
+/* Re-sensitivity forcing of the tangent.
+   kind 2, the reference's own forcing reconnected: at substage 0 only,
+     IC += dt * Mass^-1 (F MC[3n+1]) with, per mode,
+     F_alpha = -re^2 (K2^2 Qs + 2 K2 Qps + Qpps), Mass_alpha = -(K2 Qs + Qps)
+     F_beta  =  re^2 (Rps + K2 Rs),               Mass_beta  = Rs
+     (tangent_forcing.c:10-75 and increproject.c:61-104), and for the mean
+     mode F = re^2 Rps, Mass = Rs (tangent_forcing0.c:10-44 with the block
+     kept commented out in increproject0.c:45-90);
+   kind 3, the exact derivative of the discrete step with respect to Re
+     (re = 1/Re, dre/dRe = -re^2): every substage k adds
+     -re^2 dt (a_k D x_k + b_k D x_{k+1}) to the right-hand side, D the
+     viscous operator of the implicit solve and x the primal states MC[3n+k],
+     MC[3n+k+1] (from (M - re b_k dt D) x_{k+1} = (M + re a_k dt D) x_k + ...).
+   The mean flux is held fixed in both (homogeneous flux correction). */
+static void fill_v_visc(cport *s, int z, int x0, double scale)
+{
+    /* M = scale * (K2^2 Qs + 2 K2 Qps + Qpps), rows < dimQ */
+    const int X = s->X, D = s->dimQ;
+    memset(s->M, 0, sizeof(double) * (size_t)s->dimR * 9 * X);
+    for (int i = 0; i < D; ++i)
+        for (int j = 0; j < T_QSDIAG; ++j)
+            for (int x = x0; x < X; ++x) {
+                const double k2 = s->K2[z * X + x], sq = k2 * k2;
+                s->M[((size_t)i * 9 + j) * X + x] =
+                    scale * (sq * s->Qs[i * 9 + j] + 2. * k2 * s->Qps[i * 9 + j] + s->Qpps[i * 9 + j]);
+            }
+}
+
+static void fill_g_visc(cport *s, int z, int x0, double scale)
+{
+    /* M = scale * (Rps + K2 Rs), rows < dimR */
+    const int X = s->X, R = s->dimR;
+    memset(s->M, 0, sizeof(double) * (size_t)s->dimR * 9 * X);
+    for (int i = 0; i < R; ++i)
+        for (int j = 0; j < T_RSDIAG; ++j)
+            for (int x = x0; x < X; ++x) {
+                const double k2 = s->K2[z * X + x];
+                s->M[((size_t)i * 9 + j) * X + x] = scale * (s->Rps[i * 5 + j] + k2 * s->Rs[i * 5 + j]);
+            }
+}
+
+/* kind 2 on one line: C += dt Mass^-1 F x (x = MC[3n+1]) */
+static void re_force_line_ref(cport *s, int z, int x0, cpx *C, const cpx *x)
+{
+    const int X = s->X, D = s->dimQ, R = s->dimR;
+    const double re2 = s->re * s->re;
+    cpx *Ca = &C[CI(s, z, ALPHA, 0, 0)], *Cb = &C[CI(s, z, BETA, 0, 0)];
+    memset(s->Fa, 0, sizeof(cpx) * (size_t)D * X);
+    memset(s->Fb, 0, sizeof(cpx) * (size_t)R * X);
+    fill_v_visc(s, z, x0, -re2);
+    smmult(s->M, &x[CI(s, z, ALPHA, 0, 0)], s->Fa, QSDIAG - 1, QSDIAG - 1, D, X, x0);
+    fill_g_visc(s, z, x0, re2);
+    smmult(s->M, &x[CI(s, z, BETA, 0, 0)], s->Fb, RSDIAG - 1, RSDIAG - 1, R, X, x0);
+    memset(s->M, 0, sizeof(double) * (size_t)s->dimR * 9 * X);
+    for (int i = 0; i < D; ++i)
+        for (int j = 0; j < T_QSDIAG; ++j)
+            for (int xx = x0; xx < X; ++xx)
+                s->M[((size_t)i * 9 + j) * X + xx] = -(s->K2[z * X + xx] * s->Qs[i * 9 + j] + s->Qps[i * 9 + j]);
+    bsolve(s->M, s->Fa, QSDIAG - 1, QSDIAG - 1, D, X, x0);
+    memset(s->M, 0, sizeof(double) * (size_t)s->dimR * 9 * X);
+    for (int i = 0; i < R; ++i)
+        for (int j = 0; j < T_RSDIAG; ++j)
+            for (int xx = x0; xx < X; ++xx) s->M[((size_t)i * 9 + j) * X + xx] = s->Rs[i * 5 + j];
+    bsolve(s->M, s->Fb, RSDIAG - 1, RSDIAG - 1, R, X, x0);
+    for (int xx = x0; xx < X; ++xx) {
+        for (int i = 0; i < D; ++i) {
+            Ca[i * X + xx].re += s->dt * s->Fa[i * X + xx].re;
+            Ca[i * X + xx].im += s->dt * s->Fa[i * X + xx].im;
+        }
+        for (int i = 0; i < R; ++i) {
+            Cb[i * X + xx].re += s->dt * s->Fb[i * X + xx].re;
+            Cb[i * X + xx].im += s->dt * s->Fb[i * X + xx].im;
+        }
+    }
+}
+
+/* kind 3 on one line, alpha (v = ALPHA) or beta: rhs -= re^2 dt (a D xk + b D xk1) */
+static void re_force_line_exact(cport *s, int z, int x0, int v, cpx *rhs, const cpx *xk, const cpx *xk1,
+                                double ak, double bk)
+{
+    const int X = s->X, N = v == ALPHA ? s->dimQ : s->dimR;
+    const int band = v == ALPHA ? QSDIAG - 1 : RSDIAG - 1;
+    const double re2 = s->re * s->re;
+    /* alpha: D = K2^2 Qs + 2 K2 Qps + Qpps; beta: D = -(Rps + K2 Rs) */
+    if (v == ALPHA) fill_v_visc(s, z, x0, 1.0);
+    else fill_g_visc(s, z, x0, -1.0);
+    smmult(s->M, &xk[CI(s, z, v, 0, 0)], s->TM, band, band, N, X, x0);
+    for (int i = 0; i < N; ++i)
+        for (int xx = x0; xx < X; ++xx) {
+            rhs[i * X + xx].re -= re2 * s->dt * ak * s->TM[i * X + xx].re;
+            rhs[i * X + xx].im -= re2 * s->dt * ak * s->TM[i * X + xx].im;
+        }
+    smmult(s->M, &xk1[CI(s, z, v, 0, 0)], s->TM, band, band, N, X, x0);
+    for (int i = 0; i < N; ++i)
+        for (int xx = x0; xx < X; ++xx) {
+            rhs[i * X + xx].re -= re2 * s->dt * bk * s->TM[i * X + xx].re;
+            rhs[i * X + xx].im -= re2 * s->dt * bk * s->TM[i * X + xx].im;
+        }
+}
+
 /* One (kz) line of the implicit step for non-(0,0) modes.
    project.c:24-405 (forward, adj == 0) and adjproject.c:10-550 (adj == 1).
    C is the carried coefficient array, H the array holding the nonlinear
@@ -858,11 +959,12 @@ static void rhs_fb(cport *s, const cpx *H, int z, int x0, int adj)
    adjoint), store the trajectory slot (NULL: none), LUa the previous-stage
    terms for the adjoint's next-stage right-hand side. */
 static void project_line(cport *s, int k, int z, int x0, cpx *C, const cpx *H, cpx *U,
-                         cpx *store, const cpx *LUa, int adj)
+                         cpx *store, const cpx *LUa, int adj, int fkind, const cpx *xk)
 {
     const int X = s->X, D = s->dimQ, R = s->dimR;
     const double *a = adj ? aa_ : fa_, *b = adj ? ab_ : fb_, *c = adj ? ac_ : fc_, *d = adj ? ad_ : fd_;
     cpx *Ca = &C[CI(s, z, ALPHA, 0, 0)], *Cb = &C[CI(s, z, BETA, 0, 0)];
+    if (fkind == 2 && k == 0) re_force_line_ref(s, z, x0, C, xk + s->csz);  /* MC[3n+1] */
     if (k == 0) {
         fill_v_lhs(s, z, x0, a[0], 0);
         smmult(s->M, Ca, s->TM, QSDIAG - 1, QSDIAG - 1, D, X, x0);
@@ -875,6 +977,10 @@ static void project_line(cport *s, int k, int z, int x0, cpx *C, const cpx *H, c
             Ca[i * X + x].re += s->dt * c[k] * s->Fa[i * X + x].re;
             Ca[i * X + x].im += s->dt * c[k] * s->Fa[i * X + x].im;
         }
+    if (fkind == 3) {
+        re_force_line_exact(s, z, x0, ALPHA, Ca, xk, xk + s->csz, a[k], b[k]);
+        fill_v_lhs(s, z, x0, b[k], 1);
+    }
     bsolve(s->M, Ca, QSDIAG - 1, QSDIAG - 1, D, X, x0);
     if (k == 0) {
         fill_g_lhs(s, z, x0, a[0], 0);
@@ -888,6 +994,10 @@ static void project_line(cport *s, int k, int z, int x0, cpx *C, const cpx *H, c
             Cb[i * X + x].re += s->dt * c[k] * s->Fb[i * X + x].re;
             Cb[i * X + x].im += s->dt * c[k] * s->Fb[i * X + x].im;
         }
+    if (fkind == 3) {
+        re_force_line_exact(s, z, x0, BETA, Cb, xk, xk + s->csz, a[k], b[k]);
+        fill_g_lhs(s, z, x0, b[k], 1);
+    }
     bsolve(s->M, Cb, RSDIAG - 1, RSDIAG - 1, R, X, x0);
     if (store) {
         for (int v = 0; v < 2; ++v)
@@ -920,13 +1030,32 @@ static void project_line(cport *s, int k, int z, int x0, cpx *C, const cpx *H, c
    mode 1: tangent with mean-flux forcing, increproject0.c:209-214 (2.0 - sum)
    mode 2: homogeneous tangent (-sum)
    mode 3: adjoint, adjproject0.c:8-310 */
-static void project_mean(cport *s, int k, cpx *C, const cpx *H, cpx *U, cpx *store, const cpx *LUa, int mode)
+static void project_mean(cport *s, int k, cpx *C, const cpx *H, cpx *U, cpx *store, const cpx *LUa, int mode,
+                         int fkind, const cpx *xk)
 {
     const int R = s->dimR, q = s->qpts, X = s->X;
     const int adj = mode == 3;
     const double *a = adj ? aa_ : fa_, *b = adj ? ab_ : fb_, *c = adj ? ac_ : fc_, *d = adj ? ad_ : fd_;
     double *MZ = s->MZ;
     cpx *Ca = &C[CI(s, 0, ALPHA, 0, 0)], *Cb = &C[CI(s, 0, BETA, 0, 0)];
+    const double re2 = s->re * s->re;
+    if (fkind == 2 && k == 0) {
+        /* tangent_forcing0.c:31-41 on MC[3n+1], then Rs^-1 and IC += dt f */
+        const cpx *x1 = xk + s->csz;
+        for (int v = 0; v < 2; ++v) {
+            for (int i = 0; i < R; ++i)
+                for (int j = 0; j < T_RSDIAG; ++j) MZ[i * 5 + j] = re2 * s->Rps[i * 5 + j];
+            smmult_single(MZ, 5, &x1[CI(s, 0, v, 0, 0)], X, s->fa, RSDIAG - 1, RSDIAG - 1, R);
+            for (int i = 0; i < R; ++i)
+                for (int j = 0; j < T_RSDIAG; ++j) MZ[i * 5 + j] = s->Rs[i * 5 + j];
+            bsolve_single(MZ, 5, s->fa, 1, RSDIAG - 1, RSDIAG - 1, R);
+            cpx *Cv = v == ALPHA ? Ca : Cb;
+            for (int i = 0; i < R; ++i) {
+                Cv[i * X].re += s->dt * s->fa[i].re;
+                Cv[i * X].im += s->dt * s->fa[i].im;
+            }
+        }
+    }
     if (k == 0) {
         for (int i = 0; i < R; ++i)
             for (int j = 0; j < T_RSDIAG; ++j) MZ[i * 5 + j] = s->Rs[i * 5 + j] - s->re * a[0] * s->dt * s->Rps[i * 5 + j];
@@ -953,6 +1082,27 @@ static void project_mean(cport *s, int k, cpx *C, const cpx *H, cpx *U, cpx *sto
         }
         Ca[i * X].re += s->dt * c[k] * s->fa[i].re;
     }
+    if (fkind == 3) {
+        /* D0 = -Rps: rhs += re^2 dt (a Rps xk + b Rps xk1) */
+        smmult_single(s->Rps, 5, &xk[CI(s, 0, ALPHA, 0, 0)], X, s->tm, RSDIAG - 1, RSDIAG - 1, R);
+        for (int i = 0; i < R; ++i) {
+            Ca[i * X].re += re2 * s->dt * a[k] * s->tm[i].re;
+            Ca[i * X].im += re2 * s->dt * a[k] * s->tm[i].im;
+        }
+        /* the implicit term acts on the primal's solved mean flow, before
+           its flux correction: MC[3n+k+1] - 0.5 flux_t add */
+        const cpx *x1 = &xk[s->csz + CI(s, 0, ALPHA, 0, 0)];
+        const double ft = s->MFT[(x1 - CI(s, 0, ALPHA, 0, 0) - s->MC) / s->csz];
+        for (int i = 0; i < R; ++i) {
+            s->fb[i].re = x1[i * X].re - ft * s->add[i].re * 0.5;
+            s->fb[i].im = x1[i * X].im - ft * s->add[i].im * 0.5;
+        }
+        smmult_single(s->Rps, 5, s->fb, 1, s->tm, RSDIAG - 1, RSDIAG - 1, R);
+        for (int i = 0; i < R; ++i) {
+            Ca[i * X].re += re2 * s->dt * b[k] * s->tm[i].re;
+            Ca[i * X].im += re2 * s->dt * b[k] * s->tm[i].im;
+        }
+    }
     bsolve_single(MZ, 5, Ca, X, RSDIAG - 1, RSDIAG - 1, R);
     for (int i = 0; i < R; ++i)
         for (int j = 0; j < T_RSDIAG; ++j) MZ[i * 5 + j] = s->Rs[i * 5 + j] + s->re * b[k] * s->dt * s->Rps[i * 5 + j];
@@ -964,11 +1114,26 @@ static void project_mean(cport *s, int k, cpx *C, const cpx *H, cpx *U, cpx *sto
         }
         Cb[i * X].re += s->dt * c[k] * s->fb[i].re;
     }
+    if (fkind == 3) {
+        smmult_single(s->Rps, 5, &xk[CI(s, 0, BETA, 0, 0)], X, s->tm, RSDIAG - 1, RSDIAG - 1, R);
+        for (int i = 0; i < R; ++i) {
+            Cb[i * X].re += re2 * s->dt * a[k] * s->tm[i].re;
+            Cb[i * X].im += re2 * s->dt * a[k] * s->tm[i].im;
+        }
+        smmult_single(s->Rps, 5, &xk[s->csz + CI(s, 0, BETA, 0, 0)], X, s->tm, RSDIAG - 1, RSDIAG - 1, R);
+        for (int i = 0; i < R; ++i) {
+            Cb[i * X].re += re2 * s->dt * b[k] * s->tm[i].re;
+            Cb[i * X].im += re2 * s->dt * b[k] * s->tm[i].im;
+        }
+    }
     bsolve_single(MZ, 5, Cb, X, RSDIAG - 1, RSDIAG - 1, R);
     double flux_t = 0;
     for (int i = 0; i < R; ++i)
         for (int j = 0; j < q; ++j) flux_t += s->Rw[i * q + j] * Ca[i * X].re;
-    if (mode == 0) flux_t = s->flux - flux_t;
+    if (mode == 0) {
+        flux_t = s->flux - flux_t;
+        if (store) s->MFT[(store - s->MC) / s->csz] = flux_t;
+    }
     else if (mode == 1) flux_t = 2.0 - flux_t;
     else flux_t = -flux_t;
     for (int j = 0; j < R; ++j) {
@@ -1012,19 +1177,26 @@ static void project_mean(cport *s, int k, cpx *C, const cpx *H, cpx *U, cpx *sto
 
 /* one substage of the implicit solve over all modes of one field:
    channel.c:456-470 (primal), 546-573 (tangent), 668-679 (adjoint) */
-static void solve_all(cport *s, int k, cpx *C, const cpx *H, cpx *U, cpx *store, const cpx *LUa, int mean_mode)
+/* fkind 2 / 3: Re forcing from the primal states xk = MC[3n+k], xk + csz = MC[3n+k+1] */
+static void solve_all_forced(cport *s, int k, cpx *C, const cpx *H, cpx *U, cpx *store, const cpx *LUa,
+                             int mean_mode, int fkind, const cpx *xk)
 {
     const int adj = mean_mode == 3;
-    project_mean(s, k, C, H, U, store, LUa, mean_mode);
-    project_line(s, k, 0, 1, C, H, U, store, LUa, adj);
+    project_mean(s, k, C, H, U, store, LUa, mean_mode, fkind, xk);
+    project_line(s, k, 0, 1, C, H, U, store, LUa, adj, fkind, xk);
     for (int z = 1; z < s->Nz; ++z) {
         if (z == s->Nz / 2) {
             memset(&U[UI(s, z, 0, 0, 0)], 0, sizeof(cpx) * 5 * (size_t)s->qpts * s->X);
             memset(&C[CI(s, z, 0, 0, 0)], 0, sizeof(cpx) * 2 * (size_t)s->dimR * s->X);
             continue;
         }
-        project_line(s, k, z, 0, C, H, U, store, LUa, adj);
+        project_line(s, k, z, 0, C, H, U, store, LUa, adj, fkind, xk);
     }
+}
+
+static void solve_all(cport *s, int k, cpx *C, const cpx *H, cpx *U, cpx *store, const cpx *LUa, int mean_mode)
+{
+    solve_all_forced(s, k, C, H, U, store, LUa, mean_mode, 0, NULL);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1110,6 +1282,7 @@ cport *cport_init(int Nx, int Ny, int Nz, double Lx, double Lz, double Re,
     CALLOC(s->U, s->usz); CALLOC(s->IU, s->usz); CALLOC(s->AU, s->usz);
     CALLOC(s->IAU, s->usz); CALLOC(s->LU, s->usz);
     CALLOC(s->MC, s->csz * (3 * (size_t)nsteps + 1));
+    DALLOC(s->MFT, 3 * (size_t)nsteps + 1);
     CALLOC(s->MIC, s->csz * (3 * (size_t)nsteps + 1));
     CALLOC(s->CT, (size_t)MAXTT * s->pz * s->hx);
     CALLOC(s->ICT, (size_t)MAXTT * s->pz * s->hx);
@@ -1137,7 +1310,7 @@ void cport_destroy(cport *s)
     if (!s) return;
     double *d[] = { s->Kx, s->Kz, s->K2, s->cfl2, s->Qy, s->W, s->Q, s->Qp, s->Qpp, s->R, s->Rp,
                     s->Qw, s->Qpw, s->Qppw, s->Rw, s->Rpw, s->Qs, s->Qps, s->Qpps, s->Rs, s->Rps,
-                    s->M, s->MZ, s->ddt_dudt, s->ddt_v };
+                    s->M, s->MZ, s->ddt_dudt, s->ddt_v, s->MFT };
     for (size_t i = 0; i < sizeof(d) / sizeof(d[0]); ++i) free(d[i]);
     cpx *c[] = { s->C, s->IC, s->AC, s->U, s->IU, s->AU, s->IAU, s->LU, s->MC, s->MIC, s->CT, s->ICT,
                  s->Fa, s->Fb, s->TM, s->fa, s->fb, s->tm, s->add, s->ddt_dCdt };
@@ -1190,6 +1363,14 @@ int cport_primal(cport *s, int ru_steps, double *C_given)
 /* channel.c:486-587 */
 int cport_tangent(cport *s, int start_step, int end_step, double *IC_given, int inhomo)
 {
+    return cport_tangent_forcing(s, start_step, end_step, IC_given, inhomo ? 1 : 0);
+}
+
+/* forcing 0: none, 1: mean flux (the reference's inhomo != 0), 2: Re, the
+   reference's disconnected forcing reconnected, 3: Re, exact discrete
+   derivative (see re_force_line_ref / re_force_line_exact) */
+int cport_tangent_forcing(cport *s, int start_step, int end_step, double *IC_given, int forcing)
+{
     int status = 0;
     if (!(end_step > start_step && start_step >= 0 && end_step <= s->nsteps && IC_given)) return -2;
     memmove(s->C, s->MC + (size_t)start_step * 3 * s->csz, sizeof(cpx) * s->csz);
@@ -1206,7 +1387,8 @@ int cport_tangent(cport *s, int start_step, int end_step, double *IC_given, int 
                 break;
             }
             int count = n * 3 + dctr + 1;
-            solve_all(s, dctr, s->IC, s->IU, s->IU, s->MIC + (size_t)count * s->csz, NULL, inhomo ? 1 : 2);
+            solve_all_forced(s, dctr, s->IC, s->IU, s->IU, s->MIC + (size_t)count * s->csz, NULL,
+                             forcing == 1 ? 1 : 2, forcing >= 2 ? forcing : 0, s->MC + (size_t)(count - 1) * s->csz);
             solve_all(s, dctr, s->C, s->U, s->U, NULL, NULL, 0);
         }
     }

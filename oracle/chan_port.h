@@ -39,6 +39,9 @@ int cport_primal(cport *s, int ru_steps, double *C_given);
 int cport_tangent(cport *s, int start_step, int end_step, double *IC_given,
                   int inhomo);
 /* channel.c:596 adjoint() */
+/* forcing 0 none, 1 mean flux, 2 Re (reference forcing reconnected), 3 Re (exact) */
+int cport_tangent_forcing(cport *s, int start_step, int end_step, double *IC_given,
+                          int forcing);
 int cport_adjoint(cport *s, int start_step, int end_step, double *AC_given,
                   int inhomo, double strength);
 /* channel.c:704 ddt_project() */

@@ -103,6 +103,7 @@ class PortChannel(_Base):
             L.cport_destroy.argtypes = [_vp]
             L.cport_primal.argtypes = [_vp, _c_int, _vp]
             L.cport_tangent.argtypes = [_vp, _c_int, _c_int, _vp, _c_int]
+            L.cport_tangent_forcing.argtypes = [_vp, _c_int, _c_int, _vp, _c_int]
             L.cport_adjoint.argtypes = [_vp, _c_int, _c_int, _vp, _c_int, _c_dbl]
             L.cport_ddt_project.argtypes = [_vp, _c_int, _vp]
             L.cport_ddt_project.restype = _c_dbl
@@ -148,6 +149,12 @@ class PortChannel(_Base):
     def tangent(self, start, end, IC, inhomo) -> int:
         _check_coef(IC, self.coef_shape)
         return self.lib().cport_tangent(self._h, int(start), int(end), _ptr(IC), int(inhomo))
+
+    def tangent_forcing(self, start, end, IC, forcing) -> int:
+        """forcing 0 none, 1 mean flux, 2 Re (the reference's forcing
+        reconnected), 3 Re (exact derivative of the discrete step)."""
+        _check_coef(IC, self.coef_shape)
+        return self.lib().cport_tangent_forcing(self._h, int(start), int(end), _ptr(IC), int(forcing))
 
     def adjoint(self, start, end, AC, inhomo, strength) -> int:
         _check_coef(AC, self.coef_shape)

@@ -117,6 +117,15 @@ def tangent(start_step, end_step, IC_init, inhomo):
     c_channel.c_tangent(int(start_step), int(end_step), IC_init, int(inhomo))
 
 
+def tangent_forcing(start_step, end_step, IC_init, forcing):
+    """Tangent with a chosen forcing: 0 none, 1 mean flux (meanU), 2 Re with
+    the reference's forcing reconnected (channel/tangent_forcing*.c; first
+    order in dt), 3 Re, exact derivative of the discrete step."""
+    assert IC_init.shape == _shape()
+    assert 0 <= start_step <= end_step <= c_channel.c_nsteps()
+    c_channel.c_tangent_forcing(int(start_step), int(end_step), IC_init, int(forcing))
+
+
 def adjoint(start_step, end_step, AC_init, inhomo, strength):
     assert AC_init.shape == _shape()
     assert 0 <= end_step <= start_step <= c_channel.c_nsteps()

@@ -107,6 +107,8 @@ _lib.c_batch_kernel_ms.restype = _d
 _lib.c_spec2phys_noalloc.argtypes = [_vp, _vp]
 _lib.c_spec2phys_noalloc.restype = _i
 
+_lib.c_tangent_forcing.argtypes = [_i, _i, _vp, _i, _i, _i, _i, _i]
+_lib.c_tangent_forcing.restype = None
 _lib.c_mean_profile.argtypes = [_i, _i, _i, _i, _vp]
 _lib.c_mean_profile.restype = _i
 _lib.c_wall_shear.argtypes = [_i, _i, _i, _vp]
@@ -166,6 +168,13 @@ def c_primal(ru_steps, C_given):
 def c_tangent(start_step, end_step, IC_given, inhomo):
     p, s = _inplace4(IC_given, np.complex128, "c_tangent")
     _lib.c_tangent(int(start_step), int(end_step), p, *s, int(inhomo))
+
+
+def c_tangent_forcing(start_step, end_step, IC_given, forcing):
+    """c_tangent with forcing 0 none, 1 mean flux, 2 Re (the reference's
+    forcing reconnected), 3 Re (exact derivative of the discrete step)."""
+    ptr, shp = _inplace4(IC_given, np.complex128, "IC_given")
+    _lib.c_tangent_forcing(int(start_step), int(end_step), ptr, *shp, int(forcing))
 
 
 def c_adjoint(start_step, end_step, AC_given, inhomo, strength):

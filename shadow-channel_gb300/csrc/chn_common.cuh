@@ -71,6 +71,11 @@ struct Grid {
   const double* ex0;     // [2][R][5]   Rs - re a dt Rps
   const double* add0;    // [4][R]      flux-correction vectors: [0] forward, [1+bidx] adjoint
   const double* rwsum;   // [R]         sum_j Rw[i][j]
+  const double* Qs;      // [D][9]      banded Gram matrices (every other diagonal)
+  const double* Qps;     // [D][9]
+  const double* Qpps;    // [D][9]
+  const double* Rs;      // [R][5]
+  const double* Rps;     // [R][5]
   // FFT twiddles exp(-2 pi i k/N), k < N, for N = pz and N = px
   const cpx* twz;
   const cpx* twx;

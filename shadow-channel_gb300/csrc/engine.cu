@@ -131,7 +131,8 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
             T.up(h.Wq, &g.Wq) && T.up(h.Wqp, &g.Wqp) && T.up(h.Wqpp, &g.Wqpp) && T.up(h.Wr, &g.Wr) &&
             T.up(h.Wrp, &g.Wrp) && T.up(h.luA, &g.luA) && T.up(h.luB, &g.luB) && T.up(h.exA, &g.exA) &&
             T.up(h.exB, &g.exB) && T.up(h.lu0, &g.lu0) && T.up(h.ex0, &g.ex0) && T.up(h.add0, &g.add0) &&
-            T.up(h.rwsum, &g.rwsum);
+            T.up(h.rwsum, &g.rwsum) && T.up(h.Qs, &g.Qs) && T.up(h.Qps, &g.Qps) && T.up(h.Qpps, &g.Qpps) &&
+            T.up(h.Rs, &g.Rs) && T.up(h.Rps, &g.Rps);
   if (!ok) return false;
   const double* tz;
   const double* tx;
@@ -163,6 +164,7 @@ struct Work {
   cpx *Up = nullptr, *Ut = nullptr, *Uprev = nullptr, *Ul = nullptr, *dC = nullptr, *io = nullptr;
   double *Pp = nullptr, *Pt = nullptr, *Pprev = nullptr, *Pl = nullptr, *flow = nullptr;
   double *part = nullptr, *r = nullptr, *cflmax = nullptr;
+  double* Ft = nullptr;   // primal flux correction of each stored substage, [seg][3 nsteps + 1]
   uint32_t* status = nullptr;
   int* step = nullptr;
   // Primal physical-field cache: the six physical fields of the primal state
@@ -233,7 +235,8 @@ struct Work {
            alloc(&io, nt * csz) && alloc(&Pp, nseg * psz) && alloc(&Pt, nt * psz) &&
            alloc(&Pprev, nseg * psz) && alloc(&Pl, nseg * psz) && alloc(&flow, (size_t)3 * g.Q * plane_size(g)) &&
            alloc(&part, (size_t)nseg * kDotBlocks * 2) && alloc(&r, nseg) && alloc(&cflmax, nseg) &&
-           alloc(&status, nseg) && alloc(&step, 4) && alloc(&icp, nseg * csz) && alloc_cache(g);
+           alloc(&status, nseg) && alloc(&step, 4) && alloc(&icp, nseg * csz) &&
+           alloc(&Ft, (size_t)nseg * (3 * (size_t)nsteps + 1)) && alloc_cache(g);
   }
   bool alloc_cache(const Grid& g) {
     Pc = nullptr;
@@ -308,6 +311,7 @@ struct FwdOpts {
   bool cache;           // adv_primal: write the primal fields to the cache;
                         // otherwise: read them from the (valid) cache
   bool store = true;    // adv_primal: store the primal states in MC
+  uint32_t re2_mask = 0, re3_mask = 0;  // tangents with Re forcing (reference / exact)
 };
 
 static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
@@ -401,26 +405,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
       ap.sdiv = 1;
       LK(launch_products_fwd(g, ap, st));
     }
-    if (o.tangents) {
-      SolveArgs sa{};
-      sa.H = cb(w.Ut, w.usz);
-      sa.Hprev = cb(nullptr, 0);
-      sa.Cc = mb(w.Ct, w.csz);
-      sa.Sout = mb(w.St, w.csz);
-      sa.T = mb(w.MIC, w.traj);
-      sa.tdiv = w.ntan;
-      sa.tsel = w.couple;
-      sa.slot = SlotRef{w.step, 3, k + 1, (long long)w.csz};  // MIC[3n + k + 1]
-      sa.k = k;
-      sa.adjoint = 0;
-      sa.mean_mode = MEAN_TAN_HOMOG;
-      sa.forced_mask = o.forced_mask;
-      sa.mdiv = w.ntan;
-      sa.ninst = nt;
-      sa.status = w.status;
-      sa.sdiv = w.ntan;
-      LK(launch_solve(g, sa, st));
-    }
+    // the primal solve first: tangent Re forcing reads the state it stores
     if (o.adv_primal) {
       SolveArgs sa{};
       sa.H = cb(w.Up, w.usz);
@@ -439,6 +424,38 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
       sa.ninst = w.nseg;
       sa.status = w.status;
       sa.sdiv = 1;
+      sa.Fts = w.Ft;
+      sa.fts_stride = 3 * (long long)w.nsteps + 1;
+      LK(launch_solve(g, sa, st));
+    }
+    if (o.tangents) {
+      SolveArgs sa{};
+      sa.H = cb(w.Ut, w.usz);
+      sa.Hprev = cb(nullptr, 0);
+      sa.Cc = mb(w.Ct, w.csz);
+      sa.Sout = mb(w.St, w.csz);
+      sa.T = mb(w.MIC, w.traj);
+      sa.tdiv = w.ntan;
+      sa.tsel = w.couple;
+      sa.slot = SlotRef{w.step, 3, k + 1, (long long)w.csz};  // MIC[3n + k + 1]
+      sa.k = k;
+      sa.adjoint = 0;
+      sa.mean_mode = MEAN_TAN_HOMOG;
+      sa.forced_mask = o.forced_mask;
+      sa.mdiv = w.ntan;
+      sa.ninst = nt;
+      sa.status = w.status;
+      sa.sdiv = w.ntan;
+      sa.re2_mask = o.re2_mask;
+      sa.re3_mask = o.re3_mask;
+      if (o.re2_mask | o.re3_mask) {
+        // primal states MC[3n + k], MC[3n + k + 1] (stored before this solve) and their flux corrections
+        sa.Xf = cb(w.MC, w.traj);
+        sa.xslot = SlotRef{w.step, 3, k - (o.adv_primal ? 3 * o.ru : 0), (long long)w.csz};
+        sa.xdiv = w.ntan;
+        sa.Ftr = w.Ft;
+        sa.ftr_stride = 3 * (long long)w.nsteps + 1;
+      }
       LK(launch_solve(g, sa, st));
     }
   }
@@ -749,7 +766,14 @@ static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
 }
 
 // tangents (and optionally the primal) from start to end; IC device [nseg*ntan]
-static bool op_forward(Engine& e, Work& w, int start, int end, const cpx* C, const cpx* IC, uint32_t forced_mask,
+// Tangent forcings per tangent t: bit t of forced (mean flux, the reference's
+// inhomo != 0), re2 (Re, the reference's disconnected forcing reconnected),
+// re3 (Re, exact derivative of the discrete step).
+struct Forcing {
+  uint32_t forced = 0, re2 = 0, re3 = 0;
+};
+
+static bool op_forward(Engine& e, Work& w, int start, int end, const cpx* C, const cpx* IC, Forcing f,
                        bool adv_primal) {
   const size_t csz = w.csz;
   const int nt = w.nseg * w.ntan;
@@ -787,7 +811,9 @@ static bool op_forward(Engine& e, Work& w, int start, int end, const cpx* C, con
   if (!reset_status(e, w) || !set_step(e, w, start)) return false;
   const bool cache = adv_primal ? true : (!readvance && w.cached(3 * start, 3 * end));
   if (adv_primal) w.mark(3 * start, 3 * end + 1, false);
-  FwdOpts o{adv_primal || readvance, w.ntan > 0, 0, forced_mask, false, cache && !readvance, !readvance};
+  FwdOpts o{adv_primal || readvance, w.ntan > 0, 0, f.forced, false, cache && !readvance, !readvance};
+  o.re2_mask = f.re2;
+  o.re3_mask = f.re3;
   if (!run_steps(e, end - start, [&] { return enqueue_forward_step(e, w, o); })) return false;
   const bool with_vel = w.ntan > 0 && w.Pv != nullptr;
   if (adv_primal || with_vel) {
@@ -994,6 +1020,11 @@ void c_primal(int ru_steps, chn_complex* C_given, int Nz_dup, int Nvar_dup, int 
 
 void c_tangent(int start_step, int end_step, chn_complex* IC_given, int Nz_dup, int Nvar_dup, int Ny_dup,
                int Nx_dup, int inhomo) {
+  c_tangent_forcing(start_step, end_step, IC_given, Nz_dup, Nvar_dup, Ny_dup, Nx_dup, inhomo ? 1 : 0);
+}
+
+void c_tangent_forcing(int start_step, int end_step, chn_complex* IC_given, int Nz_dup, int Nvar_dup, int Ny_dup,
+                       int Nx_dup, int forcing) {
   if (!need_init("c_tangent")) return;
   Engine& e = *E;
   Work& w = e.single;
@@ -1002,9 +1033,14 @@ void c_tangent(int start_step, int end_step, chn_complex* IC_given, int Nz_dup, 
   shape_assert(start_step >= 0, "start_step >= 0");
   shape_assert(end_step <= e.nsteps, "end_step <= nsteps");
   shape_assert(IC_given != nullptr, "IC_given != 0");
+  shape_assert(forcing >= 0 && forcing <= 3, "0 <= forcing <= 3");
   const size_t bytes = sizeof(cpx) * w.csz;
   if (!h2d(e, w.io, IC_given, bytes)) return;
-  if (!op_forward(e, w, start_step, end_step, nullptr, w.io, inhomo ? 1u : 0u, false)) return;
+  Forcing f;
+  f.forced = forcing == 1 ? 1u : 0u;
+  f.re2 = forcing == 2 ? 1u : 0u;
+  f.re3 = forcing == 3 ? 1u : 0u;
+  if (!op_forward(e, w, start_step, end_step, nullptr, w.io, f, false)) return;
   if (!collect_status(e, w)) return;
   if (g_status & ST_CFL) printf("Pass1 failure\n");
   d2h(e, IC_given, w.Ct, bytes);
@@ -1210,11 +1246,16 @@ static bool batch_ready(const char* fn) {
   return true;
 }
 
-static uint32_t mask_of(const int* inhomo, int ntan) {
-  uint32_t m = 0;
-  for (int t = 0; t < ntan; ++t)
-    if (inhomo && inhomo[t]) m |= 1u << t;
-  return m;
+// batched tangents: inhomo[t] 0 none, 1 mean flux, 2 Re (reference forcing), 3 Re (exact)
+static Forcing mask_of(const int* inhomo, int ntan) {
+  Forcing f;
+  for (int t = 0; t < ntan; ++t) {
+    const int v = inhomo ? inhomo[t] : 0;
+    if (v == 2) f.re2 |= 1u << t;
+    else if (v == 3) f.re3 |= 1u << t;
+    else if (v) f.forced |= 1u << t;
+  }
+  return f;
 }
 
 int c_batch_primal_dev(int ru_steps, chn_complex* C) {

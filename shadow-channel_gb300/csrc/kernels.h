@@ -71,6 +71,22 @@ struct SolveArgs {
   int ninst;
   const uint32_t* status;
   int sdiv;
+  // Re-sensitivity forcing of tangents: bit (i % mdiv) of re2_mask selects the
+  // reference's forcing reconnected, of re3_mask the exact derivative.  The
+  // primal state before this substage of instance i is
+  //   Xf.base + (i / xdiv) * Xf.stride + xslot.slot() * xslot.stride
+  // (the state after it follows one slot later), its flux correction after
+  // this substage Ftr[(i / xdiv) * ftr_stride + xslot.slot() + 1].
+  uint32_t re2_mask, re3_mask;
+  Batch<const cpx> Xf;
+  SlotRef xslot;
+  int xdiv;
+  const double* Ftr;
+  long long ftr_stride;
+  // primal only: store flux_t of each stored substage at
+  // Fts[(i / tdiv) * fts_stride + slot] (nullable)
+  double* Fts;
+  long long fts_stride;
 };
 
 // one ddt_project / adjoint coupling for nseg segments (channel/channel.c:704-780)

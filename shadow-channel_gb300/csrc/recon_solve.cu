@@ -397,6 +397,55 @@ __device__ void band_solve_chain(const double* __restrict__ LU, int w, int dl, i
   }
 }
 
+// row r of (K2^2 Qs + 2 K2 Qps + Qpps) y and of (Rps + K2 Rs) y, the viscous
+// operators of the alpha and beta systems (channel/tangent_forcing.c:38-68)
+__device__ __forceinline__ cpx visc_v_row(const Grid& g, double k2, const cpx* y, int ystride, int r) {
+  const int dl = 4, du = 4, N = g.D;
+  int j0 = dl - r / 2;
+  if (j0 < 0) j0 = 0;
+  int j1 = (N - r + 1) / 2 + dl;
+  if (j1 > dl + du + 1) j1 = dl + du + 1;
+  const double sq = k2 * k2;
+  double re = 0.0, im = 0.0;
+  for (int j = j0; j < j1; ++j) {
+    const size_t o = (size_t)r * 9 + j;
+    const double m = sq * __ldg(g.Qs + o) + 2. * k2 * __ldg(g.Qps + o) + __ldg(g.Qpps + o);
+    const cpx v = y[(r - 2 * (dl - j)) * ystride];
+    re = fma(m, v.re, re);
+    im = fma(m, v.im, im);
+  }
+  return cpx{re, im};
+}
+
+__device__ __forceinline__ cpx visc_g_row(const Grid& g, double k2, const cpx* y, int ystride, int r) {
+  const int dl = 2, du = 2, N = g.R;
+  int j0 = dl - r / 2;
+  if (j0 < 0) j0 = 0;
+  int j1 = (N - r + 1) / 2 + dl;
+  if (j1 > dl + du + 1) j1 = dl + du + 1;
+  double re = 0.0, im = 0.0;
+  for (int j = j0; j < j1; ++j) {
+    const size_t o = (size_t)r * 5 + j;
+    const double m = __ldg(g.Rps + o) + k2 * __ldg(g.Rs + o);
+    const cpx v = y[(r - 2 * (dl - j)) * ystride];
+    re = fma(m, v.re, re);
+    im = fma(m, v.im, im);
+  }
+  return cpx{re, im};
+}
+
+// row r of Rps y for a real vector y (stride 1)
+__device__ __forceinline__ double rps_row_real(const Grid& g, const double* y, int r) {
+  const int dl = 2, du = 2, N = g.R;
+  int j0 = dl - r / 2;
+  if (j0 < 0) j0 = 0;
+  int j1 = (N - r + 1) / 2 + dl;
+  if (j1 > dl + du + 1) j1 = dl + du + 1;
+  double acc = 0.0;
+  for (int j = j0; j < j1; ++j) acc = fma(__ldg(g.Rps + (size_t)r * 5 + j), y[r - 2 * (dl - j)], acc);
+  return acc;
+}
+
 __global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
   const int ntx = (g.X + kTile - 1) / kTile;
   const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
@@ -408,9 +457,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
   cpx* __restrict__ Cc = a.Cc.at(inst);
   cpx* __restrict__ So = a.Sout.at(inst);
   cpx* Tst = nullptr;
+  int tslot = -1;
   if (a.T.base && (inst % a.tdiv) == a.tsel) {
-    const int slot = a.slot.slot();
-    if (slot >= 0) Tst = a.T.base + (long long)(inst / a.tdiv) * a.T.stride + (long long)slot * a.slot.stride;
+    tslot = a.slot.slot();
+    if (tslot >= 0) Tst = a.T.base + (long long)(inst / a.tdiv) * a.T.stride + (long long)tslot * a.slot.stride;
   }
   int mean_mode = a.mean_mode;
   if (mean_mode == MEAN_TAN_HOMOG && ((a.forced_mask >> (inst % a.mdiv)) & 1u)) mean_mode = MEAN_TAN_FORCED;
@@ -432,6 +482,70 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
   quad_rhs(g, H, z, x0, nx, adj, s);
   const double dt = g.dt;
   const int xfirst = (z == 0 && x0 == 0) ? 1 : 0;  // the mean mode has its own system
+  // Re-sensitivity forcing of this tangent (kind 2: the reference's forcing
+  // reconnected, channel/tangent_forcing.c + increproject.c:61-104, at the
+  // first substage; kind 3: the exact derivative of the discrete step,
+  // -re^2 dt (a_k D x_k + b_k D x_{k+1}) in every substage's right-hand side)
+  int fkind = 0;
+  const cpx* xk = nullptr;
+  double ft1 = 0.0;
+  if (a.re2_mask | a.re3_mask) {
+    const uint32_t bit = 1u << (inst % a.mdiv);
+    fkind = (a.re3_mask & bit) ? 3 : ((a.re2_mask & bit) ? 2 : 0);
+    if (fkind) {
+      const int xs = a.xslot.slot();
+      xk = a.Xf.at(inst / a.xdiv) + (long long)xs * a.xslot.stride;
+      if (a.Ftr) ft1 = a.Ftr[(long long)(inst / a.xdiv) * a.ftr_stride + xs + 1];
+    }
+  }
+  const double re2 = g.re * g.re;
+  const double ak = a.k == 1 ? -1. / 2 : 1. / 3.;  // forward a_k; b_k is rk.b
+  if (fkind == 2 && a.k == 0) {
+    // C += dt Mass^-1 F MC[3n+1] with F_alpha = -re^2 Dv, F_beta = re^2 (Rps + K2 Rs)
+    __syncthreads();
+    const cpx* x1 = xk + csz;
+    for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+      const int r = i / kTile, l = i - r * kTile;
+      if (l >= nx || l < xfirst) continue;
+      const int x = x0 + l;
+      const double k2 = g.K2[(size_t)z * g.X + x];
+      if (r < g.D) {
+        const cpx v = visc_v_row(g, k2, x1 + cidx(0, 0, x), g.X, r);
+        s.ra[r * kTile + l] = cpx{-re2 * v.re, -re2 * v.im};
+      }
+      const cpx w = visc_g_row(g, k2, x1 + cidx(1, 0, x), g.X, r);
+      s.rb[r * kTile + l] = cpx{re2 * w.re, re2 * w.im};
+    }
+    __syncthreads();
+    if (threadIdx.x < 8 * kTile) {  // mass matrices: the b = 0 factors
+      const int l = threadIdx.x / 8, ch = threadIdx.x % 8;
+      if (l < nx && l >= xfirst) {
+        const size_t zx = (size_t)z * g.X + x0 + l;
+        const int par = ch & 1, part = (ch >> 1) & 1;
+        if (ch < 4)
+          band_solve_chain(g.luA + ((size_t)2 * g.Nz * g.X + zx) * g.D * 9, 9, 4, 4, g.D, par,
+                           reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
+        else
+          band_solve_chain(g.luB + ((size_t)2 * g.Nz * g.X + zx) * g.R * 5, 5, 2, 2, g.R, par,
+                           reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+      const int r = i / kTile, l = i - r * kTile;
+      if (l >= nx || l < xfirst) continue;
+      const int x = x0 + l;
+      if (r < g.D) {
+        const cpx f = s.ra[r * kTile + l];
+        Cc[cidx(0, r, x)].re += dt * f.re;
+        Cc[cidx(0, r, x)].im += dt * f.im;
+      }
+      const cpx f = s.rb[r * kTile + l];
+      Cc[cidx(1, r, x)].re += dt * f.re;
+      Cc[cidx(1, r, x)].im += dt * f.im;
+    }
+    __syncthreads();
+  }
   // right-hand sides (channel/project.c:60-81, 125-130, 143-163, 202-207)
   for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
     const int r = i / kTile, l = i - r * kTile;
@@ -449,6 +563,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
       const cpx f = s.Fa[r * kTile + l];
       va.re += dt * rk.c * f.re;
       va.im += dt * rk.c * f.im;
+      if (fkind == 3) {
+        const double k2 = g.K2[zx];
+        const cpx d0 = visc_v_row(g, k2, xk + cidx(0, 0, x), g.X, r);
+        const cpx d1 = visc_v_row(g, k2, xk + csz + cidx(0, 0, x), g.X, r);
+        va.re -= re2 * dt * ak * d0.re;
+        va.im -= re2 * dt * ak * d0.im;
+        va.re -= re2 * dt * rk.b * d1.re;
+        va.im -= re2 * dt * rk.b * d1.im;
+      }
     } else {
       va = Cc[cidx(0, r, x)];  // alpha rows >= Ny-4 ride along unchanged
     }
@@ -461,6 +584,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
     const cpx f = s.Fb[r * kTile + l];
     vb.re += dt * rk.c * f.re;
     vb.im += dt * rk.c * f.im;
+    if (fkind == 3) {  // beta: D = -(Rps + K2 Rs)
+      const double k2 = g.K2[zx];
+      const cpx d0 = visc_g_row(g, k2, xk + cidx(1, 0, x), g.X, r);
+      const cpx d1 = visc_g_row(g, k2, xk + csz + cidx(1, 0, x), g.X, r);
+      vb.re += re2 * dt * ak * d0.re;
+      vb.im += re2 * dt * ak * d0.im;
+      vb.re += re2 * dt * rk.b * d1.re;
+      vb.im += re2 * dt * rk.b * d1.im;
+    }
     s.ra[r * kTile + l] = va;
     s.rb[r * kTile + l] = vb;
   }
@@ -491,6 +623,30 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
     const int lane = threadIdx.x;
     const size_t cs = (size_t)g.Q * g.X;
     const cpx* H0 = H;  // z = 0, x = 0
+    if (fkind == 2 && a.k == 0) {
+      // tangent_forcing0.c:31-41 on MC[3n+1], Rs^-1, IC += dt f (increproject0.c:45-90)
+      const cpx* x1 = xk + csz;
+      for (int i = lane; i < g.R; i += 32) {
+        const cpx p = band_matvec_row(g.Rps, 5, 2, 2, g.R, x1 + cidx(0, 0, 0), g.X, i);
+        const cpx q = band_matvec_row(g.Rps, 5, 2, 2, g.R, x1 + cidx(1, 0, 0), g.X, i);
+        ca[i] = cpx{re2 * p.re, re2 * p.im};
+        cb[i] = cpx{re2 * q.re, re2 * q.im};
+      }
+      __syncwarp();
+      if (lane < 8) {
+        const int par = lane & 1, part = (lane >> 1) & 1;
+        band_solve_chain(g.lu0 + (size_t)2 * g.R * 5, 5, 2, 2, g.R, par,
+                         reinterpret_cast<double*>(lane < 4 ? ca : cb) + part, 2);
+      }
+      __syncwarp();
+      for (int i = lane; i < g.R; i += 32) {
+        Cc[cidx(0, i, 0)].re += dt * ca[i].re;
+        Cc[cidx(0, i, 0)].im += dt * ca[i].im;
+        Cc[cidx(1, i, 0)].re += dt * cb[i].re;
+        Cc[cidx(1, i, 0)].im += dt * cb[i].im;
+      }
+      __syncwarp();
+    }
     for (int i = lane; i < g.R; i += 32) {
       double sa = 0.0, sb = 0.0;
       for (int y = 0; y < g.Q; ++y) {
@@ -516,6 +672,23 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
       }
       va.re += dt * rk.c * sa;
       vb.re += dt * rk.c * sb;
+      if (fkind == 3) {
+        // D0 = -Rps; the implicit term acts on the primal's solved mean flow
+        // before its flux correction: MC[3n+k+1] - 0.5 flux_t add
+        const cpx p0 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + cidx(0, 0, 0), g.X, i);
+        cpx p1 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + csz + cidx(0, 0, 0), g.X, i);
+        p1.re -= 0.5 * ft1 * rps_row_real(g, g.add0, i);
+        const cpx q0 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + cidx(1, 0, 0), g.X, i);
+        const cpx q1 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + csz + cidx(1, 0, 0), g.X, i);
+        va.re += re2 * dt * ak * p0.re;
+        va.im += re2 * dt * ak * p0.im;
+        va.re += re2 * dt * rk.b * p1.re;
+        va.im += re2 * dt * rk.b * p1.im;
+        vb.re += re2 * dt * ak * q0.re;
+        vb.im += re2 * dt * ak * q0.im;
+        vb.re += re2 * dt * rk.b * q1.re;
+        vb.im += re2 * dt * rk.b * q1.im;
+      }
       ca[i] = va;
       cb[i] = vb;
     }
@@ -536,6 +709,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
     else if (mean_mode == MEAN_TAN_FORCED) flux_t = 2.0 - part;
     else flux_t = -part;
     const double* add = g.add0 + (size_t)(adj ? 1 + rk.bidx : 0) * g.R;
+    if (mean_mode == MEAN_PRIMAL && a.Fts && Tst && lane == 0)
+      a.Fts[(long long)(inst / a.tdiv) * a.fts_stride + tslot] = flux_t;
     __syncwarp();
     for (int i = lane; i < g.R; i += 32) ca[i].re = ca[i].re + flux_t * add[i] * 0.5;
     __syncwarp();
