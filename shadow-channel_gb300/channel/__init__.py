@@ -34,21 +34,84 @@ def quad():
     return y.copy(), w.copy()
 
 
-def save_solution(filename, C):
-    """Save the solution C (and the last tangent) to ``filename`` (raw
-    container "SCHNRAW1", not HDF5).  Must be called after init()."""
+def save_solution(filename, C, fmt="raw"):
+    """Save the solution C (and the last tangent) to ``filename``.
+
+    fmt "raw": the library's container (8 bytes "SCHNRAW1", int32 Nx, Ny,
+    Nz, 0, float64 dt, 1/Re, mpg, then alpha, beta, ialpha, ibeta as
+    [dimR][Nz][Nx/2] complex records); fmt "npz": a numpy archive with the
+    reference's HDF5 dataset names and shapes (data_alpha, data_beta,
+    data_ialpha, data_ibeta [dimR, Nz, Nx/2] complex128; data_Nx, data_Ny,
+    data_Nz int32 [1]; data_dt, data_Re (= 1/Re), data_mpg float64 [1];
+    channel/channel.c:889-1028).  HDF5 itself is not part of this build.
+    Must be called after init()."""
     if not filename.endswith('.hd5'):
         filename += '.hd5'
     assert C.shape == _shape()
-    c_channel.c_save_solution(filename, C)
+    if fmt == "raw":
+        c_channel.c_save_solution(filename, C)
+        return
+    assert fmt == "npz", fmt
+    import os
+    import tempfile
+    fd, tmp = tempfile.mkstemp(suffix=".raw")
+    os.close(fd)
+    try:
+        c_channel.c_save_solution(tmp, C)
+        d = _read_raw(tmp)
+    finally:
+        os.unlink(tmp)
+    with open(filename, "wb") as f:
+        np.savez(f, **d)
+
+
+def _read_raw(path):
+    with open(path, "rb") as f:
+        head = f.read(8)
+        assert head == b"SCHNRAW1", "not a SCHNRAW1 solution file"
+        nx, ny, nz, _ = np.frombuffer(f.read(16), "<i4")
+        dt_, re_, mpg = np.frombuffer(f.read(24), "<f8")
+        shp = (int(ny) - 2, int(nz), int(nx) // 2)
+        n = int(np.prod(shp))
+        arrs = [np.frombuffer(f.read(16 * n), "<c16").reshape(shp).copy() for _ in range(4)]
+    d = {k: v for k, v in zip(("data_alpha", "data_beta", "data_ialpha", "data_ibeta"), arrs)}
+    d.update(data_Nx=np.array([nx], np.int32), data_Ny=np.array([ny], np.int32),
+             data_Nz=np.array([nz], np.int32), data_dt=np.array([dt_]), data_Re=np.array([re_]),
+             data_mpg=np.array([mpg]))
+    return d
+
+
+def _write_raw(path, d):
+    with open(path, "wb") as f:
+        f.write(b"SCHNRAW1")
+        f.write(np.array([d["data_Nx"][0], d["data_Ny"][0], d["data_Nz"][0], 0], "<i4").tobytes())
+        f.write(np.array([d["data_dt"][0], d["data_Re"][0], d["data_mpg"][0]], "<f8").tobytes())
+        for k in ("data_alpha", "data_beta", "data_ialpha", "data_ibeta"):
+            f.write(np.ascontiguousarray(d[k], "<c16").tobytes())
 
 
 def read_solution(filename):
-    """Read a solution written by save_solution; returns complex [Nz, 2, dimR, Nx/2]."""
+    """Read a solution written by save_solution (either format); returns
+    complex [Nz, 2, dimR, Nx/2]."""
     if not filename.endswith('.hd5'):
         filename += '.hd5'
     C = np.zeros(_shape(), complex)
-    c_channel.c_read_solution(str(filename), C)
+    with open(filename, "rb") as f:
+        is_npz = f.read(2) == b"PK"
+    if not is_npz:
+        c_channel.c_read_solution(str(filename), C)
+        return C
+    import os
+    import tempfile
+    with np.load(filename) as z:
+        d = {k: z[k] for k in z.files}
+    fd, tmp = tempfile.mkstemp(suffix=".raw")
+    os.close(fd)
+    try:
+        _write_raw(tmp, d)
+        c_channel.c_read_solution(tmp, C)
+    finally:
+        os.unlink(tmp)
     return C
 
 
