@@ -152,6 +152,25 @@ def phys_inverse_flops(ninst, g, nfields=6):
     return ninst * nfields * Q * per_plane
 
 
+def segment_step_flops(g):
+    """Nominal FP64 flop of one segment-step (primal + 3 tangents + adjoint,
+    3 substages): per field and substage the Legendre quadrature
+    4 Q (5D + 3R) Nz X (2 right-hand-side + 5 reconstruction contractions of
+    a real matrix with complex vectors) and 9 plane transforms (6 inverse + 3
+    forward) of X 5 pz log2 pz + pz 2.5 px log2 px each; the adjoint counts
+    1.5 quadratures and 15 transforms (9 inverse + 6 forward)."""
+    Nx, Ny, Nz = g["Nx"], g["Ny"], g["Nz"]
+    X, Q, R, D, pz, px = Nx // 2, 3 * Ny // 2, Ny - 2, Ny - 4, 3 * Nz // 2, 3 * Nx // 2
+    quad = 4.0 * Q * (5 * D + 3 * R) * Nz * X
+    plane = X * 5 * pz * math.log2(pz) + pz * 2.5 * px * math.log2(px)
+    return 3 * ((1 + NTAN) * (quad + 9 * Q * plane) + (1.5 * quad + 15 * Q * plane))
+
+
+# ncu DRAM bytes (read + write) of one k_phys_inverse instance: a 24-instance
+# launch at 32x65x32 moved 315.6 MB; traffic grows with the instance count
+PHYS_TRAFFIC_PER_INSTANCE_32 = 315.6e6 / 24
+
+
 def recon_flops(ninst, g):
     """Parity-split reconstruction: (3D + 2R) complex multiply-adds per plane
     pair and (kz, kx) mode, plus 24 flop of wavenumber algebra per point."""
@@ -259,11 +278,19 @@ def run_gb300(a):
     dom_ms = k_ms["phys_inverse"]
     flops = phys_inverse_flops(nt, GRID)
     achieved = flops / (dom_ms * 1e-3) / 1e12
-    roofline = {"bound": "fp64", "kernel": "k_phys_inverse (192 tangent fields)", "achieved": achieved,
-                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+    traffic = PHYS_TRAFFIC_PER_INSTANCE_32 * nt if (GRID["Nx"], GRID["Ny"], GRID["Nz"]) == (32, 65, 32) else None
+    step_flop = segment_step_flops(GRID)
+    roofline = {"bound": "fp64", "kernel": f"k_phys_inverse ({nt} tangent fields)", "achieved": achieved,
+                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                "traffic_unit": "bytes per launch",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 24-instance "
+                                  "launch, scaled by the instance count",
                 "peak_source": "measured: FP64 FMA probe in this run (c_fp64_peak_tflops)",
                 "algorithmic_flop_per_launch": flops, "kernel_ms": k_ms,
-                "recon_tflops": recon_flops(nt, GRID) / (k_ms["recon"] * 1e-3) / 1e12}
+                "recon_tflops": recon_flops(nt, GRID) / (k_ms["recon"] * 1e-3) / 1e12,
+                "step": {"algorithmic_flop_per_segment_step": step_flop,
+                         "achieved_tflops": step_flop * value / world / 1e12,
+                         "frac": step_flop * value / world / 1e12 / peak}}
 
     cc.lib.c_batch_destroy()
     cc.c_destroy()

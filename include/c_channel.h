@@ -169,6 +169,10 @@ long long c_launch_count(void);
 /* FP64 fused-multiply-add throughput of this GPU in TFLOP/s (2 flop/FMA),
    measured with a register-only kernel; used as the roofline peak. */
 double c_fp64_peak_tflops(void);
+/* throughput of one pipe in TFLOP/s (counting an FMA as 2): kind 0 FP64
+   FMA, 1 FP64 add, 2 FP64 warp matrix multiply-accumulate (m8n8k4), 3 FP32
+   FMA; NaN for other kinds */
+double c_pipe_peak_tflops(int kind);
 
 /* spec2phys without allocating: no counterpart in the reference.  For
    callers that cannot call cudaMalloc when they need a physical field (code

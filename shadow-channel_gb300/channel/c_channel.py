@@ -75,6 +75,8 @@ _lib.c_launch_count.argtypes = []
 _lib.c_launch_count.restype = ctypes.c_longlong
 _lib.c_fp64_peak_tflops.argtypes = []
 _lib.c_fp64_peak_tflops.restype = _d
+_lib.c_pipe_peak_tflops.argtypes = [_i]
+_lib.c_pipe_peak_tflops.restype = _d
 _lib.c_batch_init.argtypes = [_i, _i, _i]
 _lib.c_batch_init.restype = _i
 _lib.c_batch_primal.argtypes = [_i, _vp]

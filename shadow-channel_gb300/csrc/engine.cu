@@ -1505,20 +1505,22 @@ int c_synchronize(void) {
 
 long long c_launch_count(void) { return g_launches; }
 
-double c_fp64_peak_tflops(void) {
+double c_pipe_peak_tflops(int kind) {
+  const double fpi = probe_flop_per_thread_iter(kind);
+  if (fpi <= 0.0) return NAN;
   cudaStream_t st = E ? E->st : nullptr;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int threads = 256, blocks = sms * 8, iters = 4096;
+  const int threads = 256, blocks = sms * 8, iters = kind == 3 ? 16384 : 4096;
   double* buf = nullptr;
   if (cudaMalloc(&buf, sizeof(double) * threads * blocks) != cudaSuccess) return NAN;
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  launch_fp64_probe(buf, blocks, threads, iters, st);  // warm-up
+  launch_pipe_probe(kind, buf, blocks, threads, iters, st);  // warm-up
   cudaEventRecord(a, st);
-  for (int r = 0; r < 3; ++r) launch_fp64_probe(buf, blocks, threads, iters, st);
+  for (int r = 0; r < 3; ++r) launch_pipe_probe(kind, buf, blocks, threads, iters, st);
   cudaEventRecord(b, st);
   cudaEventSynchronize(b);
   float ms = 0.f;
@@ -1527,8 +1529,10 @@ double c_fp64_peak_tflops(void) {
   cudaEventDestroy(b);
   cudaFree(buf);
   g_launches += 4;
-  const double flop = 3.0 * blocks * threads * (double)iters * 8 * 2;
+  const double flop = 3.0 * blocks * threads * (double)iters * fpi;
   return flop / (ms * 1e-3) / 1e12;
 }
+
+double c_fp64_peak_tflops(void) { return c_pipe_peak_tflops(0); }
 
 }  // extern "C"

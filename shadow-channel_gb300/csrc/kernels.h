@@ -143,5 +143,8 @@ cudaError_t launch_project_init(const Grid& g, const cpx* Uinit, cpx* C, const d
                                 const double* luRs, cudaStream_t st);
 cudaError_t launch_step_advance(int* ctr, int delta, cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
+// pipe throughput probes: kind 0 DFMA, 1 DADD, 2 DMMA (m8n8k4 f64), 3 FFMA
+cudaError_t launch_pipe_probe(int kind, double* out, int blocks, int threads, int iters, cudaStream_t st);
+double probe_flop_per_thread_iter(int kind);
 
 }  // namespace chn

@@ -329,4 +329,62 @@ cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, c
   return cudaGetLastError();
 }
 
+// Throughput probes of the other pipes the design choices rest on: FP64 add,
+// FP64 warp-level matrix multiply-accumulate (m8n8k4), FP32 FMA.  8
+// independent chains per thread (4 accumulator pairs per warp for DMMA).
+__global__ void k_dadd_probe(double* out, int iters, double b) {
+  double x0 = threadIdx.x * 1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 += b; x1 += b; x2 += b; x3 += b; x4 += b; x5 += b; x6 += b; x7 += b;
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+__global__ void k_ffma_probe(double* out, int iters, float a, float b) {
+  float x0 = threadIdx.x * 1e-6f, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  float x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+__global__ void k_dmma_probe(double* out, int iters, double a0, double b0) {
+  const double a = a0 + threadIdx.x * 1e-12, b = b0 - threadIdx.x * 1e-12;
+  double c[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                   : "+d"(c[q][0]), "+d"(c[q][1])
+                   : "d"(a), "d"(b));
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = c[0][0] + c[0][1] + c[1][0] + c[1][1] + c[2][0] + c[2][1] +
+                                               c[3][0] + c[3][1];
+}
+
+// flop per thread per iteration of each probe kind (0 DFMA, 1 DADD, 2 DMMA, 3 FFMA)
+double probe_flop_per_thread_iter(int kind) {
+  switch (kind) {
+    case 0: return 16.0;          // 8 FMA
+    case 1: return 8.0;           // 8 adds
+    case 2: return 4 * 512.0 / 32; // 4 mma of 8x8x4 (2 flop per MAC) per warp
+    case 3: return 16.0;
+    default: return 0.0;
+  }
+}
+
+cudaError_t launch_pipe_probe(int kind, double* out, int blocks, int threads, int iters, cudaStream_t st) {
+  switch (kind) {
+    case 0: k_fp64_probe<<<blocks, threads, 0, st>>>(out, iters, 0.999999, 1e-7); break;
+    case 1: k_dadd_probe<<<blocks, threads, 0, st>>>(out, iters, 1e-7); break;
+    case 2: k_dmma_probe<<<blocks, threads, 0, st>>>(out, iters, 0.5, 0.25); break;
+    case 3: k_ffma_probe<<<blocks, threads, 0, st>>>(out, iters, 0.999999f, 1e-7f); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace chn
