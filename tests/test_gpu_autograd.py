@@ -1,0 +1,61 @@
+"""channel.autograd.TimeMeanWallShear: the checkpointed differentiable
+objective.  Its gradients (exact tangents of the discrete step, Re forcing
+kind 3 and mean-flux forcing) must match central finite differences of the
+objective to 1e-6, and checkpointing must not change the results."""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import has_gpu
+
+pytestmark = pytest.mark.gpu
+
+GRID = dict(Nx=16, Ny=33, Nz=16, Lx=2 * np.pi, Lz=np.pi, dt=0.01)
+RE, MEANU, NSTEPS = 2000.0, 1.0, 12
+
+
+@pytest.fixture(scope="module")
+def mod():
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+    torch = pytest.importorskip("torch")
+    from channel import autograd as ag
+    return torch, ag
+
+
+def _cfg(checkpoint):
+    C0 = O.synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=7, amp=5e-2)
+    return {"grid": GRID, "C0": C0, "nsteps": NSTEPS, "checkpoint": checkpoint}
+
+
+def _J(ag, Re, U, checkpoint=4):
+    return ag.primal_objective(GRID, Re, U, _cfg(checkpoint)["C0"], NSTEPS, checkpoint)[0]
+
+
+def test_gradients_match_central_differences(mod):
+    torch, ag = mod
+    Re = torch.tensor(RE, dtype=torch.float64, requires_grad=True)
+    U = torch.tensor(MEANU, dtype=torch.float64, requires_grad=True)
+    cfg = _cfg(4)
+    J = ag.TimeMeanWallShear.apply(Re, U, cfg)
+    J.backward()
+    hR, hU = 0.4, 2e-4
+    fdR = (_J(ag, RE + hR, MEANU) - _J(ag, RE - hR, MEANU)) / (2 * hR)
+    fdU = (_J(ag, RE, MEANU + hU) - _J(ag, RE, MEANU - hU)) / (2 * hU)
+    assert abs(float(Re.grad) - fdR) <= 1e-6 * abs(fdR), (float(Re.grad), fdR)
+    assert abs(float(U.grad) - fdU) <= 1e-6 * abs(fdU), (float(U.grad), fdU)
+    assert cfg["report"]["forward_s"] > 0 and cfg["report"]["backward_s"] > 0
+
+
+def test_checkpoint_spacing_does_not_change_results(mod):
+    torch, ag = mod
+    out = []
+    for ck in (3, 5, NSTEPS):
+        Re = torch.tensor(RE, dtype=torch.float64, requires_grad=True)
+        U = torch.tensor(MEANU, dtype=torch.float64, requires_grad=True)
+        J = ag.TimeMeanWallShear.apply(Re, U, _cfg(ck))
+        J.backward()
+        out.append((float(J.detach()), float(Re.grad), float(U.grad)))
+    for o in out[1:]:
+        for a, b in zip(o, out[0]):
+            assert abs(a - b) <= 1e-12 * abs(b)
