@@ -39,6 +39,7 @@ enum : uint32_t {
 // Grid description plus device tables; passed by value to every kernel.
 struct Grid {
   int Nx, Ny, Nz, X, Q, R, D, pz, px, Qh;  // Qh = (Q+1)/2 plane pairs
+  int split;             // transforms in separate z and x passes (a plane exceeds one block's shared memory)
   double dt, re, flux, norm, cfl1, cfl3;
   const double* Kx;      // [X]
   const double* Kz;      // [Nz]

@@ -146,6 +146,18 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   if (!T.up(qs, &a) || !T.up(rs, &b)) return false;
   T.luQs = const_cast<double*>(a);
   T.luRs = const_cast<double*>(b);
+  // transforms: one block per plane where the plane fits the shared memory,
+  // else separate z / x passes (CHN_SPLIT_TRANSFORMS=1 forces them)
+  int dev = 0, optin = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const char* force = getenv("CHN_SPLIT_TRANSFORMS");
+  g.split = (!fused_transforms_fit(g, optin) || (force && force[0] == '1')) ? 1 : 0;
+  if (solve_smem_bytes(g) > (size_t)optin || recon_smem_bytes(g) > (size_t)optin) {
+    set_error(1, "grid %dx%dx%d: the implicit solve needs %zu bytes of shared memory per block, the device has %d",
+              Nx, Ny, Nz, solve_smem_bytes(g), optin);
+    return false;
+  }
   prepare_kernels(g);
   CK(cudaGetLastError());
   return true;
@@ -181,6 +193,8 @@ struct Work {
   long long vslot = 0, vstride = 0;
   std::vector<char> vel_ok;    // slot i of Pv holds the fields of MIC[3i]
   cpx* icp = nullptr;          // projected IC' of the last coupling, per segment
+  cpx* Zt = nullptr;           // split transforms: spectral-column intermediate for zt_inst instances
+  int zt_inst = 0;
   bool raw_start = false;      // MC came from a laminar start without run-up
   int chain = 0;               // > 0: segments are consecutive windows of one trajectory (DdtArgs::chain)
   std::vector<void*> ptrs;
@@ -236,7 +250,18 @@ struct Work {
            alloc(&Pprev, nseg * psz) && alloc(&Pl, nseg * psz) && alloc(&flow, (size_t)3 * g.Q * plane_size(g)) &&
            alloc(&part, (size_t)nseg * kDotBlocks * 2) && alloc(&r, nseg) && alloc(&cflmax, nseg) &&
            alloc(&status, nseg) && alloc(&step, 4) && alloc(&icp, nseg * csz) &&
-           alloc(&Ft, (size_t)nseg * (3 * (size_t)nsteps + 1)) && alloc_cache(g);
+           alloc(&Ft, (size_t)nseg * (3 * (size_t)nsteps + 1)) && alloc_split(g, nt) && alloc_cache(g);
+  }
+  // split transforms (grids whose plane exceeds a block's shared memory):
+  // room for up to 2 GiB of intermediate, at least one instance
+  bool alloc_split(const Grid& g, size_t nt) {
+    if (!g.split) return true;
+    const size_t per = split_tmp_elems(g);
+    size_t n = ((size_t)2 << 30) / (per * sizeof(cpx));
+    if (n < 1) n = 1;
+    if (n > nt) n = nt;
+    zt_inst = (int)n;
+    return alloc(&Zt, n * per);
   }
   bool alloc_cache(const Grid& g) {
     Pc = nullptr;
@@ -356,6 +381,8 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     }
     if (need_primal_fields) {
       PhysArgs pp{};
+      pp.tmp = w.Zt;
+      pp.tmp_inst = w.zt_inst;
       pp.U = cb(w.Up, w.usz);
       pp.P = Batch<double>{const_cast<double*>(Pprim.base), Pprim.stride};
       pp.pslot = pslot;
@@ -370,6 +397,8 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     }
     if (o.tangents) {
       PhysArgs pt{};
+      pt.tmp = w.Zt;
+      pt.tmp_inst = w.zt_inst;
       pt.U = cb(w.Ut, w.usz);
       pt.P = mbd(w.Pt, w.psz);
       pt.pslot = noslot();
@@ -383,6 +412,8 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
         LK(launch_cache_velocity(g, w.Pt, w.psz, w.ntan, w.couple, w.Pv, w.vstride, w.vslot, w.step, 0, w.status,
                                  w.nseg, st));
       ProdArgs ap{};
+      ap.tmp = w.Zt;
+      ap.tmp_inst = w.zt_inst;
       ap.Pp = Pprim;
       ap.pdiv = w.ntan;
       ap.pslot = pslot;
@@ -395,6 +426,8 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     }
     if (o.adv_primal) {
       ProdArgs ap{};
+      ap.tmp = w.Zt;
+      ap.tmp_inst = w.zt_inst;
       ap.Pp = Pprim;
       ap.pdiv = 1;
       ap.pslot = pslot;
@@ -475,6 +508,8 @@ static bool enqueue_spec2phys(Engine& e, Work& w, Batch<const cpx> C, SlotRef sl
   ra.sdiv = 1;
   LK(launch_recon(g, ra, e.st));
   PhysArgs pa{};
+  pa.tmp = w.Zt;
+  pa.tmp_inst = w.zt_inst;
   pa.U = cb(U, w.usz);
   pa.P = mbd(P, w.psz);
   pa.nfields = 3;
@@ -540,6 +575,8 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
       r.sdiv = 1;
       r.C = cb(w.MC, w.traj);
       PhysArgs p{};
+      p.tmp = w.Zt;
+      p.tmp_inst = w.zt_inst;
       p.nfields = 6;
       p.ninst = w.nseg;
       p.status = nullptr;
@@ -571,6 +608,8 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
     rl.U = mb(w.Ul, w.usz);
     LK(launch_recon(g, rl, st));
     PhysArgs pl{};
+    pl.tmp = w.Zt;
+    pl.tmp_inst = w.zt_inst;
     pl.nfields = 3;
     pl.ninst = w.nseg;
     pl.status = nullptr;
@@ -580,6 +619,8 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
     pl.P = mbd(w.Pl, w.psz);
     LK(launch_phys_inverse(g, pl, st));
     ProdArgs a{};
+    a.tmp = w.Zt;
+    a.tmp_inst = w.zt_inst;
     a.pdiv = 1;
     a.ninst = w.nseg;
     a.status = nullptr;
@@ -751,6 +792,8 @@ static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
     r.sdiv = 1;
     LK(launch_recon(e.T.g, r, e.st));
     PhysArgs p{};
+    p.tmp = w.Zt;
+    p.tmp_inst = w.zt_inst;
     p.U = cb(w.Up, w.usz);
     p.P = mbd(w.Pc, w.cstride);
     p.pslot = noslot();
@@ -1437,6 +1480,8 @@ double c_batch_kernel_ms(int which, int reps) {
       }
       case 1: {
         PhysArgs p{};
+        p.tmp = w.Zt;
+        p.tmp_inst = w.zt_inst;
         p.U = cb(w.Ut, w.usz);
         p.P = mbd(w.Pt, w.psz);
         p.nfields = 6;
@@ -1446,6 +1491,8 @@ double c_batch_kernel_ms(int which, int reps) {
       }
       case 2: {
         ProdArgs ap{};
+        ap.tmp = w.Zt;
+        ap.tmp_inst = w.zt_inst;
         ap.Pp = cbd(w.Pp, w.psz);
         ap.pdiv = w.ntan;
         ap.Pt = cbd(w.Pt, w.psz);
@@ -1472,6 +1519,8 @@ double c_batch_kernel_ms(int which, int reps) {
       }
       case 4: {
         ProdArgs ap{};
+        ap.tmp = w.Zt;
+        ap.tmp_inst = w.zt_inst;
         ap.Pp = cbd(w.Pp, w.psz);
         ap.pdiv = 1;
         ap.Pt = cbd(w.Pl, w.psz);

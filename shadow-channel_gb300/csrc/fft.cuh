@@ -22,6 +22,7 @@ struct FftPlan {
   int n;           // length
   int np;          // number of passes
   int radix[12];   // radix of each pass in execution order
+  bool r3first;    // the radix-3 pass that meets the 3/2-padding band is pass 0 (else the last pass)
 };
 
 __host__ __device__ inline int plan_factor(int m, int* out) {
@@ -43,6 +44,7 @@ __host__ __device__ inline int plan_factor(int m, int* out) {
 __host__ __device__ inline FftPlan make_plan(int n, bool radix3_first) {
   FftPlan p;
   p.n = n;
+  p.r3first = radix3_first;
   int f[12];
   int k = plan_factor(n / 3, f);
   p.np = k + 1;
@@ -152,8 +154,10 @@ __device__ inline cpx* fft_run(const FftPlan& p, cpx* buf0, cpx* buf1, int nb, i
   int Ns = 1;
   for (int s = 0; s < p.np; ++s) {
     const int R = p.radix[s];
-    const bool zero_mid = prune && s == 0 && R == 3;
-    const bool skip_mid = prune && s == p.np - 1 && R == 3 && !zero_mid;
+    // only the designated radix-3 pass meets the zero band; n/3 may hold
+    // further factors of 3 (3Nz/2 = 72), whose passes are not pruned
+    const bool zero_mid = prune && p.r3first && s == 0 && R == 3;
+    const bool skip_mid = prune && !p.r3first && s == p.np - 1 && R == 3;
     switch (R) {
       case 2: stockham_pass<2>(in, out, p.n, Ns, nb, es, bs, tw, sign, false, false); break;
       case 3: stockham_pass<3>(in, out, p.n, Ns, nb, es, bs, tw, sign, zero_mid, skip_mid); break;

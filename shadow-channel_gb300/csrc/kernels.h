@@ -35,6 +35,8 @@ struct PhysArgs {
   double* cflmax;       // per-segment largest CFL number seen (nullable)
   int cfl_check;
   int skip_blocked;
+  cpx* tmp;             // split transforms: intermediate for tmp_inst instances of 6
+  int tmp_inst;         //   spectral columns [6][Q][pz][Nx/2] each
 };
 
 struct ProdArgs {
@@ -46,6 +48,8 @@ struct ProdArgs {
   int ninst;
   const uint32_t* status;
   int sdiv;
+  cpx* tmp;                // split transforms: as PhysArgs::tmp
+  int tmp_inst;
 };
 
 // mean-mode variants (channel/project0.c:153-168, increproject0.c:209-214, adjproject0.c:153-167)
@@ -110,6 +114,10 @@ cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t s
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st);
 
+// split-transform intermediate per instance, in complex elements
+size_t split_tmp_elems(const Grid& g);
+// whether the fused one-block-per-plane transforms fit this device's shared memory
+bool fused_transforms_fit(const Grid& g, int smem_optin);
 size_t recon_smem_bytes(const Grid& g);
 size_t phys_smem_bytes(const Grid& g, bool with_cfl);
 size_t prod_adj_smem_bytes(const Grid& g);

@@ -13,6 +13,8 @@
 // Every transform is an FP64 shared-memory Stockham FFT (fft.cuh).  The x
 // transforms of two real rows share one complex FFT (row pairs packed as
 // a + i b), so no real-to-complex post-processing pass is needed.
+#include <algorithm>
+
 #include "chn_common.cuh"
 #include "fft.cuh"
 #include "kernels.h"
@@ -329,23 +331,324 @@ __global__ void __launch_bounds__(kThreads) k_products_adj(Grid g, ProdArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// split transforms: for grids whose padded plane does not fit one block's
+// shared memory (128x129x128: a 192 x 192 plane), every 2D transform runs as
+// a z pass over chunks of Nx/2 columns and an x pass over chunks of row
+// pairs, with the spectral columns in an HBM intermediate
+// T[inst][c][Q][pz][Nx/2].  Each 1D transform is the same fft_run call on the
+// same data as in the fused kernels, so results are identical bit for bit.
+// ---------------------------------------------------------------------------
+
+static constexpr int kCols = 16;     // z pass: columns per block
+static constexpr int kColsAdj = 8;   // adjoint z pass (keeps 6 spectra per column)
+static constexpr int kPairs = 16;    // x pass: row pairs per block
+
+size_t split_tmp_elems(const Grid& g) { return (size_t)6 * g.Q * g.pz * g.X; }
+
+static size_t split_z_smem(const Grid& g, int ncol, int nkeep) {
+  return ((size_t)g.pz + 2 * (size_t)g.pz * ncol + (size_t)nkeep * g.Nz * ncol) * sizeof(cpx);
+}
+static size_t split_x_smem(const Grid& g, bool with_cfl) {
+  size_t b = ((size_t)g.px + 2 * (size_t)kPairs * g.px) * sizeof(cpx);
+  if (with_cfl) b += (size_t)2 * kPairs * g.px * sizeof(double);
+  return b;
+}
+
+bool fused_transforms_fit(const Grid& g, int smem_optin) {
+  return phys_smem_bytes(g, true) <= (size_t)smem_optin && prod_adj_smem_bytes(g) <= (size_t)smem_optin;
+}
+
+// inverse z pass: spectral fields f0..f0+nf-1 -> T (channel/pass1.c:107-110)
+__global__ void __launch_bounds__(kThreads) k_split_zinv(Grid g, PhysArgs a, int inst0, int nf, cpx* T) {
+  const int y = blockIdx.x, il = blockIdx.y, inst = inst0 + il;
+  const int nck = (g.X + kCols - 1) / kCols;
+  const int f = blockIdx.z / nck, x0 = (blockIdx.z - f * nck) * kCols;
+  const int nc = min(kCols, g.X - x0);
+  if (a.skip_blocked && blocked(a.status, a.sdiv, inst)) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  cpx* tw = reinterpret_cast<cpx*>(smem);
+  cpx* b0 = tw + g.pz;
+  cpx* b1 = b0 + (size_t)g.pz * kCols;
+  for (int i = threadIdx.x; i < g.pz; i += blockDim.x) tw[i] = g.twz[i];
+  const cpx* __restrict__ U = a.U.at(inst);
+  for (int i = threadIdx.x; i < g.pz * nc; i += blockDim.x) {
+    const int zp = i / nc, c = i - zp * nc;
+    const int z = zrow_to_kz(g, zp);
+    b0[i] = z >= 0 ? field_value(g, U, f, z, y, x0 + c) : cpx{0.0, 0.0};
+  }
+  __syncthreads();
+  const FftPlan plan = make_plan(g.pz, true);
+  const cpx* zr = fft_run(plan, b0, b1, nc, nc, 1, tw, +1, true);
+  cpx* Tf = T + (((size_t)il * nf + f) * g.Q + y) * g.pz * g.X;
+  for (int i = threadIdx.x; i < g.pz * nc; i += blockDim.x) {
+    const int zp = i / nc, c = i - zp * nc;
+    Tf[(size_t)zp * g.X + x0 + c] = zr[i];
+  }
+}
+
+// inverse x pass: row pairs of T -> physical rows of P, CFL of the velocity
+// (channel/pass1.c:111-138)
+__global__ void __launch_bounds__(kThreads) k_split_xinv(Grid g, PhysArgs a, int inst0, int nf, const cpx* T) {
+  const int y = blockIdx.x, il = blockIdx.y, inst = inst0 + il;
+  const int npair = (g.pz + 1) / 2;
+  const int p0 = blockIdx.z * kPairs, np = min(kPairs, npair - p0);
+  if (a.skip_blocked && blocked(a.status, a.sdiv, inst)) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  cpx* tw = reinterpret_cast<cpx*>(smem);
+  cpx* b0 = tw + g.px;
+  cpx* b1 = b0 + (size_t)kPairs * g.px;
+  double* cfl = reinterpret_cast<double*>(b1 + (size_t)kPairs * g.px);
+  for (int i = threadIdx.x; i < g.px; i += blockDim.x) tw[i] = g.twx[i];
+  double* __restrict__ P = a.P.at(inst);
+  if (a.pslot.stride) P += (long long)a.pslot.slot() * a.pslot.stride;
+  const FftPlan plan = make_plan(g.px, true);
+  const size_t plane = (size_t)g.pz * g.px;
+  const int r0 = 2 * p0, nr = min(2 * np, g.pz - r0);
+  bool nonfinite = false;
+  for (int f = 0; f < nf; ++f) {
+    const cpx* zr = T + (((size_t)il * nf + f) * g.Q + y) * g.pz * g.X;
+    for (int i = threadIdx.x; i < np * g.px; i += blockDim.x) {
+      const int pl = i / g.px, k = i - pl * g.px;
+      const int ra = 2 * (p0 + pl), rb = ra + 1;
+      cpx Z = {0.0, 0.0};
+      int kk = -1;
+      bool conj = false;
+      if (k < g.X) kk = k;
+      else if (k > g.px - g.X) { kk = g.px - k; conj = true; }
+      if (kk >= 0) {
+        const cpx A = zr[(size_t)ra * g.X + kk];
+        const cpx B = rb < g.pz ? zr[(size_t)rb * g.X + kk] : cpx{0.0, 0.0};
+        if (kk == 0) {
+          Z.re = A.re; Z.im = B.re;
+        } else if (!conj) {
+          Z.re = A.re - B.im; Z.im = A.im + B.re;
+        } else {
+          Z.re = A.re + B.im; Z.im = B.re - A.im;
+        }
+      }
+      b0[i] = Z;
+    }
+    __syncthreads();
+    const cpx* xr = fft_run(plan, b0, b1, np, 1, g.px, tw, +1, true);
+    double* Pf = P + ((size_t)f * g.Q + y) * plane;
+    for (int i = threadIdx.x; i < nr * g.px; i += blockDim.x) {
+      const int rl = i / g.px, xp = i - rl * g.px;
+      const cpx c = xr[(rl >> 1) * g.px + xp];
+      const double v = (rl & 1) ? c.im : c.re;
+      Pf[(size_t)(r0 + rl) * g.px + xp] = v;
+      nonfinite |= !isfinite(v);
+      if (a.cfl_check && f < 3) {
+        const double t = fabs(v) * (f == 0 ? g.cfl1 : (f == 1 ? g.cfl2[y] : g.cfl3));
+        cfl[i] = f == 0 ? t : cfl[i] + t;
+      }
+    }
+    __syncthreads();
+  }
+  if (nonfinite && a.status) atomicOr(&a.status[inst / a.sdiv], ST_NONFINITE);
+  if (a.cfl_check) {
+    __shared__ double red[kThreads];
+    double m = 0.0;
+    for (int i = threadIdx.x; i < nr * g.px; i += blockDim.x) m = fmax(m, cfl[i]);
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const double c = red[0] * g.dt;
+      if (a.cflmax) atomicMax(reinterpret_cast<unsigned long long*>(&a.cflmax[inst / a.sdiv]),
+                              (unsigned long long)__double_as_longlong(c));
+      if (c >= 2.8) atomicOr(&a.status[inst / a.sdiv], ST_CFL);
+    }
+  }
+}
+
+// product component q at flat offset o of plane y: mode 0 primal, 1 tangent,
+// 2 adjoint (q = 0..2 S = u x lambda, 3..5 T = lambda x w)
+__device__ __forceinline__ double split_product(int mode, const double* __restrict__ P,
+                                                const double* __restrict__ I, size_t fs, size_t o, int q) {
+  if (mode == 0) return prod_primal(P, fs, o, q);
+  if (mode == 1) return prod_tangent(P, I, fs, o, q);
+  const double u = P[o], v = P[fs + o], w = P[2 * fs + o];
+  const double wz = P[3 * fs + o], wx = P[4 * fs + o], wy = P[5 * fs + o];
+  const double lx = I[o], ly = I[fs + o], lz = I[2 * fs + o];
+  switch (q) {
+    case 0: return v * lz - w * ly;
+    case 1: return w * lx - u * lz;
+    case 2: return u * ly - v * lx;
+    case 3: return ly * wz - lz * wy;
+    case 4: return lz * wx - lx * wz;
+    default: return lx * wy - ly * wx;
+  }
+}
+
+// forward x pass: products of row pairs, x transform, kept bins -> T
+// (channel/pass1.c:312-330, pass2.c:474-500)
+__global__ void __launch_bounds__(kThreads) k_split_xfwd(Grid g, ProdArgs a, int mode, int inst0, cpx* T) {
+  const int y = blockIdx.x, il = blockIdx.y, inst = inst0 + il;
+  const int npair = (g.pz + 1) / 2;
+  const int p0 = blockIdx.z * kPairs, np = min(kPairs, npair - p0);
+  if (blocked(a.status, a.sdiv, inst)) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  cpx* tw = reinterpret_cast<cpx*>(smem);
+  cpx* b0 = tw + g.px;
+  cpx* b1 = b0 + (size_t)kPairs * g.px;
+  for (int i = threadIdx.x; i < g.px; i += blockDim.x) tw[i] = g.twx[i];
+  const size_t plane = (size_t)g.pz * g.px, fs = (size_t)g.Q * plane;
+  const double* __restrict__ Pp = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane +
+                                  (a.pslot.stride ? (long long)a.pslot.slot() * a.pslot.stride : 0LL);
+  const double* __restrict__ Pt = a.Pt.base ? a.Pt.at(inst) + (size_t)y * plane : nullptr;
+  const FftPlan plan = make_plan(g.px, false);
+  const int ncomp = mode == 2 ? 6 : 3;
+  const double hn = 0.5 * g.norm;
+  __syncthreads();
+  for (int q = 0; q < ncomp; ++q) {
+    for (int i = threadIdx.x; i < np * g.px; i += blockDim.x) {
+      const int pl = i / g.px, xp = i - pl * g.px;
+      const int ra = 2 * (p0 + pl);
+      const size_t oa = (size_t)ra * g.px + xp, ob = oa + g.px;
+      cpx z;
+      z.re = split_product(mode, Pp, Pt, fs, oa, q);
+      z.im = ra + 1 < g.pz ? split_product(mode, Pp, Pt, fs, ob, q) : 0.0;
+      b0[i] = z;
+    }
+    __syncthreads();
+    const cpx* xr = fft_run(plan, b0, b1, np, 1, g.px, tw, -1, true);
+    cpx* Tq = T + (((size_t)il * ncomp + q) * g.Q + y) * g.pz * g.X;
+    for (int i = threadIdx.x; i < np * g.X; i += blockDim.x) {
+      const int pl = i / g.X, k = i - pl * g.X;
+      const cpx Zk = xr[pl * g.px + k];
+      const cpx Zn = xr[pl * g.px + (k == 0 ? 0 : g.px - k)];
+      cpx A, B;
+      A.re = (Zk.re + Zn.re) * hn;
+      A.im = (Zk.im - Zn.im) * hn;
+      B.re = (Zk.im + Zn.im) * hn;
+      B.im = (Zn.re - Zk.re) * hn;
+      const int ra = 2 * (p0 + pl);
+      Tq[(size_t)ra * g.X + k] = A;
+      if (ra + 1 < g.pz) Tq[(size_t)(ra + 1) * g.X + k] = B;
+    }
+    __syncthreads();
+  }
+}
+
+// forward z pass: columns of T, z transform, truncation -> H; the adjoint
+// assembles H = -T + (i k) x S and keeps S_x, S_z (channel/pass1.c:331-371,
+// pass2.c:501-566)
+__global__ void __launch_bounds__(kThreads) k_split_zfwd(Grid g, ProdArgs a, int mode, int inst0, const cpx* T) {
+  const int y = blockIdx.x, il = blockIdx.y, inst = inst0 + il;
+  const int ncol = mode == 2 ? kColsAdj : kCols;
+  const int x0 = blockIdx.z * ncol, nc = min(ncol, g.X - x0);
+  if (blocked(a.status, a.sdiv, inst)) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  cpx* tw = reinterpret_cast<cpx*>(smem);
+  cpx* b0 = tw + g.pz;
+  cpx* b1 = b0 + (size_t)g.pz * ncol;
+  cpx* keep = b1 + (size_t)g.pz * ncol;  // adjoint: [6][Nz][ncol]
+  for (int i = threadIdx.x; i < g.pz; i += blockDim.x) tw[i] = g.twz[i];
+  cpx* __restrict__ H = a.H.at(inst);
+  const FftPlan plan = make_plan(g.pz, false);
+  const int ncomp = mode == 2 ? 6 : 3;
+  for (int q = 0; q < ncomp; ++q) {
+    const cpx* Tq = T + (((size_t)il * ncomp + q) * g.Q + y) * g.pz * g.X;
+    for (int i = threadIdx.x; i < g.pz * nc; i += blockDim.x) {
+      const int zp = i / nc, c = i - zp * nc;
+      b0[i] = Tq[(size_t)zp * g.X + x0 + c];
+    }
+    __syncthreads();
+    const cpx* zr = fft_run(plan, b0, b1, nc, nc, 1, tw, -1, true);
+    for (int i = threadIdx.x; i < g.pz * nc; i += blockDim.x) {
+      const int zp = i / nc, c = i - zp * nc;
+      const int z = zrow_to_kz(g, zp);
+      if (z < 0) continue;
+      if (mode == 2) keep[((size_t)q * g.Nz + z) * ncol + c] = zr[i];
+      else H[(((size_t)z * 5 + q) * g.Q + y) * g.X + x0 + c] = zr[i];
+    }
+    __syncthreads();
+  }
+  if (mode != 2) return;
+  for (int i = threadIdx.x; i < g.Nz * nc; i += blockDim.x) {
+    const int z = i / nc, c = i - z * nc, x = x0 + c;
+    if (z == g.Nz / 2) continue;
+    const double kx = g.Kx[x], kz = g.Kz[z];
+    auto K = [&](int q) { return keep[((size_t)q * g.Nz + z) * ncol + c]; };
+    const cpx Sx = K(0), Sy = K(1), Sz = K(2), Tx = K(3), Ty = K(4), Tz = K(5);
+    cpx hx, hy, hz;
+    hx.re = -Tx.re - kz * Sy.im;
+    hx.im = -Tx.im + kz * Sy.re;
+    hy.re = -Ty.re + kz * Sx.im - kx * Sz.im;
+    hy.im = -Ty.im - kz * Sx.re + kx * Sz.re;
+    hz.re = -Tz.re + kx * Sy.im;
+    hz.im = -Tz.im - kx * Sy.re;
+    auto slot = [&](int s) -> cpx& { return H[(((size_t)z * 5 + s) * g.Q + y) * g.X + x]; };
+    slot(0) = hz;
+    slot(1) = hx;
+    slot(2) = hy;
+    slot(3) = Sx;
+    slot(4) = Sz;
+  }
+}
+
+// instance chunks that fit the intermediate
+template <typename F>
+static cudaError_t split_chunks(int ninst, int cap, F&& body) {
+  if (cap <= 0) return cudaErrorInvalidValue;
+  for (int i0 = 0; i0 < ninst; i0 += cap) {
+    const cudaError_t e = body(i0, min(cap, ninst - i0));
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+static cudaError_t split_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t st) {
+  if (!a.tmp) return cudaErrorInvalidValue;
+  const int cap = a.tmp_inst * 6 / a.nfields;
+  return split_chunks(a.ninst, cap, [&](int i0, int n) {
+    const int nck = (g.X + kCols - 1) / kCols, npc = ((g.pz + 1) / 2 + kPairs - 1) / kPairs;
+    k_split_zinv<<<dim3(g.Q, n, a.nfields * nck), kThreads, split_z_smem(g, kCols, 0), st>>>(g, a, i0, a.nfields,
+                                                                                             a.tmp);
+    k_split_xinv<<<dim3(g.Q, n, npc), kThreads, split_x_smem(g, a.cfl_check != 0), st>>>(g, a, i0, a.nfields,
+                                                                                          a.tmp);
+    return cudaGetLastError();
+  });
+}
+
+static cudaError_t split_products(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
+  if (!a.tmp) return cudaErrorInvalidValue;
+  const int ncomp = mode == 2 ? 6 : 3;
+  const int cap = a.tmp_inst * 6 / ncomp;
+  return split_chunks(a.ninst, cap, [&](int i0, int n) {
+    const int npc = ((g.pz + 1) / 2 + kPairs - 1) / kPairs;
+    const int ncol = mode == 2 ? kColsAdj : kCols, nck = (g.X + ncol - 1) / ncol;
+    k_split_xfwd<<<dim3(g.Q, n, npc), kThreads, split_x_smem(g, false), st>>>(g, a, mode, i0, a.tmp);
+    k_split_zfwd<<<dim3(g.Q, n, nck), kThreads, split_z_smem(g, ncol, mode == 2 ? 6 : 0), st>>>(g, a, mode, i0,
+                                                                                                 a.tmp);
+    return cudaGetLastError();
+  });
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 
 cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
+  if (g.split) return split_phys_inverse(g, a, st);
   k_phys_inverse<<<dim3(g.Q, a.ninst), kThreads, phys_smem_bytes(g, a.cfl_check != 0), st>>>(g, a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
+  if (g.split) return split_products(g, a, a.Pt.base ? 1 : 0, st);
   k_products_fwd<<<dim3(g.Q, a.ninst), kThreads, phys_smem_bytes(g, false), st>>>(g, a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
+  if (g.split) return split_products(g, a, 2, st);
   k_products_adj<<<dim3(g.Q, a.ninst), kThreads, prod_adj_smem_bytes(g), st>>>(g, a);
   return cudaGetLastError();
 }
@@ -353,9 +656,19 @@ cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t s
 void prepare_recon_solve(const Grid& g);
 
 void prepare_kernels(const Grid& g) {
-  cudaFuncSetAttribute(k_phys_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)phys_smem_bytes(g, true));
-  cudaFuncSetAttribute(k_products_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)phys_smem_bytes(g, false));
-  cudaFuncSetAttribute(k_products_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prod_adj_smem_bytes(g));
+  if (g.split) {
+    cudaFuncSetAttribute(k_split_zinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_z_smem(g, kCols, 0));
+    cudaFuncSetAttribute(k_split_xinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_x_smem(g, true));
+    cudaFuncSetAttribute(k_split_xfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_x_smem(g, false));
+    cudaFuncSetAttribute(k_split_zfwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)std::max(split_z_smem(g, kCols, 0), split_z_smem(g, kColsAdj, 6)));
+  } else {
+    cudaFuncSetAttribute(k_phys_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)phys_smem_bytes(g, true));
+    cudaFuncSetAttribute(k_products_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)phys_smem_bytes(g, false));
+    cudaFuncSetAttribute(k_products_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prod_adj_smem_bytes(g));
+  }
   prepare_recon_solve(g);
 }
 
