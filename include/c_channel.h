@@ -190,6 +190,26 @@ double c_pipe_peak_tflops(int kind);
    error (c_last_error_message). */
 int c_spec2phys_noalloc(const chn_complex *C_dev, double *flow_dev);
 
+/* Uneven batches (no reference counterpart): n instances, each with its own
+   grid, Re, flux and dt, advanced together by the same kernel launches.
+   Host arrays are packed instance after instance, each in the reference
+   layout of its own grid (c_multi_coef_elems(i) complex elements; tangents:
+   the ntan arrays of an instance one after another).  Same semantics as the
+   c_batch_* calls per instance; the adjoint's coupling strength is scaled by
+   each instance's own dt. */
+int c_multi_init(int n, const int *Nx, const int *Ny, const int *Nz,
+                 const double *Lx, const double *Lz, const double *Re,
+                 const double *flux, const double *dt, int nsteps, int ntan,
+                 int couple);
+int c_multi_destroy(void);
+long long c_multi_coef_elems(int i);
+int c_multi_primal(int ru_steps, chn_complex *C);
+int c_multi_forward(int start_step, int end_step, chn_complex *C,
+                    chn_complex *IC, const int *inhomo);
+int c_multi_adjoint(int start_step, int end_step, chn_complex *AC,
+                    double strength);
+int c_multi_getsoln(int i, int i_step, chn_complex *out);
+
 /* Objectives and statistics of the stored trajectories, computed on the
    device from the coefficients (no reference C counterpart: the reference
    averages spec2phys output in Python, channel/__init__.py:217-299 and

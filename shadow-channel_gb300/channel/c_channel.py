@@ -109,6 +109,22 @@ _lib.c_batch_kernel_ms.restype = _d
 _lib.c_spec2phys_noalloc.argtypes = [_vp, _vp]
 _lib.c_spec2phys_noalloc.restype = _i
 
+_ipc = ctypes.POINTER(ctypes.c_int)
+_dpc = ctypes.POINTER(ctypes.c_double)
+_lib.c_multi_init.argtypes = [_i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i]
+_lib.c_multi_init.restype = _i
+_lib.c_multi_destroy.argtypes = []
+_lib.c_multi_destroy.restype = _i
+_lib.c_multi_coef_elems.argtypes = [_i]
+_lib.c_multi_coef_elems.restype = ctypes.c_longlong
+_lib.c_multi_primal.argtypes = [_i, _vp]
+_lib.c_multi_primal.restype = _i
+_lib.c_multi_forward.argtypes = [_i, _i, _vp, _vp, _vp]
+_lib.c_multi_forward.restype = _i
+_lib.c_multi_adjoint.argtypes = [_i, _i, _vp, _d]
+_lib.c_multi_adjoint.restype = _i
+_lib.c_multi_getsoln.argtypes = [_i, _i, _vp]
+_lib.c_multi_getsoln.restype = _i
 _lib.c_tangent_forcing.argtypes = [_i, _i, _vp, _i, _i, _i, _i, _i]
 _lib.c_tangent_forcing.restype = None
 _lib.c_mean_profile.argtypes = [_i, _i, _i, _i, _vp]

@@ -101,4 +101,26 @@ __device__ __forceinline__ cpx cmul(cpx a, cpx b) {
   return r;
 }
 
+// Uneven batches: a MULTI kernel takes its instance's grid (sizes and
+// tables) from a device array, staged once per block in shared memory; the
+// launch is sized for the largest grid (kernel argument g0) and blocks beyond
+// their own instance's range return.  Non-MULTI kernels use g0 directly.
+#define CHN_INSTANCE_GRID(g0, grids, inst)        \
+  __shared__ Grid chn_sg_;                        \
+  if (MULTI) {                                    \
+    if (threadIdx.x == 0) chn_sg_ = (grids)[inst]; \
+    __syncthreads();                              \
+  }                                               \
+  const Grid& g = MULTI ? chn_sg_ : (g0)
+
+// Allow a kernel the device's opt-in shared memory per block, less what it
+// declares statically.
+template <typename K>
+inline cudaError_t allow_max_smem(K kernel, int optin) {
+  cudaFuncAttributes fa{};
+  cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+}
+
 }  // namespace chn

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -193,6 +194,7 @@ struct Work {
   long long vslot = 0, vstride = 0;
   std::vector<char> vel_ok;    // slot i of Pv holds the fields of MIC[3i]
   cpx* icp = nullptr;          // projected IC' of the last coupling, per segment
+  const Grid* gdev = nullptr;  // uneven batch: grid of each segment (device array); null: one grid
   cpx* Zt = nullptr;           // split transforms: spectral-column intermediate for zt_inst instances
   int zt_inst = 0;
   bool raw_start = false;      // MC came from a laminar start without run-up
@@ -356,6 +358,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     const bool need_primal_fields = o.adv_primal || !use_cache;
     if (need_primal_fields) {
       ReconArgs rp{};
+      rp.grids = w.gdev;
       rp.ninst = w.nseg;
       rp.U = mb(w.Up, w.usz);
       rp.status = w.status;
@@ -371,6 +374,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     }
     if (o.tangents) {
       ReconArgs rt{};
+      rt.grids = w.gdev;
       rt.ninst = nt;
       rt.C = cb(w.St, w.csz);
       rt.slot = noslot();
@@ -381,6 +385,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     }
     if (need_primal_fields) {
       PhysArgs pp{};
+      pp.grids = w.gdev;
       pp.tmp = w.Zt;
       pp.tmp_inst = w.zt_inst;
       pp.U = cb(w.Up, w.usz);
@@ -397,6 +402,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     }
     if (o.tangents) {
       PhysArgs pt{};
+      pt.grids = w.gdev;
       pt.tmp = w.Zt;
       pt.tmp_inst = w.zt_inst;
       pt.U = cb(w.Ut, w.usz);
@@ -412,6 +418,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
         LK(launch_cache_velocity(g, w.Pt, w.psz, w.ntan, w.couple, w.Pv, w.vstride, w.vslot, w.step, 0, w.status,
                                  w.nseg, st));
       ProdArgs ap{};
+      ap.grids = w.gdev;
       ap.tmp = w.Zt;
       ap.tmp_inst = w.zt_inst;
       ap.Pp = Pprim;
@@ -426,6 +433,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     }
     if (o.adv_primal) {
       ProdArgs ap{};
+      ap.grids = w.gdev;
       ap.tmp = w.Zt;
       ap.tmp_inst = w.zt_inst;
       ap.Pp = Pprim;
@@ -441,6 +449,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     // the primal solve first: tangent Re forcing reads the state it stores
     if (o.adv_primal) {
       SolveArgs sa{};
+      sa.grids = w.gdev;
       sa.H = cb(w.Up, w.usz);
       sa.Hprev = cb(nullptr, 0);
       sa.Cc = mb(w.Cp, w.csz);
@@ -463,6 +472,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
     }
     if (o.tangents) {
       SolveArgs sa{};
+      sa.grids = w.gdev;
       sa.H = cb(w.Ut, w.usz);
       sa.Hprev = cb(nullptr, 0);
       sa.Cc = mb(w.Ct, w.csz);
@@ -500,6 +510,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
 static bool enqueue_spec2phys(Engine& e, Work& w, Batch<const cpx> C, SlotRef slot, cpx* U, double* P, int nseg) {
   const Grid& g = e.T.g;
   ReconArgs ra{};
+  ra.grids = w.gdev;
   ra.C = C;
   ra.slot = slot;
   ra.U = mb(U, w.usz);
@@ -508,6 +519,7 @@ static bool enqueue_spec2phys(Engine& e, Work& w, Batch<const cpx> C, SlotRef sl
   ra.sdiv = 1;
   LK(launch_recon(g, ra, e.st));
   PhysArgs pa{};
+  pa.grids = w.gdev;
   pa.tmp = w.Zt;
   pa.tmp_inst = w.zt_inst;
   pa.U = cb(U, w.usz);
@@ -527,7 +539,7 @@ static bool enqueue_spec2phys(Engine& e, Work& w, Batch<const cpx> C, SlotRef sl
 // primal and velocity caches instead of transforming dCdt and MIC[3 i_step].
 static bool enqueue_coupling(Engine& e, Work& w, int add, double coef, bool cached) {
   const Grid& g = e.T.g;
-  DdtArgs d{w.MC, w.traj, w.step, add, w.nseg, w.chain};
+  DdtArgs d{w.MC, w.traj, w.step, add, w.nseg, w.chain, w.gdev};
   LK(launch_ddt_diff(g, d, w.dC, e.st));
   const SlotRef icslot{w.step, 3, 3 * add, (long long)w.csz};
   if (cached) {
@@ -536,10 +548,10 @@ static bool enqueue_coupling(Engine& e, Work& w, int add, double coef, bool cach
   } else {
     if (!enqueue_spec2phys(e, w, cb(w.dC, w.csz), noslot(), w.Uprev, w.Pprev, w.nseg)) return false;
     if (!enqueue_spec2phys(e, w, cb(w.MIC, w.traj), icslot, w.Ul, w.Pl, w.nseg)) return false;
-    LK(launch_ddt_dots(g, cbd(w.Pprev, w.psz), cbd(w.Pl, w.psz), w.part, Work::kDotBlocks, w.nseg, e.st));
+    LK(launch_ddt_dots(g, cbd(w.Pprev, w.psz), cbd(w.Pl, w.psz), w.part, Work::kDotBlocks, w.nseg, e.st, w.gdev));
   }
   LK(launch_ddt_apply(g, w.part, Work::kDotBlocks, w.nseg, cb(w.MIC, w.traj), icslot, mb(w.icp, w.csz),
-                      cb(w.dC, w.csz), w.r, coef != 0.0 ? mb(w.Ca, w.csz) : mb(nullptr, 0), coef, e.st));
+                      cb(w.dC, w.csz), w.r, coef != 0.0 ? mb(w.Ca, w.csz) : mb(nullptr, 0), coef, e.st, w.gdev));
   return true;
 }
 
@@ -551,7 +563,7 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
   const Grid& g = e.T.g;
   cudaStream_t st = e.st;
   const double coef = 0.5 * strength_dt;
-  if (strength_dt != 0.0) LK(launch_sub_scaled(g, cb(w.icp, w.csz), mb(w.Ca, w.csz), coef, w.nseg, st));
+  if (strength_dt != 0.0) LK(launch_sub_scaled(g, cb(w.icp, w.csz), mb(w.Ca, w.csz), coef, w.nseg, st, w.gdev));
   // Without the cache the primal fields of substage k's previous state are the
   // current state of substage k + 1, so they are computed once: buffers A/B
   // alternate (cur: A, B, A; prev: B, A).
@@ -570,11 +582,13 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
       Pcur = cbd(cur, w.psz);
       Pprv = cbd(prv, w.psz);
       ReconArgs r{};
+      r.grids = w.gdev;
       r.ninst = w.nseg;
       r.status = nullptr;
       r.sdiv = 1;
       r.C = cb(w.MC, w.traj);
       PhysArgs p{};
+      p.grids = w.gdev;
       p.tmp = w.Zt;
       p.tmp_inst = w.zt_inst;
       p.nfields = 6;
@@ -600,6 +614,7 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
       }
     }
     ReconArgs rl{};
+    rl.grids = w.gdev;
     rl.ninst = w.nseg;
     rl.status = nullptr;
     rl.sdiv = 1;
@@ -608,6 +623,7 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
     rl.U = mb(w.Ul, w.usz);
     LK(launch_recon(g, rl, st));
     PhysArgs pl{};
+    pl.grids = w.gdev;
     pl.tmp = w.Zt;
     pl.tmp_inst = w.zt_inst;
     pl.nfields = 3;
@@ -619,6 +635,7 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
     pl.P = mbd(w.Pl, w.psz);
     LK(launch_phys_inverse(g, pl, st));
     ProdArgs a{};
+    a.grids = w.gdev;
     a.tmp = w.Zt;
     a.tmp_inst = w.zt_inst;
     a.pdiv = 1;
@@ -637,6 +654,7 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
       LK(launch_products_adj(g, a, st));
     }
     SolveArgs s{};
+    s.grids = w.gdev;
     s.H = cb(w.Up, w.usz);
     s.Hprev = cb(w.Uprev, w.usz);
     s.Cc = mb(w.Ca, w.csz);
@@ -784,6 +802,7 @@ static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
     // substage ran on; the tangent and adjoint sweeps rebuild MC[0] instead
     // (channel/channel.c:496-514), so slot 0 gets the fields of MC[0]
     ReconArgs r{};
+    r.grids = w.gdev;
     r.C = cb(w.MC, w.traj);
     r.slot = noslot();
     r.U = mb(w.Up, w.usz);
@@ -792,6 +811,7 @@ static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
     r.sdiv = 1;
     LK(launch_recon(e.T.g, r, e.st));
     PhysArgs p{};
+    p.grids = w.gdev;
     p.tmp = w.Zt;
     p.tmp_inst = w.zt_inst;
     p.U = cb(w.Up, w.usz);
@@ -877,7 +897,8 @@ static bool op_adjoint(Engine& e, Work& w, int start, int end, const cpx* AC, do
   CK(cudaMemcpyAsync(w.Ca, AC, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
   CK(cudaMemcpyAsync(w.Sa, AC, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
   if (!reset_status(e, w) || !set_step(e, w, start)) return false;
-  const double sdt = strength * e.T.g.dt;  // channel/channel.c:619
+  // channel/channel.c:619; an uneven batch scales by each segment's dt on the device
+  const double sdt = w.gdev ? strength : strength * e.T.g.dt;
   const bool cached = w.cached(3 * end, 3 * start);
   bool cpl_cached = true;
   for (int i = end; i < start; ++i) cpl_cached = cpl_cached && w.coupling_cached(i);
@@ -921,7 +942,7 @@ static double ddt_project_single(Engine& e, int i_step, cpx* IC_host) {
   const Grid& g = e.T.g;
   const size_t bytes = sizeof(cpx) * w.csz;
   if (!h2d(e, w.io, IC_host, bytes)) return NAN;
-  DdtArgs d{w.MC, w.traj, nullptr, i_step, 1, 0};
+  DdtArgs d{w.MC, w.traj, nullptr, i_step, 1, 0, nullptr};
   ++g_launches;
   if (launch_ddt_diff(g, d, w.dC, e.st) != cudaSuccess) return NAN;
   if (!enqueue_spec2phys(e, w, cb(w.dC, w.csz), noslot(), w.Uprev, w.Pprev, 1)) return NAN;
@@ -977,11 +998,11 @@ bool engine_traj(int batch, int inc, const cpx** base, long long* traj_stride, i
 // primal (channel/channel.c:704-780), in place; r[s] = num/den
 static bool batch_ddt_project(Engine& e, Work& w, int i_step, cpx* V, double* r) {
   const Grid& g = e.T.g;
-  DdtArgs d{w.MC, w.traj, nullptr, i_step, w.nseg, w.chain};
+  DdtArgs d{w.MC, w.traj, nullptr, i_step, w.nseg, w.chain, w.gdev};
   LK(launch_ddt_diff(g, d, w.dC, e.st));
   if (!enqueue_spec2phys(e, w, cb(w.dC, w.csz), noslot(), w.Uprev, w.Pprev, w.nseg)) return false;
   if (!enqueue_spec2phys(e, w, cb(V, w.csz), noslot(), w.Ul, w.Pl, w.nseg)) return false;
-  LK(launch_ddt_dots(g, cbd(w.Pprev, w.psz), cbd(w.Pl, w.psz), w.part, Work::kDotBlocks, w.nseg, e.st));
+  LK(launch_ddt_dots(g, cbd(w.Pprev, w.psz), cbd(w.Pl, w.psz), w.part, Work::kDotBlocks, w.nseg, e.st, w.gdev));
   LK(launch_ddt_apply(g, w.part, Work::kDotBlocks, w.nseg, cb(V, w.csz), noslot(), mb(V, w.csz), cb(w.dC, w.csz),
                       r ? r : w.r, mb(nullptr, 0), 0.0, e.st));
   return true;
@@ -1448,6 +1469,208 @@ int c_batch_getincresoln(int seg, int i_step, chn_complex* out) {
   return d2h(*E, out, w.MIC + (size_t)seg * w.traj + (size_t)3 * i_step * w.csz, sizeof(cpx) * w.csz) ? 0 : -1;
 }
 
+// ---------------------------------------------------------------------------
+// Uneven batches: n instances, each with its own grid, Re, flux and dt, all
+// advanced by the same launches (kernels in their MULTI form read their
+// instance's grid from a device array; buffers are padded to the largest
+// grid).  Host arrays are packed: instance after instance, each in the
+// reference layout [Nz][2][Ny-2][Nx/2] of its own grid (tangents: the ntan
+// arrays of an instance one after another).
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace chn {
+struct Multi {
+  Engine e;                    // e.T.g: launch sizes of the largest grid; e.batch: the working set
+  std::vector<DevTables> tabs; // per instance
+  std::vector<size_t> csz;     // per-instance coefficient elements
+  std::vector<size_t> off;     // packed offsets
+  Grid* gdev = nullptr;
+  void release() {
+    if (e.st) cudaStreamSynchronize(e.st);
+    if (e.have_batch) e.batch.release();
+    for (DevTables& t : tabs) t.release();
+    tabs.clear();
+    if (gdev) cudaFree(gdev);
+    gdev = nullptr;
+    if (e.st) cudaStreamDestroy(e.st);
+    e.st = nullptr;
+  }
+};
+static Multi* MX = nullptr;
+
+static bool multi_ready(const char* fn) {
+  if (!MX) {
+    set_error(-2, "%s called before c_multi_init", fn);
+    return false;
+  }
+  return true;
+}
+
+// packed host <-> padded device, one copy per instance
+static bool multi_h2d(cpx* dev, const chn_complex* host, int per) {
+  Multi& m = *MX;
+  Work& w = m.e.batch;
+  CK(cudaMemsetAsync(dev, 0, sizeof(cpx) * w.csz * (size_t)w.nseg * per, m.e.st));
+  for (int i = 0; i < w.nseg; ++i)
+    for (int t = 0; t < per; ++t)
+      CK(cudaMemcpyAsync(dev + ((size_t)i * per + t) * w.csz,
+                         reinterpret_cast<const cpx*>(host) + m.off[i] * per + (size_t)t * m.csz[i],
+                         sizeof(cpx) * m.csz[i], cudaMemcpyHostToDevice, m.e.st));
+  return true;
+}
+
+static bool multi_d2h(chn_complex* host, const cpx* dev, int per) {
+  Multi& m = *MX;
+  Work& w = m.e.batch;
+  for (int i = 0; i < w.nseg; ++i)
+    for (int t = 0; t < per; ++t)
+      CK(cudaMemcpyAsync(reinterpret_cast<cpx*>(host) + m.off[i] * per + (size_t)t * m.csz[i],
+                         dev + ((size_t)i * per + t) * w.csz, sizeof(cpx) * m.csz[i], cudaMemcpyDeviceToHost,
+                         m.e.st));
+  CK(cudaStreamSynchronize(m.e.st));
+  return true;
+}
+}  // namespace chn
+
+extern "C" {
+
+int c_multi_destroy(void) {
+  if (!MX) return 0;
+  MX->release();
+  delete MX;
+  MX = nullptr;
+  return 0;
+}
+
+int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const double* Lx, const double* Lz,
+                 const double* Re, const double* flux, const double* dt, int nsteps, int ntan, int couple) {
+  c_multi_destroy();
+  if (n <= 0 || nsteps < 0 || ntan < 0 || ntan > 32 || (ntan > 0 && (couple < 0 || couple >= ntan)) || !Nx ||
+      !Ny || !Nz || !Lx || !Lz || !Re || !flux || !dt) {
+    set_error(-4, "c_multi_init: need n > 0, nsteps >= 0, 0 <= ntan <= 32, 0 <= couple < ntan and all arrays");
+    return -4;
+  }
+  Multi* m = new Multi();
+  MX = m;
+  if (cudaStreamCreateWithFlags(&m->e.st, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error(-1, "no CUDA device available");
+    c_multi_destroy();
+    return -1;
+  }
+  m->tabs.resize(n);
+  size_t acc = 0;
+  int big = 0;
+  for (int i = 0; i < n; ++i) {
+    if (!build_device_tables(m->tabs[i], Nx[i], Ny[i], Nz[i], Lx[i], Lz[i], Re[i], flux[i], dt[i])) {
+      const int rc = g_status ? g_status : -1;
+      c_multi_destroy();
+      return rc;
+    }
+    const size_t c = coef_size(m->tabs[i].g);
+    if (c > coef_size(m->tabs[big].g)) big = i;
+    m->csz.push_back(c);
+    m->off.push_back(acc);
+    acc += c;
+  }
+  // launch sizes: the maxima over the instances (tables of the largest one)
+  Grid gmax = m->tabs[big].g;
+  for (int i = 0; i < n; ++i) {
+    const Grid& g = m->tabs[i].g;
+    gmax.Nx = std::max(gmax.Nx, g.Nx); gmax.Ny = std::max(gmax.Ny, g.Ny); gmax.Nz = std::max(gmax.Nz, g.Nz);
+    gmax.X = std::max(gmax.X, g.X); gmax.Q = std::max(gmax.Q, g.Q); gmax.R = std::max(gmax.R, g.R);
+    gmax.D = std::max(gmax.D, g.D); gmax.pz = std::max(gmax.pz, g.pz); gmax.px = std::max(gmax.px, g.px);
+    gmax.Qh = std::max(gmax.Qh, g.Qh);
+  }
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const char* force = getenv("CHN_SPLIT_TRANSFORMS");
+  gmax.split = (!fused_transforms_fit(gmax, optin) || (force && force[0] == '1')) ? 1 : 0;
+  if (solve_smem_bytes(gmax) > (size_t)optin) {
+    set_error(1, "c_multi_init: the largest grid needs more shared memory than the device has");
+    c_multi_destroy();
+    return 1;
+  }
+  std::vector<Grid> gs(n);
+  for (int i = 0; i < n; ++i) {
+    gs[i] = m->tabs[i].g;
+    gs[i].split = gmax.split;
+  }
+  if (cudaMalloc(&m->gdev, sizeof(Grid) * n) != cudaSuccess ||
+      cudaMemcpy(m->gdev, gs.data(), sizeof(Grid) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+    set_error(-1, "c_multi_init: device allocation failed");
+    c_multi_destroy();
+    return -1;
+  }
+  m->e.T.g = gmax;
+  m->e.nsteps = nsteps;
+  if (!m->e.batch.create(gmax, n, ntan, nsteps, couple)) {
+    const int rc = g_status ? g_status : -1;
+    c_multi_destroy();
+    return rc;
+  }
+  m->e.batch.gdev = m->gdev;
+  m->e.have_batch = true;
+  g_status = 0;
+  g_msg.clear();
+  return 0;
+}
+
+long long c_multi_coef_elems(int i) {
+  if (!MX || i < 0 || i >= (int)MX->csz.size()) return -1;
+  return (long long)MX->csz[i];
+}
+
+int c_multi_primal(int ru_steps, chn_complex* C) {
+  if (!multi_ready("c_multi_primal")) return g_status;
+  if (!C) {
+    set_error(-4, "c_multi_primal: an uneven batch starts from given states");
+    return -4;
+  }
+  Work& w = MX->e.batch;
+  if (!multi_h2d(w.dC, C, 1)) return -1;
+  if (!op_primal(MX->e, w, ru_steps, w.dC)) return g_status;
+  if (!multi_d2h(C, w.Cp, 1)) return -1;
+  return collect_status(MX->e, w) ? g_status : -1;
+}
+
+int c_multi_forward(int start_step, int end_step, chn_complex* C, chn_complex* IC, const int* inhomo) {
+  if (!multi_ready("c_multi_forward")) return g_status;
+  Work& w = MX->e.batch;
+  if (!(end_step > start_step && start_step >= 0 && end_step <= w.nsteps) || !C || (w.ntan > 0 && !IC)) {
+    set_error(-4, "c_multi_forward: need 0 <= start < end <= nsteps and the state arrays");
+    return -4;
+  }
+  if (!multi_h2d(w.dC, C, 1)) return -1;
+  if (w.ntan > 0 && !multi_h2d(w.io, IC, w.ntan)) return -1;
+  if (!op_forward(MX->e, w, start_step, end_step, w.dC, w.io, mask_of(inhomo, w.ntan), true)) return g_status;
+  if (!multi_d2h(C, w.Cp, 1)) return -1;
+  if (w.ntan > 0 && !multi_d2h(IC, w.Ct, w.ntan)) return -1;
+  return collect_status(MX->e, w) ? g_status : -1;
+}
+
+int c_multi_adjoint(int start_step, int end_step, chn_complex* AC, double strength) {
+  if (!multi_ready("c_multi_adjoint")) return g_status;
+  Work& w = MX->e.batch;
+  if (!(end_step < start_step && end_step >= 0 && start_step <= w.nsteps) || !AC) {
+    set_error(-4, "c_multi_adjoint: need 0 <= end < start <= nsteps and the state array");
+    return -4;
+  }
+  if (!multi_h2d(w.io, AC, 1)) return -1;
+  if (!op_adjoint(MX->e, w, start_step, end_step, w.io, strength)) return g_status;
+  if (!multi_d2h(AC, w.Ca, 1)) return -1;
+  return collect_status(MX->e, w) ? g_status : -1;
+}
+
+int c_multi_getsoln(int i, int i_step, chn_complex* out) {
+  if (!multi_ready("c_multi_getsoln")) return g_status;
+  Work& w = MX->e.batch;
+  if (i < 0 || i >= w.nseg || i_step < 0 || i_step > w.nsteps || !out) return -4;
+  return d2h(MX->e, out, w.MC + (size_t)i * w.traj + (size_t)3 * i_step * w.csz, sizeof(cpx) * MX->csz[i]) ? 0
+                                                                                                            : -1;
+}
+
 void* c_stream(void) { return E ? (void*)E->st : nullptr; }
 
 // Average device time (ms, CUDA events on the library stream) of one launch
@@ -1471,6 +1694,7 @@ double c_batch_kernel_ms(int which, int reps) {
     switch (which) {
       case 0: {
         ReconArgs r{};
+        r.grids = w.gdev;
         r.ninst = nt;
         r.C = cb(w.St, w.csz);
         r.slot = noslot();
@@ -1480,6 +1704,7 @@ double c_batch_kernel_ms(int which, int reps) {
       }
       case 1: {
         PhysArgs p{};
+        p.grids = w.gdev;
         p.tmp = w.Zt;
         p.tmp_inst = w.zt_inst;
         p.U = cb(w.Ut, w.usz);
@@ -1491,6 +1716,7 @@ double c_batch_kernel_ms(int which, int reps) {
       }
       case 2: {
         ProdArgs ap{};
+        ap.grids = w.gdev;
         ap.tmp = w.Zt;
         ap.tmp_inst = w.zt_inst;
         ap.Pp = cbd(w.Pp, w.psz);
@@ -1503,6 +1729,7 @@ double c_batch_kernel_ms(int which, int reps) {
       }
       case 3: {
         SolveArgs sa{};
+        sa.grids = w.gdev;
         sa.H = cb(w.Ut, w.usz);
         sa.Hprev = cb(nullptr, 0);
         sa.Cc = mb(w.io, w.csz);   // scratch copy: the carried state is left alone
@@ -1519,6 +1746,7 @@ double c_batch_kernel_ms(int which, int reps) {
       }
       case 4: {
         ProdArgs ap{};
+        ap.grids = w.gdev;
         ap.tmp = w.Zt;
         ap.tmp_inst = w.zt_inst;
         ap.Pp = cbd(w.Pp, w.psz);

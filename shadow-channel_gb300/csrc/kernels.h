@@ -22,6 +22,7 @@ struct ReconArgs {
   int ninst;
   const uint32_t* status;
   int sdiv;
+  const Grid* grids;    // uneven batch: grid of each instance (device array), else null
 };
 
 struct PhysArgs {
@@ -37,6 +38,7 @@ struct PhysArgs {
   int skip_blocked;
   cpx* tmp;             // split transforms: intermediate for tmp_inst instances of 6
   int tmp_inst;         //   spectral columns [6][Q][pz][Nx/2] each
+  const Grid* grids;    // uneven batch: grid of each instance
 };
 
 struct ProdArgs {
@@ -50,6 +52,7 @@ struct ProdArgs {
   int sdiv;
   cpx* tmp;                // split transforms: as PhysArgs::tmp
   int tmp_inst;
+  const Grid* grids;       // uneven batch: grid of each instance
 };
 
 // mean-mode variants (channel/project0.c:153-168, increproject0.c:209-214, adjproject0.c:153-167)
@@ -91,6 +94,7 @@ struct SolveArgs {
   // Fts[(i / tdiv) * fts_stride + slot] (nullable)
   double* Fts;
   long long fts_stride;
+  const Grid* grids;        // uneven batch: grid of each instance
 };
 
 // one ddt_project / adjoint coupling for nseg segments (channel/channel.c:704-780)
@@ -104,6 +108,7 @@ struct DdtArgs {
   // steps long; at i_step 0 segment s > 0 takes its earlier state from
   // segment s - 1, step chain - 1 (the reference's global step before the window)
   int chain;
+  const Grid* grids;        // uneven batch: grid of each segment (its sizes, weights and dt)
 };
 
 void prepare_kernels(const Grid& g);  // function attributes; call once, outside graph capture
@@ -129,11 +134,12 @@ cudaError_t launch_flow_out(const Grid& g, const double* P, double* flow, cudaSt
 cudaError_t launch_ddt_diff(const Grid& g, const DdtArgs& d, cpx* dC, cudaStream_t st);
 // per-segment partial sums of sum a*b*W[y], sum a*a*W[y] over 3 fields: part[s][nblk][2]
 cudaError_t launch_ddt_dots(const Grid& g, Batch<const double> Pa, Batch<const double> Pb, double* part,
-                            int nblk, int nseg, cudaStream_t st);
+                            int nblk, int nseg, cudaStream_t st, const Grid* grids = nullptr);
 // r = num/den; IC' = IC - r dC (written to ICdst when non-null); AC -= coef * IC'
+// (grids non-null: the coefficient is coef * dt of each segment's grid)
 cudaError_t launch_ddt_apply(const Grid& g, const double* part, int nblk, int nseg, Batch<const cpx> ICsrc,
                              SlotRef icslot, Batch<cpx> ICdst, Batch<const cpx> dC, double* r_out,
-                             Batch<cpx> AC, double coef, cudaStream_t st);
+                             Batch<cpx> AC, double coef, cudaStream_t st, const Grid* grids = nullptr);
 // the same partial sums from field caches: dCdt's fields from primal cache
 // slots i+ and i- ([seg][slot][6][Q][pz][px]), the tangent's from velocity
 // cache slot i ([seg][step][3][Q][pz][px])
@@ -146,7 +152,7 @@ cudaError_t launch_cache_velocity(const Grid& g, const double* P, long long pstr
                                   const uint32_t* status, int nseg, cudaStream_t st);
 // AC[s] -= coef * src[s]
 cudaError_t launch_sub_scaled(const Grid& g, Batch<const cpx> src, Batch<cpx> ac, double coef, int nseg,
-                              cudaStream_t st);
+                              cudaStream_t st, const Grid* grids = nullptr);
 cudaError_t launch_project_init(const Grid& g, const cpx* Uinit, cpx* C, const double* luQs,
                                 const double* luRs, cudaStream_t st);
 cudaError_t launch_step_advance(int* ctr, int delta, cudaStream_t st);

@@ -24,8 +24,9 @@ cudaError_t launch_flow_out(const Grid& g, const double* P, double* flow, cudaSt
 }
 
 // dCdt = (1/dt) (MC[i+] - MC[i-]) per segment (channel/channel.c:728-740)
-__global__ void k_ddt_diff(size_t n, double rdt, DdtArgs d, cpx* __restrict__ dC) {
+__global__ void k_ddt_diff(size_t n, double rdt0, DdtArgs d, cpx* __restrict__ dC) {
   const int s = blockIdx.y;
+  const double rdt = d.grids ? 1.0 / d.grids[s].dt : rdt0;
   const int i_step = d.step_ptr ? *d.step_ptr + d.step_add : d.step_add;
   const bool cross = i_step == 0 && d.chain > 0 && s > 0;
   const int ip = cross ? 0 : (i_step == 0 ? 3 : 3 * i_step);
@@ -48,8 +49,11 @@ cudaError_t launch_ddt_diff(const Grid& g, const DdtArgs& d, cpx* dC, cudaStream
 
 // per-segment partial sums of the weighted inner products
 // (channel/channel.c:746-764); fixed block count and order: deterministic
-__global__ void k_ddt_dots(Grid g, Batch<const double> Pa, Batch<const double> Pb, double* __restrict__ part) {
+template <bool MULTI>
+__global__ void k_ddt_dots(const __grid_constant__ Grid g0, Batch<const double> Pa, Batch<const double> Pb,
+                           double* __restrict__ part, const Grid* grids) {
   const int s = blockIdx.y;
+  CHN_INSTANCE_GRID(g0, grids, s);
   const size_t plane = (size_t)g.pz * g.px;
   const size_t n = (size_t)3 * g.Q * plane;
   const double* a_ = Pa.at(s);
@@ -79,8 +83,9 @@ __global__ void k_ddt_dots(Grid g, Batch<const double> Pa, Batch<const double> P
 }
 
 cudaError_t launch_ddt_dots(const Grid& g, Batch<const double> Pa, Batch<const double> Pb, double* part,
-                            int nblk, int nseg, cudaStream_t st) {
-  k_ddt_dots<<<dim3(nblk, nseg), 256, 0, st>>>(g, Pa, Pb, part);
+                            int nblk, int nseg, cudaStream_t st, const Grid* grids) {
+  if (grids) k_ddt_dots<true><<<dim3(nblk, nseg), 256, 0, st>>>(g, Pa, Pb, part, grids);
+  else k_ddt_dots<false><<<dim3(nblk, nseg), 256, 0, st>>>(g, Pa, Pb, part, nullptr);
   return cudaGetLastError();
 }
 
@@ -88,10 +93,12 @@ cudaError_t launch_ddt_dots(const Grid& g, Batch<const double> Pa, Batch<const d
 // dudt = (P(MC[i+]) - P(MC[i-])) / dt from the primal cache (the transform is
 // linear, so this is spec2phys of the finite difference), v from the cache of
 // the coupled tangent's fields at stage 0 of step i (spec2phys(MIC[3i])).
-__global__ void k_ddt_dots_cached(Grid g, DdtArgs d, const double* __restrict__ Pc, long long cstride,
-                                  long long psz, const double* __restrict__ Pv, long long vstride,
-                                  long long vslot, double* __restrict__ part) {
+template <bool MULTI>
+__global__ void k_ddt_dots_cached(const __grid_constant__ Grid g0, DdtArgs d, const double* __restrict__ Pc,
+                                  long long cstride, long long psz, const double* __restrict__ Pv,
+                                  long long vstride, long long vslot, double* __restrict__ part) {
   const int s = blockIdx.y;
+  CHN_INSTANCE_GRID(g0, d.grids, s);
   const int i_step = d.step_ptr ? *d.step_ptr + d.step_add : d.step_add;
   const bool cross = i_step == 0 && d.chain > 0 && s > 0;
   const int ip = cross ? 0 : (i_step == 0 ? 3 : 3 * i_step);
@@ -129,7 +136,10 @@ __global__ void k_ddt_dots_cached(Grid g, DdtArgs d, const double* __restrict__ 
 cudaError_t launch_ddt_dots_cached(const Grid& g, const DdtArgs& d, const double* Pc, long long cstride,
                                    long long psz, const double* Pv, long long vstride, long long vslot,
                                    double* part, int nblk, cudaStream_t st) {
-  k_ddt_dots_cached<<<dim3(nblk, d.nseg), 256, 0, st>>>(g, d, Pc, cstride, psz, Pv, vstride, vslot, part);
+  if (d.grids)
+    k_ddt_dots_cached<true><<<dim3(nblk, d.nseg), 256, 0, st>>>(g, d, Pc, cstride, psz, Pv, vstride, vslot, part);
+  else
+    k_ddt_dots_cached<false><<<dim3(nblk, d.nseg), 256, 0, st>>>(g, d, Pc, cstride, psz, Pv, vstride, vslot, part);
   return cudaGetLastError();
 }
 
@@ -159,8 +169,9 @@ cudaError_t launch_cache_velocity(const Grid& g, const double* P, long long pstr
 
 // AC -= coef * IC' for an IC' projected earlier (the same update as k_ddt_apply)
 __global__ void k_sub_scaled(size_t n, const cpx* __restrict__ src, long long sstride, cpx* __restrict__ ac,
-                             long long astride, double coef) {
+                             long long astride, double coef0, const Grid* grids) {
   const int s = blockIdx.y;
+  const double coef = grids ? coef0 * grids[s].dt : coef0;
   const cpx* v_ = src + (long long)s * sstride;
   cpx* a_ = ac + (long long)s * astride;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -171,10 +182,11 @@ __global__ void k_sub_scaled(size_t n, const cpx* __restrict__ src, long long ss
 }
 
 cudaError_t launch_sub_scaled(const Grid& g, Batch<const cpx> src, Batch<cpx> ac, double coef, int nseg,
-                              cudaStream_t st) {
+                              cudaStream_t st, const Grid* grids) {
   const size_t n = coef_size(g);
   const unsigned nb = (unsigned)((n + 255) / 256);
-  k_sub_scaled<<<dim3(nb < 512 ? nb : 512, nseg), 256, 0, st>>>(n, src.base, src.stride, ac.base, ac.stride, coef);
+  k_sub_scaled<<<dim3(nb < 512 ? nb : 512, nseg), 256, 0, st>>>(n, src.base, src.stride, ac.base, ac.stride, coef,
+                                                                 grids);
   return cudaGetLastError();
 }
 
@@ -182,8 +194,9 @@ cudaError_t launch_sub_scaled(const Grid& g, Batch<const cpx> src, Batch<cpx> ac
 // AC -= 0.5*strength*dt*IC' (channel/channel.c:628-631, 686-689)
 __global__ void k_ddt_apply(size_t n, const double* __restrict__ part, int nblk, Batch<const cpx> ICsrc,
                             SlotRef icslot, Batch<cpx> ICdst, Batch<const cpx> dC, double* __restrict__ r_out,
-                            Batch<cpx> AC, double coef) {
+                            Batch<cpx> AC, double coef0, const Grid* grids) {
   const int s = blockIdx.y;
+  const double coef = grids ? coef0 * grids[s].dt : coef0;
   __shared__ double r_s;
   if (threadIdx.x == 0) {
     double num = 0.0, den = 0.0;
@@ -215,11 +228,11 @@ __global__ void k_ddt_apply(size_t n, const double* __restrict__ part, int nblk,
 
 cudaError_t launch_ddt_apply(const Grid& g, const double* part, int nblk, int nseg, Batch<const cpx> ICsrc,
                              SlotRef icslot, Batch<cpx> ICdst, Batch<const cpx> dC, double* r_out,
-                             Batch<cpx> AC, double coef, cudaStream_t st) {
+                             Batch<cpx> AC, double coef, cudaStream_t st, const Grid* grids) {
   const size_t n = coef_size(g);
   const unsigned nb = (unsigned)((n + 255) / 256);
   k_ddt_apply<<<dim3(nb < 512 ? nb : 512, nseg), 256, 0, st>>>(n, part, nblk, ICsrc, icslot, ICdst, dC, r_out, AC,
-                                                                coef);
+                                                                coef, grids);
   return cudaGetLastError();
 }
 

@@ -91,8 +91,11 @@ __device__ __forceinline__ int zrow_to_kz(const Grid& g, int zp) {
   return -1;
 }
 
-__global__ void __launch_bounds__(kThreads) k_phys_inverse(Grid g, PhysArgs a) {
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_phys_inverse(const __grid_constant__ Grid g0, PhysArgs a) {
   const int inst = blockIdx.y, y = blockIdx.x;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
+  if (y >= g.Q) return;
   if (a.skip_blocked && blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
   PhysSmem s = carve(g, smem, a.cfl_check != 0);
@@ -217,8 +220,11 @@ __device__ inline cpx* forward_plane(const Grid& g, PhysSmem& s, const FftPlan& 
   return fft_run(pzF, s.zb0, s.zb1, g.X, g.X, 1, s.twz, -1, true);
 }
 
-__global__ void __launch_bounds__(kThreads) k_products_fwd(Grid g, ProdArgs a) {
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_products_fwd(const __grid_constant__ Grid g0, ProdArgs a) {
   const int inst = blockIdx.y, y = blockIdx.x;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
+  if (y >= g.Q) return;
   if (blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
   PhysSmem s = carve(g, smem, false);
@@ -257,8 +263,11 @@ size_t prod_adj_smem_bytes(const Grid& g) {
   return phys_smem_bytes(g, false) + (size_t)6 * g.Nz * g.X * sizeof(cpx);
 }
 
-__global__ void __launch_bounds__(kThreads) k_products_adj(Grid g, ProdArgs a) {
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant__ Grid g0, ProdArgs a) {
   const int inst = blockIdx.y, y = blockIdx.x;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
+  if (y >= g.Q) return;
   if (blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
   PhysSmem s = carve(g, smem, false);
@@ -355,14 +364,19 @@ static size_t split_x_smem(const Grid& g, bool with_cfl) {
 }
 
 bool fused_transforms_fit(const Grid& g, int smem_optin) {
-  return phys_smem_bytes(g, true) <= (size_t)smem_optin && prod_adj_smem_bytes(g) <= (size_t)smem_optin;
+  const size_t room = (size_t)smem_optin - 4096;  // static shared memory of the kernels (reductions, grid)
+  return phys_smem_bytes(g, true) <= room && prod_adj_smem_bytes(g) <= room;
 }
 
 // inverse z pass: spectral fields f0..f0+nf-1 -> T (channel/pass1.c:107-110)
-__global__ void __launch_bounds__(kThreads) k_split_zinv(Grid g, PhysArgs a, int inst0, int nf, cpx* T) {
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_split_zinv(const __grid_constant__ Grid g0, PhysArgs a, int inst0,
+                                                         int nf, cpx* T) {
   const int y = blockIdx.x, il = blockIdx.y, inst = inst0 + il;
-  const int nck = (g.X + kCols - 1) / kCols;
+  const int nck = (g0.X + kCols - 1) / kCols;
   const int f = blockIdx.z / nck, x0 = (blockIdx.z - f * nck) * kCols;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
+  if (y >= g.Q || x0 >= g.X) return;
   const int nc = min(kCols, g.X - x0);
   if (a.skip_blocked && blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -379,7 +393,7 @@ __global__ void __launch_bounds__(kThreads) k_split_zinv(Grid g, PhysArgs a, int
   __syncthreads();
   const FftPlan plan = make_plan(g.pz, true);
   const cpx* zr = fft_run(plan, b0, b1, nc, nc, 1, tw, +1, true);
-  cpx* Tf = T + (((size_t)il * nf + f) * g.Q + y) * g.pz * g.X;
+  cpx* Tf = T + (((size_t)il * nf + f) * g0.Q + y) * g0.pz * g0.X;
   for (int i = threadIdx.x; i < g.pz * nc; i += blockDim.x) {
     const int zp = i / nc, c = i - zp * nc;
     Tf[(size_t)zp * g.X + x0 + c] = zr[i];
@@ -388,10 +402,15 @@ __global__ void __launch_bounds__(kThreads) k_split_zinv(Grid g, PhysArgs a, int
 
 // inverse x pass: row pairs of T -> physical rows of P, CFL of the velocity
 // (channel/pass1.c:111-138)
-__global__ void __launch_bounds__(kThreads) k_split_xinv(Grid g, PhysArgs a, int inst0, int nf, const cpx* T) {
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_split_xinv(const __grid_constant__ Grid g0, PhysArgs a, int inst0,
+                                                         int nf, const cpx* T) {
   const int y = blockIdx.x, il = blockIdx.y, inst = inst0 + il;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
   const int npair = (g.pz + 1) / 2;
-  const int p0 = blockIdx.z * kPairs, np = min(kPairs, npair - p0);
+  const int p0 = blockIdx.z * kPairs;
+  if (y >= g.Q || p0 >= npair) return;
+  const int np = min(kPairs, npair - p0);
   if (a.skip_blocked && blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
   cpx* tw = reinterpret_cast<cpx*>(smem);
@@ -406,7 +425,7 @@ __global__ void __launch_bounds__(kThreads) k_split_xinv(Grid g, PhysArgs a, int
   const int r0 = 2 * p0, nr = min(2 * np, g.pz - r0);
   bool nonfinite = false;
   for (int f = 0; f < nf; ++f) {
-    const cpx* zr = T + (((size_t)il * nf + f) * g.Q + y) * g.pz * g.X;
+    const cpx* zr = T + (((size_t)il * nf + f) * g0.Q + y) * g0.pz * g0.X;
     for (int i = threadIdx.x; i < np * g.px; i += blockDim.x) {
       const int pl = i / g.px, k = i - pl * g.px;
       const int ra = 2 * (p0 + pl), rb = ra + 1;
@@ -485,10 +504,15 @@ __device__ __forceinline__ double split_product(int mode, const double* __restri
 
 // forward x pass: products of row pairs, x transform, kept bins -> T
 // (channel/pass1.c:312-330, pass2.c:474-500)
-__global__ void __launch_bounds__(kThreads) k_split_xfwd(Grid g, ProdArgs a, int mode, int inst0, cpx* T) {
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_split_xfwd(const __grid_constant__ Grid g0, ProdArgs a, int mode,
+                                                         int inst0, cpx* T) {
   const int y = blockIdx.x, il = blockIdx.y, inst = inst0 + il;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
   const int npair = (g.pz + 1) / 2;
-  const int p0 = blockIdx.z * kPairs, np = min(kPairs, npair - p0);
+  const int p0 = blockIdx.z * kPairs;
+  if (y >= g.Q || p0 >= npair) return;
+  const int np = min(kPairs, npair - p0);
   if (blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
   cpx* tw = reinterpret_cast<cpx*>(smem);
@@ -515,7 +539,7 @@ __global__ void __launch_bounds__(kThreads) k_split_xfwd(Grid g, ProdArgs a, int
     }
     __syncthreads();
     const cpx* xr = fft_run(plan, b0, b1, np, 1, g.px, tw, -1, true);
-    cpx* Tq = T + (((size_t)il * ncomp + q) * g.Q + y) * g.pz * g.X;
+    cpx* Tq = T + (((size_t)il * ncomp + q) * g0.Q + y) * g0.pz * g0.X;
     for (int i = threadIdx.x; i < np * g.X; i += blockDim.x) {
       const int pl = i / g.X, k = i - pl * g.X;
       const cpx Zk = xr[pl * g.px + k];
@@ -536,10 +560,15 @@ __global__ void __launch_bounds__(kThreads) k_split_xfwd(Grid g, ProdArgs a, int
 // forward z pass: columns of T, z transform, truncation -> H; the adjoint
 // assembles H = -T + (i k) x S and keeps S_x, S_z (channel/pass1.c:331-371,
 // pass2.c:501-566)
-__global__ void __launch_bounds__(kThreads) k_split_zfwd(Grid g, ProdArgs a, int mode, int inst0, const cpx* T) {
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_split_zfwd(const __grid_constant__ Grid g0, ProdArgs a, int mode,
+                                                         int inst0, const cpx* T) {
   const int y = blockIdx.x, il = blockIdx.y, inst = inst0 + il;
   const int ncol = mode == 2 ? kColsAdj : kCols;
-  const int x0 = blockIdx.z * ncol, nc = min(ncol, g.X - x0);
+  const int x0 = blockIdx.z * ncol;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
+  if (y >= g.Q || x0 >= g.X) return;
+  const int nc = min(ncol, g.X - x0);
   if (blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
   cpx* tw = reinterpret_cast<cpx*>(smem);
@@ -551,7 +580,7 @@ __global__ void __launch_bounds__(kThreads) k_split_zfwd(Grid g, ProdArgs a, int
   const FftPlan plan = make_plan(g.pz, false);
   const int ncomp = mode == 2 ? 6 : 3;
   for (int q = 0; q < ncomp; ++q) {
-    const cpx* Tq = T + (((size_t)il * ncomp + q) * g.Q + y) * g.pz * g.X;
+    const cpx* Tq = T + (((size_t)il * ncomp + q) * g0.Q + y) * g0.pz * g0.X;
     for (int i = threadIdx.x; i < g.pz * nc; i += blockDim.x) {
       const int zp = i / nc, c = i - zp * nc;
       b0[i] = Tq[(size_t)zp * g.X + x0 + c];
@@ -606,10 +635,15 @@ static cudaError_t split_phys_inverse(const Grid& g, const PhysArgs& a, cudaStre
   const int cap = a.tmp_inst * 6 / a.nfields;
   return split_chunks(a.ninst, cap, [&](int i0, int n) {
     const int nck = (g.X + kCols - 1) / kCols, npc = ((g.pz + 1) / 2 + kPairs - 1) / kPairs;
-    k_split_zinv<<<dim3(g.Q, n, a.nfields * nck), kThreads, split_z_smem(g, kCols, 0), st>>>(g, a, i0, a.nfields,
-                                                                                             a.tmp);
-    k_split_xinv<<<dim3(g.Q, n, npc), kThreads, split_x_smem(g, a.cfl_check != 0), st>>>(g, a, i0, a.nfields,
-                                                                                          a.tmp);
+    const dim3 gz(g.Q, n, a.nfields * nck), gx(g.Q, n, npc);
+    const size_t sz = split_z_smem(g, kCols, 0), sx = split_x_smem(g, a.cfl_check != 0);
+    if (a.grids) {
+      k_split_zinv<true><<<gz, kThreads, sz, st>>>(g, a, i0, a.nfields, a.tmp);
+      k_split_xinv<true><<<gx, kThreads, sx, st>>>(g, a, i0, a.nfields, a.tmp);
+    } else {
+      k_split_zinv<false><<<gz, kThreads, sz, st>>>(g, a, i0, a.nfields, a.tmp);
+      k_split_xinv<false><<<gx, kThreads, sx, st>>>(g, a, i0, a.nfields, a.tmp);
+    }
     return cudaGetLastError();
   });
 }
@@ -621,9 +655,15 @@ static cudaError_t split_products(const Grid& g, const ProdArgs& a, int mode, cu
   return split_chunks(a.ninst, cap, [&](int i0, int n) {
     const int npc = ((g.pz + 1) / 2 + kPairs - 1) / kPairs;
     const int ncol = mode == 2 ? kColsAdj : kCols, nck = (g.X + ncol - 1) / ncol;
-    k_split_xfwd<<<dim3(g.Q, n, npc), kThreads, split_x_smem(g, false), st>>>(g, a, mode, i0, a.tmp);
-    k_split_zfwd<<<dim3(g.Q, n, nck), kThreads, split_z_smem(g, ncol, mode == 2 ? 6 : 0), st>>>(g, a, mode, i0,
-                                                                                                 a.tmp);
+    const dim3 gx(g.Q, n, npc), gz(g.Q, n, nck);
+    const size_t sx = split_x_smem(g, false), sz = split_z_smem(g, ncol, mode == 2 ? 6 : 0);
+    if (a.grids) {
+      k_split_xfwd<true><<<gx, kThreads, sx, st>>>(g, a, mode, i0, a.tmp);
+      k_split_zfwd<true><<<gz, kThreads, sz, st>>>(g, a, mode, i0, a.tmp);
+    } else {
+      k_split_xfwd<false><<<gx, kThreads, sx, st>>>(g, a, mode, i0, a.tmp);
+      k_split_zfwd<false><<<gz, kThreads, sz, st>>>(g, a, mode, i0, a.tmp);
+    }
     return cudaGetLastError();
   });
 }
@@ -635,41 +675,54 @@ static cudaError_t split_products(const Grid& g, const ProdArgs& a, int mode, cu
 cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
   if (g.split) return split_phys_inverse(g, a, st);
-  k_phys_inverse<<<dim3(g.Q, a.ninst), kThreads, phys_smem_bytes(g, a.cfl_check != 0), st>>>(g, a);
+  const size_t sm = phys_smem_bytes(g, a.cfl_check != 0);
+  if (a.grids) k_phys_inverse<true><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
+  else k_phys_inverse<false><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
   if (g.split) return split_products(g, a, a.Pt.base ? 1 : 0, st);
-  k_products_fwd<<<dim3(g.Q, a.ninst), kThreads, phys_smem_bytes(g, false), st>>>(g, a);
+  const size_t sm = phys_smem_bytes(g, false);
+  if (a.grids) k_products_fwd<true><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
+  else k_products_fwd<false><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
   if (g.split) return split_products(g, a, 2, st);
-  k_products_adj<<<dim3(g.Q, a.ninst), kThreads, prod_adj_smem_bytes(g), st>>>(g, a);
+  const size_t sm = prod_adj_smem_bytes(g);
+  if (a.grids) k_products_adj<true><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
+  else k_products_adj<false><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
   return cudaGetLastError();
 }
 
-void prepare_recon_solve(const Grid& g);
+void prepare_recon_solve(int optin);
+
+// Every kernel may use up to the device's opt-in shared memory per block: the
+// single-grid engine and an uneven batch (sized for its largest grid) share
+// the kernels, so the limit is not tied to one grid.
+template <bool MULTI>
+static void prepare_transforms(int optin) {
+  allow_max_smem(k_split_zinv<MULTI>, optin);
+  allow_max_smem(k_split_xinv<MULTI>, optin);
+  allow_max_smem(k_split_xfwd<MULTI>, optin);
+  allow_max_smem(k_split_zfwd<MULTI>, optin);
+  allow_max_smem(k_phys_inverse<MULTI>, optin);
+  allow_max_smem(k_products_fwd<MULTI>, optin);
+  allow_max_smem(k_products_adj<MULTI>, optin);
+}
 
 void prepare_kernels(const Grid& g) {
-  if (g.split) {
-    cudaFuncSetAttribute(k_split_zinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_z_smem(g, kCols, 0));
-    cudaFuncSetAttribute(k_split_xinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_x_smem(g, true));
-    cudaFuncSetAttribute(k_split_xfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_x_smem(g, false));
-    cudaFuncSetAttribute(k_split_zfwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)std::max(split_z_smem(g, kCols, 0), split_z_smem(g, kColsAdj, 6)));
-  } else {
-    cudaFuncSetAttribute(k_phys_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)phys_smem_bytes(g, true));
-    cudaFuncSetAttribute(k_products_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)phys_smem_bytes(g, false));
-    cudaFuncSetAttribute(k_products_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prod_adj_smem_bytes(g));
-  }
-  prepare_recon_solve(g);
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  (void)g;
+  prepare_transforms<false>(optin);
+  prepare_transforms<true>(optin);
+  prepare_recon_solve(optin);
 }
 
 }  // namespace chn

@@ -34,10 +34,13 @@ __device__ __forceinline__ void cfma(double w, const cpx& a, double& re, double&
 // reconstruction
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kThreads) k_recon(Grid g, ReconArgs a) {
-  const int ntx = (g.X + kTile - 1) / kTile;
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_recon(const __grid_constant__ Grid g0, ReconArgs a) {
+  const int ntx = (g0.X + kTile - 1) / kTile;
   const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
   const int inst = blockIdx.y;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
+  if (z >= g.Nz || tx * kTile >= g.X) return;
   if (z == g.Nz / 2) return;  // never read (channel/pass1.c:51-85 skips it)
   if (blocked(a.status, a.sdiv, inst)) return;
   const int x0 = tx * kTile;
@@ -167,7 +170,8 @@ size_t recon_smem_bytes(const Grid& g) { return (size_t)2 * g.R * kTile * sizeof
 cudaError_t launch_recon(const Grid& g, const ReconArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
   const int ntx = (g.X + kTile - 1) / kTile;
-  k_recon<<<dim3(g.Nz * ntx, a.ninst), kThreads, recon_smem_bytes(g), st>>>(g, a);
+  if (a.grids) k_recon<true><<<dim3(g.Nz * ntx, a.ninst), kThreads, recon_smem_bytes(g), st>>>(g, a);
+  else k_recon<false><<<dim3(g.Nz * ntx, a.ninst), kThreads, recon_smem_bytes(g), st>>>(g, a);
   return cudaGetLastError();
 }
 
@@ -446,10 +450,13 @@ __device__ __forceinline__ double rps_row_real(const Grid& g, const double* y, i
   return acc;
 }
 
-__global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
-  const int ntx = (g.X + kTile - 1) / kTile;
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ Grid g0, SolveArgs a) {
+  const int ntx = (g0.X + kTile - 1) / kTile;
   const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
   const int inst = blockIdx.y;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
+  if (z >= g.Nz || tx * kTile >= g.X) return;
   if (blocked(a.status, a.sdiv, inst)) return;
   const int x0 = tx * kTile;
   const int nx = min(kTile, g.X - x0);
@@ -829,13 +836,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(Grid g, SolveArgs a) {
 cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
   const int ntx = (g.X + kTile - 1) / kTile;
-  k_solve<<<dim3(g.Nz * ntx, a.ninst), kThreads, solve_smem_bytes(g), st>>>(g, a);
+  if (a.grids) k_solve<true><<<dim3(g.Nz * ntx, a.ninst), kThreads, solve_smem_bytes(g), st>>>(g, a);
+  else k_solve<false><<<dim3(g.Nz * ntx, a.ninst), kThreads, solve_smem_bytes(g), st>>>(g, a);
   return cudaGetLastError();
 }
 
-void prepare_recon_solve(const Grid& g) {
-  cudaFuncSetAttribute(k_recon, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)recon_smem_bytes(g));
-  cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)solve_smem_bytes(g));
+void prepare_recon_solve(int optin) {
+  allow_max_smem(k_recon<false>, optin);
+  allow_max_smem(k_solve<false>, optin);
+  allow_max_smem(k_recon<true>, optin);
+  allow_max_smem(k_solve<true>, optin);
 }
 
 }  // namespace chn
