@@ -280,6 +280,7 @@ def run_gb300(a):
     achieved = flops / (dom_ms * 1e-3) / 1e12
     traffic = PHYS_TRAFFIC_PER_INSTANCE_32 * nt if (GRID["Nx"], GRID["Ny"], GRID["Nz"]) == (32, 65, 32) else None
     step_flop = segment_step_flops(GRID)
+    autotune = json.loads(cc.lib.c_autotune_report().decode() or "{}")
     roofline = {"bound": "fp64", "kernel": f"k_phys_inverse ({nt} tangent fields)", "achieved": achieved,
                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                 "traffic_unit": "bytes per launch",
@@ -301,7 +302,7 @@ def run_gb300(a):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic seeded states (no dataset; reference restart files absent)",
-            "config": CONFIG, "e2e": e2e, "roofline": roofline, "gpu_launches": launches,
+            "config": CONFIG, "e2e": e2e, "roofline": roofline, "gpu_launches": launches, "autotune": autotune,
             "clocks": clk.summary()}
     if plain:
         line["plain_gpu"] = plain

@@ -173,6 +173,9 @@ double c_fp64_peak_tflops(void);
    FMA, 1 FP64 add, 2 FP64 warp matrix multiply-accumulate (m8n8k4), 3 FP32
    FMA; NaN for other kinds */
 double c_pipe_peak_tflops(int kind);
+/* the transform autotuner's timings (ms per batched substage) and choice
+   for the last c_batch_init / c_multi_init, as a JSON object ("" before) */
+const char *c_autotune_report(void);
 
 /* spec2phys without allocating: no counterpart in the reference.  For
    callers that cannot call cudaMalloc when they need a physical field (code

@@ -77,6 +77,8 @@ _lib.c_fp64_peak_tflops.argtypes = []
 _lib.c_fp64_peak_tflops.restype = _d
 _lib.c_pipe_peak_tflops.argtypes = [_i]
 _lib.c_pipe_peak_tflops.restype = _d
+_lib.c_autotune_report.argtypes = []
+_lib.c_autotune_report.restype = ctypes.c_char_p
 _lib.c_batch_init.argtypes = [_i, _i, _i]
 _lib.c_batch_init.restype = _i
 _lib.c_batch_primal.argtypes = [_i, _vp]

@@ -39,7 +39,9 @@ enum : uint32_t {
 // Grid description plus device tables; passed by value to every kernel.
 struct Grid {
   int Nx, Ny, Nz, X, Q, R, D, pz, px, Qh;  // Qh = (Q+1)/2 plane pairs
-  int split;             // transforms in separate z and x passes (a plane exceeds one block's shared memory)
+  int split;             // transforms in separate z and x passes (required when a plane exceeds
+                         // one block's shared memory; else chosen by the autotuner)
+  int tvar;              // split-transform variant (block size and chunk)
   double dt, re, flux, norm, cfl1, cfl3;
   const double* Kx;      // [X]
   const double* Kz;      // [Nz]

@@ -154,6 +154,13 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const char* force = getenv("CHN_SPLIT_TRANSFORMS");
   g.split = (!fused_transforms_fit(g, optin) || (force && force[0] == '1')) ? 1 : 0;
+  g.tvar = 0;
+  const char* var = getenv("CHN_SPLIT_VARIANT");  // with CHN_SPLIT_TRANSFORMS=1: this variant
+  if (force && force[0] == '1' && var) g.tvar = atoi(var);
+  if (g.split && !split_variant_fits(g.tvar, g, optin)) {
+    set_error(1, "grid %dx%dx%d: the split transforms need more shared memory than the device has", Nx, Ny, Nz);
+    return false;
+  }
   if (solve_smem_bytes(g) > (size_t)optin || recon_smem_bytes(g) > (size_t)optin) {
     set_error(1, "grid %dx%dx%d: the implicit solve needs %zu bytes of shared memory per block, the device has %d",
               Nx, Ny, Nz, solve_smem_bytes(g), optin);
@@ -254,10 +261,10 @@ struct Work {
            alloc(&status, nseg) && alloc(&step, 4) && alloc(&icp, nseg * csz) &&
            alloc(&Ft, (size_t)nseg * (3 * (size_t)nsteps + 1)) && alloc_split(g, nt) && alloc_cache(g);
   }
-  // split transforms (grids whose plane exceeds a block's shared memory):
-  // room for up to 2 GiB of intermediate, at least one instance
+  // split transforms (required where a plane exceeds a block's shared
+  // memory, else an autotuner candidate): room for up to 2 GiB of
+  // intermediate, at least one instance
   bool alloc_split(const Grid& g, size_t nt) {
-    if (!g.split) return true;
     const size_t per = split_tmp_elems(g);
     size_t n = ((size_t)2 << 30) / (per * sizeof(cpx));
     if (n < 1) n = 1;
@@ -738,6 +745,114 @@ static bool collect_status(Engine& e, Work& w) {
   if (any & ST_CFL) g_msg = "CFL condition violated: time loop stopped (channel/pass1.c:133-137)";
   else if (any & ST_NONFINITE) g_msg = "non-finite values in the physical fields";
   else g_msg.clear();
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// autotuner: the transform kernels (inverse of six fields, tangent products,
+// adjoint products) of one batched substage, timed on the working set's
+// buffers for the one-block-per-plane kernels (where a plane fits) and every
+// split variant that fits; the fastest is kept in the engine's grid.  All
+// candidates compute identical results.  CHN_AUTOTUNE=0 skips it.
+// ---------------------------------------------------------------------------
+
+static std::string g_tune_report;
+
+static bool autotune_transforms(Engine& e, Work& w) {
+  const char* off = getenv("CHN_AUTOTUNE");
+  if (off && off[0] == '0') return true;
+  const char* force = getenv("CHN_SPLIT_TRANSFORMS");
+  if (force && force[0] == '1') return true;
+  Grid& g = e.T.g;
+  int dev = 0, optin = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  struct Cand {
+    int split, tvar;
+    float ms;
+  };
+  std::vector<Cand> cands;
+  if (fused_transforms_fit(g, optin)) cands.push_back({0, 0, 0.f});
+  for (int v = 0; v < split_variant_count(); ++v)
+    if (split_variant_fits(v, g, optin)) cands.push_back({1, v, 0.f});
+  if (cands.size() < 2 || !w.Zt) return true;
+  const int nt = w.nseg * (w.ntan > 0 ? w.ntan : 1);
+  auto enqueue = [&]() -> bool {
+    PhysArgs p{};
+    p.U = cb(w.Ut, w.usz);
+    p.P = mbd(w.Pt, w.psz);
+    p.nfields = 6;
+    p.ninst = nt;
+    p.sdiv = 1;
+    p.tmp = w.Zt;
+    p.tmp_inst = w.zt_inst;
+    p.grids = w.gdev;
+    LK(launch_phys_inverse(g, p, e.st));
+    ProdArgs f{};
+    f.Pp = cbd(w.Pp, w.psz);
+    f.pdiv = w.ntan > 0 ? w.ntan : 1;
+    f.Pt = cbd(w.Pt, w.psz);
+    f.H = mb(w.Ut, w.usz);
+    f.ninst = nt;
+    f.sdiv = 1;
+    f.tmp = w.Zt;
+    f.tmp_inst = w.zt_inst;
+    f.grids = w.gdev;
+    LK(launch_products_fwd(g, f, e.st));
+    ProdArgs b = f;
+    b.pdiv = 1;
+    b.Pt = cbd(w.Pl, w.psz);
+    b.H = mb(w.Up, w.usz);
+    b.ninst = w.nseg;
+    LK(launch_products_adj(g, b, e.st));
+    return true;
+  };
+  cudaEvent_t t0, t1;
+  CK(cudaEventCreate(&t0));
+  CK(cudaEventCreate(&t1));
+  const int saved_split = g.split, saved_tvar = g.tvar;
+  bool ok = true;
+  for (Cand& c : cands) {
+    g.split = c.split;
+    g.tvar = c.tvar;
+    ok = ok && enqueue();  // warm-up
+    ok = ok && cudaEventRecord(t0, e.st) == cudaSuccess;
+    for (int r = 0; r < 3; ++r) ok = ok && enqueue();
+    ok = ok && cudaEventRecord(t1, e.st) == cudaSuccess && cudaEventSynchronize(t1) == cudaSuccess;
+    if (!ok) break;
+    cudaEventElapsedTime(&c.ms, t0, t1);
+    c.ms /= 3;
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (!ok) {
+    g.split = saved_split;
+    g.tvar = saved_tvar;
+    return false;
+  }
+  const Cand* best = &cands[0];
+  for (const Cand& c : cands)
+    if (c.ms < best->ms) best = &c;
+  g.split = best->split;
+  g.tvar = best->tvar;
+  char buf[160];
+  g_tune_report = "{";
+  for (const Cand& c : cands) {
+    if (c.split) {
+      const TransformVariant v = split_variant(c.tvar);
+      snprintf(buf, sizeof(buf), "\"split_nt%d_ch%d\": %.4f, ", v.nt, v.ch, c.ms);
+    } else {
+      snprintf(buf, sizeof(buf), "\"fused\": %.4f, ", c.ms);
+    }
+    g_tune_report += buf;
+  }
+  if (best->split) {
+    const TransformVariant v = split_variant(best->tvar);
+    snprintf(buf, sizeof(buf), "\"chosen\": \"split_nt%d_ch%d\", \"instances\": %d}", v.nt, v.ch, nt);
+  } else {
+    snprintf(buf, sizeof(buf), "\"chosen\": \"fused\", \"instances\": %d}", nt);
+  }
+  g_tune_report += buf;
   return true;
 }
 
@@ -1289,6 +1404,7 @@ int c_batch_init_steps(int nseg, int ntan, int couple, int nsteps) {
     return g_status;
   }
   e.have_batch = true;
+  if (!autotune_transforms(e, e.batch)) return g_status;
   g_status = 0;
   return 0;
 }
@@ -1612,6 +1728,11 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
   }
   m->e.batch.gdev = m->gdev;
   m->e.have_batch = true;
+  if (!autotune_transforms(m->e, m->e.batch)) {
+    const int rc = g_status ? g_status : -1;
+    c_multi_destroy();
+    return rc;
+  }
   g_status = 0;
   g_msg.clear();
   return 0;
@@ -1781,6 +1902,8 @@ int c_synchronize(void) {
 }
 
 long long c_launch_count(void) { return g_launches; }
+
+const char* c_autotune_report(void) { return g_tune_report.c_str(); }
 
 double c_pipe_peak_tflops(int kind) {
   const double fpi = probe_flop_per_thread_iter(kind);

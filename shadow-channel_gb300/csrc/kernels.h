@@ -123,6 +123,13 @@ cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st);
 size_t split_tmp_elems(const Grid& g);
 // whether the fused one-block-per-plane transforms fit this device's shared memory
 bool fused_transforms_fit(const Grid& g, int smem_optin);
+// split-transform variants (block size, chunk) the autotuner chooses from
+struct TransformVariant {
+  int nt, ch;
+};
+int split_variant_count();
+TransformVariant split_variant(int v);
+bool split_variant_fits(int v, const Grid& g, int optin);
 size_t recon_smem_bytes(const Grid& g);
 size_t phys_smem_bytes(const Grid& g, bool with_cfl);
 size_t prod_adj_smem_bytes(const Grid& g);

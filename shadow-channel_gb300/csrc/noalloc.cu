@@ -73,7 +73,10 @@ extern "C" int c_spec2phys_noalloc(const chn_complex* C_dev, double* flow_dev) {
     engine_set_error(-2, "c_spec2phys_noalloc called before c_init");
     return -2;
   }
-  const Grid& g = *gp;
+  // the one-block-per-plane transforms (they need no intermediate; every
+  // grid within the capacity below fits them)
+  Grid g = *gp;
+  g.split = 0;
   const size_t need_u = u_size(g);
   const size_t need_p = (size_t)3 * g.Q * plane_size(g);
   if (need_u > kNoAllocU || need_p > kNoAllocP) {

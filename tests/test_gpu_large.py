@@ -2,8 +2,9 @@
 transforms as separate z and x passes (csrc/phys.cu, split transforms).
 
 - The split passes are the fused kernels' 1D transforms on the same data, so
-  forcing them (CHN_SPLIT_TRANSFORMS=1) at 32x65x32 must reproduce the fused
-  results bit for bit through primal, tangents and the coupled adjoint.
+  forcing them (CHN_SPLIT_TRANSFORMS=1, each block-size / chunk variant the
+  autotuner chooses from) at 32x65x32 must reproduce the fused results bit
+  for bit through primal, tangents and the coupled adjoint.
 - 48x97x48 (the adjoint products no longer fit) and 128x129x128 (nothing
   fits) against the oracle, one step each way.
 """
@@ -39,7 +40,8 @@ def gpu():
         pytest.skip("no CUDA device")
 
 
-def test_split_transforms_bitwise_equal_fused(gpu):
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_split_transforms_bitwise_equal_fused(gpu, variant):
     code = r"""
 import ctypes, json, sys, numpy as np
 sys.path.insert(0, 'shadow-channel_gb300'); sys.path.insert(0, 'oracle')
@@ -64,7 +66,7 @@ print(json.dumps({k: v.view(np.float64).ravel().tolist() for k, v in
     root = O.HERE.parent
     outs = []
     for split in ("0", "1"):
-        env = dict(os.environ, CHN_SPLIT_TRANSFORMS=split)
+        env = dict(os.environ, CHN_SPLIT_TRANSFORMS=split, CHN_SPLIT_VARIANT=str(variant), CHN_AUTOTUNE="0")
         r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True, text=True,
                            timeout=600)
         assert r.returncode == 0, r.stderr[-2000:]
