@@ -57,6 +57,8 @@ def args_parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the uneven-batch and 128x129x128 measurements")
     ap.add_argument("--segments", type=int, default=NSEG,
                     help="segments per GPU (default 64; smaller only for profiling captures)")
     ap.add_argument("--runup", type=int, default=RUNUP,
@@ -307,6 +309,9 @@ def run_gb300(a):
     if plain:
         line["plain_gpu"] = plain
         line["plain_gpu"]["batched_over_plain"] = (value / world) / plain["value"]
+    if not a.no_extras and rank == 0:
+        line["uneven_batch"] = uneven_batch(cc)
+        line["large_grid"] = large_grid(cc)
     if rank == 0 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
@@ -318,6 +323,70 @@ def run_gb300(a):
 def ctypes_int_array(vals):
     import ctypes
     return (ctypes.c_int * len(vals))(*vals)
+
+
+def uneven_batch(cc, n=128, steps=5):
+    """128 instances with grids drawn from 16x33x16, 32x65x32, 48x97x48, Re
+    from [2000, 4000] and dt at half the CFL limit of a laminar estimate,
+    advanced by the same launches (c_multi_*): one primal sweep and one
+    adjoint sweep of `steps` steps; instance-steps per second of each."""
+    import ctypes
+    from channel.synthetic import synthetic_state
+    rng = np.random.default_rng(3)
+    grids = [(16, 33, 16), (32, 65, 32), (48, 97, 48)]
+    pick = rng.integers(0, 3, n)
+    Re = rng.uniform(2000.0, 4000.0, n)
+    inst = []
+    for i in range(n):
+        Nx, Ny, Nz = grids[pick[i]]
+        # CFL_MAX 2.8 (channel/pass1.c:133) with |u| ~ 1.5 flux/2 at the finest
+        # spacing of each direction; half of it
+        dx, dz = 2 * math.pi / (1.5 * Nx), math.pi / (1.5 * Nz)
+        dy = 1.0 - math.cos(math.pi / (1.5 * Ny))
+        dt = 0.5 * 2.8 / (1.5 / dx + 0.1 / dy + 0.1 / dz)
+        inst.append((Nx, Ny, Nz, float(Re[i]), min(dt, 0.01)))
+    arr = lambda v, t: (t * n)(*v)
+    t0 = time.perf_counter()
+    rc = cc.lib.c_multi_init(n, arr([x[0] for x in inst], ctypes.c_int), arr([x[1] for x in inst], ctypes.c_int),
+                             arr([x[2] for x in inst], ctypes.c_int), arr([2 * math.pi] * n, ctypes.c_double),
+                             arr([math.pi] * n, ctypes.c_double), arr([x[3] for x in inst], ctypes.c_double),
+                             arr([2.0] * n, ctypes.c_double), arr([x[4] for x in inst], ctypes.c_double), steps, 0, 0)
+    assert rc == 0, cc.c_last_error_message()
+    init_s = time.perf_counter() - t0
+    C = np.concatenate([synthetic_state(*x[:3], seed=i).ravel() for i, x in enumerate(inst)])
+    AC = np.concatenate([synthetic_state(*x[:3], seed=500 + i, laminar=False).ravel() for i, x in enumerate(inst)])
+    tune = json.loads(cc.lib.c_autotune_report().decode() or "{}")
+    t0 = time.perf_counter()
+    assert cc.lib.c_multi_primal(0, C.ctypes.data) == 0, cc.c_last_error_message()
+    t1 = time.perf_counter()
+    assert cc.lib.c_multi_adjoint(steps, 0, AC.ctypes.data, 0.0) == 0, cc.c_last_error_message()
+    t2 = time.perf_counter()
+    cc.lib.c_multi_destroy()
+    counts = {f"{g[0]}x{g[1]}x{g[2]}": int((pick == k).sum()) for k, g in enumerate(grids)}
+    return {"instances": n, "grids": counts, "steps": steps, "init_s": init_s,
+            "primal_instance_steps_per_s": n * steps / (t1 - t0),
+            "adjoint_instance_steps_per_s": n * steps / (t2 - t1), "autotune": tune,
+            "note": "host arrays, copies included; one launch per kernel and substage for all instances"}
+
+
+def large_grid(cc, nsteps=8):
+    """128x129x128, Lx 4 pi, Lz 2 pi, Re 3300, dt 0.002: the checkpointed
+    forward + adjoint (channel.checkpoint) with the HBM-sized interval and a
+    short one to expose the recomputation overhead."""
+    from channel import checkpoint
+    from channel.synthetic import synthetic_state
+    grid = dict(Nx=128, Ny=129, Nz=128, Lx=4 * math.pi, Lz=2 * math.pi, Re=3300.0, flux=2.0, dt=0.002)
+    C0 = synthetic_state(128, 129, 128, seed=1)
+    AC0 = synthetic_state(128, 129, 128, seed=2, laminar=False)
+    out = {"grid": "128x129x128", "steps": nsteps,
+           "hbm_spacing_for_5000_steps": checkpoint.choose_spacing(grid, 5000)}
+    for name, sp in (("one_interval", nsteps), ("interval_2", 2)):
+        _, _, rep = checkpoint.forward_adjoint(grid, C0, nsteps, AC0, spacing=sp)
+        rep["primal_steps_per_s"] = nsteps / rep["forward_s"]
+        rep["adjoint_steps_per_s"] = nsteps / rep["adjoint_s"]
+        out[name] = rep
+    cc.c_destroy()
+    return out
 
 
 def plain_gpu(cc, C, IC, AC, K):
