@@ -42,6 +42,7 @@ struct Grid {
   int split;             // transforms in separate z and x passes (required when a plane exceeds
                          // one block's shared memory; else chosen by the autotuner)
   int tvar;              // split-transform variant (block size and chunk)
+  int general;           // 3Nz/2 or 3Nx/2 needs radix 5 or 7 (slower, register-heavy transforms)
   double dt, re, flux, norm, cfl1, cfl3;
   const double* Kx;      // [X]
   const double* Kz;      // [Nz]

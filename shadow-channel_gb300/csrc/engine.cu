@@ -23,6 +23,7 @@
 
 #include "../../include/c_channel.h"
 #include "chn_common.cuh"
+#include "fft.cuh"
 #include "kernels.h"
 #include "setup.h"
 
@@ -153,6 +154,7 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const char* force = getenv("CHN_SPLIT_TRANSFORMS");
+  g.general = (radix234_only(g.pz) && radix234_only(g.px)) ? 0 : 1;
   g.split = (!fused_transforms_fit(g, optin) || (force && force[0] == '1')) ? 1 : 0;
   g.tvar = 0;
   const char* var = getenv("CHN_SPLIT_VARIANT");  // with CHN_SPLIT_TRANSFORMS=1: this variant
@@ -1697,6 +1699,7 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
     gmax.X = std::max(gmax.X, g.X); gmax.Q = std::max(gmax.Q, g.Q); gmax.R = std::max(gmax.R, g.R);
     gmax.D = std::max(gmax.D, g.D); gmax.pz = std::max(gmax.pz, g.pz); gmax.px = std::max(gmax.px, g.px);
     gmax.Qh = std::max(gmax.Qh, g.Qh);
+    gmax.general = std::max(gmax.general, g.general);
   }
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);

@@ -40,6 +40,15 @@ __host__ __device__ inline int plan_factor(int m, int* out) {
   return k;
 }
 
+// lengths 3 * 2^i * 3^j need only radices 2, 3, 4
+__host__ __device__ inline bool radix234_only(int n) {
+  if (n % 3) return false;
+  int m = n / 3;
+  while (m % 2 == 0) m /= 2;
+  while (m % 3 == 0) m /= 3;
+  return m == 1;
+}
+
 // inverse plan: radix 3 first; forward plan: radix 3 last
 __host__ __device__ inline FftPlan make_plan(int n, bool radix3_first) {
   FftPlan p;
@@ -147,6 +156,9 @@ __device__ void stockham_pass(const cpx* __restrict__ in, cpx* __restrict__ out,
 
 // Run a full transform; data starts in buf0, result ends in the returned buffer.
 // Callers must __syncthreads() before (data ready) and after (result ready).
+// GENERAL = false compiles radices 2, 3 and 4 only (lengths 3 * 2^i * 3^j): the
+// radix-5 and -7 butterflies more than double the registers of a kernel.
+template <bool GENERAL = true>
 __device__ inline cpx* fft_run(const FftPlan& p, cpx* buf0, cpx* buf1, int nb, int es, int bs,
                                const cpx* tw, int sign, bool prune) {
   cpx* in = buf0;
@@ -162,8 +174,12 @@ __device__ inline cpx* fft_run(const FftPlan& p, cpx* buf0, cpx* buf1, int nb, i
       case 2: stockham_pass<2>(in, out, p.n, Ns, nb, es, bs, tw, sign, false, false); break;
       case 3: stockham_pass<3>(in, out, p.n, Ns, nb, es, bs, tw, sign, zero_mid, skip_mid); break;
       case 4: stockham_pass<4>(in, out, p.n, Ns, nb, es, bs, tw, sign, false, false); break;
-      case 5: stockham_pass<5>(in, out, p.n, Ns, nb, es, bs, tw, sign, false, false); break;
-      case 7: stockham_pass<7>(in, out, p.n, Ns, nb, es, bs, tw, sign, false, false); break;
+      case 5:
+        if constexpr (GENERAL) stockham_pass<5>(in, out, p.n, Ns, nb, es, bs, tw, sign, false, false);
+        break;
+      case 7:
+        if constexpr (GENERAL) stockham_pass<7>(in, out, p.n, Ns, nb, es, bs, tw, sign, false, false);
+        break;
       default: break;  // sizes are validated on the host
     }
     Ns *= R;

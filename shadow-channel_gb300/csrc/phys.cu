@@ -58,7 +58,7 @@ __device__ inline void load_tw(const Grid& g, PhysSmem& s) {
   for (int i = threadIdx.x; i < g.px; i += blockDim.x) s.twx[i] = g.twx[i];
 }
 
-template <bool MULTI>
+template <bool MULTI, bool GEN>
 __global__ void __launch_bounds__(kThreads) k_phys_inverse(const __grid_constant__ Grid g0, PhysArgs a) {
   const int inst = blockIdx.y, y = blockIdx.x;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(kThreads) k_phys_inverse(const __grid_constant
       s.zb0[i] = v;
     }
     __syncthreads();
-    cpx* zr = fft_run(pz_plan, s.zb0, s.zb1, g.X, g.X, 1, s.twz, +1, true);
+    cpx* zr = fft_run<GEN>(pz_plan, s.zb0, s.zb1, g.X, g.X, 1, s.twz, +1, true);
     // pack rows (2p, 2p+1) as A + iB with the Hermitian extension in x
     for (int i = threadIdx.x; i < npair * g.px; i += blockDim.x) {
       const int p = i / g.px, k = i - p * g.px;
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kThreads) k_phys_inverse(const __grid_constant
       s.xb0[i] = Z;
     }
     __syncthreads();
-    cpx* xr = fft_run(px_plan, s.xb0, s.xb1, npair, 1, g.px, s.twx, +1, true);
+    cpx* xr = fft_run<GEN>(px_plan, s.xb0, s.xb1, npair, 1, g.px, s.twx, +1, true);
     double* Pf = P + ((size_t)f * g.Q + y) * plane;
     for (int i = threadIdx.x; i < g.pz * g.px; i += blockDim.x) {
       const int zp = i / g.px, xp = i - zp * g.px;
@@ -147,9 +147,10 @@ __global__ void __launch_bounds__(kThreads) k_phys_inverse(const __grid_constant
 
 // forward transform of the product rows held in xb0; leaves the kept,
 // scaled spectral rows in the returned z buffer
+template <bool GEN>
 __device__ inline cpx* forward_plane(const Grid& g, PhysSmem& s, const FftPlan& pxF, const FftPlan& pzF) {
   const int npair = (g.pz + 1) / 2;
-  cpx* xr = fft_run(pxF, s.xb0, s.xb1, npair, 1, g.px, s.twx, -1, true);
+  cpx* xr = fft_run<GEN>(pxF, s.xb0, s.xb1, npair, 1, g.px, s.twx, -1, true);
   const double hn = 0.5 * g.norm;
   for (int i = threadIdx.x; i < npair * g.X; i += blockDim.x) {
     const int p = i / g.X, k = i - p * g.X;
@@ -164,10 +165,10 @@ __device__ inline cpx* forward_plane(const Grid& g, PhysSmem& s, const FftPlan& 
     if (2 * p + 1 < g.pz) s.zb0[(2 * p + 1) * g.X + k] = B;
   }
   __syncthreads();
-  return fft_run(pzF, s.zb0, s.zb1, g.X, g.X, 1, s.twz, -1, true);
+  return fft_run<GEN>(pzF, s.zb0, s.zb1, g.X, g.X, 1, s.twz, -1, true);
 }
 
-template <bool MULTI>
+template <bool MULTI, bool GEN>
 __global__ void __launch_bounds__(kThreads) k_products_fwd(const __grid_constant__ Grid g0, ProdArgs a) {
   const int inst = blockIdx.y, y = blockIdx.x;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(kThreads) k_products_fwd(const __grid_constant
       s.xb0[i] = z;
     }
     __syncthreads();
-    cpx* zr = forward_plane(g, s, pxF, pzF);
+    cpx* zr = forward_plane<GEN>(g, s, pxF, pzF);
     for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x) {
       const int zp = i / g.X, x = i - zp * g.X;
       const int z = zrow_to_kz(g, zp);
@@ -210,7 +211,7 @@ size_t prod_adj_smem_bytes(const Grid& g) {
   return phys_smem_bytes(g, false) + (size_t)6 * g.Nz * g.X * sizeof(cpx);
 }
 
-template <bool MULTI>
+template <bool MULTI, bool GEN>
 __global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant__ Grid g0, ProdArgs a) {
   const int inst = blockIdx.y, y = blockIdx.x;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant
       s.xb0[i] = cpx{val[0], val[1]};
     }
     __syncthreads();
-    cpx* zr = forward_plane(g, s, pxF, pzF);
+    cpx* zr = forward_plane<GEN>(g, s, pxF, pzF);
     for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x) {
       const int zp = i / g.X, x = i - zp * g.X;
       const int z = zrow_to_kz(g, zp);
@@ -336,12 +337,24 @@ static int split_index(const Grid& g) { return (g.tvar >= 0 && g.tvar < kNumSpli
 // launchers
 // ---------------------------------------------------------------------------
 
+// the instance of a fused kernel for this launch: uneven batch or not,
+// general radices or 2/3/4 only
+#define CHN_LAUNCH_FUSED(K, grid, smem, st, g, a)                               \
+  do {                                                                            \
+    if ((a).grids) {                                                              \
+      if ((g).general) K<true, true><<<grid, kThreads, smem, st>>>(g, a);        \
+      else K<true, false><<<grid, kThreads, smem, st>>>(g, a);                   \
+    } else {                                                                      \
+      if ((g).general) K<false, true><<<grid, kThreads, smem, st>>>(g, a);       \
+      else K<false, false><<<grid, kThreads, smem, st>>>(g, a);                  \
+    }                                                                             \
+  } while (0)
+
 cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
   if (g.split) return kSplit[split_index(g)].inverse(g, a, st);
   const size_t sm = phys_smem_bytes(g, a.cfl_check != 0);
-  if (a.grids) k_phys_inverse<true><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
-  else k_phys_inverse<false><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
+  CHN_LAUNCH_FUSED(k_phys_inverse, dim3(g.Q, a.ninst), sm, st, g, a);
   return cudaGetLastError();
 }
 
@@ -349,8 +362,7 @@ cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t s
   if (a.ninst <= 0) return cudaSuccess;
   if (g.split) return kSplit[split_index(g)].products(g, a, a.Pt.base ? 1 : 0, st);
   const size_t sm = phys_smem_bytes(g, false);
-  if (a.grids) k_products_fwd<true><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
-  else k_products_fwd<false><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
+  CHN_LAUNCH_FUSED(k_products_fwd, dim3(g.Q, a.ninst), sm, st, g, a);
   return cudaGetLastError();
 }
 
@@ -358,8 +370,7 @@ cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t s
   if (a.ninst <= 0) return cudaSuccess;
   if (g.split) return kSplit[split_index(g)].products(g, a, 2, st);
   const size_t sm = prod_adj_smem_bytes(g);
-  if (a.grids) k_products_adj<true><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
-  else k_products_adj<false><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
+  CHN_LAUNCH_FUSED(k_products_adj, dim3(g.Q, a.ninst), sm, st, g, a);
   return cudaGetLastError();
 }
 
@@ -368,11 +379,11 @@ void prepare_recon_solve(int optin);
 // Every kernel may use up to the device's opt-in shared memory per block: the
 // single-grid engine and an uneven batch (sized for its largest grid) share
 // the kernels, so the limit is not tied to one grid.
-template <bool MULTI>
+template <bool MULTI, bool GEN>
 static void prepare_transforms(int optin) {
-  allow_max_smem(k_phys_inverse<MULTI>, optin);
-  allow_max_smem(k_products_fwd<MULTI>, optin);
-  allow_max_smem(k_products_adj<MULTI>, optin);
+  allow_max_smem(k_phys_inverse<MULTI, GEN>, optin);
+  allow_max_smem(k_products_fwd<MULTI, GEN>, optin);
+  allow_max_smem(k_products_adj<MULTI, GEN>, optin);
 }
 
 void prepare_kernels(const Grid& g) {
@@ -380,8 +391,10 @@ void prepare_kernels(const Grid& g) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   (void)g;
-  prepare_transforms<false>(optin);
-  prepare_transforms<true>(optin);
+  prepare_transforms<false, false>(optin);
+  prepare_transforms<false, true>(optin);
+  prepare_transforms<true, false>(optin);
+  prepare_transforms<true, true>(optin);
   for (const SplitEntry& e : kSplit) e.prepare(optin);
   prepare_recon_solve(optin);
 }

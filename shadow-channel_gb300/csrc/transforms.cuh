@@ -9,7 +9,8 @@
 // 3Nz/2 = 48, CH = 48 and NT = 192 every pass is an exact multiple of the
 // block.  Each 1D transform is the same fft_run sequence on the same data as
 // in the one-block-per-plane kernels, so every variant gives identical
-// results; the autotuner picks the fastest per grid.
+// results; the autotuner picks the fastest per grid.  Lengths 3 * 2^i * 3^j
+// only (radices 2, 3, 4).
 #pragma once
 
 #include <algorithm>
@@ -61,7 +62,7 @@ __global__ void __launch_bounds__(NT) k_tz_inv(const __grid_constant__ Grid g0, 
   }
   __syncthreads();
   const FftPlan plan = make_plan(g.pz, true);
-  const cpx* zr = fft_run(plan, b0, b1, nc, nc, 1, tw, +1, true);
+  const cpx* zr = fft_run<false>(plan, b0, b1, nc, nc, 1, tw, +1, true);
   for (int i = threadIdx.x; i < g.pz * nc; i += NT) {
     const int zp = i / nc, cl = i - zp * nc;
     const int gc = c0 + cl, x = gc / nf, f = gc - x * nf;
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(NT) k_tx_inv(const __grid_constant__ Grid g0, 
   }
   __syncthreads();
   const FftPlan plan = make_plan(g.px, true);
-  const cpx* xr = fft_run(plan, b0, b1, nr, 1, g.px, tw, +1, true);
+  const cpx* xr = fft_run<false>(plan, b0, b1, nr, 1, g.px, tw, +1, true);
   const size_t plane = (size_t)g.pz * g.px;
   bool nonfinite = false;
   for (int i = threadIdx.x; i < nr * 2 * g.px; i += NT) {
@@ -188,7 +189,7 @@ __global__ void __launch_bounds__(NT) k_tx_fwd(const __grid_constant__ Grid g0, 
   }
   __syncthreads();
   const FftPlan plan = make_plan(g.px, false);
-  const cpx* xr = fft_run(plan, b0, b1, nr, 1, g.px, tw, -1, true);
+  const cpx* xr = fft_run<false>(plan, b0, b1, nr, 1, g.px, tw, -1, true);
   const double hn = 0.5 * g.norm;
   for (int i = threadIdx.x; i < nr * g.X; i += NT) {
     const int rl = i / g.X, k = i - rl * g.X;
@@ -232,7 +233,7 @@ __global__ void __launch_bounds__(NT) k_tz_fwd(const __grid_constant__ Grid g0, 
   }
   __syncthreads();
   const FftPlan plan = make_plan(g.pz, false);
-  const cpx* zr = fft_run(plan, b0, b1, nc, nc, 1, tw, -1, true);
+  const cpx* zr = fft_run<false>(plan, b0, b1, nc, nc, 1, tw, -1, true);
   cpx* __restrict__ H = a.H.at(inst);
   for (int i = threadIdx.x; i < g.pz * nc; i += NT) {
     const int zp = i / nc, cl = i - zp * nc;
@@ -319,6 +320,7 @@ void prepare_split_t(int optin) {
 
 template <int CH>
 bool split_fits_t(const Grid& g, int optin) {
+  if (g.general) return false;  // the split passes compile radices 2, 3, 4 only
   const size_t room = (size_t)optin - 4096;
   return tz_smem<CH>(g, true) <= room && tx_smem<CH>(g) <= room;
 }
