@@ -29,23 +29,34 @@ struct PhysSmem {
   double* cfl;
 };
 
-__device__ inline PhysSmem carve(const Grid& g, unsigned char* base, bool with_cfl) {
+// Three buffer regions: A (the larger of a z block and an x block), B (a z
+// block), C (an x block).  The z result is dead once it is packed into the x
+// rows (inverse), and the x result once its kept bins are extracted
+// (forward), so one region serves both phases:
+//   inverse: z ping-pong A <-> B, x ping-pong C <-> A
+//   forward: x ping-pong C <-> A, z ping-pong B <-> A
+__device__ inline PhysSmem carve(const Grid& g, unsigned char* base, bool with_cfl, bool forward) {
   PhysSmem s;
   const int npair = (g.pz + 1) / 2;
+  const size_t zsz = (size_t)g.pz * g.X, xsz = (size_t)npair * g.px;
   cpx* p = reinterpret_cast<cpx*>(base);
   s.twz = p; p += g.pz;
   s.twx = p; p += g.px;
-  s.zb0 = p; p += (size_t)g.pz * g.X;
-  s.zb1 = p; p += (size_t)g.pz * g.X;
-  s.xb0 = p; p += (size_t)npair * g.px;
-  s.xb1 = p; p += (size_t)npair * g.px;
+  cpx* A = p; p += zsz > xsz ? zsz : xsz;
+  cpx* B = p; p += zsz;
+  cpx* C = p; p += xsz;
+  s.xb0 = C;
+  s.xb1 = A;
+  s.zb0 = forward ? B : A;
+  s.zb1 = forward ? A : B;
   s.cfl = with_cfl ? reinterpret_cast<double*>(p) : nullptr;
   return s;
 }
 
 __host__ __device__ inline size_t phys_smem_hd(const Grid& g, bool with_cfl) {
   const int npair = (g.pz + 1) / 2;
-  size_t n = (size_t)g.pz + g.px + 2 * (size_t)g.pz * g.X + 2 * (size_t)npair * g.px;
+  const size_t zsz = (size_t)g.pz * g.X, xsz = (size_t)npair * g.px;
+  size_t n = (size_t)g.pz + g.px + (zsz > xsz ? zsz : xsz) + zsz + xsz;
   size_t b = n * sizeof(cpx);
   if (with_cfl) b += (size_t)g.pz * g.px * sizeof(double);
   return b;
@@ -65,7 +76,7 @@ __global__ void __launch_bounds__(kThreads) k_phys_inverse(const __grid_constant
   if (y >= g.Q) return;
   if (a.skip_blocked && blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
-  PhysSmem s = carve(g, smem, a.cfl_check != 0);
+  PhysSmem s = carve(g, smem, a.cfl_check != 0, false);
   load_tw(g, s);
   const cpx* __restrict__ U = a.U.at(inst);
   double* __restrict__ P = a.P.at(inst);
@@ -175,7 +186,7 @@ __global__ void __launch_bounds__(kThreads) k_products_fwd(const __grid_constant
   if (y >= g.Q) return;
   if (blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
-  PhysSmem s = carve(g, smem, false);
+  PhysSmem s = carve(g, smem, false, true);
   load_tw(g, s);
   const size_t plane = (size_t)g.pz * g.px, fs = (size_t)g.Q * plane;
   const double* __restrict__ Pp = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane +
@@ -218,7 +229,7 @@ __global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant
   if (y >= g.Q) return;
   if (blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
-  PhysSmem s = carve(g, smem, false);
+  PhysSmem s = carve(g, smem, false, true);
   cpx* keep = reinterpret_cast<cpx*>(smem + phys_smem_hd(g, false));  // [6][Nz][X]
   load_tw(g, s);
   const size_t plane = (size_t)g.pz * g.px, fs = (size_t)g.Q * plane;
