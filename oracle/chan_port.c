@@ -1132,7 +1132,8 @@ static void project_mean(cport *s, int k, cpx *C, const cpx *H, cpx *U, cpx *sto
         for (int j = 0; j < q; ++j) flux_t += s->Rw[i * q + j] * Ca[i * X].re;
     if (mode == 0) {
         flux_t = s->flux - flux_t;
-        if (store) s->MFT[(store - s->MC) / s->csz] = flux_t;
+        if (store && store >= s->MC && store < s->MC + (3 * (size_t)s->nsteps + 1) * s->csz)
+            s->MFT[(store - s->MC) / s->csz] = flux_t;
     }
     else if (mode == 1) flux_t = 2.0 - flux_t;
     else flux_t = -flux_t;
@@ -1535,4 +1536,502 @@ const double *cport_table(cport *s, int which)
                           s->Qs, s->Qps, s->Qpps, s->Rs, s->Rps };
     if (which < 0 || which >= (int)(sizeof(t) / sizeof(t[0]))) return NULL;
     return t[which];
+}
+
+/* ================================================================== */
+/* Exact discrete adjoint of the homogeneous tangent step (no reference */
+/* counterpart: the reference's adjoint, cport_adjoint, integrates the  */
+/* continuous adjoint equations with reversed RK coefficients and is    */
+/* not the transpose of its tangent).  Reverse mode by hand of          */
+/* cport_tangent_forcing(kind 0): every linear piece of a tangent        */
+/* substage is transposed with respect to the Euclidean inner product   */
+/* of the real and imaginary parts of all coefficients.                 */
+/* ================================================================== */
+
+/* smmult transposed: ybar += A^T bbar */
+static void smmult_T(const double *A, const cpx *bbar, cpx *ybar, int dl, int du, int N, int X, int x0)
+{
+#define A3(i, j, x) A[((size_t)(i) * 9 + (j)) * X + (x)]
+    for (int i = 0; i < N; ++i)
+        for (int j = MAXI(0, dl - (i / 2)); j < MINI(dl + du + 1, (N - i + 1) / 2 + dl); ++j)
+            for (int x = x0; x < X; ++x) {
+                ybar[(i - 2 * (dl - j)) * X + x].re += A3(i, j, x) * bbar[i * X + x].re;
+                ybar[(i - 2 * (dl - j)) * X + x].im += A3(i, j, x) * bbar[i * X + x].im;
+            }
+#undef A3
+}
+
+/* bsolve transposed: solves A^T y = b in place with the same no-pivot
+   every-other-diagonal factorisation A = L U (U^T first, then L^T) */
+static void bsolve_T(double *A, cpx *b, int dl, int du, int N, int X, int x0)
+{
+#define A3(i, j, x) A[((size_t)(i) * 9 + (j)) * X + (x)]
+    for (int i = 2; i < N; ++i) {
+        for (int j = MAXI(0, dl - (i / 2)); j < dl; ++j) {
+            for (int k = 1; k <= j - MAXI(0, dl - (i / 2)); ++k)
+                for (int x = x0; x < X; ++x)
+                    A3(i, j, x) = A3(i, j, x) - A3(i, j - k, x) * A3(i - 2 * (dl - j + k), dl + k, x);
+            for (int x = x0; x < X; ++x) A3(i, j, x) = A3(i, j, x) / A3(i - 2 * (dl - j), dl, x);
+        }
+        for (int j = 0; j < MINI(du, (N - i + 1) / 2); ++j)
+            for (int k = 1; k <= MINI(i / 2, MINI(dl, du - j)); ++k)
+                for (int x = x0; x < X; ++x)
+                    A3(i, j + dl, x) = A3(i, j + dl, x) - A3(i, dl - k, x) * A3(i - 2 * k, dl + j + k, x);
+    }
+    /* U^T w = b, U(m, m + 2j) = A[m][dl + j]: ascending */
+    for (int i = 0; i < N; ++i) {
+        for (int j = 1; j <= du; ++j) {
+            const int m = i - 2 * j;
+            if (m < 0) break;
+            if (j > MINI(du, ((N - m + 1) / 2 - 1))) continue;
+            for (int x = x0; x < X; ++x) {
+                b[i * X + x].re -= A3(m, dl + j, x) * b[m * X + x].re;
+                b[i * X + x].im -= A3(m, dl + j, x) * b[m * X + x].im;
+            }
+        }
+        for (int x = x0; x < X; ++x) {
+            b[i * X + x].re /= A3(i, dl, x);
+            b[i * X + x].im /= A3(i, dl, x);
+        }
+    }
+    /* L^T y = w, L(m, m - 2(dl - j)) = A[m][j], unit diagonal: descending */
+    for (int i = N - 1; i >= 0; --i)
+        for (int j = 0; j < dl; ++j) {
+            const int m = i + 2 * (dl - j);
+            if (m >= N || m < 2 || j < MAXI(0, dl - (m / 2))) continue;
+            for (int x = x0; x < X; ++x) {
+                b[i * X + x].re -= A3(m, j, x) * b[m * X + x].re;
+                b[i * X + x].im -= A3(m, j, x) * b[m * X + x].im;
+            }
+        }
+#undef A3
+}
+
+/* single-matrix versions (mean mode), element strides bs / ys */
+static void smmult_single_T(const double *A, int w, const cpx *bbar, int bs, cpx *ybar, int ys, int dl, int du, int N)
+{
+    for (int i = 0; i < N; ++i)
+        for (int j = MAXI(0, dl - (i / 2)); j < MINI(dl + du + 1, (N - i + 1) / 2 + dl); ++j) {
+            ybar[(i - 2 * (dl - j)) * ys].re += A[i * w + j] * bbar[i * bs].re;
+            ybar[(i - 2 * (dl - j)) * ys].im += A[i * w + j] * bbar[i * bs].im;
+        }
+}
+
+static void bsolve_single_T(double *A, int w, cpx *b, int bs, int dl, int du, int N)
+{
+#define A2(i, j) A[(size_t)(i) * w + (j)]
+    for (int i = 2; i < N; ++i) {
+        for (int j = MAXI(0, dl - (i / 2)); j < dl; ++j) {
+            for (int k = 1; k <= j - MAXI(0, dl - (i / 2)); ++k)
+                A2(i, j) = A2(i, j) - A2(i, j - k) * A2(i - 2 * (dl - j + k), dl + k);
+            A2(i, j) = A2(i, j) / A2(i - 2 * (dl - j), dl);
+        }
+        for (int j = 0; j < MINI(du, (N - i + 1) / 2); ++j)
+            for (int k = 1; k <= MINI(i / 2, MINI(dl, du - j)); ++k)
+                A2(i, j + dl) = A2(i, j + dl) - A2(i, dl - k) * A2(i - 2 * k, dl + j + k);
+    }
+    for (int i = 0; i < N; ++i) {
+        for (int j = 1; j <= du; ++j) {
+            const int m = i - 2 * j;
+            if (m < 0) break;
+            if (j > MINI(du, ((N - m + 1) / 2 - 1))) continue;
+            b[i * bs].re -= A2(m, dl + j) * b[m * bs].re;
+            b[i * bs].im -= A2(m, dl + j) * b[m * bs].im;
+        }
+        b[i * bs].re /= A2(i, dl);
+        b[i * bs].im /= A2(i, dl);
+    }
+    for (int i = N - 1; i >= 0; --i)
+        for (int j = 0; j < dl; ++j) {
+            const int m = i + 2 * (dl - j);
+            if (m >= N || m < 2 || j < MAXI(0, dl - (m / 2))) continue;
+            b[i * bs].re -= A2(m, j) * b[m * bs].re;
+            b[i * bs].im -= A2(m, j) * b[m * bs].im;
+        }
+#undef A2
+}
+
+/* recon_line transposed: Ub (5 components of line z) -> Cb (accumulate) */
+static void recon_line_T(cport *s, const cpx *Ub, cpx *Cb, int z, int x0)
+{
+    const int X = s->X, q = s->qpts, D = s->dimQ, R = s->dimR;
+    const double kz = s->Kz[z];
+    for (int i = 0; i < q; ++i)
+        for (int x = x0; x < X; ++x) {
+            const double kx = s->Kx[x], k2 = s->K2[z * X + x];
+            const cpx ux = Ub[UI(s, z, XEL, i, x)], uz = Ub[UI(s, z, ZEL, i, x)];
+            const cpx dx = Ub[UI(s, z, DXEL, i, x)], dz = Ub[UI(s, z, DZEL, i, x)];
+            /* forward: u = -i (kx Xp + kz Zp)/k2, w = i (kx Zp - kz Xp)/k2 with
+               Xp = -Qp a, Zp = R b; du = i (kx dx - kz dz)/k2, dw = i (kx dz + kz dx)/k2
+               with dx = Qpp a, dz = Rp b */
+            cpx xp, zp, ddx, ddz;
+            xp.re = (-kx * ux.im - kz * uz.im) / k2;   /* (i kx u + i kz w)/k2 */
+            xp.im = (kx * ux.re + kz * uz.re) / k2;
+            zp.re = (-kz * ux.im + kx * uz.im) / k2;   /* (i kz u - i kx w)/k2 */
+            zp.im = (kz * ux.re - kx * uz.re) / k2;
+            ddx.re = (kx * dx.im + kz * dz.im) / k2;   /* -(i kx du + i kz dw)/k2 */
+            ddx.im = (-kx * dx.re - kz * dz.re) / k2;
+            ddz.re = (-kz * dx.im + kx * dz.im) / k2;  /* (i kz du - i kx dw)/k2 */
+            ddz.im = (kz * dx.re - kx * dz.re) / k2;
+            const cpx v = Ub[UI(s, z, YEL, i, x)];
+            for (int j = 0; j < D; ++j) {
+                cpx *a = &Cb[CI(s, z, ALPHA, j, x)];
+                a->re += s->Q[i * D + j] * v.re - s->Qp[i * D + j] * xp.re + s->Qpp[i * D + j] * ddx.re;
+                a->im += s->Q[i * D + j] * v.im - s->Qp[i * D + j] * xp.im + s->Qpp[i * D + j] * ddx.im;
+            }
+            for (int j = 0; j < R; ++j) {
+                cpx *b = &Cb[CI(s, z, BETA, j, x)];
+                b->re += s->R[i * R + j] * zp.re + s->Rp[i * R + j] * ddz.re;
+                b->im += s->R[i * R + j] * zp.im + s->Rp[i * R + j] * ddz.im;
+            }
+        }
+}
+
+static void recon_mean_T(cport *s, const cpx *Ub, cpx *Cb)
+{
+    const int q = s->qpts, R = s->dimR;
+    for (int i = 0; i < q; ++i) {
+        const cpx u = Ub[UI(s, 0, XEL, i, 0)], du = Ub[UI(s, 0, DXEL, i, 0)];
+        const cpx w = Ub[UI(s, 0, ZEL, i, 0)], dw = Ub[UI(s, 0, DZEL, i, 0)];
+        for (int j = 0; j < R; ++j) {
+            cpx *a = &Cb[CI(s, 0, ALPHA, j, 0)], *b = &Cb[CI(s, 0, BETA, j, 0)];
+            a->re += s->R[i * R + j] * u.re + s->Rp[i * R + j] * du.re;
+            a->im += s->R[i * R + j] * u.im + s->Rp[i * R + j] * du.im;
+            b->re += s->R[i * R + j] * w.re + s->Rp[i * R + j] * dw.re;
+            b->im += s->R[i * R + j] * w.im + s->Rp[i * R + j] * dw.im;
+        }
+    }
+}
+
+static void recon_T(cport *s, const cpx *Ub, cpx *Cb)
+{
+    recon_mean_T(s, Ub, Cb);
+    recon_line_T(s, Ub, Cb, 0, 1);
+    for (int z = 1; z < s->Nz; ++z)
+        if (z != s->Nz / 2) recon_line_T(s, Ub, Cb, z, 0);
+}
+
+/* rhs_fa / rhs_fb transposed: Fa_bar (D rows), Fb_bar (R rows) of line z -> Hbar (accumulate) */
+static void quad_line_T(cport *s, const cpx *Fab, const cpx *Fbb, cpx *Hb, int z, int x0)
+{
+    const int X = s->X, D = s->dimQ, R = s->dimR, q = s->qpts;
+    const double kz = s->Kz[z];
+    for (int j = 0; j < q; ++j)
+        for (int x = x0; x < X; ++x) {
+            const double kx = s->Kx[x], k2 = s->K2[z * X + x];
+            cpx pa = {0.0, 0.0}, qa = {0.0, 0.0}, rb = {0.0, 0.0};
+            for (int i = 0; i < D; ++i) {
+                pa.re += s->Qpw[i * q + j] * Fab[i * X + x].re;
+                pa.im += s->Qpw[i * q + j] * Fab[i * X + x].im;
+                qa.re += s->Qw[i * q + j] * Fab[i * X + x].re;
+                qa.im += s->Qw[i * q + j] * Fab[i * X + x].im;
+            }
+            for (int i = 0; i < R; ++i) {
+                rb.re += s->Rw[i * q + j] * Fbb[i * X + x].re;
+                rb.im += s->Rw[i * q + j] * Fbb[i * X + x].im;
+            }
+            /* forward: Fa = Qpw (i kx Hx + i kz Hz) - K2 Qw Hy, Fb = Rw (i kz Hx - i kx Hz) */
+            cpx *hx = &Hb[UI(s, z, HXEL, j, x)], *hy = &Hb[UI(s, z, HYEL, j, x)], *hz = &Hb[UI(s, z, HZEL, j, x)];
+            hx->re += kx * pa.im + kz * rb.im;      /* -i kx pa - i kz rb */
+            hx->im += -kx * pa.re - kz * rb.re;
+            hz->re += kz * pa.im - kx * rb.im;      /* -i kz pa + i kx rb */
+            hz->im += -kz * pa.re + kx * rb.re;
+            hy->re += -k2 * qa.re;
+            hy->im += -k2 * qa.im;
+        }
+}
+
+/* primal real fields of one state on every plane: [Q][MAXT][pz][hx], as pass1 */
+static void primal_fields(cport *s, const cpx *C, cpx *out)
+{
+    recon(s, C, s->U);
+    const size_t per = (size_t)MAXT * s->pz * s->hx;
+    for (int y = 0; y < s->qpts; ++y) {
+        cpx *T = out + (size_t)y * per;
+        memset(T, 0, sizeof(cpx) * per);
+        load_curl(s, T, s->U, y);
+        for (int i = 0; i < MAXT; ++i) inverse_field(s, T, i);
+    }
+}
+
+/* the tangent half of pass1 transposed: Hbar (slots HZ, HX, HY of the kept
+   modes) -> Ubar (5 components, accumulate); RTs the primal real fields */
+static void pass1_T(cport *s, const cpx *RTs, const cpx *Hb, cpx *Ub)
+{
+    const int pz = s->pz, px = s->px, hx = s->hx, rp = px + 2, X = s->X, Nz = s->Nz;
+    const size_t idx = (size_t)pz * rp, per = (size_t)MAXT * pz * hx;
+    const double norm = 1.0 / ((3. * s->Nx / 2.) * (3. * s->Nz / 2.));
+    cpx *NT = s->ICT;  /* product cotangents [3][pz][hx] */
+    cpx *FT = s->CT;   /* field cotangents [6][pz][hx] */
+    for (int y = 0; y < s->qpts; ++y) {
+        const double *RT = (const double *)(RTs + (size_t)y * per);
+        memset(NT, 0, sizeof(cpx) * (size_t)3 * pz * hx);
+        /* store_field and scale_field transposed: kept rows, x < X */
+        for (int c = 0; c < 3; ++c)
+            for (int zp = 0; zp < pz; ++zp) {
+                int z = -1;
+                if (zp < Nz / 2) z = zp;
+                else if (zp > Nz) z = zp - Nz / 2;
+                if (z < 0) continue;
+                for (int x = 0; x < X; ++x) {
+                    const cpx h = Hb[UI(s, z, c, y, x)];
+                    NT[TI(s, c, zp, x)].re = norm * h.re;
+                    NT[TI(s, c, zp, x)].im = norm * h.im;
+                }
+            }
+        for (int c = 0; c < 3; ++c) {
+            cpx *base = &NT[TI(s, c, 0, 0)];
+            /* the z transform (sign -1) transposed: sign +1, columns x < X */
+            for (int x = 0; x < X; ++x) offt_exec(s->pf1, base + x, hx, base + x, hx);
+            /* the real-to-complex x transform transposed: halve bins 1..px/2-1, then c2r */
+            for (int zp = 0; zp < pz; ++zp) {
+                cpx *row = base + (size_t)zp * hx;
+                for (int k = 1; k < hx - 1; ++k) { row[k].re *= 0.5; row[k].im *= 0.5; }
+                offt_c2r(s->pr1, row, 1, (double *)row, 1);
+            }
+        }
+        const double *NR = (const double *)NT;
+        double *FR = (double *)FT;
+        memset(FT, 0, sizeof(cpx) * per);
+        /* the tangent products (pass1.c:145-170) transposed */
+        for (int zp = 0; zp < pz; ++zp)
+            for (int x = 0; x < px; ++x) {
+                const size_t o = (size_t)zp * rp + x;
+                const double nx = NR[HXEL * idx + o], ny = NR[HYEL * idx + o], nz = NR[HZEL * idx + o];
+                const double u = RT[XEL * idx + o], v = RT[YEL * idx + o], w = RT[ZEL * idx + o];
+                const double wz = RT[WZEL * idx + o], wx = RT[WXEL * idx + o], wy = RT[WYEL * idx + o];
+                FR[XEL * idx + o] = -ny * wz + nz * wy;
+                FR[YEL * idx + o] = nx * wz - nz * wx;
+                FR[ZEL * idx + o] = -nx * wy + ny * wx;
+                FR[WZEL * idx + o] = nx * v - ny * u;
+                FR[WXEL * idx + o] = ny * w - nz * v;
+                FR[WYEL * idx + o] = -nx * w + nz * u;
+            }
+        for (int f = 0; f < MAXT; ++f) {
+            cpx *base = &FT[TI(s, f, 0, 0)];
+            /* c2r transposed: r2c, double bins 1..px/2-1 */
+            for (int zp = 0; zp < pz; ++zp) {
+                cpx *row = base + (size_t)zp * hx;
+                offt_r2c(s->pr2, (double *)row, 1, row, 1);
+                for (int k = 1; k < hx - 1; ++k) { row[k].re *= 2.0; row[k].im *= 2.0; }
+            }
+            /* the inverse z transform (sign +1) transposed: sign -1, columns x < X */
+            for (int x = 0; x < X; ++x) offt_exec(s->pf2, base + x, hx, base + x, hx);
+        }
+        /* load_curl transposed: wz = -du + i kx v, wx = dw - i kz v, wy = i kz u - i kx w */
+        for (int zp = 0; zp < pz; ++zp) {
+            int z = -1;
+            if (zp < Nz / 2) z = zp;
+            else if (zp > Nz) z = zp - Nz / 2;
+            if (z < 0) continue;
+            const double kz = s->Kz[z];
+            for (int x = 0; x < X; ++x) {
+                const double kx = s->Kx[x];
+                const cpx t0 = FT[TI(s, XEL, zp, x)], t1 = FT[TI(s, YEL, zp, x)], t2 = FT[TI(s, ZEL, zp, x)];
+                const cpx t3 = FT[TI(s, WZEL, zp, x)], t4 = FT[TI(s, WXEL, zp, x)], t5 = FT[TI(s, WYEL, zp, x)];
+                cpx *uu = &Ub[UI(s, z, XEL, y, x)], *vv = &Ub[UI(s, z, YEL, y, x)], *ww = &Ub[UI(s, z, ZEL, y, x)];
+                cpx *dx = &Ub[UI(s, z, DXEL, y, x)], *dz = &Ub[UI(s, z, DZEL, y, x)];
+                /* u += t0 - i kz t5 ; v += t1 - i kx t3 + i kz t4 ; w += t2 + i kx t5 */
+                uu->re += t0.re + kz * t5.im;
+                uu->im += t0.im - kz * t5.re;
+                vv->re += t1.re + kx * t3.im - kz * t4.im;
+                vv->im += t1.im - kx * t3.re + kz * t4.re;
+                ww->re += t2.re - kx * t5.im;
+                ww->im += t2.im + kx * t5.re;
+                dx->re -= t3.re;
+                dx->im -= t3.im;
+                dz->re += t4.re;
+                dz->im += t4.im;
+            }
+        }
+    }
+}
+
+/* one substage reversed.  In: cb (carried cotangent after the substage) and
+   ub (velocity cotangent after it); out: the same before the substage.  Hb
+   is scratch of the U size; RTs the primal fields of substage k. */
+static void substage_T(cport *s, int k, cpx *cb, cpx *ub, cpx *Hb, cpx *xb, const cpx *RTs)
+{
+    const int X = s->X, D = s->dimQ, R = s->dimR, q = s->qpts;
+    const double *a = fa_, *b = fb_, *c = fc_, *d = fd_;
+    memset(Hb, 0, sizeof(cpx) * s->usz);
+    memset(xb, 0, sizeof(cpx) * s->csz);
+    recon_T(s, ub, xb);
+    memset(ub, 0, sizeof(cpx) * s->usz);
+    /* ---- mean mode ---- */
+    {
+        double *MZ = s->MZ;
+        cpx *xa = &xb[CI(s, 0, ALPHA, 0, 0)], *xbb = &xb[CI(s, 0, BETA, 0, 0)];
+        cpx *ca = &cb[CI(s, 0, ALPHA, 0, 0)], *cbb = &cb[CI(s, 0, BETA, 0, 0)];
+        cpx *fab = s->fa, *fbb = s->fb;
+        memset(fab, 0, sizeof(cpx) * R);
+        memset(fbb, 0, sizeof(cpx) * R);
+        if (k != 2) {
+            for (int i = 0; i < R; ++i)
+                for (int j = 0; j < T_RSDIAG; ++j) MZ[i * 5 + j] = s->Rs[i * 5 + j] - s->re * a[k + 1] * s->dt * s->Rps[i * 5 + j];
+            smmult_single_T(MZ, 5, ca, X, xa, X, RSDIAG - 1, RSDIAG - 1, R);
+            smmult_single_T(MZ, 5, cbb, X, xbb, X, RSDIAG - 1, RSDIAG - 1, R);
+            for (int i = 0; i < R; ++i) {
+                fab[i].re = s->dt * d[k + 1] * ca[i * X].re;
+                fbb[i].re = s->dt * d[k + 1] * cbb[i * X].re;
+            }
+        } else {
+            for (int i = 0; i < R; ++i) {
+                xa[i * X].re += ca[i * X].re; xa[i * X].im += ca[i * X].im;
+                xbb[i * X].re += cbb[i * X].re; xbb[i * X].im += cbb[i * X].im;
+            }
+        }
+        /* homogeneous flux correction x = xs + 0.5 add (-rwsum . xs.re), transposed */
+        for (int i = 0; i < R; ++i)
+            for (int j = 0; j < T_RSDIAG; ++j) MZ[i * 5 + j] = s->Rs[i * 5 + j];
+        memset(s->add, 0, sizeof(cpx) * (size_t)R);
+        for (int i = 0; i < R; ++i)
+            for (int j = 0; j < q; ++j) s->add[i].re += s->Rw[i * q + j];
+        bsolve_single(MZ, 5, s->add, 1, RSDIAG - 1, RSDIAG - 1, R);
+        double ax = 0.0;
+        for (int j = 0; j < R; ++j) ax += s->add[j].re * xa[j * X].re;
+        for (int i = 0; i < R; ++i) {
+            double rws = 0.0;
+            for (int j = 0; j < q; ++j) rws += s->Rw[i * q + j];
+            xa[i * X].re -= 0.5 * rws * ax;
+        }
+        for (int v = 0; v < 2; ++v) {
+            for (int i = 0; i < R; ++i)
+                for (int j = 0; j < T_RSDIAG; ++j) MZ[i * 5 + j] = s->Rs[i * 5 + j] + s->re * b[k] * s->dt * s->Rps[i * 5 + j];
+            bsolve_single_T(MZ, 5, v == ALPHA ? xa : xbb, X, RSDIAG - 1, RSDIAG - 1, R);
+        }
+        for (int i = 0; i < R; ++i) {
+            fab[i].re += s->dt * c[k] * xa[i * X].re;
+            fbb[i].re += s->dt * c[k] * xbb[i * X].re;
+        }
+        for (int i = 0; i < R; ++i) { ca[i * X].re = 0; ca[i * X].im = 0; cbb[i * X].re = 0; cbb[i * X].im = 0; }
+        if (k == 0) {
+            for (int i = 0; i < R; ++i)
+                for (int j = 0; j < T_RSDIAG; ++j) MZ[i * 5 + j] = s->Rs[i * 5 + j] - s->re * a[0] * s->dt * s->Rps[i * 5 + j];
+            smmult_single_T(MZ, 5, xa, X, ca, X, RSDIAG - 1, RSDIAG - 1, R);
+            smmult_single_T(MZ, 5, xbb, X, cbb, X, RSDIAG - 1, RSDIAG - 1, R);
+        } else {
+            for (int i = 0; i < R; ++i) { ca[i * X] = xa[i * X]; cbb[i * X] = xbb[i * X]; }
+        }
+        /* the mean quadrature fa = Rw Hx.re, fb = Rw Hz.re transposed */
+        for (int j = 0; j < q; ++j) {
+            double sa = 0.0, sb = 0.0;
+            for (int i = 0; i < R; ++i) { sa += s->Rw[i * q + j] * fab[i].re; sb += s->Rw[i * q + j] * fbb[i].re; }
+            Hb[UI(s, 0, HXEL, j, 0)].re += sa;
+            Hb[UI(s, 0, HZEL, j, 0)].re += sb;
+        }
+    }
+    /* ---- lines ---- */
+    for (int z = 0; z < s->Nz; ++z) {
+        const int x0 = z == 0 ? 1 : 0;
+        cpx *Ca = &cb[CI(s, z, ALPHA, 0, 0)], *Cbt = &cb[CI(s, z, BETA, 0, 0)];
+        cpx *Xa = &xb[CI(s, z, ALPHA, 0, 0)], *Xbt = &xb[CI(s, z, BETA, 0, 0)];
+        if (z == s->Nz / 2) {
+            for (int v = 0; v < 2; ++v)
+                for (int i = 0; i < R; ++i)
+                    for (int x = 0; x < X; ++x) { cb[CI(s, z, v, i, x)].re = 0; cb[CI(s, z, v, i, x)].im = 0; }
+            continue;
+        }
+        memset(s->Fa, 0, sizeof(cpx) * (size_t)R * X);
+        memset(s->Fb, 0, sizeof(cpx) * (size_t)R * X);
+        if (k != 2) {
+            fill_v_lhs(s, z, x0, a[k + 1], 0);
+            smmult_T(s->M, Ca, Xa, QSDIAG - 1, QSDIAG - 1, D, X, x0);
+            fill_g_lhs(s, z, x0, a[k + 1], 0);
+            smmult_T(s->M, Cbt, Xbt, RSDIAG - 1, RSDIAG - 1, R, X, x0);
+            for (int x = x0; x < X; ++x) {
+                for (int i = 0; i < D; ++i) {
+                    s->Fa[i * X + x].re = s->dt * d[k + 1] * Ca[i * X + x].re;
+                    s->Fa[i * X + x].im = s->dt * d[k + 1] * Ca[i * X + x].im;
+                }
+                for (int i = 0; i < R; ++i) {
+                    s->Fb[i * X + x].re = s->dt * d[k + 1] * Cbt[i * X + x].re;
+                    s->Fb[i * X + x].im = s->dt * d[k + 1] * Cbt[i * X + x].im;
+                }
+            }
+        } else {
+            for (int x = x0; x < X; ++x) {
+                for (int i = 0; i < D; ++i) { Xa[i * X + x].re += Ca[i * X + x].re; Xa[i * X + x].im += Ca[i * X + x].im; }
+                for (int i = 0; i < R; ++i) { Xbt[i * X + x].re += Cbt[i * X + x].re; Xbt[i * X + x].im += Cbt[i * X + x].im; }
+            }
+        }
+        /* alpha rows >= D ride along unchanged */
+        for (int x = x0; x < X; ++x)
+            for (int i = D; i < R; ++i) Xa[i * X + x] = Ca[i * X + x];
+        fill_v_lhs(s, z, x0, b[k], 1);
+        bsolve_T(s->M, Xa, QSDIAG - 1, QSDIAG - 1, D, X, x0);
+        fill_g_lhs(s, z, x0, b[k], 1);
+        bsolve_T(s->M, Xbt, RSDIAG - 1, RSDIAG - 1, R, X, x0);
+        for (int x = x0; x < X; ++x) {
+            for (int i = 0; i < D; ++i) {
+                s->Fa[i * X + x].re += s->dt * c[k] * Xa[i * X + x].re;
+                s->Fa[i * X + x].im += s->dt * c[k] * Xa[i * X + x].im;
+            }
+            for (int i = 0; i < R; ++i) {
+                s->Fb[i * X + x].re += s->dt * c[k] * Xbt[i * X + x].re;
+                s->Fb[i * X + x].im += s->dt * c[k] * Xbt[i * X + x].im;
+            }
+        }
+        for (int x = x0; x < X; ++x) {
+            for (int i = 0; i < D; ++i) { Ca[i * X + x].re = 0; Ca[i * X + x].im = 0; }
+            for (int i = D; i < R; ++i) Ca[i * X + x] = Xa[i * X + x];
+            for (int i = 0; i < R; ++i) { Cbt[i * X + x].re = 0; Cbt[i * X + x].im = 0; }
+        }
+        if (k == 0) {
+            fill_v_lhs(s, z, x0, a[0], 0);
+            smmult_T(s->M, Xa, Ca, QSDIAG - 1, QSDIAG - 1, D, X, x0);
+            fill_g_lhs(s, z, x0, a[0], 0);
+            smmult_T(s->M, Xbt, Cbt, RSDIAG - 1, RSDIAG - 1, R, X, x0);
+        } else {
+            for (int x = x0; x < X; ++x) {
+                for (int i = 0; i < D; ++i) Ca[i * X + x] = Xa[i * X + x];
+                for (int i = 0; i < R; ++i) Cbt[i * X + x] = Xbt[i * X + x];
+            }
+        }
+        quad_line_T(s, s->Fa, s->Fb, Hb, z, x0);
+    }
+    pass1_T(s, RTs, Hb, ub);
+}
+
+/* the transpose of cport_tangent_forcing(end -> start, kind 0) applied to
+   AC_given (the cotangent at start_step > end_step).  The tangent
+   linearises about the primal re-advanced from MC[3 end] rebuilt into
+   velocity (channel/channel.c:496-514, 557-571), which after a laminar start
+   without run-up differs from the stored trajectory, so the primal states
+   are re-advanced here the same way. */
+int cport_adjoint_exact(cport *s, int start_step, int end_step, double *AC_given)
+{
+    if (!(start_step > end_step && end_step >= 0 && start_step <= s->nsteps && AC_given)) return -2;
+    const int nst = start_step - end_step;
+    const size_t per = (size_t)s->qpts * MAXT * s->pz * s->hx;
+    cpx *X = (cpx *)malloc(sizeof(cpx) * s->csz * (3 * (size_t)nst + 1));
+    cpx *RTs = (cpx *)malloc(sizeof(cpx) * per);
+    cpx *cb = (cpx *)calloc(s->csz, sizeof(cpx));
+    cpx *xb = (cpx *)calloc(s->csz, sizeof(cpx));
+    cpx *ub = (cpx *)calloc(s->usz, sizeof(cpx));
+    cpx *Hb = (cpx *)calloc(s->usz, sizeof(cpx));
+    int status = 0;
+    if (!X || !RTs || !cb || !xb || !ub || !Hb) { status = -3; goto done; }
+    /* primal states before every substage, re-advanced as the tangent does */
+    memmove(s->C, s->MC + (size_t)end_step * 3 * s->csz, sizeof(cpx) * s->csz);
+    memcpy(X, s->C, sizeof(cpx) * s->csz);
+    recon(s, s->C, s->U);
+    for (int n = 0; n < nst && status == 0; ++n)
+        for (int k = 0; k < 3; ++k) {
+            if (pass1(s, k) != 0) { status = -1; break; }
+            solve_all(s, k, s->C, s->U, s->U, X + (size_t)(3 * n + k + 1) * s->csz, NULL, 0);
+        }
+    if (status) goto done;
+    memcpy(cb, AC_given, sizeof(cpx) * s->csz);
+    for (int n = nst - 1; n >= 0; --n)
+        for (int k = 2; k >= 0; --k) {
+            primal_fields(s, X + (size_t)(3 * n + k) * s->csz, RTs);
+            substage_T(s, k, cb, ub, Hb, xb, RTs);
+        }
+    /* the tangent starts from IU = Recon(IC) */
+    recon_T(s, ub, cb);
+    memcpy(AC_given, cb, sizeof(cpx) * s->csz);
+done:
+    free(X); free(RTs); free(cb); free(xb); free(ub); free(Hb);
+    return status;
 }

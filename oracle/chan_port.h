@@ -42,6 +42,10 @@ int cport_tangent(cport *s, int start_step, int end_step, double *IC_given,
 /* forcing 0 none, 1 mean flux, 2 Re (reference forcing reconnected), 3 Re (exact) */
 int cport_tangent_forcing(cport *s, int start_step, int end_step, double *IC_given,
                           int forcing);
+/* the transpose of the homogeneous tangent (cport_tangent_forcing kind 0)
+   from end_step to start_step (start > end) applied to AC_given in place;
+   no reference counterpart */
+int cport_adjoint_exact(cport *s, int start_step, int end_step, double *AC_given);
 int cport_adjoint(cport *s, int start_step, int end_step, double *AC_given,
                   int inhomo, double strength);
 /* channel.c:704 ddt_project() */

@@ -104,6 +104,7 @@ class PortChannel(_Base):
             L.cport_primal.argtypes = [_vp, _c_int, _vp]
             L.cport_tangent.argtypes = [_vp, _c_int, _c_int, _vp, _c_int]
             L.cport_tangent_forcing.argtypes = [_vp, _c_int, _c_int, _vp, _c_int]
+            L.cport_adjoint_exact.argtypes = [_vp, _c_int, _c_int, _vp]
             L.cport_adjoint.argtypes = [_vp, _c_int, _c_int, _vp, _c_int, _c_dbl]
             L.cport_ddt_project.argtypes = [_vp, _c_int, _vp]
             L.cport_ddt_project.restype = _c_dbl
@@ -159,6 +160,12 @@ class PortChannel(_Base):
     def adjoint(self, start, end, AC, inhomo, strength) -> int:
         _check_coef(AC, self.coef_shape)
         return self.lib().cport_adjoint(self._h, int(start), int(end), _ptr(AC), int(inhomo), float(strength))
+
+    def adjoint_exact(self, start, end, AC) -> int:
+        """The transpose of the homogeneous tangent from end to start
+        (start > end) applied to AC in place."""
+        _check_coef(AC, self.coef_shape)
+        return self.lib().cport_adjoint_exact(self._h, int(start), int(end), _ptr(AC))
 
     def ddt_project(self, i_step, IC) -> float:
         _check_coef(IC, self.coef_shape)
