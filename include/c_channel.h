@@ -59,6 +59,15 @@ void c_tangent_forcing(int start_step, int end_step, chn_complex *IC_given,
 void c_adjoint(int start_step, int end_step, chn_complex *AC_given,
                int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup, int inhomo,
                double strength);
+/* The exact discrete adjoint: the transpose of the homogeneous tangent
+   (c_tangent with inhomo 0, c_tangent_forcing with forcing 0) from end_step
+   to start_step, applied in place to AC_given, the cotangent at
+   start_step > end_step: <AC, T v> = <T^T AC, v> in the Euclidean inner
+   product of the real and imaginary parts.  No reference counterpart: the
+   reference's adjoint (channel/channel.c:596-696) integrates the continuous
+   adjoint equations with reversed RK coefficients.  No ddt coupling. */
+void c_adjoint_exact(int start_step, int end_step, chn_complex *AC_given,
+                     int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup);
 
 /* channel.i:96-105 -> channel.c:704 ddt_project() */
 double c_ddt_project(int i_step, chn_complex *IC_given, int Nz_dup,
@@ -129,6 +138,9 @@ int c_batch_forward(int start_step, int end_step, chn_complex *C,
 /* adjoints; AC [nseg][...] in/out */
 int c_batch_adjoint(int start_step, int end_step, chn_complex *AC,
                     double strength);
+/* exact discrete adjoints (as c_adjoint_exact) on the stored primal
+   trajectories; AC [nseg][...] in/out */
+int c_batch_adjoint_exact(int start_step, int end_step, chn_complex *AC);
 /* MC / MIC of one segment at step i_step into out [Nz][2][dimR][Nx/2] */
 int c_batch_getsoln(int seg, int i_step, chn_complex *out);
 int c_batch_getincresoln(int seg, int i_step, chn_complex *out);
@@ -151,6 +163,7 @@ int c_batch_forward_dev(int start_step, int end_step, chn_complex *C,
                         chn_complex *IC, const int *inhomo);
 int c_batch_adjoint_dev(int start_step, int end_step, chn_complex *AC,
                         double strength);
+int c_batch_adjoint_exact_dev(int start_step, int end_step, chn_complex *AC);
 int c_batch_primal_dev(int ru_steps, chn_complex *C);
 int c_batch_tangent_dev(int start_step, int end_step, chn_complex *IC,
                         const int *inhomo);
@@ -211,6 +224,7 @@ int c_multi_forward(int start_step, int end_step, chn_complex *C,
                     chn_complex *IC, const int *inhomo);
 int c_multi_adjoint(int start_step, int end_step, chn_complex *AC,
                     double strength);
+int c_multi_adjoint_exact(int start_step, int end_step, chn_complex *AC);
 int c_multi_getsoln(int i, int i_step, chn_complex *out);
 
 /* Objectives and statistics of the stored trajectories, computed on the

@@ -6,6 +6,7 @@ reference's extension keeps working:
     c_primal(ru_steps, C)                  C: complex128 [Nz, 2, Ny-2, Nx/2], in place
     c_tangent(start, end, IC, inhomo)
     c_adjoint(start, end, AC, inhomo, strength)
+    c_adjoint_exact(start, end, AC)        transpose of the homogeneous tangent (no SWIG counterpart)
     c_ddt_project(i_step, IC) -> float
     c_getsoln(i_step) / c_getincresoln(i_step) -> ndarray (library-owned buffer)
     c_spec2phys(C, flow)                   flow: float64 [3, 3Nx/2, qpts, 3Nz/2]
@@ -48,6 +49,8 @@ _lib.c_tangent.argtypes = [_i, _i, _vp, _i, _i, _i, _i, _i]
 _lib.c_tangent.restype = None
 _lib.c_adjoint.argtypes = [_i, _i, _vp, _i, _i, _i, _i, _i, _d]
 _lib.c_adjoint.restype = None
+_lib.c_adjoint_exact.argtypes = [_i, _i, _vp, _i, _i, _i, _i]
+_lib.c_adjoint_exact.restype = None
 _lib.c_ddt_project.argtypes = [_i, _vp, _i, _i, _i, _i]
 _lib.c_ddt_project.restype = _d
 _lib.c_getsoln.argtypes = [_i, _pp, _ip, _ip, _ip, _ip]
@@ -89,6 +92,8 @@ _lib.c_batch_forward.argtypes = [_i, _i, _vp, _vp, _vp]
 _lib.c_batch_forward.restype = _i
 _lib.c_batch_adjoint.argtypes = [_i, _i, _vp, _d]
 _lib.c_batch_adjoint.restype = _i
+_lib.c_batch_adjoint_exact.argtypes = [_i, _i, _vp]
+_lib.c_batch_adjoint_exact.restype = _i
 _lib.c_batch_getsoln.argtypes = [_i, _i, _vp]
 _lib.c_batch_getsoln.restype = _i
 _lib.c_batch_getincresoln.argtypes = [_i, _i, _vp]
@@ -102,6 +107,8 @@ _lib.c_batch_forward_dev.argtypes = [_i, _i, _vp, _vp, _vp]
 _lib.c_batch_forward_dev.restype = _i
 _lib.c_batch_adjoint_dev.argtypes = [_i, _i, _vp, _d]
 _lib.c_batch_adjoint_dev.restype = _i
+_lib.c_batch_adjoint_exact_dev.argtypes = [_i, _i, _vp]
+_lib.c_batch_adjoint_exact_dev.restype = _i
 
 _lib.c_stream.argtypes = []
 _lib.c_stream.restype = _vp
@@ -125,6 +132,8 @@ _lib.c_multi_forward.argtypes = [_i, _i, _vp, _vp, _vp]
 _lib.c_multi_forward.restype = _i
 _lib.c_multi_adjoint.argtypes = [_i, _i, _vp, _d]
 _lib.c_multi_adjoint.restype = _i
+_lib.c_multi_adjoint_exact.argtypes = [_i, _i, _vp]
+_lib.c_multi_adjoint_exact.restype = _i
 _lib.c_multi_getsoln.argtypes = [_i, _i, _vp]
 _lib.c_multi_getsoln.restype = _i
 _lib.c_tangent_forcing.argtypes = [_i, _i, _vp, _i, _i, _i, _i, _i]
@@ -200,6 +209,14 @@ def c_tangent_forcing(start_step, end_step, IC_given, forcing):
 def c_adjoint(start_step, end_step, AC_given, inhomo, strength):
     p, s = _inplace4(AC_given, np.complex128, "c_adjoint")
     _lib.c_adjoint(int(start_step), int(end_step), p, *s, int(inhomo), float(strength))
+
+
+def c_adjoint_exact(start_step, end_step, AC_given):
+    """The transpose of the homogeneous tangent from end_step to start_step
+    (start_step > end_step), applied to AC_given in place: <AC, T v> equals
+    <T^T AC, v> for every v, with T v = c_tangent(end_step, start_step, v, 0)."""
+    p, s = _inplace4(AC_given, np.complex128, "c_adjoint_exact")
+    _lib.c_adjoint_exact(int(start_step), int(end_step), p, *s)
 
 
 def c_ddt_project(i_step, IC_given):

@@ -686,6 +686,86 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
   return true;
 }
 
+// One step of the exact discrete adjoint of the homogeneous tangent, for
+// step n = *step - 1 (the counter then moves down by one): substages 2, 1, 0
+// transposed.  w.Ca carries the state cotangent, w.Ul the velocity
+// cotangent, w.Uprev H_bar, w.Pl its physical fields; the primal fields of
+// the state before substage k, slot 3n + k of `traj` (segment stride
+// `tstride`), come from the field cache or are rebuilt into w.Pp.
+static bool enqueue_adjoint_exact_step(Engine& e, Work& w, bool cached, const cpx* traj, long long tstride) {
+  const Grid& g = e.T.g;
+  cudaStream_t st = e.st;
+  for (int k = 2; k >= 0; --k) {
+    SolveTArgs t{};
+    t.grids = w.gdev;
+    t.Ub = cb(w.Ul, w.usz);
+    t.Cc = mb(w.Ca, w.csz);
+    t.Hb = mb(w.Uprev, w.usz);
+    t.k = k;
+    t.final_only = 0;
+    t.ninst = w.nseg;
+    t.status = nullptr;
+    t.sdiv = 1;
+    LK(launch_solve_T(g, t, st));
+    PhysArgs ph{};
+    ph.grids = w.gdev;
+    ph.tmp = w.Zt;
+    ph.tmp_inst = w.zt_inst;
+    ph.U = cb(w.Uprev, w.usz);
+    ph.P = mbd(w.Pl, w.psz);
+    ph.pslot = noslot();
+    ph.nfields = 3;
+    ph.ninst = w.nseg;
+    ph.status = nullptr;
+    ph.sdiv = 1;
+    LK(launch_phys_inverse(g, ph, st));
+    Batch<const double> Pprim = cbd(w.Pp, w.psz);
+    SlotRef pslot = noslot();
+    if (cached) {
+      Pprim = cbd(w.Pc, w.cstride);
+      pslot = SlotRef{w.step, 3, k - 3, (long long)w.psz};  // slot 3(*step - 1) + k
+    } else {
+      ReconArgs r{};
+      r.grids = w.gdev;
+      r.C = cb(traj, tstride);
+      r.slot = SlotRef{w.step, 3, k - 3, (long long)w.csz};
+      r.U = mb(w.Up, w.usz);
+      r.ninst = w.nseg;
+      r.status = nullptr;
+      r.sdiv = 1;
+      LK(launch_recon(g, r, st));
+      PhysArgs pp{};
+      pp.grids = w.gdev;
+      pp.tmp = w.Zt;
+      pp.tmp_inst = w.zt_inst;
+      pp.U = cb(w.Up, w.usz);
+      pp.P = mbd(w.Pp, w.psz);
+      pp.pslot = noslot();
+      pp.nfields = 6;
+      pp.ninst = w.nseg;
+      pp.status = nullptr;
+      pp.sdiv = 1;
+      LK(launch_phys_inverse(g, pp, st));
+    }
+    ProdArgs a{};
+    a.grids = w.gdev;
+    a.tmp = w.Zt;
+    a.tmp_inst = w.zt_inst;
+    a.Pp = Pprim;
+    a.pdiv = 1;
+    a.pslot = pslot;
+    a.Pt = cbd(w.Pl, w.psz);
+    a.H = mb(w.Ul, w.usz);
+    a.ninst = w.nseg;
+    a.status = nullptr;
+    a.sdiv = 1;
+    a.exact = 1;
+    LK(launch_products_adj(g, a, st));
+  }
+  LK(launch_step_advance(w.step, -1, st));
+  return true;
+}
+
 // capture one step into a graph and replay it nsteps times
 template <typename F>
 static bool run_steps(Engine& e, int nsteps, F&& enqueue) {
@@ -1023,6 +1103,87 @@ static bool op_adjoint(Engine& e, Work& w, int start, int end, const cpx* AC, do
   return run_steps(e, start - end, [&] { return enqueue_adjoint_step(e, w, sdt, cached, cpl_cached); });
 }
 
+// The transpose of the homogeneous tangent from `end` to `start` applied to
+// AC (device, nseg arrays) at step `start`; the result (the cotangent at
+// step `end`) is left in w.Ca.  The tangent linearises about the primal
+// re-advanced from MC[3 end] rebuilt into velocity (channel/channel.c:496-514),
+// which is the stored trajectory except after a laminar start without
+// run-up with end == 0: then the primal is re-advanced here into a
+// temporary trajectory, as op_forward does.
+static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* AC) {
+  const size_t csz = w.csz;
+  const bool readvance = w.raw_start && end == 0;
+  cpx* scratch = nullptr;
+  double* scratch_ft = nullptr;
+  if (!reset_status(e, w)) return false;
+  if (readvance) {
+    const size_t tbytes = sizeof(cpx) * (size_t)w.nseg * (size_t)w.traj;
+    const size_t fbytes = sizeof(double) * (size_t)w.nseg * (3 * (size_t)w.nsteps + 1);
+    if (cudaMalloc(&scratch, tbytes) != cudaSuccess || cudaMalloc(&scratch_ft, fbytes) != cudaSuccess) {
+      cudaGetLastError();
+      if (scratch) cudaFree(scratch);
+      set_error(-1, "c_adjoint_exact: no device memory for the re-advanced primal trajectory");
+      return false;
+    }
+    CK(cudaMemcpy2DAsync(w.Cp, csz * sizeof(cpx), w.MC, w.traj * sizeof(cpx), csz * sizeof(cpx), w.nseg,
+                         cudaMemcpyDeviceToDevice, e.st));
+    CK(cudaMemcpyAsync(w.Sp, w.Cp, sizeof(cpx) * csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
+    CK(cudaMemcpy2DAsync(scratch, w.traj * sizeof(cpx), w.Cp, csz * sizeof(cpx), csz * sizeof(cpx), w.nseg,
+                         cudaMemcpyDeviceToDevice, e.st));
+    // the forward sweep stores into w.MC / w.Ft: point them at the scratch
+    // trajectory while its steps are enqueued
+    cpx* keep_mc = w.MC;
+    double* keep_ft = w.Ft;
+    w.MC = scratch;
+    w.Ft = scratch_ft;
+    bool ok = set_step(e, w, 0);
+    FwdOpts o{true, false, 0, 0u, false, false, true};
+    ok = ok && run_steps(e, start, [&] { return enqueue_forward_step(e, w, o); });
+    w.MC = keep_mc;
+    w.Ft = keep_ft;
+    if (!ok) {
+      cudaStreamSynchronize(e.st);
+      cudaFree(scratch);
+      cudaFree(scratch_ft);
+      return false;
+    }
+  }
+  bool ok = true;
+  const cpx* traj = readvance ? scratch : w.MC;
+  const bool cached = !readvance && w.cached(3 * end, 3 * start);
+  if (cudaMemcpyAsync(w.Ca, AC, sizeof(cpx) * csz * w.nseg, cudaMemcpyDeviceToDevice, e.st) != cudaSuccess ||
+      cudaMemsetAsync(w.Ul, 0, sizeof(cpx) * w.usz * w.nseg, e.st) != cudaSuccess) {
+    set_error(-1, "c_adjoint_exact: copy failed");
+    ok = false;
+  }
+  ok = ok && set_step(e, w, start);
+  ok = ok && run_steps(e, start - end, [&] { return enqueue_adjoint_exact_step(e, w, cached, traj, w.traj); });
+  if (ok) {
+    // the tangent starts from IU = Recon(IC)
+    SolveTArgs t{};
+    t.grids = w.gdev;
+    t.Ub = cb(w.Ul, w.usz);
+    t.Cc = mb(w.Ca, w.csz);
+    t.Hb = mb(nullptr, 0);
+    t.k = 0;
+    t.final_only = 1;
+    t.ninst = w.nseg;
+    t.status = nullptr;
+    t.sdiv = 1;
+    const cudaError_t le = launch_solve_T(e.T.g, t, e.st);
+    if (le != cudaSuccess) {
+      set_error(-1, "launch_solve_T: %s", cudaGetErrorString(le));
+      ok = false;
+    }
+  }
+  if (readvance) {
+    cudaStreamSynchronize(e.st);
+    cudaFree(scratch);
+    cudaFree(scratch_ft);
+  }
+  return ok;
+}
+
 // ---------------------------------------------------------------------------
 // helpers for the host-array API
 // ---------------------------------------------------------------------------
@@ -1242,6 +1403,23 @@ void c_adjoint(int start_step, int end_step, chn_complex* AC_given, int Nz_dup, 
   const size_t bytes = sizeof(cpx) * w.csz;
   if (!h2d(e, w.io, AC_given, bytes)) return;
   if (!op_adjoint(e, w, start_step, end_step, w.io, strength)) return;
+  if (!collect_status(e, w)) return;
+  d2h(e, AC_given, w.Ca, bytes);
+}
+
+void c_adjoint_exact(int start_step, int end_step, chn_complex* AC_given, int Nz_dup, int Nvar_dup, int Ny_dup,
+                     int Nx_dup) {
+  if (!need_init("c_adjoint_exact")) return;
+  Engine& e = *E;
+  Work& w = e.single;
+  check_coef_dims(e.T.g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
+  shape_assert(end_step < start_step, "end_step < start_step");
+  shape_assert(end_step >= 0, "end_step >= 0");
+  shape_assert(start_step <= e.nsteps, "start_step <= nsteps");
+  shape_assert(AC_given != nullptr, "AC_given != 0");
+  const size_t bytes = sizeof(cpx) * w.csz;
+  if (!h2d(e, w.io, AC_given, bytes)) return;
+  if (!op_adjoint_exact(e, w, start_step, end_step, w.io)) return;
   if (!collect_status(e, w)) return;
   d2h(e, AC_given, w.Ca, bytes);
 }
@@ -1494,6 +1672,19 @@ int c_batch_adjoint_dev(int start_step, int end_step, chn_complex* AC, double st
   return collect_status(*E, w) ? g_status : -1;
 }
 
+int c_batch_adjoint_exact_dev(int start_step, int end_step, chn_complex* AC) {
+  if (!batch_ready("c_batch_adjoint_exact_dev")) return g_status;
+  Work& w = E->batch;
+  if (!(end_step < start_step && end_step >= 0 && start_step <= E->batch.nsteps) || !AC) {
+    set_error(-4, "c_batch_adjoint_exact: need 0 <= end < start <= nsteps and the state array");
+    return -4;
+  }
+  if (!op_adjoint_exact(*E, w, start_step, end_step, reinterpret_cast<cpx*>(AC))) return g_status;
+  if (cudaMemcpyAsync(AC, w.Ca, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, E->st) != cudaSuccess)
+    return -1;
+  return collect_status(*E, w) ? g_status : -1;
+}
+
 // host-array variants: staged through the working set's own device buffers
 // (dC holds the primal states, io the tangent / adjoint states)
 int c_batch_primal(int ru_steps, chn_complex* C) {
@@ -1536,6 +1727,20 @@ int c_batch_adjoint(int start_step, int end_step, chn_complex* AC, double streng
   const size_t bytes = sizeof(cpx) * w.csz * w.nseg;
   if (!h2d(*E, w.io, AC, bytes)) return -1;
   const int rc = c_batch_adjoint_dev(start_step, end_step, reinterpret_cast<chn_complex*>(w.io), strength);
+  if (!d2h(*E, AC, w.io, bytes)) return -1;
+  return rc;
+}
+
+int c_batch_adjoint_exact(int start_step, int end_step, chn_complex* AC) {
+  if (!batch_ready("c_batch_adjoint_exact")) return g_status;
+  Work& w = E->batch;
+  if (!AC) {
+    set_error(-4, "c_batch_adjoint_exact: null state array");
+    return -4;
+  }
+  const size_t bytes = sizeof(cpx) * w.csz * w.nseg;
+  if (!h2d(*E, w.io, AC, bytes)) return -1;
+  const int rc = c_batch_adjoint_exact_dev(start_step, end_step, reinterpret_cast<chn_complex*>(w.io));
   if (!d2h(*E, AC, w.io, bytes)) return -1;
   return rc;
 }
@@ -1783,6 +1988,19 @@ int c_multi_adjoint(int start_step, int end_step, chn_complex* AC, double streng
   }
   if (!multi_h2d(w.io, AC, 1)) return -1;
   if (!op_adjoint(MX->e, w, start_step, end_step, w.io, strength)) return g_status;
+  if (!multi_d2h(AC, w.Ca, 1)) return -1;
+  return collect_status(MX->e, w) ? g_status : -1;
+}
+
+int c_multi_adjoint_exact(int start_step, int end_step, chn_complex* AC) {
+  if (!multi_ready("c_multi_adjoint_exact")) return g_status;
+  Work& w = MX->e.batch;
+  if (!(end_step < start_step && end_step >= 0 && start_step <= w.nsteps) || !AC) {
+    set_error(-4, "c_multi_adjoint_exact: need 0 <= end < start <= nsteps and the state array");
+    return -4;
+  }
+  if (!multi_h2d(w.io, AC, 1)) return -1;
+  if (!op_adjoint_exact(MX->e, w, start_step, end_step, w.io)) return g_status;
   if (!multi_d2h(AC, w.Ca, 1)) return -1;
   return collect_status(MX->e, w) ? g_status : -1;
 }

@@ -53,6 +53,10 @@ struct ProdArgs {
   cpx* tmp;                // split transforms: as PhysArgs::tmp
   int tmp_inst;
   const Grid* grids;       // uneven batch: grid of each instance
+  // adjoint products only: 1 = the exact transpose of the tangent products
+  // (Pt holds the physical fields of the scaled H_bar, slots Hz, Hx, Hy; H
+  // receives the velocity cotangent u, v, w, du/dy, dw/dy)
+  int exact;
 };
 
 // mean-mode variants (channel/project0.c:153-168, increproject0.c:209-214, adjproject0.c:153-167)
@@ -97,6 +101,22 @@ struct SolveArgs {
   const Grid* grids;        // uneven batch: grid of each instance
 };
 
+// One substage of the exact discrete adjoint of the homogeneous tangent
+// (adjoint_exact.cu), one block per (instance, kz line, kx tile): the
+// transpose of the quadrature, banded solve and reconstruction of a tangent
+// substage.  final_only: Cc += Recon^T(Ub) (the sweep's start state) only.
+struct SolveTArgs {
+  Batch<const cpx> Ub;      // velocity cotangent after the substage, U layout
+  Batch<cpx> Cc;            // carried cotangent: after the substage in, before it out (in place)
+  Batch<cpx> Hb;            // H_bar out, slots 0..2 (Hz, Hx, Hy), scaled for the inverse transform
+  int k;                    // RK substage 0..2
+  int final_only;
+  int ninst;
+  const uint32_t* status;
+  int sdiv;
+  const Grid* grids;        // uneven batch: grid of each instance
+};
+
 // one ddt_project / adjoint coupling for nseg segments (channel/channel.c:704-780)
 struct DdtArgs {
   const cpx* MC;            // segment s trajectory: MC + s * traj_stride
@@ -118,6 +138,7 @@ cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t s
 cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st);
+cudaError_t launch_solve_T(const Grid& g, const SolveTArgs& a, cudaStream_t st);
 
 // split-transform intermediate per instance, in complex elements
 size_t split_tmp_elems(const Grid& g);

@@ -8,7 +8,9 @@
 //                    channel/pass1.c:212-371
 //   k_products_adj   S = u x lambda, T = lambda x w, forward transforms and
 //                    the assembly H = -T + (i k) x S, keeping S_x, S_z.
-//                    channel/pass2.c:224-566
+//                    channel/pass2.c:224-566.  With `exact`: the transpose
+//                    of the tangent products and of the vorticity load
+//                    (the exact discrete adjoint, adjoint_exact.cu).
 //
 // Every transform is an FP64 shared-memory Stockham FFT (fft.cuh).  The x
 // transforms of two real rows share one complex FFT (row pairs packed as
@@ -159,10 +161,11 @@ __global__ void __launch_bounds__(kThreads) k_phys_inverse(const __grid_constant
 // forward transform of the product rows held in xb0; leaves the kept,
 // scaled spectral rows in the returned z buffer
 template <bool GEN>
-__device__ inline cpx* forward_plane(const Grid& g, PhysSmem& s, const FftPlan& pxF, const FftPlan& pzF) {
+__device__ inline cpx* forward_plane(const Grid& g, PhysSmem& s, const FftPlan& pxF, const FftPlan& pzF,
+                                     double scale) {
   const int npair = (g.pz + 1) / 2;
   cpx* xr = fft_run<GEN>(pxF, s.xb0, s.xb1, npair, 1, g.px, s.twx, -1, true);
-  const double hn = 0.5 * g.norm;
+  const double hn = 0.5 * scale;
   for (int i = threadIdx.x; i < npair * g.X; i += blockDim.x) {
     const int p = i / g.X, k = i - p * g.X;
     const cpx Zk = xr[p * g.px + k];
@@ -208,7 +211,7 @@ __global__ void __launch_bounds__(kThreads) k_products_fwd(const __grid_constant
       s.xb0[i] = z;
     }
     __syncthreads();
-    cpx* zr = forward_plane<GEN>(g, s, pxF, pzF);
+    cpx* zr = forward_plane<GEN>(g, s, pxF, pzF, g.norm);
     for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x) {
       const int zp = i / g.X, x = i - zp * g.X;
       const int z = zrow_to_kz(g, zp);
@@ -235,13 +238,15 @@ __global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant
   const size_t plane = (size_t)g.pz * g.px, fs = (size_t)g.Q * plane;
   const double* __restrict__ P = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane +
                                  (a.pslot.stride ? (long long)a.pslot.slot() * a.pslot.stride : 0LL);
-  const double* __restrict__ L = a.Pt.at(inst) + (size_t)y * plane;  // lambda: 3 fields
+  const double* __restrict__ L = a.Pt.at(inst) + (size_t)y * plane;  // lambda (exact: N_bar): 3 fields
   cpx* __restrict__ H = a.H.at(inst);
   const FftPlan pxF = make_plan(g.px, false);
   const FftPlan pzF = make_plan(g.pz, false);
   const int npair = (g.pz + 1) / 2;
+  const bool exact = a.exact != 0;
   __syncthreads();
   // q = 0..2: S_x, S_y, S_z = u x lambda; q = 3..5: T_x, T_y, T_z = lambda x w
+  // (exact: the cotangents of u, v, w, wz, wx, wy)
   for (int q = 0; q < 6; ++q) {
     for (int i = threadIdx.x; i < npair * g.px; i += blockDim.x) {
       const int p = i / g.px, xp = i - p * g.px;
@@ -249,6 +254,10 @@ __global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant
       for (int h = 0; h < 2; ++h) {
         if (2 * p + h >= g.pz) break;
         const size_t o = (size_t)(2 * p + h) * g.px + xp;
+        if (exact) {
+          val[h] = prod_transpose(P, L, fs, o, q);
+          continue;
+        }
         const double u = P[o], v = P[fs + o], w = P[2 * fs + o];
         const double wz = P[3 * fs + o], wx = P[4 * fs + o], wy = P[5 * fs + o];
         const double lx = L[o], ly = L[fs + o], lz = L[2 * fs + o];
@@ -266,7 +275,7 @@ __global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant
       s.xb0[i] = cpx{val[0], val[1]};
     }
     __syncthreads();
-    cpx* zr = forward_plane<GEN>(g, s, pxF, pzF);
+    cpx* zr = forward_plane<GEN>(g, s, pxF, pzF, exact ? 1.0 : g.norm);
     for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x) {
       const int zp = i / g.X, x = i - zp * g.X;
       const int z = zrow_to_kz(g, zp);
@@ -278,6 +287,12 @@ __global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant
   for (int i = threadIdx.x; i < g.Nz * g.X; i += blockDim.x) {
     const int z = i / g.X, x = i - z * g.X;
     if (z == g.Nz / 2) continue;
+    if (exact) {
+      exact_assemble(g, H, z, y, x, keep[(0 * g.Nz + z) * g.X + x], keep[(1 * g.Nz + z) * g.X + x],
+                     keep[(2 * g.Nz + z) * g.X + x], keep[(3 * g.Nz + z) * g.X + x],
+                     keep[(4 * g.Nz + z) * g.X + x], keep[(5 * g.Nz + z) * g.X + x]);
+      continue;
+    }
     const double kx = g.Kx[x], kz = g.Kz[z];
     const cpx Sx = keep[(0 * g.Nz + z) * g.X + x], Sy = keep[(1 * g.Nz + z) * g.X + x];
     const cpx Sz = keep[(2 * g.Nz + z) * g.X + x], Tx = keep[(3 * g.Nz + z) * g.X + x];
@@ -379,13 +394,14 @@ cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t s
 
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
-  if (g.split) return kSplit[split_index(g)].products(g, a, 2, st);
+  if (g.split) return kSplit[split_index(g)].products(g, a, a.exact ? 3 : 2, st);
   const size_t sm = prod_adj_smem_bytes(g);
   CHN_LAUNCH_FUSED(k_products_adj, dim3(g.Q, a.ninst), sm, st, g, a);
   return cudaGetLastError();
 }
 
 void prepare_recon_solve(int optin);
+void prepare_solve_T(int optin);
 
 // Every kernel may use up to the device's opt-in shared memory per block: the
 // single-grid engine and an uneven batch (sized for its largest grid) share
@@ -408,6 +424,7 @@ void prepare_kernels(const Grid& g) {
   prepare_transforms<true, true>(optin);
   for (const SplitEntry& e : kSplit) e.prepare(optin);
   prepare_recon_solve(optin);
+  prepare_solve_T(optin);
 }
 
 }  // namespace chn

@@ -59,12 +59,31 @@ __device__ __forceinline__ double prod_tangent(const double* __restrict__ P, con
   return iw * wx - iu * wz + w * iwx - u * iwz;
 }
 
+// the transpose of the tangent products (channel/pass1.c:145-170) with
+// respect to the tangent fields: n = (nz, nx, ny) the cotangents of the
+// products Hz, Hx, Hy (fields 0..2 of N); q = 0..5 the cotangents of
+// u, v, w, wz, wx, wy
+__device__ __forceinline__ double prod_transpose(const double* __restrict__ P, const double* __restrict__ N,
+                                                 size_t fs, size_t o, int q) {
+  const double nz = N[o], nx = N[fs + o], ny = N[2 * fs + o];
+  switch (q) {
+    case 0: return nz * P[5 * fs + o] - ny * P[3 * fs + o];   // u:  nz wy - ny wz
+    case 1: return nx * P[3 * fs + o] - nz * P[4 * fs + o];   // v:  nx wz - nz wx
+    case 2: return ny * P[4 * fs + o] - nx * P[5 * fs + o];   // w:  ny wx - nx wy
+    case 3: return nx * P[fs + o] - ny * P[o];                // wz: nx v - ny u
+    case 4: return ny * P[2 * fs + o] - nz * P[fs + o];       // wx: ny w - nz v
+    default: return nz * P[o] - nx * P[2 * fs + o];           // wy: nz u - nx w
+  }
+}
+
 // product component q at flat offset o of plane y: mode 0 primal, 1 tangent,
-// 2 adjoint (q = 0..2 S = u x lambda, 3..5 T = lambda x w)
+// 2 adjoint (q = 0..2 S = u x lambda, 3..5 T = lambda x w), 3 the exact
+// transpose of the tangent products
 __device__ __forceinline__ double split_product(int mode, const double* __restrict__ P,
                                                 const double* __restrict__ I, size_t fs, size_t o, int q) {
   if (mode == 0) return prod_primal(P, fs, o, q);
   if (mode == 1) return prod_tangent(P, I, fs, o, q);
+  if (mode == 3) return prod_transpose(P, I, fs, o, q);
   const double u = P[o], v = P[fs + o], w = P[2 * fs + o];
   const double wz = P[3 * fs + o], wx = P[4 * fs + o], wy = P[5 * fs + o];
   const double lx = I[o], ly = I[fs + o], lz = I[2 * fs + o];
@@ -96,6 +115,23 @@ __device__ __forceinline__ void adjoint_assemble(const Grid& g, cpx* __restrict_
   slot(2) = hy;
   slot(3) = Sx;
   slot(4) = Sz;
+}
+
+// the transpose of the vorticity load (channel/pass1.c:58-104) applied to
+// the forward-transformed field cotangents t0..t5 (u, v, w, wz, wx, wy),
+// with the factor 2 of the transposed complex-to-real x transform off the
+// kx = 0 column:
+//   u = t0 - i kz t5,  v = t1 - i kx t3 + i kz t4,  w = t2 + i kx t5,
+//   du/dy = -t3,  dw/dy = t4
+__device__ __forceinline__ void exact_assemble(const Grid& g, cpx* __restrict__ U, int z, int y, int x, cpx t0,
+                                               cpx t1, cpx t2, cpx t3, cpx t4, cpx t5) {
+  const double kx = g.Kx[x], kz = g.Kz[z], f = x == 0 ? 1.0 : 2.0;
+  auto slot = [&](int c) -> cpx& { return U[(((size_t)z * 5 + c) * g.Q + y) * g.X + x]; };
+  slot(0) = cpx{f * (t0.re + kz * t5.im), f * (t0.im - kz * t5.re)};
+  slot(1) = cpx{f * (t1.re + kx * t3.im - kz * t4.im), f * (t1.im - kx * t3.re + kz * t4.re)};
+  slot(2) = cpx{f * (t2.re - kx * t5.im), f * (t2.im + kx * t5.re)};
+  slot(3) = cpx{-f * t3.re, -f * t3.im};
+  slot(4) = cpx{f * t4.re, f * t4.im};
 }
 
 }  // namespace chn

@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(NT) k_tx_fwd(const __grid_constant__ Grid g0, 
   const int y = blockIdx.x, il = blockIdx.y, inst = inst0 + il;
   const int r0 = blockIdx.z * CH;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
-  const int ncomp = mode == 2 ? 6 : 3;
+  const int ncomp = mode >= 2 ? 6 : 3;
   const int npair = (g.pz + 1) / 2, nrow = npair * ncomp;
   if (y >= g.Q || r0 >= nrow) return;
   const int nr = min(CH, nrow - r0);
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(NT) k_tx_fwd(const __grid_constant__ Grid g0, 
   __syncthreads();
   const FftPlan plan = make_plan(g.px, false);
   const cpx* xr = fft_run<false>(plan, b0, b1, nr, 1, g.px, tw, -1, true);
-  const double hn = 0.5 * g.norm;
+  const double hn = mode == 3 ? 0.5 : 0.5 * g.norm;  // the transpose carries no 1/(px pz)
   for (int i = threadIdx.x; i < nr * g.X; i += NT) {
     const int rl = i / g.X, k = i - rl * g.X;
     const int gr = r0 + rl, p = gr / ncomp, q = gr - p * ncomp, ra = 2 * p;
@@ -208,14 +208,15 @@ __global__ void __launch_bounds__(NT) k_tx_fwd(const __grid_constant__ Grid g0, 
 }
 
 // forward z pass: columns of T, z transform, truncation -> H; the adjoint
-// assembles H from its 6 spectra per column (CH is a multiple of 6)
+// (and the exact transpose, mode 3) assembles H from its 6 spectra per
+// column (CH is a multiple of 6)
 template <bool MULTI, int NT, int CH>
 __global__ void __launch_bounds__(NT) k_tz_fwd(const __grid_constant__ Grid g0, ProdArgs a, int mode, int inst0,
                                                const cpx* T) {
   const int y = blockIdx.x, il = blockIdx.y, inst = inst0 + il;
   const int c0 = blockIdx.z * CH;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
-  const int ncomp = mode == 2 ? 6 : 3;
+  const int ncomp = mode >= 2 ? 6 : 3;
   const int ncol = ncomp * g.X;
   if (y >= g.Q || c0 >= ncol) return;
   const int nc = min(CH, ncol - c0);
@@ -240,18 +241,21 @@ __global__ void __launch_bounds__(NT) k_tz_fwd(const __grid_constant__ Grid g0, 
     const int z = zrow_to_kz(g, zp);
     if (z < 0) continue;
     const int gc = c0 + cl, x = gc / ncomp, q = gc - x * ncomp;
-    if (mode == 2) keep[(size_t)cl * g.Nz + z] = zr[i];
+    if (mode >= 2) keep[(size_t)cl * g.Nz + z] = zr[i];
     else H[(((size_t)z * 5 + q) * g.Q + y) * g.X + x] = zr[i];
   }
-  if (mode != 2) return;
+  if (mode < 2) return;
   __syncthreads();
   const int nx = nc / 6;
   for (int i = threadIdx.x; i < g.Nz * nx; i += NT) {
     const int xl = i / g.Nz, z = i - xl * g.Nz;
     if (z == g.Nz / 2) continue;
     const cpx* K = keep + (size_t)xl * 6 * g.Nz + z;
-    adjoint_assemble(g, H, z, y, c0 / 6 + xl, K[0], K[g.Nz], K[2 * g.Nz], K[3 * g.Nz], K[4 * g.Nz],
-                     K[5 * g.Nz]);
+    if (mode == 3)
+      exact_assemble(g, H, z, y, c0 / 6 + xl, K[0], K[g.Nz], K[2 * g.Nz], K[3 * g.Nz], K[4 * g.Nz], K[5 * g.Nz]);
+    else
+      adjoint_assemble(g, H, z, y, c0 / 6 + xl, K[0], K[g.Nz], K[2 * g.Nz], K[3 * g.Nz], K[4 * g.Nz],
+                       K[5 * g.Nz]);
   }
 }
 
@@ -289,12 +293,12 @@ cudaError_t split_inverse_t(const Grid& g, const PhysArgs& a, cudaStream_t st) {
 template <int NT, int CH>
 cudaError_t split_products_t(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
   if (!a.tmp) return cudaErrorInvalidValue;
-  const int ncomp = mode == 2 ? 6 : 3;
+  const int ncomp = mode >= 2 ? 6 : 3;
   const int cap = a.tmp_inst * 6 / ncomp;
   return split_chunks(a.ninst, cap, [&](int i0, int n) {
     const int npair = (g.pz + 1) / 2;
     const dim3 gx(g.Q, n, (npair * ncomp + CH - 1) / CH), gz(g.Q, n, (ncomp * g.X + CH - 1) / CH);
-    const size_t sx = tx_smem<CH>(g), sz = tz_smem<CH>(g, mode == 2);
+    const size_t sx = tx_smem<CH>(g), sz = tz_smem<CH>(g, mode >= 2);
     if (a.grids) {
       k_tx_fwd<true, NT, CH><<<gx, NT, sx, st>>>(g, a, mode, i0, a.tmp);
       k_tz_fwd<true, NT, CH><<<gz, NT, sz, st>>>(g, a, mode, i0, a.tmp);

@@ -4,9 +4,11 @@ transforms as separate z and x passes (csrc/phys.cu, split transforms).
 - The split passes are the fused kernels' 1D transforms on the same data, so
   forcing them (CHN_SPLIT_TRANSFORMS=1, each block-size / chunk variant the
   autotuner chooses from) at 32x65x32 must reproduce the fused results bit
-  for bit through primal, tangents and the coupled adjoint.
+  for bit through primal, tangents, the coupled adjoint and the exact
+  adjoint.
 - 48x97x48 (the adjoint products no longer fit) and 128x129x128 (nothing
-  fits) against the oracle, one step each way.
+  fits) against the oracle, one step each way, and the exact adjoint's
+  dot-product identity.
 """
 import json
 import os
@@ -58,10 +60,12 @@ AC = np.stack([synthetic_state(32, 65, 32, seed=20 + s, laminar=False) for s in 
 inh = (ctypes.c_int * 2)(0, 1)
 assert lib.c_batch_forward(0, 3, C.ctypes.data, IC.ctypes.data, inh) == 0, cc.c_last_error_message()
 assert lib.c_batch_adjoint(3, 0, AC.ctypes.data, 1.0) == 0, cc.c_last_error_message()
+AE = np.stack([synthetic_state(32, 65, 32, seed=30 + s, laminar=False) for s in range(2)])
+assert lib.c_batch_adjoint_exact(3, 0, AE.ctypes.data) == 0, cc.c_last_error_message()
 flow = np.zeros((3, 48, 97, 48))
 cc.c_spec2phys(np.ascontiguousarray(C[0]), flow)
 print(json.dumps({k: v.view(np.float64).ravel().tolist() for k, v in
-                  (("C", C), ("IC", IC), ("AC", AC), ("flow", flow))}))
+                  (("C", C), ("IC", IC), ("AC", AC), ("AE", AE), ("flow", flow))}))
 """
     root = O.HERE.parent
     outs = []
@@ -71,7 +75,7 @@ print(json.dumps({k: v.view(np.float64).ravel().tolist() for k, v in
                            timeout=600)
         assert r.returncode == 0, r.stderr[-2000:]
         outs.append(json.loads(next(ln for ln in r.stdout.splitlines() if ln.startswith("{"))))
-    for key in ("C", "IC", "AC", "flow"):
+    for key in ("C", "IC", "AC", "AE", "flow"):
         assert np.array_equal(np.array(outs[0][key]), np.array(outs[1][key])), key
 
 
@@ -105,3 +109,15 @@ def test_large_grid_one_step_each_way(gpu, grid):
     assert rel(res["gpu"][0], res["ref"][0]) <= tp
     assert rel(res["gpu"][1], res["ref"][1]) <= tt
     assert rel(res["gpu"][2], res["ref"][2]) <= ta
+    # the exact adjoint: the dot-product identity with the homogeneous
+    # tangent on the GPU, and the oracle's transpose within the tangent floor
+    v, lam = IC0.copy(), AC0.copy()
+    cc.c_tangent(0, 1, v, 0)
+    cc.c_adjoint_exact(1, 0, lam)
+    assert cc.c_last_error() == 0, cc.c_last_error_message()
+    d = lambda a, b: float(np.sum(a.real * b.real + a.imag * b.imag))
+    lhs, rhs = d(AC0, v), d(lam, IC0)
+    assert abs(lhs - rhs) <= 1e-11 * np.linalg.norm(AC0) * np.linalg.norm(v), (lhs, rhs)
+    ref = AC0.copy()
+    assert port.adjoint_exact(1, 0, ref) == 0
+    assert rel(lam, ref) <= tt
