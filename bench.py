@@ -295,6 +295,9 @@ def run_gb300(a):
                          "achieved_tflops": step_flop * value / world / 1e12,
                          "frac": step_flop * value / world / 1e12 / peak}}
 
+    exact = None
+    if not a.no_extras and rank == 0:
+        exact = exact_adjoint_timing(cc, torch, stream, dAC, K)
     cc.lib.c_batch_destroy()
     cc.c_destroy()
     plain = None
@@ -309,6 +312,8 @@ def run_gb300(a):
     if plain:
         line["plain_gpu"] = plain
         line["plain_gpu"]["batched_over_plain"] = (value / world) / plain["value"]
+    if exact:
+        line["exact_adjoint"] = exact
     if not a.no_extras and rank == 0:
         line["uneven_batch"] = uneven_batch(cc)
         line["large_grid"] = large_grid(cc)
@@ -318,6 +323,30 @@ def run_gb300(a):
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def exact_adjoint_timing(cc, torch, stream, dAC, K):
+    """The exact discrete adjoint (c_batch_adjoint_exact_dev, the transpose of
+    the homogeneous tangent) over the stored K-step trajectories of the batch,
+    timed with CUDA events on the library stream beside the reference's
+    adjoint (c_batch_adjoint_dev, strength 1) on the same batch."""
+    out = {}
+    lam = dAC.clone()
+    for name, call in (("reference_adjoint", lambda: cc.lib.c_batch_adjoint_dev(K, 0, lam.data_ptr(), 1.0)),
+                       ("exact_adjoint", lambda: cc.lib.c_batch_adjoint_exact_dev(K, 0, lam.data_ptr()))):
+        assert call() == 0, cc.c_last_error_message()  # warm-up (graph instantiation)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            assert call() == 0, cc.c_last_error_message()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 3
+        out[name] = {"segment_steps_per_s": NSEG * K / (ms * 1e-3), "ms_per_sweep": ms}
+    out["note"] = (f"{NSEG} segments x {K} steps of stored trajectory; the exact adjoint needs one transposed "
+                   "product pass per substage where the reference's needs two")
+    return out
 
 
 def ctypes_int_array(vals):

@@ -68,6 +68,15 @@ void c_adjoint(int start_step, int end_step, chn_complex *AC_given,
    adjoint equations with reversed RK coefficients.  No ddt coupling. */
 void c_adjoint_exact(int start_step, int end_step, chn_complex *AC_given,
                      int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup);
+/* c_adjoint_exact with a source added after every step:
+     lambda_n = T_n^T lambda_{n+1} + src,  n = start_step - 1 .. end_step,
+   lambda_{start_step} = AC_given, the result lambda_{end_step} in AC_given:
+   the gradient with respect to the state at end_step of a sum over steps
+   end_step .. start_step - 1 of <src, C_n> (src the gradient of a linear
+   per-step functional, e.g. the wall shear).  No reference counterpart. */
+void c_adjoint_exact_source(int start_step, int end_step,
+                            chn_complex *AC_given, const chn_complex *src,
+                            int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup);
 
 /* channel.i:96-105 -> channel.c:704 ddt_project() */
 double c_ddt_project(int i_step, chn_complex *IC_given, int Nz_dup,
@@ -164,6 +173,8 @@ int c_batch_forward_dev(int start_step, int end_step, chn_complex *C,
 int c_batch_adjoint_dev(int start_step, int end_step, chn_complex *AC,
                         double strength);
 int c_batch_adjoint_exact_dev(int start_step, int end_step, chn_complex *AC);
+int c_batch_adjoint_exact_source_dev(int start_step, int end_step,
+                                     chn_complex *AC, const chn_complex *src);
 int c_batch_primal_dev(int ru_steps, chn_complex *C);
 int c_batch_tangent_dev(int start_step, int end_step, chn_complex *IC,
                         const int *inhomo);
@@ -240,6 +251,10 @@ int c_multi_getsoln(int i, int i_step, chn_complex *out);
      each quadrature point, out [end-start][qpts].
    Batch variants: the same for every segment, out [nseg][end-start][...]. */
 int c_mean_profile(int inc, int comp, int start_step, int end_step, double *out);
+/* the weights Rp0 = R'(-1) of the wall shear, out[dimR]: c_wall_shear's
+   dU/dy = sum_r Rp0[r] Re(C[0][0][r][0]) (dW/dy likewise on beta), i.e. the
+   gradient of the wall shear with respect to the mean-mode coefficients */
+int c_wall_shear_weights(double *out);
 int c_wall_shear(int inc, int start_step, int end_step, double *out);
 int c_mean_product(int inc_a, int comp_a, int inc_b, int comp_b, int start_step,
                    int end_step, double *out);

@@ -7,12 +7,17 @@ returns the time-mean wall shear
     J = (1/N) sum_{n=0}^{N-1} dU/dy(y = -1) at step n
 
 (the reference's Uxb of the mean flow, channel/project0.c:224-234), and
-whose backward returns dJ/dRe and dJ/dmeanU.  The derivatives are exact
-derivatives of the discrete RK3 scheme: tangent sweeps with the Re forcing
-(c_tangent_forcing kind 3) and the mean-flux forcing (kind 1, the
-reference's inhomogeneous tangent), whose wall shear is read from the
-stored tangent trajectory.  For a scalar parameter the tangent sweep costs
-what one adjoint sweep costs and carries no transposition error.
+whose backward returns dJ/dRe, dJ/dmeanU and, when the initial state is
+passed as a tensor, dJ/dC0.  The derivatives are exact derivatives of the
+discrete RK3 scheme: tangent sweeps with the Re forcing (c_tangent_forcing
+kind 3) and the mean-flux forcing (kind 1, the reference's inhomogeneous
+tangent), whose wall shear is read from the stored tangent trajectory; and
+for the state, one reverse sweep of the exact discrete adjoint
+(c_adjoint_exact_source, the transpose of the homogeneous tangent) with the
+wall-shear weights as its per-step source:
+    dJ/dC0 = (1/N) sum_n T(0 -> n)^T g,   g = Rp0 on Re C[0, 0, :, 0].
+For a scalar parameter the tangent sweep costs what one adjoint sweep costs;
+for the state (every coefficient at once) only the adjoint sweep is cheap.
 
 Memory: the primal is checkpointed every ``checkpoint`` steps (one
 coefficient array per checkpoint, host memory); the backward recomputes the
@@ -59,6 +64,27 @@ def primal_objective(grid, Re, meanU, C0, nsteps, checkpoint):
     return J / nsteps, ckpts, chunks
 
 
+def state_gradient(grid, Re, meanU, ckpts, chunks, nsteps):
+    """dJ/dC0 (complex, the gradient with respect to the real and imaginary
+    parts) by the exact discrete adjoint, one checkpoint interval at a time
+    from the last: each interval's primal is recomputed from its checkpoint
+    and its transposed tangent carries lambda back with the source
+    g / nsteps added at every step."""
+    shape = ckpts[0].shape
+    lam = np.zeros(shape, np.complex128)
+    src = None
+    for C, k in zip(reversed(ckpts), reversed(chunks)):
+        _init(grid, Re, meanU, k)
+        c_channel.c_primal(0, C.copy())
+        if src is None:
+            src = np.zeros(shape, np.complex128)
+            src[0, 0, :, 0] = c_channel.c_wall_shear_weights() / nsteps
+        c_channel.c_adjoint_exact_source(k, 0, lam, src)
+        if c_channel.c_last_error() != 0:
+            raise RuntimeError("adjoint sweep failed: " + c_channel.c_last_error_message())
+    return lam
+
+
 def tangent_gradients(grid, Re, meanU, ckpts, chunks, nsteps, kinds=(3, 1)):
     """dJ/dparameter for each tangent forcing kind (3: Re, 1: meanU),
     recomputing each checkpoint interval's primal from its checkpoint."""
@@ -75,21 +101,27 @@ def tangent_gradients(grid, Re, meanU, ckpts, chunks, nsteps, kinds=(3, 1)):
 
 
 class TimeMeanWallShear(torch.autograd.Function):
-    """J(Re, meanU) = time-mean lower-wall shear of the primal from C0.
+    """J(Re, meanU, C0) = time-mean lower-wall shear of the primal from C0.
 
-    Usage: ``J = TimeMeanWallShear.apply(Re, meanU, cfg)`` with Re, meanU
-    0-d float64 tensors and cfg a dict: grid (Nx, Ny, Nz, Lx, Lz, dt), C0
-    (complex [Nz, 2, Ny-2, Nx/2]), nsteps, checkpoint.
+    Usage: ``J = TimeMeanWallShear.apply(Re, meanU, cfg[, C0])`` with Re,
+    meanU 0-d float64 tensors and cfg a dict: grid (Nx, Ny, Nz, Lx, Lz, dt),
+    C0 (complex [Nz, 2, Ny-2, Nx/2]), nsteps, checkpoint.  The optional
+    tensor C0 (float64 [Nz, 2, Ny-2, Nx/2, 2], the real view of the complex
+    state, e.g. ``torch.view_as_real``) replaces cfg["C0"] and receives
+    dJ/dC0 when it requires grad.
     """
 
     @staticmethod
-    def forward(ctx, Re, meanU, cfg):
+    def forward(ctx, Re, meanU, cfg, C0=None):
         t0 = time.perf_counter()
-        J, ckpts, chunks = primal_objective(cfg["grid"], float(Re), float(meanU), cfg["C0"], int(cfg["nsteps"]),
+        c0 = cfg["C0"] if C0 is None else \
+            np.ascontiguousarray(C0.detach().cpu().numpy()).view(np.complex128)[..., 0]
+        J, ckpts, chunks = primal_objective(cfg["grid"], float(Re), float(meanU), c0, int(cfg["nsteps"]),
                                             int(cfg["checkpoint"]))
         ctx.cfg = cfg
         ctx.params = (float(Re), float(meanU))
         ctx.ckpts, ctx.chunks = ckpts, chunks
+        ctx.c0_meta = None if C0 is None else (C0.shape, C0.dtype, C0.device)
         ctx.report = {"forward_s": time.perf_counter() - t0}
         cfg.setdefault("report", {}).update(ctx.report)
         return torch.tensor(J, dtype=torch.float64)
@@ -98,12 +130,24 @@ class TimeMeanWallShear(torch.autograd.Function):
     def backward(ctx, gJ):
         t0 = time.perf_counter()
         Re, meanU = ctx.params
-        d = tangent_gradients(ctx.cfg["grid"], Re, meanU, ctx.ckpts, ctx.chunks, int(ctx.cfg["nsteps"]))
-        ctx.cfg["report"]["backward_s"] = time.perf_counter() - t0
         g = float(gJ)
-        return (torch.tensor(g * d[3], dtype=torch.float64), torch.tensor(g * d[1], dtype=torch.float64), None)
+        nsteps = int(ctx.cfg["nsteps"])
+        gRe = gU = gC = None
+        if ctx.needs_input_grad[0] or ctx.needs_input_grad[1]:
+            d = tangent_gradients(ctx.cfg["grid"], Re, meanU, ctx.ckpts, ctx.chunks, nsteps)
+            gRe = torch.tensor(g * d[3], dtype=torch.float64)
+            gU = torch.tensor(g * d[1], dtype=torch.float64)
+        if ctx.c0_meta is not None and len(ctx.needs_input_grad) > 3 and ctx.needs_input_grad[3]:
+            lam = state_gradient(ctx.cfg["grid"], Re, meanU, ctx.ckpts, ctx.chunks, nsteps)
+            shape, dtype, device = ctx.c0_meta
+            gC = torch.from_numpy(np.ascontiguousarray(lam).view(np.float64).reshape(shape) * g).to(
+                device=device, dtype=dtype)
+        ctx.cfg["report"]["backward_s"] = time.perf_counter() - t0
+        return gRe, gU, None, gC
 
 
-def time_mean_wall_shear(Re, meanU, cfg):
+def time_mean_wall_shear(Re, meanU, cfg, C0=None):
     """Functional form of TimeMeanWallShear.apply."""
-    return TimeMeanWallShear.apply(Re, meanU, cfg)
+    if C0 is None:
+        return TimeMeanWallShear.apply(Re, meanU, cfg)
+    return TimeMeanWallShear.apply(Re, meanU, cfg, C0)

@@ -51,6 +51,8 @@ _lib.c_adjoint.argtypes = [_i, _i, _vp, _i, _i, _i, _i, _i, _d]
 _lib.c_adjoint.restype = None
 _lib.c_adjoint_exact.argtypes = [_i, _i, _vp, _i, _i, _i, _i]
 _lib.c_adjoint_exact.restype = None
+_lib.c_adjoint_exact_source.argtypes = [_i, _i, _vp, _vp, _i, _i, _i, _i]
+_lib.c_adjoint_exact_source.restype = None
 _lib.c_ddt_project.argtypes = [_i, _vp, _i, _i, _i, _i]
 _lib.c_ddt_project.restype = _d
 _lib.c_getsoln.argtypes = [_i, _pp, _ip, _ip, _ip, _ip]
@@ -109,6 +111,8 @@ _lib.c_batch_adjoint_dev.argtypes = [_i, _i, _vp, _d]
 _lib.c_batch_adjoint_dev.restype = _i
 _lib.c_batch_adjoint_exact_dev.argtypes = [_i, _i, _vp]
 _lib.c_batch_adjoint_exact_dev.restype = _i
+_lib.c_batch_adjoint_exact_source_dev.argtypes = [_i, _i, _vp, _vp]
+_lib.c_batch_adjoint_exact_source_dev.restype = _i
 
 _lib.c_stream.argtypes = []
 _lib.c_stream.restype = _vp
@@ -140,6 +144,8 @@ _lib.c_tangent_forcing.argtypes = [_i, _i, _vp, _i, _i, _i, _i, _i]
 _lib.c_tangent_forcing.restype = None
 _lib.c_mean_profile.argtypes = [_i, _i, _i, _i, _vp]
 _lib.c_mean_profile.restype = _i
+_lib.c_wall_shear_weights.argtypes = [_vp]
+_lib.c_wall_shear_weights.restype = _i
 _lib.c_wall_shear.argtypes = [_i, _i, _i, _vp]
 _lib.c_wall_shear.restype = _i
 _lib.c_mean_product.argtypes = [_i, _i, _i, _i, _i, _i, _vp]
@@ -219,6 +225,16 @@ def c_adjoint_exact(start_step, end_step, AC_given):
     _lib.c_adjoint_exact(int(start_step), int(end_step), p, *s)
 
 
+def c_adjoint_exact_source(start_step, end_step, AC_given, src):
+    """c_adjoint_exact with src added after every step (lambda_n = T_n^T
+    lambda_{n+1} + src): the gradient of a per-step sum of <src, C_n>."""
+    p, s = _inplace4(AC_given, np.complex128, "c_adjoint_exact_source")
+    q, t = _inplace4(src, np.complex128, "src")
+    if t != s:
+        raise ValueError("src must have the shape of AC_given")
+    _lib.c_adjoint_exact_source(int(start_step), int(end_step), p, q, *s)
+
+
 def c_ddt_project(i_step, IC_given):
     p, s = _inplace4(IC_given, np.complex128, "c_ddt_project")
     return _lib.c_ddt_project(int(i_step), p, *s)
@@ -270,6 +286,13 @@ def c_wall_shear(inc, start_step, end_step):
     """dU/dy, dW/dy of the mean flow at y = -1 per step: float64 [end-start, 2]."""
     out = np.zeros((end_step - start_step, 2))
     _check(_lib.c_wall_shear(int(inc), int(start_step), int(end_step), out.ctypes.data))
+    return out
+
+
+def c_wall_shear_weights():
+    """Rp0 = R'(-1), float64 [dimR]: dU/dy at y = -1 is Rp0 . Re(C[0, 0, :, 0])."""
+    out = np.zeros(c_dimR())
+    _check(_lib.c_wall_shear_weights(out.ctypes.data))
     return out
 
 

@@ -517,6 +517,33 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
   }
 }
 
+// Ca[i] += src[i] over each instance's coefficient array (the per-step
+// source of a time-summed objective)
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads) k_add_source(const __grid_constant__ Grid g0, Batch<const cpx> src,
+                                                         Batch<cpx> ca, const Grid* grids) {
+  const int inst = blockIdx.y;
+  CHN_INSTANCE_GRID(g0, grids, inst);
+  const size_t n = coef_size(g);
+  const cpx* __restrict__ s = src.at(inst);
+  cpx* __restrict__ c = ca.at(inst);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    c[i].re += s[i].re;
+    c[i].im += s[i].im;
+  }
+}
+
+cudaError_t launch_add_source(const Grid& g, Batch<const cpx> src, Batch<cpx> ca, int ninst, cudaStream_t st,
+                              const Grid* grids) {
+  if (ninst <= 0) return cudaSuccess;
+  const size_t n = coef_size(g);
+  int blocks = (int)((n + kThreads - 1) / kThreads);
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  if (grids) k_add_source<true><<<dim3(blocks, ninst), kThreads, 0, st>>>(g, src, ca, grids);
+  else k_add_source<false><<<dim3(blocks, ninst), kThreads, 0, st>>>(g, src, ca, grids);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_solve_T(const Grid& g, const SolveTArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
   const int ntx = (g.X + kTile - 1) / kTile;

@@ -692,7 +692,8 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
 // cotangent, w.Uprev H_bar, w.Pl its physical fields; the primal fields of
 // the state before substage k, slot 3n + k of `traj` (segment stride
 // `tstride`), come from the field cache or are rebuilt into w.Pp.
-static bool enqueue_adjoint_exact_step(Engine& e, Work& w, bool cached, const cpx* traj, long long tstride) {
+static bool enqueue_adjoint_exact_step(Engine& e, Work& w, bool cached, const cpx* traj, long long tstride,
+                                       const cpx* src) {
   const Grid& g = e.T.g;
   cudaStream_t st = e.st;
   for (int k = 2; k >= 0; --k) {
@@ -762,6 +763,8 @@ static bool enqueue_adjoint_exact_step(Engine& e, Work& w, bool cached, const cp
     a.exact = 1;
     LK(launch_products_adj(g, a, st));
   }
+  // the source of the state this step started from: lambda_n += src
+  if (src) LK(launch_add_source(g, cb(src, w.csz), mb(w.Ca, w.csz), w.nseg, st, w.gdev));
   LK(launch_step_advance(w.step, -1, st));
   return true;
 }
@@ -1109,8 +1112,11 @@ static bool op_adjoint(Engine& e, Work& w, int start, int end, const cpx* AC, do
 // re-advanced from MC[3 end] rebuilt into velocity (channel/channel.c:496-514),
 // which is the stored trajectory except after a laminar start without
 // run-up with end == 0: then the primal is re-advanced here into a
-// temporary trajectory, as op_forward does.
-static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* AC) {
+// temporary trajectory, as op_forward does.  With `src` (device, nseg
+// arrays) every step adds it after its transposition:
+//   lambda_n = T_n^T lambda_{n+1} + src,  n = start - 1 .. end,
+// the cotangent of a sum over steps end .. start - 1 of a linear functional.
+static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* AC, const cpx* src = nullptr) {
   const size_t csz = w.csz;
   const bool readvance = w.raw_start && end == 0;
   cpx* scratch = nullptr;
@@ -1157,7 +1163,7 @@ static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* 
     ok = false;
   }
   ok = ok && set_step(e, w, start);
-  ok = ok && run_steps(e, start - end, [&] { return enqueue_adjoint_exact_step(e, w, cached, traj, w.traj); });
+  ok = ok && run_steps(e, start - end, [&] { return enqueue_adjoint_exact_step(e, w, cached, traj, w.traj, src); });
   if (ok) {
     // the tangent starts from IU = Recon(IC)
     SolveTArgs t{};
@@ -1424,6 +1430,23 @@ void c_adjoint_exact(int start_step, int end_step, chn_complex* AC_given, int Nz
   d2h(e, AC_given, w.Ca, bytes);
 }
 
+void c_adjoint_exact_source(int start_step, int end_step, chn_complex* AC_given, const chn_complex* src,
+                            int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup) {
+  if (!need_init("c_adjoint_exact_source")) return;
+  Engine& e = *E;
+  Work& w = e.single;
+  check_coef_dims(e.T.g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
+  shape_assert(end_step < start_step, "end_step < start_step");
+  shape_assert(end_step >= 0, "end_step >= 0");
+  shape_assert(start_step <= e.nsteps, "start_step <= nsteps");
+  shape_assert(AC_given != nullptr && src != nullptr, "AC_given != 0 && src != 0");
+  const size_t bytes = sizeof(cpx) * w.csz;
+  if (!h2d(e, w.io, AC_given, bytes) || !h2d(e, w.icp, src, bytes)) return;
+  if (!op_adjoint_exact(e, w, start_step, end_step, w.io, w.icp)) return;
+  if (!collect_status(e, w)) return;
+  d2h(e, AC_given, w.Ca, bytes);
+}
+
 double c_ddt_project(int i_step, chn_complex* IC_given, int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup) {
   if (!need_init("c_ddt_project")) return NAN;
   check_coef_dims(E->T.g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
@@ -1672,17 +1695,23 @@ int c_batch_adjoint_dev(int start_step, int end_step, chn_complex* AC, double st
   return collect_status(*E, w) ? g_status : -1;
 }
 
-int c_batch_adjoint_exact_dev(int start_step, int end_step, chn_complex* AC) {
+int c_batch_adjoint_exact_source_dev(int start_step, int end_step, chn_complex* AC, const chn_complex* src) {
   if (!batch_ready("c_batch_adjoint_exact_dev")) return g_status;
   Work& w = E->batch;
   if (!(end_step < start_step && end_step >= 0 && start_step <= E->batch.nsteps) || !AC) {
     set_error(-4, "c_batch_adjoint_exact: need 0 <= end < start <= nsteps and the state array");
     return -4;
   }
-  if (!op_adjoint_exact(*E, w, start_step, end_step, reinterpret_cast<cpx*>(AC))) return g_status;
+  if (!op_adjoint_exact(*E, w, start_step, end_step, reinterpret_cast<cpx*>(AC),
+                        reinterpret_cast<const cpx*>(src)))
+    return g_status;
   if (cudaMemcpyAsync(AC, w.Ca, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, E->st) != cudaSuccess)
     return -1;
   return collect_status(*E, w) ? g_status : -1;
+}
+
+int c_batch_adjoint_exact_dev(int start_step, int end_step, chn_complex* AC) {
+  return c_batch_adjoint_exact_source_dev(start_step, end_step, AC, nullptr);
 }
 
 // host-array variants: staged through the working set's own device buffers

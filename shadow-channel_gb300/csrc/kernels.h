@@ -139,6 +139,9 @@ cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t s
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st);
 cudaError_t launch_solve_T(const Grid& g, const SolveTArgs& a, cudaStream_t st);
+// ca[i] += src[i] per instance (grids: each instance's own coefficient size)
+cudaError_t launch_add_source(const Grid& g, Batch<const cpx> src, Batch<cpx> ca, int ninst, cudaStream_t st,
+                              const Grid* grids = nullptr);
 
 // split-transform intermediate per instance, in complex elements
 size_t split_tmp_elems(const Grid& g);

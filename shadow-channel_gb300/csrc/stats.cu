@@ -253,6 +253,18 @@ int c_mean_profile(int inc, int comp, int start_step, int end_step, double* out)
   return to_host(n, out, [&](double* d) { return mean_profile(0, inc, comp, start_step, end_step, d); });
 }
 
+int c_wall_shear_weights(double* out) {
+  const Grid* g = nullptr;
+  cudaStream_t st = nullptr;
+  if (!out || !engine_grid_stream(&g, &st)) {
+    engine_set_error(-2, "c_wall_shear_weights: needs c_init first and an output array");
+    return -2;
+  }
+  const std::vector<double> rp0 = rp_at(g->R, -1.0);
+  for (size_t i = 0; i < rp0.size(); ++i) out[i] = rp0[i];
+  return 0;
+}
+
 int c_wall_shear(int inc, int start_step, int end_step, double* out) {
   const size_t n = (size_t)(end_step > start_step ? end_step - start_step : 0) * 2;
   return to_host(n, out, [&](double* d) { return wall_shear(0, inc, start_step, end_step, d); });

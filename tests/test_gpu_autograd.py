@@ -59,3 +59,31 @@ def test_checkpoint_spacing_does_not_change_results(mod):
     for o in out[1:]:
         for a, b in zip(o, out[0]):
             assert abs(a - b) <= 1e-12 * abs(b)
+
+
+def test_state_gradient_matches_central_differences(mod):
+    """dJ/dC0 from the exact discrete adjoint (one reverse sweep per
+    checkpoint interval) against central differences of J along two random
+    directions, to 1e-6; checkpoint spacing leaves it unchanged to rounding."""
+    torch, ag = mod
+    C0 = _cfg(4)["C0"]
+    grads = []
+    for ck in (4, NSTEPS):
+        Re = torch.tensor(RE, dtype=torch.float64)
+        U = torch.tensor(MEANU, dtype=torch.float64)
+        Ct = torch.from_numpy(C0.view(np.float64).reshape(C0.shape + (2,)).copy()).requires_grad_(True)
+        J = ag.time_mean_wall_shear(Re, U, _cfg(ck), Ct)
+        J.backward()
+        assert Re.grad is None and Ct.grad is not None
+        grads.append(Ct.grad.numpy().copy())
+    g = grads[0]
+    assert np.linalg.norm(grads[1] - g) <= 1e-12 * np.linalg.norm(g)
+    for seed in (11, 12):
+        d = O.synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=seed, laminar=False)
+        d *= 1e-2 * np.linalg.norm(C0) / np.linalg.norm(d)
+        h = 1e-2
+        Jp = ag.primal_objective(GRID, RE, MEANU, C0 + h * d, NSTEPS, 4)[0]
+        Jm = ag.primal_objective(GRID, RE, MEANU, C0 - h * d, NSTEPS, 4)[0]
+        fd = (Jp - Jm) / (2 * h)
+        an = float(np.sum(g * d.view(np.float64).reshape(g.shape)))
+        assert abs(an - fd) <= 1e-6 * abs(fd), (an, fd)
