@@ -58,7 +58,9 @@ def args_parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the uneven-batch and 128x129x128 measurements")
+                    help="skip the exact-adjoint, uneven-batch and 128x129x128 measurements")
+    ap.add_argument("--extras", default="exact,uneven,large",
+                    help="comma list of the extra measurements to run: exact, uneven, large")
     ap.add_argument("--segments", type=int, default=NSEG,
                     help="segments per GPU (default 64; smaller only for profiling captures)")
     ap.add_argument("--runup", type=int, default=RUNUP,
@@ -169,8 +171,8 @@ def segment_step_flops(g):
 
 
 # ncu DRAM bytes (read + write) of one k_phys_inverse instance: a 24-instance
-# launch at 32x65x32 moved 315.6 MB; traffic grows with the instance count
-PHYS_TRAFFIC_PER_INSTANCE_32 = 315.6e6 / 24
+# launch at 32x65x32 moved 427.1 MB (147.9 read + 279.2 write); traffic grows with the instance count
+PHYS_TRAFFIC_PER_INSTANCE_32 = 427.1e6 / 24
 
 
 def recon_flops(ninst, g):
@@ -295,8 +297,9 @@ def run_gb300(a):
                          "achieved_tflops": step_flop * value / world / 1e12,
                          "frac": step_flop * value / world / 1e12 / peak}}
 
+    extras = set() if a.no_extras else {e.strip() for e in a.extras.split(",") if e.strip()}
     exact = None
-    if not a.no_extras and rank == 0:
+    if "exact" in extras and rank == 0:
         exact = exact_adjoint_timing(cc, torch, stream, dAC, K)
     cc.lib.c_batch_destroy()
     cc.c_destroy()
@@ -314,8 +317,9 @@ def run_gb300(a):
         line["plain_gpu"]["batched_over_plain"] = (value / world) / plain["value"]
     if exact:
         line["exact_adjoint"] = exact
-    if not a.no_extras and rank == 0:
+    if "uneven" in extras and rank == 0:
         line["uneven_batch"] = uneven_batch(cc)
+    if "large" in extras and rank == 0:
         line["large_grid"] = large_grid(cc)
     if rank == 0 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
