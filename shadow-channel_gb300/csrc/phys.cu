@@ -221,9 +221,7 @@ __global__ void __launch_bounds__(kThreads) k_products_fwd(const __grid_constant
   }
 }
 
-size_t prod_adj_smem_bytes(const Grid& g) {
-  return phys_smem_bytes(g, false) + (size_t)6 * g.Nz * g.X * sizeof(cpx);
-}
+size_t prod_adj_smem_bytes(const Grid& g) { return phys_smem_bytes(g, false); }
 
 template <bool MULTI, bool GEN>
 __global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant__ Grid g0, ProdArgs a) {
@@ -233,7 +231,6 @@ __global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant
   if (blocked(a.status, a.sdiv, inst)) return;
   extern __shared__ __align__(16) unsigned char smem[];
   PhysSmem s = carve(g, smem, false, true);
-  cpx* keep = reinterpret_cast<cpx*>(smem + phys_smem_hd(g, false));  // [6][Nz][X]
   load_tw(g, s);
   const size_t plane = (size_t)g.pz * g.px, fs = (size_t)g.Q * plane;
   const double* __restrict__ P = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane +
@@ -276,40 +273,14 @@ __global__ void __launch_bounds__(kThreads) k_products_adj(const __grid_constant
     }
     __syncthreads();
     cpx* zr = forward_plane<GEN>(g, s, pxF, pzF, exact ? 1.0 : g.norm);
+    // fold product q into the output slots (the (zp, x) -> thread map is the
+    // same for every q, so each thread re-reads only its own partial sums)
     for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x) {
       const int zp = i / g.X, x = i - zp * g.X;
       const int z = zrow_to_kz(g, zp);
-      if (z >= 0) keep[((size_t)q * g.Nz + z) * g.X + x] = zr[i];
+      if (z >= 0) assemble_stage(g, exact, H, z, y, x, q, zr[i]);
     }
     __syncthreads();
-  }
-  // H = -T + (i kz S_y, -i kz S_x + i kx S_z, -i kx S_y); keep S_x, S_z
-  for (int i = threadIdx.x; i < g.Nz * g.X; i += blockDim.x) {
-    const int z = i / g.X, x = i - z * g.X;
-    if (z == g.Nz / 2) continue;
-    if (exact) {
-      exact_assemble(g, H, z, y, x, keep[(0 * g.Nz + z) * g.X + x], keep[(1 * g.Nz + z) * g.X + x],
-                     keep[(2 * g.Nz + z) * g.X + x], keep[(3 * g.Nz + z) * g.X + x],
-                     keep[(4 * g.Nz + z) * g.X + x], keep[(5 * g.Nz + z) * g.X + x]);
-      continue;
-    }
-    const double kx = g.Kx[x], kz = g.Kz[z];
-    const cpx Sx = keep[(0 * g.Nz + z) * g.X + x], Sy = keep[(1 * g.Nz + z) * g.X + x];
-    const cpx Sz = keep[(2 * g.Nz + z) * g.X + x], Tx = keep[(3 * g.Nz + z) * g.X + x];
-    const cpx Ty = keep[(4 * g.Nz + z) * g.X + x], Tz = keep[(5 * g.Nz + z) * g.X + x];
-    cpx hx, hy, hz;
-    hx.re = -Tx.re - kz * Sy.im;
-    hx.im = -Tx.im + kz * Sy.re;
-    hy.re = -Ty.re + kz * Sx.im - kx * Sz.im;
-    hy.im = -Ty.im - kz * Sx.re + kx * Sz.re;
-    hz.re = -Tz.re + kx * Sy.im;
-    hz.im = -Tz.im - kx * Sy.re;
-    auto slot = [&](int c) -> cpx& { return H[(((size_t)z * 5 + c) * g.Q + y) * g.X + x]; };
-    slot(0) = hz;
-    slot(1) = hx;
-    slot(2) = hy;
-    slot(3) = Sx;
-    slot(4) = Sz;
   }
 }
 

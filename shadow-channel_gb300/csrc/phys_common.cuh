@@ -97,41 +97,52 @@ __device__ __forceinline__ double split_product(int mode, const double* __restri
   }
 }
 
-// the adjoint's assembly H = -T + (i kz S_y, -i kz S_x + i kx S_z, -i kx S_y),
-// keeping S_x, S_z (channel/pass2.c:501-566)
-__device__ __forceinline__ void adjoint_assemble(const Grid& g, cpx* __restrict__ H, int z, int y, int x,
-                                                 cpx Sx, cpx Sy, cpx Sz, cpx Tx, cpx Ty, cpx Tz) {
-  const double kx = g.Kx[x], kz = g.Kz[z];
-  cpx hx, hy, hz;
-  hx.re = -Tx.re - kz * Sy.im;
-  hx.im = -Tx.im + kz * Sy.re;
-  hy.re = -Ty.re + kz * Sx.im - kx * Sz.im;
-  hy.im = -Ty.im - kz * Sx.re + kx * Sz.re;
-  hz.re = -Tz.re + kx * Sy.im;
-  hz.im = -Tz.im - kx * Sy.re;
-  auto slot = [&](int c) -> cpx& { return H[(((size_t)z * 5 + c) * g.Q + y) * g.X + x]; };
-  slot(0) = hz;
-  slot(1) = hx;
-  slot(2) = hy;
-  slot(3) = Sx;
-  slot(4) = Sz;
-}
-
-// the transpose of the vorticity load (channel/pass1.c:58-104) applied to
-// the forward-transformed field cotangents t0..t5 (u, v, w, wz, wx, wy),
-// with the factor 2 of the transposed complex-to-real x transform off the
-// kx = 0 column:
+// The adjoint's output slots assembled one forward-transformed product at
+// a time, so a kernel needs no buffer for all six: stage q folds product q
+// into the slots it feeds, reading the partial sums earlier stages stored
+// (the same thread owns an output element through all six stages).
+//   reference adjoint (channel/pass2.c:501-566), products S_x, S_y, S_z,
+//   T_x, T_y, T_z:  H = -T + (i kz S_y, -i kz S_x + i kx S_z, -i kx S_y)
+//   in slots Hx 1, Hy 2, Hz 0, keeping S_x, S_z in slots 3, 4;
+//   exact transpose (`exact`), products t0..t5 = the cotangents of
+//   u, v, w, wz, wx, wy (the transpose of the vorticity load,
+//   channel/pass1.c:58-104), times 2 off the kx = 0 column (the transposed
+//   complex-to-real x transform):
 //   u = t0 - i kz t5,  v = t1 - i kx t3 + i kz t4,  w = t2 + i kx t5,
-//   du/dy = -t3,  dw/dy = t4
-__device__ __forceinline__ void exact_assemble(const Grid& g, cpx* __restrict__ U, int z, int y, int x, cpx t0,
-                                               cpx t1, cpx t2, cpx t3, cpx t4, cpx t5) {
-  const double kx = g.Kx[x], kz = g.Kz[z], f = x == 0 ? 1.0 : 2.0;
-  auto slot = [&](int c) -> cpx& { return U[(((size_t)z * 5 + c) * g.Q + y) * g.X + x]; };
-  slot(0) = cpx{f * (t0.re + kz * t5.im), f * (t0.im - kz * t5.re)};
-  slot(1) = cpx{f * (t1.re + kx * t3.im - kz * t4.im), f * (t1.im - kx * t3.re + kz * t4.re)};
-  slot(2) = cpx{f * (t2.re - kx * t5.im), f * (t2.im + kx * t5.re)};
-  slot(3) = cpx{-f * t3.re, -f * t3.im};
-  slot(4) = cpx{f * t4.re, f * t4.im};
+//   du/dy = -t3,  dw/dy = t4.
+// Explicit roundings (no contraction) make every kernel that uses this
+// produce the same bits.
+__device__ __forceinline__ void assemble_stage(const Grid& g, bool exact, cpx* __restrict__ H, int z, int y, int x,
+                                               int q, cpx t) {
+  const double kx = g.Kx[x], kz = g.Kz[z];
+  auto slot = [&](int c) -> cpx& { return H[(((size_t)z * 5 + c) * g.Q + y) * g.X + x]; };
+  auto scale = [](double a, cpx v) { return cpx{__dmul_rn(a, v.re), __dmul_rn(a, v.im)}; };
+  auto add = [](cpx a, cpx b) { return cpx{__dadd_rn(a.re, b.re), __dadd_rn(a.im, b.im)}; };
+  auto sub = [](cpx a, cpx b) { return cpx{__dsub_rn(a.re, b.re), __dsub_rn(a.im, b.im)}; };
+  auto imul = [](double k, cpx v) { return cpx{__dmul_rn(-k, v.im), __dmul_rn(k, v.re)}; };  // i k v
+  if (!exact) {
+    switch (q) {
+      case 0: slot(3) = t; slot(2) = imul(-kz, t); break;                   // S_x
+      case 1: slot(1) = imul(kz, t); slot(0) = imul(-kx, t); break;          // S_y
+      case 2: slot(4) = t; slot(2) = add(slot(2), imul(kx, t)); break;      // S_z
+      case 3: slot(1) = sub(slot(1), t); break;                             // T_x
+      case 4: slot(2) = sub(slot(2), t); break;                             // T_y
+      default: slot(0) = sub(slot(0), t); break;                            // T_z
+    }
+    return;
+  }
+  const double f = x == 0 ? 1.0 : 2.0;
+  switch (q) {
+    case 0: slot(0) = scale(f, t); break;
+    case 1: slot(1) = scale(f, t); break;
+    case 2: slot(2) = scale(f, t); break;
+    case 3: slot(1) = add(slot(1), scale(f, imul(-kx, t))); slot(3) = scale(-f, t); break;
+    case 4: slot(1) = add(slot(1), scale(f, imul(kz, t))); slot(4) = scale(f, t); break;
+    default:
+      slot(0) = add(slot(0), scale(f, imul(-kz, t)));
+      slot(2) = add(slot(2), scale(f, imul(kx, t)));
+      break;
+  }
 }
 
 }  // namespace chn

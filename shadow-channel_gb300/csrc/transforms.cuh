@@ -251,11 +251,7 @@ __global__ void __launch_bounds__(NT) k_tz_fwd(const __grid_constant__ Grid g0, 
     const int xl = i / g.Nz, z = i - xl * g.Nz;
     if (z == g.Nz / 2) continue;
     const cpx* K = keep + (size_t)xl * 6 * g.Nz + z;
-    if (mode == 3)
-      exact_assemble(g, H, z, y, c0 / 6 + xl, K[0], K[g.Nz], K[2 * g.Nz], K[3 * g.Nz], K[4 * g.Nz], K[5 * g.Nz]);
-    else
-      adjoint_assemble(g, H, z, y, c0 / 6 + xl, K[0], K[g.Nz], K[2 * g.Nz], K[3 * g.Nz], K[4 * g.Nz],
-                       K[5 * g.Nz]);
+    for (int q = 0; q < 6; ++q) assemble_stage(g, mode == 3, H, z, y, c0 / 6 + xl, q, K[q * g.Nz]);
   }
 }
 

@@ -6,9 +6,9 @@ transforms as separate z and x passes (csrc/phys.cu, split transforms).
   autotuner chooses from) at 32x65x32 must reproduce the fused results bit
   for bit through primal, tangents, the coupled adjoint and the exact
   adjoint.
-- 48x97x48 (the adjoint products no longer fit) and 128x129x128 (nothing
-  fits) against the oracle, one step each way, and the exact adjoint's
-  dot-product identity.
+- 48x97x48 (113 KB per plane) and 128x129x128 (no plane fits a block:
+  split transforms) against the oracle, one step each way, and the exact
+  adjoint's dot-product identity.
 """
 import json
 import os
