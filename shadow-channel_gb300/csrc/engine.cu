@@ -203,6 +203,7 @@ struct Work {
   long long vslot = 0, vstride = 0;
   std::vector<char> vel_ok;    // slot i of Pv holds the fields of MIC[3i]
   cpx* icp = nullptr;          // projected IC' of the last coupling, per segment
+  cpx* src = nullptr;          // per-step source of the exact adjoint (host-array entry point), per segment
   const Grid* gdev = nullptr;  // uneven batch: grid of each segment (device array); null: one grid
   cpx* Zt = nullptr;           // split transforms: spectral-column intermediate for zt_inst instances
   int zt_inst = 0;
@@ -260,7 +261,7 @@ struct Work {
            alloc(&io, nt * csz) && alloc(&Pp, nseg * psz) && alloc(&Pt, nt * psz) &&
            alloc(&Pprev, nseg * psz) && alloc(&Pl, nseg * psz) && alloc(&flow, (size_t)3 * g.Q * plane_size(g)) &&
            alloc(&part, (size_t)nseg * kDotBlocks * 2) && alloc(&r, nseg) && alloc(&cflmax, nseg) &&
-           alloc(&status, nseg) && alloc(&step, 4) && alloc(&icp, nseg * csz) &&
+           alloc(&status, nseg) && alloc(&step, 4) && alloc(&icp, nseg * csz) && alloc(&src, nseg * csz) &&
            alloc(&Ft, (size_t)nseg * (3 * (size_t)nsteps + 1)) && alloc_split(g, nt) && alloc_cache(g);
   }
   // split transforms (required where a plane exceeds a block's shared
@@ -1441,8 +1442,8 @@ void c_adjoint_exact_source(int start_step, int end_step, chn_complex* AC_given,
   shape_assert(start_step <= e.nsteps, "start_step <= nsteps");
   shape_assert(AC_given != nullptr && src != nullptr, "AC_given != 0 && src != 0");
   const size_t bytes = sizeof(cpx) * w.csz;
-  if (!h2d(e, w.io, AC_given, bytes) || !h2d(e, w.icp, src, bytes)) return;
-  if (!op_adjoint_exact(e, w, start_step, end_step, w.io, w.icp)) return;
+  if (!h2d(e, w.io, AC_given, bytes) || !h2d(e, w.src, src, bytes)) return;
+  if (!op_adjoint_exact(e, w, start_step, end_step, w.io, w.src)) return;
   if (!collect_status(e, w)) return;
   d2h(e, AC_given, w.Ca, bytes);
 }
