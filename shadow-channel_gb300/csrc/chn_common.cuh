@@ -83,6 +83,12 @@ struct Grid {
   // FFT twiddles exp(-2 pi i k/N), k < N, for N = pz and N = px
   const cpx* twz;
   const cpx* twx;
+  // tensor-core reconstruction (recon_tc.cu): base-256 digits of the five
+  // bases in mma A-fragment order [5][ceil(Q/16)][ceil(R/16)][7][32 lanes][4],
+  // and the row exponents [5][Q] (|basis row| < 2^tcE); tc = 0: FP64 kernel
+  const uint32_t* tcA;
+  const int* tcE;
+  int tc;
 };
 
 __host__ __device__ inline size_t coef_size(const Grid& g) { return (size_t)g.Nz * 2 * g.R * g.X; }

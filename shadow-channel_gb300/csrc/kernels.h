@@ -134,6 +134,9 @@ struct DdtArgs {
 void prepare_kernels(const Grid& g);  // function attributes; call once, outside graph capture
 
 cudaError_t launch_recon(const Grid& g, const ReconArgs& a, cudaStream_t st);
+// the reconstruction on the tensor cores (exact digit products, one FP64 rounding)
+cudaError_t launch_recon_tc(const Grid& g, const ReconArgs& a, cudaStream_t st);
+size_t recon_tc_smem_bytes(const Grid& g);
 cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t st);
 cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st);

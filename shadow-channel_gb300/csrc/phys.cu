@@ -373,6 +373,7 @@ cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t s
 
 void prepare_recon_solve(int optin);
 void prepare_solve_T(int optin);
+void prepare_recon_tc(int optin);
 
 // Every kernel may use up to the device's opt-in shared memory per block: the
 // single-grid engine and an uneven batch (sized for its largest grid) share
@@ -396,6 +397,7 @@ void prepare_kernels(const Grid& g) {
   for (const SplitEntry& e : kSplit) e.prepare(optin);
   prepare_recon_solve(optin);
   prepare_solve_T(optin);
+  prepare_recon_tc(optin);
 }
 
 }  // namespace chn

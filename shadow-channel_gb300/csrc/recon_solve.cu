@@ -169,6 +169,7 @@ size_t recon_smem_bytes(const Grid& g) { return (size_t)2 * g.R * kTile * sizeof
 
 cudaError_t launch_recon(const Grid& g, const ReconArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
+  if (g.tc) return launch_recon_tc(g, a, st);
   const int ntx = (g.X + kTile - 1) / kTile;
   if (a.grids) k_recon<true><<<dim3(g.Nz * ntx, a.ninst), kThreads, recon_smem_bytes(g), st>>>(g, a);
   else k_recon<false><<<dim3(g.Nz * ntx, a.ninst), kThreads, recon_smem_bytes(g), st>>>(g, a);

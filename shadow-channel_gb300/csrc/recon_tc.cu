@@ -1,0 +1,325 @@
+// Coefficients -> velocity (channel/initAlphaBeta2.c:12-240) on the tensor
+// cores, exact to the FP64 rounding of its result.
+//
+// The reconstruction is five real contractions per (kz, kx) column,
+//   v = Q alpha, Q' alpha, Q'' alpha, g = R beta, R' beta   (Q planes each),
+// followed by the K-algebra that mixes them into u, w, du/dy, dw/dy.  On
+// GB300 the FP64 pipe (1.2 TFLOP/s) bounds the direct form; here each
+// contraction runs as a bf16 tensor-core GEMM on integer digits:
+//   - every basis row (plane y) and every coefficient column is scaled by a
+//     power of two into an integer of 56 significant bits, written as seven
+//     balanced base-256 digits (the top digit in [-256, 256], the others in
+//     [-128, 127]); digits are exact in bf16;
+//   - digit products of level l = i + k accumulate in FP32 through
+//     mma.sync m16n8k16 (bf16 inputs, FP32 accumulator).  With K <= 112
+//     terms a level's partial sums stay below 2^24, so FP32 holds them
+//     exactly;
+//   - levels l < 7 are kept (the rest lie below 2^-56 of the operands'
+//     scale), recombined exactly in 64-bit integers and rounded once to FP64
+//     by one fma.
+// Only the rounding, the K-algebra and the (kx, kz) = (0, 0) mean mode
+// (computed directly) use the FP64 pipe.  Results agree with the FP64
+// contraction to its own rounding.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "chn_common.cuh"
+#include "kernels.h"
+#include "setup.h"
+
+namespace chn {
+
+static constexpr int kThreads = 256;
+static constexpr int kTile = 16;   // kx columns per block (32 real columns: re, im interleaved)
+static constexpr int kDig = 7;     // base-256 digits per operand
+static constexpr int kChunkKT = 7; // k-tiles per exact FP32 accumulation chunk (K <= 112)
+
+// ---------------------------------------------------------------------------
+// host: basis digit tables in mma A-fragment order
+// ---------------------------------------------------------------------------
+
+static inline uint16_t bf16_bits_of_int(int d) {
+  const float f = (float)d;  // |d| <= 256: exact in bf16, low 16 bits zero
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return (uint16_t)(u >> 16);
+}
+
+// seven balanced base-256 digits of x (|x| < 2^56), most significant first
+static inline void digits56(long long x, int* d) {
+  for (int i = kDig - 1; i >= 1; --i) {
+    const long long lo = ((x + 128) & 255) - 128;
+    d[i] = (int)lo;
+    x = (x - lo) >> 8;
+  }
+  d[0] = (int)x;
+}
+
+int recon_tc_ktiles(const Grid& g) { return (g.R + 15) / 16; }
+int recon_tc_mtiles(const Grid& g) { return (g.Q + 15) / 16; }
+
+bool build_recon_tc_tables(const HostTables& h, std::vector<uint32_t>& frag, std::vector<int>& ex) {
+  const int Q = h.Q, MT = (h.Q + 15) / 16, KT = (h.R + 15) / 16;
+  const std::vector<double>* B[5] = {&h.Bq, &h.Bqp, &h.Bqpp, &h.Br, &h.Brp};
+  frag.assign((size_t)5 * MT * KT * kDig * 32 * 4, 0u);
+  ex.assign((size_t)5 * Q, -1022);
+  std::vector<int> dig((size_t)Q * (KT * 16) * kDig, 0);
+  for (int b = 0; b < 5; ++b) {
+    const int K = b < 3 ? h.D : h.R;
+    const double* M = B[b]->data();
+    std::fill(dig.begin(), dig.end(), 0);
+    for (int y = 0; y < Q; ++y) {
+      double mx = 0.0;
+      for (int j = 0; j < K; ++j) mx = std::fmax(mx, std::fabs(M[(size_t)y * K + j]));
+      if (mx == 0.0) continue;
+      int e = 0;
+      std::frexp(mx, &e);  // |M[y][j]| < 2^e
+      ex[(size_t)b * Q + y] = e;
+      for (int j = 0; j < K; ++j) {
+        const long long x = std::llround(std::ldexp(M[(size_t)y * K + j], 56 - e));
+        digits56(x, &dig[((size_t)y * (KT * 16) + j) * kDig]);
+      }
+    }
+    auto at = [&](int y, int k, int i) -> uint16_t {
+      if (y >= Q || k >= K) return 0;
+      return bf16_bits_of_int(dig[((size_t)y * (KT * 16) + k) * kDig + i]);
+    };
+    for (int mt = 0; mt < MT; ++mt)
+      for (int kt = 0; kt < KT; ++kt)
+        for (int i = 0; i < kDig; ++i)
+          for (int lane = 0; lane < 32; ++lane) {
+            const int g = lane >> 2, t = lane & 3;
+            const int r0 = mt * 16 + g, r1 = r0 + 8, k0 = kt * 16 + 2 * t;
+            uint32_t* f = &frag[(((((size_t)b * MT + mt) * KT + kt) * kDig + i) * 32 + lane) * 4];
+            f[0] = (uint32_t)at(r0, k0, i) | ((uint32_t)at(r0, k0 + 1, i) << 16);
+            f[1] = (uint32_t)at(r1, k0, i) | ((uint32_t)at(r1, k0 + 1, i) << 16);
+            f[2] = (uint32_t)at(r0, k0 + 8, i) | ((uint32_t)at(r0, k0 + 9, i) << 16);
+            f[3] = (uint32_t)at(r1, k0 + 8, i) | ((uint32_t)at(r1, k0 + 9, i) << 16);
+          }
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// device
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void mma_bf16_16816(float* d, const uint4& a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
+}
+
+__host__ __device__ inline int recon_tc_kstride(int KT) { return KT * 16 + 8; }  // bf16 per digit row (padded)
+
+size_t recon_tc_smem_bytes(const Grid& g) {
+  const int KT = (g.R + 15) / 16;
+  return (size_t)2 * kDig * 32 * recon_tc_kstride(KT) * sizeof(uint16_t) + 2 * kTile * sizeof(int);
+}
+
+// the seven digits of v * 2^(56 - ex) from the bit pattern (integer ops only);
+// ex bounds the column: |v| < 2^ex
+__device__ __forceinline__ long long scaled56(double v, int ex) {
+  const long long bits = __double_as_longlong(v);
+  const int ef = (int)((bits >> 52) & 0x7FF);
+  if (ef == 0) return 0;  // zero (denormals are below every scale in use)
+  long long sig = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+  const int s = ef - 1019 - ex;  // <= 3
+  if (s >= 0) sig <<= s;
+  else if (s > -62) sig = (sig + (1LL << (-s - 1))) >> (-s);
+  else sig = 0;
+  return bits < 0 ? -sig : sig;
+}
+
+// exact value (H 2^32 + L) 2^e rounded once to FP64
+__device__ __forceinline__ double round_scaled(long long H, long long L, int e) {
+  if (e >= -1022 && e + 32 <= 1023) {
+    const double s = __longlong_as_double((long long)(e + 1023) << 52);
+    const double s32 = __longlong_as_double((long long)(e + 32 + 1023) << 52);
+    return fma((double)H, s32, (double)L * s);
+  }
+  return fma((double)H, scalbn(1.0, e + 32), scalbn((double)L, e));
+}
+
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant__ Grid g0, ReconArgs a) {
+  const int ntx = (g0.X + kTile - 1) / kTile;
+  const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
+  const int inst = blockIdx.y;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
+  if (z >= g.Nz || tx * kTile >= g.X) return;
+  if (z == g.Nz / 2) return;  // never read (channel/pass1.c:51-85 skips it)
+  if (a.status != nullptr && (a.status[inst / a.sdiv] & ST_CFL) != 0) return;
+  const int x0 = tx * kTile;
+  const int nx = min(kTile, g.X - x0);
+  const int KT = (g.R + 15) / 16, KS = recon_tc_kstride(KT), MT = (g.Q + 15) / 16;
+  const bool meancol = (z == 0 && x0 == 0);  // column 0 of this tile is the mean mode
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint16_t* dig = reinterpret_cast<uint16_t*>(smem);  // [cls][digit][n 32][KS]
+  int* exc = reinterpret_cast<int*>(smem + (size_t)2 * kDig * 32 * KS * sizeof(uint16_t));  // [cls][16]
+  const cpx* __restrict__ C = a.C.at(inst);
+  if (a.slot.stride) C += (long long)a.slot.slot() * a.slot.stride;
+  auto cval = [&](int cls, int j, int col) -> cpx {
+    const int K = cls == 0 ? g.D : g.R;
+    if (j >= K || col >= nx || (meancol && col == 0)) return cpx{0.0, 0.0};
+    return C[(((size_t)z * 2 + cls) * g.R + j) * g.X + x0 + col];
+  };
+  // column exponents: |c| < 2^exc over the column's real and imaginary parts
+  for (int i = threadIdx.x; i < 2 * kTile; i += blockDim.x) exc[i] = 0;
+  __syncthreads();
+  const int nent = 2 * (KT * 16) * kTile;
+  for (int i = threadIdx.x; i < nent; i += blockDim.x) {
+    const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
+    const cpx v = cval(cls, j, col);
+    const int e1 = (int)((__double_as_longlong(v.re) >> 52) & 0x7FF);
+    const int e2 = (int)((__double_as_longlong(v.im) >> 52) & 0x7FF);
+    const int e = max(e1, e2);
+    if (e) atomicMax(&exc[cls * kTile + col], e);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nent; i += blockDim.x) {
+    const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
+    const cpx v = cval(cls, j, col);
+    const int ex = exc[cls * kTile + col] - 1022;
+    for (int p = 0; p < 2; ++p) {
+      long long x = scaled56(p ? v.im : v.re, ex);
+      int d[kDig];
+      for (int q = kDig - 1; q >= 1; --q) {
+        const long long lo = ((x + 128) & 255) - 128;
+        d[q] = (int)lo;
+        x = (x - lo) >> 8;
+      }
+      d[0] = (int)x;
+      const int n = 2 * col + p;
+#pragma unroll
+      for (int q = 0; q < kDig; ++q) {
+        const __nv_bfloat16 h = __float2bfloat16_rn((float)d[q]);
+        dig[(((size_t)cls * kDig + q) * 32 + n) * KS + j] = *reinterpret_cast<const uint16_t*>(&h);
+      }
+    }
+  }
+  __syncthreads();
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
+  const int NT = (2 * nx + 7) / 8;  // n-tiles of 8 real columns (4 complex)
+  const uint4* __restrict__ A = reinterpret_cast<const uint4*>(g.tcA);
+  cpx* __restrict__ U = a.U.at(inst);
+  const size_t cs = (size_t)g.Q * g.X;
+  const int order[5] = {0, 1, 3, 2, 4};
+  for (int item = warp; item < MT * NT; item += blockDim.x >> 5) {
+    const int mt = item / NT, nt = item - mt * NT;
+    const int col = nt * 4 + t;  // this thread's complex column
+    const int n = nt * 8 + gq;   // the B-fragment column this thread loads
+    cpx held[2];                 // Q' alpha, then Q'' alpha, at rows gq and gq + 8
+    for (int ob = 0; ob < 5; ++ob) {
+      const int b = order[ob], cls = b < 3 ? 0 : 1;
+      const int KTb = ((cls == 0 ? g.D : g.R) + 15) / 16;
+      const int ecol = exc[cls * kTile + col] - 1022;
+      double part[4] = {0.0, 0.0, 0.0, 0.0};  // sums of earlier chunks (only when K > 112)
+      long long H[4], L[4];
+      for (int kc = 0; kc < KTb; kc += kChunkKT) {
+        float acc[kDig][4];
+#pragma unroll
+        for (int l = 0; l < kDig; ++l)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+        const int kend = min(KTb, kc + kChunkKT);
+        for (int kt = kc; kt < kend; ++kt) {
+          const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + ((size_t)cls * kDig * 32 + n) * KS + kt * 16);
+#pragma unroll
+          for (int i = 0; i < kDig; ++i) {
+            const uint4 af = __ldg(&A[(((((size_t)b * MT + mt) * KT + kt) * kDig + i) * 32 + lane)]);
+#pragma unroll
+            for (int k = 0; k < kDig - i; ++k) {
+              const uint32_t* row = brow + (size_t)k * 32 * KS / 2;
+              mma_bf16_16816(acc[i + k], af, row[t], row[t + 4]);
+            }
+          }
+        }
+        // the chunk's exact level sums as 64-bit integers
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          long long lv[kDig];
+#pragma unroll
+          for (int l = 0; l < kDig; ++l) lv[l] = (long long)__float2int_rn(acc[l][r]);
+          H[r] = (lv[0] << 16) + (lv[1] << 8) + lv[2];
+          L[r] = (lv[3] << 24) + (lv[4] << 16) + (lv[5] << 8) + lv[6];
+        }
+        if (kend < KTb) {  // more chunks follow: keep this one as FP64
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            const int y = mt * 16 + gq + 8 * (r >> 1);
+            const int e = g.tcE[(size_t)b * g.Q + min(y, g.Q - 1)] + ecol - 64;
+            part[r] += round_scaled(H[r], L[r], e);
+          }
+        }
+      }
+#pragma unroll
+      for (int rr = 0; rr < 2; ++rr) {
+        const int y = mt * 16 + gq + 8 * rr;
+        if (y >= g.Q || col >= nx || (meancol && col == 0)) continue;
+        const int e = g.tcE[(size_t)b * g.Q + y] + ecol - 64;
+        const cpx val = {part[2 * rr] + round_scaled(H[2 * rr], L[2 * rr], e),
+                         part[2 * rr + 1] + round_scaled(H[2 * rr + 1], L[2 * rr + 1], e)};
+        const int x = x0 + col;
+        cpx* out = U + ((size_t)z * 5 * g.Q + y) * g.X + x;
+        const double ax = g.kxK2[(size_t)z * g.X + x], az = g.kzK2[(size_t)z * g.X + x];
+        if (b == 0) {
+          out[cs] = val;  // v = Q alpha
+        } else if (b == 1 || b == 2) {
+          held[rr] = val;
+        } else if (b == 3) {
+          // u = (kx Im f + kz Im g)/K2 - i (kx Re f + kz Re g)/K2 etc., f = -Q' alpha
+          const cpx f = {-held[rr].re, -held[rr].im}, gg = val;
+          out[0] = cpx{fma(ax, f.im, az * gg.im), -fma(ax, f.re, az * gg.re)};
+          out[2 * cs] = cpx{fma(-ax, gg.im, az * f.im), fma(ax, gg.re, -az * f.re)};
+        } else {
+          const cpx qpp = held[rr], rp = val;
+          out[3 * cs] = cpx{fma(-ax, qpp.im, az * rp.im), fma(ax, qpp.re, -az * rp.re)};
+          out[4 * cs] = cpx{-fma(ax, rp.im, az * qpp.im), fma(ax, rp.re, az * qpp.re)};
+        }
+      }
+    }
+  }
+  if (meancol) {
+    // (kx, kz) = (0, 0): u = R a, du = R' a, v = 0, w = R b, dw = R' b
+    // (channel/initAlphaBeta2.c:25-68), direct FP64
+    for (int y = threadIdx.x; y < g.Q; y += blockDim.x) {
+      double ur = 0, ui = 0, dur = 0, dui = 0, wr = 0, wi = 0, dwr = 0, dwi = 0;
+      for (int j = 0; j < g.R; ++j) {
+        const double r = __ldg(g.Br + (size_t)y * g.R + j), rp = __ldg(g.Brp + (size_t)y * g.R + j);
+        const cpx al = C[((size_t)0 * g.R + j) * g.X], be = C[((size_t)1 * g.R + j) * g.X];
+        ur = fma(r, al.re, ur); ui = fma(r, al.im, ui);
+        dur = fma(rp, al.re, dur); dui = fma(rp, al.im, dui);
+        wr = fma(r, be.re, wr); wi = fma(r, be.im, wi);
+        dwr = fma(rp, be.re, dwr); dwi = fma(rp, be.im, dwi);
+      }
+      cpx* out = U + (size_t)y * g.X;
+      out[0] = cpx{ur, ui};
+      out[cs] = cpx{0.0, 0.0};
+      out[2 * cs] = cpx{wr, wi};
+      out[3 * cs] = cpx{dur, dui};
+      out[4 * cs] = cpx{dwr, dwi};
+    }
+  }
+}
+
+cudaError_t launch_recon_tc(const Grid& g, const ReconArgs& a, cudaStream_t st) {
+  const int ntx = (g.X + kTile - 1) / kTile;
+  const size_t sm = recon_tc_smem_bytes(g);
+  if (a.grids) k_recon_tc<true><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
+  else k_recon_tc<false><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
+  return cudaGetLastError();
+}
+
+void prepare_recon_tc(int optin) {
+  allow_max_smem(k_recon_tc<false>, optin);
+  allow_max_smem(k_recon_tc<true>, optin);
+}
+
+}  // namespace chn

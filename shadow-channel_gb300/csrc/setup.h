@@ -3,6 +3,8 @@
 // the LU factors of every implicit operator the RK3 step can ask for.
 #pragma once
 
+#include <stdint.h>
+
 #include <vector>
 
 namespace chn {
@@ -34,5 +36,9 @@ bool build_tables(int Nx, int Ny, int Nz, double Lx, double Lz, double Re, doubl
 // elimination order, channel/mvOps.c:35-65): L multipliers left of column
 // dl, the pivots in column dl, U to the right.
 void band_lu(double* A, int w, int dl, int du, int N);
+
+// base-256 digit tables of the five Legendre bases for the tensor-core
+// reconstruction (recon_tc.cu)
+bool build_recon_tc_tables(const HostTables& h, std::vector<uint32_t>& frag, std::vector<int>& ex);
 
 }  // namespace chn
