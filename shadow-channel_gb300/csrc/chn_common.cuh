@@ -88,6 +88,10 @@ struct Grid {
   // and the row exponents [5][Q] (|basis row| < 2^tcE); tc = 0: FP64 kernel
   const uint32_t* tcA;
   const int* tcE;
+  // the weighted transposes Qw, Qpw, Qppw, Rw, Rpw likewise, rows padded to R:
+  // [5][ceil(R/16)][ceil(Q/16)][7][32][4], row exponents [5][R]
+  const uint32_t* tcW;
+  const int* tcWE;
   int tc;
 };
 

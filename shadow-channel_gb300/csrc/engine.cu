@@ -149,9 +149,11 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   T.luQs = const_cast<double*>(a);
   T.luRs = const_cast<double*>(b);
   {
-    std::vector<uint32_t> frag;
-    std::vector<int> ex;
-    if (!build_recon_tc_tables(h, frag, ex) || !T.up(frag, &g.tcA) || !T.up(ex, &g.tcE)) return false;
+    std::vector<uint32_t> frag, wfrag;
+    std::vector<int> ex, wex;
+    if (!build_recon_tc_tables(h, frag, ex, wfrag, wex) || !T.up(frag, &g.tcA) || !T.up(ex, &g.tcE) ||
+        !T.up(wfrag, &g.tcW) || !T.up(wex, &g.tcWE))
+      return false;
   }
   // transforms: one block per plane where the plane fits the shared memory,
   // else separate z / x passes (CHN_SPLIT_TRANSFORMS=1 forces them)
@@ -168,7 +170,7 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
     set_error(1, "grid %dx%dx%d: the split transforms need more shared memory than the device has", Nx, Ny, Nz);
     return false;
   }
-  // reconstruction on the tensor cores unless CHN_RECON_FP64=1 (or it does not fit)
+  // reconstruction and quadratures on the tensor cores unless CHN_RECON_FP64=1 (or it does not fit)
   const char* fp64 = getenv("CHN_RECON_FP64");
   g.tc = (!(fp64 && fp64[0] == '1') && recon_tc_smem_bytes(g) + 4096 <= (size_t)optin) ? 1 : 0;
   if (solve_smem_bytes(g) > (size_t)optin || recon_smem_bytes(g) > (size_t)optin) {

@@ -15,6 +15,7 @@
 // the FP64 multiply-adds of every quadrature and reconstruction.
 #include "chn_common.cuh"
 #include "kernels.h"
+#include "tc_common.cuh"
 
 namespace chn {
 
@@ -213,9 +214,14 @@ struct SolveSmem {
   double* m0; // mean-mode scratch
 };
 
+// digits of one quadrature input for the tensor-core quadrature: [7][32][KS] bf16 + 16 exponents
+__host__ __device__ inline size_t solve_tc_kstride(const Grid& g) { return (size_t)((g.Q + 15) / 16) * 16 + 8; }
+
 __host__ __device__ inline size_t solve_hc_elems(const Grid& g) {
   size_t hc = (size_t)g.Qh * kTile * 6, r = 2 * (size_t)g.R * kTile;
-  return hc > r ? hc : r;
+  const size_t tc = ((size_t)kDig * 32 * solve_tc_kstride(g) * 2 + 16 * sizeof(int) + sizeof(cpx) - 1) / sizeof(cpx);
+  if (r > hc) hc = r;
+  return tc > hc ? tc : hc;
 }
 
 size_t solve_smem_bytes(const Grid& g) {
@@ -360,6 +366,129 @@ __device__ void quad_rhs(const Grid& g, const cpx* __restrict__ H, int z, int x0
   }
 }
 
+// The same right-hand side on the tensor cores (tc_common.cuh): each input
+// vector over the Q planes, per column, as base-256 digits (shared memory
+// of the FP64 version's parity-combined inputs), times the digit tables of
+// the weighted transposes; one FP64 rounding per contraction.
+//   Fa = Qpw P - K2 Qw Hy [+ Qppw Sa],   Fb = Rw G [+ Rpw Sb]
+__device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int x0, int nx, bool adj,
+                            SolveSmem& s) {
+  const int KT = (g.Q + 15) / 16, MTw = (g.R + 15) / 16;
+  const size_t KS = solve_tc_kstride(g);
+  uint16_t* dig = reinterpret_cast<uint16_t*>(s.hc);             // [7][32 columns][KS]
+  int* exc = reinterpret_cast<int*>(dig + (size_t)kDig * 32 * KS);  // [16]
+  const double kz = g.Kz[z];
+  const size_t cs = (size_t)g.Q * g.X;
+  const cpx* Hz_ = H + (size_t)z * 5 * cs;  // slot c at Hz_ + c*cs + y*X + x
+  // input q: 0 P = i(kx Hx + kz Hz), 1 Hy, 2 Sa = -i(kz Sx - kx Sz), 3 G = i(kz Hx - kx Hz),
+  // 4 Sb = i(kz Sz + kx Sx); weight table: Qpw 1, Qw 0, Qppw 2, Rw 3, Rpw 4
+  auto input = [&](int q, int y, int col) -> cpx {
+    const int x = x0 + col;
+    const double kx = g.Kx[x];
+    const cpx* b = Hz_ + (size_t)y * g.X + x;
+    switch (q) {
+      case 0: { const cpx hx = b[cs], hz = b[0];
+                return cpx{-kx * hx.im - kz * hz.im, kx * hx.re + kz * hz.re}; }
+      case 1: return b[2 * cs];
+      case 2: { const cpx sx = b[3 * cs], sz = b[4 * cs];
+                return cpx{kz * sx.im - kx * sz.im, -kz * sx.re + kx * sz.re}; }
+      case 3: { const cpx hx = b[cs], hz = b[0];
+                return cpx{-kz * hx.im + kx * hz.im, kz * hx.re - kx * hz.re}; }
+      default: { const cpx sx = b[3 * cs], sz = b[4 * cs];
+                 return cpx{-kz * sz.im - kx * sx.im, kz * sz.re + kx * sx.re}; }
+    }
+  };
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
+  const int NT = (2 * nx + 7) / 8;
+  const uint4* __restrict__ W = reinterpret_cast<const uint4*>(g.tcW);
+  const int qs[5] = {0, 1, 3, 2, 4};
+  const int nq = adj ? 5 : 3;
+  for (int iq = 0; iq < nq; ++iq) {
+    const int q = adj ? iq : qs[iq];
+    const int w = q == 0 ? 1 : (q == 1 ? 0 : q);
+    const bool toA = q < 3;
+    const int N = toA ? g.D : g.R;
+    cpx* F = toA ? s.Fa : s.Fb;
+    const bool first = (q == 0 || q == 3);
+    for (int i = threadIdx.x; i < kTile; i += blockDim.x) exc[i] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < g.Q * kTile; i += blockDim.x) {
+      const int y = i / kTile, col = i - y * kTile;
+      if (col >= nx) continue;
+      const cpx v = input(q, y, col);
+      const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
+                        (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
+      if (e) atomicMax(&exc[col], e);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < KT * 16 * kTile; i += blockDim.x) {
+      const int y = i / kTile, col = i - y * kTile;
+      const cpx v = (y < g.Q && col < nx) ? input(q, y, col) : cpx{0.0, 0.0};
+      const int ex = exc[col] - 1022;
+      digits_bf16(scaled56(v.re, ex), dig + (size_t)(2 * col) * KS + y, 32 * KS);
+      digits_bf16(scaled56(v.im, ex), dig + (size_t)(2 * col + 1) * KS + y, 32 * KS);
+    }
+    __syncthreads();
+    const int MTn = (N + 15) / 16;
+    for (int item = warp; item < MTn * NT; item += blockDim.x >> 5) {
+      const int mt = item / NT, nt = item - mt * NT;
+      const int col = nt * 4 + t, n = nt * 8 + gq;
+      const int ecol = exc[min(col, kTile - 1)] - 1022;
+      double part[4] = {0.0, 0.0, 0.0, 0.0};
+      long long Hh[4], Ll[4];
+      for (int kc = 0; kc < KT; kc += kChunkKT) {
+        float acc[kDig][4];
+#pragma unroll
+        for (int l = 0; l < kDig; ++l)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+        const int kend = min(KT, kc + kChunkKT);
+        for (int kt = kc; kt < kend; ++kt) {
+          const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
+#pragma unroll
+          for (int i = 0; i < kDig; ++i) {
+            const uint4 af = __ldg(&W[((((size_t)w * MTw + mt) * KT + kt) * kDig + i) * 32 + lane]);
+#pragma unroll
+            for (int k = 0; k < kDig - i; ++k) {
+              const uint32_t* row = brow + (size_t)k * 32 * KS / 2;
+              mma_bf16_16816(acc[i + k], af, row[t], row[t + 4]);
+            }
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) fold_levels(acc, r, Hh[r], Ll[r]);
+        if (kend < KT) {
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            const int row = mt * 16 + gq + 8 * (r >> 1);
+            part[r] += round_scaled(Hh[r], Ll[r], g.tcWE[(size_t)w * g.R + min(row, g.R - 1)] + ecol - 64);
+          }
+        }
+      }
+#pragma unroll
+      for (int rr = 0; rr < 2; ++rr) {
+        const int row = mt * 16 + gq + 8 * rr;
+        if (row >= N || col >= nx) continue;
+        const int e = g.tcWE[(size_t)w * g.R + row] + ecol - 64;
+        const cpx val = {part[2 * rr] + round_scaled(Hh[2 * rr], Ll[2 * rr], e),
+                         part[2 * rr + 1] + round_scaled(Hh[2 * rr + 1], Ll[2 * rr + 1], e)};
+        cpx& f = F[row * kTile + col];
+        if (first) {
+          f = val;
+        } else if (q == 1) {
+          const double k2 = g.K2[(size_t)z * g.X + x0 + col];
+          f.re = fma(-k2, val.re, f.re);
+          f.im = fma(-k2, val.im, f.im);
+        } else {
+          f.re += val.re;
+          f.im += val.im;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // out[i] = sum_j A[i][j] y[i + 2(j - dl)] over the valid band (channel/mvOps.c:198-220)
 __device__ __forceinline__ cpx band_matvec_row(const double* __restrict__ A, int w, int dl, int du, int N,
                                                const cpx* y, int ystride, int i) {
@@ -487,7 +616,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   const RKc rk = rk_coeffs(a.k, a.adjoint);
   const bool adj = a.adjoint != 0;
   const cpx* __restrict__ H = a.H.at(inst);
-  quad_rhs(g, H, z, x0, nx, adj, s);
+  if (g.tc) quad_rhs_tc(g, H, z, x0, nx, adj, s);
+  else quad_rhs(g, H, z, x0, nx, adj, s);
   const double dt = g.dt;
   const int xfirst = (z == 0 && x0 == 0) ? 1 : 0;  // the mean mode has its own system
   // Re-sensitivity forcing of this tangent (kind 2: the reference's forcing
@@ -761,7 +891,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   //  channel/adjproject.c:393-549)
   if (adj) {
     __syncthreads();
-    quad_rhs(g, a.Hprev.at(inst), z, x0, nx, true, s);
+    if (g.tc) quad_rhs_tc(g, a.Hprev.at(inst), z, x0, nx, true, s);
+    else quad_rhs(g, a.Hprev.at(inst), z, x0, nx, true, s);
     if (xfirst == 1 && threadIdx.x < 32) {
       // mean mode fa/fb from the previous-stage terms (channel/adjproject0.c:254-294)
       const cpx* H0 = a.Hprev.at(inst);

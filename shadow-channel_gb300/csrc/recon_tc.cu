@@ -29,76 +29,78 @@
 #include "chn_common.cuh"
 #include "kernels.h"
 #include "setup.h"
+#include "tc_common.cuh"
 
 namespace chn {
 
 static constexpr int kThreads = 256;
 static constexpr int kTile = 16;   // kx columns per block (32 real columns: re, im interleaved)
-static constexpr int kDig = 7;     // base-256 digits per operand
-static constexpr int kChunkKT = 7; // k-tiles per exact FP32 accumulation chunk (K <= 112)
 
 // ---------------------------------------------------------------------------
 // host: basis digit tables in mma A-fragment order
 // ---------------------------------------------------------------------------
 
-static inline uint16_t bf16_bits_of_int(int d) {
-  const float f = (float)d;  // |d| <= 256: exact in bf16, low 16 bits zero
-  uint32_t u;
-  std::memcpy(&u, &f, 4);
-  return (uint16_t)(u >> 16);
-}
-
-// seven balanced base-256 digits of x (|x| < 2^56), most significant first
-static inline void digits56(long long x, int* d) {
-  for (int i = kDig - 1; i >= 1; --i) {
-    const long long lo = ((x + 128) & 255) - 128;
-    d[i] = (int)lo;
-    x = (x - lo) >> 8;
-  }
-  d[0] = (int)x;
-}
-
 int recon_tc_ktiles(const Grid& g) { return (g.R + 15) / 16; }
 int recon_tc_mtiles(const Grid& g) { return (g.Q + 15) / 16; }
 
-bool build_recon_tc_tables(const HostTables& h, std::vector<uint32_t>& frag, std::vector<int>& ex) {
-  const int Q = h.Q, MT = (h.Q + 15) / 16, KT = (h.R + 15) / 16;
-  const std::vector<double>* B[5] = {&h.Bq, &h.Bqp, &h.Bqpp, &h.Br, &h.Brp};
-  frag.assign((size_t)5 * MT * KT * kDig * 32 * 4, 0u);
-  ex.assign((size_t)5 * Q, -1022);
-  std::vector<int> dig((size_t)Q * (KT * 16) * kDig, 0);
-  for (int b = 0; b < 5; ++b) {
-    const int K = b < 3 ? h.D : h.R;
-    const double* M = B[b]->data();
-    std::fill(dig.begin(), dig.end(), 0);
-    for (int y = 0; y < Q; ++y) {
-      double mx = 0.0;
-      for (int j = 0; j < K; ++j) mx = std::fmax(mx, std::fabs(M[(size_t)y * K + j]));
-      if (mx == 0.0) continue;
-      int e = 0;
-      std::frexp(mx, &e);  // |M[y][j]| < 2^e
-      ex[(size_t)b * Q + y] = e;
-      for (int j = 0; j < K; ++j) {
-        const long long x = std::llround(std::ldexp(M[(size_t)y * K + j], 56 - e));
-        digits56(x, &dig[((size_t)y * (KT * 16) + j) * kDig]);
-      }
+bool append_digit_table(const double* M, int rows, int K, int MT, int KT, std::vector<uint32_t>& frag,
+                        std::vector<int>& ex) {
+  const size_t base = frag.size();
+  frag.resize(base + (size_t)MT * KT * kDig * 32 * 4, 0u);
+  const size_t ebase = ex.size();
+  ex.resize(ebase + rows, -1022);
+  std::vector<int> dig((size_t)rows * (KT * 16) * kDig, 0);
+  for (int y = 0; y < rows; ++y) {
+    double mx = 0.0;
+    for (int j = 0; j < K; ++j) mx = std::fmax(mx, std::fabs(M[(size_t)y * K + j]));
+    if (mx == 0.0) continue;
+    int e = 0;
+    std::frexp(mx, &e);  // |M[y][j]| < 2^e
+    ex[ebase + y] = e;
+    for (int j = 0; j < K; ++j) {
+      const long long x = std::llround(std::ldexp(M[(size_t)y * K + j], 56 - e));
+      digits56(x, &dig[((size_t)y * (KT * 16) + j) * kDig]);
     }
-    auto at = [&](int y, int k, int i) -> uint16_t {
-      if (y >= Q || k >= K) return 0;
-      return bf16_bits_of_int(dig[((size_t)y * (KT * 16) + k) * kDig + i]);
-    };
-    for (int mt = 0; mt < MT; ++mt)
-      for (int kt = 0; kt < KT; ++kt)
-        for (int i = 0; i < kDig; ++i)
-          for (int lane = 0; lane < 32; ++lane) {
-            const int g = lane >> 2, t = lane & 3;
-            const int r0 = mt * 16 + g, r1 = r0 + 8, k0 = kt * 16 + 2 * t;
-            uint32_t* f = &frag[(((((size_t)b * MT + mt) * KT + kt) * kDig + i) * 32 + lane) * 4];
-            f[0] = (uint32_t)at(r0, k0, i) | ((uint32_t)at(r0, k0 + 1, i) << 16);
-            f[1] = (uint32_t)at(r1, k0, i) | ((uint32_t)at(r1, k0 + 1, i) << 16);
-            f[2] = (uint32_t)at(r0, k0 + 8, i) | ((uint32_t)at(r0, k0 + 9, i) << 16);
-            f[3] = (uint32_t)at(r1, k0 + 8, i) | ((uint32_t)at(r1, k0 + 9, i) << 16);
-          }
+  }
+  auto at = [&](int y, int k, int i) -> uint16_t {
+    if (y >= rows || k >= K) return 0;
+    return bf16_bits_of_int(dig[((size_t)y * (KT * 16) + k) * kDig + i]);
+  };
+  for (int mt = 0; mt < MT; ++mt)
+    for (int kt = 0; kt < KT; ++kt)
+      for (int i = 0; i < kDig; ++i)
+        for (int lane = 0; lane < 32; ++lane) {
+          const int g = lane >> 2, t = lane & 3;
+          const int r0 = mt * 16 + g, r1 = r0 + 8, k0 = kt * 16 + 2 * t;
+          uint32_t* f = &frag[base + ((((size_t)mt * KT + kt) * kDig + i) * 32 + lane) * 4];
+          f[0] = (uint32_t)at(r0, k0, i) | ((uint32_t)at(r0, k0 + 1, i) << 16);
+          f[1] = (uint32_t)at(r1, k0, i) | ((uint32_t)at(r1, k0 + 1, i) << 16);
+          f[2] = (uint32_t)at(r0, k0 + 8, i) | ((uint32_t)at(r0, k0 + 9, i) << 16);
+          f[3] = (uint32_t)at(r1, k0 + 8, i) | ((uint32_t)at(r1, k0 + 9, i) << 16);
+        }
+  return true;
+}
+
+// the five bases [Q][D or R] (rows: planes) and the five weighted
+// transposes [D or R][Q] (rows: basis index) as digit tables
+bool build_recon_tc_tables(const HostTables& h, std::vector<uint32_t>& frag, std::vector<int>& ex,
+                           std::vector<uint32_t>& wfrag, std::vector<int>& wex) {
+  const int MT = (h.Q + 15) / 16, KT = (h.R + 15) / 16;
+  const std::vector<double>* B[5] = {&h.Bq, &h.Bqp, &h.Bqpp, &h.Br, &h.Brp};
+  frag.clear();
+  ex.clear();
+  for (int b = 0; b < 5; ++b)
+    if (!append_digit_table(B[b]->data(), h.Q, b < 3 ? h.D : h.R, MT, KT, frag, ex)) return false;
+  const int MTw = (h.R + 15) / 16, KTw = (h.Q + 15) / 16;
+  const std::vector<double>* W[5] = {&h.Wq, &h.Wqp, &h.Wqpp, &h.Wr, &h.Wrp};
+  wfrag.clear();
+  wex.clear();
+  for (int b = 0; b < 5; ++b) {
+    // rows padded to R so that every table has MTw row tiles and R exponents
+    std::vector<double> m((size_t)h.R * h.Q, 0.0);
+    const int rows = b < 3 ? h.D : h.R;
+    std::copy(W[b]->begin(), W[b]->begin() + (size_t)rows * h.Q, m.begin());
+    if (!append_digit_table(m.data(), h.R, h.Q, MTw, KTw, wfrag, wex)) return false;
   }
   return true;
 }
@@ -107,43 +109,11 @@ bool build_recon_tc_tables(const HostTables& h, std::vector<uint32_t>& frag, std
 // device
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ void mma_bf16_16816(float* d, const uint4& a, uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
-}
-
 __host__ __device__ inline int recon_tc_kstride(int KT) { return KT * 16 + 8; }  // bf16 per digit row (padded)
 
 size_t recon_tc_smem_bytes(const Grid& g) {
   const int KT = (g.R + 15) / 16;
   return (size_t)2 * kDig * 32 * recon_tc_kstride(KT) * sizeof(uint16_t) + 2 * kTile * sizeof(int);
-}
-
-// the seven digits of v * 2^(56 - ex) from the bit pattern (integer ops only);
-// ex bounds the column: |v| < 2^ex
-__device__ __forceinline__ long long scaled56(double v, int ex) {
-  const long long bits = __double_as_longlong(v);
-  const int ef = (int)((bits >> 52) & 0x7FF);
-  if (ef == 0) return 0;  // zero (denormals are below every scale in use)
-  long long sig = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
-  const int s = ef - 1019 - ex;  // <= 3
-  if (s >= 0) sig <<= s;
-  else if (s > -62) sig = (sig + (1LL << (-s - 1))) >> (-s);
-  else sig = 0;
-  return bits < 0 ? -sig : sig;
-}
-
-// exact value (H 2^32 + L) 2^e rounded once to FP64
-__device__ __forceinline__ double round_scaled(long long H, long long L, int e) {
-  if (e >= -1022 && e + 32 <= 1023) {
-    const double s = __longlong_as_double((long long)(e + 1023) << 52);
-    const double s32 = __longlong_as_double((long long)(e + 32 + 1023) << 52);
-    return fma((double)H, s32, (double)L * s);
-  }
-  return fma((double)H, scalbn(1.0, e + 32), scalbn((double)L, e));
 }
 
 template <bool MULTI>

@@ -37,8 +37,9 @@ bool build_tables(int Nx, int Ny, int Nz, double Lx, double Lz, double Re, doubl
 // dl, the pivots in column dl, U to the right.
 void band_lu(double* A, int w, int dl, int du, int N);
 
-// base-256 digit tables of the five Legendre bases for the tensor-core
-// reconstruction (recon_tc.cu)
-bool build_recon_tc_tables(const HostTables& h, std::vector<uint32_t>& frag, std::vector<int>& ex);
+// base-256 digit tables of the five Legendre bases and of their weighted
+// transposes for the tensor-core contractions (recon_tc.cu, tc_common.cuh)
+bool build_recon_tc_tables(const HostTables& h, std::vector<uint32_t>& frag, std::vector<int>& ex,
+                           std::vector<uint32_t>& wfrag, std::vector<int>& wex);
 
 }  // namespace chn

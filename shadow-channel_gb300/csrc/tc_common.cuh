@@ -1,0 +1,110 @@
+// Exact FP64 contractions on the bf16 tensor cores (shared by the
+// reconstruction, recon_tc.cu, and the quadratures of the implicit solve,
+// recon_solve.cu).
+//
+// An operand row or column is scaled by a power of two into an integer of 56
+// significant bits and written as seven balanced base-256 digits (the top
+// digit in [-256, 256], the others in [-128, 127]), each exact in bf16.
+// Digit products of level l = i + k accumulate in FP32 through mma.sync
+// m16n8k16; with at most 112 terms per chunk a level's partial sums stay
+// below 2^24, so FP32 holds them exactly.  Levels l < 7 are kept (the rest
+// lie below 2^-56 of the operands' scale), recombined exactly in 64-bit
+// integers and rounded once to FP64.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <cstring>
+#include <vector>
+
+#include "chn_common.cuh"
+
+namespace chn {
+
+static constexpr int kDig = 7;      // base-256 digits per operand
+static constexpr int kChunkKT = 7;  // k-tiles per exact FP32 accumulation chunk (K <= 112)
+
+inline uint16_t bf16_bits_of_int(int d) {
+  const float f = (float)d;  // |d| <= 256: exact in bf16, low 16 bits zero
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return (uint16_t)(u >> 16);
+}
+
+// seven balanced base-256 digits of x (|x| < 2^56), most significant first
+inline void digits56(long long x, int* d) {
+  for (int i = kDig - 1; i >= 1; --i) {
+    const long long lo = ((x + 128) & 255) - 128;
+    d[i] = (int)lo;
+    x = (x - lo) >> 8;
+  }
+  d[0] = (int)x;
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float* d, const uint4& a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
+}
+
+// the seven digits of v * 2^(56 - ex) from the bit pattern (integer ops only);
+// ex bounds the column: |v| < 2^ex
+__device__ __forceinline__ long long scaled56(double v, int ex) {
+  const long long bits = __double_as_longlong(v);
+  const int ef = (int)((bits >> 52) & 0x7FF);
+  if (ef == 0) return 0;  // zero (denormals are below every scale in use)
+  long long sig = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+  const int s = ef - 1019 - ex;  // <= 3
+  if (s >= 0) sig <<= s;
+  else if (s > -62) sig = (sig + (1LL << (-s - 1))) >> (-s);
+  else sig = 0;
+  return bits < 0 ? -sig : sig;
+}
+
+// exact value (H 2^32 + L) 2^e rounded once to FP64
+__device__ __forceinline__ double round_scaled(long long H, long long L, int e) {
+  if (e >= -1022 && e + 32 <= 1023) {
+    const double s = __longlong_as_double((long long)(e + 1023) << 52);
+    const double s32 = __longlong_as_double((long long)(e + 32 + 1023) << 52);
+    return fma((double)H, s32, (double)L * s);
+  }
+  return fma((double)H, scalbn(1.0, e + 32), scalbn((double)L, e));
+}
+
+
+// seven balanced digits of x (|x| < 2^56) as bf16 bit patterns, most significant first
+__device__ __forceinline__ void digits_bf16(long long x, uint16_t* out, size_t stride) {
+  int d[kDig];
+#pragma unroll
+  for (int q = kDig - 1; q >= 1; --q) {
+    const long long lo = ((x + 128) & 255) - 128;
+    d[q] = (int)lo;
+    x = (x - lo) >> 8;
+  }
+  d[0] = (int)x;
+#pragma unroll
+  for (int q = 0; q < kDig; ++q) {
+    const __nv_bfloat16 h = __float2bfloat16_rn((float)d[q]);
+    out[(size_t)q * stride] = *reinterpret_cast<const uint16_t*>(&h);
+  }
+}
+
+// the exact level sums of one mma accumulator element as (H, L): the sum is
+// (H 2^32 + L) 2^(e_row + e_col - 64) for operands scaled to 56-bit integers
+__device__ __forceinline__ void fold_levels(const float (&acc)[kDig][4], int r, long long& H, long long& L) {
+  long long lv[kDig];
+#pragma unroll
+  for (int l = 0; l < kDig; ++l) lv[l] = (long long)__float2int_rn(acc[l][r]);
+  H = (lv[0] << 16) + (lv[1] << 8) + lv[2];
+  L = (lv[3] << 24) + (lv[4] << 16) + (lv[5] << 8) + lv[6];
+}
+
+// host: digit table of a row-major matrix M[rows][K] in mma A-fragment order
+// [MT][KT][7][32 lanes][4] (appended to frag), row exponents appended to ex
+bool append_digit_table(const double* M, int rows, int K, int MT, int KT, std::vector<uint32_t>& frag,
+                        std::vector<int>& ex);
+
+}  // namespace chn

@@ -1,9 +1,11 @@
-"""The reconstruction on the tensor cores (csrc/recon_tc.cu: base-256 digit
-products in bf16 mma with exact FP32 level sums, recombined in 64-bit
-integers and rounded once) against the direct FP64 contraction
-(CHN_RECON_FP64=1, csrc/recon_solve.cu k_recon).
+"""The Legendre contractions on the tensor cores (csrc/tc_common.cuh: base-256
+digit products in bf16 mma with exact FP32 level sums, recombined in 64-bit
+integers and rounded once), in the reconstruction (csrc/recon_tc.cu) and in
+the quadrature right-hand sides of the implicit solve (quad_rhs_tc,
+csrc/recon_solve.cu), against the direct FP64 contractions
+(CHN_RECON_FP64=1 switches both back: k_recon and quad_rhs).
 
-Both evaluate the same five contractions; the digit form is the correctly
+Both evaluate the same contractions; the digit form is the correctly
 rounded value of the 56-bit truncated operands' exact sum, the FP64 form
 accumulates K rounded products.  spec2phys (reconstruction + inverse
 transforms) of one state must agree to 1e-14 of the field scale on every
