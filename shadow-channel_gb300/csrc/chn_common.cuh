@@ -93,6 +93,14 @@ struct Grid {
   const uint32_t* tcW;
   const int* tcWE;
   int tc;
+  // inverse transforms as DFT GEMMs on the tensor cores (phys_tc.cu): the z
+  // stage's matrix [2 pz][2 (Nz - 1)] and the x stage's [px][2X] as digit
+  // tables with row exponents; tci = 0: the FFT kernels
+  const uint32_t* tcZ;
+  const int* tcZE;
+  const uint32_t* tcX;
+  const int* tcXE;
+  int tci;
 };
 
 __host__ __device__ inline size_t coef_size(const Grid& g) { return (size_t)g.Nz * 2 * g.R * g.X; }

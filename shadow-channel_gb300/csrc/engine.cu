@@ -154,6 +154,11 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
     if (!build_recon_tc_tables(h, frag, ex, wfrag, wex) || !T.up(frag, &g.tcA) || !T.up(ex, &g.tcE) ||
         !T.up(wfrag, &g.tcW) || !T.up(wex, &g.tcWE))
       return false;
+    std::vector<uint32_t> zf, xf;
+    std::vector<int> ze, xe;
+    if (!build_phys_tc_tables(h, zf, ze, xf, xe) || !T.up(zf, &g.tcZ) || !T.up(ze, &g.tcZE) || !T.up(xf, &g.tcX) ||
+        !T.up(xe, &g.tcXE))
+      return false;
   }
   // transforms: one block per plane where the plane fits the shared memory,
   // else separate z / x passes (CHN_SPLIT_TRANSFORMS=1 forces them)
@@ -173,6 +178,9 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   // reconstruction and quadratures on the tensor cores unless CHN_RECON_FP64=1 (or it does not fit)
   const char* fp64 = getenv("CHN_RECON_FP64");
   g.tc = (!(fp64 && fp64[0] == '1') && recon_tc_smem_bytes(g) + 4096 <= (size_t)optin) ? 1 : 0;
+  // inverse transforms on the tensor cores unless CHN_TRANSFORMS_FP64=1 (or they do not fit)
+  const char* tfp64 = getenv("CHN_TRANSFORMS_FP64");
+  g.tci = (!(tfp64 && tfp64[0] == '1') && phys_tc_fits(g, optin)) ? 1 : 0;
   if (solve_smem_bytes(g) > (size_t)optin || recon_smem_bytes(g) > (size_t)optin) {
     set_error(1, "grid %dx%dx%d: the implicit solve needs %zu bytes of shared memory per block, the device has %d",
               Nx, Ny, Nz, solve_smem_bytes(g), optin);
@@ -1945,12 +1953,15 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
     gmax.D = std::max(gmax.D, g.D); gmax.pz = std::max(gmax.pz, g.pz); gmax.px = std::max(gmax.px, g.px);
     gmax.Qh = std::max(gmax.Qh, g.Qh);
     gmax.general = std::max(gmax.general, g.general);
+    gmax.tc = std::min(gmax.tc, g.tc);
+    gmax.tci = std::min(gmax.tci, g.tci);
   }
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const char* force = getenv("CHN_SPLIT_TRANSFORMS");
   gmax.split = (!fused_transforms_fit(gmax, optin) || (force && force[0] == '1')) ? 1 : 0;
+  if (!phys_tc_fits(gmax, optin)) gmax.tci = 0;
   if (solve_smem_bytes(gmax) > (size_t)optin) {
     set_error(1, "c_multi_init: the largest grid needs more shared memory than the device has");
     c_multi_destroy();
@@ -1960,6 +1971,8 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
   for (int i = 0; i < n; ++i) {
     gs[i] = m->tabs[i].g;
     gs[i].split = gmax.split;
+    gs[i].tc = gmax.tc;
+    gs[i].tci = gmax.tci;
   }
   if (cudaMalloc(&m->gdev, sizeof(Grid) * n) != cudaSuccess ||
       cudaMemcpy(m->gdev, gs.data(), sizeof(Grid) * n, cudaMemcpyHostToDevice) != cudaSuccess) {

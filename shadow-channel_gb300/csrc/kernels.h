@@ -138,6 +138,9 @@ cudaError_t launch_recon(const Grid& g, const ReconArgs& a, cudaStream_t st);
 cudaError_t launch_recon_tc(const Grid& g, const ReconArgs& a, cudaStream_t st);
 size_t recon_tc_smem_bytes(const Grid& g);
 cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t st);
+// the inverse transforms as exact digit GEMMs on the tensor cores (fused, one block per plane)
+cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st);
+bool phys_tc_fits(const Grid& g, int optin);
 cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st);

@@ -349,6 +349,9 @@ static int split_index(const Grid& g) { return (g.tvar >= 0 && g.tvar < kNumSpli
 
 cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
+  // the tensor-core inverse wherever it fits (its results do not depend on
+  // the autotuner's choice among the bit-identical FFT variants)
+  if (g.tci) return launch_phys_inverse_tc(g, a, st);
   if (g.split) return kSplit[split_index(g)].inverse(g, a, st);
   const size_t sm = phys_smem_bytes(g, a.cfl_check != 0);
   CHN_LAUNCH_FUSED(k_phys_inverse, dim3(g.Q, a.ninst), sm, st, g, a);
@@ -374,6 +377,7 @@ cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t s
 void prepare_recon_solve(int optin);
 void prepare_solve_T(int optin);
 void prepare_recon_tc(int optin);
+void prepare_phys_tc(int optin);
 
 // Every kernel may use up to the device's opt-in shared memory per block: the
 // single-grid engine and an uneven batch (sized for its largest grid) share
@@ -398,6 +402,7 @@ void prepare_kernels(const Grid& g) {
   prepare_recon_solve(optin);
   prepare_solve_T(optin);
   prepare_recon_tc(optin);
+  prepare_phys_tc(optin);
 }
 
 }  // namespace chn

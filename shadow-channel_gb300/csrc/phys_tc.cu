@@ -1,0 +1,323 @@
+// The inverse 3/2-padded transforms (channel/pass1.c:42-114,
+// channel/spec2phys.c:39-76) as exact digit GEMMs on the tensor cores.
+//
+// One block per (instance, plane y), two fields per pass:
+//   z stage   Z[m][x] = sum_kz F[kz][x] exp(+2 pi i m zp(kz)/pz) over the
+//             Nz - 1 kept rows: a real GEMM with 2 pz rows (Re, Im of Z),
+//             K = 2 (Nz - 1) (Re, Im of F interleaved), one column per (field, x);
+//   x stage   P[m][xp] = Re Z[m][0] + 2 sum_{0<j<X} Re(Z[m][j] exp(+2 pi i j xp/px))
+//             (the complex-to-real transform; the imaginary part of the
+//             kx = 0 bin is ignored as by c2r): px rows, K = 2X, one column
+//             per (field, m).
+// The DFT matrices hold the FFT's own twiddle doubles; operands are base-256
+// digits with exact FP32 level sums (tc_common.cuh), so each output is the
+// once-rounded value of the sum of the 56-bit operands.  The intermediate Z
+// is rounded to FP64 in shared memory between the stages.  Same outputs,
+// CFL check and status bits as k_phys_inverse.
+#include <cmath>
+#include <vector>
+
+#include "chn_common.cuh"
+#include "kernels.h"
+#include "phys_common.cuh"
+#include "setup.h"
+#include "tc_common.cuh"
+
+namespace chn {
+
+static constexpr int kThreads = 256;
+static constexpr int kFB = 2;  // fields per pass
+
+// ---------------------------------------------------------------------------
+// host tables
+// ---------------------------------------------------------------------------
+
+bool build_phys_tc_tables(const HostTables& h, std::vector<uint32_t>& zfrag, std::vector<int>& zex,
+                          std::vector<uint32_t>& xfrag, std::vector<int>& xex) {
+  const int pz = h.pz, px = h.px, Nz = h.Nz, X = h.X;
+  const int Kz = 2 * (Nz - 1), Kx = 2 * X;
+  std::vector<double> Az((size_t)2 * pz * Kz, 0.0), Ax((size_t)px * Kx, 0.0);
+  for (int m = 0; m < pz; ++m)
+    for (int kk = 0; kk < Nz - 1; ++kk) {
+      const int zp = kk < Nz / 2 ? kk : kk + 1 + Nz / 2;  // padded row of kept kz index kk
+      const int idx = (int)(((long long)m * zp) % pz);
+      const double c = h.twz[2 * idx], s = -h.twz[2 * idx + 1];  // exp(+i theta) = conj(exp(-i theta))
+      Az[(size_t)m * Kz + 2 * kk] = c;
+      Az[(size_t)m * Kz + 2 * kk + 1] = -s;
+      Az[(size_t)(pz + m) * Kz + 2 * kk] = s;
+      Az[(size_t)(pz + m) * Kz + 2 * kk + 1] = c;
+    }
+  for (int xp = 0; xp < px; ++xp) {
+    Ax[(size_t)xp * Kx] = 1.0;
+    for (int j = 1; j < X; ++j) {
+      const int idx = (int)(((long long)j * xp) % px);
+      const double c = h.twx[2 * idx], s = -h.twx[2 * idx + 1];
+      Ax[(size_t)xp * Kx + 2 * j] = 2.0 * c;
+      Ax[(size_t)xp * Kx + 2 * j + 1] = -2.0 * s;
+    }
+  }
+  zfrag.clear(); zex.clear(); xfrag.clear(); xex.clear();
+  return append_digit_table(Az.data(), 2 * pz, Kz, (2 * pz + 15) / 16, (Kz + 15) / 16, zfrag, zex) &&
+         append_digit_table(Ax.data(), px, Kx, (px + 15) / 16, (Kx + 15) / 16, xfrag, xex);
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory plan
+// ---------------------------------------------------------------------------
+
+struct PhysTcDims {
+  int KTz, KTx, MTz, MTx, KSz, KSx, NZ, NX;  // NZ = columns of the z stage, NX = of the x stage
+};
+
+__host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g) {
+  PhysTcDims d;
+  d.KTz = (2 * (g.Nz - 1) + 15) / 16;
+  d.KTx = (2 * g.X + 15) / 16;
+  d.MTz = (2 * g.pz + 15) / 16;
+  d.MTx = (g.px + 15) / 16;
+  d.KSz = d.KTz * 16 + 8;
+  d.KSx = d.KTx * 16 + 8;
+  d.NZ = kFB * g.X;
+  d.NX = kFB * g.pz;
+  return d;
+}
+
+__host__ __device__ inline size_t phys_tc_dbuf_bytes(const Grid& g) {
+  const PhysTcDims d = phys_tc_dims(g);
+  const size_t z = (size_t)kDig * ((d.NZ + 7) / 8 * 8) * d.KSz * 2, x = (size_t)kDig * ((d.NX + 7) / 8 * 8) * d.KSx * 2;
+  return (z > x ? z : x + 0);
+}
+
+size_t phys_tc_smem_bytes(const Grid& g, bool with_cfl) {
+  const PhysTcDims d = phys_tc_dims(g);
+  size_t b = 0;
+  b += (size_t)((d.NZ + 3) / 4 * 4) * sizeof(int);            // z-stage column exponents
+  b += (size_t)((d.NX + 3) / 4 * 4) * sizeof(int);            // x-stage column exponents
+  b += (phys_tc_dbuf_bytes(g) + 15) / 16 * 16;                 // digits (z, then x)
+  b += (size_t)kFB * g.pz * g.X * sizeof(cpx);                 // Z intermediate
+  (void)with_cfl;  // the CFL number is read back from the written fields
+  return b;
+}
+
+// ---------------------------------------------------------------------------
+// kernel
+// ---------------------------------------------------------------------------
+
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads, 2) k_phys_inverse_tc(const __grid_constant__ Grid g0, PhysArgs a) {
+  const int inst = blockIdx.y, y = blockIdx.x;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
+  if (y >= g.Q) return;
+  if (a.skip_blocked && blocked(a.status, a.sdiv, inst)) return;
+  const PhysTcDims d = phys_tc_dims(g);
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned char* p = smem;
+  int* exz = reinterpret_cast<int*>(p); p += (size_t)((d.NZ + 3) / 4 * 4) * sizeof(int);
+  int* exx = reinterpret_cast<int*>(p); p += (size_t)((d.NX + 3) / 4 * 4) * sizeof(int);
+  uint16_t* dig = reinterpret_cast<uint16_t*>(p); p += (phys_tc_dbuf_bytes(g) + 15) / 16 * 16;
+  cpx* Zb = reinterpret_cast<cpx*>(p);  // [fl][m][x]
+
+  const cpx* __restrict__ U = a.U.at(inst);
+  double* __restrict__ P = a.P.at(inst);
+  if (a.pslot.stride) P += (long long)a.pslot.slot() * a.pslot.stride;
+  const size_t plane = (size_t)g.pz * g.px;
+  const uint4* __restrict__ Az = reinterpret_cast<const uint4*>(g.tcZ);
+  const uint4* __restrict__ Ax = reinterpret_cast<const uint4*>(g.tcX);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
+  const int nwarp = blockDim.x >> 5;
+  const int Kk = g.Nz - 1;  // kept kz rows
+  bool nonfinite = false;
+  for (int f0 = 0; f0 < a.nfields; f0 += kFB) {
+    const int nfb = min(kFB, a.nfields - f0);
+    // ---- z stage: columns n = fl * X + x, K = 2 Kk (Re, Im interleaved)
+    for (int i = threadIdx.x; i < d.NZ; i += blockDim.x) exz[i] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nfb * g.X * Kk; i += blockDim.x) {
+      const int n = i / Kk, kk = i - n * Kk, fl = n / g.X, x = n - fl * g.X;
+      const int z = kk < g.Nz / 2 ? kk : kk + 1;
+      const cpx v = field_value(g, U, f0 + fl, z, y, x);
+      const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
+                        (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
+      if (e) atomicMax(&exz[n], e);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < d.NZ * d.KTz * 8; i += blockDim.x) {
+      const int n = i / (d.KTz * 8), kk = i - n * (d.KTz * 8), fl = n / g.X, x = n - fl * g.X;
+      cpx v = {0.0, 0.0};
+      if (kk < Kk && fl < nfb) v = field_value(g, U, f0 + fl, kk < g.Nz / 2 ? kk : kk + 1, y, x);
+      const int ex = exz[n] - 1022;
+      digits_bf16(scaled56(v.re, ex), dig + (size_t)n * d.KSz + 2 * kk, (size_t)((d.NZ + 7) / 8 * 8) * d.KSz);
+      digits_bf16(scaled56(v.im, ex), dig + (size_t)n * d.KSz + 2 * kk + 1, (size_t)((d.NZ + 7) / 8 * 8) * d.KSz);
+    }
+    __syncthreads();
+    {
+      const int NT = (nfb * g.X + 7) / 8;
+      const size_t dstride = (size_t)((d.NZ + 7) / 8 * 8) * d.KSz;  // bf16 between digits
+      for (int item = warp; item < d.MTz * NT; item += nwarp) {
+        const int mt = item / NT, nt = item - mt * NT;
+        const int n = nt * 8 + gq;
+        float acc[kDig][4];
+        double part[4] = {0.0, 0.0, 0.0, 0.0};
+        long long H[4], L[4];
+        for (int kc = 0; kc < d.KTz; kc += kChunkKT) {
+#pragma unroll
+          for (int l = 0; l < kDig; ++l)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+          const int kend = min(d.KTz, kc + kChunkKT);
+          for (int kt = kc; kt < kend; ++kt) {
+            const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * d.KSz + kt * 16);
+#pragma unroll
+            for (int i = 0; i < kDig; ++i) {
+              const uint4 af = __ldg(&Az[(((size_t)mt * d.KTz + kt) * kDig + i) * 32 + lane]);
+#pragma unroll
+              for (int k = 0; k < kDig - i; ++k) {
+                const uint32_t* row = brow + (size_t)k * dstride / 2;
+                mma_bf16_16816(acc[i + k], af, row[t], row[t + 4]);
+              }
+            }
+          }
+#pragma unroll
+          for (int r = 0; r < 4; ++r) fold_levels(acc, r, H[r], L[r]);
+          if (kend < d.KTz) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              const int row = min(mt * 16 + gq + 8 * (r >> 1), 2 * g.pz - 1);
+              const int col = min(nt * 8 + 2 * t + (r & 1), d.NZ - 1);
+              part[r] += round_scaled(H[r], L[r], g.tcZE[row] + exz[col] - 1022 - 64);
+            }
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int row = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
+          if (row >= 2 * g.pz || col >= nfb * g.X) continue;
+          double v = round_fast(H[r], L[r], g.tcZE[row] + exz[col] - 1022 - 64);
+          if (d.KTz > kChunkKT) v += part[r];
+          const int fl = col / g.X, x = col - fl * g.X;
+          const int m = row < g.pz ? row : row - g.pz;
+          cpx& zr = Zb[((size_t)fl * g.pz + m) * g.X + x];
+          if (row < g.pz) zr.re = v;
+          else zr.im = v;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- x stage: columns n = fl * pz + m, K = 2X (Re, Im of Z[m][j]; Im of j = 0 unused)
+    for (int i = threadIdx.x; i < d.NX; i += blockDim.x) exx[i] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nfb * g.pz * g.X; i += blockDim.x) {
+      const int n = i / g.X, j = i - n * g.X;
+      const cpx v = Zb[(size_t)n * g.X + j];
+      const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
+                        j ? (int)((__double_as_longlong(v.im) >> 52) & 0x7FF) : 0);
+      if (e) atomicMax(&exx[n], e);
+    }
+    __syncthreads();
+    const size_t xstride = (size_t)((d.NX + 7) / 8 * 8) * d.KSx;
+    for (int i = threadIdx.x; i < d.NX * d.KTx * 8; i += blockDim.x) {
+      const int n = i / (d.KTx * 8), j = i - n * (d.KTx * 8);
+      cpx v = {0.0, 0.0};
+      if (j < g.X && n < nfb * g.pz) v = Zb[(size_t)n * g.X + j];
+      if (j == 0) v.im = 0.0;
+      const int ex = exx[n] - 1022;
+      digits_bf16(scaled56(v.re, ex), dig + (size_t)n * d.KSx + 2 * j, xstride);
+      digits_bf16(scaled56(v.im, ex), dig + (size_t)n * d.KSx + 2 * j + 1, xstride);
+    }
+    __syncthreads();
+    {
+      const int NT = (nfb * g.pz + 7) / 8;
+      for (int item = warp; item < d.MTx * NT; item += nwarp) {
+        const int mt = item / NT, nt = item - mt * NT;
+        const int n = nt * 8 + gq;
+        float acc[kDig][4];
+        double part[4] = {0.0, 0.0, 0.0, 0.0};
+        long long H[4], L[4];
+        for (int kc = 0; kc < d.KTx; kc += kChunkKT) {
+#pragma unroll
+          for (int l = 0; l < kDig; ++l)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+          const int kend = min(d.KTx, kc + kChunkKT);
+          for (int kt = kc; kt < kend; ++kt) {
+            const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * d.KSx + kt * 16);
+#pragma unroll
+            for (int i = 0; i < kDig; ++i) {
+              const uint4 af = __ldg(&Ax[(((size_t)mt * d.KTx + kt) * kDig + i) * 32 + lane]);
+#pragma unroll
+              for (int k = 0; k < kDig - i; ++k) {
+                const uint32_t* row = brow + (size_t)k * xstride / 2;
+                mma_bf16_16816(acc[i + k], af, row[t], row[t + 4]);
+              }
+            }
+          }
+#pragma unroll
+          for (int r = 0; r < 4; ++r) fold_levels(acc, r, H[r], L[r]);
+          if (kend < d.KTx) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              const int row = min(mt * 16 + gq + 8 * (r >> 1), g.px - 1);
+              const int col = min(nt * 8 + 2 * t + (r & 1), d.NX - 1);
+              part[r] += round_scaled(H[r], L[r], g.tcXE[row] + exx[col] - 1022 - 64);
+            }
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int xp = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
+          if (xp >= g.px || col >= nfb * g.pz) continue;
+          double v = round_fast(H[r], L[r], g.tcXE[xp] + exx[col] - 1022 - 64);
+          if (d.KTx > kChunkKT) v += part[r];
+          const int fl = col / g.pz, m = col - fl * g.pz, f = f0 + fl;
+          P[((size_t)f * g.Q + y) * plane + (size_t)m * g.px + xp] = v;
+          nonfinite |= !finite_bits(v);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (nonfinite && a.status) atomicOr(&a.status[inst / a.sdiv], ST_NONFINITE);
+  if (a.cfl_check) {
+    // block max of the CFL field (channel/pass1.c:116-138), from the written
+    // velocity fields (this block's own stores)
+    __shared__ double red[kThreads];
+    double mx = 0.0;
+    const double* Pu = P + (size_t)y * plane;
+    const size_t fs = (size_t)g.Q * plane;
+    const double c2 = g.cfl2[y];
+    for (int i = threadIdx.x; i < g.pz * g.px; i += blockDim.x)
+      mx = fmax(mx, fabs(Pu[i]) * g.cfl1 + fabs(Pu[fs + i]) * c2 + fabs(Pu[2 * fs + i]) * g.cfl3);
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const double c = red[0] * g.dt;
+      if (a.cflmax)
+        atomicMax(reinterpret_cast<unsigned long long*>(&a.cflmax[inst / a.sdiv]),
+                  (unsigned long long)__double_as_longlong(c));
+      if (c >= 2.8) atomicOr(&a.status[inst / a.sdiv], ST_CFL);
+    }
+  }
+}
+
+bool phys_tc_fits(const Grid& g, int optin) {
+  // the kernel's static shared memory (reduction, staged grid) is below 4 KB
+  return phys_tc_smem_bytes(g, true) + 4096 <= (size_t)optin;
+}
+
+cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st) {
+  const size_t sm = phys_tc_smem_bytes(g, a.cfl_check != 0);
+  if (a.grids) k_phys_inverse_tc<true><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
+  else k_phys_inverse_tc<false><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
+  return cudaGetLastError();
+}
+
+void prepare_phys_tc(int optin) {
+  allow_max_smem(k_phys_inverse_tc<false>, optin);
+  allow_max_smem(k_phys_inverse_tc<true>, optin);
+}
+
+}  // namespace chn

@@ -234,8 +234,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
         const int y = mt * 16 + gq + 8 * rr;
         if (y >= g.Q || col >= nx || (meancol && col == 0)) continue;
         const int e = g.tcE[(size_t)b * g.Q + y] + ecol - 64;
-        const cpx val = {part[2 * rr] + round_scaled(H[2 * rr], L[2 * rr], e),
-                         part[2 * rr + 1] + round_scaled(H[2 * rr + 1], L[2 * rr + 1], e)};
+        cpx val = {round_fast(H[2 * rr], L[2 * rr], e), round_fast(H[2 * rr + 1], L[2 * rr + 1], e)};
+        if (KTb > kChunkKT) {
+          val.re += part[2 * rr];
+          val.im += part[2 * rr + 1];
+        }
         const int x = x0 + col;
         cpx* out = U + ((size_t)z * 5 * g.Q + y) * g.X + x;
         const double ax = g.kxK2[(size_t)z * g.X + x], az = g.kzK2[(size_t)z * g.X + x];

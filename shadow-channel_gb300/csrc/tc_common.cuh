@@ -75,6 +75,30 @@ __device__ __forceinline__ double round_scaled(long long H, long long L, int e) 
 }
 
 
+// (H 2^32 + L) 2^e with one FP64 conversion: the sum is folded into one
+// int64 keeping at least 62 significant bits (|H| < 2^41, |L| < 2^50), the
+// conversion rounds it, and the power of two goes into the exponent field
+// with integer arithmetic.  Faithful (the folded-away low bits lie more
+// than 8 bits below the result's last place); the FP64 pipe sees one
+// conversion per value.
+__device__ __forceinline__ double round_fast(long long H, long long L, int e) {
+  const unsigned long long aH = (unsigned long long)(H < 0 ? -H : H);
+  const int sh = max(0, 34 - __clzll((long long)aH));  // |T| < 2^63
+  const long long T = (long long)((unsigned long long)H << (32 - sh)) + (L >> sh);
+  if (T == 0) return 0.0;
+  const double v = (double)T;
+  const long long bits = __double_as_longlong(v);
+  const int es = e + sh;
+  const int ex = (int)((bits >> 52) & 0x7FF) + es;
+  if (ex > 0 && ex < 2047) return __longlong_as_double(bits + ((long long)es << 52));
+  return scalbn(v, es);
+}
+
+// x is neither infinite nor NaN (integer test on the exponent field)
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7FF) != 0x7FF;
+}
+
 // seven balanced digits of x (|x| < 2^56) as bf16 bit patterns, most significant first
 __device__ __forceinline__ void digits_bf16(long long x, uint16_t* out, size_t stride) {
   int d[kDig];

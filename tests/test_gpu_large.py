@@ -1,11 +1,13 @@
 """Grids whose padded planes exceed one block's shared memory run their 2D
 transforms as separate z and x passes (csrc/phys.cu, split transforms).
 
-- The split passes are the fused kernels' 1D transforms on the same data, so
-  forcing them (CHN_SPLIT_TRANSFORMS=1, each block-size / chunk variant the
-  autotuner chooses from) at 32x65x32 must reproduce the fused results bit
-  for bit through primal, tangents, the coupled adjoint and the exact
-  adjoint.
+- The split passes are the fused FFT kernels' 1D transforms on the same
+  data, so forcing them (CHN_SPLIT_TRANSFORMS=1, each block-size / chunk
+  variant the autotuner chooses from) at 32x65x32 must reproduce the fused
+  FFT results bit for bit through primal, tangents, the coupled adjoint and
+  the exact adjoint (CHN_TRANSFORMS_FP64=1 keeps the inverse on the FFT
+  kernels in both runs; the tensor-core inverse is compared with them in
+  test_gpu_recon_tc.py).
 - 48x97x48 (113 KB per plane) and 128x129x128 (no plane fits a block:
   split transforms) against the oracle, one step each way, and the exact
   adjoint's dot-product identity.
@@ -70,7 +72,8 @@ print(json.dumps({k: v.view(np.float64).ravel().tolist() for k, v in
     root = O.HERE.parent
     outs = []
     for split in ("0", "1"):
-        env = dict(os.environ, CHN_SPLIT_TRANSFORMS=split, CHN_SPLIT_VARIANT=str(variant), CHN_AUTOTUNE="0")
+        env = dict(os.environ, CHN_SPLIT_TRANSFORMS=split, CHN_SPLIT_VARIANT=str(variant), CHN_AUTOTUNE="0",
+                   CHN_TRANSFORMS_FP64="1")
         r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True, text=True,
                            timeout=600)
         assert r.returncode == 0, r.stderr[-2000:]

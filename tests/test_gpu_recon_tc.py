@@ -1,9 +1,10 @@
-"""The Legendre contractions on the tensor cores (csrc/tc_common.cuh: base-256
-digit products in bf16 mma with exact FP32 level sums, recombined in 64-bit
-integers and rounded once), in the reconstruction (csrc/recon_tc.cu) and in
-the quadrature right-hand sides of the implicit solve (quad_rhs_tc,
-csrc/recon_solve.cu), against the direct FP64 contractions
-(CHN_RECON_FP64=1 switches both back: k_recon and quad_rhs).
+"""The contractions on the tensor cores (csrc/tc_common.cuh: base-256 digit
+products in bf16 mma with exact FP32 level sums, recombined in 64-bit
+integers and rounded once) -- the reconstruction (csrc/recon_tc.cu), the
+quadrature right-hand sides of the implicit solve (quad_rhs_tc,
+csrc/recon_solve.cu) and the inverse transforms as DFT GEMMs
+(csrc/phys_tc.cu) -- against the FP64 kernels (CHN_RECON_FP64=1 and
+CHN_TRANSFORMS_FP64=1 switch them back: k_recon, quad_rhs, the FFTs).
 
 Both evaluate the same contractions; the digit form is the correctly
 rounded value of the 56-bit truncated operands' exact sum, the FP64 form
@@ -60,7 +61,7 @@ def test_tensor_core_reconstruction_matches_fp64(grid):
     root = O.HERE.parent
     outs = []
     for fp64 in ("0", "1"):
-        env = dict(os.environ, CHN_RECON_FP64=fp64)
+        env = dict(os.environ, CHN_RECON_FP64=fp64, CHN_TRANSFORMS_FP64=fp64)
         r = subprocess.run([sys.executable, "-c", CODE, *map(str, grid)], cwd=root, env=env, capture_output=True,
                            text=True, timeout=600)
         assert r.returncode == 0, r.stderr[-2000:]
@@ -70,7 +71,10 @@ def test_tensor_core_reconstruction_matches_fp64(grid):
     scale = np.abs(ref["flow"]).max()
     assert np.abs(tc["flow"] - ref["flow"]).max() <= 1e-14 * scale
     n = grid[3]
-    tol_step = 2e-11 if grid[0] >= 32 else 5e-12
-    assert rel(tc["C"], ref["C"]) <= tol_step * n
-    assert rel(tc["IC"], ref["IC"]) <= 1e-11 * n
-    assert rel(tc["AC"], ref["AC"]) <= 3e-11 * n
+    # per-step tolerances: those of test_gpu_parity.py, and at 48x97x48 the
+    # one-step FMA/no-FMA floors of test_gpu_large.py (3.2e-11, 1.7e-10,
+    # 8.8e-11, held at twice that)
+    tp, tt, ta = (7e-11, 4e-10, 2e-10) if grid[0] >= 48 else ((2e-11 if grid[0] >= 32 else 5e-12), 1e-11, 3e-11)
+    assert rel(tc["C"], ref["C"]) <= tp * n
+    assert rel(tc["IC"], ref["IC"]) <= tt * n
+    assert rel(tc["AC"], ref["AC"]) <= ta * n
