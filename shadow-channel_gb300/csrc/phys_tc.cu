@@ -11,8 +11,8 @@
 //             per (field, m).
 // The DFT matrices hold the FFT's own twiddle doubles; operands are base-256
 // digits with exact FP32 level sums (tc_common.cuh), so each output is the
-// once-rounded value of the sum of the 56-bit operands.  The intermediate Z
-// is rounded to FP64 in shared memory between the stages.  Same outputs,
+// (faithfully) rounded value of the exact sum of the 56-bit operands.  The
+// intermediate Z is rounded to FP64 in shared memory between the stages.  Same outputs,
 // CFL check and status bits as k_phys_inverse.
 #include <cmath>
 #include <vector>
@@ -132,22 +132,29 @@ __global__ void __launch_bounds__(kThreads, 2) k_phys_inverse_tc(const __grid_co
     // ---- z stage: columns n = fl * X + x, K = 2 Kk (Re, Im interleaved)
     for (int i = threadIdx.x; i < d.NZ; i += blockDim.x) exz[i] = 0;
     __syncthreads();
+    // the inputs are staged in the Z buffer (free until the z stage writes it:
+    // X (Nz - 1) <= pz X values per field)
+    cpx* Fin = Zb;  // [n][kk]
     for (int i = threadIdx.x; i < nfb * g.X * Kk; i += blockDim.x) {
       const int n = i / Kk, kk = i - n * Kk, fl = n / g.X, x = n - fl * g.X;
       const int z = kk < g.Nz / 2 ? kk : kk + 1;
       const cpx v = field_value(g, U, f0 + fl, z, y, x);
+      Fin[i] = v;
       const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
                         (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
       if (e) atomicMax(&exz[n], e);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < d.NZ * d.KTz * 8; i += blockDim.x) {
-      const int n = i / (d.KTz * 8), kk = i - n * (d.KTz * 8), fl = n / g.X, x = n - fl * g.X;
-      cpx v = {0.0, 0.0};
-      if (kk < Kk && fl < nfb) v = field_value(g, U, f0 + fl, kk < g.Nz / 2 ? kk : kk + 1, y, x);
-      const int ex = exz[n] - 1022;
-      digits_bf16(scaled56(v.re, ex), dig + (size_t)n * d.KSz + 2 * kk, (size_t)((d.NZ + 7) / 8 * 8) * d.KSz);
-      digits_bf16(scaled56(v.im, ex), dig + (size_t)n * d.KSz + 2 * kk + 1, (size_t)((d.NZ + 7) / 8 * 8) * d.KSz);
+    {
+      const size_t zstride = (size_t)((d.NZ + 7) / 8 * 8) * d.KSz / 2;  // words between digits
+      uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
+      for (int i = threadIdx.x; i < d.NZ * d.KTz * 8; i += blockDim.x) {
+        const int n = i / (d.KTz * 8), kk = i - n * (d.KTz * 8);
+        cpx v = {0.0, 0.0};
+        if (kk < Kk && n < nfb * g.X) v = Fin[n * Kk + kk];
+        const int ex = exz[n] - 1022;
+        digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSz) / 2 + kk, zstride);
+      }
     }
     __syncthreads();
     {
@@ -167,14 +174,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_phys_inverse_tc(const __grid_co
           const int kend = min(d.KTz, kc + kChunkKT);
           for (int kt = kc; kt < kend; ++kt) {
             const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * d.KSz + kt * 16);
+            uint32_t b0[kDig], b1[kDig];
+#pragma unroll
+            for (int k = 0; k < kDig; ++k) {
+              b0[k] = brow[(size_t)k * dstride / 2 + t];
+              b1[k] = brow[(size_t)k * dstride / 2 + t + 4];
+            }
 #pragma unroll
             for (int i = 0; i < kDig; ++i) {
               const uint4 af = __ldg(&Az[(((size_t)mt * d.KTz + kt) * kDig + i) * 32 + lane]);
 #pragma unroll
-              for (int k = 0; k < kDig - i; ++k) {
-                const uint32_t* row = brow + (size_t)k * dstride / 2;
-                mma_bf16_16816(acc[i + k], af, row[t], row[t + 4]);
-              }
+              for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
             }
           }
 #pragma unroll
@@ -215,14 +225,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_phys_inverse_tc(const __grid_co
     }
     __syncthreads();
     const size_t xstride = (size_t)((d.NX + 7) / 8 * 8) * d.KSx;
-    for (int i = threadIdx.x; i < d.NX * d.KTx * 8; i += blockDim.x) {
-      const int n = i / (d.KTx * 8), j = i - n * (d.KTx * 8);
-      cpx v = {0.0, 0.0};
-      if (j < g.X && n < nfb * g.pz) v = Zb[(size_t)n * g.X + j];
-      if (j == 0) v.im = 0.0;
-      const int ex = exx[n] - 1022;
-      digits_bf16(scaled56(v.re, ex), dig + (size_t)n * d.KSx + 2 * j, xstride);
-      digits_bf16(scaled56(v.im, ex), dig + (size_t)n * d.KSx + 2 * j + 1, xstride);
+    {
+      uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
+      for (int i = threadIdx.x; i < d.NX * d.KTx * 8; i += blockDim.x) {
+        const int n = i / (d.KTx * 8), j = i - n * (d.KTx * 8);
+        cpx v = {0.0, 0.0};
+        if (j < g.X && n < nfb * g.pz) v = Zb[(size_t)n * g.X + j];
+        if (j == 0) v.im = 0.0;
+        const int ex = exx[n] - 1022;
+        digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSx) / 2 + j, xstride / 2);
+      }
     }
     __syncthreads();
     {
@@ -241,14 +253,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_phys_inverse_tc(const __grid_co
           const int kend = min(d.KTx, kc + kChunkKT);
           for (int kt = kc; kt < kend; ++kt) {
             const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * d.KSx + kt * 16);
+            uint32_t b0[kDig], b1[kDig];
+#pragma unroll
+            for (int k = 0; k < kDig; ++k) {
+              b0[k] = brow[(size_t)k * xstride / 2 + t];
+              b1[k] = brow[(size_t)k * xstride / 2 + t + 4];
+            }
 #pragma unroll
             for (int i = 0; i < kDig; ++i) {
               const uint4 af = __ldg(&Ax[(((size_t)mt * d.KTx + kt) * kDig + i) * 32 + lane]);
 #pragma unroll
-              for (int k = 0; k < kDig - i; ++k) {
-                const uint32_t* row = brow + (size_t)k * xstride / 2;
-                mma_bf16_16816(acc[i + k], af, row[t], row[t + 4]);
-              }
+              for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
             }
           }
 #pragma unroll

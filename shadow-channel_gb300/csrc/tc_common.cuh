@@ -116,6 +116,25 @@ __device__ __forceinline__ void digits_bf16(long long x, uint16_t* out, size_t s
   }
 }
 
+// the balanced digits of two values (re, im) packed per digit into one 32-bit
+// word (re in the low half): out[q * stride] for q = 0..6
+__device__ __forceinline__ void digits_pair_bf16(long long xr, long long xi, uint32_t* out, size_t stride) {
+  int dr[kDig], di[kDig];
+#pragma unroll
+  for (int q = kDig - 1; q >= 1; --q) {
+    const long long lr = ((xr + 128) & 255) - 128, li = ((xi + 128) & 255) - 128;
+    dr[q] = (int)lr;
+    di[q] = (int)li;
+    xr = (xr - lr) >> 8;
+    xi = (xi - li) >> 8;
+  }
+  dr[0] = (int)xr;
+  di[0] = (int)xi;
+#pragma unroll
+  for (int q = 0; q < kDig; ++q)  // |d| <= 256: the float's upper half is the exact bf16
+    out[(size_t)q * stride] = (__float_as_uint((float)dr[q]) >> 16) | (__float_as_uint((float)di[q]) & 0xFFFF0000u);
+}
+
 // the exact level sums of one mma accumulator element as (H, L): the sum is
 // (H 2^32 + L) 2^(e_row + e_col - 64) for operands scaled to 56-bit integers
 __device__ __forceinline__ void fold_levels(const float (&acc)[kDig][4], int r, long long& H, long long& L) {
