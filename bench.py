@@ -170,9 +170,29 @@ def segment_step_flops(g):
     return 3 * ((1 + NTAN) * (quad + 9 * Q * plane) + (1.5 * quad + 15 * Q * plane))
 
 
-# ncu DRAM bytes (read + write) of one k_phys_inverse instance: a 24-instance
-# launch at 32x65x32 moved 427.1 MB (147.9 read + 279.2 write); traffic grows with the instance count
-PHYS_TRAFFIC_PER_INSTANCE_32 = 427.1e6 / 24
+# ncu DRAM bytes (read + write) of one k_phys_inverse_tc instance: a 24-instance
+# launch at 32x65x32 moved 301.2 MB (92.9 read + 208.3 write); traffic grows with the instance count
+PHYS_TRAFFIC_PER_INSTANCE_32 = 301.2e6 / 24
+
+
+def tc_inverse_mma_flops(ninst, g, nfields=6):
+    """bf16 tensor-core flop of one k_phys_inverse_tc launch: per pair of
+    fields a z-stage GEMM (2 pz x 2 (Nz-1) x 2X) and an x-stage GEMM
+    (px x 2X x 2 pz) in m16n8k16 tiles, each tile 28 digit-pair MMAs."""
+    X, Nz = g["Nx"] // 2, g["Nz"]
+    pz, px, Q = 3 * Nz // 2, 3 * g["Nx"] // 2, 3 * g["Ny"] // 2
+    t = lambda n, d: (n + d - 1) // d
+    per_pair = 28 * (t(2 * pz, 16) * t(2 * X, 8) * t(2 * (Nz - 1), 16) + t(px, 16) * t(2 * pz, 8) * t(2 * X, 16))
+    return ninst * Q * t(nfields, 2) * per_pair * 4096.0
+
+
+def measured_bf16_peak():
+    """bf16 dense TFLOP/s measured on the GB300s (MEASURED_PEAKS.json), else the fallback"""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured (MEASURED_PEAKS.json, cuBLAS bf16 burst)"
+    except Exception:
+        return 1900.0, "fallback 1.9 PFLOP/s"
 
 
 def recon_flops(ninst, g):
@@ -282,16 +302,24 @@ def run_gb300(a):
     dom_ms = k_ms["phys_inverse"]
     flops = phys_inverse_flops(nt, GRID)
     achieved = flops / (dom_ms * 1e-3) / 1e12
+    tc_flops = tc_inverse_mma_flops(nt, GRID)
+    bf16_peak, bf16_src = measured_bf16_peak()
     traffic = PHYS_TRAFFIC_PER_INSTANCE_32 * nt if (GRID["Nx"], GRID["Ny"], GRID["Nz"]) == (32, 65, 32) else None
     step_flop = segment_step_flops(GRID)
     autotune = json.loads(cc.lib.c_autotune_report().decode() or "{}")
-    roofline = {"bound": "fp64", "kernel": f"k_phys_inverse ({nt} tangent fields)", "achieved": achieved,
+    roofline = {"bound": "fp64", "kernel": f"k_phys_inverse_tc ({nt} tangent fields)", "achieved": achieved,
                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                 "traffic_unit": "bytes per launch",
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 24-instance "
                                   "launch, scaled by the instance count",
                 "peak_source": "measured: FP64 FMA probe in this run (c_fp64_peak_tflops)",
                 "algorithmic_flop_per_launch": flops, "kernel_ms": k_ms,
+                "note": "k_phys_inverse runs as exact digit GEMMs on the tensor cores (k_phys_inverse_tc); "
+                        "achieved counts the FFT's nominal FP64 flop it replaces (FP64-equivalent)",
+                "tensor": {"achieved": tc_flops / (dom_ms * 1e-3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                           "frac": tc_flops / (dom_ms * 1e-3) / 1e12 / bf16_peak, "peak_source": bf16_src,
+                           "mma_flop_per_launch": tc_flops,
+                           "what": "bf16 m16n8k16 digit-product flop of the launch (28 digit pairs per tile)"},
                 "recon_tflops": recon_flops(nt, GRID) / (k_ms["recon"] * 1e-3) / 1e12,
                 "step": {"algorithmic_flop_per_segment_step": step_flop,
                          "achieved_tflops": step_flop * value / world / 1e12,
@@ -409,9 +437,10 @@ def autograd_config(C0, nsteps=1000, checkpoint=50):
     time-mean lower-wall shear over `nsteps` steps from the run-up parent
     field, checkpoints every `checkpoint` steps (channel.autograd), with
     dJ/dRe, dJ/dmeanU (exact tangents) and dJ/dC0 (exact adjoint) against
-    central differences: meanU at relative step 1e-6, C0 at 1e-6 |C0| along
-    one seeded direction, Re at relative steps 1e-3 .. 1e-6 (the headline
-    comparison at 1e-3; the sweep shows the rounding-noise floor)."""
+    central differences: meanU at relative step 1e-6; C0 along one seeded
+    direction of norm |C0| and Re at relative steps 1e-3 .. 1e-6 (headline
+    comparisons at 1e-4 and 1e-3; the sweeps show the rounding-noise floor
+    of J in the differences)."""
     import torch
     from channel import autograd as ag
     from channel.synthetic import synthetic_state
@@ -438,8 +467,10 @@ def autograd_config(C0, nsteps=1000, checkpoint=50):
     fdU = (J_of(Re0, U0 + hU, C0) - J_of(Re0, U0 - hU, C0)) / (2 * hU)
     d = synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=77, laminar=False)
     d *= np.linalg.norm(C0) / np.linalg.norm(d)
-    hC = 1e-6
-    fdC = (J_of(Re0, U0, C0 + hC * d) - J_of(Re0, U0, C0 - hC * d)) / (2 * hC)
+    fd_c0 = {}
+    for hC in (1e-3, 1e-4, 1e-5, 1e-6):
+        fd_c0[f"{hC:g}"] = (J_of(Re0, U0, C0 + hC * d) - J_of(Re0, U0, C0 - hC * d)) / (2 * hC)
+    fdC = fd_c0["0.0001"]
     anC = float(np.sum(Ct.grad.numpy() * d.view(np.float64).reshape(Ct.shape)))
     rel = lambda a, b: abs(a - b) / abs(b)
     return {"grid": "32x65x32", "steps": nsteps, "checkpoint_every": checkpoint, "J": float(J.detach()),
@@ -449,10 +480,11 @@ def autograd_config(C0, nsteps=1000, checkpoint=50):
             "rel_err_Re_by_relative_step": {k: rel(float(Re.grad), v) for k, v in fd_re.items()},
             "dJ_dmeanU": float(U.grad), "fd_dJ_dmeanU": fdU, "rel_err_meanU": rel(float(U.grad), fdU),
             "dJ_dC0_dir": anC, "fd_dJ_dC0_dir": fdC, "rel_err_C0": rel(anC, fdC),
+            "rel_err_C0_by_relative_step": {k: rel(anC, v) for k, v in fd_c0.items()},
             "fd_s": time.perf_counter() - t0,
             "note": "backward = 2 exact tangent sweeps + 1 exact-adjoint sweep, each interval recomputed "
-                    "from its checkpoint; central differences: meanU and C0 at relative step 1e-6, Re at 1e-3 "
-                    "(the sweep shows the rounding-noise floor below 1e-4)"}
+                    "from its checkpoint; central differences: meanU at relative step 1e-6, C0 at 1e-4, Re at 1e-3 "
+                    "(the sweeps show the rounding-noise floor at smaller steps)"}
 
 
 def large_grid(cc, nsteps=8):
