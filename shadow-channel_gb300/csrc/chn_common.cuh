@@ -101,6 +101,15 @@ struct Grid {
   const uint32_t* tcX;
   const int* tcXE;
   int tci;
+  // forward transforms likewise (phys_tc.cu, k_products_tc): x stage
+  // [2X][px] (1/(px pz) folded in), z stage [2 (Nz - 1)][2 pz]; tcf = 0: the FFT kernels
+  const uint32_t* tcFX;
+  const int* tcFXE;
+  const uint32_t* tcFXU;  // the x stage without the 1/(px pz) (exact transpose)
+  const int* tcFXUE;
+  const uint32_t* tcFZ;
+  const int* tcFZE;
+  int tcf;
 };
 
 __host__ __device__ inline size_t coef_size(const Grid& g) { return (size_t)g.Nz * 2 * g.R * g.X; }

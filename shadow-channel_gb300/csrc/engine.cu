@@ -159,6 +159,11 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
     if (!build_phys_tc_tables(h, zf, ze, xf, xe) || !T.up(zf, &g.tcZ) || !T.up(ze, &g.tcZE) || !T.up(xf, &g.tcX) ||
         !T.up(xe, &g.tcXE))
       return false;
+    std::vector<uint32_t> fxf, fzf, fuf;
+    std::vector<int> fxe, fze, fue;
+    if (!build_fwd_tc_tables(h, fxf, fxe, fzf, fze, fuf, fue) || !T.up(fxf, &g.tcFX) || !T.up(fxe, &g.tcFXE) ||
+        !T.up(fzf, &g.tcFZ) || !T.up(fze, &g.tcFZE) || !T.up(fuf, &g.tcFXU) || !T.up(fue, &g.tcFXUE))
+      return false;
   }
   // transforms: one block per plane where the plane fits the shared memory,
   // else separate z / x passes (CHN_SPLIT_TRANSFORMS=1 forces them)
@@ -181,6 +186,7 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   // inverse transforms on the tensor cores unless CHN_TRANSFORMS_FP64=1 (or they do not fit)
   const char* tfp64 = getenv("CHN_TRANSFORMS_FP64");
   g.tci = (!(tfp64 && tfp64[0] == '1') && phys_tc_fits(g, optin)) ? 1 : 0;
+  g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_fits(g, optin)) ? 1 : 0;
   if (solve_smem_bytes(g) > (size_t)optin || recon_smem_bytes(g) > (size_t)optin) {
     set_error(1, "grid %dx%dx%d: the implicit solve needs %zu bytes of shared memory per block, the device has %d",
               Nx, Ny, Nz, solve_smem_bytes(g), optin);
@@ -1955,6 +1961,7 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
     gmax.general = std::max(gmax.general, g.general);
     gmax.tc = std::min(gmax.tc, g.tc);
     gmax.tci = std::min(gmax.tci, g.tci);
+    gmax.tcf = std::min(gmax.tcf, g.tcf);
   }
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
@@ -1962,6 +1969,7 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
   const char* force = getenv("CHN_SPLIT_TRANSFORMS");
   gmax.split = (!fused_transforms_fit(gmax, optin) || (force && force[0] == '1')) ? 1 : 0;
   if (!phys_tc_fits(gmax, optin)) gmax.tci = 0;
+  if (!fwd_tc_fits(gmax, optin)) gmax.tcf = 0;
   if (solve_smem_bytes(gmax) > (size_t)optin) {
     set_error(1, "c_multi_init: the largest grid needs more shared memory than the device has");
     c_multi_destroy();
@@ -1973,6 +1981,7 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
     gs[i].split = gmax.split;
     gs[i].tc = gmax.tc;
     gs[i].tci = gmax.tci;
+    gs[i].tcf = gmax.tcf;
   }
   if (cudaMalloc(&m->gdev, sizeof(Grid) * n) != cudaSuccess ||
       cudaMemcpy(m->gdev, gs.data(), sizeof(Grid) * n, cudaMemcpyHostToDevice) != cudaSuccess) {

@@ -141,6 +141,9 @@ cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t s
 // the inverse transforms as exact digit GEMMs on the tensor cores (fused, one block per plane)
 cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st);
 bool phys_tc_fits(const Grid& g, int optin);
+// products + forward transforms as digit GEMMs (mode 0 primal, 1 tangent, 2 adjoint, 3 exact transpose)
+cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st);
+bool fwd_tc_fits(const Grid& g, int optin);
 cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st);

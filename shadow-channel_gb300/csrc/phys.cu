@@ -360,6 +360,7 @@ cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t s
 
 cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
+  if (g.tcf) return launch_products_tc(g, a, a.Pt.base ? 1 : 0, st);
   if (g.split) return kSplit[split_index(g)].products(g, a, a.Pt.base ? 1 : 0, st);
   const size_t sm = phys_smem_bytes(g, false);
   CHN_LAUNCH_FUSED(k_products_fwd, dim3(g.Q, a.ninst), sm, st, g, a);
@@ -368,6 +369,7 @@ cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t s
 
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
+  if (g.tcf) return launch_products_tc(g, a, a.exact ? 3 : 2, st);
   if (g.split) return kSplit[split_index(g)].products(g, a, a.exact ? 3 : 2, st);
   const size_t sm = prod_adj_smem_bytes(g);
   CHN_LAUNCH_FUSED(k_products_adj, dim3(g.Q, a.ninst), sm, st, g, a);

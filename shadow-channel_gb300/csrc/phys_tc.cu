@@ -61,6 +61,43 @@ bool build_phys_tc_tables(const HostTables& h, std::vector<uint32_t>& zfrag, std
          append_digit_table(Ax.data(), px, Kx, (px + 15) / 16, (Kx + 15) / 16, xfrag, xex);
 }
 
+// forward transforms (channel/pass1.c:312-339): x stage Y[zp][kx] =
+// norm sum_xp p[zp][xp] exp(-2 pi i kx xp/px) for kx < X (rows 2kx, 2kx+1 =
+// Re, Im; the 1/(px pz) scaling folded in; the exact transpose's products
+// take an unscaled copy), z stage F[kz][kx] = sum_zp
+// Y[zp][kx] exp(-2 pi i zp(kz) zp/pz) for the Nz - 1 kept rows (rows 2kk,
+// 2kk+1; K = 2 pz with Re, Im of Y interleaved)
+bool build_fwd_tc_tables(const HostTables& h, std::vector<uint32_t>& xfrag, std::vector<int>& xex,
+                         std::vector<uint32_t>& zfrag, std::vector<int>& zex, std::vector<uint32_t>& ufrag,
+                         std::vector<int>& uex) {
+  const int pz = h.pz, px = h.px, Nz = h.Nz, X = h.X, Kk = Nz - 1;
+  const double norm = 1.0 / ((3. * h.Nx / 2.) * (3. * h.Nz / 2.));
+  std::vector<double> Ax((size_t)2 * X * px, 0.0), Au((size_t)2 * X * px, 0.0), Az((size_t)2 * Kk * 2 * pz, 0.0);
+  for (int kx = 0; kx < X; ++kx)
+    for (int xp = 0; xp < px; ++xp) {
+      const int idx = (int)(((long long)kx * xp) % px);
+      Au[(size_t)(2 * kx) * px + xp] = h.twx[2 * idx];           // cos
+      Au[(size_t)(2 * kx + 1) * px + xp] = h.twx[2 * idx + 1];   // -sin
+      Ax[(size_t)(2 * kx) * px + xp] = h.twx[2 * idx] * norm;
+      Ax[(size_t)(2 * kx + 1) * px + xp] = h.twx[2 * idx + 1] * norm;
+    }
+  for (int kk = 0; kk < Kk; ++kk) {
+    const int zo = kk < Nz / 2 ? kk : kk + 1 + Nz / 2;  // padded output row of kept index kk
+    for (int zp = 0; zp < pz; ++zp) {
+      const int idx = (int)(((long long)zo * zp) % pz);
+      const double c = h.twz[2 * idx], ms = h.twz[2 * idx + 1];  // cos, -sin
+      Az[(size_t)(2 * kk) * 2 * pz + 2 * zp] = c;
+      Az[(size_t)(2 * kk) * 2 * pz + 2 * zp + 1] = -ms;
+      Az[(size_t)(2 * kk + 1) * 2 * pz + 2 * zp] = ms;
+      Az[(size_t)(2 * kk + 1) * 2 * pz + 2 * zp + 1] = c;
+    }
+  }
+  xfrag.clear(); xex.clear(); zfrag.clear(); zex.clear(); ufrag.clear(); uex.clear();
+  return append_digit_table(Ax.data(), 2 * X, px, (2 * X + 15) / 16, (px + 15) / 16, xfrag, xex) &&
+         append_digit_table(Au.data(), 2 * X, px, (2 * X + 15) / 16, (px + 15) / 16, ufrag, uex) &&
+         append_digit_table(Az.data(), 2 * Kk, 2 * pz, (2 * Kk + 15) / 16, (2 * pz + 15) / 16, zfrag, zex);
+}
+
 // ---------------------------------------------------------------------------
 // shared-memory plan
 // ---------------------------------------------------------------------------
@@ -318,6 +355,208 @@ __global__ void __launch_bounds__(kThreads, 2) k_phys_inverse_tc(const __grid_co
   }
 }
 
+// ---------------------------------------------------------------------------
+// products + forward transforms
+// ---------------------------------------------------------------------------
+
+struct FwdTcDims {
+  int KTx, KTz, MTx, MTz, KSx, KSz, pzp, Xp, Kk;
+};
+
+__host__ __device__ inline FwdTcDims fwd_tc_dims(const Grid& g) {
+  FwdTcDims d;
+  d.Kk = g.Nz - 1;
+  d.KTx = (g.px + 15) / 16;
+  d.KTz = (2 * g.pz + 15) / 16;
+  d.MTx = (2 * g.X + 15) / 16;
+  d.MTz = (2 * d.Kk + 15) / 16;
+  d.KSx = d.KTx * 16 + 8;
+  d.KSz = d.KTz * 16 + 8;
+  d.pzp = (g.pz + 7) / 8 * 8;
+  d.Xp = (g.X + 7) / 8 * 8;
+  return d;
+}
+
+size_t fwd_tc_smem_bytes(const Grid& g) {
+  const FwdTcDims d = fwd_tc_dims(g);
+  const size_t dx = (size_t)kDig * d.pzp * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
+  const size_t stage = (size_t)g.pz * g.px * sizeof(double), yb = (size_t)g.pz * g.X * sizeof(cpx);
+  size_t b = (size_t)((g.pz + 3) / 4 * 4 + (g.X + 3) / 4 * 4) * sizeof(int);
+  b += ((dx > dz ? dx : dz) + 15) / 16 * 16;
+  b += ((stage > yb ? stage : yb) + 15) / 16 * 16;
+  b += (size_t)d.Kk * g.X * sizeof(cpx);
+  return b;
+}
+
+// one exact digit GEMM tile loop over k-tiles kt0..kt1 of a fixed table A
+// (fragment order [mt][KT][7][32][4]) and smem digits of column n
+__device__ __forceinline__ void tc_tile(const uint4* __restrict__ A, int mt, int KT, const uint16_t* dig, size_t KS,
+                                        size_t dstride, int n, int lane, int t, float (&acc)[kDig][4]) {
+#pragma unroll
+  for (int l = 0; l < kDig; ++l)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+  for (int kt = 0; kt < KT; ++kt) {
+    const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
+    uint32_t b0[kDig], b1[kDig];
+#pragma unroll
+    for (int k = 0; k < kDig; ++k) {
+      b0[k] = brow[(size_t)k * dstride / 2 + t];
+      b1[k] = brow[(size_t)k * dstride / 2 + t + 4];
+    }
+#pragma unroll
+    for (int i = 0; i < kDig; ++i) {
+      const uint4 af = __ldg(&A[(((size_t)mt * KT + kt) * kDig + i) * 32 + lane]);
+#pragma unroll
+      for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
+    }
+  }
+}
+
+// The products of one plane (mode 0 primal, 1 tangent, 2 adjoint S and T,
+// 3 the exact transpose; split_product) and their forward transforms as
+// digit GEMMs, one component at a time; modes 0/1 write H slots 0..2, modes
+// 2/3 fold each component into the output slots (assemble_stage).  Same
+// outputs as k_products_fwd / k_products_adj.  K <= 112 per stage (single
+// FP32 chunk): fwd_tc_fits checks it.
+template <bool MULTI>
+__global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_constant__ Grid g0, ProdArgs a, int mode) {
+  const int inst = blockIdx.y, y = blockIdx.x;
+  CHN_INSTANCE_GRID(g0, a.grids, inst);
+  if (y >= g.Q) return;
+  if (blocked(a.status, a.sdiv, inst)) return;
+  const FwdTcDims d = fwd_tc_dims(g);
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned char* p = smem;
+  int* exx = reinterpret_cast<int*>(p); p += (size_t)((g.pz + 3) / 4 * 4) * sizeof(int);
+  int* exz = reinterpret_cast<int*>(p); p += (size_t)((g.X + 3) / 4 * 4) * sizeof(int);
+  uint16_t* dig = reinterpret_cast<uint16_t*>(p);
+  {
+    const size_t dx = (size_t)kDig * d.pzp * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
+    p += ((dx > dz ? dx : dz) + 15) / 16 * 16;
+  }
+  double* stage = reinterpret_cast<double*>(p);  // [zp][xp] products, then Y [zp][kx] (cpx)
+  cpx* Yb = reinterpret_cast<cpx*>(p);
+  {
+    const size_t st = (size_t)g.pz * g.px * sizeof(double), yb = (size_t)g.pz * g.X * sizeof(cpx);
+    p += ((st > yb ? st : yb) + 15) / 16 * 16;
+  }
+  cpx* Fb = reinterpret_cast<cpx*>(p);  // [kk][kx]
+  const size_t plane = (size_t)g.pz * g.px, fs = (size_t)g.Q * plane;
+  const double* __restrict__ Pp = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane +
+                                  (a.pslot.stride ? (long long)a.pslot.slot() * a.pslot.stride : 0LL);
+  const double* __restrict__ Pt = a.Pt.base ? a.Pt.at(inst) + (size_t)y * plane : nullptr;
+  cpx* __restrict__ H = a.H.at(inst);
+  // the exact transpose's forward transforms carry no 1/(px pz)
+  const uint4* __restrict__ Ax = reinterpret_cast<const uint4*>(mode == 3 ? g.tcFXU : g.tcFX);
+  const int* __restrict__ AxE = mode == 3 ? g.tcFXUE : g.tcFXE;
+  const uint4* __restrict__ Az = reinterpret_cast<const uint4*>(g.tcFZ);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
+  const int nwarp = blockDim.x >> 5;
+  const int ncomp = mode >= 2 ? 6 : 3;
+  const size_t xstride = (size_t)d.pzp * d.KSx, zstride = (size_t)d.Xp * d.KSz;  // bf16 between digits
+  for (int q = 0; q < ncomp; ++q) {
+    // ---- products of component q, row exponents (one column per zp)
+    for (int i = threadIdx.x; i < g.pz; i += blockDim.x) exx[i] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < g.pz * g.px; i += blockDim.x) {
+      const double v = split_product(mode, Pp, Pt, fs, i, q);
+      stage[i] = v;
+      const int e = (int)((__double_as_longlong(v) >> 52) & 0x7FF);
+      if (e) atomicMax(&exx[i / g.px], e);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < d.pzp * (d.KTx * 16); i += blockDim.x) {
+      const int n = i / (d.KTx * 16), k = i - n * (d.KTx * 16);
+      const double v = (n < g.pz && k < g.px) ? stage[(size_t)n * g.px + k] : 0.0;
+      digits_bf16(scaled56(v, exx[min(n, g.pz - 1)] - 1022), dig + (size_t)n * d.KSx + k, xstride);
+    }
+    __syncthreads();
+    // ---- x stage: rows 2kx (+1), columns zp; Y into the staging region
+    {
+      const int NT = d.pzp / 8;
+      for (int item = warp; item < d.MTx * NT; item += nwarp) {
+        const int mt = item / NT, nt = item - mt * NT;
+        float acc[kDig][4];
+        tc_tile(Ax, mt, d.KTx, dig, d.KSx, xstride, nt * 8 + gq, lane, t, acc);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int row = mt * 16 + gq + 8 * (r >> 1), zp = nt * 8 + 2 * t + (r & 1);
+          if (row >= 2 * g.X || zp >= g.pz) continue;
+          long long Hh, Ll;
+          fold_levels(acc, r, Hh, Ll);
+          const double v = round_fast(Hh, Ll, AxE[row] + exx[zp] - 1022 - 64);
+          cpx& yv = Yb[(size_t)zp * g.X + (row >> 1)];
+          if (row & 1) yv.im = v;
+          else yv.re = v;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- z stage inputs: columns kx, K = 2 pz (Re, Im of Y[zp][kx] interleaved)
+    for (int i = threadIdx.x; i < g.X; i += blockDim.x) exz[i] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x) {
+      const cpx v = Yb[i];
+      const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
+                        (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
+      if (e) atomicMax(&exz[i % g.X], e);
+    }
+    __syncthreads();
+    {
+      uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
+      for (int i = threadIdx.x; i < d.Xp * (d.KTz * 8); i += blockDim.x) {
+        const int n = i / (d.KTz * 8), zp = i - n * (d.KTz * 8);
+        const cpx v = (n < g.X && zp < g.pz) ? Yb[(size_t)zp * g.X + n] : cpx{0.0, 0.0};
+        const int ex = exz[min(n, g.X - 1)] - 1022;
+        digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSz) / 2 + zp, zstride / 2);
+      }
+    }
+    __syncthreads();
+    // ---- z stage: rows 2kk (+1), columns kx -> Fb
+    {
+      const int NT = d.Xp / 8;
+      for (int item = warp; item < d.MTz * NT; item += nwarp) {
+        const int mt = item / NT, nt = item - mt * NT;
+        float acc[kDig][4];
+        tc_tile(Az, mt, d.KTz, dig, d.KSz, zstride, nt * 8 + gq, lane, t, acc);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int row = mt * 16 + gq + 8 * (r >> 1), kx = nt * 8 + 2 * t + (r & 1);
+          if (row >= 2 * d.Kk || kx >= g.X) continue;
+          long long Hh, Ll;
+          fold_levels(acc, r, Hh, Ll);
+          const double v = round_fast(Hh, Ll, g.tcFZE[row] + exz[kx] - 1022 - 64);
+          cpx& fv = Fb[(size_t)(row >> 1) * g.X + kx];
+          if (row & 1) fv.im = v;
+          else fv.re = v;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- outputs (the (kk, kx) -> thread map is the same for every q)
+    for (int i = threadIdx.x; i < d.Kk * g.X; i += blockDim.x) {
+      const int kk = i / g.X, x = i - kk * g.X;
+      const int z = kk < g.Nz / 2 ? kk : kk + 1;
+      if (mode < 2) H[(((size_t)z * 5 + q) * g.Q + y) * g.X + x] = Fb[i];
+      else assemble_stage(g, mode == 3, H, z, y, x, q, Fb[i]);
+    }
+    __syncthreads();
+  }
+}
+
+bool fwd_tc_fits(const Grid& g, int optin) {
+  const FwdTcDims d = fwd_tc_dims(g);
+  return d.KTx <= kChunkKT && d.KTz <= kChunkKT && fwd_tc_smem_bytes(g) + 4096 <= (size_t)optin;
+}
+
+cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
+  const size_t sm = fwd_tc_smem_bytes(g);
+  if (a.grids) k_products_tc<true><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a, mode);
+  else k_products_tc<false><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a, mode);
+  return cudaGetLastError();
+}
+
 bool phys_tc_fits(const Grid& g, int optin) {
   // the kernel's static shared memory (reduction, staged grid) is below 4 KB
   return phys_tc_smem_bytes(g, true) + 4096 <= (size_t)optin;
@@ -333,6 +572,8 @@ cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_
 void prepare_phys_tc(int optin) {
   allow_max_smem(k_phys_inverse_tc<false>, optin);
   allow_max_smem(k_phys_inverse_tc<true>, optin);
+  allow_max_smem(k_products_tc<false>, optin);
+  allow_max_smem(k_products_tc<true>, optin);
 }
 
 }  // namespace chn
