@@ -99,16 +99,26 @@ __device__ __forceinline__ bool finite_bits(double x) {
   return ((__double_as_longlong(x) >> 52) & 0x7FF) != 0x7FF;
 }
 
+// Balanced digits without a carry chain: with B = sum_{i<6} 128 * 256^i,
+// x + B = sum_{q>=1} (d_q + 128) 256^(6-q) + d_0 256^6, so every lower digit
+// is an unsigned byte of x + B less 128 and the top digit its arithmetic
+// shift by 48.  Seven independent extractions.
+__device__ __forceinline__ void balanced_digits(long long x, int (&d)[kDig]) {
+  const long long xb = x + 0x808080808080LL;
+  const unsigned lo = (unsigned)xb, hi = (unsigned)(xb >> 32);
+  d[6] = (int)(lo & 255u) - 128;
+  d[5] = (int)((lo >> 8) & 255u) - 128;
+  d[4] = (int)((lo >> 16) & 255u) - 128;
+  d[3] = (int)(lo >> 24) - 128;
+  d[2] = (int)(hi & 255u) - 128;
+  d[1] = (int)((hi >> 8) & 255u) - 128;
+  d[0] = (int)(xb >> 48);
+}
+
 // seven balanced digits of x (|x| < 2^56) as bf16 bit patterns, most significant first
 __device__ __forceinline__ void digits_bf16(long long x, uint16_t* out, size_t stride) {
   int d[kDig];
-#pragma unroll
-  for (int q = kDig - 1; q >= 1; --q) {
-    const long long lo = ((x + 128) & 255) - 128;
-    d[q] = (int)lo;
-    x = (x - lo) >> 8;
-  }
-  d[0] = (int)x;
+  balanced_digits(x, d);
 #pragma unroll
   for (int q = 0; q < kDig; ++q) {
     const __nv_bfloat16 h = __float2bfloat16_rn((float)d[q]);
@@ -120,16 +130,8 @@ __device__ __forceinline__ void digits_bf16(long long x, uint16_t* out, size_t s
 // word (re in the low half): out[q * stride] for q = 0..6
 __device__ __forceinline__ void digits_pair_bf16(long long xr, long long xi, uint32_t* out, size_t stride) {
   int dr[kDig], di[kDig];
-#pragma unroll
-  for (int q = kDig - 1; q >= 1; --q) {
-    const long long lr = ((xr + 128) & 255) - 128, li = ((xi + 128) & 255) - 128;
-    dr[q] = (int)lr;
-    di[q] = (int)li;
-    xr = (xr - lr) >> 8;
-    xi = (xi - li) >> 8;
-  }
-  dr[0] = (int)xr;
-  di[0] = (int)xi;
+  balanced_digits(xr, dr);
+  balanced_digits(xi, di);
 #pragma unroll
   for (int q = 0; q < kDig; ++q)  // |d| <= 256: the float's upper half is the exact bf16
     out[(size_t)q * stride] = (__float_as_uint((float)dr[q]) >> 16) | (__float_as_uint((float)di[q]) & 0xFFFF0000u);
