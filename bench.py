@@ -439,8 +439,8 @@ def autograd_config(C0, nsteps=1000, checkpoint=50):
     dJ/dRe, dJ/dmeanU (exact tangents) and dJ/dC0 (exact adjoint) against
     central differences: meanU at relative step 1e-6; C0 along one seeded
     direction of norm |C0| and Re at relative steps 1e-3 .. 1e-6 (headline
-    comparisons at 1e-4 and 1e-3; the sweeps show the rounding-noise floor
-    of J in the differences)."""
+    comparisons at 1e-5 and 1e-3, where truncation and rounding noise
+    balance; the sweeps show both)."""
     import torch
     from channel import autograd as ag
     from channel.synthetic import synthetic_state
@@ -470,7 +470,7 @@ def autograd_config(C0, nsteps=1000, checkpoint=50):
     fd_c0 = {}
     for hC in (1e-3, 1e-4, 1e-5, 1e-6):
         fd_c0[f"{hC:g}"] = (J_of(Re0, U0, C0 + hC * d) - J_of(Re0, U0, C0 - hC * d)) / (2 * hC)
-    fdC = fd_c0["0.0001"]
+    fdC = fd_c0["1e-05"]
     anC = float(np.sum(Ct.grad.numpy() * d.view(np.float64).reshape(Ct.shape)))
     rel = lambda a, b: abs(a - b) / abs(b)
     return {"grid": "32x65x32", "steps": nsteps, "checkpoint_every": checkpoint, "J": float(J.detach()),
@@ -483,8 +483,8 @@ def autograd_config(C0, nsteps=1000, checkpoint=50):
             "rel_err_C0_by_relative_step": {k: rel(anC, v) for k, v in fd_c0.items()},
             "fd_s": time.perf_counter() - t0,
             "note": "backward = 2 exact tangent sweeps + 1 exact-adjoint sweep, each interval recomputed "
-                    "from its checkpoint; central differences: meanU at relative step 1e-6, C0 at 1e-4, Re at 1e-3 "
-                    "(the sweeps show the rounding-noise floor at smaller steps)"}
+                    "from its checkpoint; central differences: meanU at relative step 1e-6, C0 at 1e-5, Re at 1e-3 "
+                    "(the sweeps show truncation at larger steps, rounding noise at smaller)"}
 
 
 def large_grid(cc, nsteps=8):

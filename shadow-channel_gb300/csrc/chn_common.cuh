@@ -101,6 +101,7 @@ struct Grid {
   const uint32_t* tcX;
   const int* tcXE;
   int tci;
+  int tcminb;  // blocks per SM the tensor-core inverse is compiled for (2 or 3; autotuned)
   // forward transforms likewise (phys_tc.cu, k_products_tc): x stage
   // [2X][px] (1/(px pz) folded in), z stage [2 (Nz - 1)][2 pz]; tcf = 0: the FFT kernels
   const uint32_t* tcFX;

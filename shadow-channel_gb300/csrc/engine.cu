@@ -187,6 +187,7 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   const char* tfp64 = getenv("CHN_TRANSFORMS_FP64");
   g.tci = (!(tfp64 && tfp64[0] == '1') && phys_tc_fits(g, optin)) ? 1 : 0;
   g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_fits(g, optin)) ? 1 : 0;
+  g.tcminb = 3;  // until the autotuner has timed both builds
   if (solve_smem_bytes(g) > (size_t)optin || recon_smem_bytes(g) > (size_t)optin) {
     set_error(1, "grid %dx%dx%d: the implicit solve needs %zu bytes of shared memory per block, the device has %d",
               Nx, Ny, Nz, solve_smem_bytes(g), optin);
@@ -878,13 +879,20 @@ static bool autotune_transforms(Engine& e, Work& w) {
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   struct Cand {
-    int split, tvar;
+    int split, tvar, minb;
     float ms;
   };
   std::vector<Cand> cands;
-  if (fused_transforms_fit(g, optin)) cands.push_back({0, 0, 0.f});
-  for (int v = 0; v < split_variant_count(); ++v)
-    if (split_variant_fits(v, g, optin)) cands.push_back({1, v, 0.f});
+  if (g.tci && g.tcf) {
+    // both transforms on the tensor cores: the FFT variants are unused; time
+    // the two register budgets of the tensor-core inverse
+    cands.push_back({g.split, g.tvar, 2, 0.f});
+    cands.push_back({g.split, g.tvar, 3, 0.f});
+  } else {
+    if (fused_transforms_fit(g, optin)) cands.push_back({0, 0, g.tcminb, 0.f});
+    for (int v = 0; v < split_variant_count(); ++v)
+      if (split_variant_fits(v, g, optin)) cands.push_back({1, v, g.tcminb, 0.f});
+  }
   if (cands.size() < 2 || !w.Zt) return true;
   const int nt = w.nseg * (w.ntan > 0 ? w.ntan : 1);
   auto enqueue = [&]() -> bool {
@@ -920,11 +928,12 @@ static bool autotune_transforms(Engine& e, Work& w) {
   cudaEvent_t t0, t1;
   CK(cudaEventCreate(&t0));
   CK(cudaEventCreate(&t1));
-  const int saved_split = g.split, saved_tvar = g.tvar;
+  const int saved_split = g.split, saved_tvar = g.tvar, saved_minb = g.tcminb;
   bool ok = true;
   for (Cand& c : cands) {
     g.split = c.split;
     g.tvar = c.tvar;
+    g.tcminb = c.minb;
     ok = ok && enqueue();  // warm-up
     ok = ok && cudaEventRecord(t0, e.st) == cudaSuccess;
     for (int r = 0; r < 3; ++r) ok = ok && enqueue();
@@ -938,6 +947,7 @@ static bool autotune_transforms(Engine& e, Work& w) {
   if (!ok) {
     g.split = saved_split;
     g.tvar = saved_tvar;
+    g.tcminb = saved_minb;
     return false;
   }
   const Cand* best = &cands[0];
@@ -945,10 +955,14 @@ static bool autotune_transforms(Engine& e, Work& w) {
     if (c.ms < best->ms) best = &c;
   g.split = best->split;
   g.tvar = best->tvar;
+  g.tcminb = best->minb;
   char buf[160];
   g_tune_report = "{";
+  const bool tcv = g.tci && g.tcf;
   for (const Cand& c : cands) {
-    if (c.split) {
+    if (tcv) {
+      snprintf(buf, sizeof(buf), "\"tc_inverse_minb%d\": %.4f, ", c.minb, c.ms);
+    } else if (c.split) {
       const TransformVariant v = split_variant(c.tvar);
       snprintf(buf, sizeof(buf), "\"split_nt%d_ch%d\": %.4f, ", v.nt, v.ch, c.ms);
     } else {
@@ -956,7 +970,9 @@ static bool autotune_transforms(Engine& e, Work& w) {
     }
     g_tune_report += buf;
   }
-  if (best->split) {
+  if (tcv) {
+    snprintf(buf, sizeof(buf), "\"chosen\": \"tc_inverse_minb%d\", \"instances\": %d}", best->minb, nt);
+  } else if (best->split) {
     const TransformVariant v = split_variant(best->tvar);
     snprintf(buf, sizeof(buf), "\"chosen\": \"split_nt%d_ch%d\", \"instances\": %d}", v.nt, v.ch, nt);
   } else {
@@ -1982,6 +1998,7 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
     gs[i].tc = gmax.tc;
     gs[i].tci = gmax.tci;
     gs[i].tcf = gmax.tcf;
+    gs[i].tcminb = gmax.tcminb;
   }
   if (cudaMalloc(&m->gdev, sizeof(Grid) * n) != cudaSuccess ||
       cudaMemcpy(m->gdev, gs.data(), sizeof(Grid) * n, cudaMemcpyHostToDevice) != cudaSuccess) {

@@ -15,6 +15,7 @@
 // intermediate Z is rounded to FP64 in shared memory between the stages.  Same outputs,
 // CFL check and status bits as k_phys_inverse.
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "chn_common.cuh"
@@ -115,7 +116,7 @@ __host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g) {
   d.KSz = d.KTz * 16 + 8;
   d.KSx = d.KTx * 16 + 8;
   d.NZ = kFB * g.X;
-  d.NX = kFB * g.pz;
+  d.NX = g.pz;  // the x stage runs one field at a time
   return d;
 }
 
@@ -140,8 +141,8 @@ size_t phys_tc_smem_bytes(const Grid& g, bool with_cfl) {
 // kernel
 // ---------------------------------------------------------------------------
 
-template <bool MULTI>
-__global__ void __launch_bounds__(kThreads, 2) k_phys_inverse_tc(const __grid_constant__ Grid g0, PhysArgs a) {
+template <bool MULTI, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid_constant__ Grid g0, PhysArgs a) {
   const int inst = blockIdx.y, y = blockIdx.x;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
   if (y >= g.Q) return;
@@ -250,83 +251,87 @@ __global__ void __launch_bounds__(kThreads, 2) k_phys_inverse_tc(const __grid_co
       }
     }
     __syncthreads();
-    // ---- x stage: columns n = fl * pz + m, K = 2X (Re, Im of Z[m][j]; Im of j = 0 unused)
-    for (int i = threadIdx.x; i < d.NX; i += blockDim.x) exx[i] = 0;
-    __syncthreads();
-    for (int i = threadIdx.x; i < nfb * g.pz * g.X; i += blockDim.x) {
-      const int n = i / g.X, j = i - n * g.X;
-      const cpx v = Zb[(size_t)n * g.X + j];
-      const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
-                        j ? (int)((__double_as_longlong(v.im) >> 52) & 0x7FF) : 0);
-      if (e) atomicMax(&exx[n], e);
-    }
-    __syncthreads();
-    const size_t xstride = (size_t)((d.NX + 7) / 8 * 8) * d.KSx;
-    {
-      uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
-      for (int i = threadIdx.x; i < d.NX * d.KTx * 8; i += blockDim.x) {
-        const int n = i / (d.KTx * 8), j = i - n * (d.KTx * 8);
-        cpx v = {0.0, 0.0};
-        if (j < g.X && n < nfb * g.pz) v = Zb[(size_t)n * g.X + j];
-        if (j == 0) v.im = 0.0;
-        const int ex = exx[n] - 1022;
-        digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSx) / 2 + j, xstride / 2);
+    // ---- x stage, one field at a time: columns n = m, K = 2X (Re, Im of
+    // Z[m][j]; Im of j = 0 unused)
+    const size_t xstride = (size_t)((g.pz + 7) / 8 * 8) * d.KSx;
+    for (int fl = 0; fl < nfb; ++fl) {
+      const cpx* Zf = Zb + (size_t)fl * g.pz * g.X;
+      for (int i = threadIdx.x; i < g.pz; i += blockDim.x) exx[i] = 0;
+      __syncthreads();
+      for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x) {
+        const int n = i / g.X, j = i - n * g.X;
+        const cpx v = Zf[i];
+        const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
+                          j ? (int)((__double_as_longlong(v.im) >> 52) & 0x7FF) : 0);
+        if (e) atomicMax(&exx[n], e);
       }
-    }
-    __syncthreads();
-    {
-      const int NT = (nfb * g.pz + 7) / 8;
-      for (int item = warp; item < d.MTx * NT; item += nwarp) {
-        const int mt = item / NT, nt = item - mt * NT;
-        const int n = nt * 8 + gq;
-        float acc[kDig][4];
-        double part[4] = {0.0, 0.0, 0.0, 0.0};
-        long long H[4], L[4];
-        for (int kc = 0; kc < d.KTx; kc += kChunkKT) {
+      __syncthreads();
+      {
+        uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
+        const int npad = (g.pz + 7) / 8 * 8;
+        for (int i = threadIdx.x; i < npad * d.KTx * 8; i += blockDim.x) {
+          const int n = i / (d.KTx * 8), j = i - n * (d.KTx * 8);
+          cpx v = {0.0, 0.0};
+          if (j < g.X && n < g.pz) v = Zf[(size_t)n * g.X + j];
+          if (j == 0) v.im = 0.0;
+          const int ex = exx[min(n, g.pz - 1)] - 1022;
+          digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSx) / 2 + j, xstride / 2);
+        }
+      }
+      __syncthreads();
+      {
+        const int NT = (g.pz + 7) / 8;
+        for (int item = warp; item < d.MTx * NT; item += nwarp) {
+          const int mt = item / NT, nt = item - mt * NT;
+          const int n = nt * 8 + gq;
+          float acc[kDig][4];
+          double part[4] = {0.0, 0.0, 0.0, 0.0};
+          long long H[4], L[4];
+          for (int kc = 0; kc < d.KTx; kc += kChunkKT) {
 #pragma unroll
-          for (int l = 0; l < kDig; ++l)
+            for (int l = 0; l < kDig; ++l)
 #pragma unroll
-            for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
-          const int kend = min(d.KTx, kc + kChunkKT);
-          for (int kt = kc; kt < kend; ++kt) {
-            const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * d.KSx + kt * 16);
-            uint32_t b0[kDig], b1[kDig];
+              for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+            const int kend = min(d.KTx, kc + kChunkKT);
+            for (int kt = kc; kt < kend; ++kt) {
+              const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * d.KSx + kt * 16);
+              uint32_t b0[kDig], b1[kDig];
 #pragma unroll
-            for (int k = 0; k < kDig; ++k) {
-              b0[k] = brow[(size_t)k * xstride / 2 + t];
-              b1[k] = brow[(size_t)k * xstride / 2 + t + 4];
+              for (int k = 0; k < kDig; ++k) {
+                b0[k] = brow[(size_t)k * xstride / 2 + t];
+                b1[k] = brow[(size_t)k * xstride / 2 + t + 4];
+              }
+#pragma unroll
+              for (int i = 0; i < kDig; ++i) {
+                const uint4 af = __ldg(&Ax[(((size_t)mt * d.KTx + kt) * kDig + i) * 32 + lane]);
+#pragma unroll
+                for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
+              }
             }
 #pragma unroll
-            for (int i = 0; i < kDig; ++i) {
-              const uint4 af = __ldg(&Ax[(((size_t)mt * d.KTx + kt) * kDig + i) * 32 + lane]);
+            for (int r = 0; r < 4; ++r) fold_levels(acc, r, H[r], L[r]);
+            if (kend < d.KTx) {
 #pragma unroll
-              for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
+              for (int r = 0; r < 4; ++r) {
+                const int row = min(mt * 16 + gq + 8 * (r >> 1), g.px - 1);
+                const int col = min(nt * 8 + 2 * t + (r & 1), g.pz - 1);
+                part[r] += round_scaled(H[r], L[r], g.tcXE[row] + exx[col] - 1022 - 64);
+              }
             }
           }
 #pragma unroll
-          for (int r = 0; r < 4; ++r) fold_levels(acc, r, H[r], L[r]);
-          if (kend < d.KTx) {
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-              const int row = min(mt * 16 + gq + 8 * (r >> 1), g.px - 1);
-              const int col = min(nt * 8 + 2 * t + (r & 1), d.NX - 1);
-              part[r] += round_scaled(H[r], L[r], g.tcXE[row] + exx[col] - 1022 - 64);
-            }
+          for (int r = 0; r < 4; ++r) {
+            const int xp = mt * 16 + gq + 8 * (r >> 1), m = nt * 8 + 2 * t + (r & 1);
+            if (xp >= g.px || m >= g.pz) continue;
+            double v = round_fast(H[r], L[r], g.tcXE[xp] + exx[m] - 1022 - 64);
+            if (d.KTx > kChunkKT) v += part[r];
+            P[((size_t)(f0 + fl) * g.Q + y) * plane + (size_t)m * g.px + xp] = v;
+            nonfinite |= !finite_bits(v);
           }
         }
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          const int xp = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
-          if (xp >= g.px || col >= nfb * g.pz) continue;
-          double v = round_fast(H[r], L[r], g.tcXE[xp] + exx[col] - 1022 - 64);
-          if (d.KTx > kChunkKT) v += part[r];
-          const int fl = col / g.pz, m = col - fl * g.pz, f = f0 + fl;
-          P[((size_t)f * g.Q + y) * plane + (size_t)m * g.px + xp] = v;
-          nonfinite |= !finite_bits(v);
-        }
       }
+      __syncthreads();
     }
-    __syncthreads();
   }
   if (nonfinite && a.status) atomicOr(&a.status[inst / a.sdiv], ST_NONFINITE);
   if (a.cfl_check) {
@@ -562,16 +567,27 @@ bool phys_tc_fits(const Grid& g, int optin) {
   return phys_tc_smem_bytes(g, true) + 4096 <= (size_t)optin;
 }
 
+// Two builds of the kernel: for 2 blocks per SM (128 registers) and for 3
+// (80 registers, some spilled); Grid::tcminb selects (the autotuner times
+// both; the results are identical)
 cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st) {
   const size_t sm = phys_tc_smem_bytes(g, a.cfl_check != 0);
-  if (a.grids) k_phys_inverse_tc<true><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
-  else k_phys_inverse_tc<false><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a);
+  const dim3 grid(g.Q, a.ninst);
+  if (g.tcminb == 3) {
+    if (a.grids) k_phys_inverse_tc<true, 3><<<grid, kThreads, sm, st>>>(g, a);
+    else k_phys_inverse_tc<false, 3><<<grid, kThreads, sm, st>>>(g, a);
+  } else {
+    if (a.grids) k_phys_inverse_tc<true, 2><<<grid, kThreads, sm, st>>>(g, a);
+    else k_phys_inverse_tc<false, 2><<<grid, kThreads, sm, st>>>(g, a);
+  }
   return cudaGetLastError();
 }
 
 void prepare_phys_tc(int optin) {
-  allow_max_smem(k_phys_inverse_tc<false>, optin);
-  allow_max_smem(k_phys_inverse_tc<true>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 2>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 2>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 3>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 3>, optin);
   allow_max_smem(k_products_tc<false>, optin);
   allow_max_smem(k_products_tc<true>, optin);
 }
