@@ -393,27 +393,44 @@ size_t fwd_tc_smem_bytes(const Grid& g) {
   return b;
 }
 
-// one exact digit GEMM tile loop over k-tiles kt0..kt1 of a fixed table A
-// (fragment order [mt][KT][7][32][4]) and smem digits of column n
+// One exact digit GEMM tile of a fixed table A (fragment order
+// [mt][KT][7][32][4]) against the smem digits of column n, over all KT
+// k-tiles: FP32 level sums per chunk of at most 7 k-tiles (exact), folded
+// into the 64-bit integers H, L per accumulator element (exact across
+// chunks: |H| < 2^41, |L| < 2^50 per chunk)
 __device__ __forceinline__ void tc_tile(const uint4* __restrict__ A, int mt, int KT, const uint16_t* dig, size_t KS,
-                                        size_t dstride, int n, int lane, int t, float (&acc)[kDig][4]) {
+                                        size_t dstride, int n, int lane, int t, long long (&H)[4],
+                                        long long (&L)[4]) {
 #pragma unroll
-  for (int l = 0; l < kDig; ++l)
+  for (int r = 0; r < 4; ++r) { H[r] = 0; L[r] = 0; }
+  for (int kc = 0; kc < KT; kc += kChunkKT) {
+    float acc[kDig][4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
-  for (int kt = 0; kt < KT; ++kt) {
-    const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
-    uint32_t b0[kDig], b1[kDig];
+    for (int l = 0; l < kDig; ++l)
 #pragma unroll
-    for (int k = 0; k < kDig; ++k) {
-      b0[k] = brow[(size_t)k * dstride / 2 + t];
-      b1[k] = brow[(size_t)k * dstride / 2 + t + 4];
+      for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+    const int kend = min(KT, kc + kChunkKT);
+    for (int kt = kc; kt < kend; ++kt) {
+      const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
+      uint32_t b0[kDig], b1[kDig];
+#pragma unroll
+      for (int k = 0; k < kDig; ++k) {
+        b0[k] = brow[(size_t)k * dstride / 2 + t];
+        b1[k] = brow[(size_t)k * dstride / 2 + t + 4];
+      }
+#pragma unroll
+      for (int i = 0; i < kDig; ++i) {
+        const uint4 af = __ldg(&A[(((size_t)mt * KT + kt) * kDig + i) * 32 + lane]);
+#pragma unroll
+        for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
+      }
     }
 #pragma unroll
-    for (int i = 0; i < kDig; ++i) {
-      const uint4 af = __ldg(&A[(((size_t)mt * KT + kt) * kDig + i) * 32 + lane]);
-#pragma unroll
-      for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
+    for (int r = 0; r < 4; ++r) {
+      long long h, l;
+      fold_levels(acc, r, h, l);
+      H[r] += h;
+      L[r] += l;
     }
   }
 }
@@ -422,8 +439,7 @@ __device__ __forceinline__ void tc_tile(const uint4* __restrict__ A, int mt, int
 // 3 the exact transpose; split_product) and their forward transforms as
 // digit GEMMs, one component at a time; modes 0/1 write H slots 0..2, modes
 // 2/3 fold each component into the output slots (assemble_stage).  Same
-// outputs as k_products_fwd / k_products_adj.  K <= 112 per stage (single
-// FP32 chunk): fwd_tc_fits checks it.
+// outputs as k_products_fwd / k_products_adj.
 template <bool MULTI>
 __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_constant__ Grid g0, ProdArgs a, int mode) {
   const int inst = blockIdx.y, y = blockIdx.x;
@@ -482,15 +498,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
       const int NT = d.pzp / 8;
       for (int item = warp; item < d.MTx * NT; item += nwarp) {
         const int mt = item / NT, nt = item - mt * NT;
-        float acc[kDig][4];
-        tc_tile(Ax, mt, d.KTx, dig, d.KSx, xstride, nt * 8 + gq, lane, t, acc);
+        long long Hh[4], Ll[4];
+        tc_tile(Ax, mt, d.KTx, dig, d.KSx, xstride, nt * 8 + gq, lane, t, Hh, Ll);
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int row = mt * 16 + gq + 8 * (r >> 1), zp = nt * 8 + 2 * t + (r & 1);
           if (row >= 2 * g.X || zp >= g.pz) continue;
-          long long Hh, Ll;
-          fold_levels(acc, r, Hh, Ll);
-          const double v = round_fast(Hh, Ll, AxE[row] + exx[zp] - 1022 - 64);
+          const double v = round_fast(Hh[r], Ll[r], AxE[row] + exx[zp] - 1022 - 64);
           cpx& yv = Yb[(size_t)zp * g.X + (row >> 1)];
           if (row & 1) yv.im = v;
           else yv.re = v;
@@ -523,15 +537,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
       const int NT = d.Xp / 8;
       for (int item = warp; item < d.MTz * NT; item += nwarp) {
         const int mt = item / NT, nt = item - mt * NT;
-        float acc[kDig][4];
-        tc_tile(Az, mt, d.KTz, dig, d.KSz, zstride, nt * 8 + gq, lane, t, acc);
+        long long Hh[4], Ll[4];
+        tc_tile(Az, mt, d.KTz, dig, d.KSz, zstride, nt * 8 + gq, lane, t, Hh, Ll);
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int row = mt * 16 + gq + 8 * (r >> 1), kx = nt * 8 + 2 * t + (r & 1);
           if (row >= 2 * d.Kk || kx >= g.X) continue;
-          long long Hh, Ll;
-          fold_levels(acc, r, Hh, Ll);
-          const double v = round_fast(Hh, Ll, g.tcFZE[row] + exz[kx] - 1022 - 64);
+          const double v = round_fast(Hh[r], Ll[r], g.tcFZE[row] + exz[kx] - 1022 - 64);
           cpx& fv = Fb[(size_t)(row >> 1) * g.X + kx];
           if (row & 1) fv.im = v;
           else fv.re = v;
@@ -550,10 +562,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
   }
 }
 
-bool fwd_tc_fits(const Grid& g, int optin) {
-  const FwdTcDims d = fwd_tc_dims(g);
-  return d.KTx <= kChunkKT && d.KTz <= kChunkKT && fwd_tc_smem_bytes(g) + 4096 <= (size_t)optin;
-}
+// Used where two blocks fit an SM (up to 32x65x32): at 48x97x48 a block
+// needs 149 KB, one per SM, and the FFT kernels (two per SM) are faster,
+// also for an uneven batch, whose every instance runs at the largest
+// grid's shared memory.
+bool fwd_tc_fits(const Grid& g, int optin) { return 2 * (fwd_tc_smem_bytes(g) + 4096) <= (size_t)optin + 4096; }
 
 cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
   const size_t sm = fwd_tc_smem_bytes(g);
