@@ -156,22 +156,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
     const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
     const cpx v = cval(cls, j, col);
     const int ex = exc[cls * kTile + col] - 1022;
-    for (int p = 0; p < 2; ++p) {
-      long long x = scaled56(p ? v.im : v.re, ex);
-      int d[kDig];
-      for (int q = kDig - 1; q >= 1; --q) {
-        const long long lo = ((x + 128) & 255) - 128;
-        d[q] = (int)lo;
-        x = (x - lo) >> 8;
-      }
-      d[0] = (int)x;
-      const int n = 2 * col + p;
-#pragma unroll
-      for (int q = 0; q < kDig; ++q) {
-        const __nv_bfloat16 h = __float2bfloat16_rn((float)d[q]);
-        dig[(((size_t)cls * kDig + q) * 32 + n) * KS + j] = *reinterpret_cast<const uint16_t*>(&h);
-      }
-    }
+    for (int p = 0; p < 2; ++p)  // digit q of column n at dig[((cls * 7 + q) * 32 + n) * KS + j]
+      digits_bf16(scaled56(p ? v.im : v.re, ex), dig + ((size_t)cls * kDig * 32 + 2 * col + p) * KS + j,
+                  (size_t)32 * KS);
   }
   __syncthreads();
 

@@ -101,40 +101,44 @@ __device__ __forceinline__ bool finite_bits(double x) {
 
 // Balanced digits without a carry chain: with B = sum_{i<6} 128 * 256^i,
 // x + B = sum_{q>=1} (d_q + 128) 256^(6-q) + d_0 256^6, so every lower digit
-// is an unsigned byte of x + B less 128 and the top digit its arithmetic
-// shift by 48.  Seven independent extractions.
-__device__ __forceinline__ void balanced_digits(long long x, int (&d)[kDig]) {
+// is an unsigned byte of x + B less 128 and the top digit (in [-256, 256])
+// its arithmetic shift by 48.  The digits come out as FP32 values without an
+// integer-to-float conversion: for 0 <= u < 2^23 the bit pattern
+// 0x4B000000 | u is the float 2^23 + u, so a byte b placed under that
+// exponent (one byte permute) less 2^23 + 128 is b - 128, exactly (one FP32
+// add); the top digit goes the same way through u = d_0 + 256.  Every digit
+// has at most 8 significant bits, so the float's upper half is its exact bf16.
+__device__ __forceinline__ void balanced_digits_f32(long long x, float (&f)[kDig]) {
   const long long xb = x + 0x808080808080LL;
   const unsigned lo = (unsigned)xb, hi = (unsigned)(xb >> 32);
-  d[6] = (int)(lo & 255u) - 128;
-  d[5] = (int)((lo >> 8) & 255u) - 128;
-  d[4] = (int)((lo >> 16) & 255u) - 128;
-  d[3] = (int)(lo >> 24) - 128;
-  d[2] = (int)(hi & 255u) - 128;
-  d[1] = (int)((hi >> 8) & 255u) - 128;
-  d[0] = (int)(xb >> 48);
+  constexpr float kOff = 8388736.0f;  // 2^23 + 128
+  // __byte_perm selector 0x765k: byte 0 from byte k of the word, bytes 1-3 from 0x4B000000
+  f[6] = __uint_as_float(__byte_perm(lo, 0x4B000000u, 0x7650)) - kOff;
+  f[5] = __uint_as_float(__byte_perm(lo, 0x4B000000u, 0x7651)) - kOff;
+  f[4] = __uint_as_float(__byte_perm(lo, 0x4B000000u, 0x7652)) - kOff;
+  f[3] = __uint_as_float(__byte_perm(lo, 0x4B000000u, 0x7653)) - kOff;
+  f[2] = __uint_as_float(__byte_perm(hi, 0x4B000000u, 0x7650)) - kOff;
+  f[1] = __uint_as_float(__byte_perm(hi, 0x4B000000u, 0x7651)) - kOff;
+  f[0] = __uint_as_float((unsigned)(((int)hi >> 16) + (0x4B000000 + 256))) - 8388864.0f;  // 2^23 + 256
 }
 
 // seven balanced digits of x (|x| < 2^56) as bf16 bit patterns, most significant first
 __device__ __forceinline__ void digits_bf16(long long x, uint16_t* out, size_t stride) {
-  int d[kDig];
-  balanced_digits(x, d);
+  float f[kDig];
+  balanced_digits_f32(x, f);
 #pragma unroll
-  for (int q = 0; q < kDig; ++q) {
-    const __nv_bfloat16 h = __float2bfloat16_rn((float)d[q]);
-    out[(size_t)q * stride] = *reinterpret_cast<const uint16_t*>(&h);
-  }
+  for (int q = 0; q < kDig; ++q) out[(size_t)q * stride] = (uint16_t)(__float_as_uint(f[q]) >> 16);
 }
 
 // the balanced digits of two values (re, im) packed per digit into one 32-bit
 // word (re in the low half): out[q * stride] for q = 0..6
 __device__ __forceinline__ void digits_pair_bf16(long long xr, long long xi, uint32_t* out, size_t stride) {
-  int dr[kDig], di[kDig];
-  balanced_digits(xr, dr);
-  balanced_digits(xi, di);
+  float fr[kDig], fi[kDig];
+  balanced_digits_f32(xr, fr);
+  balanced_digits_f32(xi, fi);
 #pragma unroll
-  for (int q = 0; q < kDig; ++q)  // |d| <= 256: the float's upper half is the exact bf16
-    out[(size_t)q * stride] = (__float_as_uint((float)dr[q]) >> 16) | (__float_as_uint((float)di[q]) & 0xFFFF0000u);
+  for (int q = 0; q < kDig; ++q)  // the upper halves of the two floats
+    out[(size_t)q * stride] = __byte_perm(__float_as_uint(fr[q]), __float_as_uint(fi[q]), 0x7632);
 }
 
 // the exact level sums of one mma accumulator element as (H, L): the sum is
