@@ -93,13 +93,17 @@ struct Grid {
   const uint32_t* tcW;
   const int* tcWE;
   int tc;
-  // inverse transforms as DFT GEMMs on the tensor cores (phys_tc.cu): the z
-  // stage's matrix [2 pz][2 (Nz - 1)] and the x stage's [px][2X] as digit
-  // tables with row exponents; tci = 0: the FFT kernels
+  // inverse transforms as DFT GEMMs on the tensor cores (phys_tc.cu), each
+  // stage split radix-2 into even and odd modes where its length is even:
+  // the z stage's matrix [2 pz / 2][even | odd modes (Re, Im)] and the x
+  // stage's [px / 2][even | odd j (Re, Im)] as digit tables with row
+  // exponents, and the z stage's K-word -> kept kz index map (-1: padding);
+  // tci = 0: the FFT kernels
   const uint32_t* tcZ;
   const int* tcZE;
   const uint32_t* tcX;
   const int* tcXE;
+  const int* tcZM;
   int tci;
   int tcminb;  // blocks per SM the tensor-core inverse is compiled for (2 or 3; autotuned)
   // forward transforms likewise (phys_tc.cu, k_products_tc): x stage

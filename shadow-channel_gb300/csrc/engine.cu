@@ -155,9 +155,9 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
         !T.up(wfrag, &g.tcW) || !T.up(wex, &g.tcWE))
       return false;
     std::vector<uint32_t> zf, xf;
-    std::vector<int> ze, xe;
-    if (!build_phys_tc_tables(h, zf, ze, xf, xe) || !T.up(zf, &g.tcZ) || !T.up(ze, &g.tcZE) || !T.up(xf, &g.tcX) ||
-        !T.up(xe, &g.tcXE))
+    std::vector<int> ze, xe, zm;
+    if (!build_phys_tc_tables(h, zf, ze, xf, xe, zm) || !T.up(zf, &g.tcZ) || !T.up(ze, &g.tcZE) ||
+        !T.up(xf, &g.tcX) || !T.up(xe, &g.tcXE) || !T.up(zm, &g.tcZM))
       return false;
     std::vector<uint32_t> fxf, fzf, fuf;
     std::vector<int> fxe, fze, fue;

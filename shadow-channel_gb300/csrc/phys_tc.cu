@@ -3,12 +3,20 @@
 //
 // One block per (instance, plane y), two fields per pass:
 //   z stage   Z[m][x] = sum_kz F[kz][x] exp(+2 pi i m zp(kz)/pz) over the
-//             Nz - 1 kept rows: a real GEMM with 2 pz rows (Re, Im of Z),
-//             K = 2 (Nz - 1) (Re, Im of F interleaved), one column per (field, x);
+//             Nz - 1 kept rows, one column per (field, x);
 //   x stage   P[m][xp] = Re Z[m][0] + 2 sum_{0<j<X} Re(Z[m][j] exp(+2 pi i j xp/px))
 //             (the complex-to-real transform; the imaginary part of the
-//             kx = 0 bin is ignored as by c2r): px rows, K = 2X, one column
-//             per (field, m).
+//             kx = 0 bin is ignored as by c2r), one column per m.
+// Each stage is split radix-2 where its length n is even: with
+// exp(2 pi i k (m + n/2)/n) = (-1)^k exp(2 pi i k m/n), the outputs m and
+// m + n/2 are E + O and E - O for the sums E, O over the even and odd k, so
+// a stage is one GEMM with half the rows (m < n/2) whose K holds the even
+// modes and then the odd ones; the two partial sums stay exact 64-bit
+// integers (the E and O rows of a table share their row exponent) and their
+// sum and difference are rounded once each.  z stage: rows Re, Im of
+// Z[m < pz/2] (2 pz/2 rows), K = Re, Im of the even-zp and odd-zp modes;
+// x stage: rows xp < px/2, K = Re, Im of the even and odd j.  An odd length
+// keeps one class (the full DFT).
 // The DFT matrices hold the FFT's own twiddle doubles; operands are base-256
 // digits with exact FP32 level sums (tc_common.cuh), so each output is the
 // (faithfully) rounded value of the exact sum of the 56-bit operands.  The
@@ -33,33 +41,90 @@ static constexpr int kFB = 2;  // fields per pass
 // host tables
 // ---------------------------------------------------------------------------
 
+// kept kz modes of even / odd padded index zp (kk < Nz/2: zp = kk; else
+// zp = kk + 1 + Nz/2, which runs over the odd Nz + 1 ... 3Nz/2 - 1); an odd
+// pz keeps all modes in one class
+__host__ __device__ inline void z_class_counts(int Nz, int pz, int& nE, int& nO) {
+  if (pz % 2) {
+    nE = Nz - 1;
+    nO = 0;
+    return;
+  }
+  const int h = Nz / 2;
+  nE = (h + 1) / 2 + (h - 1) / 2;
+  nO = h / 2 + h / 2;
+}
+
+// the kept kz modes of one class of the z stage's radix-2 split (padded
+// index zp even or odd; the only class for an odd pz)
+static void z_class_modes(int Nz, int pz, int cls, std::vector<int>& kk_of) {
+  kk_of.clear();
+  for (int kk = 0; kk < Nz - 1; ++kk) {
+    const int zp = kk < Nz / 2 ? kk : kk + 1 + Nz / 2;  // padded row of kept kz index kk
+    if (pz % 2 || (zp & 1) == cls) kk_of.push_back(kk);
+  }
+}
+
 bool build_phys_tc_tables(const HostTables& h, std::vector<uint32_t>& zfrag, std::vector<int>& zex,
-                          std::vector<uint32_t>& xfrag, std::vector<int>& xex) {
+                          std::vector<uint32_t>& xfrag, std::vector<int>& xex, std::vector<int>& zmap) {
   const int pz = h.pz, px = h.px, Nz = h.Nz, X = h.X;
-  const int Kz = 2 * (Nz - 1), Kx = 2 * X;
-  std::vector<double> Az((size_t)2 * pz * Kz, 0.0), Ax((size_t)px * Kx, 0.0);
-  for (int m = 0; m < pz; ++m)
-    for (int kk = 0; kk < Nz - 1; ++kk) {
-      const int zp = kk < Nz / 2 ? kk : kk + 1 + Nz / 2;  // padded row of kept kz index kk
-      const int idx = (int)(((long long)m * zp) % pz);
-      const double c = h.twz[2 * idx], s = -h.twz[2 * idx + 1];  // exp(+i theta) = conj(exp(-i theta))
-      Az[(size_t)m * Kz + 2 * kk] = c;
-      Az[(size_t)m * Kz + 2 * kk + 1] = -s;
-      Az[(size_t)(pz + m) * Kz + 2 * kk] = s;
-      Az[(size_t)(pz + m) * Kz + 2 * kk + 1] = c;
+  const int Rz = pz % 2 ? 1 : 2, Rx = px % 2 ? 1 : 2, pzh = pz / Rz, pxh = px / Rx;
+  std::vector<int> zE, zO;
+  z_class_modes(Nz, pz, 0, zE);
+  if (Rz == 2) z_class_modes(Nz, pz, 1, zO);
+  int nE = 0, nO = 0;
+  z_class_counts(Nz, pz, nE, nO);  // the kernel's closed form
+  if (nE != (int)zE.size() || nO != (int)zO.size()) return false;
+  const int nxE = (X + Rx - 1) / Rx, nxO = X - nxE;
+  const int KTzE = (2 * (int)zE.size() + 15) / 16, KTzO = (2 * (int)zO.size() + 15) / 16;
+  const int KTxE = (2 * nxE + 15) / 16, KTxO = (2 * nxO + 15) / 16;
+  const int Kz = (KTzE + KTzO) * 16, Kx = (KTxE + KTxO) * 16;
+  // z stage: rows Re Z[m], Im Z[m] (m < pzh); K words: even modes, then odd
+  std::vector<double> Az((size_t)2 * pzh * Kz, 0.0), Ax((size_t)pxh * Kx, 0.0);
+  zmap.assign((size_t)Kz / 2, -1);
+  for (int c = 0; c < 2; ++c) {
+    const std::vector<int>& modes = c ? zO : zE;
+    const int w0 = c ? KTzE * 8 : 0;
+    for (int e = 0; e < (int)modes.size(); ++e) {
+      const int kk = modes[e], zp = kk < Nz / 2 ? kk : kk + 1 + Nz / 2, w = w0 + e;
+      zmap[w] = kk;
+      for (int m = 0; m < pzh; ++m) {
+        const int idx = (int)(((long long)m * zp) % pz);
+        const double cs = h.twz[2 * idx], sn = -h.twz[2 * idx + 1];  // exp(+i theta) = conj(exp(-i theta))
+        Az[(size_t)m * Kz + 2 * w] = cs;
+        Az[(size_t)m * Kz + 2 * w + 1] = -sn;
+        Az[(size_t)(pzh + m) * Kz + 2 * w] = sn;
+        Az[(size_t)(pzh + m) * Kz + 2 * w + 1] = cs;
+      }
     }
-  for (int xp = 0; xp < px; ++xp) {
-    Ax[(size_t)xp * Kx] = 1.0;
-    for (int j = 1; j < X; ++j) {
+  }
+  // x stage: rows xp < pxh; K words: j = Rx e (even), then j = 2 o + 1 (odd)
+  for (int w = 0; w < Kx / 2; ++w) {
+    int j;
+    if (w < KTxE * 8) {
+      if (w >= nxE) continue;
+      j = Rx * w;
+    } else {
+      const int o = w - KTxE * 8;
+      if (o >= nxO) continue;
+      j = 2 * o + 1;
+    }
+    for (int xp = 0; xp < pxh; ++xp) {
+      if (j == 0) {
+        Ax[(size_t)xp * Kx + 2 * w] = 1.0;
+        continue;
+      }
       const int idx = (int)(((long long)j * xp) % px);
-      const double c = h.twx[2 * idx], s = -h.twx[2 * idx + 1];
-      Ax[(size_t)xp * Kx + 2 * j] = 2.0 * c;
-      Ax[(size_t)xp * Kx + 2 * j + 1] = -2.0 * s;
+      const double cs = h.twx[2 * idx], sn = -h.twx[2 * idx + 1];
+      Ax[(size_t)xp * Kx + 2 * w] = 2.0 * cs;
+      Ax[(size_t)xp * Kx + 2 * w + 1] = -2.0 * sn;
     }
   }
   zfrag.clear(); zex.clear(); xfrag.clear(); xex.clear();
-  return append_digit_table(Az.data(), 2 * pz, Kz, (2 * pz + 15) / 16, (Kz + 15) / 16, zfrag, zex) &&
-         append_digit_table(Ax.data(), px, Kx, (px + 15) / 16, (Kx + 15) / 16, xfrag, xex);
+  // one table per stage with both classes in its K: a row's exponent covers
+  // its even and odd parts, so their integer sums add exactly
+  return append_digit_table(Az.data(), 2 * pzh, Kz, (2 * pzh + 15) / 16, Kz / 16, zfrag, zex) &&
+         append_digit_table(Ax.data(), pxh, Kx, (pxh + 15) / 16, Kx / 16, xfrag, xex);
 }
 
 // forward transforms (channel/pass1.c:312-339): x stage Y[zp][kx] =
@@ -104,15 +169,28 @@ bool build_fwd_tc_tables(const HostTables& h, std::vector<uint32_t>& xfrag, std:
 // ---------------------------------------------------------------------------
 
 struct PhysTcDims {
-  int KTz, KTx, MTz, MTx, KSz, KSx, NZ, NX;  // NZ = columns of the z stage, NX = of the x stage
+  int Rz, Rx, pzh, pxh;           // radix of each stage's split, output rows per half
+  int nxE, nxO;                   // x modes of even / odd j
+  int KTzE, KTz, KTxE, KTx;       // k-tiles of the even class, and in all
+  int MTz, MTx, KSz, KSx, NZ, NX;  // NZ = columns of the z stage, NX = of the x stage
 };
 
 __host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g) {
   PhysTcDims d;
-  d.KTz = (2 * (g.Nz - 1) + 15) / 16;
-  d.KTx = (2 * g.X + 15) / 16;
-  d.MTz = (2 * g.pz + 15) / 16;
-  d.MTx = (g.px + 15) / 16;
+  d.Rz = g.pz % 2 ? 1 : 2;
+  d.Rx = g.px % 2 ? 1 : 2;
+  d.pzh = g.pz / d.Rz;
+  d.pxh = g.px / d.Rx;
+  int nzE, nzO;
+  z_class_counts(g.Nz, g.pz, nzE, nzO);
+  d.nxE = (g.X + d.Rx - 1) / d.Rx;
+  d.nxO = g.X - d.nxE;
+  d.KTzE = (2 * nzE + 15) / 16;
+  d.KTz = d.KTzE + (2 * nzO + 15) / 16;
+  d.KTxE = (2 * d.nxE + 15) / 16;
+  d.KTx = d.KTxE + (2 * d.nxO + 15) / 16;
+  d.MTz = (2 * d.pzh + 15) / 16;
+  d.MTx = (d.pxh + 15) / 16;
   d.KSz = d.KTz * 16 + 8;
   d.KSx = d.KTx * 16 + 8;
   d.NZ = kFB * g.X;
@@ -135,6 +213,54 @@ size_t phys_tc_smem_bytes(const Grid& g, bool with_cfl) {
   b += (size_t)kFB * g.pz * g.X * sizeof(cpx);                 // Z intermediate
   (void)with_cfl;  // the CFL number is read back from the written fields
   return b;
+}
+
+// One exact digit GEMM tile of a fixed table A (fragment order
+// [mt][KT][7][32][4]) against the smem digits of column n, over the k-tiles
+// [k0, k1): FP32 level sums per chunk of at most 7 k-tiles (exact), folded
+// into the 64-bit integers H, L per accumulator element (exact across
+// chunks: |H| < 2^41, |L| < 2^50 per chunk); an empty range gives zeros
+__device__ __forceinline__ void tc_tile_range(const uint4* __restrict__ A, int mt, int KT, int k0, int k1,
+                                              const uint16_t* dig, size_t KS, size_t dstride, int n, int lane, int t,
+                                              long long (&H)[4], long long (&L)[4]) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) { H[r] = 0; L[r] = 0; }
+  for (int kc = k0; kc < k1; kc += kChunkKT) {
+    float acc[kDig][4];
+#pragma unroll
+    for (int l = 0; l < kDig; ++l)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+    const int kend = min(k1, kc + kChunkKT);
+    for (int kt = kc; kt < kend; ++kt) {
+      const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
+      uint32_t b0[kDig], b1[kDig];
+#pragma unroll
+      for (int k = 0; k < kDig; ++k) {
+        b0[k] = brow[(size_t)k * dstride / 2 + t];
+        b1[k] = brow[(size_t)k * dstride / 2 + t + 4];
+      }
+#pragma unroll
+      for (int i = 0; i < kDig; ++i) {
+        const uint4 af = __ldg(&A[(((size_t)mt * KT + kt) * kDig + i) * 32 + lane]);
+#pragma unroll
+        for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      long long h, l;
+      fold_levels(acc, r, h, l);
+      H[r] += h;
+      L[r] += l;
+    }
+  }
+}
+
+__device__ __forceinline__ void tc_tile(const uint4* __restrict__ A, int mt, int KT, const uint16_t* dig, size_t KS,
+                                        size_t dstride, int n, int lane, int t, long long (&H)[4],
+                                        long long (&L)[4]) {
+  tc_tile_range(A, mt, KT, 0, KT, dig, KS, dstride, n, lane, t, H, L);
 }
 
 // ---------------------------------------------------------------------------
@@ -167,7 +293,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
   bool nonfinite = false;
   for (int f0 = 0; f0 < a.nfields; f0 += kFB) {
     const int nfb = min(kFB, a.nfields - f0);
-    // ---- z stage: columns n = fl * X + x, K = 2 Kk (Re, Im interleaved)
+    // ---- z stage: columns n = fl * X + x
     for (int i = threadIdx.x; i < d.NZ; i += blockDim.x) exz[i] = 0;
     __syncthreads();
     // the inputs are staged in the Z buffer (free until the z stage writes it:
@@ -184,75 +310,53 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
     }
     __syncthreads();
     {
+      // K words (Re, Im of one mode): the even-zp modes, then the odd ones
+      const int KW = d.KTz * 8;
       const size_t zstride = (size_t)((d.NZ + 7) / 8 * 8) * d.KSz / 2;  // words between digits
       uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
-      for (int i = threadIdx.x; i < d.NZ * d.KTz * 8; i += blockDim.x) {
-        const int n = i / (d.KTz * 8), kk = i - n * (d.KTz * 8);
+      for (int i = threadIdx.x; i < d.NZ * KW; i += blockDim.x) {
+        const int n = i / KW, w = i - n * KW;
+        const int kk = g.tcZM[w];
         cpx v = {0.0, 0.0};
-        if (kk < Kk && n < nfb * g.X) v = Fin[n * Kk + kk];
+        if (kk >= 0 && n < nfb * g.X) v = Fin[n * Kk + kk];
         const int ex = exz[n] - 1022;
-        digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSz) / 2 + kk, zstride);
+        digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSz) / 2 + w, zstride);
       }
     }
     __syncthreads();
     {
+      // rows Re Z[m], Im Z[m] for m < pzh; E + O -> Z[m], E - O -> Z[m + pzh]
       const int NT = (nfb * g.X + 7) / 8;
       const size_t dstride = (size_t)((d.NZ + 7) / 8 * 8) * d.KSz;  // bf16 between digits
       for (int item = warp; item < d.MTz * NT; item += nwarp) {
         const int mt = item / NT, nt = item - mt * NT;
         const int n = nt * 8 + gq;
-        float acc[kDig][4];
-        double part[4] = {0.0, 0.0, 0.0, 0.0};
-        long long H[4], L[4];
-        for (int kc = 0; kc < d.KTz; kc += kChunkKT) {
-#pragma unroll
-          for (int l = 0; l < kDig; ++l)
-#pragma unroll
-            for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
-          const int kend = min(d.KTz, kc + kChunkKT);
-          for (int kt = kc; kt < kend; ++kt) {
-            const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * d.KSz + kt * 16);
-            uint32_t b0[kDig], b1[kDig];
-#pragma unroll
-            for (int k = 0; k < kDig; ++k) {
-              b0[k] = brow[(size_t)k * dstride / 2 + t];
-              b1[k] = brow[(size_t)k * dstride / 2 + t + 4];
-            }
-#pragma unroll
-            for (int i = 0; i < kDig; ++i) {
-              const uint4 af = __ldg(&Az[(((size_t)mt * d.KTz + kt) * kDig + i) * 32 + lane]);
-#pragma unroll
-              for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
-            }
-          }
-#pragma unroll
-          for (int r = 0; r < 4; ++r) fold_levels(acc, r, H[r], L[r]);
-          if (kend < d.KTz) {
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-              const int row = min(mt * 16 + gq + 8 * (r >> 1), 2 * g.pz - 1);
-              const int col = min(nt * 8 + 2 * t + (r & 1), d.NZ - 1);
-              part[r] += round_scaled(H[r], L[r], g.tcZE[row] + exz[col] - 1022 - 64);
-            }
-          }
-        }
+        long long HE[4], LE[4], HO[4], LO[4];
+        tc_tile_range(Az, mt, d.KTz, 0, d.KTzE, dig, d.KSz, dstride, n, lane, t, HE, LE);
+        tc_tile_range(Az, mt, d.KTz, d.KTzE, d.KTz, dig, d.KSz, dstride, n, lane, t, HO, LO);
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int row = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
-          if (row >= 2 * g.pz || col >= nfb * g.X) continue;
-          double v = round_fast(H[r], L[r], g.tcZE[row] + exz[col] - 1022 - 64);
-          if (d.KTz > kChunkKT) v += part[r];
-          const int fl = col / g.X, x = col - fl * g.X;
-          const int m = row < g.pz ? row : row - g.pz;
-          cpx& zr = Zb[((size_t)fl * g.pz + m) * g.X + x];
-          if (row < g.pz) zr.re = v;
-          else zr.im = v;
+          if (row >= 2 * d.pzh || col >= nfb * g.X) continue;
+          const int e = g.tcZE[row] + exz[col] - 1022 - 64;
+          const bool im = row >= d.pzh;
+          const int m = im ? row - d.pzh : row, fl = col / g.X, x = col - fl * g.X;
+          const double vp = round_fast(HE[r] + HO[r], LE[r] + LO[r], e);
+          cpx& zp = Zb[((size_t)fl * g.pz + m) * g.X + x];
+          if (im) zp.im = vp;
+          else zp.re = vp;
+          if (d.Rz == 2) {
+            const double vm = round_fast(HE[r] - HO[r], LE[r] - LO[r], e);
+            cpx& zm = Zb[((size_t)fl * g.pz + m + d.pzh) * g.X + x];
+            if (im) zm.im = vm;
+            else zm.re = vm;
+          }
         }
       }
     }
     __syncthreads();
-    // ---- x stage, one field at a time: columns n = m, K = 2X (Re, Im of
-    // Z[m][j]; Im of j = 0 unused)
+    // ---- x stage, one field at a time: columns n = m, K words: Re, Im of
+    // Z[m][j] for the even j, then the odd j (Im of j = 0 unused)
     const size_t xstride = (size_t)((g.pz + 7) / 8 * 8) * d.KSx;
     for (int fl = 0; fl < nfb; ++fl) {
       const cpx* Zf = Zb + (size_t)fl * g.pz * g.X;
@@ -268,65 +372,41 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
       __syncthreads();
       {
         uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
-        const int npad = (g.pz + 7) / 8 * 8;
-        for (int i = threadIdx.x; i < npad * d.KTx * 8; i += blockDim.x) {
-          const int n = i / (d.KTx * 8), j = i - n * (d.KTx * 8);
+        const int npad = (g.pz + 7) / 8 * 8, KW = d.KTx * 8, WE = d.KTxE * 8;
+        for (int i = threadIdx.x; i < npad * KW; i += blockDim.x) {
+          const int n = i / KW, w = i - n * KW;
+          const int j = w < WE ? (w < d.nxE ? d.Rx * w : -1) : (w - WE < d.nxO ? 2 * (w - WE) + 1 : -1);
           cpx v = {0.0, 0.0};
-          if (j < g.X && n < g.pz) v = Zf[(size_t)n * g.X + j];
+          if (j >= 0 && n < g.pz) v = Zf[(size_t)n * g.X + j];
           if (j == 0) v.im = 0.0;
           const int ex = exx[min(n, g.pz - 1)] - 1022;
-          digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSx) / 2 + j, xstride / 2);
+          digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSx) / 2 + w, xstride / 2);
         }
       }
       __syncthreads();
       {
+        // rows xp < pxh; E + O -> P[xp], E - O -> P[xp + pxh]
         const int NT = (g.pz + 7) / 8;
         for (int item = warp; item < d.MTx * NT; item += nwarp) {
           const int mt = item / NT, nt = item - mt * NT;
           const int n = nt * 8 + gq;
-          float acc[kDig][4];
-          double part[4] = {0.0, 0.0, 0.0, 0.0};
-          long long H[4], L[4];
-          for (int kc = 0; kc < d.KTx; kc += kChunkKT) {
-#pragma unroll
-            for (int l = 0; l < kDig; ++l)
-#pragma unroll
-              for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
-            const int kend = min(d.KTx, kc + kChunkKT);
-            for (int kt = kc; kt < kend; ++kt) {
-              const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * d.KSx + kt * 16);
-              uint32_t b0[kDig], b1[kDig];
-#pragma unroll
-              for (int k = 0; k < kDig; ++k) {
-                b0[k] = brow[(size_t)k * xstride / 2 + t];
-                b1[k] = brow[(size_t)k * xstride / 2 + t + 4];
-              }
-#pragma unroll
-              for (int i = 0; i < kDig; ++i) {
-                const uint4 af = __ldg(&Ax[(((size_t)mt * d.KTx + kt) * kDig + i) * 32 + lane]);
-#pragma unroll
-                for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
-              }
-            }
-#pragma unroll
-            for (int r = 0; r < 4; ++r) fold_levels(acc, r, H[r], L[r]);
-            if (kend < d.KTx) {
-#pragma unroll
-              for (int r = 0; r < 4; ++r) {
-                const int row = min(mt * 16 + gq + 8 * (r >> 1), g.px - 1);
-                const int col = min(nt * 8 + 2 * t + (r & 1), g.pz - 1);
-                part[r] += round_scaled(H[r], L[r], g.tcXE[row] + exx[col] - 1022 - 64);
-              }
-            }
-          }
+          long long HE[4], LE[4], HO[4], LO[4];
+          tc_tile_range(Ax, mt, d.KTx, 0, d.KTxE, dig, d.KSx, xstride, n, lane, t, HE, LE);
+          tc_tile_range(Ax, mt, d.KTx, d.KTxE, d.KTx, dig, d.KSx, xstride, n, lane, t, HO, LO);
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
             const int xp = mt * 16 + gq + 8 * (r >> 1), m = nt * 8 + 2 * t + (r & 1);
-            if (xp >= g.px || m >= g.pz) continue;
-            double v = round_fast(H[r], L[r], g.tcXE[xp] + exx[m] - 1022 - 64);
-            if (d.KTx > kChunkKT) v += part[r];
-            P[((size_t)(f0 + fl) * g.Q + y) * plane + (size_t)m * g.px + xp] = v;
-            nonfinite |= !finite_bits(v);
+            if (xp >= d.pxh || m >= g.pz) continue;
+            const int e = g.tcXE[xp] + exx[m] - 1022 - 64;
+            double* Pr = P + ((size_t)(f0 + fl) * g.Q + y) * plane + (size_t)m * g.px;
+            const double vp = round_fast(HE[r] + HO[r], LE[r] + LO[r], e);
+            Pr[xp] = vp;
+            nonfinite |= !finite_bits(vp);
+            if (d.Rx == 2) {
+              const double vm = round_fast(HE[r] - HO[r], LE[r] - LO[r], e);
+              Pr[xp + d.pxh] = vm;
+              nonfinite |= !finite_bits(vm);
+            }
           }
         }
       }
@@ -391,48 +471,6 @@ size_t fwd_tc_smem_bytes(const Grid& g) {
   b += ((stage > yb ? stage : yb) + 15) / 16 * 16;
   b += (size_t)d.Kk * g.X * sizeof(cpx);
   return b;
-}
-
-// One exact digit GEMM tile of a fixed table A (fragment order
-// [mt][KT][7][32][4]) against the smem digits of column n, over all KT
-// k-tiles: FP32 level sums per chunk of at most 7 k-tiles (exact), folded
-// into the 64-bit integers H, L per accumulator element (exact across
-// chunks: |H| < 2^41, |L| < 2^50 per chunk)
-__device__ __forceinline__ void tc_tile(const uint4* __restrict__ A, int mt, int KT, const uint16_t* dig, size_t KS,
-                                        size_t dstride, int n, int lane, int t, long long (&H)[4],
-                                        long long (&L)[4]) {
-#pragma unroll
-  for (int r = 0; r < 4; ++r) { H[r] = 0; L[r] = 0; }
-  for (int kc = 0; kc < KT; kc += kChunkKT) {
-    float acc[kDig][4];
-#pragma unroll
-    for (int l = 0; l < kDig; ++l)
-#pragma unroll
-      for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
-    const int kend = min(KT, kc + kChunkKT);
-    for (int kt = kc; kt < kend; ++kt) {
-      const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
-      uint32_t b0[kDig], b1[kDig];
-#pragma unroll
-      for (int k = 0; k < kDig; ++k) {
-        b0[k] = brow[(size_t)k * dstride / 2 + t];
-        b1[k] = brow[(size_t)k * dstride / 2 + t + 4];
-      }
-#pragma unroll
-      for (int i = 0; i < kDig; ++i) {
-        const uint4 af = __ldg(&A[(((size_t)mt * KT + kt) * kDig + i) * 32 + lane]);
-#pragma unroll
-        for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      long long h, l;
-      fold_levels(acc, r, h, l);
-      H[r] += h;
-      L[r] += l;
-    }
-  }
 }
 
 // The products of one plane (mode 0 primal, 1 tangent, 2 adjoint S and T,

@@ -43,7 +43,7 @@ bool build_recon_tc_tables(const HostTables& h, std::vector<uint32_t>& frag, std
                            std::vector<uint32_t>& wfrag, std::vector<int>& wex);
 // DFT matrices of the inverse z and x transforms as digit tables (phys_tc.cu)
 bool build_phys_tc_tables(const HostTables& h, std::vector<uint32_t>& zfrag, std::vector<int>& zex,
-                          std::vector<uint32_t>& xfrag, std::vector<int>& xex);
+                          std::vector<uint32_t>& xfrag, std::vector<int>& xex, std::vector<int>& zmap);
 // DFT matrices of the forward x and z transforms as digit tables (phys_tc.cu)
 bool build_fwd_tc_tables(const HostTables& h, std::vector<uint32_t>& xfrag, std::vector<int>& xex,
                          std::vector<uint32_t>& zfrag, std::vector<int>& zex, std::vector<uint32_t>& ufrag,
