@@ -194,7 +194,7 @@ __host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g) {
   d.KSz = d.KTz * 16 + 8;
   d.KSx = d.KTx * 16 + 8;
   d.NZ = kFB * g.X;
-  d.NX = g.pz;  // the x stage runs one field at a time
+  d.NX = kFB * g.pz;  // the x stage: one column per (field, m)
   return d;
 }
 
@@ -291,22 +291,31 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
   const int nwarp = blockDim.x >> 5;
   const int Kk = g.Nz - 1;  // kept kz rows
   bool nonfinite = false;
+  for (int i = threadIdx.x; i < d.NZ; i += blockDim.x) exz[i] = 0;
+  __syncthreads();
   for (int f0 = 0; f0 < a.nfields; f0 += kFB) {
     const int nfb = min(kFB, a.nfields - f0);
-    // ---- z stage: columns n = fl * X + x
-    for (int i = threadIdx.x; i < d.NZ; i += blockDim.x) exz[i] = 0;
-    __syncthreads();
-    // the inputs are staged in the Z buffer (free until the z stage writes it:
-    // X (Nz - 1) <= pz X values per field)
+    // ---- z stage: columns n = fl * X + x.  The inputs are staged in the Z
+    // buffer (free until the z stage writes it: X (Nz - 1) <= pz X values per
+    // field); each thread keeps one column (consecutive threads: consecutive
+    // x, coalesced loads) and its exponent maximum.  The x stage's column
+    // exponents are cleared here and gathered by the z stage's epilogue.
     cpx* Fin = Zb;  // [n][kk]
-    for (int i = threadIdx.x; i < nfb * g.X * Kk; i += blockDim.x) {
-      const int n = i / Kk, kk = i - n * Kk, fl = n / g.X, x = n - fl * g.X;
-      const int z = kk < g.Nz / 2 ? kk : kk + 1;
-      const cpx v = field_value(g, U, f0 + fl, z, y, x);
-      Fin[i] = v;
-      const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
-                        (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
-      if (e) atomicMax(&exz[n], e);
+    for (int i = threadIdx.x; i < d.NX; i += blockDim.x) exx[i] = 0;
+    {
+      const int ncol = nfb * g.X, per = blockDim.x / ncol;
+      if ((int)threadIdx.x < per * ncol) {
+        const int n = threadIdx.x % ncol, fl = n / g.X, x = n - fl * g.X;
+        int emax = 0;
+        for (int kk = threadIdx.x / ncol; kk < Kk; kk += per) {
+          const int z = kk < g.Nz / 2 ? kk : kk + 1;
+          const cpx v = field_value(g, U, f0 + fl, z, y, x);
+          Fin[(size_t)n * Kk + kk] = v;
+          emax = max(emax, max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
+                               (int)((__double_as_longlong(v.im) >> 52) & 0x7FF)));
+        }
+        if (emax) atomicMax(&exz[n], emax);
+      }
     }
     __syncthreads();
     {
@@ -325,7 +334,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
     }
     __syncthreads();
     {
-      // rows Re Z[m], Im Z[m] for m < pzh; E + O -> Z[m], E - O -> Z[m + pzh]
+      // rows Re Z[m], Im Z[m] for m < pzh; E + O -> Z[m], E - O -> Z[m + pzh];
+      // the exponent of each value into its x-stage column (fl, m) (not the
+      // imaginary part of the kx = 0 bin, which c2r ignores)
       const int NT = (nfb * g.X + 7) / 8;
       const size_t dstride = (size_t)((d.NZ + 7) / 8 * 8) * d.KSz;  // bf16 between digits
       for (int item = warp; item < d.MTz * NT; item += nwarp) {
@@ -341,77 +352,73 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
           const int e = g.tcZE[row] + exz[col] - 1022 - 64;
           const bool im = row >= d.pzh;
           const int m = im ? row - d.pzh : row, fl = col / g.X, x = col - fl * g.X;
+          const bool counts = !(im && x == 0);
           const double vp = round_fast(HE[r] + HO[r], LE[r] + LO[r], e);
           cpx& zp = Zb[((size_t)fl * g.pz + m) * g.X + x];
           if (im) zp.im = vp;
           else zp.re = vp;
+          const int ep = (int)((__double_as_longlong(vp) >> 52) & 0x7FF);
+          if (counts && ep) atomicMax(&exx[fl * g.pz + m], ep);
           if (d.Rz == 2) {
             const double vm = round_fast(HE[r] - HO[r], LE[r] - LO[r], e);
             cpx& zm = Zb[((size_t)fl * g.pz + m + d.pzh) * g.X + x];
             if (im) zm.im = vm;
             else zm.re = vm;
+            const int em = (int)((__double_as_longlong(vm) >> 52) & 0x7FF);
+            if (counts && em) atomicMax(&exx[fl * g.pz + m + d.pzh], em);
           }
         }
       }
     }
     __syncthreads();
-    // ---- x stage, one field at a time: columns n = m, K words: Re, Im of
-    // Z[m][j] for the even j, then the odd j (Im of j = 0 unused)
-    const size_t xstride = (size_t)((g.pz + 7) / 8 * 8) * d.KSx;
-    for (int fl = 0; fl < nfb; ++fl) {
-      const cpx* Zf = Zb + (size_t)fl * g.pz * g.X;
-      for (int i = threadIdx.x; i < g.pz; i += blockDim.x) exx[i] = 0;
-      __syncthreads();
-      for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x) {
-        const int n = i / g.X, j = i - n * g.X;
-        const cpx v = Zf[i];
-        const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
-                          j ? (int)((__double_as_longlong(v.im) >> 52) & 0x7FF) : 0);
-        if (e) atomicMax(&exx[n], e);
+    // ---- x stage, both fields: columns n = fl * pz + m, K words: Re, Im of
+    // Z[m][j] for the even j, then the odd j (Im of j = 0 unused).  The z
+    // stage's column exponents are cleared for the next pass.
+    const int ncx = nfb * g.pz;
+    const size_t xstride = (size_t)((d.NX + 7) / 8 * 8) * d.KSx;
+    for (int i = threadIdx.x; i < d.NZ; i += blockDim.x) exz[i] = 0;
+    {
+      uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
+      const int npad = (ncx + 7) / 8 * 8, KW = d.KTx * 8, WE = d.KTxE * 8;
+      for (int i = threadIdx.x; i < npad * KW; i += blockDim.x) {
+        const int n = i / KW, w = i - n * KW;
+        const int j = w < WE ? (w < d.nxE ? d.Rx * w : -1) : (w - WE < d.nxO ? 2 * (w - WE) + 1 : -1);
+        cpx v = {0.0, 0.0};
+        if (j >= 0 && n < ncx) v = Zb[(size_t)n * g.X + j];
+        if (j == 0) v.im = 0.0;
+        const int ex = exx[min(n, ncx - 1)] - 1022;
+        digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSx) / 2 + w, xstride / 2);
       }
-      __syncthreads();
-      {
-        uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
-        const int npad = (g.pz + 7) / 8 * 8, KW = d.KTx * 8, WE = d.KTxE * 8;
-        for (int i = threadIdx.x; i < npad * KW; i += blockDim.x) {
-          const int n = i / KW, w = i - n * KW;
-          const int j = w < WE ? (w < d.nxE ? d.Rx * w : -1) : (w - WE < d.nxO ? 2 * (w - WE) + 1 : -1);
-          cpx v = {0.0, 0.0};
-          if (j >= 0 && n < g.pz) v = Zf[(size_t)n * g.X + j];
-          if (j == 0) v.im = 0.0;
-          const int ex = exx[min(n, g.pz - 1)] - 1022;
-          digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSx) / 2 + w, xstride / 2);
-        }
-      }
-      __syncthreads();
-      {
-        // rows xp < pxh; E + O -> P[xp], E - O -> P[xp + pxh]
-        const int NT = (g.pz + 7) / 8;
-        for (int item = warp; item < d.MTx * NT; item += nwarp) {
-          const int mt = item / NT, nt = item - mt * NT;
-          const int n = nt * 8 + gq;
-          long long HE[4], LE[4], HO[4], LO[4];
-          tc_tile_range(Ax, mt, d.KTx, 0, d.KTxE, dig, d.KSx, xstride, n, lane, t, HE, LE);
-          tc_tile_range(Ax, mt, d.KTx, d.KTxE, d.KTx, dig, d.KSx, xstride, n, lane, t, HO, LO);
+    }
+    __syncthreads();
+    {
+      // rows xp < pxh; E + O -> P[xp], E - O -> P[xp + pxh]
+      const int NT = (ncx + 7) / 8;
+      for (int item = warp; item < d.MTx * NT; item += nwarp) {
+        const int mt = item / NT, nt = item - mt * NT;
+        const int n = nt * 8 + gq;
+        long long HE[4], LE[4], HO[4], LO[4];
+        tc_tile_range(Ax, mt, d.KTx, 0, d.KTxE, dig, d.KSx, xstride, n, lane, t, HE, LE);
+        tc_tile_range(Ax, mt, d.KTx, d.KTxE, d.KTx, dig, d.KSx, xstride, n, lane, t, HO, LO);
 #pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            const int xp = mt * 16 + gq + 8 * (r >> 1), m = nt * 8 + 2 * t + (r & 1);
-            if (xp >= d.pxh || m >= g.pz) continue;
-            const int e = g.tcXE[xp] + exx[m] - 1022 - 64;
-            double* Pr = P + ((size_t)(f0 + fl) * g.Q + y) * plane + (size_t)m * g.px;
-            const double vp = round_fast(HE[r] + HO[r], LE[r] + LO[r], e);
-            Pr[xp] = vp;
-            nonfinite |= !finite_bits(vp);
-            if (d.Rx == 2) {
-              const double vm = round_fast(HE[r] - HO[r], LE[r] - LO[r], e);
-              Pr[xp + d.pxh] = vm;
-              nonfinite |= !finite_bits(vm);
-            }
+        for (int r = 0; r < 4; ++r) {
+          const int xp = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
+          if (xp >= d.pxh || col >= ncx) continue;
+          const int fl = col / g.pz, m = col - fl * g.pz;
+          const int e = g.tcXE[xp] + exx[col] - 1022 - 64;
+          double* Pr = P + ((size_t)(f0 + fl) * g.Q + y) * plane + (size_t)m * g.px;
+          const double vp = round_fast(HE[r] + HO[r], LE[r] + LO[r], e);
+          Pr[xp] = vp;
+          nonfinite |= !finite_bits(vp);
+          if (d.Rx == 2) {
+            const double vm = round_fast(HE[r] - HO[r], LE[r] - LO[r], e);
+            Pr[xp + d.pxh] = vm;
+            nonfinite |= !finite_bits(vm);
           }
         }
       }
-      __syncthreads();
     }
+    __syncthreads();
   }
   if (nonfinite && a.status) atomicOr(&a.status[inst / a.sdiv], ST_NONFINITE);
   if (a.cfl_check) {
@@ -614,8 +621,9 @@ cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaS
 }
 
 bool phys_tc_fits(const Grid& g, int optin) {
-  // the kernel's static shared memory (reduction, staged grid) is below 4 KB
-  return phys_tc_smem_bytes(g, true) + 4096 <= (size_t)optin;
+  // the kernel's static shared memory (reduction, staged grid) is below 4 KB;
+  // the input staging keeps one thread per z-stage column
+  return kFB * g.X <= kThreads && phys_tc_smem_bytes(g, true) + 4096 <= (size_t)optin;
 }
 
 // Two builds of the kernel: for 2 blocks per SM (128 registers) and for 3
