@@ -58,29 +58,28 @@ __device__ __forceinline__ cpx band_matvecT_row(const double* __restrict__ A, in
 
 // A^T y = b for one parity chain, A = L U the no-pivot factors of
 // channel/mvOps.c:29-91 (L unit lower in columns j < dl, U in dl..dl+du):
-// U^T w = b ascending, then L^T y = w descending
-__device__ void band_solveT_chain(const double* __restrict__ LU, int w, int dl, int du, int N, int par, double* b,
-                                  int bstride) {
+// U^T w = b ascending, then L^T y = w descending; RD the reciprocal pivots
+// (the forward chain multiplies by them too)
+template <int W, int DL, int DU>
+__device__ void band_solveT_chain(const double* __restrict__ LU, const double* __restrict__ RD, int N, int par,
+                                  double* b, int bstride) {
   for (int i = par; i < N; i += 2) {
     double acc = b[i * bstride];
-    for (int j = 1; j <= du; ++j) {
+#pragma unroll
+    for (int j = 1; j <= DU; ++j) {
       const int m = i - 2 * j;
-      if (m < 0) break;
-      int jm = (N - m + 1) / 2 - 1;
-      if (jm > du) jm = du;
-      if (j > jm) continue;
-      acc = fma(-__ldg(LU + (size_t)m * w + dl + j), b[m * bstride], acc);
+      // row m of U holds column i when m >= 0 and j <= min(DU, (N - m + 1) / 2 - 1)
+      if (m >= 0 && j <= (N - m + 1) / 2 - 1) acc = fma(-__ldg(LU + (size_t)m * W + DL + j), b[m * bstride], acc);
     }
-    b[i * bstride] = acc / __ldg(LU + (size_t)i * w + dl);
+    b[i * bstride] = acc * __ldg(RD + i);
   }
   const int ilast = ((N - 1 - par) % 2 == 0) ? N - 1 : N - 2;
   for (int i = ilast; i >= 0; i -= 2) {
     double acc = b[i * bstride];
-    for (int t = 1; t <= dl; ++t) {
+#pragma unroll
+    for (int t = 1; t <= DL; ++t) {
       const int m = i + 2 * t;
-      if (m >= N) break;
-      if (t > m / 2) continue;
-      acc = fma(-__ldg(LU + (size_t)m * w + dl - t), b[m * bstride], acc);
+      if (m < N && t <= m / 2) acc = fma(-__ldg(LU + (size_t)m * W + DL - t), b[m * bstride], acc);
     }
     b[i * bstride] = acc;
   }
@@ -346,11 +345,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
       const size_t zx = (size_t)z * g.X + x0 + l;
       const int par = ch & 1, part = (ch >> 1) & 1;
       if (ch < 4)
-        band_solveT_chain(g.luA + ((size_t)bidx * g.Nz * g.X + zx) * g.D * 9, 9, 4, 4, g.D, par,
-                          reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
+        band_solveT_chain<9, 4, 4>(g.luA + ((size_t)bidx * g.Nz * g.X + zx) * g.D * 9,
+                                   g.rdA + ((size_t)bidx * g.Nz * g.X + zx) * g.D, g.D, par,
+                                   reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
       else
-        band_solveT_chain(g.luB + ((size_t)bidx * g.Nz * g.X + zx) * g.R * 5, 5, 2, 2, g.R, par,
-                          reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
+        band_solveT_chain<5, 2, 2>(g.luB + ((size_t)bidx * g.Nz * g.X + zx) * g.R * 5,
+                                   g.rdB + ((size_t)bidx * g.Nz * g.X + zx) * g.R, g.R, par,
+                                   reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
     }
   }
   __syncthreads();
@@ -412,8 +413,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
     __syncwarp();
     if (lane < 8) {
       const int par = lane & 1, pt = (lane >> 1) & 1;
-      band_solveT_chain(g.lu0 + (size_t)bidx * g.R * 5, 5, 2, 2, g.R, par,
-                        reinterpret_cast<double*>(lane < 4 ? ca : cb) + pt, 2);
+      band_solveT_chain<5, 2, 2>(g.lu0 + (size_t)bidx * g.R * 5, g.rd0 + (size_t)bidx * g.R, g.R, par,
+                                 reinterpret_cast<double*>(lane < 4 ? ca : cb) + pt, 2);
     }
     __syncwarp();
     for (int i = lane; i < g.R; i += 32) {

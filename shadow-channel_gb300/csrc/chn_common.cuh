@@ -72,6 +72,9 @@ struct Grid {
   const double* exB;     // [2][Nz][X][R][5]
   // mean-flow (kx,kz) = (0,0) systems on the R basis
   const double* lu0;     // [3][R][5]   Rs + re b dt Rps, LU factors
+  const double* rdA;     // [3][Nz][X][D] reciprocal pivots of luA (centre column)
+  const double* rdB;     // [3][Nz][X][R] of luB
+  const double* rd0;     // [3][R]        of lu0
   const double* ex0;     // [2][R][5]   Rs - re a dt Rps
   const double* add0;    // [4][R]      flux-correction vectors: [0] forward, [1+bidx] adjoint
   const double* rwsum;   // [R]         sum_j Rw[i][j]

@@ -134,7 +134,8 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
             T.up(h.Wrp, &g.Wrp) && T.up(h.luA, &g.luA) && T.up(h.luB, &g.luB) && T.up(h.exA, &g.exA) &&
             T.up(h.exB, &g.exB) && T.up(h.lu0, &g.lu0) && T.up(h.ex0, &g.ex0) && T.up(h.add0, &g.add0) &&
             T.up(h.rwsum, &g.rwsum) && T.up(h.Qs, &g.Qs) && T.up(h.Qps, &g.Qps) && T.up(h.Qpps, &g.Qpps) &&
-            T.up(h.Rs, &g.Rs) && T.up(h.Rps, &g.Rps);
+            T.up(h.Rs, &g.Rs) && T.up(h.Rps, &g.Rps) && T.up(h.rdA, &g.rdA) && T.up(h.rdB, &g.rdB) &&
+            T.up(h.rd0, &g.rd0);
   if (!ok) return false;
   const double* tz;
   const double* tx;
@@ -187,7 +188,7 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   const char* tfp64 = getenv("CHN_TRANSFORMS_FP64");
   g.tci = (!(tfp64 && tfp64[0] == '1') && phys_tc_fits(g, optin)) ? 1 : 0;
   g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_fits(g, optin)) ? 1 : 0;
-  g.tcminb = 3;  // until the autotuner has timed both builds
+  g.tcminb = 2;  // until the autotuner has timed both builds (3 blocks rarely fit the shared memory)
   if (solve_smem_bytes(g) > (size_t)optin || recon_smem_bytes(g) > (size_t)optin) {
     set_error(1, "grid %dx%dx%d: the implicit solve needs %zu bytes of shared memory per block, the device has %d",
               Nx, Ny, Nz, solve_smem_bytes(g), optin);

@@ -510,27 +510,31 @@ __device__ __forceinline__ cpx band_matvec_row(const double* __restrict__ A, int
 }
 
 // one elimination chain (fixed parity, real or imaginary part) of the
-// no-pivot every-other-diagonal LU solve (channel/mvOps.c:29-91)
-__device__ void band_solve_chain(const double* __restrict__ LU, int w, int dl, int du, int N, int par,
+// no-pivot every-other-diagonal LU solve (channel/mvOps.c:29-91); W, DL, DU
+// the band layout (width, lower, upper), RD the reciprocal pivots.  The band
+// loops are unrolled with per-row predicates, the multiply-adds in the
+// reference's order.
+template <int W, int DL, int DU>
+__device__ void band_solve_chain(const double* __restrict__ LU, const double* __restrict__ RD, int N, int par,
                                  double* b, int bstride) {
   for (int i = par; i < N; i += 2) {
     if (i < 2) continue;
-    int j0 = dl - i / 2;
-    if (j0 < 0) j0 = 0;
+    const int j0 = DL - i / 2;
     double acc = b[i * bstride];
-    for (int j = j0; j < dl; ++j) acc = fma(-__ldg(LU + (size_t)i * w + j), b[(i - 2 * (dl - j)) * bstride], acc);
+#pragma unroll
+    for (int j = 0; j < DL; ++j)
+      if (j >= j0) acc = fma(-__ldg(LU + (size_t)i * W + j), b[(i - 2 * (DL - j)) * bstride], acc);
     b[i * bstride] = acc;
   }
   // back substitution: the last row of this parity first
-  int ilast = ((N - 1 - par) % 2 == 0) ? N - 1 : N - 2;
+  const int ilast = ((N - 1 - par) % 2 == 0) ? N - 1 : N - 2;
   for (int i = ilast; i >= 0; i -= 2) {
     double acc = b[i * bstride];
-    if (i <= N - 3) {
-      int jm = (N - i + 1) / 2 - 1;
-      if (jm > du) jm = du;
-      for (int j = 1; j <= jm; ++j) acc = fma(-__ldg(LU + (size_t)i * w + dl + j), b[(i + 2 * j) * bstride], acc);
-    }
-    b[i * bstride] = acc / __ldg(LU + (size_t)i * w + dl);
+    const int jm = min(DU, (N - i + 1) / 2 - 1);  // no terms for i > N - 3
+#pragma unroll
+    for (int j = 1; j <= DU; ++j)
+      if (j <= jm) acc = fma(-__ldg(LU + (size_t)i * W + DL + j), b[(i + 2 * j) * bstride], acc);
+    b[i * bstride] = acc * __ldg(RD + i);
   }
 }
 
@@ -664,11 +668,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
         const size_t zx = (size_t)z * g.X + x0 + l;
         const int par = ch & 1, part = (ch >> 1) & 1;
         if (ch < 4)
-          band_solve_chain(g.luA + ((size_t)2 * g.Nz * g.X + zx) * g.D * 9, 9, 4, 4, g.D, par,
-                           reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
+          band_solve_chain<9, 4, 4>(g.luA + ((size_t)2 * g.Nz * g.X + zx) * g.D * 9,
+                                    g.rdA + ((size_t)2 * g.Nz * g.X + zx) * g.D, g.D, par,
+                                    reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
         else
-          band_solve_chain(g.luB + ((size_t)2 * g.Nz * g.X + zx) * g.R * 5, 5, 2, 2, g.R, par,
-                           reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
+          band_solve_chain<5, 2, 2>(g.luB + ((size_t)2 * g.Nz * g.X + zx) * g.R * 5,
+                                    g.rdB + ((size_t)2 * g.Nz * g.X + zx) * g.R, g.R, par,
+                                    reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
       }
     }
     __syncthreads();
@@ -746,11 +752,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
       const size_t zx = (size_t)z * g.X + x;
       const int par = ch & 1, part = (ch >> 1) & 1;
       if (ch < 4) {
-        const double* LU = g.luA + ((size_t)rk.bidx * g.Nz * g.X + zx) * g.D * 9;
-        band_solve_chain(LU, 9, 4, 4, g.D, par, reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
+        const size_t sys = (size_t)rk.bidx * g.Nz * g.X + zx;
+        band_solve_chain<9, 4, 4>(g.luA + sys * g.D * 9, g.rdA + sys * g.D, g.D, par,
+                                  reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
       } else {
-        const double* LU = g.luB + ((size_t)rk.bidx * g.Nz * g.X + zx) * g.R * 5;
-        band_solve_chain(LU, 5, 2, 2, g.R, par, reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
+        const size_t sys = (size_t)rk.bidx * g.Nz * g.X + zx;
+        band_solve_chain<5, 2, 2>(g.luB + sys * g.R * 5, g.rdB + sys * g.R, g.R, par,
+                                  reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
       }
     }
   }
@@ -776,8 +784,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
       __syncwarp();
       if (lane < 8) {
         const int par = lane & 1, part = (lane >> 1) & 1;
-        band_solve_chain(g.lu0 + (size_t)2 * g.R * 5, 5, 2, 2, g.R, par,
-                         reinterpret_cast<double*>(lane < 4 ? ca : cb) + part, 2);
+        band_solve_chain<5, 2, 2>(g.lu0 + (size_t)2 * g.R * 5, g.rd0 + (size_t)2 * g.R, g.R, par,
+                                  reinterpret_cast<double*>(lane < 4 ? ca : cb) + part, 2);
       }
       __syncwarp();
       for (int i = lane; i < g.R; i += 32) {
@@ -835,10 +843,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     }
     __syncwarp();
     if (lane < 8) {
-      const double* LU = g.lu0 + (size_t)rk.bidx * g.R * 5;
       const int par = lane & 1, part = (lane >> 1) & 1;
       cpx* vec = (lane < 4) ? ca : cb;
-      band_solve_chain(LU, 5, 2, 2, g.R, par, reinterpret_cast<double*>(vec) + part, 2);
+      band_solve_chain<5, 2, 2>(g.lu0 + (size_t)rk.bidx * g.R * 5, g.rd0 + (size_t)rk.bidx * g.R, g.R, par,
+                                reinterpret_cast<double*>(vec) + part, 2);
     }
     __syncwarp();
     // constant mass flux: a += 0.5 * flux_t * add (channel/project0.c:153-168)

@@ -297,6 +297,18 @@ bool build_tables(int Nx, int Ny, int Nz, double Lx, double Lz, double Re, doubl
     band_solve(A, 5, 2, 2, R, v.data());
     std::memcpy(&t.add0[(size_t)(1 + bi) * R], v.data(), sizeof(double) * R);
   }
+  // the back substitution multiplies by the pivot's reciprocal (one FP64
+  // rounding more than the reference's division, channel/mvOps.c:80-90)
+  auto recip = [](const std::vector<double>& lu, int w, int dl, std::vector<double>& rd) {
+    rd.assign(lu.size() / w, 0.0);
+    for (size_t r = 0; r < rd.size(); ++r) {
+      const double p = lu[r * w + dl];
+      rd[r] = p != 0.0 ? 1.0 / p : 0.0;
+    }
+  };
+  recip(t.luA, 9, 4, t.rdA);
+  recip(t.luB, 5, 2, t.rdB);
+  recip(t.lu0, 5, 2, t.rd0);
   {
     std::vector<double> A(t.Rs);
     band_lu(A.data(), 5, 2, 2, R);

@@ -23,6 +23,7 @@ struct HostTables {
   double cfl1, cfl3;
   std::vector<double> luA, luB, exA, exB;   // see Grid in chn_common.cuh
   std::vector<double> lu0, ex0, add0, rwsum;
+  std::vector<double> rdA, rdB, rd0;         // reciprocals of the LU pivots (0 where a pivot is 0)
   std::vector<double> twz, twx;             // interleaved re,im
 };
 
