@@ -340,7 +340,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
   __syncthreads();
   // L^{-T}: per column 4 chains for alpha, 4 for beta (parity x re/im)
   if (threadIdx.x < 8 * kTile) {
-    const int l = threadIdx.x / 8, ch = threadIdx.x % 8;
+    // threads [0, 4 kTile) run the alpha chains, [4 kTile, 8 kTile) the beta
+    // ones: a warp holds one system (no divergence between the two bands)
+    const int l = (threadIdx.x % (4 * kTile)) / 4, ch = 4 * (threadIdx.x / (4 * kTile)) + threadIdx.x % 4;
     if (l < nx && l >= xfirst) {
       const size_t zx = (size_t)z * g.X + x0 + l;
       const int par = ch & 1, part = (ch >> 1) & 1;

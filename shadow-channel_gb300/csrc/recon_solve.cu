@@ -443,17 +443,30 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
 #pragma unroll
           for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
         const int kend = min(KT, kc + kChunkKT);
+        // the weight fragments of k-tile kt + 1 load while kt's products run
+        // (the tables live in L2)
+        const uint4* Wm = W + (((size_t)w * MTw + mt) * KT) * kDig * 32 + lane;
+        uint4 af[kDig];
+#pragma unroll
+        for (int i = 0; i < kDig; ++i) af[i] = __ldg(Wm + ((size_t)kc * kDig + i) * 32);
         for (int kt = kc; kt < kend; ++kt) {
+          const int kn = min(kt + 1, kend - 1);
+          uint4 an[kDig];
+#pragma unroll
+          for (int i = 0; i < kDig; ++i) an[i] = __ldg(Wm + ((size_t)kn * kDig + i) * 32);
           const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
+          uint32_t b0[kDig], b1[kDig];
 #pragma unroll
-          for (int i = 0; i < kDig; ++i) {
-            const uint4 af = __ldg(&W[((((size_t)w * MTw + mt) * KT + kt) * kDig + i) * 32 + lane]);
-#pragma unroll
-            for (int k = 0; k < kDig - i; ++k) {
-              const uint32_t* row = brow + (size_t)k * 32 * KS / 2;
-              mma_bf16_16816(acc[i + k], af, row[t], row[t + 4]);
-            }
+          for (int k = 0; k < kDig; ++k) {
+            b0[k] = brow[(size_t)k * 32 * KS / 2 + t];
+            b1[k] = brow[(size_t)k * 32 * KS / 2 + t + 4];
           }
+#pragma unroll
+          for (int i = 0; i < kDig; ++i)
+#pragma unroll
+            for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af[i], b0[k], b1[k]);
+#pragma unroll
+          for (int i = 0; i < kDig; ++i) af[i] = an[i];
         }
 #pragma unroll
         for (int r = 0; r < 4; ++r) fold_levels(acc, r, Hh[r], Ll[r]);
@@ -663,7 +676,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     }
     __syncthreads();
     if (threadIdx.x < 8 * kTile) {  // mass matrices: the b = 0 factors
-      const int l = threadIdx.x / 8, ch = threadIdx.x % 8;
+      const int l = (threadIdx.x % (4 * kTile)) / 4, ch = 4 * (threadIdx.x / (4 * kTile)) + threadIdx.x % 4;
       if (l < nx && l >= xfirst) {
         const size_t zx = (size_t)z * g.X + x0 + l;
         const int par = ch & 1, part = (ch >> 1) & 1;
@@ -746,7 +759,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   __syncthreads();
   // banded solves: per column 4 chains for alpha, 4 for beta (parity x re/im)
   if (threadIdx.x < 8 * kTile) {
-    const int l = threadIdx.x / 8, ch = threadIdx.x % 8;
+    // threads [0, 4 kTile) run the alpha chains, [4 kTile, 8 kTile) the beta
+    // ones: a warp holds one system (no divergence between the two bands)
+    const int l = (threadIdx.x % (4 * kTile)) / 4, ch = 4 * (threadIdx.x / (4 * kTile)) + threadIdx.x % 4;
     if (l < nx && l >= xfirst) {
       const int x = x0 + l;
       const size_t zx = (size_t)z * g.X + x;
