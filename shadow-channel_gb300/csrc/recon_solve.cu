@@ -21,6 +21,7 @@ namespace chn {
 
 static constexpr int kThreads = 256;
 static constexpr int kTile = 16;   // kx columns per block
+static constexpr int kQuadRegs = 8;  // quadrature inputs a thread keeps in registers (Q <= 128)
 
 __device__ __forceinline__ bool blocked(const uint32_t* status, int sdiv, int inst) {
   return status != nullptr && (status[inst / sdiv] & ST_CFL) != 0;
@@ -412,21 +413,46 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
     const bool first = (q == 0 || q == 3);
     for (int i = threadIdx.x; i < kTile; i += blockDim.x) exc[i] = 0;
     __syncthreads();
-    for (int i = threadIdx.x; i < g.Q * kTile; i += blockDim.x) {
-      const int y = i / kTile, col = i - y * kTile;
-      if (col >= nx) continue;
-      const cpx v = input(q, y, col);
-      const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
-                        (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
-      if (e) atomicMax(&exc[col], e);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < KT * 16 * kTile; i += blockDim.x) {
-      const int y = i / kTile, col = i - y * kTile;
-      const cpx v = (y < g.Q && col < nx) ? input(q, y, col) : cpx{0.0, 0.0};
+    if (KT <= kQuadRegs && blockDim.x == 16 * kTile) {
+      // thread t holds column t % kTile, planes t / kTile + 16 k (k < KT):
+      // its inputs stay in registers from the exponent maximum to the digits
+      const int col = threadIdx.x % kTile, y0 = threadIdx.x / kTile;
+      cpx vin[kQuadRegs];
+      int emax = 0;
+#pragma unroll
+      for (int k = 0; k < kQuadRegs; ++k) {
+        const int y = y0 + 16 * k;
+        vin[k] = (k < KT && y < g.Q && col < nx) ? input(q, y, col) : cpx{0.0, 0.0};
+        emax = max(emax, max((int)((__double_as_longlong(vin[k].re) >> 52) & 0x7FF),
+                             (int)((__double_as_longlong(vin[k].im) >> 52) & 0x7FF)));
+      }
+      if (emax) atomicMax(&exc[col], emax);
+      __syncthreads();
       const int ex = exc[col] - 1022;
-      digits_bf16(scaled56(v.re, ex), dig + (size_t)(2 * col) * KS + y, 32 * KS);
-      digits_bf16(scaled56(v.im, ex), dig + (size_t)(2 * col + 1) * KS + y, 32 * KS);
+#pragma unroll
+      for (int k = 0; k < kQuadRegs; ++k) {
+        if (k >= KT) break;
+        const int y = y0 + 16 * k;
+        digits_bf16(scaled56(vin[k].re, ex), dig + (size_t)(2 * col) * KS + y, 32 * KS);
+        digits_bf16(scaled56(vin[k].im, ex), dig + (size_t)(2 * col + 1) * KS + y, 32 * KS);
+      }
+    } else {
+      for (int i = threadIdx.x; i < g.Q * kTile; i += blockDim.x) {
+        const int y = i / kTile, col = i - y * kTile;
+        if (col >= nx) continue;
+        const cpx v = input(q, y, col);
+        const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
+                          (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
+        if (e) atomicMax(&exc[col], e);
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < KT * 16 * kTile; i += blockDim.x) {
+        const int y = i / kTile, col = i - y * kTile;
+        const cpx v = (y < g.Q && col < nx) ? input(q, y, col) : cpx{0.0, 0.0};
+        const int ex = exc[col] - 1022;
+        digits_bf16(scaled56(v.re, ex), dig + (size_t)(2 * col) * KS + y, 32 * KS);
+        digits_bf16(scaled56(v.im, ex), dig + (size_t)(2 * col + 1) * KS + y, 32 * KS);
+      }
     }
     __syncthreads();
     const int MTn = (N + 15) / 16;
