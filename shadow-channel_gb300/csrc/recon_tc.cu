@@ -35,6 +35,7 @@ namespace chn {
 
 static constexpr int kThreads = 256;
 static constexpr int kTile = 16;   // kx columns per block (32 real columns: re, im interleaved)
+static constexpr int kReconRegs = 8;  // coefficient rows a thread keeps in registers per class (R <= 128)
 
 // ---------------------------------------------------------------------------
 // host: basis digit tables in mma A-fragment order
@@ -143,22 +144,53 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
   for (int i = threadIdx.x; i < 2 * kTile; i += blockDim.x) exc[i] = 0;
   __syncthreads();
   const int nent = 2 * (KT * 16) * kTile;
-  for (int i = threadIdx.x; i < nent; i += blockDim.x) {
-    const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
-    const cpx v = cval(cls, j, col);
-    const int e1 = (int)((__double_as_longlong(v.re) >> 52) & 0x7FF);
-    const int e2 = (int)((__double_as_longlong(v.im) >> 52) & 0x7FF);
-    const int e = max(e1, e2);
-    if (e) atomicMax(&exc[cls * kTile + col], e);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nent; i += blockDim.x) {
-    const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
-    const cpx v = cval(cls, j, col);
-    const int ex = exc[cls * kTile + col] - 1022;
-    for (int p = 0; p < 2; ++p)  // digit q of column n at dig[((cls * 7 + q) * 32 + n) * KS + j]
-      digits_bf16(scaled56(p ? v.im : v.re, ex), dig + ((size_t)cls * kDig * 32 + 2 * col + p) * KS + j,
-                  (size_t)32 * KS);
+  if (KT <= kReconRegs && blockDim.x == 16 * kTile) {
+    // thread t holds column t % kTile, rows t / kTile + 16 k of both classes:
+    // its coefficients stay in registers from the exponent maxima to the digits
+    const int col = threadIdx.x % kTile, j0 = threadIdx.x / kTile;
+    cpx vin[2][kReconRegs];
+    int emax[2] = {0, 0};
+#pragma unroll
+    for (int cls = 0; cls < 2; ++cls)
+#pragma unroll
+      for (int k = 0; k < kReconRegs; ++k) {
+        vin[cls][k] = k < KT ? cval(cls, j0 + 16 * k, col) : cpx{0.0, 0.0};
+        emax[cls] = max(emax[cls], max((int)((__double_as_longlong(vin[cls][k].re) >> 52) & 0x7FF),
+                                       (int)((__double_as_longlong(vin[cls][k].im) >> 52) & 0x7FF)));
+      }
+#pragma unroll
+    for (int cls = 0; cls < 2; ++cls)
+      if (emax[cls]) atomicMax(&exc[cls * kTile + col], emax[cls]);
+    __syncthreads();
+#pragma unroll
+    for (int cls = 0; cls < 2; ++cls) {
+      const int ex = exc[cls * kTile + col] - 1022;
+#pragma unroll
+      for (int k = 0; k < kReconRegs; ++k) {
+        if (k >= KT) break;
+        for (int p = 0; p < 2; ++p)  // digit q of column n at dig[((cls * 7 + q) * 32 + n) * KS + j]
+          digits_bf16(scaled56(p ? vin[cls][k].im : vin[cls][k].re, ex),
+                      dig + ((size_t)cls * kDig * 32 + 2 * col + p) * KS + j0 + 16 * k, (size_t)32 * KS);
+      }
+    }
+  } else {
+    for (int i = threadIdx.x; i < nent; i += blockDim.x) {
+      const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
+      const cpx v = cval(cls, j, col);
+      const int e1 = (int)((__double_as_longlong(v.re) >> 52) & 0x7FF);
+      const int e2 = (int)((__double_as_longlong(v.im) >> 52) & 0x7FF);
+      const int e = max(e1, e2);
+      if (e) atomicMax(&exc[cls * kTile + col], e);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nent; i += blockDim.x) {
+      const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
+      const cpx v = cval(cls, j, col);
+      const int ex = exc[cls * kTile + col] - 1022;
+      for (int p = 0; p < 2; ++p)  // digit q of column n at dig[((cls * 7 + q) * 32 + n) * KS + j]
+        digits_bf16(scaled56(p ? v.im : v.re, ex), dig + ((size_t)cls * kDig * 32 + 2 * col + p) * KS + j,
+                    (size_t)32 * KS);
+    }
   }
   __syncthreads();
 
