@@ -68,6 +68,20 @@ def args_parse():
     return ap.parse_args()
 
 
+def emit(line):
+    """Print the result as one JSON line of its own: the library (and the
+    oracle) write the reference's banners through C stdio, whose buffer is
+    flushed first so that no banner text lands on the JSON line."""
+    import ctypes
+    sys.stdout.flush()
+    try:
+        ctypes.CDLL(None).fflush(None)
+    except (OSError, AttributeError):
+        pass
+    sys.stdout.write("\n" + json.dumps(line) + "\n")
+    sys.stdout.flush()
+
+
 def grid_args(nsteps):
     g = GRID
     return (g["Nx"], g["Ny"], g["Nz"], g["Lx"], g["Lz"], g["Re"], g["flux"], g["dt"], nsteps)
@@ -354,7 +368,7 @@ def run_gb300(a):
     if rank == 0 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        emit(line)
     if dist:
         dist.destroy_process_group()
 
@@ -590,7 +604,7 @@ def run_reference(a):
                              "sample": f"{cores} processes x 1 segment x {steps} segment-step at 32x65x32 "
                                        f"(oracle/chan_port.c, the reference algorithm)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    emit(line)
 
 
 if __name__ == "__main__":
