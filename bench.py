@@ -185,8 +185,8 @@ def segment_step_flops(g):
 
 
 # ncu DRAM bytes (read + write) of one k_phys_inverse_tc instance: a 24-instance
-# launch at 32x65x32 moved 301.2 MB (92.9 read + 208.3 write); traffic grows with the instance count
-PHYS_TRAFFIC_PER_INSTANCE_32 = 301.2e6 / 24
+# launch at 32x65x32 moved 295.8 MB (92.6 read + 203.2 write); traffic grows with the instance count
+PHYS_TRAFFIC_PER_INSTANCE_32 = 295.8e6 / 24
 
 
 def tc_inverse_mma_flops(ninst, g, nfields=6):
