@@ -451,6 +451,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
 // products + forward transforms
 // ---------------------------------------------------------------------------
 
+static constexpr int kPB = 3;  // products computed per pass over the plane
+
 struct FwdTcDims {
   int KTx, KTz, MTx, MTz, KSx, KSz, pzp, Xp, Kk;
 };
@@ -469,23 +471,32 @@ __host__ __device__ inline FwdTcDims fwd_tc_dims(const Grid& g) {
   return d;
 }
 
-size_t fwd_tc_smem_bytes(const Grid& g) {
+// pb product planes per pass: kPB for the forward modes (0, 1), one for the
+// adjoint modes (2, 3), whose six transforms per plane run faster with the
+// L1 space the smaller footprint leaves to the tables
+inline int products_per_pass(int mode) { return mode >= 2 ? 1 : kPB; }
+
+size_t fwd_tc_smem_bytes(const Grid& g, int pb) {
   const FwdTcDims d = fwd_tc_dims(g);
   const size_t dx = (size_t)kDig * d.pzp * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
-  const size_t stage = (size_t)g.pz * g.px * sizeof(double), yb = (size_t)g.pz * g.X * sizeof(cpx);
-  size_t b = (size_t)((g.pz + 3) / 4 * 4 + (g.X + 3) / 4 * 4) * sizeof(int);
+  // kPB product planes (Y of the component in flight overlays its own plane:
+  // pz X complex values <= pz px doubles)
+  const size_t stage = (size_t)pb * g.pz * g.px * sizeof(double);
+  size_t b = (size_t)(pb * ((g.pz + 3) / 4 * 4) + (g.X + 3) / 4 * 4) * sizeof(int);
   b += ((dx > dz ? dx : dz) + 15) / 16 * 16;
-  b += ((stage > yb ? stage : yb) + 15) / 16 * 16;
+  b += (stage + 15) / 16 * 16;
   b += (size_t)d.Kk * g.X * sizeof(cpx);
   return b;
 }
 
 // The products of one plane (mode 0 primal, 1 tangent, 2 adjoint S and T,
 // 3 the exact transpose; split_product) and their forward transforms as
-// digit GEMMs, one component at a time; modes 0/1 write H slots 0..2, modes
-// 2/3 fold each component into the output slots (assemble_stage).  Same
-// outputs as k_products_fwd / k_products_adj.
-template <bool MULTI>
+// digit GEMMs: the products of three components in one pass over the plane
+// (each field loaded once), then the transforms one component at a time;
+// modes 0/1 write H slots 0..2, modes 2/3 fold each component into the
+// output slots (assemble_stage).  Same outputs as k_products_fwd /
+// k_products_adj.
+template <bool MULTI, int PB>
 __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_constant__ Grid g0, ProdArgs a, int mode) {
   const int inst = blockIdx.y, y = blockIdx.x;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
@@ -494,19 +505,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
   const FwdTcDims d = fwd_tc_dims(g);
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* p = smem;
-  int* exx = reinterpret_cast<int*>(p); p += (size_t)((g.pz + 3) / 4 * 4) * sizeof(int);
+  const int exs = (g.pz + 3) / 4 * 4, pb = PB;
+  int* exx3 = reinterpret_cast<int*>(p); p += (size_t)pb * exs * sizeof(int);  // [c][zp]
   int* exz = reinterpret_cast<int*>(p); p += (size_t)((g.X + 3) / 4 * 4) * sizeof(int);
   uint16_t* dig = reinterpret_cast<uint16_t*>(p);
   {
     const size_t dx = (size_t)kDig * d.pzp * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
     p += ((dx > dz ? dx : dz) + 15) / 16 * 16;
   }
-  double* stage = reinterpret_cast<double*>(p);  // [zp][xp] products, then Y [zp][kx] (cpx)
-  cpx* Yb = reinterpret_cast<cpx*>(p);
-  {
-    const size_t st = (size_t)g.pz * g.px * sizeof(double), yb = (size_t)g.pz * g.X * sizeof(cpx);
-    p += ((st > yb ? st : yb) + 15) / 16 * 16;
-  }
+  double* stage3 = reinterpret_cast<double*>(p);  // [c][zp][xp] products; Y [zp][kx] (cpx) over plane c
+  p += ((size_t)pb * g.pz * g.px * sizeof(double) + 15) / 16 * 16;
   cpx* Fb = reinterpret_cast<cpx*>(p);  // [kk][kx]
   const size_t plane = (size_t)g.pz * g.px, fs = (size_t)g.Q * plane;
   const double* __restrict__ Pp = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane +
@@ -522,16 +530,31 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
   const int ncomp = mode >= 2 ? 6 : 3;
   const size_t xstride = (size_t)d.pzp * d.KSx, zstride = (size_t)d.Xp * d.KSz;  // bf16 between digits
   for (int q = 0; q < ncomp; ++q) {
-    // ---- products of component q, row exponents (one column per zp)
-    for (int i = threadIdx.x; i < g.pz; i += blockDim.x) exx[i] = 0;
-    __syncthreads();
-    for (int i = threadIdx.x; i < g.pz * g.px; i += blockDim.x) {
-      const double v = split_product(mode, Pp, Pt, fs, i, q);
-      stage[i] = v;
-      const int e = (int)((__double_as_longlong(v) >> 52) & 0x7FF);
-      if (e) atomicMax(&exx[i / g.px], e);
+    const int c = q % pb;
+    double* stage = stage3 + (size_t)c * plane;
+    cpx* Yb = reinterpret_cast<cpx*>(stage);
+    int* exx = exx3 + c * exs;
+    if (c == 0) {
+      // ---- products of components q .. q+2 (each field loaded once per
+      // point), row exponents (one column per zp)
+      for (int i = threadIdx.x; i < pb * exs; i += blockDim.x) exx3[i] = 0;
+      __syncthreads();
+      const int nc = min(pb, ncomp - q);
+      for (int i = threadIdx.x; i < g.pz * g.px; i += blockDim.x) {
+        double v[PB];
+#pragma unroll
+        for (int cc = 0; cc < PB; ++cc) v[cc] = cc < nc ? split_product(mode, Pp, Pt, fs, i, q + cc) : 0.0;
+        const int row = i / g.px;
+#pragma unroll
+        for (int cc = 0; cc < PB; ++cc) {
+          if (cc >= nc) break;
+          stage3[(size_t)cc * plane + i] = v[cc];
+          const int e = (int)((__double_as_longlong(v[cc]) >> 52) & 0x7FF);
+          if (e) atomicMax(&exx3[cc * exs + row], e);
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
     for (int i = threadIdx.x; i < d.pzp * (d.KTx * 16); i += blockDim.x) {
       const int n = i / (d.KTx * 16), k = i - n * (d.KTx * 16);
       const double v = (n < g.pz && k < g.px) ? stage[(size_t)n * g.px + k] : 0.0;
@@ -611,12 +634,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
 // needs 149 KB, one per SM, and the FFT kernels (two per SM) are faster,
 // also for an uneven batch, whose every instance runs at the largest
 // grid's shared memory.
-bool fwd_tc_fits(const Grid& g, int optin) { return 2 * (fwd_tc_smem_bytes(g) + 4096) <= (size_t)optin + 4096; }
+bool fwd_tc_fits(const Grid& g, int optin) {
+  return 2 * (fwd_tc_smem_bytes(g, kPB) + 4096) <= (size_t)optin + 4096;
+}
 
 cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
-  const size_t sm = fwd_tc_smem_bytes(g);
-  if (a.grids) k_products_tc<true><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a, mode);
-  else k_products_tc<false><<<dim3(g.Q, a.ninst), kThreads, sm, st>>>(g, a, mode);
+  const size_t sm = fwd_tc_smem_bytes(g, products_per_pass(mode));
+  const dim3 grid(g.Q, a.ninst);
+  if (products_per_pass(mode) == kPB) {
+    if (a.grids) k_products_tc<true, kPB><<<grid, kThreads, sm, st>>>(g, a, mode);
+    else k_products_tc<false, kPB><<<grid, kThreads, sm, st>>>(g, a, mode);
+  } else {
+    if (a.grids) k_products_tc<true, 1><<<grid, kThreads, sm, st>>>(g, a, mode);
+    else k_products_tc<false, 1><<<grid, kThreads, sm, st>>>(g, a, mode);
+  }
   return cudaGetLastError();
 }
 
@@ -647,8 +678,10 @@ void prepare_phys_tc(int optin) {
   allow_max_smem(k_phys_inverse_tc<true, 2>, optin);
   allow_max_smem(k_phys_inverse_tc<false, 3>, optin);
   allow_max_smem(k_phys_inverse_tc<true, 3>, optin);
-  allow_max_smem(k_products_tc<false>, optin);
-  allow_max_smem(k_products_tc<true>, optin);
+  allow_max_smem(k_products_tc<false, kPB>, optin);
+  allow_max_smem(k_products_tc<true, kPB>, optin);
+  allow_max_smem(k_products_tc<false, 1>, optin);
+  allow_max_smem(k_products_tc<true, 1>, optin);
 }
 
 }  // namespace chn
