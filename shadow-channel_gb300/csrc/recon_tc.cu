@@ -218,17 +218,27 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
 #pragma unroll
           for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
         const int kend = min(KTb, kc + kChunkKT);
+        // the basis fragments of k-tile kt + 1 load while kt's products run
+        const uint4* Am = A + (((size_t)b * MT + mt) * KT) * kDig * 32 + lane;
+        uint4 af[kDig];
+#pragma unroll
+        for (int i = 0; i < kDig; ++i) af[i] = __ldg(Am + ((size_t)kc * kDig + i) * 32);
         for (int kt = kc; kt < kend; ++kt) {
+          const int kn = min(kt + 1, kend - 1);
+          uint4 an[kDig];
+#pragma unroll
+          for (int i = 0; i < kDig; ++i) an[i] = __ldg(Am + ((size_t)kn * kDig + i) * 32);
           const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + ((size_t)cls * kDig * 32 + n) * KS + kt * 16);
 #pragma unroll
           for (int i = 0; i < kDig; ++i) {
-            const uint4 af = __ldg(&A[(((((size_t)b * MT + mt) * KT + kt) * kDig + i) * 32 + lane)]);
 #pragma unroll
             for (int k = 0; k < kDig - i; ++k) {
               const uint32_t* row = brow + (size_t)k * 32 * KS / 2;
-              mma_bf16_16816(acc[i + k], af, row[t], row[t + 4]);
+              mma_bf16_16816(acc[i + k], af[i], row[t], row[t + 4]);
             }
           }
+#pragma unroll
+          for (int i = 0; i < kDig; ++i) af[i] = an[i];
         }
         // the chunk's exact level sums as 64-bit integers
 #pragma unroll
