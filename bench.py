@@ -184,20 +184,48 @@ def segment_step_flops(g):
     return 3 * ((1 + NTAN) * (quad + 9 * Q * plane) + (1.5 * quad + 15 * Q * plane))
 
 
-# ncu DRAM bytes (read + write) of one k_phys_inverse_tc instance: a 24-instance
-# launch at 32x65x32 moved 295.8 MB (92.6 read + 203.2 write); traffic grows with the instance count
+# ncu DRAM bytes (read + write) of one instance of a 24-instance launch at
+# 32x65x32 (traffic grows with the instance count): k_phys_inverse_tc 295.8 MB
+# (92.6 read + 203.2 write), k_products_tc tangent mode 387.8 MB (343.5 + 44.3)
 PHYS_TRAFFIC_PER_INSTANCE_32 = 295.8e6 / 24
+PROD_TRAFFIC_PER_INSTANCE_32 = 387.8e6 / 24
+
+
+def products_fwd_flops(ninst, g):
+    """Tangent products and their forward transforms per plane: 3 components
+    of u' x w + u x w' (4 multiplies, 3 adds per point) and 3 forward 2D
+    transforms (the inverse's nominal FFT flop)."""
+    Nx, Ny, Nz = g["Nx"], g["Ny"], g["Nz"]
+    Q, pz, px = 3 * Ny // 2, 3 * Nz // 2, 3 * Nx // 2
+    return ninst * 3 * Q * 7.0 * pz * px + phys_inverse_flops(ninst, g, nfields=3)
 
 
 def tc_inverse_mma_flops(ninst, g, nfields=6):
     """bf16 tensor-core flop of one k_phys_inverse_tc launch: per pair of
-    fields a z-stage GEMM (2 pz x 2 (Nz-1) x 2X) and an x-stage GEMM
-    (px x 2X x 2 pz) in m16n8k16 tiles, each tile 28 digit-pair MMAs."""
+    fields the radix-2 z-stage GEMM (pz rows x 2 (Nz-1) x 2X, the even and
+    odd modes' k-tiles) and x-stage GEMM (px/2 rows x 2X x 2 pz) in m16n8k16
+    tiles, each tile 28 digit-pair MMAs."""
     X, Nz = g["Nx"] // 2, g["Nz"]
     pz, px, Q = 3 * Nz // 2, 3 * g["Nx"] // 2, 3 * g["Ny"] // 2
     t = lambda n, d: (n + d - 1) // d
-    per_pair = 28 * (t(2 * pz, 16) * t(2 * X, 8) * t(2 * (Nz - 1), 16) + t(px, 16) * t(2 * pz, 8) * t(2 * X, 16))
+    h = Nz // 2
+    nzE, nzO = ((Nz - 1, 0) if pz % 2 else ((h + 1) // 2 + (h - 1) // 2, h // 2 + h // 2))
+    ktz = t(2 * nzE, 16) + t(2 * nzO, 16)
+    ktx = t(2 * ((X + 1) // 2), 16) + t(2 * (X // 2), 16)
+    pzh = pz // 2 if pz % 2 == 0 else pz
+    per_pair = 28 * (t(2 * pzh, 16) * ktz * t(2 * X, 8) + t(px // 2, 16) * ktx * t(2 * pz, 8))
     return ninst * Q * t(nfields, 2) * per_pair * 4096.0
+
+
+def tc_products_mma_flops(ninst, g, ncomp=3):
+    """bf16 tensor-core flop of one k_products_tc launch: per component an
+    x-stage GEMM (2X x px x pz) and a z-stage GEMM (2 (Nz-1) x 2 pz x X) in
+    m16n8k16 tiles of 28 digit-pair MMAs."""
+    X, Nz = g["Nx"] // 2, g["Nz"]
+    pz, px, Q = 3 * Nz // 2, 3 * g["Nx"] // 2, 3 * g["Ny"] // 2
+    t = lambda n, d: (n + d - 1) // d
+    per = 28 * (t(2 * X, 16) * t(px, 16) * t(pz, 8) + t(2 * (Nz - 1), 16) * t(2 * pz, 16) * t(X, 8))
+    return ninst * Q * ncomp * per * 4096.0
 
 
 def measured_bf16_peak():
@@ -313,27 +341,41 @@ def run_gb300(a):
     nt = NSEG * NTAN
     k_ms = {name: cc.lib.c_batch_kernel_ms(i, 5) for i, name in
             enumerate(["recon", "phys_inverse", "products_fwd", "solve", "products_adj"])}
-    dom_ms = k_ms["phys_inverse"]
-    flops = phys_inverse_flops(nt, GRID)
+    # the dominant kernel of the step: k_products_tc (37.5% of the sweeps'
+    # kernel time, k_phys_inverse_tc 32.8%: profiles/launches_bench64_32x65x32.md);
+    # its tangent launch (192 instances) stands for it
+    dom_ms = k_ms["products_fwd"]
+    flops = products_fwd_flops(nt, GRID)
     achieved = flops / (dom_ms * 1e-3) / 1e12
-    tc_flops = tc_inverse_mma_flops(nt, GRID)
+    tc_flops = tc_products_mma_flops(nt, GRID)
     bf16_peak, bf16_src = measured_bf16_peak()
-    traffic = PHYS_TRAFFIC_PER_INSTANCE_32 * nt if (GRID["Nx"], GRID["Ny"], GRID["Nz"]) == (32, 65, 32) else None
+    at32 = (GRID["Nx"], GRID["Ny"], GRID["Nz"]) == (32, 65, 32)
+    traffic = PROD_TRAFFIC_PER_INSTANCE_32 * nt if at32 else None
+    inv_ms = k_ms["phys_inverse"]
+    inv_flops, inv_tc = phys_inverse_flops(nt, GRID), tc_inverse_mma_flops(nt, GRID)
     step_flop = segment_step_flops(GRID)
     autotune = json.loads(cc.lib.c_autotune_report().decode() or "{}")
-    roofline = {"bound": "fp64", "kernel": f"k_phys_inverse_tc ({nt} tangent fields)", "achieved": achieved,
+    roofline = {"bound": "fp64", "kernel": f"k_products_tc ({nt} tangent instances, 3 products)",
+                "achieved": achieved,
                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                 "traffic_unit": "bytes per launch",
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 24-instance "
                                   "launch, scaled by the instance count",
                 "peak_source": "measured: FP64 FMA probe in this run (c_fp64_peak_tflops)",
                 "algorithmic_flop_per_launch": flops, "kernel_ms": k_ms,
-                "note": "k_phys_inverse runs as exact digit GEMMs on the tensor cores (k_phys_inverse_tc); "
-                        "achieved counts the FFT's nominal FP64 flop it replaces (FP64-equivalent)",
+                "note": "the products are FP64; their forward transforms run as exact digit GEMMs on the "
+                        "tensor cores; achieved counts the products' flop and the FFT's nominal FP64 flop "
+                        "the transforms replace (FP64-equivalent)",
                 "tensor": {"achieved": tc_flops / (dom_ms * 1e-3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
                            "frac": tc_flops / (dom_ms * 1e-3) / 1e12 / bf16_peak, "peak_source": bf16_src,
                            "mma_flop_per_launch": tc_flops,
                            "what": "bf16 m16n8k16 digit-product flop of the launch (28 digit pairs per tile)"},
+                "phys_inverse_tc": {"kernel": f"k_phys_inverse_tc ({nt} x 6 tangent fields)",
+                                    "achieved_tflops_fp64_equivalent": inv_flops / (inv_ms * 1e-3) / 1e12,
+                                    "frac_fp64": inv_flops / (inv_ms * 1e-3) / 1e12 / peak,
+                                    "tensor_tflops": inv_tc / (inv_ms * 1e-3) / 1e12,
+                                    "tensor_frac": inv_tc / (inv_ms * 1e-3) / 1e12 / bf16_peak,
+                                    "traffic": PHYS_TRAFFIC_PER_INSTANCE_32 * nt if at32 else None},
                 "recon_tflops": recon_flops(nt, GRID) / (k_ms["recon"] * 1e-3) / 1e12,
                 "step": {"algorithmic_flop_per_segment_step": step_flop,
                          "achieved_tflops": step_flop * value / world / 1e12,
