@@ -20,6 +20,7 @@
 // physical fields to u_in_bar.
 #include "chn_common.cuh"
 #include "kernels.h"
+#include "tc_common.cuh"
 
 namespace chn {
 
@@ -94,8 +95,18 @@ struct SolveTSmem {
   double* m0;  // mean mode: fa[R], fb[R], ca[R] (cpx), cb[R] (cpx)
 };
 
+// bytes of the tensor-core digits: Recon^T's [7][32][Q pad] (+ exponents),
+// Quad^T's two [7][32][R pad] (+ exponents)
+__host__ __device__ inline size_t solveT_tc_bytes(const Grid& g) {
+  const size_t rq = (size_t)kDig * 32 * ((g.Q + 15) / 16 * 16 + 8) * 2 + kTile * sizeof(int);
+  const size_t qt = (size_t)2 * kDig * 32 * ((g.R + 15) / 16 * 16 + 8) * 2 + 2 * kTile * sizeof(int);
+  return rq > qt ? rq : qt;
+}
+
 __host__ __device__ inline size_t solveT_hc_elems(const Grid& g) {
   size_t hc = (size_t)g.Qh * kTile * 6, r = 2 * (size_t)g.R * kTile;
+  const size_t tc = (solveT_tc_bytes(g) + sizeof(cpx) - 1) / sizeof(cpx);
+  if (tc > hc) hc = tc;
   return hc > r ? hc : r;
 }
 
@@ -220,6 +231,198 @@ __device__ void recon_T_tile(const Grid& g, const cpx* __restrict__ Ub, int z, i
   }
 }
 
+// ---------------------------------------------------------------------------
+// the transposed contractions on the tensor cores (tc_common.cuh), the
+// scheme of the forward quadratures (quad_rhs_tc in recon_solve.cu)
+// ---------------------------------------------------------------------------
+
+static constexpr int kTRegs = 8;  // plane inputs a thread keeps in registers (Q <= 128)
+
+// comb(row, col, v) for rows < N and columns col < nx of the contraction of
+// table b (row-major [rows][Q] digits: [b][ceil(R/16)][KT][7][32][4], row
+// exponents TE[b * R + row]) with the per-column plane inputs in(y, col)
+// (Re and Im as two GEMM columns sharing the column exponent)
+template <typename In, typename Comb>
+__device__ void contract_planes_tc(const Grid& g, const uint4* __restrict__ T, const int* __restrict__ TE, int b,
+                                   int N, int nx, In input, Comb comb, uint16_t* dig, int* exc) {
+  const int KT = (g.Q + 15) / 16, MTw = (g.R + 15) / 16;
+  const size_t KS = (size_t)KT * 16 + 8;
+  for (int i = threadIdx.x; i < kTile; i += blockDim.x) exc[i] = 0;
+  __syncthreads();
+  if (KT <= kTRegs && blockDim.x == 16 * kTile) {
+    const int col = threadIdx.x % kTile, y0 = threadIdx.x / kTile;
+    cpx vin[kTRegs];
+    int emax = 0;
+#pragma unroll
+    for (int k = 0; k < kTRegs; ++k) {
+      const int y = y0 + 16 * k;
+      vin[k] = (k < KT && y < g.Q && col < nx) ? input(y, col) : cpx{0.0, 0.0};
+      emax = max(emax, max((int)((__double_as_longlong(vin[k].re) >> 52) & 0x7FF),
+                           (int)((__double_as_longlong(vin[k].im) >> 52) & 0x7FF)));
+    }
+    if (emax) atomicMax(&exc[col], emax);
+    __syncthreads();
+    const int ex = exc[col] - 1022;
+#pragma unroll
+    for (int k = 0; k < kTRegs; ++k) {
+      if (k >= KT) break;
+      const int y = y0 + 16 * k;
+      digits_bf16(scaled56(vin[k].re, ex), dig + (size_t)(2 * col) * KS + y, 32 * KS);
+      digits_bf16(scaled56(vin[k].im, ex), dig + (size_t)(2 * col + 1) * KS + y, 32 * KS);
+    }
+  } else {
+    for (int i = threadIdx.x; i < g.Q * kTile; i += blockDim.x) {
+      const int y = i / kTile, col = i - y * kTile;
+      if (col >= nx) continue;
+      const cpx v = input(y, col);
+      const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
+                        (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
+      if (e) atomicMax(&exc[col], e);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < KT * 16 * kTile; i += blockDim.x) {
+      const int y = i / kTile, col = i - y * kTile;
+      const cpx v = (y < g.Q && col < nx) ? input(y, col) : cpx{0.0, 0.0};
+      const int ex = exc[col] - 1022;
+      digits_bf16(scaled56(v.re, ex), dig + (size_t)(2 * col) * KS + y, 32 * KS);
+      digits_bf16(scaled56(v.im, ex), dig + (size_t)(2 * col + 1) * KS + y, 32 * KS);
+    }
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
+  const int NT = (2 * nx + 7) / 8, MTn = (N + 15) / 16;
+  for (int item = warp; item < MTn * NT; item += blockDim.x >> 5) {
+    const int mt = item / NT, nt = item - mt * NT;
+    const int col = nt * 4 + t, n = nt * 8 + gq;
+    const int ecol = exc[min(col, kTile - 1)] - 1022;
+    double part[4] = {0.0, 0.0, 0.0, 0.0};
+    long long Hh[4], Ll[4];
+    const uint4* Tm = T + (((size_t)b * MTw + mt) * KT) * kDig * 32 + lane;
+    for (int kc = 0; kc < KT; kc += kChunkKT) {
+      float acc[kDig][4];
+#pragma unroll
+      for (int l = 0; l < kDig; ++l)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+      const int kend = min(KT, kc + kChunkKT);
+      for (int kt = kc; kt < kend; ++kt) {
+        const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
+        uint32_t b0[kDig], b1[kDig];
+#pragma unroll
+        for (int k = 0; k < kDig; ++k) {
+          b0[k] = brow[(size_t)k * 32 * KS / 2 + t];
+          b1[k] = brow[(size_t)k * 32 * KS / 2 + t + 4];
+        }
+#pragma unroll
+        for (int i = 0; i < kDig; ++i) {
+          const uint4 af = __ldg(Tm + ((size_t)kt * kDig + i) * 32);
+#pragma unroll
+          for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r) fold_levels(acc, r, Hh[r], Ll[r]);
+      if (kend < KT) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int row = min(mt * 16 + gq + 8 * (r >> 1), g.R - 1);
+          part[r] += round_scaled(Hh[r], Ll[r], TE[(size_t)b * g.R + row] + ecol - 64);
+        }
+      }
+    }
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+      const int row = mt * 16 + gq + 8 * rr;
+      if (row >= N || col >= nx) continue;
+      const int e = TE[(size_t)b * g.R + row] + ecol - 64;
+      cpx val = {round_fast(Hh[2 * rr], Ll[2 * rr], e), round_fast(Hh[2 * rr + 1], Ll[2 * rr + 1], e)};
+      if (KT > kChunkKT) {
+        val.re += part[2 * rr];
+        val.im += part[2 * rr + 1];
+      }
+      comb(row, col, val);
+    }
+  }
+  __syncthreads();
+}
+
+// Recon^T (as recon_T_tile) with its five contractions on the tensor cores
+// (the mean column, col < xfirst, gets zeros: it has its own rows)
+__device__ void recon_T_tc(const Grid& g, const cpx* __restrict__ Ub, int z, int x0, int nx, int xfirst,
+                           SolveTSmem& s) {
+  const size_t cs = (size_t)g.Q * g.X;
+  const cpx* Uz = Ub + (size_t)z * 5 * cs;
+  uint16_t* dig = reinterpret_cast<uint16_t*>(s.hc);
+  int* exc = reinterpret_cast<int*>(dig + (size_t)kDig * 32 * ((size_t)(g.Q + 15) / 16 * 16 + 8));
+  const uint4* T = reinterpret_cast<const uint4*>(g.tcBT);
+  auto at = [&](int c, int y, int col) { return Uz[(size_t)c * cs + (size_t)y * g.X + x0 + col]; };
+  auto axz = [&](int col, double& ax, double& az) {
+    ax = g.kxK2[(size_t)z * g.X + x0 + col];
+    az = g.kzK2[(size_t)z * g.X + x0 + col];
+  };
+  // alpha_bar = Q^T v_bar - Q'^T Xp_bar + Q''^T dx_bar -> s.Fa
+  contract_planes_tc(
+      g, T, g.tcBTE, 0, g.D, nx,
+      [&](int y, int col) { return col < xfirst ? cpx{0.0, 0.0} : at(1, y, col); },
+      [&](int row, int col, cpx v) { s.Fa[row * kTile + col] = v; }, dig, exc);
+  contract_planes_tc(
+      g, T, g.tcBTE, 1, g.D, nx,
+      [&](int y, int col) {
+        if (col < xfirst) return cpx{0.0, 0.0};
+        double ax, az;
+        axz(col, ax, az);
+        const cpx u = at(0, y, col), w = at(2, y, col);
+        return cpx{-fma(ax, u.im, az * w.im), fma(ax, u.re, az * w.re)};  // Xp_bar = i(ax u + az w)
+      },
+      [&](int row, int col, cpx v) {
+        cpx& f = s.Fa[row * kTile + col];
+        f.re -= v.re;
+        f.im -= v.im;
+      },
+      dig, exc);
+  contract_planes_tc(
+      g, T, g.tcBTE, 2, g.D, nx,
+      [&](int y, int col) {
+        if (col < xfirst) return cpx{0.0, 0.0};
+        double ax, az;
+        axz(col, ax, az);
+        const cpx du = at(3, y, col), dw = at(4, y, col);
+        return cpx{fma(ax, du.im, az * dw.im), -fma(ax, du.re, az * dw.re)};  // dx_bar = -i(ax du + az dw)
+      },
+      [&](int row, int col, cpx v) {
+        cpx& f = s.Fa[row * kTile + col];
+        f.re += v.re;
+        f.im += v.im;
+      },
+      dig, exc);
+  // beta_bar = R^T Zp_bar + R'^T dz_bar -> s.Fb
+  contract_planes_tc(
+      g, T, g.tcBTE, 3, g.R, nx,
+      [&](int y, int col) {
+        if (col < xfirst) return cpx{0.0, 0.0};
+        double ax, az;
+        axz(col, ax, az);
+        const cpx u = at(0, y, col), w = at(2, y, col);
+        return cpx{fma(ax, w.im, -az * u.im), fma(az, u.re, -ax * w.re)};  // Zp_bar = i(az u - ax w)
+      },
+      [&](int row, int col, cpx v) { s.Fb[row * kTile + col] = v; }, dig, exc);
+  contract_planes_tc(
+      g, T, g.tcBTE, 4, g.R, nx,
+      [&](int y, int col) {
+        if (col < xfirst) return cpx{0.0, 0.0};
+        double ax, az;
+        axz(col, ax, az);
+        const cpx du = at(3, y, col), dw = at(4, y, col);
+        return cpx{fma(ax, dw.im, -az * du.im), fma(az, du.re, -ax * dw.re)};  // dz_bar = i(az du - ax dw)
+      },
+      [&](int row, int col, cpx v) {
+        cpx& f = s.Fb[row * kTile + col];
+        f.re += v.re;
+        f.im += v.im;
+      },
+      dig, exc);
+}
+
 // Recon^T of the mean mode, row i (transpose of channel/initAlphaBeta2.c:25-68):
 // a_bar = R^T u_bar + R'^T du_bar, b_bar = R^T w_bar + R'^T dw_bar
 __device__ __forceinline__ void recon_T_mean_row(const Grid& g, const cpx* __restrict__ Ub, int i, cpx& a, cpx& b) {
@@ -236,6 +439,118 @@ __device__ __forceinline__ void recon_T_mean_row(const Grid& g, const cpx* __res
   }
   a = cpx{ar, ai};
   b = cpx{br, bi};
+}
+
+// H_bar = Quad^T(F_bar) on the tensor cores for the columns [xfirst, nx):
+// per plane y the contractions over the modes pa = Qpw^T Fa, qa = Qw^T Fa,
+// rb = Rw^T Fb as GEMMs (rows: planes), then the combination of the FP64
+// loop in k_solve_T (the mean column keeps that loop)
+__device__ void quad_T_tc(const Grid& g, int z, int x0, int nx, int xfirst, SolveTSmem& s, cpx* __restrict__ Hb) {
+  const int KTr = (g.R + 15) / 16, MTq = (g.Q + 15) / 16;
+  const size_t KS = (size_t)KTr * 16 + 8;
+  uint16_t* dA = reinterpret_cast<uint16_t*>(s.hc);             // [7][32][KS] digits of Fa
+  uint16_t* dB = dA + (size_t)kDig * 32 * KS;                    // digits of Fb
+  int* exa = reinterpret_cast<int*>(dB + (size_t)kDig * 32 * KS);  // [2][kTile] column exponents
+  for (int i = threadIdx.x; i < 2 * kTile; i += blockDim.x) exa[i] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < (g.D + g.R) * kTile; i += blockDim.x) {
+    const bool fb = i >= g.D * kTile;
+    const int j = fb ? i - g.D * kTile : i, row = j / kTile, col = j - row * kTile;
+    if (col >= nx || col < xfirst) continue;
+    const cpx v = (fb ? s.Fb : s.Fa)[row * kTile + col];
+    const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
+                      (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
+    if (e) atomicMax(&exa[(fb ? kTile : 0) + col], e);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 2 * KTr * 16 * kTile; i += blockDim.x) {
+    const bool fb = i >= KTr * 16 * kTile;
+    const int j = fb ? i - KTr * 16 * kTile : i, row = j / kTile, col = j - row * kTile;
+    const int N = fb ? g.R : g.D;
+    const cpx v = (row < N && col < nx && col >= xfirst) ? (fb ? s.Fb : s.Fa)[row * kTile + col] : cpx{0.0, 0.0};
+    const int ex = exa[(fb ? kTile : 0) + col] - 1022;
+    uint16_t* d = fb ? dB : dA;
+    digits_bf16(scaled56(v.re, ex), d + (size_t)(2 * col) * KS + row, 32 * KS);
+    digits_bf16(scaled56(v.im, ex), d + (size_t)(2 * col + 1) * KS + row, 32 * KS);
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
+  const int NT = (2 * nx + 7) / 8;
+  const uint4* __restrict__ W = reinterpret_cast<const uint4*>(g.tcWT);
+  const size_t cs = (size_t)g.Q * g.X;
+  const double kz = g.Kz[z];
+  for (int item = warp; item < MTq * NT; item += blockDim.x >> 5) {
+    const int mt = item / NT, nt = item - mt * NT;
+    const int col = nt * 4 + t, n = nt * 8 + gq;
+    double v[3][4];  // pa, qa, rb at (rows gq, gq + 8) x (Re, Im)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const uint16_t* d = b < 2 ? dA : dB;
+      const int ecol = exa[(b < 2 ? 0 : kTile) + min(col, kTile - 1)] - 1022;
+      const uint4* Wm = W + (((size_t)b * MTq + mt) * KTr) * kDig * 32 + lane;
+      double part[4] = {0.0, 0.0, 0.0, 0.0};
+      long long Hh[4], Ll[4];
+      for (int kc = 0; kc < KTr; kc += kChunkKT) {
+        float acc[kDig][4];
+#pragma unroll
+        for (int l = 0; l < kDig; ++l)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+        const int kend = min(KTr, kc + kChunkKT);
+        for (int kt = kc; kt < kend; ++kt) {
+          const uint32_t* brow = reinterpret_cast<const uint32_t*>(d + (size_t)n * KS + kt * 16);
+          uint32_t b0[kDig], b1[kDig];
+#pragma unroll
+          for (int k = 0; k < kDig; ++k) {
+            b0[k] = brow[(size_t)k * 32 * KS / 2 + t];
+            b1[k] = brow[(size_t)k * 32 * KS / 2 + t + 4];
+          }
+#pragma unroll
+          for (int i = 0; i < kDig; ++i) {
+            const uint4 af = __ldg(Wm + ((size_t)kt * kDig + i) * 32);
+#pragma unroll
+            for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) fold_levels(acc, r, Hh[r], Ll[r]);
+        if (kend < KTr) {
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            const int y = min(mt * 16 + gq + 8 * (r >> 1), g.Q - 1);
+            part[r] += round_scaled(Hh[r], Ll[r], g.tcWTE[(size_t)b * g.Q + y] + ecol - 64);
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int y = min(mt * 16 + gq + 8 * (r >> 1), g.Q - 1);
+        v[b][r] = round_fast(Hh[r], Ll[r], g.tcWTE[(size_t)b * g.Q + y] + ecol - 64);
+        if (KTr > kChunkKT) v[b][r] += part[r];
+      }
+    }
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+      const int y = mt * 16 + gq + 8 * rr;
+      if (y >= g.Q || col >= nx || col < xfirst) continue;
+      const int x = x0 + col;
+      const double kx = g.Kx[x], k2 = g.K2[(size_t)z * g.X + x];
+      const double scl = x == 0 ? g.norm : 0.5 * g.norm;
+      const cpx pa = {v[0][2 * rr], v[0][2 * rr + 1]}, qa = {v[1][2 * rr], v[1][2 * rr + 1]};
+      const cpx rb = {v[2][2 * rr], v[2][2 * rr + 1]};
+      cpx hx, hy, hz;
+      hx.re = scl * (kx * pa.im + kz * rb.im);  // -i kx pa - i kz rb
+      hx.im = -scl * (kx * pa.re + kz * rb.re);
+      hz.re = scl * (kz * pa.im - kx * rb.im);  // -i kz pa + i kx rb
+      hz.im = scl * (kx * rb.re - kz * pa.re);
+      hy.re = -scl * k2 * qa.re;
+      hy.im = -scl * k2 * qa.im;
+      cpx* out = Hb + ((size_t)z * 5 * g.Q + y) * g.X + x;
+      out[0] = hz;
+      out[cs] = hx;
+      out[2 * cs] = hy;
+    }
+  }
 }
 
 template <bool MULTI>
@@ -263,7 +578,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
   SolveTSmem s = carve_solveT(g, smem);
   const cpx* __restrict__ Ub = a.Ub.at(inst);
   const int xfirst = (z == 0 && x0 == 0) ? 1 : 0;
-  recon_T_tile(g, Ub, z, x0, nx, xfirst, s);
+  if (g.tc) recon_T_tc(g, Ub, z, x0, nx, xfirst, s);
+  else recon_T_tile(g, Ub, z, x0, nx, xfirst, s);
   if (a.final_only) {
     // the sweep's start state: IU = Recon(IC), so IC_bar += Recon^T(IU_bar)
     for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
@@ -440,8 +756,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
   // halved off the kx = 0 column (the transpose of the real-to-complex x
   // transform).  Plane pairs (y, -y) share the sums: weights of even type
   // (Qw, Rw) give E + O / E - O, of odd type (Qpw) E + O / O - E.
+  if (g.tc) quad_T_tc(g, z, x0, nx, xfirst, s, a.Hb.at(inst));
   const int lx = threadIdx.x % kTile, grp = threadIdx.x / kTile, ngrp = blockDim.x / kTile;
   if (lx >= nx) return;
+  if (g.tc && lx >= xfirst) return;  // the tensor cores took every column but the mean one
   const int x = x0 + lx;
   const bool mean = (z == 0 && x == 0);
   const double kx = g.Kx[x], kz = g.Kz[z], k2 = g.K2[(size_t)z * g.X + x];

@@ -95,6 +95,14 @@ struct Grid {
   // [5][ceil(R/16)][ceil(Q/16)][7][32][4], row exponents [5][R]
   const uint32_t* tcW;
   const int* tcWE;
+  // the exact adjoint's transposed contractions (adjoint_exact.cu): the five
+  // bases transposed without weights, rows padded to R, in tcW's layout
+  // [5][ceil(R/16)][ceil(Q/16)][7][32][4] with exponents [5][R]; and Qpw, Qw,
+  // Rw plane-major [3][ceil(Q/16)][ceil(R/16)][7][32][4], exponents [3][Q]
+  const uint32_t* tcBT;
+  const int* tcBTE;
+  const uint32_t* tcWT;
+  const int* tcWTE;
   int tc;
   // inverse transforms as DFT GEMMs on the tensor cores (phys_tc.cu), each
   // stage split radix-2 into even and odd modes where its length is even:

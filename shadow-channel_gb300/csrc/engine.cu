@@ -152,6 +152,11 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   {
     std::vector<uint32_t> frag, wfrag;
     std::vector<int> ex, wex;
+    std::vector<uint32_t> btf, wtf;
+    std::vector<int> bte, wte;
+    if (!build_adj_tc_tables(h, btf, bte, wtf, wte) || !T.up(btf, &g.tcBT) || !T.up(bte, &g.tcBTE) ||
+        !T.up(wtf, &g.tcWT) || !T.up(wte, &g.tcWTE))
+      return false;
     if (!build_recon_tc_tables(h, frag, ex, wfrag, wex) || !T.up(frag, &g.tcA) || !T.up(ex, &g.tcE) ||
         !T.up(wfrag, &g.tcW) || !T.up(wex, &g.tcWE))
       return false;

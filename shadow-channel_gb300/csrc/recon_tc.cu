@@ -106,6 +106,35 @@ bool build_recon_tc_tables(const HostTables& h, std::vector<uint32_t>& frag, std
   return true;
 }
 
+// the exact adjoint's tables: the bases transposed ([D or R][Q], rows
+// padded to R) for Recon^T, and the weighted transposes of Qpw, Qw, Rw
+// turned plane-major ([Q][D or R], columns padded to R) for Quad^T
+bool build_adj_tc_tables(const HostTables& h, std::vector<uint32_t>& btfrag, std::vector<int>& btex,
+                         std::vector<uint32_t>& wtfrag, std::vector<int>& wtex) {
+  const int MTw = (h.R + 15) / 16, KTq = (h.Q + 15) / 16;
+  const std::vector<double>* B[5] = {&h.Bq, &h.Bqp, &h.Bqpp, &h.Br, &h.Brp};
+  btfrag.clear();
+  btex.clear();
+  for (int b = 0; b < 5; ++b) {
+    const int cols = b < 3 ? h.D : h.R;  // B[b] is [Q][cols]
+    std::vector<double> m((size_t)h.R * h.Q, 0.0);
+    for (int i = 0; i < cols; ++i)
+      for (int y = 0; y < h.Q; ++y) m[(size_t)i * h.Q + y] = (*B[b])[(size_t)y * cols + i];
+    if (!append_digit_table(m.data(), h.R, h.Q, MTw, KTq, btfrag, btex)) return false;
+  }
+  const std::vector<double>* W[3] = {&h.Wqp, &h.Wq, &h.Wr};  // [D or R][Q]
+  wtfrag.clear();
+  wtex.clear();
+  for (int b = 0; b < 3; ++b) {
+    const int rows = b < 2 ? h.D : h.R;
+    std::vector<double> m((size_t)h.Q * h.R, 0.0);
+    for (int y = 0; y < h.Q; ++y)
+      for (int i = 0; i < rows; ++i) m[(size_t)y * h.R + i] = (*W[b])[(size_t)i * h.Q + y];
+    if (!append_digit_table(m.data(), h.Q, h.R, KTq, MTw, wtfrag, wtex)) return false;
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // device
 // ---------------------------------------------------------------------------

@@ -42,6 +42,8 @@ void band_lu(double* A, int w, int dl, int du, int N);
 // transposes for the tensor-core contractions (recon_tc.cu, tc_common.cuh)
 bool build_recon_tc_tables(const HostTables& h, std::vector<uint32_t>& frag, std::vector<int>& ex,
                            std::vector<uint32_t>& wfrag, std::vector<int>& wex);
+bool build_adj_tc_tables(const HostTables& h, std::vector<uint32_t>& btfrag, std::vector<int>& btex,
+                         std::vector<uint32_t>& wtfrag, std::vector<int>& wtex);
 // DFT matrices of the inverse z and x transforms as digit tables (phys_tc.cu)
 bool build_phys_tc_tables(const HostTables& h, std::vector<uint32_t>& zfrag, std::vector<int>& zex,
                           std::vector<uint32_t>& xfrag, std::vector<int>& xex, std::vector<int>& zmap);
