@@ -295,51 +295,14 @@ __device__ void contract_planes_tc(const Grid& g, const uint4* __restrict__ T, c
     const int mt = item / NT, nt = item - mt * NT;
     const int col = nt * 4 + t, n = nt * 8 + gq;
     const int ecol = exc[min(col, kTile - 1)] - 1022;
-    double part[4] = {0.0, 0.0, 0.0, 0.0};
     long long Hh[4], Ll[4];
-    const uint4* Tm = T + (((size_t)b * MTw + mt) * KT) * kDig * 32 + lane;
-    for (int kc = 0; kc < KT; kc += kChunkKT) {
-      float acc[kDig][4];
-#pragma unroll
-      for (int l = 0; l < kDig; ++l)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
-      const int kend = min(KT, kc + kChunkKT);
-      for (int kt = kc; kt < kend; ++kt) {
-        const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
-        uint32_t b0[kDig], b1[kDig];
-#pragma unroll
-        for (int k = 0; k < kDig; ++k) {
-          b0[k] = brow[(size_t)k * 32 * KS / 2 + t];
-          b1[k] = brow[(size_t)k * 32 * KS / 2 + t + 4];
-        }
-#pragma unroll
-        for (int i = 0; i < kDig; ++i) {
-          const uint4 af = __ldg(Tm + ((size_t)kt * kDig + i) * 32);
-#pragma unroll
-          for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
-        }
-      }
-#pragma unroll
-      for (int r = 0; r < 4; ++r) fold_levels(acc, r, Hh[r], Ll[r]);
-      if (kend < KT) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          const int row = min(mt * 16 + gq + 8 * (r >> 1), g.R - 1);
-          part[r] += round_scaled(Hh[r], Ll[r], TE[(size_t)b * g.R + row] + ecol - 64);
-        }
-      }
-    }
+    tc_tile(T + (size_t)b * MTw * KT * kDig * 32, mt, KT, dig, KS, (size_t)32 * KS, n, lane, t, Hh, Ll);
 #pragma unroll
     for (int rr = 0; rr < 2; ++rr) {
       const int row = mt * 16 + gq + 8 * rr;
       if (row >= N || col >= nx) continue;
       const int e = TE[(size_t)b * g.R + row] + ecol - 64;
-      cpx val = {round_fast(Hh[2 * rr], Ll[2 * rr], e), round_fast(Hh[2 * rr + 1], Ll[2 * rr + 1], e)};
-      if (KT > kChunkKT) {
-        val.re += part[2 * rr];
-        val.im += part[2 * rr + 1];
-      }
+      const cpx val = {round_fast(Hh[2 * rr], Ll[2 * rr], e), round_fast(Hh[2 * rr + 1], Ll[2 * rr + 1], e)};
       comb(row, col, val);
     }
   }
@@ -487,46 +450,12 @@ __device__ void quad_T_tc(const Grid& g, int z, int x0, int nx, int xfirst, Solv
     for (int b = 0; b < 3; ++b) {
       const uint16_t* d = b < 2 ? dA : dB;
       const int ecol = exa[(b < 2 ? 0 : kTile) + min(col, kTile - 1)] - 1022;
-      const uint4* Wm = W + (((size_t)b * MTq + mt) * KTr) * kDig * 32 + lane;
-      double part[4] = {0.0, 0.0, 0.0, 0.0};
       long long Hh[4], Ll[4];
-      for (int kc = 0; kc < KTr; kc += kChunkKT) {
-        float acc[kDig][4];
-#pragma unroll
-        for (int l = 0; l < kDig; ++l)
-#pragma unroll
-          for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
-        const int kend = min(KTr, kc + kChunkKT);
-        for (int kt = kc; kt < kend; ++kt) {
-          const uint32_t* brow = reinterpret_cast<const uint32_t*>(d + (size_t)n * KS + kt * 16);
-          uint32_t b0[kDig], b1[kDig];
-#pragma unroll
-          for (int k = 0; k < kDig; ++k) {
-            b0[k] = brow[(size_t)k * 32 * KS / 2 + t];
-            b1[k] = brow[(size_t)k * 32 * KS / 2 + t + 4];
-          }
-#pragma unroll
-          for (int i = 0; i < kDig; ++i) {
-            const uint4 af = __ldg(Wm + ((size_t)kt * kDig + i) * 32);
-#pragma unroll
-            for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
-          }
-        }
-#pragma unroll
-        for (int r = 0; r < 4; ++r) fold_levels(acc, r, Hh[r], Ll[r]);
-        if (kend < KTr) {
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            const int y = min(mt * 16 + gq + 8 * (r >> 1), g.Q - 1);
-            part[r] += round_scaled(Hh[r], Ll[r], g.tcWTE[(size_t)b * g.Q + y] + ecol - 64);
-          }
-        }
-      }
+      tc_tile(W + (size_t)b * MTq * KTr * kDig * 32, mt, KTr, d, KS, (size_t)32 * KS, n, lane, t, Hh, Ll);
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const int y = min(mt * 16 + gq + 8 * (r >> 1), g.Q - 1);
         v[b][r] = round_fast(Hh[r], Ll[r], g.tcWTE[(size_t)b * g.Q + y] + ecol - 64);
-        if (KTr > kChunkKT) v[b][r] += part[r];
       }
     }
 #pragma unroll

@@ -215,54 +215,6 @@ size_t phys_tc_smem_bytes(const Grid& g, bool with_cfl) {
   return b;
 }
 
-// One exact digit GEMM tile of a fixed table A (fragment order
-// [mt][KT][7][32][4]) against the smem digits of column n, over the k-tiles
-// [k0, k1): FP32 level sums per chunk of at most 7 k-tiles (exact), folded
-// into the 64-bit integers H, L per accumulator element (exact across
-// chunks: |H| < 2^41, |L| < 2^50 per chunk); an empty range gives zeros
-__device__ __forceinline__ void tc_tile_range(const uint4* __restrict__ A, int mt, int KT, int k0, int k1,
-                                              const uint16_t* dig, size_t KS, size_t dstride, int n, int lane, int t,
-                                              long long (&H)[4], long long (&L)[4]) {
-#pragma unroll
-  for (int r = 0; r < 4; ++r) { H[r] = 0; L[r] = 0; }
-  for (int kc = k0; kc < k1; kc += kChunkKT) {
-    float acc[kDig][4];
-#pragma unroll
-    for (int l = 0; l < kDig; ++l)
-#pragma unroll
-      for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
-    const int kend = min(k1, kc + kChunkKT);
-    for (int kt = kc; kt < kend; ++kt) {
-      const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
-      uint32_t b0[kDig], b1[kDig];
-#pragma unroll
-      for (int k = 0; k < kDig; ++k) {
-        b0[k] = brow[(size_t)k * dstride / 2 + t];
-        b1[k] = brow[(size_t)k * dstride / 2 + t + 4];
-      }
-#pragma unroll
-      for (int i = 0; i < kDig; ++i) {
-        const uint4 af = __ldg(&A[(((size_t)mt * KT + kt) * kDig + i) * 32 + lane]);
-#pragma unroll
-        for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af, b0[k], b1[k]);
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      long long h, l;
-      fold_levels(acc, r, h, l);
-      H[r] += h;
-      L[r] += l;
-    }
-  }
-}
-
-__device__ __forceinline__ void tc_tile(const uint4* __restrict__ A, int mt, int KT, const uint16_t* dig, size_t KS,
-                                        size_t dstride, int n, int lane, int t, long long (&H)[4],
-                                        long long (&L)[4]) {
-  tc_tile_range(A, mt, KT, 0, KT, dig, KS, dstride, n, lane, t, H, L);
-}
-
 // ---------------------------------------------------------------------------
 // kernel
 // ---------------------------------------------------------------------------
