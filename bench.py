@@ -346,8 +346,8 @@ def run_gb300(a):
     k_ms = {name: cc.lib.c_batch_kernel_ms(i, 5) for i, name in
             enumerate(["recon", "phys_inverse", "products_fwd", "solve", "products_adj"])}
     # the dominant kernel of the step: k_products_tc (37.5% of the sweeps'
-    # kernel time, k_phys_inverse_tc 32.8%: profiles/launches_bench64_32x65x32.md);
-    # its tangent launch (192 instances) stands for it
+    # kernel time in the ncu launch list of this benchmark, k_phys_inverse_tc
+    # 32.8%); its tangent launch (192 instances) stands for it
     dom_ms = k_ms["products_fwd"]
     flops = products_fwd_flops(nt, GRID)
     achieved = flops / (dom_ms * 1e-3) / 1e12
