@@ -460,60 +460,14 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
       const int mt = item / NT, nt = item - mt * NT;
       const int col = nt * 4 + t, n = nt * 8 + gq;
       const int ecol = exc[min(col, kTile - 1)] - 1022;
-      double part[4] = {0.0, 0.0, 0.0, 0.0};
       long long Hh[4], Ll[4];
-      for (int kc = 0; kc < KT; kc += kChunkKT) {
-        float acc[kDig][4];
-#pragma unroll
-        for (int l = 0; l < kDig; ++l)
-#pragma unroll
-          for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
-        const int kend = min(KT, kc + kChunkKT);
-        // the weight fragments of k-tile kt + 1 load while kt's products run
-        // (the tables live in L2)
-        const uint4* Wm = W + (((size_t)w * MTw + mt) * KT) * kDig * 32 + lane;
-        uint4 af[kDig];
-#pragma unroll
-        for (int i = 0; i < kDig; ++i) af[i] = __ldg(Wm + ((size_t)kc * kDig + i) * 32);
-        for (int kt = kc; kt < kend; ++kt) {
-          const int kn = min(kt + 1, kend - 1);
-          uint4 an[kDig];
-#pragma unroll
-          for (int i = 0; i < kDig; ++i) an[i] = __ldg(Wm + ((size_t)kn * kDig + i) * 32);
-          const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
-          uint32_t b0[kDig], b1[kDig];
-#pragma unroll
-          for (int k = 0; k < kDig; ++k) {
-            b0[k] = brow[(size_t)k * 32 * KS / 2 + t];
-            b1[k] = brow[(size_t)k * 32 * KS / 2 + t + 4];
-          }
-#pragma unroll
-          for (int i = 0; i < kDig; ++i)
-#pragma unroll
-            for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af[i], b0[k], b1[k]);
-#pragma unroll
-          for (int i = 0; i < kDig; ++i) af[i] = an[i];
-        }
-#pragma unroll
-        for (int r = 0; r < 4; ++r) fold_levels(acc, r, Hh[r], Ll[r]);
-        if (kend < KT) {
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            const int row = mt * 16 + gq + 8 * (r >> 1);
-            part[r] += round_scaled(Hh[r], Ll[r], g.tcWE[(size_t)w * g.R + min(row, g.R - 1)] + ecol - 64);
-          }
-        }
-      }
+      tc_tile_pf(W + (size_t)w * MTw * KT * kDig * 32, mt, KT, KT, dig, KS, (size_t)32 * KS, n, lane, t, Hh, Ll);
 #pragma unroll
       for (int rr = 0; rr < 2; ++rr) {
         const int row = mt * 16 + gq + 8 * rr;
         if (row >= N || col >= nx) continue;
         const int e = g.tcWE[(size_t)w * g.R + row] + ecol - 64;
-        cpx val = {round_fast(Hh[2 * rr], Ll[2 * rr], e), round_fast(Hh[2 * rr + 1], Ll[2 * rr + 1], e)};
-        if (KT > kChunkKT) {
-          val.re += part[2 * rr];
-          val.im += part[2 * rr + 1];
-        }
+        const cpx val = {round_fast(Hh[2 * rr], Ll[2 * rr], e), round_fast(Hh[2 * rr + 1], Ll[2 * rr + 1], e)};
         cpx& f = F[row * kTile + col];
         if (first) {
           f = val;

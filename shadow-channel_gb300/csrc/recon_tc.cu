@@ -238,65 +238,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
       const int b = order[ob], cls = b < 3 ? 0 : 1;
       const int KTb = ((cls == 0 ? g.D : g.R) + 15) / 16;
       const int ecol = exc[cls * kTile + col] - 1022;
-      double part[4] = {0.0, 0.0, 0.0, 0.0};  // sums of earlier chunks (only when K > 112)
       long long H[4], L[4];
-      for (int kc = 0; kc < KTb; kc += kChunkKT) {
-        float acc[kDig][4];
-#pragma unroll
-        for (int l = 0; l < kDig; ++l)
-#pragma unroll
-          for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
-        const int kend = min(KTb, kc + kChunkKT);
-        // the basis fragments of k-tile kt + 1 load while kt's products run
-        const uint4* Am = A + (((size_t)b * MT + mt) * KT) * kDig * 32 + lane;
-        uint4 af[kDig];
-#pragma unroll
-        for (int i = 0; i < kDig; ++i) af[i] = __ldg(Am + ((size_t)kc * kDig + i) * 32);
-        for (int kt = kc; kt < kend; ++kt) {
-          const int kn = min(kt + 1, kend - 1);
-          uint4 an[kDig];
-#pragma unroll
-          for (int i = 0; i < kDig; ++i) an[i] = __ldg(Am + ((size_t)kn * kDig + i) * 32);
-          const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + ((size_t)cls * kDig * 32 + n) * KS + kt * 16);
-#pragma unroll
-          for (int i = 0; i < kDig; ++i) {
-#pragma unroll
-            for (int k = 0; k < kDig - i; ++k) {
-              const uint32_t* row = brow + (size_t)k * 32 * KS / 2;
-              mma_bf16_16816(acc[i + k], af[i], row[t], row[t + 4]);
-            }
-          }
-#pragma unroll
-          for (int i = 0; i < kDig; ++i) af[i] = an[i];
-        }
-        // the chunk's exact level sums as 64-bit integers
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          long long lv[kDig];
-#pragma unroll
-          for (int l = 0; l < kDig; ++l) lv[l] = (long long)__float2int_rn(acc[l][r]);
-          H[r] = (lv[0] << 16) + (lv[1] << 8) + lv[2];
-          L[r] = (lv[3] << 24) + (lv[4] << 16) + (lv[5] << 8) + lv[6];
-        }
-        if (kend < KTb) {  // more chunks follow: keep this one as FP64
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            const int y = mt * 16 + gq + 8 * (r >> 1);
-            const int e = g.tcE[(size_t)b * g.Q + min(y, g.Q - 1)] + ecol - 64;
-            part[r] += round_scaled(H[r], L[r], e);
-          }
-        }
-      }
+      tc_tile_pf(A + (size_t)b * MT * KT * kDig * 32, mt, KT, KTb, dig + (size_t)cls * kDig * 32 * KS, KS,
+                 (size_t)32 * KS, n, lane, t, H, L);
 #pragma unroll
       for (int rr = 0; rr < 2; ++rr) {
         const int y = mt * 16 + gq + 8 * rr;
         if (y >= g.Q || col >= nx || (meancol && col == 0)) continue;
         const int e = g.tcE[(size_t)b * g.Q + y] + ecol - 64;
-        cpx val = {round_fast(H[2 * rr], L[2 * rr], e), round_fast(H[2 * rr + 1], L[2 * rr + 1], e)};
-        if (KTb > kChunkKT) {
-          val.re += part[2 * rr];
-          val.im += part[2 * rr + 1];
-        }
+        const cpx val = {round_fast(H[2 * rr], L[2 * rr], e), round_fast(H[2 * rr + 1], L[2 * rr + 1], e)};
         const int x = x0 + col;
         cpx* out = U + ((size_t)z * 5 * g.Q + y) * g.X + x;
         const double ax = g.kxK2[(size_t)z * g.X + x], az = g.kzK2[(size_t)z * g.X + x];

@@ -199,6 +199,54 @@ __device__ __forceinline__ void tc_tile(const uint4* __restrict__ A, int mt, int
   tc_tile_range(A, mt, KT, 0, KT, dig, KS, dstride, n, lane, t, H, L);
 }
 
+// The same tile over the k-tiles [0, k1) of a table with KT k-tiles per row
+// tile, with the table fragments of k-tile kt + 1 loaded while kt's products
+// run (for tables that live in L2)
+__device__ __forceinline__ void tc_tile_pf(const uint4* __restrict__ A, int mt, int KT, int k1, const uint16_t* dig,
+                                           size_t KS, size_t dstride, int n, int lane, int t, long long (&H)[4],
+                                           long long (&L)[4]) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) { H[r] = 0; L[r] = 0; }
+  const uint4* Am = A + (size_t)mt * KT * kDig * 32 + lane;
+  for (int kc = 0; kc < k1; kc += kChunkKT) {
+    float acc[kDig][4];
+#pragma unroll
+    for (int l = 0; l < kDig; ++l)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[l][r] = 0.f;
+    const int kend = min(k1, kc + kChunkKT);
+    uint4 af[kDig];
+#pragma unroll
+    for (int i = 0; i < kDig; ++i) af[i] = __ldg(Am + ((size_t)kc * kDig + i) * 32);
+    for (int kt = kc; kt < kend; ++kt) {
+      const int kn = min(kt + 1, kend - 1);
+      uint4 an[kDig];
+#pragma unroll
+      for (int i = 0; i < kDig; ++i) an[i] = __ldg(Am + ((size_t)kn * kDig + i) * 32);
+      const uint32_t* brow = reinterpret_cast<const uint32_t*>(dig + (size_t)n * KS + kt * 16);
+      uint32_t b0[kDig], b1[kDig];
+#pragma unroll
+      for (int k = 0; k < kDig; ++k) {
+        b0[k] = brow[(size_t)k * dstride / 2 + t];
+        b1[k] = brow[(size_t)k * dstride / 2 + t + 4];
+      }
+#pragma unroll
+      for (int i = 0; i < kDig; ++i)
+#pragma unroll
+        for (int k = 0; k < kDig - i; ++k) mma_bf16_16816(acc[i + k], af[i], b0[k], b1[k]);
+#pragma unroll
+      for (int i = 0; i < kDig; ++i) af[i] = an[i];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      long long h, l;
+      fold_levels(acc, r, h, l);
+      H[r] += h;
+      L[r] += l;
+    }
+  }
+}
+
 // host: digit table of a row-major matrix M[rows][K] in mma A-fragment order
 // [MT][KT][7][32 lanes][4] (appended to frag), row exponents appended to ex
 bool append_digit_table(const double* M, int rows, int K, int MT, int KT, std::vector<uint32_t>& frag,
