@@ -17,6 +17,8 @@
 #ifndef SHADOW_CHANNEL_GB300_C_CHANNEL_H
 #define SHADOW_CHANNEL_GB300_C_CHANNEL_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -286,6 +288,18 @@ int c_lss_minres_dev(const chn_complex *b, chn_complex *x, double tol, int maxit
    the table size, or -1 for bad arguments. */
 int c_setup_table(int Nx, int Ny, int Nz, double Lx, double Lz, double Re,
                   double flux, double dt, int which, double *out, int n);
+
+/* Host-only, no device: the digit tables of the tensor-core contractions
+   for a grid (base-256 digits of 56-bit scaled rows in mma fragment order,
+   and the row exponents).  which: 0 the five bases [5][Q/16][R/16] tiles,
+   1 their weighted transposes, 2 the inverse transform's z stage, 3 its x
+   stage, 4 the forward x stage, 5 the forward z stage, 6 the unscaled
+   forward x stage, 7 the bases transposed, 8 Qpw, Qw, Rw plane-major.
+   sizes[0] = uint32 words, sizes[1] = exponents; frag / ex are written when
+   large enough.  Returns 0, or -1 for bad arguments. */
+int c_setup_tc_table(int Nx, int Ny, int Nz, double Lx, double Lz, double Re,
+                     double flux, double dt, int which, uint32_t *frag,
+                     long long nfrag, int *ex, long long nex, long long *sizes);
 
 #ifdef __cplusplus
 }

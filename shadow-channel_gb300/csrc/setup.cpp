@@ -340,3 +340,28 @@ extern "C" int c_setup_table(int Nx, int Ny, int Nz, double Lx, double Lz, doubl
   if (out && n >= (int)a.size()) std::memcpy(out, a.data(), sizeof(double) * a.size());
   return (int)a.size();
 }
+
+extern "C" int c_setup_tc_table(int Nx, int Ny, int Nz, double Lx, double Lz, double Re, double flux, double dt,
+                                int which, uint32_t* frag, long long nfrag, int* ex, long long nex,
+                                long long* sizes) {
+  chn::HostTables t;
+  const char* err = nullptr;
+  if (!sizes || !chn::build_tables(Nx, Ny, Nz, Lx, Lz, Re, flux, dt, t, &err)) return -1;
+  std::vector<uint32_t> f[3];
+  std::vector<int> e[3], m;
+  bool ok = false;
+  int sel = 0;
+  switch (which) {
+    case 0: case 1: ok = chn::build_recon_tc_tables(t, f[0], e[0], f[1], e[1]); sel = which; break;
+    case 2: case 3: ok = chn::build_phys_tc_tables(t, f[0], e[0], f[1], e[1], m); sel = which - 2; break;
+    case 4: case 5: case 6: ok = chn::build_fwd_tc_tables(t, f[0], e[0], f[1], e[1], f[2], e[2]); sel = which - 4; break;
+    case 7: case 8: ok = chn::build_adj_tc_tables(t, f[0], e[0], f[1], e[1]); sel = which - 7; break;
+    default: return -1;
+  }
+  if (!ok) return -1;
+  sizes[0] = (long long)f[sel].size();
+  sizes[1] = (long long)e[sel].size();
+  if (frag && nfrag >= sizes[0]) std::memcpy(frag, f[sel].data(), sizeof(uint32_t) * f[sel].size());
+  if (ex && nex >= sizes[1]) std::memcpy(ex, e[sel].data(), sizeof(int) * e[sel].size());
+  return 0;
+}
