@@ -41,9 +41,6 @@ static constexpr int kReconRegs = 8;  // coefficient rows a thread keeps in regi
 // host: basis digit tables in mma A-fragment order
 // ---------------------------------------------------------------------------
 
-int recon_tc_ktiles(const Grid& g) { return (g.R + 15) / 16; }
-int recon_tc_mtiles(const Grid& g) { return (g.Q + 15) / 16; }
-
 bool append_digit_table(const double* M, int rows, int K, int MT, int KT, std::vector<uint32_t>& frag,
                         std::vector<int>& ex) {
   const size_t base = frag.size();

@@ -64,17 +64,6 @@ __device__ __forceinline__ long long scaled56(double v, int ex) {
   return bits < 0 ? -sig : sig;
 }
 
-// exact value (H 2^32 + L) 2^e rounded once to FP64
-__device__ __forceinline__ double round_scaled(long long H, long long L, int e) {
-  if (e >= -1022 && e + 32 <= 1023) {
-    const double s = __longlong_as_double((long long)(e + 1023) << 52);
-    const double s32 = __longlong_as_double((long long)(e + 32 + 1023) << 52);
-    return fma((double)H, s32, (double)L * s);
-  }
-  return fma((double)H, scalbn(1.0, e + 32), scalbn((double)L, e));
-}
-
-
 // (H 2^32 + L) 2^e with one FP64 conversion: the sum is folded into one
 // int64 keeping at least 62 significant bits (|H| < 2^41, |L| < 2^50), the
 // conversion rounds it, and the power of two goes into the exponent field
