@@ -58,9 +58,10 @@ def args_parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the exact-adjoint, uneven-batch, 128x129x128 and autograd measurements")
-    ap.add_argument("--extras", default="exact,uneven,large,grad",
-                    help="comma list of the extra measurements to run: exact, uneven, large, grad")
+                    help="run none of the extra measurements (the default runs none either)")
+    ap.add_argument("--extras", default="",
+                    help="comma list of extra measurements, printed on a second JSON line: exact, uneven, "
+                         "large, large5000, grad (default: none)")
     ap.add_argument("--segments", type=int, default=NSEG,
                     help="segments per GPU (default 64; smaller only for profiling captures)")
     ap.add_argument("--runup", type=int, default=RUNUP,
@@ -338,52 +339,16 @@ def run_gb300(a):
     assert rc1 == 0 and rc2 == 0, cc.c_last_error_message()
     bytes_in = (hC.nbytes + hIC.nbytes + hAC.nbytes)
     e2e = {"value": NSEG * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bytes_in // K,
-           "d2h_bytes_per_step": bytes_in // K}
+           "d2h_bytes_per_step": bytes_in // K,
+           "note": "the sweep entry points copy the segments' C, IC, AC in and out once per call; per-step "
+                   "bytes are those copies divided by the K steps of the sweep"}
 
     # roofline of the dominant kernel: CUDA events on the library stream
-    peak = cc.c_fp64_peak_tflops()
     nt = NSEG * NTAN
     k_ms = {name: cc.lib.c_batch_kernel_ms(i, 5) for i, name in
             enumerate(["recon", "phys_inverse", "products_fwd", "solve", "products_adj"])}
-    # the dominant kernel of the step: k_products_tc (37.5% of the sweeps'
-    # kernel time in the ncu launch list of this benchmark, k_phys_inverse_tc
-    # 32.8%); its tangent launch (192 instances) stands for it
-    dom_ms = k_ms["products_fwd"]
-    flops = products_fwd_flops(nt, GRID)
-    achieved = flops / (dom_ms * 1e-3) / 1e12
-    tc_flops = tc_products_mma_flops(nt, GRID)
-    bf16_peak, bf16_src = measured_bf16_peak()
-    at32 = (GRID["Nx"], GRID["Ny"], GRID["Nz"]) == (32, 65, 32)
-    traffic = PROD_TRAFFIC_PER_INSTANCE_32 * nt if at32 else None
-    inv_ms = k_ms["phys_inverse"]
-    inv_flops, inv_tc = phys_inverse_flops(nt, GRID), tc_inverse_mma_flops(nt, GRID)
-    step_flop = segment_step_flops(GRID)
+    roofline = dominant_roofline(cc, k_ms, nt, value / world)
     autotune = json.loads(cc.lib.c_autotune_report().decode() or "{}")
-    roofline = {"bound": "fp64", "kernel": f"k_products_tc ({nt} tangent instances, 3 products)",
-                "achieved": achieved,
-                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
-                "traffic_unit": "bytes per launch",
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 24-instance "
-                                  "launch, scaled by the instance count",
-                "peak_source": "measured: FP64 FMA probe in this run (c_fp64_peak_tflops)",
-                "algorithmic_flop_per_launch": flops, "kernel_ms": k_ms,
-                "note": "the products are FP64; their forward transforms run as exact digit GEMMs on the "
-                        "tensor cores; achieved counts the products' flop and the FFT's nominal FP64 flop "
-                        "the transforms replace (FP64-equivalent)",
-                "tensor": {"achieved": tc_flops / (dom_ms * 1e-3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
-                           "frac": tc_flops / (dom_ms * 1e-3) / 1e12 / bf16_peak, "peak_source": bf16_src,
-                           "mma_flop_per_launch": tc_flops,
-                           "what": "bf16 m16n8k16 digit-product flop of the launch (28 digit pairs per tile)"},
-                "phys_inverse_tc": {"kernel": f"k_phys_inverse_tc ({nt} x 6 tangent fields)",
-                                    "achieved_tflops_fp64_equivalent": inv_flops / (inv_ms * 1e-3) / 1e12,
-                                    "frac_fp64": inv_flops / (inv_ms * 1e-3) / 1e12 / peak,
-                                    "tensor_tflops": inv_tc / (inv_ms * 1e-3) / 1e12,
-                                    "tensor_frac": inv_tc / (inv_ms * 1e-3) / 1e12 / bf16_peak,
-                                    "traffic": PHYS_TRAFFIC_PER_INSTANCE_32 * nt if at32 else None},
-                "recon_tflops": recon_flops(nt, GRID) / (k_ms["recon"] * 1e-3) / 1e12,
-                "step": {"algorithmic_flop_per_segment_step": step_flop,
-                         "achieved_tflops": step_flop * value / world / 1e12,
-                         "frac": step_flop * value / world / 1e12 / peak}}
 
     extras = set() if a.no_extras else {e.strip() for e in a.extras.split(",") if e.strip()}
     exact = None
@@ -393,30 +358,108 @@ def run_gb300(a):
     cc.c_destroy()
     plain = None
     if not a.no_plain and rank == 0:
-        plain = plain_gpu(cc, Cseg[0], IC0[:NTAN], AC0[0], min(K, 6))
+        plain = plain_gpu(cc, Cseg[0], IC0[:NTAN], AC0[0], K)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic seeded states (no dataset; reference restart files absent)",
-            "config": CONFIG, "e2e": e2e, "roofline": roofline, "gpu_launches": launches, "autotune": autotune,
-            "clocks": clk.summary()}
+            "config": CONFIG}
     if plain:
+        # the metric's headline: batched segment-steps/s over the plain
+        # one-trajectory-per-launch path, both over the same K steps
+        line["batched_over_plain"] = (value / world) / plain["value"]
         line["plain_gpu"] = plain
-        line["plain_gpu"]["batched_over_plain"] = (value / world) / plain["value"]
-    if exact:
-        line["exact_adjoint"] = exact
-    if "uneven" in extras and rank == 0:
-        line["uneven_batch"] = uneven_batch(cc)
-    if "large" in extras and rank == 0:
-        line["large_grid"] = large_grid(cc)
-    if "grad" in extras and rank == 0:
-        line["autograd_32x65x32"] = autograd_config(Cp)
+    line.update({"e2e": e2e, "roofline": roofline, "gpu_launches": launches, "clocks": clk.summary()})
     if rank == 0 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
+    line["autotune"] = autotune
+    extra = {}
+    if exact:
+        extra["exact_adjoint"] = exact
+    if "uneven" in extras and rank == 0:
+        extra["uneven_batch"] = uneven_batch(cc)
+    if "large" in extras and rank == 0:
+        extra["large_grid"] = large_grid(cc)
+    if "large5000" in extras and rank == 0:
+        extra["large_grid_5000"] = large_grid_horizon(cc)
+    if "grad" in extras and rank == 0:
+        extra["autograd_32x65x32"] = autograd_config(Cp)
     if rank == 0:
         emit(line)
+        if extra:
+            emit({"extras_of": METRIC, **extra})
     if dist:
         dist.destroy_process_group()
+
+
+def products_fwd_bytes(ninst, g):
+    """Algorithmic HBM bytes of one tangent-mode k_products_tc launch: each
+    tangent's six physical fields in, the primal's six fields shared by the
+    segment's NTAN tangents, and the three nonlinear-term components out
+    (complex, [Nz][3][Q][X])."""
+    Nx, Ny, Nz = g["Nx"], g["Ny"], g["Nz"]
+    X, Q, pz, px = Nx // 2, 3 * Ny // 2, 3 * Nz // 2, 3 * Nx // 2
+    fields = 6.0 * Q * pz * px * 8
+    return ninst * (fields + fields / NTAN + 3.0 * Nz * Q * X * 16)
+
+
+def phys_inverse_bytes(ninst, g, nfields=6):
+    """Algorithmic HBM bytes of one k_phys_inverse_tc launch: the five
+    velocity components in (complex, [Nz][5][Q][X]), the physical fields out."""
+    Nx, Ny, Nz = g["Nx"], g["Ny"], g["Nz"]
+    X, Q, pz, px = Nx // 2, 3 * Ny // 2, 3 * Nz // 2, 3 * Nx // 2
+    return ninst * (5.0 * Nz * Q * X * 16 + nfields * Q * pz * px * 8.0)
+
+
+def measured_hbm_peak():
+    """HBM GB/s measured on the GB300s (MEASURED_PEAKS.json), else the fallback"""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, STREAM-style copy)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def dominant_roofline(cc, k_ms, nt, value_per_gpu):
+    """Roofline of the dominant kernel of the step, k_products_tc (its
+    192-instance tangent launch; 37.5% of the sweeps' kernel time in the ncu
+    launch list of this workload, k_phys_inverse_tc 32.8%): achieved
+    algorithmic bytes per launch / CUDA-event duration against the measured
+    HBM peak, with the tensor-pipe view (bf16 digit-product flop against the
+    measured bf16 peak) and the FP64-equivalent view beside it."""
+    dom_ms = k_ms["products_fwd"]
+    hbm_peak, hbm_src = measured_hbm_peak()
+    bf16_peak, bf16_src = measured_bf16_peak()
+    at32 = (GRID["Nx"], GRID["Ny"], GRID["Nz"]) == (32, 65, 32)
+    nbytes = products_fwd_bytes(nt, GRID)
+    gbs = nbytes / (dom_ms * 1e-3) / 1e9
+    tc_flops = tc_products_mma_flops(nt, GRID)
+    fp64_peak = cc.c_fp64_peak_tflops()
+    flops = products_fwd_flops(nt, GRID)
+    inv_ms = k_ms["phys_inverse"]
+    inv_bytes, inv_tc = phys_inverse_bytes(nt, GRID), tc_inverse_mma_flops(nt, GRID)
+    step_flop = segment_step_flops(GRID)
+    return {"bound": "hbm", "kernel": f"k_products_tc ({nt} tangent instances, 3 products)",
+            "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak, "peak_source": hbm_src,
+            "traffic": PROD_TRAFFIC_PER_INSTANCE_32 * nt if at32 else None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 24-instance launch, "
+                              "scaled by the instance count (bytes per launch)",
+            "algorithmic_bytes_per_launch": nbytes, "kernel_ms": k_ms,
+            "note": "latency-bound (neither HBM nor a pipe is saturated); tensor and FP64 views below",
+            "tensor": {"achieved": tc_flops / (dom_ms * 1e-3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                       "frac": tc_flops / (dom_ms * 1e-3) / 1e12 / bf16_peak, "peak_source": bf16_src,
+                       "mma_flop_per_launch": tc_flops},
+            "fp64_equivalent": {"achieved": flops / (dom_ms * 1e-3) / 1e12, "peak": fp64_peak,
+                                "unit": "TFLOP/s", "frac": flops / (dom_ms * 1e-3) / 1e12 / fp64_peak,
+                                "peak_source": "FP64 FMA probe in this run (c_fp64_peak_tflops)"},
+            "phys_inverse_tc": {"kernel": f"k_phys_inverse_tc ({nt} x 6 tangent fields)", "ms": inv_ms,
+                                "achieved_gbs": inv_bytes / (inv_ms * 1e-3) / 1e9,
+                                "frac_hbm": inv_bytes / (inv_ms * 1e-3) / 1e9 / hbm_peak,
+                                "tensor_frac": inv_tc / (inv_ms * 1e-3) / 1e12 / bf16_peak,
+                                "traffic": PHYS_TRAFFIC_PER_INSTANCE_32 * nt if at32 else None},
+            "step": {"algorithmic_flop_per_segment_step": step_flop,
+                     "achieved_tflops": step_flop * value_per_gpu / 1e12,
+                     "frac_of_fp64_fma_peak": step_flop * value_per_gpu / 1e12 / fp64_peak}}
 
 
 def exact_adjoint_timing(cc, torch, stream, dAC, K):
@@ -567,6 +610,26 @@ def large_grid(cc, nsteps=8):
     return out
 
 
+def large_grid_horizon(cc, nsteps=5000):
+    """128x129x128 forward + adjoint over the full 5000-step horizon with the
+    checkpoint interval sized to the free HBM (channel.checkpoint): the
+    primal keeps one checkpoint per interval, the adjoint recomputes each
+    interval from its checkpoint; rates and recomputation overhead."""
+    from channel import checkpoint
+    from channel.synthetic import synthetic_state
+    grid = dict(Nx=128, Ny=129, Nz=128, Lx=4 * math.pi, Lz=2 * math.pi, Re=3300.0, flux=2.0, dt=0.002)
+    C0 = synthetic_state(128, 129, 128, seed=1)
+    AC0 = synthetic_state(128, 129, 128, seed=2, laminar=False)
+    spacing = checkpoint.choose_spacing(grid, nsteps)
+    _, AC, rep = checkpoint.forward_adjoint(grid, C0, nsteps, AC0, spacing=spacing)
+    rep["primal_steps_per_s"] = nsteps / rep["forward_s"]
+    rep["adjoint_steps_per_s"] = nsteps / rep["adjoint_s"]
+    rep["adjoint_finite"] = bool(np.isfinite(AC).all())
+    rep["grid"] = "128x129x128"
+    cc.c_destroy()
+    return rep
+
+
 def plain_gpu(cc, C, IC, AC, K):
     """One trajectory per launch sequence through the reference entry points
     (c_primal, three c_tangent calls, c_adjoint coupled to the last tangent)
@@ -594,35 +657,62 @@ def plain_gpu(cc, C, IC, AC, K):
 # CPU: the reference algorithm (oracle restatement) on the host cores
 # ---------------------------------------------------------------------------
 
-def _cpu_segment(steps, seed):
+def _segment_case(steps, seed):
+    """a constructed oracle instance and one segment's inputs (not timed)"""
     import oracle as O
     ch = O.PortChannel(*grid_args(steps))
     C = O.synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=seed)
     IC = [O.synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=seed + 1 + t, laminar=False)
           for t in range(NTAN)]
     AC = O.synthetic_state(GRID["Nx"], GRID["Ny"], GRID["Nz"], seed=seed + 9, laminar=False)
-    t0 = time.perf_counter()
-    ch.primal(0, C)
+    return ch, C, IC, AC
+
+
+def _segment_steps(ch, C, IC, AC, steps):
+    """the reference sequence of one segment over `steps` steps: primal, the
+    tangents (each re-running the primal, as the reference's tangent does),
+    the adjoint coupled to the last tangent with strength 1"""
+    ch.primal(0, C.copy())
     for t in range(NTAN):
-        ch.tangent(0, steps, IC[t], INHOMO[t])
-    ch.adjoint(steps, 0, AC, 0, 1.0)
-    dt_ = time.perf_counter() - t0
-    ch.close()
-    return dt_
+        ch.tangent(0, steps, IC[t].copy(), INHOMO[t])
+    ch.adjoint(steps, 0, AC.copy(), 0, 1.0)
 
 
 def cpu_baseline(steps=2):
     import oracle as O
     O.build_port()
-    dt_ = _cpu_segment(steps, 0)
+    ch, C, IC, AC = _segment_case(steps, 0)
+    t0 = time.perf_counter()
+    _segment_steps(ch, C, IC, AC, steps)
+    dt_ = time.perf_counter() - t0
+    ch.close()
     return {"value": steps / dt_, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"1 segment x {steps} segment-steps (primal, 3 tangents each re-running the primal as "
-                      f"the reference does, adjoint with strength 1) at 32x65x32, oracle/chan_port.c, 1 thread",
+                      f"the reference does, adjoint with strength 1) at 32x65x32, oracle/chan_port.c, 1 thread, "
+                      f"instance constructed before the timed region",
             "seconds": dt_}
 
 
+REF_STEPS = 2   # segment-steps per process in one sample of the reference arm
+
+
+def _reference_worker(rank, nsamples, barrier, queue):
+    """one host core: constructs its oracle instance once, then for every
+    sample waits at the barrier and times REF_STEPS segment-steps"""
+    ch, C, IC, AC = _segment_case(REF_STEPS, 200 + 10 * rank)
+    for k in range(nsamples):
+        barrier.wait()
+        t0 = time.clock_gettime(time.CLOCK_MONOTONIC)
+        _segment_steps(ch, C, IC, AC, REF_STEPS)
+        queue.put((k, rank, t0, time.clock_gettime(time.CLOCK_MONOTONIC)))
+    ch.close()
+
+
 def run_reference(a):
-    """The reference algorithm on all host cores: one segment per process."""
+    """The reference algorithm on all host cores: one segment per process
+    (as drivers/mpi_wrapper.py runs one segment per rank).  Each process
+    builds its oracle instance before any timing; a sample starts every
+    process at a barrier and lasts from the first start to the last end."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -630,25 +720,32 @@ def run_reference(a):
     import oracle as O
     O.build_port()
     cores = os.cpu_count() or 1
-    steps = 1
-    W = 0
+    W = max(1, min(a.warmup, 1))
+    K = max(2, min(a.steps, 3))
     ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        pool.starmap(_cpu_segment, [(1, 100 + i) for i in range(min(cores, 2))])  # warm-up
-        vals = []
-        for k in range(max(1, min(a.steps, 2))):
-            t0 = time.perf_counter()
-            pool.starmap(_cpu_segment, [(steps, 200 + 10 * i + k) for i in range(cores)])
-            vals.append(time.perf_counter() - t0)
-    wall = statistics.median(vals)
-    value = cores * steps / wall
+    barrier = ctx.Barrier(cores)
+    queue = ctx.Queue()
+    procs = [ctx.Process(target=_reference_worker, args=(r, W + K, barrier, queue)) for r in range(cores)]
+    for p in procs:
+        p.start()
+    spans = {}
+    for _ in range(cores * (W + K)):
+        k, r, t0, t1 = queue.get()
+        s0, s1 = spans.get(k, (t0, t1))
+        spans[k] = (min(s0, t0), max(s1, t1))
+    for p in procs:
+        p.join()
+    walls = [spans[k][1] - spans[k][0] for k in range(W, W + K)]
+    wall = statistics.median(walls)
+    value = cores * REF_STEPS / wall
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
-            "steps": len(vals), "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True,
+            "steps": K, "warmup": W, "ms_per_step": wall * 1e3 / REF_STEPS, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded states",
             "config": CONFIG,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{cores} processes x 1 segment x {steps} segment-step at 32x65x32 "
-                                       f"(oracle/chan_port.c, the reference algorithm)"},
+                             "sample": f"{cores} processes x 1 segment x {REF_STEPS} segment-steps at 32x65x32 "
+                                       f"per sample (oracle/chan_port.c, the reference algorithm bit for bit); "
+                                       f"instances built before timing; median of {K} samples after {W} warm-up"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     emit(line)
 
