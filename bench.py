@@ -249,6 +249,30 @@ def recon_flops(ninst, g):
 
 
 # ---------------------------------------------------------------------------
+# replicas (one process per GPU; segments never exchange data inside a sweep)
+# ---------------------------------------------------------------------------
+
+def max_over_replicas(ms, dist=None):
+    """The timed region's duration across the replicas: every rank waits at
+    a barrier after its own timed region, and the slowest rank's time is the
+    job's (all-reduce MAX over the process group; the rank's own time
+    without one)."""
+    if dist is None:
+        return float(ms)
+    import torch
+    dist.barrier()
+    t = torch.tensor([float(ms)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, nseg, K, ms):
+    """Whole-job segment-steps per second: every rank advances its own nseg
+    segments by K steps (weak scaling) in the slowest rank's ms."""
+    return world * nseg * K / (ms * 1e-3)
+
+
+# ---------------------------------------------------------------------------
 # the GB300 arm
 # ---------------------------------------------------------------------------
 
@@ -312,14 +336,8 @@ def run_gb300(a):
         e1.record(stream)
         torch.cuda.synchronize()
     launches = cc.c_launch_count() - launches0
-    if dist:
-        dist.barrier()
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * NSEG * K / (ms * 1e-3)
+    ms = max_over_replicas(e0.elapsed_time(e1), dist)
+    value = replica_value(world, NSEG, K, ms)
 
     # end to end through the host-array C ABI (H2D of the inputs and D2H of
     # the results inside the timed region), from pinned host buffers

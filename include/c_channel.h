@@ -295,8 +295,10 @@ int c_setup_table(int Nx, int Ny, int Nz, double Lx, double Lz, double Re,
    1 their weighted transposes, 2 the inverse transform's z stage, 3 its x
    stage, 4 the forward x stage, 5 the forward z stage, 6 the unscaled
    forward x stage, 7 the bases transposed, 8 Qpw, Qw, Rw plane-major.
-   sizes[0] = uint32 words, sizes[1] = exponents; frag / ex are written when
-   large enough.  Returns 0, or -1 for bad arguments. */
+   sizes[0] = uint32 words, sizes[1] = exponents.  With frag and ex null the
+   call is a size query; a non-null buffer shorter than its table
+   (nfrag < sizes[0] or nex < sizes[1]) is refused with -2 and nothing is
+   written.  Returns 0, -1 for bad arguments, -2 for a short buffer. */
 int c_setup_tc_table(int Nx, int Ny, int Nz, double Lx, double Lz, double Re,
                      double flux, double dt, int which, uint32_t *frag,
                      long long nfrag, int *ex, long long nex, long long *sizes);

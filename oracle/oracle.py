@@ -29,7 +29,11 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 PORT_LIB = HERE / "_build" / "libchanport.so"
 REF_LIB = HERE / "_ref" / "libref_channel.so"
-REF_DIR = Path("/root/reference/channel")
+# The reference's channel/ directory: $SHADOW_CHANNEL_REFERENCE (the root of
+# a reference checkout), else a checkout named "reference" beside this
+# repository; absent on hosts that only run the port.
+REF_DIR = Path(os.environ["SHADOW_CHANNEL_REFERENCE"]) / "channel" if os.environ.get(
+    "SHADOW_CHANNEL_REFERENCE") else HERE.parent.parent / "reference" / "channel"
 
 _c_int = ctypes.c_int
 _c_dbl = ctypes.c_double

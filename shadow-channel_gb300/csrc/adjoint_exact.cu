@@ -302,7 +302,8 @@ __device__ void contract_planes_tc(const Grid& g, const uint4* __restrict__ T, c
       const int row = mt * 16 + gq + 8 * rr;
       if (row >= N || col >= nx) continue;
       const int e = TE[(size_t)b * g.R + row] + ecol - 64;
-      const cpx val = {round_fast(Hh[2 * rr], Ll[2 * rr], e), round_fast(Hh[2 * rr + 1], Ll[2 * rr + 1], e)};
+      const cpx val = {round_col(Hh[2 * rr], Ll[2 * rr], e, ecol + 1022),
+                       round_col(Hh[2 * rr + 1], Ll[2 * rr + 1], e, ecol + 1022)};
       comb(row, col, val);
     }
   }
@@ -455,7 +456,7 @@ __device__ void quad_T_tc(const Grid& g, int z, int x0, int nx, int xfirst, Solv
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const int y = min(mt * 16 + gq + 8 * (r >> 1), g.Q - 1);
-        v[b][r] = round_fast(Hh[r], Ll[r], g.tcWTE[(size_t)b * g.Q + y] + ecol - 64);
+        v[b][r] = round_col(Hh[r], Ll[r], g.tcWTE[(size_t)b * g.Q + y] + ecol - 64, ecol + 1022);
       }
     }
 #pragma unroll

@@ -10,6 +10,7 @@
 // The reference keeps one solver per process in globals (channel/main.h:81-201)
 // and the Python layer enforces a single init (channel/__init__.py:80-82);
 // this library keeps one Engine per process likewise.
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -57,10 +58,22 @@ static void set_error(int code, const char* fmt, ...) {
     }                                                                              \
   } while (0)
 
-#define LK(call)            \
-  do {                      \
-    ++g_launches;           \
-    CK(call);               \
+// an NVTX range around each kernel launch (named by the launch call) and
+// each entry-point operation: profilers that attach an NVTX tool see which
+// sweep and substage a kernel was enqueued from; without a tool the calls
+// return at once
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
+#define LK(call)                    \
+  do {                              \
+    ++g_launches;                   \
+    NvtxRange nvtx_launch_(#call);  \
+    CK(call);                       \
   } while (0)
 
 // the reference asserts shapes and aborts (channel/channel.i:45-48)
@@ -273,7 +286,20 @@ struct Work {
     *p = reinterpret_cast<T*>(q);
     return true;
   }
+  // Instantiated one-step graphs, kept across calls: the key holds every
+  // value the captured launches read (sweep kind, options, the arrays they
+  // address, the grid's kernel variants), so a matching entry replays the
+  // same launches.  At most kMaxGraphs, the oldest dropped first.
+  struct StepGraph {
+    std::string key;
+    cudaGraphExec_t exec;
+    long long per_step;
+  };
+  std::vector<StepGraph> graphs;
+  static constexpr size_t kMaxGraphs = 32;
   void release() {
+    for (StepGraph& sg : graphs) cudaGraphExecDestroy(sg.exec);
+    graphs.clear();
     for (void* p : ptrs) cudaFree(p);
     ptrs.clear();
     *this = Work();
@@ -801,36 +827,73 @@ static bool enqueue_adjoint_exact_step(Engine& e, Work& w, bool cached, const cp
   return true;
 }
 
-// capture one step into a graph and replay it nsteps times
+// the key of a step graph: raw bytes of the values its launches read
+struct GraphKey {
+  std::string s;
+  template <typename T>
+  GraphKey& add(const T& v) {
+    s.append(reinterpret_cast<const char*>(&v), sizeof(T));
+    return *this;
+  }
+};
+
+// what every step graph of a working set reads besides its own options:
+// the grid (sizes, tables, kernel variants) and the arrays that a sweep may
+// point elsewhere for its duration, and the LSS window chaining of the
+// coupling's time derivative
+static GraphKey step_key(const Engine& e, const Work& w, char kind) {
+  GraphKey k;
+  k.add(kind).add(e.T.g).add(w.MC).add(w.Ft).add(w.gdev).add(w.nseg).add(w.ntan).add(w.chain);
+  return k;
+}
+
+static GraphKey& add_opts(GraphKey& k, const FwdOpts& o) {
+  return k.add(o.adv_primal).add(o.tangents).add(o.ru).add(o.forced_mask).add(o.raw_u_first).add(o.cache)
+      .add(o.store).add(o.re2_mask).add(o.re3_mask);
+}
+
+// one step captured into a graph (or taken from the working set's graphs
+// when the key matches) and replayed nsteps times
 template <typename F>
-static bool run_steps(Engine& e, int nsteps, F&& enqueue) {
+static bool run_steps(Engine& e, Work& w, const GraphKey& key, int nsteps, F&& enqueue) {
   if (nsteps <= 0) return true;
   if (nsteps == 1) return enqueue();
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  CK(cudaStreamBeginCapture(e.st, cudaStreamCaptureModeThreadLocal));
-  const long long before = g_launches;
-  bool ok = enqueue();
-  cudaError_t ce = cudaStreamEndCapture(e.st, &graph);
-  if (!ok) {
-    if (graph) cudaGraphDestroy(graph);
-    return false;
+  Work::StepGraph* sg = nullptr;
+  for (Work::StepGraph& x : w.graphs)
+    if (x.key == key.s) sg = &x;
+  int replays = nsteps;
+  if (!sg) {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    CK(cudaStreamBeginCapture(e.st, cudaStreamCaptureModeThreadLocal));
+    const long long before = g_launches;
+    bool ok = enqueue();
+    cudaError_t ce = cudaStreamEndCapture(e.st, &graph);
+    if (!ok) {
+      if (graph) cudaGraphDestroy(graph);
+      return false;
+    }
+    CK(ce);
+    const long long per_step = g_launches - before;
+    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ie);
+    if (w.graphs.size() >= Work::kMaxGraphs) {
+      cudaGraphExecDestroy(w.graphs.front().exec);
+      w.graphs.erase(w.graphs.begin());
+    }
+    w.graphs.push_back(Work::StepGraph{key.s, exec, per_step});
+    sg = &w.graphs.back();
+    replays = nsteps - 1;  // the capture counted one step's launches
   }
-  CK(ce);
-  const long long per_step = g_launches - before;
-  cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);
-  CK(ie);
   for (int n = 0; n < nsteps; ++n) {
-    cudaError_t le = cudaGraphLaunch(exec, e.st);
+    cudaError_t le = cudaGraphLaunch(sg->exec, e.st);
     if (le != cudaSuccess) {
-      cudaGraphExecDestroy(exec);
       set_error(-1, "cudaGraphLaunch: %s", cudaGetErrorString(le));
       return false;
     }
   }
-  g_launches += per_step * (nsteps - 1);
-  CK(cudaGraphExecDestroy(exec));
+  g_launches += sg->per_step * replays;
   return true;
 }
 
@@ -994,6 +1057,7 @@ static bool autotune_transforms(Engine& e, Work& w) {
 
 // primal from C (device, nseg arrays) or, when C == nullptr, the laminar start
 static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
+  NvtxRange nvtx_op("op_primal");
   const size_t csz = w.csz;
   CK(cudaMemsetAsync(w.MC, 0, sizeof(cpx) * (size_t)w.nseg * w.traj, e.st));
   if (C) {
@@ -1041,7 +1105,8 @@ static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
     }
     const int cnt = n1 - n;
     n = n1;
-    return run_steps(e, cnt, [&] { return enqueue_forward_step(e, w, oo); });
+    GraphKey key = step_key(e, w, 'p');
+    return run_steps(e, w, add_opts(key, oo), cnt, [&] { return enqueue_forward_step(e, w, oo); });
   };
   if (!run_range(ru, false) || !run_range(ru + w.nsteps, true)) return false;
   if (!C && ru == 0 && w.Pc && w.nsteps > 0) {
@@ -1085,6 +1150,7 @@ struct Forcing {
 
 static bool op_forward(Engine& e, Work& w, int start, int end, const cpx* C, const cpx* IC, Forcing f,
                        bool adv_primal) {
+  NvtxRange nvtx_op(adv_primal ? "op_forward" : "op_tangent");
   const size_t csz = w.csz;
   const int nt = w.nseg * w.ntan;
   if (adv_primal) {
@@ -1124,7 +1190,8 @@ static bool op_forward(Engine& e, Work& w, int start, int end, const cpx* C, con
   FwdOpts o{adv_primal || readvance, w.ntan > 0, 0, f.forced, false, cache && !readvance, !readvance};
   o.re2_mask = f.re2;
   o.re3_mask = f.re3;
-  if (!run_steps(e, end - start, [&] { return enqueue_forward_step(e, w, o); })) return false;
+  GraphKey key = step_key(e, w, 'f');
+  if (!run_steps(e, w, add_opts(key, o), end - start, [&] { return enqueue_forward_step(e, w, o); })) return false;
   const bool with_vel = w.ntan > 0 && w.Pv != nullptr;
   if (adv_primal || with_vel) {
     if (!collect_status(e, w)) return false;
@@ -1141,6 +1208,7 @@ static bool op_forward(Engine& e, Work& w, int start, int end, const cpx* C, con
 }
 
 static bool op_adjoint(Engine& e, Work& w, int start, int end, const cpx* AC, double strength) {
+  NvtxRange nvtx_op("op_adjoint");
   CK(cudaMemcpyAsync(w.Ca, AC, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
   CK(cudaMemcpyAsync(w.Sa, AC, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, e.st));
   if (!reset_status(e, w) || !set_step(e, w, start)) return false;
@@ -1150,7 +1218,9 @@ static bool op_adjoint(Engine& e, Work& w, int start, int end, const cpx* AC, do
   bool cpl_cached = true;
   for (int i = end; i < start; ++i) cpl_cached = cpl_cached && w.coupling_cached(i);
   if (sdt != 0.0 && start > end && !enqueue_coupling(e, w, 0, 0.0, w.coupling_cached(start))) return false;
-  return run_steps(e, start - end, [&] { return enqueue_adjoint_step(e, w, sdt, cached, cpl_cached); });
+  GraphKey key = step_key(e, w, 'a');
+  key.add(sdt).add(cached).add(cpl_cached);
+  return run_steps(e, w, key, start - end, [&] { return enqueue_adjoint_step(e, w, sdt, cached, cpl_cached); });
 }
 
 // The transpose of the homogeneous tangent from `end` to `start` applied to
@@ -1164,6 +1234,7 @@ static bool op_adjoint(Engine& e, Work& w, int start, int end, const cpx* AC, do
 //   lambda_n = T_n^T lambda_{n+1} + src,  n = start - 1 .. end,
 // the cotangent of a sum over steps end .. start - 1 of a linear functional.
 static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* AC, const cpx* src = nullptr) {
+  NvtxRange nvtx_op("op_adjoint_exact");
   const size_t csz = w.csz;
   const bool readvance = w.raw_start && end == 0;
   cpx* scratch = nullptr;
@@ -1191,7 +1262,8 @@ static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* 
     w.Ft = scratch_ft;
     bool ok = set_step(e, w, 0);
     FwdOpts o{true, false, 0, 0u, false, false, true};
-    ok = ok && run_steps(e, start, [&] { return enqueue_forward_step(e, w, o); });
+    GraphKey key = step_key(e, w, 'r');
+    ok = ok && run_steps(e, w, add_opts(key, o), start, [&] { return enqueue_forward_step(e, w, o); });
     w.MC = keep_mc;
     w.Ft = keep_ft;
     if (!ok) {
@@ -1210,7 +1282,10 @@ static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* 
     ok = false;
   }
   ok = ok && set_step(e, w, start);
-  ok = ok && run_steps(e, start - end, [&] { return enqueue_adjoint_exact_step(e, w, cached, traj, w.traj, src); });
+  GraphKey key = step_key(e, w, 'x');
+  key.add(cached).add(traj).add(w.traj).add(src);
+  ok = ok && run_steps(e, w, key, start - end,
+                       [&] { return enqueue_adjoint_exact_step(e, w, cached, traj, w.traj, src); });
   if (ok) {
     // the tangent starts from IU = Recon(IC)
     SolveTArgs t{};

@@ -73,10 +73,30 @@ extern "C" int c_spec2phys_noalloc(const chn_complex* C_dev, double* flow_dev) {
     engine_set_error(-2, "c_spec2phys_noalloc called before c_init");
     return -2;
   }
-  // the one-block-per-plane transforms (they need no intermediate; every
-  // grid within the capacity below fits them)
+  // the one-block-per-plane transforms: they need no intermediate array.
+  // The tensor-core inverse (the default) fits every grid within the
+  // capacity below; the FP64 one (CHN_TRANSFORMS_FP64=1, or where the
+  // tensor-core inverse did not fit at c_init) is checked against the
+  // device's shared memory per block.
   Grid g = *gp;
   g.split = 0;
+  if (!g.tci) {
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+      engine_set_error(-1, "c_spec2phys_noalloc: no usable current device");
+      return -1;
+    }
+    if (!fused_transforms_fit(g, optin)) {
+      char msg[256];
+      snprintf(msg, sizeof(msg),
+               "c_spec2phys_noalloc: grid %dx%dx%d: the one-block-per-plane FP64 transforms need %zu bytes of "
+               "shared memory per block, the device allows %d",
+               g.Nx, g.Ny, g.Nz, phys_smem_bytes(g, true), optin);
+      engine_set_error(-5, msg);
+      return -5;
+    }
+  }
   const size_t need_u = u_size(g);
   const size_t need_p = (size_t)3 * g.Q * plane_size(g);
   if (need_u > kNoAllocU || need_p > kNoAllocP) {

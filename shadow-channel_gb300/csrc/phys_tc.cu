@@ -305,14 +305,14 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
           const bool im = row >= d.pzh;
           const int m = im ? row - d.pzh : row, fl = col / g.X, x = col - fl * g.X;
           const bool counts = !(im && x == 0);
-          const double vp = round_fast(HE[r] + HO[r], LE[r] + LO[r], e);
+          const double vp = round_col(HE[r] + HO[r], LE[r] + LO[r], e, exz[col]);
           cpx& zp = Zb[((size_t)fl * g.pz + m) * g.X + x];
           if (im) zp.im = vp;
           else zp.re = vp;
           const int ep = (int)((__double_as_longlong(vp) >> 52) & 0x7FF);
           if (counts && ep) atomicMax(&exx[fl * g.pz + m], ep);
           if (d.Rz == 2) {
-            const double vm = round_fast(HE[r] - HO[r], LE[r] - LO[r], e);
+            const double vm = round_col(HE[r] - HO[r], LE[r] - LO[r], e, exz[col]);
             cpx& zm = Zb[((size_t)fl * g.pz + m + d.pzh) * g.X + x];
             if (im) zm.im = vm;
             else zm.re = vm;
@@ -359,11 +359,11 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
           const int fl = col / g.pz, m = col - fl * g.pz;
           const int e = g.tcXE[xp] + exx[col] - 1022 - 64;
           double* Pr = P + ((size_t)(f0 + fl) * g.Q + y) * plane + (size_t)m * g.px;
-          const double vp = round_fast(HE[r] + HO[r], LE[r] + LO[r], e);
+          const double vp = round_col(HE[r] + HO[r], LE[r] + LO[r], e, exx[col]);
           Pr[xp] = vp;
           nonfinite |= !finite_bits(vp);
           if (d.Rx == 2) {
-            const double vm = round_fast(HE[r] - HO[r], LE[r] - LO[r], e);
+            const double vm = round_col(HE[r] - HO[r], LE[r] - LO[r], e, exx[col]);
             Pr[xp + d.pxh] = vm;
             nonfinite |= !finite_bits(vm);
           }
@@ -524,7 +524,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
         for (int r = 0; r < 4; ++r) {
           const int row = mt * 16 + gq + 8 * (r >> 1), zp = nt * 8 + 2 * t + (r & 1);
           if (row >= 2 * g.X || zp >= g.pz) continue;
-          const double v = round_fast(Hh[r], Ll[r], AxE[row] + exx[zp] - 1022 - 64);
+          const double v = round_col(Hh[r], Ll[r], AxE[row] + exx[zp] - 1022 - 64, exx[zp]);
           cpx& yv = Yb[(size_t)zp * g.X + (row >> 1)];
           if (row & 1) yv.im = v;
           else yv.re = v;
@@ -563,7 +563,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
         for (int r = 0; r < 4; ++r) {
           const int row = mt * 16 + gq + 8 * (r >> 1), kx = nt * 8 + 2 * t + (r & 1);
           if (row >= 2 * d.Kk || kx >= g.X) continue;
-          const double v = round_fast(Hh[r], Ll[r], g.tcFZE[row] + exz[kx] - 1022 - 64);
+          const double v = round_col(Hh[r], Ll[r], g.tcFZE[row] + exz[kx] - 1022 - 64, exz[kx]);
           cpx& fv = Fb[(size_t)(row >> 1) * g.X + kx];
           if (row & 1) fv.im = v;
           else fv.re = v;

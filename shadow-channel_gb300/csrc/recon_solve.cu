@@ -467,7 +467,8 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
         const int row = mt * 16 + gq + 8 * rr;
         if (row >= N || col >= nx) continue;
         const int e = g.tcWE[(size_t)w * g.R + row] + ecol - 64;
-        const cpx val = {round_fast(Hh[2 * rr], Ll[2 * rr], e), round_fast(Hh[2 * rr + 1], Ll[2 * rr + 1], e)};
+        const cpx val = {round_col(Hh[2 * rr], Ll[2 * rr], e, ecol + 1022),
+                         round_col(Hh[2 * rr + 1], Ll[2 * rr + 1], e, ecol + 1022)};
         cpx& f = F[row * kTile + col];
         if (first) {
           f = val;

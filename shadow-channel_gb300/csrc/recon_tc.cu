@@ -243,7 +243,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
         const int y = mt * 16 + gq + 8 * rr;
         if (y >= g.Q || col >= nx || (meancol && col == 0)) continue;
         const int e = g.tcE[(size_t)b * g.Q + y] + ecol - 64;
-        const cpx val = {round_fast(H[2 * rr], L[2 * rr], e), round_fast(H[2 * rr + 1], L[2 * rr + 1], e)};
+        const cpx val = {round_col(H[2 * rr], L[2 * rr], e, ecol + 1022),
+                         round_col(H[2 * rr + 1], L[2 * rr + 1], e, ecol + 1022)};
         const int x = x0 + col;
         cpx* out = U + ((size_t)z * 5 * g.Q + y) * g.X + x;
         const double ax = g.kxK2[(size_t)z * g.X + x], az = g.kzK2[(size_t)z * g.X + x];

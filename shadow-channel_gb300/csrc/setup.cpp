@@ -361,7 +361,9 @@ extern "C" int c_setup_tc_table(int Nx, int Ny, int Nz, double Lx, double Lz, do
   if (!ok) return -1;
   sizes[0] = (long long)f[sel].size();
   sizes[1] = (long long)e[sel].size();
-  if (frag && nfrag >= sizes[0]) std::memcpy(frag, f[sel].data(), sizeof(uint32_t) * f[sel].size());
-  if (ex && nex >= sizes[1]) std::memcpy(ex, e[sel].data(), sizeof(int) * e[sel].size());
+  // null buffers: a size query; a buffer shorter than its table: an error
+  if ((frag && nfrag < sizes[0]) || (ex && nex < sizes[1])) return -2;
+  if (frag) std::memcpy(frag, f[sel].data(), sizeof(uint32_t) * f[sel].size());
+  if (ex) std::memcpy(ex, e[sel].data(), sizeof(int) * e[sel].size());
   return 0;
 }

@@ -83,6 +83,13 @@ __device__ __forceinline__ double round_fast(long long H, long long L, int e) {
   return scalbn(v, es);
 }
 
+// round_fast for an output of a column whose largest biased exponent field
+// is ce: a column that held an infinity or a NaN (ce = 0x7FF; its digits
+// carry no meaning) gives NaN, as the FP64 sum would
+__device__ __forceinline__ double round_col(long long H, long long L, int e, int ce) {
+  return ce == 0x7FF ? __longlong_as_double(0x7FF8000000000000LL) : round_fast(H, L, e);
+}
+
 // x is neither infinite nor NaN (integer test on the exponent field)
 __device__ __forceinline__ bool finite_bits(double x) {
   return ((__double_as_longlong(x) >> 52) & 0x7FF) != 0x7FF;

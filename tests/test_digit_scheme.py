@@ -88,19 +88,60 @@ def test_contraction_is_faithful():
         assert abs(Fraction(v) - true) <= 2 * n * Fraction(2) ** -55 * scale + abs(true) * Fraction(2) ** -52
 
 
-def test_chunk_bound_worst_case():
-    """112 terms whose digits all take their largest same-sign values (top
-    digit 255, the others 127: the largest |x| < 2^56 with such digits):
-    every FP32 level sum of the chunk stays an exact integer below 2^24."""
-    x = sum(d * 256 ** (6 - i) for i, d in enumerate([255] + [127] * 6))
-    d = digits(x)
-    assert d == [255] + [127] * 6
+def test_level_bounds_below_2_24():
+    """The analytic bound of every level: with |d0| <= 256 and |d_i| <= 128
+    (i >= 1) a term of level l contributes at most
+    sum_{i+k=l} max|a_i| max|b_k|; level 6 is the largest,
+    2 * 256 * 128 + 5 * 128^2 = 147456 per term, and 112 terms give
+    16,515,072 < 2^24: every partial sum of a chunk is an integer FP32 holds
+    exactly."""
+    top = [256] + [128] * 6
+    bounds = [K_CHUNK * sum(top[i] * top[l - i] for i in range(l + 1) if l - i < 7) for l in range(7)]
+    assert bounds[6] == 16_515_072 == max(bounds)
+    assert all(b < 2 ** 24 for b in bounds)
+
+
+def _chunk_sums_exact(da, db):
+    """FP32 level sums of K_CHUNK equal terms, against exact integers"""
     acc = np.zeros(7, np.float32)
     exact = [0] * 7
     for _ in range(K_CHUNK):
         for i in range(7):
             for k in range(7 - i):
-                acc[i + k] = np.float32(acc[i + k] + np.float32(d[i] * d[k]))
-                exact[i + k] += d[i] * d[k]
-    assert max(exact) < 2 ** 24
-    assert [int(v) for v in acc] == exact
+                acc[i + k] = np.float32(acc[i + k] + np.float32(da[i] * db[k]))
+                exact[i + k] += da[i] * db[k]
+    return acc, exact
+
+
+def test_chunk_bound_worst_case():
+    """The extreme digit vectors a 56-bit operand can take, each summed over
+    a full chunk of 112 terms: every FP32 level sum stays an exact integer
+    below 2^24.  Cases: top digit 256 with every lower digit -128 (the
+    largest magnitudes, reachable because the lower digits pull |x| below
+    2^56); the sign-aligned maximum of |level 6| (top digit -255, lower
+    digits -128: every product of level 6 positive; a top digit of -256
+    with them would leave the range); the largest same-sign positive digits
+    (255, 127, ...); and mixed pairs of them."""
+    S = sum(256 ** i for i in range(6))
+    cases = {
+        "256,-128": 256 * 256 ** 6 - 128 * S,
+        "-255,-128": -255 * 256 ** 6 - 128 * S,
+        "255,127": sum(d * 256 ** (6 - i) for i, d in enumerate([255] + [127] * 6)),
+        "-256,127": -256 * 256 ** 6 + 127 * S,
+    }
+    want = {"256,-128": [256] + [-128] * 6, "-255,-128": [-255] + [-128] * 6,
+            "255,127": [255] + [127] * 6, "-256,127": [-256] + [127] * 6}
+    dig = {}
+    for name, x in cases.items():
+        assert abs(x) < 2 ** 56, name
+        dig[name] = digits(x)
+        assert dig[name] == want[name], name
+    worst6 = 0
+    for na, da in dig.items():
+        for nb, db in dig.items():
+            acc, exact = _chunk_sums_exact(da, db)
+            assert max(abs(v) for v in exact) < 2 ** 24, (na, nb)
+            assert [int(v) for v in acc] == exact, (na, nb)
+            worst6 = max(worst6, abs(exact[6]))
+    # the sign-aligned case reaches 112 * (2 * 255 * 128 + 5 * 128^2)
+    assert worst6 == K_CHUNK * (2 * 255 * 128 + 5 * 128 * 128)

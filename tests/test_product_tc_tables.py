@@ -168,3 +168,19 @@ def test_adjoint_tables(lib):
         ref = np.zeros((Q, R))
         ref[:, :rows] = setup(lib, which, (rows, Q)).T
         assert close(dec[b][:, :R], ref), b
+
+
+def test_short_buffer_is_refused(lib):
+    """A non-null buffer shorter than its table is an error (-2), not a
+    silent success that leaves the caller's memory unwritten; null buffers
+    stay a size query."""
+    L = lib
+    sizes = (ctypes.c_longlong * 2)()
+    assert L.c_setup_tc_table(*GRID, 2, None, 0, None, 0, sizes) == 0
+    frag = np.full(sizes[0], 7, np.uint32)
+    ex = np.full(sizes[1], 7, np.int32)
+    assert L.c_setup_tc_table(*GRID, 2, frag.ctypes.data, sizes[0] - 1, ex.ctypes.data, sizes[1], sizes) == -2
+    assert L.c_setup_tc_table(*GRID, 2, frag.ctypes.data, sizes[0], ex.ctypes.data, sizes[1] - 1, sizes) == -2
+    assert (frag == 7).all() and (ex == 7).all()
+    assert L.c_setup_tc_table(*GRID, 2, frag.ctypes.data, sizes[0], None, 0, sizes) == 0
+    assert not (frag == 7).all()
