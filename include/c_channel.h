@@ -79,6 +79,19 @@ void c_adjoint_exact(int start_step, int end_step, chn_complex *AC_given,
 void c_adjoint_exact_source(int start_step, int end_step,
                             chn_complex *AC_given, const chn_complex *src,
                             int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup);
+/* c_adjoint_exact_source (src may be null: no source) that also returns the
+   two parameter gradients of the same functional in grad[2]:
+     grad[0] = dJ/dmeanU, the cotangents of the mean-flux forcing the
+               reference's inhomogeneous tangent adds to every substage
+               (channel/increproject0.c:209-214; c_tangent_forcing kind 1);
+     grad[1] = dJ/dRe, of the exact Re forcing -re^2 dt (a_k D x_k +
+               b_k D x_{k+1}) of every substage (c_tangent_forcing kind 3),
+   where J = <AC_given, C_start_step> + sum_n <src, C_n>: one reverse sweep
+   gives what one forced tangent sweep per parameter gives.  The Re parts
+   are summed in a fixed order (bit-reproducible).  Returns the status
+   (c_last_error).  No reference counterpart. */
+int c_adjoint_exact_grad(int start_step, int end_step, chn_complex *AC_given,
+                         const chn_complex *src, double *grad);
 
 /* channel.i:96-105 -> channel.c:704 ddt_project() */
 double c_ddt_project(int i_step, chn_complex *IC_given, int Nz_dup,
@@ -130,7 +143,11 @@ double c_last_cfl(void);
 
 /* Batched segments: nseg independent trajectories on the c_init grid, each
    with ntan tangents; the adjoint couples (strength != 0) to the stored
-   trajectory of tangent `couple`.  Host arrays, segment-major. */
+   trajectory of tangent `couple`.  Host arrays, segment-major.  The sweep
+   calls return the call's status, the value c_last_error() returns after
+   it: a segment stopped by the CFL limit or holding non-finite values
+   gives bits 0 / 1 and leaves the other segments' results as they would
+   be without it. */
 int c_batch_init(int nseg, int ntan, int couple);
 /* the same with a trajectory length of the batch's own (<= any length; the
    reference's nsteps of c_init is not used by the batch) */
@@ -177,6 +194,11 @@ int c_batch_adjoint_dev(int start_step, int end_step, chn_complex *AC,
 int c_batch_adjoint_exact_dev(int start_step, int end_step, chn_complex *AC);
 int c_batch_adjoint_exact_source_dev(int start_step, int end_step,
                                      chn_complex *AC, const chn_complex *src);
+/* the same with the parameter gradients of c_adjoint_exact_grad per segment:
+   grad (host) [nseg][2] = dJ/dmeanU, dJ/dRe; src device, may be null */
+int c_batch_adjoint_exact_grad_dev(int start_step, int end_step,
+                                   chn_complex *AC, const chn_complex *src,
+                                   double *grad);
 int c_batch_primal_dev(int ru_steps, chn_complex *C);
 int c_batch_tangent_dev(int start_step, int end_step, chn_complex *IC,
                         const int *inhomo);

@@ -19,7 +19,7 @@ ROOT = HERE.parent
 CSRC = HERE / "csrc"
 OUT_DIR = HERE / "_build"
 LIB = HERE / "libc_channel.so"
-SOURCES = ["engine.cu", "phys.cu", "phys_tc.cu", "recon_solve.cu", "recon_tc.cu", "adjoint_exact.cu", "misc.cu", "noalloc.cu", "lss.cu", "stats.cu", "split_variants_a.cu", "split_variants_b.cu", "setup.cpp"]
+SOURCES = ["engine.cu", "phys.cu", "phys_tc.cu", "phys_tc5.cu", "recon_solve.cu", "recon_tc.cu", "adjoint_exact.cu", "misc.cu", "noalloc.cu", "lss.cu", "stats.cu", "split_variants_a.cu", "split_variants_b.cu", "setup.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -9,15 +9,15 @@ returns the time-mean wall shear
 (the reference's Uxb of the mean flow, channel/project0.c:224-234), and
 whose backward returns dJ/dRe, dJ/dmeanU and, when the initial state is
 passed as a tensor, dJ/dC0.  The derivatives are exact derivatives of the
-discrete RK3 scheme: tangent sweeps with the Re forcing (c_tangent_forcing
-kind 3) and the mean-flux forcing (kind 1, the reference's inhomogeneous
-tangent), whose wall shear is read from the stored tangent trajectory; and
-for the state, one reverse sweep of the exact discrete adjoint
-(c_adjoint_exact_source, the transpose of the homogeneous tangent) with the
+discrete RK3 scheme, all three from ONE reverse sweep of the exact discrete
+adjoint (c_adjoint_exact_grad, the transpose of the tangent) with the
 wall-shear weights as its per-step source:
-    dJ/dC0 = (1/N) sum_n T(0 -> n)^T g,   g = Rp0 on Re C[0, 0, :, 0].
-For a scalar parameter the tangent sweep costs what one adjoint sweep costs;
-for the state (every coefficient at once) only the adjoint sweep is cheap.
+    dJ/dC0 = (1/N) sum_n T(0 -> n)^T g,   g = Rp0 on Re C[0, 0, :, 0],
+and dJ/dRe, dJ/dmeanU from the cotangents of the exact Re forcing
+(c_tangent_forcing kind 3) and of the mean-flux forcing (kind 1, the
+reference's inhomogeneous tangent) at every substage of the same sweep.
+``tangent_gradients`` gives the two parameter derivatives by the forced
+tangent sweeps instead (one sweep per parameter), as a cross-check.
 
 Memory: the primal is checkpointed every ``checkpoint`` steps (one
 coefficient array per checkpoint, host memory); the backward recomputes the
@@ -64,25 +64,28 @@ def primal_objective(grid, Re, meanU, C0, nsteps, checkpoint):
     return J / nsteps, ckpts, chunks
 
 
-def state_gradient(grid, Re, meanU, ckpts, chunks, nsteps):
-    """dJ/dC0 (complex, the gradient with respect to the real and imaginary
-    parts) by the exact discrete adjoint, one checkpoint interval at a time
-    from the last: each interval's primal is recomputed from its checkpoint
-    and its transposed tangent carries lambda back with the source
-    g / nsteps added at every step."""
+def adjoint_gradients(grid, Re, meanU, ckpts, chunks, nsteps):
+    """(dJ/dC0, dJ/dmeanU, dJ/dRe) from one exact-adjoint sweep, one
+    checkpoint interval at a time from the last: each interval's primal is
+    recomputed from its checkpoint, its transposed tangent carries lambda
+    back with the source g / nsteps added at every step, and the interval's
+    parameter gradients (the forcings' cotangents along it) add up."""
     shape = ckpts[0].shape
     lam = np.zeros(shape, np.complex128)
     src = None
+    gU = gRe = 0.0
     for C, k in zip(reversed(ckpts), reversed(chunks)):
         _init(grid, Re, meanU, k)
         c_channel.c_primal(0, C.copy())
         if src is None:
             src = np.zeros(shape, np.complex128)
             src[0, 0, :, 0] = c_channel.c_wall_shear_weights() / nsteps
-        c_channel.c_adjoint_exact_source(k, 0, lam, src)
+        u, r = c_channel.c_adjoint_exact_grad(k, 0, lam, src)
         if c_channel.c_last_error() != 0:
             raise RuntimeError("adjoint sweep failed: " + c_channel.c_last_error_message())
-    return lam
+        gU += u
+        gRe += r
+    return lam, gU, gRe
 
 
 def tangent_gradients(grid, Re, meanU, ckpts, chunks, nsteps, kinds=(3, 1)):
@@ -133,12 +136,12 @@ class TimeMeanWallShear(torch.autograd.Function):
         g = float(gJ)
         nsteps = int(ctx.cfg["nsteps"])
         gRe = gU = gC = None
-        if ctx.needs_input_grad[0] or ctx.needs_input_grad[1]:
-            d = tangent_gradients(ctx.cfg["grid"], Re, meanU, ctx.ckpts, ctx.chunks, nsteps)
-            gRe = torch.tensor(g * d[3], dtype=torch.float64)
-            gU = torch.tensor(g * d[1], dtype=torch.float64)
+        lam, dU, dRe = adjoint_gradients(ctx.cfg["grid"], Re, meanU, ctx.ckpts, ctx.chunks, nsteps)
+        if ctx.needs_input_grad[0]:
+            gRe = torch.tensor(g * dRe, dtype=torch.float64)
+        if ctx.needs_input_grad[1]:
+            gU = torch.tensor(g * dU, dtype=torch.float64)
         if ctx.c0_meta is not None and len(ctx.needs_input_grad) > 3 and ctx.needs_input_grad[3]:
-            lam = state_gradient(ctx.cfg["grid"], Re, meanU, ctx.ckpts, ctx.chunks, nsteps)
             shape, dtype, device = ctx.c0_meta
             gC = torch.from_numpy(np.ascontiguousarray(lam).view(np.float64).reshape(shape) * g).to(
                 device=device, dtype=dtype)

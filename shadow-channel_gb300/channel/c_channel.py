@@ -53,6 +53,8 @@ _lib.c_adjoint_exact.argtypes = [_i, _i, _vp, _i, _i, _i, _i]
 _lib.c_adjoint_exact.restype = None
 _lib.c_adjoint_exact_source.argtypes = [_i, _i, _vp, _vp, _i, _i, _i, _i]
 _lib.c_adjoint_exact_source.restype = None
+_lib.c_adjoint_exact_grad.argtypes = [_i, _i, _vp, _vp, _vp]
+_lib.c_adjoint_exact_grad.restype = _i
 _lib.c_ddt_project.argtypes = [_i, _vp, _i, _i, _i, _i]
 _lib.c_ddt_project.restype = _d
 _lib.c_getsoln.argtypes = [_i, _pp, _ip, _ip, _ip, _ip]
@@ -113,6 +115,8 @@ _lib.c_batch_adjoint_exact_dev.argtypes = [_i, _i, _vp]
 _lib.c_batch_adjoint_exact_dev.restype = _i
 _lib.c_batch_adjoint_exact_source_dev.argtypes = [_i, _i, _vp, _vp]
 _lib.c_batch_adjoint_exact_source_dev.restype = _i
+_lib.c_batch_adjoint_exact_grad_dev.argtypes = [_i, _i, _vp, _vp, _vp]
+_lib.c_batch_adjoint_exact_grad_dev.restype = _i
 
 _lib.c_stream.argtypes = []
 _lib.c_stream.restype = _vp
@@ -233,6 +237,23 @@ def c_adjoint_exact_source(start_step, end_step, AC_given, src):
     if t != s:
         raise ValueError("src must have the shape of AC_given")
     _lib.c_adjoint_exact_source(int(start_step), int(end_step), p, q, *s)
+
+
+def c_adjoint_exact_grad(start_step, end_step, AC_given, src=None):
+    """c_adjoint_exact_source (src None: no source) returning
+    (dJ/dmeanU, dJ/dRe) of J = <AC, C_start> + sum_n <src, C_n> from the same
+    reverse sweep (the cotangents of the mean-flux and exact Re forcings)."""
+    p, s = _inplace4(AC_given, np.complex128, "c_adjoint_exact_grad")
+    q = None
+    if src is not None:
+        q, t = _inplace4(src, np.complex128, "src")
+        if t != s:
+            raise ValueError("src must have the shape of AC_given")
+    grad = np.zeros(2)
+    rc = _lib.c_adjoint_exact_grad(int(start_step), int(end_step), p, q, grad.ctypes.data)
+    if rc < 0:
+        raise RuntimeError("c_adjoint_exact_grad: " + c_last_error_message())
+    return float(grad[0]), float(grad[1])
 
 
 def c_ddt_project(i_step, IC_given):

@@ -20,6 +20,7 @@
 // physical fields to u_in_bar.
 #include "chn_common.cuh"
 #include "kernels.h"
+#include "solve_common.cuh"
 #include "tc_common.cuh"
 
 namespace chn {
@@ -603,6 +604,36 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
     }
   }
   __syncthreads();
+  // dJ/dRe: <c2_bar, f_Re> of this block's columns (the forcing of
+  // recon_solve.cu's kind 3 rebuilt from the stored primal states)
+  const bool want_g = a.gacc != nullptr;
+  const cpx* xk = nullptr;
+  double ft1 = 0.0, gpart = 0.0;
+  const double re2 = g.re * g.re;
+  const double akf = k == 1 ? -1. / 2 : 1. / 3.;                  // forward a_k
+  const double bkf = k == 0 ? 1. / 6 : (k == 1 ? 2. / 3 : 0.0);  // forward b_k
+  if (want_g) {
+    const int xs = a.xslot.slot();
+    xk = a.Xf + (long long)inst * a.xstride + (long long)xs * a.xslot.stride;
+    if (a.Ftr) ft1 = a.Ftr[(long long)inst * a.ftr_stride + xs + 1];
+    const size_t csz = coef_size(g);
+    for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+      const int r = i / kTile, l = i - r * kTile;
+      if (l >= nx || l < xfirst) continue;
+      const int x = x0 + l;
+      const double k2 = g.K2[(size_t)z * g.X + x];
+      if (r < g.D) {
+        const cpx d0 = visc_v_row(g, k2, xk + cidx(0, 0, x), g.X, r);
+        const cpx d1 = visc_v_row(g, k2, xk + csz + cidx(0, 0, x), g.X, r);
+        const cpx c2 = s.ra[r * kTile + l];
+        gpart -= re2 * dt * (c2.re * (akf * d0.re + bkf * d1.re) + c2.im * (akf * d0.im + bkf * d1.im));
+      }
+      const cpx d0 = visc_g_row(g, k2, xk + cidx(1, 0, x), g.X, r);
+      const cpx d1 = visc_g_row(g, k2, xk + csz + cidx(1, 0, x), g.X, r);
+      const cpx c2 = s.rb[r * kTile + l];
+      gpart += re2 * dt * (c2.re * (akf * d0.re + bkf * d1.re) + c2.im * (akf * d0.im + bkf * d1.im));
+    }
+  }
   // F_bar += dt c_k c2_bar; c_in_bar = E_0^T c2_bar (k == 0) or c2_bar
   for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
     const int r = i / kTile, l = i - r * kTile;
@@ -656,6 +687,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
     double part = 0.0;
     for (int i = lane; i < g.R; i += 32) part = fma(g.add0[i], ca[i].re, part);
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    // the forced tangent adds 0.5 * 2.0 * add to this line's real part
+    // (channel/increproject0.c:209-214): its cotangent is <add, x_bar.re>
+    if (want_g && lane == 0) a.gacc[(long long)inst * a.gstride] += part;
     __syncwarp();
     for (int i = lane; i < g.R; i += 32) ca[i].re = fma(-0.5 * part, g.rwsum[i], ca[i].re);
     __syncwarp();
@@ -665,6 +699,22 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
                                  reinterpret_cast<double*>(lane < 4 ? ca : cb) + pt, 2);
     }
     __syncwarp();
+    if (want_g) {
+      // the mean lines' Re forcing: D0 = -Rps on the primal's solved mean flow
+      // before its flux correction, MC[3n + k + 1] - 0.5 flux_t add
+      const size_t csz = coef_size(g);
+      double mp = 0.0;
+      for (int i = lane; i < g.R; i += 32) {
+        const cpx p0 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + cidx(0, 0, 0), g.X, i);
+        cpx p1 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + csz + cidx(0, 0, 0), g.X, i);
+        p1.re -= 0.5 * ft1 * rps_row_real(g, g.add0, i);
+        const cpx q0 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + cidx(1, 0, 0), g.X, i);
+        const cpx q1 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + csz + cidx(1, 0, 0), g.X, i);
+        mp += re2 * dt * (ca[i].re * (akf * p0.re + bkf * p1.re) + ca[i].im * (akf * p0.im + bkf * p1.im));
+        mp += re2 * dt * (cb[i].re * (akf * q0.re + bkf * q1.re) + cb[i].im * (akf * q0.im + bkf * q1.im));
+      }
+      gpart += mp;  // lane partials; the block reduction below adds every thread's
+    }
     for (int i = lane; i < g.R; i += 32) {
       fa[i] = fma(dt * ck, ca[i].re, fa[i]);
       fb[i] = fma(dt * ck, cb[i].re, fb[i]);
@@ -678,6 +728,19 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
     }
   }
   __syncthreads();
+  if (want_g) {
+    // deterministic block sum of the Re parts into this block's slot
+    __shared__ double gred[kThreads / 32];
+    double v = gpart;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) gred[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += gred[w];
+      a.gacc[(long long)inst * a.gstride + 1 + blockIdx.x] += t;
+    }
+  }
   // H_bar = Quad^T(F_bar) (transpose of channel/project.c:97-115, 177-191):
   //   Hx_bar = -i kx Qpw^T Fa_bar - i kz Rw^T Fb_bar
   //   Hz_bar = -i kz Qpw^T Fa_bar + i kx Rw^T Fb_bar,  Hy_bar = -K2 Qw^T Fa_bar

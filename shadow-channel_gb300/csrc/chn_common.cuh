@@ -117,6 +117,13 @@ struct Grid {
   const int* tcZM;
   int tci;
   int tcminb;  // blocks per SM the tensor-core inverse is compiled for (2 or 3; autotuned)
+  // the same inverse on the fifth-generation tensor cores (phys_tc5.cu,
+  // tcgen05.mma with tensor-memory accumulators): the two stages' digit
+  // tables as stacked B operands in the K-major canonical layout; tc5 = 0:
+  // the mma.sync kernel above (uneven batches always take it)
+  const unsigned char* t5Z;
+  const unsigned char* t5X;
+  int tc5;
   // forward transforms likewise (phys_tc.cu, k_products_tc): x stage
   // [2X][px] (1/(px pz) folded in), z stage [2 (Nz - 1)][2 pz]; tcf = 0: the FFT kernels
   const uint32_t* tcFX;

@@ -207,6 +207,15 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   g.tci = (!(tfp64 && tfp64[0] == '1') && phys_tc_fits(g, optin)) ? 1 : 0;
   g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_fits(g, optin)) ? 1 : 0;
   g.tcminb = 2;  // until the autotuner has timed both builds (3 blocks rarely fit the shared memory)
+  // the inverse on tcgen05 where it fits, with CHN_INVERSE_TC5=1 (the
+  // mma.sync kernel stays the default: it is the faster one today)
+  const char* t5 = getenv("CHN_INVERSE_TC5");
+  g.tc5 = 0;
+  if (g.tci && (t5 && t5[0] == '1') && phys_tc5_fits(g, 6, optin)) {
+    std::vector<uint8_t> zt, xt;
+    if (!build_phys_tc5_tables(h, zt, xt) || !T.up(zt, &g.t5Z) || !T.up(xt, &g.t5X)) return false;
+    g.tc5 = 1;
+  }
   if (solve_smem_bytes(g) > (size_t)optin || recon_smem_bytes(g) > (size_t)optin) {
     set_error(1, "grid %dx%dx%d: the implicit solve needs %zu bytes of shared memory per block, the device has %d",
               Nx, Ny, Nz, solve_smem_bytes(g), optin);
@@ -248,6 +257,11 @@ struct Work {
   std::vector<char> vel_ok;    // slot i of Pv holds the fields of MIC[3i]
   cpx* icp = nullptr;          // projected IC' of the last coupling, per segment
   cpx* src = nullptr;          // per-step source of the exact adjoint (host-array entry point), per segment
+  // parameter gradients of the exact adjoint, per segment: [0] dJ/dmeanU,
+  // [1 + block] the solve blocks' parts of dJ/dRe (summed on the host)
+  double* gacc = nullptr;
+  int gstride = 0;
+  std::vector<double> grad;    // [nseg][2] after the last gradient sweep: dJ/dmeanU, dJ/dRe
   const Grid* gdev = nullptr;  // uneven batch: grid of each segment (device array); null: one grid
   cpx* Zt = nullptr;           // split transforms: spectral-column intermediate for zt_inst instances
   int zt_inst = 0;
@@ -319,7 +333,12 @@ struct Work {
            alloc(&Pprev, nseg * psz) && alloc(&Pl, nseg * psz) && alloc(&flow, (size_t)3 * g.Q * plane_size(g)) &&
            alloc(&part, (size_t)nseg * kDotBlocks * 2) && alloc(&r, nseg) && alloc(&cflmax, nseg) &&
            alloc(&status, nseg) && alloc(&step, 4) && alloc(&icp, nseg * csz) && alloc(&src, nseg * csz) &&
-           alloc(&Ft, (size_t)nseg * (3 * (size_t)nsteps + 1)) && alloc_split(g, nt) && alloc_cache(g);
+           alloc(&Ft, (size_t)nseg * (3 * (size_t)nsteps + 1)) && alloc_split(g, nt) && alloc_cache(g) &&
+           alloc_grad(g);
+  }
+  bool alloc_grad(const Grid& g) {
+    gstride = 1 + g.Nz * ((g.X + 15) / 16);  // the solve's blocks: kz lines x 16-column tiles
+    return alloc(&gacc, (size_t)nseg * gstride);
   }
   // split transforms (required where a plane exceeds a block's shared
   // memory, else an autotuner candidate): room for up to 2 GiB of
@@ -751,7 +770,7 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
 // the state before substage k, slot 3n + k of `traj` (segment stride
 // `tstride`), come from the field cache or are rebuilt into w.Pp.
 static bool enqueue_adjoint_exact_step(Engine& e, Work& w, bool cached, const cpx* traj, long long tstride,
-                                       const cpx* src) {
+                                       const cpx* src, const double* ftr = nullptr, bool grad = false) {
   const Grid& g = e.T.g;
   cudaStream_t st = e.st;
   for (int k = 2; k >= 0; --k) {
@@ -765,6 +784,15 @@ static bool enqueue_adjoint_exact_step(Engine& e, Work& w, bool cached, const cp
     t.ninst = w.nseg;
     t.status = nullptr;
     t.sdiv = 1;
+    if (grad) {
+      t.gacc = w.gacc;
+      t.gstride = w.gstride;
+      t.Xf = traj;
+      t.xstride = tstride;
+      t.xslot = SlotRef{w.step, 3, k - 3, (long long)w.csz};  // MC[3n + k]: slot 3(*step - 1) + k
+      t.Ftr = ftr;
+      t.ftr_stride = 3 * (long long)w.nsteps + 1;
+    }
     LK(launch_solve_T(g, t, st));
     PhysArgs ph{};
     ph.grids = w.gdev;
@@ -925,6 +953,10 @@ static bool collect_status(Engine& e, Work& w) {
   if (any & ST_CFL) g_msg = "CFL condition violated: time loop stopped (channel/pass1.c:133-137)";
   else if (any & ST_NONFINITE) g_msg = "non-finite values in the physical fields";
   else g_msg.clear();
+  if (tc5_take_error()) {
+    set_error(-3, "a tensor-core wait of the inverse transform expired; its results are not valid");
+    return false;
+  }
   return true;
 }
 
@@ -1233,7 +1265,8 @@ static bool op_adjoint(Engine& e, Work& w, int start, int end, const cpx* AC, do
 // arrays) every step adds it after its transposition:
 //   lambda_n = T_n^T lambda_{n+1} + src,  n = start - 1 .. end,
 // the cotangent of a sum over steps end .. start - 1 of a linear functional.
-static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* AC, const cpx* src = nullptr) {
+static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* AC, const cpx* src = nullptr,
+                             bool grad = false) {
   NvtxRange nvtx_op("op_adjoint_exact");
   const size_t csz = w.csz;
   const bool readvance = w.raw_start && end == 0;
@@ -1275,7 +1308,12 @@ static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* 
   }
   bool ok = true;
   const cpx* traj = readvance ? scratch : w.MC;
+  const double* ftr = readvance ? scratch_ft : w.Ft;
   const bool cached = !readvance && w.cached(3 * end, 3 * start);
+  if (grad && cudaMemsetAsync(w.gacc, 0, sizeof(double) * (size_t)w.nseg * w.gstride, e.st) != cudaSuccess) {
+    set_error(-1, "c_adjoint_exact: gradient accumulator reset failed");
+    ok = false;
+  }
   if (cudaMemcpyAsync(w.Ca, AC, sizeof(cpx) * csz * w.nseg, cudaMemcpyDeviceToDevice, e.st) != cudaSuccess ||
       cudaMemsetAsync(w.Ul, 0, sizeof(cpx) * w.usz * w.nseg, e.st) != cudaSuccess) {
     set_error(-1, "c_adjoint_exact: copy failed");
@@ -1283,9 +1321,27 @@ static bool op_adjoint_exact(Engine& e, Work& w, int start, int end, const cpx* 
   }
   ok = ok && set_step(e, w, start);
   GraphKey key = step_key(e, w, 'x');
-  key.add(cached).add(traj).add(w.traj).add(src);
+  key.add(cached).add(traj).add(w.traj).add(src).add(grad).add(ftr);
   ok = ok && run_steps(e, w, key, start - end,
-                       [&] { return enqueue_adjoint_exact_step(e, w, cached, traj, w.traj, src); });
+                       [&] { return enqueue_adjoint_exact_step(e, w, cached, traj, w.traj, src, ftr, grad); });
+  if (ok && grad) {
+    // per segment: dJ/dmeanU, and dJ/dRe as the blocks' parts summed in order
+    std::vector<double> h((size_t)w.nseg * w.gstride);
+    if (cudaMemcpyAsync(h.data(), w.gacc, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, e.st) != cudaSuccess ||
+        cudaStreamSynchronize(e.st) != cudaSuccess) {
+      set_error(-1, "c_adjoint_exact: gradient read-back failed");
+      ok = false;
+    } else {
+      w.grad.assign((size_t)2 * w.nseg, 0.0);
+      for (int s = 0; s < w.nseg; ++s) {
+        const double* r = h.data() + (size_t)s * w.gstride;
+        double re = 0.0;
+        for (int b = 1; b < w.gstride; ++b) re += r[b];
+        w.grad[2 * s] = r[0];
+        w.grad[2 * s + 1] = re;
+      }
+    }
+  }
   if (ok) {
     // the tangent starts from IU = Recon(IC)
     SolveTArgs t{};
@@ -1569,6 +1625,26 @@ void c_adjoint_exact_source(int start_step, int end_step, chn_complex* AC_given,
   d2h(e, AC_given, w.Ca, bytes);
 }
 
+int c_adjoint_exact_grad(int start_step, int end_step, chn_complex* AC_given, const chn_complex* src,
+                         double* grad) {
+  if (!need_init("c_adjoint_exact_grad")) return g_status;
+  Engine& e = *E;
+  Work& w = e.single;
+  if (!(end_step < start_step && end_step >= 0 && start_step <= e.nsteps) || !AC_given || !grad) {
+    set_error(-4, "c_adjoint_exact_grad: need 0 <= end < start <= nsteps, the state array and grad[2]");
+    return -4;
+  }
+  const size_t bytes = sizeof(cpx) * w.csz;
+  if (!h2d(e, w.io, AC_given, bytes)) return -1;
+  if (src && !h2d(e, w.src, src, bytes)) return -1;
+  if (!op_adjoint_exact(e, w, start_step, end_step, w.io, src ? w.src : nullptr, true)) return g_status;
+  if (!collect_status(e, w)) return g_status;
+  if (!d2h(e, AC_given, w.Ca, bytes)) return -1;
+  grad[0] = w.grad[0];
+  grad[1] = w.grad[1];
+  return g_status;
+}
+
 double c_ddt_project(int i_step, chn_complex* IC_given, int Nz_dup, int Nvar_dup, int Ny_dup, int Nx_dup) {
   if (!need_init("c_ddt_project")) return NAN;
   check_coef_dims(E->T.g, Nz_dup, Nvar_dup, Ny_dup, Nx_dup);
@@ -1834,6 +1910,24 @@ int c_batch_adjoint_exact_source_dev(int start_step, int end_step, chn_complex* 
 
 int c_batch_adjoint_exact_dev(int start_step, int end_step, chn_complex* AC) {
   return c_batch_adjoint_exact_source_dev(start_step, end_step, AC, nullptr);
+}
+
+int c_batch_adjoint_exact_grad_dev(int start_step, int end_step, chn_complex* AC, const chn_complex* src,
+                                   double* grad) {
+  if (!batch_ready("c_batch_adjoint_exact_grad_dev")) return g_status;
+  Work& w = E->batch;
+  if (!(end_step < start_step && end_step >= 0 && start_step <= w.nsteps) || !AC || !grad) {
+    set_error(-4, "c_batch_adjoint_exact_grad_dev: need 0 <= end < start <= nsteps, the state array and grad");
+    return -4;
+  }
+  if (!op_adjoint_exact(*E, w, start_step, end_step, reinterpret_cast<cpx*>(AC), reinterpret_cast<const cpx*>(src),
+                        true))
+    return g_status;
+  if (cudaMemcpyAsync(AC, w.Ca, sizeof(cpx) * w.csz * w.nseg, cudaMemcpyDeviceToDevice, E->st) != cudaSuccess)
+    return -1;
+  if (!collect_status(*E, w)) return -1;
+  std::copy(w.grad.begin(), w.grad.end(), grad);
+  return g_status;
 }
 
 // host-array variants: staged through the working set's own device buffers

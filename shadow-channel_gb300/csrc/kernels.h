@@ -115,6 +115,20 @@ struct SolveTArgs {
   const uint32_t* status;
   int sdiv;
   const Grid* grids;        // uneven batch: grid of each instance
+  // Parameter gradients (gacc null: none).  Per instance, gacc[i * gstride]
+  // accumulates <x_bar, add> of the mean line over the substages (the
+  // cotangent of the mean-flux forcing of the tangent: dJ/dmeanU), and
+  // gacc[i * gstride + 1 + block] this block's <c2_bar, f_Re> (the cotangent
+  // of the exact Re forcing, f_Re = -re^2 dt (a_k D x_k + b_k D x_{k+1}):
+  // dJ/dRe), from the primal states x_k = MC[3n + k] at Xf + i * xstride,
+  // slot xslot, and the flux corrections Ftr[i * ftr_stride + slot].
+  double* gacc;
+  int gstride;
+  const cpx* Xf;
+  long long xstride;
+  SlotRef xslot;
+  const double* Ftr;
+  long long ftr_stride;
 };
 
 // one ddt_project / adjoint coupling for nseg segments (channel/channel.c:704-780)
@@ -141,6 +155,11 @@ cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t s
 // the inverse transforms as exact digit GEMMs on the tensor cores (fused, one block per plane)
 cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st);
 bool phys_tc_fits(const Grid& g, int optin);
+// the inverse on tcgen05 (phys_tc5.cu): fits for nf fields; the error word
+// of its bounded waits (returned and cleared)
+cudaError_t launch_phys_inverse_tc5(const Grid& g, const PhysArgs& a, cudaStream_t st);
+bool phys_tc5_fits(const Grid& g, int nf, int optin);
+int tc5_take_error();
 // products + forward transforms as digit GEMMs (mode 0 primal, 1 tangent, 2 adjoint, 3 exact transpose)
 cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st);
 bool fwd_tc_fits(const Grid& g, int optin);

@@ -351,6 +351,7 @@ cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t s
   if (a.ninst <= 0) return cudaSuccess;
   // the tensor-core inverse wherever it fits (its results do not depend on
   // the autotuner's choice among the bit-identical FFT variants)
+  if (g.tc5 && !a.grids) return launch_phys_inverse_tc5(g, a, st);  // fits every nfields once 6 fit
   if (g.tci) return launch_phys_inverse_tc(g, a, st);
   if (g.split) return kSplit[split_index(g)].inverse(g, a, st);
   const size_t sm = phys_smem_bytes(g, a.cfl_check != 0);
@@ -380,6 +381,7 @@ void prepare_recon_solve(int optin);
 void prepare_solve_T(int optin);
 void prepare_recon_tc(int optin);
 void prepare_phys_tc(int optin);
+void prepare_phys_tc5(int optin);
 
 // Every kernel may use up to the device's opt-in shared memory per block: the
 // single-grid engine and an uneven batch (sized for its largest grid) share
@@ -405,6 +407,7 @@ void prepare_kernels(const Grid& g) {
   prepare_solve_T(optin);
   prepare_recon_tc(optin);
   prepare_phys_tc(optin);
+  prepare_phys_tc5(optin);
 }
 
 }  // namespace chn

@@ -30,30 +30,16 @@
 #include "kernels.h"
 #include "phys_common.cuh"
 #include "setup.h"
+#include "phys_tc.cuh"
 #include "tc_common.cuh"
 
 namespace chn {
 
 static constexpr int kThreads = 256;
-static constexpr int kFB = 2;  // fields per pass
 
 // ---------------------------------------------------------------------------
 // host tables
 // ---------------------------------------------------------------------------
-
-// kept kz modes of even / odd padded index zp (kk < Nz/2: zp = kk; else
-// zp = kk + 1 + Nz/2, which runs over the odd Nz + 1 ... 3Nz/2 - 1); an odd
-// pz keeps all modes in one class
-__host__ __device__ inline void z_class_counts(int Nz, int pz, int& nE, int& nO) {
-  if (pz % 2) {
-    nE = Nz - 1;
-    nO = 0;
-    return;
-  }
-  const int h = Nz / 2;
-  nE = (h + 1) / 2 + (h - 1) / 2;
-  nO = h / 2 + h / 2;
-}
 
 // the kept kz modes of one class of the z stage's radix-2 split (padded
 // index zp even or odd; the only class for an odd pz)
@@ -65,8 +51,11 @@ static void z_class_modes(int Nz, int pz, int cls, std::vector<int>& kk_of) {
   }
 }
 
-bool build_phys_tc_tables(const HostTables& h, std::vector<uint32_t>& zfrag, std::vector<int>& zex,
-                          std::vector<uint32_t>& xfrag, std::vector<int>& xex, std::vector<int>& zmap) {
+// the two stages' matrices (rows x K words of Re, Im) and the z stage's
+// K-word -> kept kz map, shared by the mma.sync tables below and the
+// tcgen05 tables of phys_tc5.cu
+bool phys_tc_matrices(const HostTables& h, std::vector<double>& Az, std::vector<double>& Ax,
+                      std::vector<int>& zmap, int& zrows, int& Kz, int& xrows, int& Kx) {
   const int pz = h.pz, px = h.px, Nz = h.Nz, X = h.X;
   const int Rz = pz % 2 ? 1 : 2, Rx = px % 2 ? 1 : 2, pzh = pz / Rz, pxh = px / Rx;
   std::vector<int> zE, zO;
@@ -78,9 +67,13 @@ bool build_phys_tc_tables(const HostTables& h, std::vector<uint32_t>& zfrag, std
   const int nxE = (X + Rx - 1) / Rx, nxO = X - nxE;
   const int KTzE = (2 * (int)zE.size() + 15) / 16, KTzO = (2 * (int)zO.size() + 15) / 16;
   const int KTxE = (2 * nxE + 15) / 16, KTxO = (2 * nxO + 15) / 16;
-  const int Kz = (KTzE + KTzO) * 16, Kx = (KTxE + KTxO) * 16;
+  Kz = (KTzE + KTzO) * 16;
+  Kx = (KTxE + KTxO) * 16;
+  zrows = 2 * pzh;
+  xrows = pxh;
   // z stage: rows Re Z[m], Im Z[m] (m < pzh); K words: even modes, then odd
-  std::vector<double> Az((size_t)2 * pzh * Kz, 0.0), Ax((size_t)pxh * Kx, 0.0);
+  Az.assign((size_t)2 * pzh * Kz, 0.0);
+  Ax.assign((size_t)pxh * Kx, 0.0);
   zmap.assign((size_t)Kz / 2, -1);
   for (int c = 0; c < 2; ++c) {
     const std::vector<int>& modes = c ? zO : zE;
@@ -120,11 +113,19 @@ bool build_phys_tc_tables(const HostTables& h, std::vector<uint32_t>& zfrag, std
       Ax[(size_t)xp * Kx + 2 * w + 1] = -2.0 * sn;
     }
   }
+  return true;
+}
+
+bool build_phys_tc_tables(const HostTables& h, std::vector<uint32_t>& zfrag, std::vector<int>& zex,
+                          std::vector<uint32_t>& xfrag, std::vector<int>& xex, std::vector<int>& zmap) {
+  std::vector<double> Az, Ax;
+  int zrows = 0, Kz = 0, xrows = 0, Kx = 0;
+  if (!phys_tc_matrices(h, Az, Ax, zmap, zrows, Kz, xrows, Kx)) return false;
   zfrag.clear(); zex.clear(); xfrag.clear(); xex.clear();
   // one table per stage with both classes in its K: a row's exponent covers
   // its even and odd parts, so their integer sums add exactly
-  return append_digit_table(Az.data(), 2 * pzh, Kz, (2 * pzh + 15) / 16, Kz / 16, zfrag, zex) &&
-         append_digit_table(Ax.data(), pxh, Kx, (pxh + 15) / 16, Kx / 16, xfrag, xex);
+  return append_digit_table(Az.data(), zrows, Kz, (zrows + 15) / 16, Kz / 16, zfrag, zex) &&
+         append_digit_table(Ax.data(), xrows, Kx, (xrows + 15) / 16, Kx / 16, xfrag, xex);
 }
 
 // forward transforms (channel/pass1.c:312-339): x stage Y[zp][kx] =
@@ -167,36 +168,6 @@ bool build_fwd_tc_tables(const HostTables& h, std::vector<uint32_t>& xfrag, std:
 // ---------------------------------------------------------------------------
 // shared-memory plan
 // ---------------------------------------------------------------------------
-
-struct PhysTcDims {
-  int Rz, Rx, pzh, pxh;           // radix of each stage's split, output rows per half
-  int nxE, nxO;                   // x modes of even / odd j
-  int KTzE, KTz, KTxE, KTx;       // k-tiles of the even class, and in all
-  int MTz, MTx, KSz, KSx, NZ, NX;  // NZ = columns of the z stage, NX = of the x stage
-};
-
-__host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g) {
-  PhysTcDims d;
-  d.Rz = g.pz % 2 ? 1 : 2;
-  d.Rx = g.px % 2 ? 1 : 2;
-  d.pzh = g.pz / d.Rz;
-  d.pxh = g.px / d.Rx;
-  int nzE, nzO;
-  z_class_counts(g.Nz, g.pz, nzE, nzO);
-  d.nxE = (g.X + d.Rx - 1) / d.Rx;
-  d.nxO = g.X - d.nxE;
-  d.KTzE = (2 * nzE + 15) / 16;
-  d.KTz = d.KTzE + (2 * nzO + 15) / 16;
-  d.KTxE = (2 * d.nxE + 15) / 16;
-  d.KTx = d.KTxE + (2 * d.nxO + 15) / 16;
-  d.MTz = (2 * d.pzh + 15) / 16;
-  d.MTx = (d.pxh + 15) / 16;
-  d.KSz = d.KTz * 16 + 8;
-  d.KSx = d.KTx * 16 + 8;
-  d.NZ = kFB * g.X;
-  d.NX = kFB * g.pz;  // the x stage: one column per (field, m)
-  return d;
-}
 
 __host__ __device__ inline size_t phys_tc_dbuf_bytes(const Grid& g) {
   const PhysTcDims d = phys_tc_dims(g);

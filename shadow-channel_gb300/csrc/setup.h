@@ -47,6 +47,8 @@ bool build_adj_tc_tables(const HostTables& h, std::vector<uint32_t>& btfrag, std
 // DFT matrices of the inverse z and x transforms as digit tables (phys_tc.cu)
 bool build_phys_tc_tables(const HostTables& h, std::vector<uint32_t>& zfrag, std::vector<int>& zex,
                           std::vector<uint32_t>& xfrag, std::vector<int>& xex, std::vector<int>& zmap);
+// the same matrices' digit tables as tcgen05 B operands (phys_tc5.cu)
+bool build_phys_tc5_tables(const HostTables& h, std::vector<uint8_t>& zt, std::vector<uint8_t>& xt);
 // DFT matrices of the forward x and z transforms as digit tables (phys_tc.cu)
 bool build_fwd_tc_tables(const HostTables& h, std::vector<uint32_t>& xfrag, std::vector<int>& xex,
                          std::vector<uint32_t>& zfrag, std::vector<int>& zex, std::vector<uint32_t>& ufrag,

@@ -1,7 +1,8 @@
 """channel.autograd.TimeMeanWallShear: the checkpointed differentiable
-objective.  Its gradients (exact tangents of the discrete step, Re forcing
-kind 3 and mean-flux forcing) must match central finite differences of the
-objective to 1e-6, and checkpointing must not change the results."""
+objective.  Its gradients (dJ/dRe, dJ/dmeanU and dJ/dC0 from one exact-adjoint
+sweep) must match central finite differences of the objective to 1e-6 and
+the forced tangent sweeps (Re forcing kind 3, mean-flux forcing kind 1) to
+rounding, and checkpointing must not change the results."""
 import numpy as np
 import pytest
 
@@ -45,6 +46,18 @@ def test_gradients_match_central_differences(mod):
     assert abs(float(Re.grad) - fdR) <= 1e-6 * abs(fdR), (float(Re.grad), fdR)
     assert abs(float(U.grad) - fdU) <= 1e-6 * abs(fdU), (float(U.grad), fdU)
     assert cfg["report"]["forward_s"] > 0 and cfg["report"]["backward_s"] > 0
+
+
+def test_adjoint_parameter_gradients_match_tangent_sweeps(mod):
+    """the single reverse sweep's dJ/dRe, dJ/dmeanU against one forced
+    tangent sweep per parameter over the same checkpoint intervals"""
+    torch, ag = mod
+    cfg = _cfg(5)
+    J, ckpts, chunks = ag.primal_objective(GRID, RE, MEANU, cfg["C0"], NSTEPS, 5)
+    _, dU, dRe = ag.adjoint_gradients(GRID, RE, MEANU, ckpts, chunks, NSTEPS)
+    t = ag.tangent_gradients(GRID, RE, MEANU, ckpts, chunks, NSTEPS)
+    assert abs(dRe - t[3]) <= 1e-9 * abs(t[3]), (dRe, t[3])
+    assert abs(dU - t[1]) <= 1e-9 * abs(t[1]), (dU, t[1])
 
 
 def test_checkpoint_spacing_does_not_change_results(mod):

@@ -56,10 +56,12 @@ def _run(cc, C, IC, AC, strength=1.0):
     try:
         hC, hIC, hAC = C.copy(), IC.copy(), AC.copy()
         inh = (ctypes.c_int * NTAN)(*INHOMO)
-        assert lib.c_batch_forward(0, n, hC.ctypes.data, hIC.ctypes.data, inh) == 0
+        rc = lib.c_batch_forward(0, n, hC.ctypes.data, hIC.ctypes.data, inh)
         st_fwd, cfl_fwd = cc.c_last_error(), cc.c_last_cfl()
-        assert lib.c_batch_adjoint(n, 0, hAC.ctypes.data, strength) == 0
+        assert rc == st_fwd and rc >= 0, (rc, cc.c_last_error_message())   # the call returns its status
+        rc = lib.c_batch_adjoint(n, 0, hAC.ctypes.data, strength)
         st_adj = cc.c_last_error()
+        assert rc == st_adj and rc >= 0, (rc, cc.c_last_error_message())
         out = np.zeros(C[0].shape, np.complex128)
         MC, MIC = [], []
         for s in range(NSEG):
