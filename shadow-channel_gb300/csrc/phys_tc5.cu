@@ -50,7 +50,8 @@
 
 namespace chn {
 
-static constexpr int kT5Threads = 256;
+static constexpr int kT5Threads = 512;       // 16 warps: latency hiding at one CTA per SM
+static constexpr int kT5Groups = kT5Threads / 128;  // warps sharing a tensor-memory lane quarter
 static constexpr int kT5Cols = 512;        // tensor-memory columns per CTA (one CTA per SM)
 static constexpr int kT5XO = 256;          // x stage: odd-class accumulators at this column
 static constexpr long long kT5WaitCycles = 2000000000LL;  // ~1 s at 2 GHz
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_phys_inverse_tc5(const __grid
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sp + 16);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int q = warp & 3, half = warp >> 2;  // tensor-memory lane quarter, row half
+  const int q = warp & 3, grp = warp >> 2;  // tensor-memory lane quarter, row group of the folds
   const uint32_t bar_tab = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
   if (tid == 0) {
     mbar_init(bar_tab, 1);
@@ -352,9 +353,13 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_phys_inverse_tc5(const __grid
     __syncthreads();
     // ---- digits of every z k-tile (even modes, then odd): A blocks [i][kt]
     {
+      // a warp's 32 stores fill one 128-byte row set of a core matrix pair
+      // (8 rows x 4 words): lane = (n & 7) + 8 (w & 3), conflict-free
       const int KW = d.KTz * 8;
-      for (int idx = tid; idx < t.ncz * KW; idx += kT5Threads) {
-        const int n = idx % t.ncz, w = idx / t.ncz;
+      for (int idx = tid; idx < t.RGz * 8 * KW; idx += kT5Threads) {
+        const int rest = idx >> 5, ng = rest % t.RGz, wg = rest / t.RGz;
+        const int n = ng * 8 + (idx & 7), w = wg * 4 + ((idx >> 3) & 3);
+        if (n >= t.ncz) continue;
         const int kk = g.tcZM[w];
         cpx v = {0.0, 0.0};
         if (kk >= 0) v = Fin[(size_t)n * Kk + kk];
@@ -380,19 +385,19 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_phys_inverse_tc5(const __grid
     fence_after();
     const bool zwarp = 32 * q < t.ncz;
     const int nz = 32 * q + lane;
-    const int rows_half = t.NpZ / 2;
+    const int rows_grp = t.NpZ / kT5Groups;  // a multiple of 4
     // fold the even sums into (H, L) pairs in the Z buffer slots of the two
     // outputs they feed
     if (zwarp) {
-      for (int r0 = half * rows_half; r0 < (half + 1) * rows_half; r0 += 8) {
-        float lv[kDig][8];
+      for (int r0 = grp * rows_grp; r0 < (grp + 1) * rows_grp; r0 += 4) {
+        float lv[kDig][4];
 #pragma unroll
-        for (int l = 0; l < kDig; ++l) tmem_ld<8>(tm + ((uint32_t)(32 * q) << 16) + (uint32_t)(l * t.NpZ + r0), lv[l]);
+        for (int l = 0; l < kDig; ++l) tmem_ld<4>(tm + ((uint32_t)(32 * q) << 16) + (uint32_t)(l * t.NpZ + r0), lv[l]);
         tmem_wait_ld();
         if (nz < t.ncz) {
           const int f = nz / g.X, x = nz - f * g.X;
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
+          for (int j = 0; j < 4; ++j) {
             const int r = r0 + j;
             if (r >= 2 * d.pzh) break;
             float c[kDig];
@@ -423,16 +428,16 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_phys_inverse_tc5(const __grid
     if (!ok) break;
     fence_after();
     if (zwarp) {
-      for (int r0 = half * rows_half; r0 < (half + 1) * rows_half; r0 += 8) {
-        float lv[kDig][8];
+      for (int r0 = grp * rows_grp; r0 < (grp + 1) * rows_grp; r0 += 4) {
+        float lv[kDig][4];
 #pragma unroll
-        for (int l = 0; l < kDig; ++l) tmem_ld<8>(tm + ((uint32_t)(32 * q) << 16) + (uint32_t)(l * t.NpZ + r0), lv[l]);
+        for (int l = 0; l < kDig; ++l) tmem_ld<4>(tm + ((uint32_t)(32 * q) << 16) + (uint32_t)(l * t.NpZ + r0), lv[l]);
         tmem_wait_ld();
         if (nz < t.ncz) {
           const int f = nz / g.X, x = nz - f * g.X;
           const int ez = exz[nz];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
+          for (int j = 0; j < 4; ++j) {
             const int r = r0 + j;
             if (r >= 2 * d.pzh) break;
             float c[kDig];
@@ -470,7 +475,8 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_phys_inverse_tc5(const __grid
     for (int tile = 0; tile < t.ntile; ++tile) {
       const int c0 = tile * 128, nct = min(128, t.ncx - c0);
       for (int idx = tid; idx < 128 * KWx; idx += kT5Threads) {
-        const int nl = idx & 127, w = idx >> 7, n = c0 + nl;
+        const int rest = idx >> 5, ng = rest & 15, wg = rest >> 4;
+        const int nl = ng * 8 + (idx & 7), w = wg * 4 + ((idx >> 3) & 3), n = c0 + nl;
         const int j = w < WE ? (w < d.nxE ? d.Rx * w : -1) : (w - WE < d.nxO ? 2 * (w - WE) + 1 : -1);
         cpx v = {0.0, 0.0};
         int ex = 0;
@@ -499,9 +505,9 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_phys_inverse_tc5(const __grid
       fence_after();
       {
         const int nl = 32 * q + lane, n = c0 + nl;
-        const int rows_x = t.NpX / 2;
+        const int rows_x = ((d.pxh + kT5Groups - 1) / kT5Groups + 3) / 4 * 4;  // rows per group, 4 | rows_x
         const int ecol = nl < nct ? exx[n] : 0;
-        for (int r0 = half * rows_x; r0 < (half + 1) * rows_x; r0 += 4) {
+        for (int r0 = grp * rows_x; r0 < (grp + 1) * rows_x; r0 += 4) {
           if (r0 >= d.pxh) break;
           float lvE[kDig][4], lvO[kDig][4];
 #pragma unroll
