@@ -207,14 +207,15 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   g.tci = (!(tfp64 && tfp64[0] == '1') && phys_tc_fits(g, optin)) ? 1 : 0;
   g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_fits(g, optin)) ? 1 : 0;
   g.tcminb = 2;  // until the autotuner has timed both builds (3 blocks rarely fit the shared memory)
-  // the inverse on tcgen05 where it fits, with CHN_INVERSE_TC5=1 (the
-  // mma.sync kernel stays the default: it is the faster one today)
+  // the inverse on tcgen05 where it fits: a candidate of the autotuner
+  // (bit-identical results); CHN_INVERSE_TC5=1 forces it, =0 leaves it out
   const char* t5 = getenv("CHN_INVERSE_TC5");
   g.tc5 = 0;
-  if (g.tci && (t5 && t5[0] == '1') && phys_tc5_fits(g, 6, optin)) {
+  g.t5Z = g.t5X = nullptr;
+  if (g.tci && !(t5 && t5[0] == '0') && phys_tc5_fits(g, 6, optin)) {
     std::vector<uint8_t> zt, xt;
     if (!build_phys_tc5_tables(h, zt, xt) || !T.up(zt, &g.t5Z) || !T.up(xt, &g.t5X)) return false;
-    g.tc5 = 1;
+    g.tc5 = (t5 && t5[0] == '1') ? 1 : 0;
   }
   if (solve_smem_bytes(g) > (size_t)optin || recon_smem_bytes(g) > (size_t)optin) {
     set_error(1, "grid %dx%dx%d: the implicit solve needs %zu bytes of shared memory per block, the device has %d",
@@ -980,19 +981,24 @@ static bool autotune_transforms(Engine& e, Work& w) {
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   struct Cand {
-    int split, tvar, minb;
+    int split, tvar, minb, tc5;
     float ms;
   };
   std::vector<Cand> cands;
+  const char* t5env = getenv("CHN_INVERSE_TC5");
+  const bool t5forced = t5env && (t5env[0] == '0' || t5env[0] == '1');
   if (g.tci && g.tcf) {
     // both transforms on the tensor cores: the FFT variants are unused; time
-    // the two register budgets of the tensor-core inverse
-    cands.push_back({g.split, g.tvar, 2, 0.f});
-    cands.push_back({g.split, g.tvar, 3, 0.f});
+    // the two register budgets of the mma.sync inverse and the tcgen05 one
+    if (!(t5forced && g.tc5)) {
+      cands.push_back({g.split, g.tvar, 2, 0, 0.f});
+      cands.push_back({g.split, g.tvar, 3, 0, 0.f});
+    }
+    if (g.t5Z && !(t5forced && !g.tc5) && !w.gdev) cands.push_back({g.split, g.tvar, 2, 1, 0.f});
   } else {
-    if (fused_transforms_fit(g, optin)) cands.push_back({0, 0, g.tcminb, 0.f});
+    if (fused_transforms_fit(g, optin)) cands.push_back({0, 0, g.tcminb, 0, 0.f});
     for (int v = 0; v < split_variant_count(); ++v)
-      if (split_variant_fits(v, g, optin)) cands.push_back({1, v, g.tcminb, 0.f});
+      if (split_variant_fits(v, g, optin)) cands.push_back({1, v, g.tcminb, 0, 0.f});
   }
   if (cands.size() < 2 || !w.Zt) return true;
   const int nt = w.nseg * (w.ntan > 0 ? w.ntan : 1);
@@ -1029,12 +1035,13 @@ static bool autotune_transforms(Engine& e, Work& w) {
   cudaEvent_t t0, t1;
   CK(cudaEventCreate(&t0));
   CK(cudaEventCreate(&t1));
-  const int saved_split = g.split, saved_tvar = g.tvar, saved_minb = g.tcminb;
+  const int saved_split = g.split, saved_tvar = g.tvar, saved_minb = g.tcminb, saved_tc5 = g.tc5;
   bool ok = true;
   for (Cand& c : cands) {
     g.split = c.split;
     g.tvar = c.tvar;
     g.tcminb = c.minb;
+    g.tc5 = c.tc5;
     ok = ok && enqueue();  // warm-up
     ok = ok && cudaEventRecord(t0, e.st) == cudaSuccess;
     for (int r = 0; r < 3; ++r) ok = ok && enqueue();
@@ -1049,6 +1056,7 @@ static bool autotune_transforms(Engine& e, Work& w) {
     g.split = saved_split;
     g.tvar = saved_tvar;
     g.tcminb = saved_minb;
+    g.tc5 = saved_tc5;
     return false;
   }
   const Cand* best = &cands[0];
@@ -1057,11 +1065,14 @@ static bool autotune_transforms(Engine& e, Work& w) {
   g.split = best->split;
   g.tvar = best->tvar;
   g.tcminb = best->minb;
+  g.tc5 = best->tc5;
   char buf[160];
   g_tune_report = "{";
   const bool tcv = g.tci && g.tcf;
   for (const Cand& c : cands) {
-    if (tcv) {
+    if (tcv && c.tc5) {
+      snprintf(buf, sizeof(buf), "\"tc_inverse_tcgen05\": %.4f, ", c.ms);
+    } else if (tcv) {
       snprintf(buf, sizeof(buf), "\"tc_inverse_minb%d\": %.4f, ", c.minb, c.ms);
     } else if (c.split) {
       const TransformVariant v = split_variant(c.tvar);
@@ -1071,7 +1082,9 @@ static bool autotune_transforms(Engine& e, Work& w) {
     }
     g_tune_report += buf;
   }
-  if (tcv) {
+  if (tcv && best->tc5) {
+    snprintf(buf, sizeof(buf), "\"chosen\": \"tc_inverse_tcgen05\", \"instances\": %d}", nt);
+  } else if (tcv) {
     snprintf(buf, sizeof(buf), "\"chosen\": \"tc_inverse_minb%d\", \"instances\": %d}", best->minb, nt);
   } else if (best->split) {
     const TransformVariant v = split_variant(best->tvar);
