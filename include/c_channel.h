@@ -316,7 +316,10 @@ int c_setup_table(int Nx, int Ny, int Nz, double Lx, double Lz, double Re,
    and the row exponents).  which: 0 the five bases [5][Q/16][R/16] tiles,
    1 their weighted transposes, 2 the inverse transform's z stage, 3 its x
    stage, 4 the forward x stage, 5 the forward z stage, 6 the unscaled
-   forward x stage, 7 the bases transposed, 8 Qpw, Qw, Rw plane-major.
+   forward x stage, 7 the bases transposed, 8 Qpw, Qw, Rw plane-major,
+   9 / 10 the inverse's z / x stage as the tcgen05 kernel's B operands
+   (the seven digit planes stacked along N, K-major core matrices; bytes
+   as 32-bit words), with the exponents of tables 2 / 3.
    sizes[0] = uint32 words, sizes[1] = exponents.  With frag and ex null the
    call is a size query; a non-null buffer shorter than its table
    (nfrag < sizes[0] or nex < sizes[1]) is refused with -2 and nothing is

@@ -356,6 +356,17 @@ extern "C" int c_setup_tc_table(int Nx, int Ny, int Nz, double Lx, double Lz, do
     case 2: case 3: ok = chn::build_phys_tc_tables(t, f[0], e[0], f[1], e[1], m); sel = which - 2; break;
     case 4: case 5: case 6: ok = chn::build_fwd_tc_tables(t, f[0], e[0], f[1], e[1], f[2], e[2]); sel = which - 4; break;
     case 7: case 8: ok = chn::build_adj_tc_tables(t, f[0], e[0], f[1], e[1]); sel = which - 7; break;
+    case 9: case 10: {
+      // the tcgen05 inverse's stacked tables (bytes as 32-bit words) with the
+      // row exponents of the mma.sync tables they share
+      std::vector<uint8_t> zt, xt;
+      ok = chn::build_phys_tc5_tables(t, zt, xt) && chn::build_phys_tc_tables(t, f[2], e[0], f[2], e[1], m);
+      const std::vector<uint8_t>& b = which == 9 ? zt : xt;
+      f[which - 9].assign(b.size() / 4, 0u);
+      if (!b.empty()) std::memcpy(f[which - 9].data(), b.data(), b.size());
+      sel = which - 9;
+      break;
+    }
     default: return -1;
   }
   if (!ok) return -1;

@@ -184,3 +184,48 @@ def test_short_buffer_is_refused(lib):
     assert (frag == 7).all() and (ex == 7).all()
     assert L.c_setup_tc_table(*GRID, 2, frag.ctypes.data, sizes[0], None, 0, sizes) == 0
     assert not (frag == 7).all()
+
+
+def decode_umma(words, ex, rows, K):
+    """The tcgen05 inverse's stacked B-operand table back to its matrix:
+    k-tile blocks of 7 Np / 8 row groups x 256 bytes, element (row' = i Np
+    + r, k) of digit plane i at ((row'/8) 2 + (k%16)/8) 128 + (row'%8) 16
+    + (k%8) 2 in its block (8 x 16-byte core matrices, K-major)."""
+    b = np.ascontiguousarray(words).view(np.uint8)
+    Np = (rows + 15) // 16 * 16
+    KT = K // 16
+    rg = 7 * Np // 8
+    assert b.size == KT * rg * 256
+    bits = b.view(np.uint16).astype(np.uint32) << 16
+    dig = bits.view(np.float32).astype(np.int64)
+    val = np.zeros((Np, K), np.int64)
+    for i in range(7):
+        for r in range(Np):
+            for k in range(K):
+                rp = i * Np + r
+                off = (((k // 16) * rg + rp // 8) * 2 + (k % 16) // 8) * 128 + (rp % 8) * 16 + (k % 8) * 2
+                val[r, k] += dig[off // 2] * 256 ** (6 - i)
+    assert np.all(val[rows:] == 0)
+    return val[:rows].astype(np.float64) * np.exp2(ex.astype(np.float64) - 56.0)[:, None]
+
+
+@pytest.mark.parametrize("which, mma_which", [(9, 2), (10, 3)])
+def test_tcgen05_tables_decode_to_the_same_matrices(lib, which, mma_which):
+    """The stacked tables of the tcgen05 inverse hold, digit for digit, the
+    matrices of the mma.sync inverse's tables (same rows, exponents, K order)"""
+    Nx, Ny, Nz = GRID[:3]
+    pz, px, X = 3 * Nz // 2, 3 * Nx // 2, Nx // 2
+    words, ex = tc_table(lib, which)
+    frag2, ex2 = tc_table(lib, mma_which)
+    assert np.array_equal(ex, ex2)
+    if which == 9:
+        rows = 2 * (pz // 2)
+        nE = sum(1 for kk in range(Nz - 1) if (kk if kk < Nz // 2 else kk + 1 + Nz // 2) % 2 == 0)
+        K = ((2 * nE + 15) // 16 + (2 * (Nz - 1 - nE) + 15) // 16) * 16
+    else:
+        rows = px // 2
+        nxE = (X + 1) // 2
+        K = ((2 * nxE + 15) // 16 + (2 * (X - nxE) + 15) // 16) * 16
+    dec = decode_umma(words, ex, rows, K)
+    ref = decode(frag2, ex2, 1, (rows + 15) // 16, K // 16)[0][:rows]
+    assert np.array_equal(dec, ref)
