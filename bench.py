@@ -557,7 +557,7 @@ def autograd_config(C0, nsteps=1000, checkpoint=50):
     """The differentiable single trajectory at 32x65x32, Re 3300, dt 0.005:
     time-mean lower-wall shear over `nsteps` steps from the run-up parent
     field, checkpoints every `checkpoint` steps (channel.autograd), with
-    dJ/dRe, dJ/dmeanU (exact tangents) and dJ/dC0 (exact adjoint) against
+    dJ/dRe, dJ/dmeanU and dJ/dC0 (one exact-adjoint sweep) against
     central differences: meanU at relative step 1e-6; C0 along one seeded
     direction of norm |C0| and Re at relative steps 1e-3 .. 1e-6 (headline
     comparisons at 1e-5 and 1e-3, where truncation and rounding noise
@@ -603,9 +603,9 @@ def autograd_config(C0, nsteps=1000, checkpoint=50):
             "dJ_dC0_dir": anC, "fd_dJ_dC0_dir": fdC, "rel_err_C0": rel(anC, fdC),
             "rel_err_C0_by_relative_step": {k: rel(anC, v) for k, v in fd_c0.items()},
             "fd_s": time.perf_counter() - t0,
-            "note": "backward = 2 exact tangent sweeps + 1 exact-adjoint sweep, each interval recomputed "
-                    "from its checkpoint; central differences: meanU at relative step 1e-6, C0 at 1e-5, Re at 1e-3 "
-                    "(the sweeps show truncation at larger steps, rounding noise at smaller)"}
+            "note": "backward = one exact-adjoint sweep giving dJ/dC0, dJ/dmeanU and dJ/dRe, each interval "
+                    "recomputed from its checkpoint; central differences: meanU at relative step 1e-6, C0 at 1e-5, "
+                    "Re at 1e-3 (the sweeps show truncation at larger steps, rounding noise at smaller)"}
 
 
 def large_grid(cc, nsteps=8):
