@@ -243,6 +243,7 @@ struct Work {
   double* Ft = nullptr;   // primal flux correction of each stored substage, [seg][3 nsteps + 1]
   uint32_t* status = nullptr;
   int* step = nullptr;
+  int* loopctr = nullptr;      // steps left in the device-side loop of a sweep graph
   // Primal physical-field cache: the six physical fields of the primal state
   // before every substage of the stored trajectory, [seg][3 nsteps][6][Q][pz][px].
   // Tangent and adjoint sweeps read them instead of rebuilding them from MC.
@@ -333,7 +334,8 @@ struct Work {
            alloc(&io, nt * csz) && alloc(&Pp, nseg * psz) && alloc(&Pt, nt * psz) &&
            alloc(&Pprev, nseg * psz) && alloc(&Pl, nseg * psz) && alloc(&flow, (size_t)3 * g.Q * plane_size(g)) &&
            alloc(&part, (size_t)nseg * kDotBlocks * 2) && alloc(&r, nseg) && alloc(&cflmax, nseg) &&
-           alloc(&status, nseg) && alloc(&step, 4) && alloc(&icp, nseg * csz) && alloc(&src, nseg * csz) &&
+           alloc(&status, nseg) && alloc(&step, 4) && alloc(&loopctr, 1) && alloc(&icp, nseg * csz) &&
+           alloc(&src, nseg * csz) &&
            alloc(&Ft, (size_t)nseg * (3 * (size_t)nsteps + 1)) && alloc_split(g, nt) && alloc_cache(g) &&
            alloc_grad(g);
   }
@@ -881,8 +883,11 @@ static GraphKey& add_opts(GraphKey& k, const FwdOpts& o) {
       .add(o.store).add(o.re2_mask).add(o.re3_mask);
 }
 
-// one step captured into a graph (or taken from the working set's graphs
-// when the key matches) and replayed nsteps times
+// A multi-step sweep as ONE graph launch: a graph whose while node runs one
+// captured step followed by k_loop_next, which counts the device-side
+// steps-left counter down and ends the loop after the last step.  The graph
+// is built once per working set and key (or taken from the working set's
+// graphs when the key matches); each sweep sets the counter and launches it.
 template <typename F>
 static bool run_steps(Engine& e, Work& w, const GraphKey& key, int nsteps, F&& enqueue) {
   if (nsteps <= 0) return true;
@@ -890,21 +895,42 @@ static bool run_steps(Engine& e, Work& w, const GraphKey& key, int nsteps, F&& e
   Work::StepGraph* sg = nullptr;
   for (Work::StepGraph& x : w.graphs)
     if (x.key == key.s) sg = &x;
-  int replays = nsteps;
   if (!sg) {
     cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    CK(cudaStreamBeginCapture(e.st, cudaStreamCaptureModeThreadLocal));
-    const long long before = g_launches;
-    bool ok = enqueue();
-    cudaError_t ce = cudaStreamEndCapture(e.st, &graph);
-    if (!ok) {
-      if (graph) cudaGraphDestroy(graph);
+    CK(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle h{};
+    cudaGraphNodeParams p{};
+    cudaGraphNode_t node = nullptr;
+    cudaError_t ge = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+    if (ge == cudaSuccess) {
+      p.type = cudaGraphNodeTypeConditional;
+      p.conditional.handle = h;
+      p.conditional.type = cudaGraphCondTypeWhile;
+      p.conditional.size = 1;
+      ge = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &p);
+    }
+    if (ge == cudaSuccess)
+      ge = cudaStreamBeginCaptureToGraph(e.st, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal);
+    if (ge != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      set_error(-1, "sweep graph: %s", cudaGetErrorString(ge));
       return false;
     }
-    CK(ce);
+    const long long before = g_launches;
+    bool ok = enqueue();
+    ok = ok && launch_loop_next(w.loopctr, h, e.st) == cudaSuccess;
+    cudaGraph_t body = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(e.st, &body);
     const long long per_step = g_launches - before;
-    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    g_launches = before;  // counted for every step the launch below runs
+    if (!ok || ce != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      if (ok) set_error(-1, "sweep graph capture: %s", cudaGetErrorString(ce));
+      return false;
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     CK(ie);
     if (w.graphs.size() >= Work::kMaxGraphs) {
@@ -913,16 +939,14 @@ static bool run_steps(Engine& e, Work& w, const GraphKey& key, int nsteps, F&& e
     }
     w.graphs.push_back(Work::StepGraph{key.s, exec, per_step});
     sg = &w.graphs.back();
-    replays = nsteps - 1;  // the capture counted one step's launches
   }
-  for (int n = 0; n < nsteps; ++n) {
-    cudaError_t le = cudaGraphLaunch(sg->exec, e.st);
-    if (le != cudaSuccess) {
-      set_error(-1, "cudaGraphLaunch: %s", cudaGetErrorString(le));
-      return false;
-    }
+  LK(launch_loop_set(w.loopctr, nsteps, e.st));
+  const cudaError_t le = cudaGraphLaunch(sg->exec, e.st);
+  if (le != cudaSuccess) {
+    set_error(-1, "cudaGraphLaunch: %s", cudaGetErrorString(le));
+    return false;
   }
-  g_launches += sg->per_step * replays;
+  g_launches += sg->per_step * nsteps;
   return true;
 }
 

@@ -325,6 +325,28 @@ cudaError_t launch_step_advance(int* ctr, int delta, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// The device-side loop of a multi-step sweep: the sweep is one graph launch
+// whose while-node body is one step followed by k_loop_next, which counts
+// the steps left down and keeps the loop running while any are left (the
+// condition is the count's positivity, so the loop ends after at most the
+// count k_loop_set wrote before the launch).
+__global__ void k_loop_set(int* ctr, int n) { ctr[0] = n; }
+
+__global__ void k_loop_next(int* ctr, cudaGraphConditionalHandle h) {
+  const int left = --ctr[0];
+  cudaGraphSetConditional(h, left > 0 ? 1u : 0u);
+}
+
+cudaError_t launch_loop_set(int* ctr, int n, cudaStream_t st) {
+  k_loop_set<<<1, 1, 0, st>>>(ctr, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_loop_next(int* ctr, cudaGraphConditionalHandle h, cudaStream_t st) {
+  k_loop_next<<<1, 1, 0, st>>>(ctr, h);
+  return cudaGetLastError();
+}
+
 // FP64 fused multiply-add throughput probe: 8 independent chains per thread,
 // registers only; out gets one value per thread so nothing is optimised away.
 __global__ void k_fp64_probe(double* out, int iters, double a, double b) {
