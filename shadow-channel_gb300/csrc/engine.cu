@@ -207,6 +207,10 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   g.tci = (!(tfp64 && tfp64[0] == '1') && phys_tc_fits(g, optin)) ? 1 : 0;
   g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_fits(g, optin)) ? 1 : 0;
   g.tcminb = 2;  // until the autotuner has timed both builds (3 blocks rarely fit the shared memory)
+  // the solve's block tile: 16 until the autotuner has timed both;
+  // CHN_SOLVE_TILE=8 or 16 fixes it (and skips that timing)
+  const char* stl = getenv("CHN_SOLVE_TILE");
+  g.stile = (stl && atoi(stl) == 8) ? 8 : 16;
   // the inverse on tcgen05 where it fits: a candidate of the autotuner
   // (bit-identical results); CHN_INVERSE_TC5=1 forces it, =0 leaves it out
   const char* t5 = getenv("CHN_INVERSE_TC5");
@@ -1125,6 +1129,68 @@ static bool autotune_transforms(Engine& e, Work& w) {
 // ---------------------------------------------------------------------------
 
 // primal from C (device, nseg arrays) or, when C == nullptr, the laminar start
+// autotuner, the implicit solve: the block tile (kx columns per block, 16
+// or 8) timed on one batched tangent solve of the working set; both compute
+// the same results.  The choice and the times join c_autotune_report.
+static bool autotune_solve(Engine& e, Work& w) {
+  const char* off = getenv("CHN_AUTOTUNE");
+  const char* fixed = getenv("CHN_SOLVE_TILE");
+  if ((off && off[0] == '0') || (fixed && fixed[0])) return true;
+  Grid& g = e.T.g;
+  const int nt = w.nseg * (w.ntan > 0 ? w.ntan : 1);
+  SolveArgs sa{};
+  sa.grids = w.gdev;
+  sa.H = cb(w.Ut, w.usz);
+  sa.Hprev = cb(nullptr, 0);
+  sa.Cc = mb(w.io, w.csz);  // scratch: no state of the working set is touched
+  sa.Sout = mb(w.io, w.csz);
+  sa.T = mb(nullptr, 0);
+  sa.tdiv = 1;
+  sa.slot = noslot();
+  sa.k = 1;
+  sa.mean_mode = MEAN_TAN_HOMOG;
+  sa.mdiv = w.ntan > 0 ? w.ntan : 1;
+  sa.ninst = nt;
+  sa.sdiv = w.ntan > 0 ? w.ntan : 1;
+  const int tiles[2] = {16, 8};
+  float ms[2] = {0.f, 0.f};
+  cudaEvent_t t0, t1;
+  CK(cudaEventCreate(&t0));
+  CK(cudaEventCreate(&t1));
+  const int saved = g.stile;
+  bool ok = true;
+  for (int c = 0; c < 2 && ok; ++c) {
+    g.stile = tiles[c];
+    ok = launch_solve(g, sa, e.st) == cudaSuccess;  // warm-up
+    ok = ok && cudaEventRecord(t0, e.st) == cudaSuccess;
+    for (int r = 0; r < 3 && ok; ++r) ok = launch_solve(g, sa, e.st) == cudaSuccess;
+    ok = ok && cudaEventRecord(t1, e.st) == cudaSuccess && cudaEventSynchronize(t1) == cudaSuccess;
+    if (ok) cudaEventElapsedTime(&ms[c], t0, t1);
+    ms[c] /= 3;
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  g_launches += ok ? 8 : 0;
+  if (!ok) {
+    g.stile = saved;
+    set_error(-1, "solve autotuner: %s", cudaGetErrorString(cudaGetLastError()));
+    return false;
+  }
+  g.stile = ms[1] < ms[0] ? 8 : 16;
+  char buf[160];
+  snprintf(buf, sizeof(buf), "\"solve_tile16\": %.4f, \"solve_tile8\": %.4f, \"solve_chosen\": \"tile%d\"", ms[0],
+           ms[1], g.stile);
+  if (g_tune_report.size() > 1 && g_tune_report.back() == '}') {
+    g_tune_report.pop_back();
+    g_tune_report += ", ";
+  } else {
+    g_tune_report = "{";
+  }
+  g_tune_report += buf;
+  g_tune_report += "}";
+  return true;
+}
+
 static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
   NvtxRange nvtx_op("op_primal");
   const size_t csz = w.csz;
@@ -1842,7 +1908,8 @@ int c_batch_init_steps(int nseg, int ntan, int couple, int nsteps) {
     return g_status;
   }
   e.have_batch = true;
-  if (!autotune_transforms(e, e.batch)) return g_status;
+  g_tune_report.clear();
+  if (!autotune_transforms(e, e.batch) || !autotune_solve(e, e.batch)) return g_status;
   g_status = 0;
   return 0;
 }
@@ -2227,7 +2294,8 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
   }
   m->e.batch.gdev = m->gdev;
   m->e.have_batch = true;
-  if (!autotune_transforms(m->e, m->e.batch)) {
+  g_tune_report.clear();
+  if (!autotune_transforms(m->e, m->e.batch) || !autotune_solve(m->e, m->e.batch)) {
     const int rc = g_status ? g_status : -1;
     c_multi_destroy();
     return rc;

@@ -216,28 +216,40 @@ struct SolveSmem {
   double* m0; // mean-mode scratch
 };
 
-// digits of one quadrature input for the tensor-core quadrature: [7][32][KS] bf16 + 16 exponents
+// The solve's functions below take the block's tile width (kx columns per
+// block, 16 or 8: the autotuner's choice, Grid::stile) as the template
+// parameter kTile, which stands for the file's 16 inside them.
+
+// digits of one quadrature input for the tensor-core quadrature:
+// [7][2 kTile columns][KS] bf16 + kTile exponents
 __host__ __device__ inline size_t solve_tc_kstride(const Grid& g) { return (size_t)((g.Q + 15) / 16) * 16 + 8; }
 
+template <int kTile>
 __host__ __device__ inline size_t solve_hc_elems(const Grid& g) {
   size_t hc = (size_t)g.Qh * kTile * 6, r = 2 * (size_t)g.R * kTile;
-  const size_t tc = ((size_t)kDig * 32 * solve_tc_kstride(g) * 2 + 16 * sizeof(int) + sizeof(cpx) - 1) / sizeof(cpx);
+  const size_t tc =
+      ((size_t)kDig * 2 * kTile * solve_tc_kstride(g) * 2 + kTile * sizeof(int) + sizeof(cpx) - 1) / sizeof(cpx);
   if (r > hc) hc = r;
   return tc > hc ? tc : hc;
 }
 
-size_t solve_smem_bytes(const Grid& g) {
-  size_t n = solve_hc_elems(g) + (size_t)g.D * kTile + (size_t)g.R * kTile;
+template <int kTile>
+size_t solve_smem_bytes_t(const Grid& g) {
+  size_t n = solve_hc_elems<kTile>(g) + (size_t)g.D * kTile + (size_t)g.R * kTile;
   return n * sizeof(cpx) + (size_t)8 * g.R * sizeof(double);
 }
 
+// the widest tile's (the fit check of a grid)
+size_t solve_smem_bytes(const Grid& g) { return solve_smem_bytes_t<16>(g); }
+
+template <int kTile>
 __device__ inline SolveSmem carve_solve(const Grid& g, unsigned char* base) {
   SolveSmem s;
   cpx* p = reinterpret_cast<cpx*>(base);
   s.hc = p;
   s.ra = p;
   s.rb = p + (size_t)g.R * kTile;
-  p += solve_hc_elems(g);
+  p += solve_hc_elems<kTile>(g);
   s.Fa = p; p += (size_t)g.D * kTile;
   s.Fb = p; p += (size_t)g.R * kTile;
   s.m0 = reinterpret_cast<double*>(p);
@@ -248,6 +260,7 @@ __device__ inline SolveSmem carve_solve(const Grid& g, unsigned char* base) {
 //   Fa = Qpw . i(kx Hx + kz Hz) - K2 Qw . Hy  [+ Qppw . -i(kz Sx - kx Sz)]
 //   Fb = Rw . i(kz Hx - kx Hz)                [+ Rpw  .  i(kz Sz + kx Sx)]
 // (channel/project.c:97-115, 177-191; channel/adjproject.c:113-134, 218-234)
+template <int kTile>
 __device__ void quad_rhs(const Grid& g, const cpx* __restrict__ H, int z, int x0, int nx, bool adj,
                          SolveSmem& s) {
   const int lx = threadIdx.x % kTile, grp = threadIdx.x / kTile, ngrp = blockDim.x / kTile;
@@ -373,12 +386,14 @@ __device__ void quad_rhs(const Grid& g, const cpx* __restrict__ H, int z, int x0
 // of the FP64 version's parity-combined inputs), times the digit tables of
 // the weighted transposes; one FP64 rounding per contraction.
 //   Fa = Qpw P - K2 Qw Hy [+ Qppw Sa],   Fb = Rw G [+ Rpw Sb]
+template <int kTile>
 __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int x0, int nx, bool adj,
                             SolveSmem& s) {
+  constexpr int NC = 2 * kTile;  // digit columns: Re, Im of each kx column
   const int KT = (g.Q + 15) / 16, MTw = (g.R + 15) / 16;
   const size_t KS = solve_tc_kstride(g);
-  uint16_t* dig = reinterpret_cast<uint16_t*>(s.hc);             // [7][32 columns][KS]
-  int* exc = reinterpret_cast<int*>(dig + (size_t)kDig * 32 * KS);  // [16]
+  uint16_t* dig = reinterpret_cast<uint16_t*>(s.hc);             // [7][NC][KS]
+  int* exc = reinterpret_cast<int*>(dig + (size_t)kDig * NC * KS);  // [kTile]
   const double kz = g.Kz[z];
   const size_t cs = (size_t)g.Q * g.X;
   const cpx* Hz_ = H + (size_t)z * 5 * cs;  // slot c at Hz_ + c*cs + y*X + x
@@ -434,8 +449,8 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
       for (int k = 0; k < kQuadRegs; ++k) {
         if (k >= KT) break;
         const int y = y0 + 16 * k;
-        digits_bf16(scaled56(vin[k].re, ex), dig + (size_t)(2 * col) * KS + y, 32 * KS);
-        digits_bf16(scaled56(vin[k].im, ex), dig + (size_t)(2 * col + 1) * KS + y, 32 * KS);
+        digits_bf16(scaled56(vin[k].re, ex), dig + (size_t)(2 * col) * KS + y, NC * KS);
+        digits_bf16(scaled56(vin[k].im, ex), dig + (size_t)(2 * col + 1) * KS + y, NC * KS);
       }
     } else {
       for (int i = threadIdx.x; i < g.Q * kTile; i += blockDim.x) {
@@ -451,8 +466,8 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
         const int y = i / kTile, col = i - y * kTile;
         const cpx v = (y < g.Q && col < nx) ? input(q, y, col) : cpx{0.0, 0.0};
         const int ex = exc[col] - 1022;
-        digits_bf16(scaled56(v.re, ex), dig + (size_t)(2 * col) * KS + y, 32 * KS);
-        digits_bf16(scaled56(v.im, ex), dig + (size_t)(2 * col + 1) * KS + y, 32 * KS);
+        digits_bf16(scaled56(v.re, ex), dig + (size_t)(2 * col) * KS + y, NC * KS);
+        digits_bf16(scaled56(v.im, ex), dig + (size_t)(2 * col + 1) * KS + y, NC * KS);
       }
     }
     __syncthreads();
@@ -462,7 +477,7 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
       const int col = nt * 4 + t, n = nt * 8 + gq;
       const int ecol = exc[min(col, kTile - 1)] - 1022;
       long long Hh[4], Ll[4];
-      tc_tile_pf(W + (size_t)w * MTw * KT * kDig * 32, mt, KT, KT, dig, KS, (size_t)32 * KS, n, lane, t, Hh, Ll);
+      tc_tile_pf(W + (size_t)w * MTw * KT * kDig * 32, mt, KT, KT, dig, KS, (size_t)NC * KS, n, lane, t, Hh, Ll);
 #pragma unroll
       for (int rr = 0; rr < 2; ++rr) {
         const int row = mt * 16 + gq + 8 * rr;
@@ -520,7 +535,7 @@ __device__ void band_solve_chain(const double* __restrict__ LU, const double* __
 
 
 
-template <bool MULTI>
+template <bool MULTI, int kTile>
 __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ Grid g0, SolveArgs a) {
   const int ntx = (g0.X + kTile - 1) / kTile;
   const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
@@ -552,12 +567,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     return;
   }
   extern __shared__ __align__(16) unsigned char smem[];
-  SolveSmem s = carve_solve(g, smem);
+  SolveSmem s = carve_solve<kTile>(g, smem);
   const RKc rk = rk_coeffs(a.k, a.adjoint);
   const bool adj = a.adjoint != 0;
   const cpx* __restrict__ H = a.H.at(inst);
-  if (g.tc) quad_rhs_tc(g, H, z, x0, nx, adj, s);
-  else quad_rhs(g, H, z, x0, nx, adj, s);
+  if (g.tc) quad_rhs_tc<kTile>(g, H, z, x0, nx, adj, s);
+  else quad_rhs<kTile>(g, H, z, x0, nx, adj, s);
   const double dt = g.dt;
   const int xfirst = (z == 0 && x0 == 0) ? 1 : 0;  // the mean mode has its own system
   // Re-sensitivity forcing of this tangent (kind 2: the reference's forcing
@@ -837,8 +852,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   //  channel/adjproject.c:393-549)
   if (adj) {
     __syncthreads();
-    if (g.tc) quad_rhs_tc(g, a.Hprev.at(inst), z, x0, nx, true, s);
-    else quad_rhs(g, a.Hprev.at(inst), z, x0, nx, true, s);
+    if (g.tc) quad_rhs_tc<kTile>(g, a.Hprev.at(inst), z, x0, nx, true, s);
+    else quad_rhs<kTile>(g, a.Hprev.at(inst), z, x0, nx, true, s);
     if (xfirst == 1 && threadIdx.x < 32) {
       // mean mode fa/fb from the previous-stage terms (channel/adjproject0.c:254-294)
       const cpx* H0 = a.Hprev.at(inst);
@@ -911,19 +926,29 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   }
 }
 
+template <int T>
+static void launch_solve_t(const Grid& g, const SolveArgs& a, cudaStream_t st) {
+  const int ntx = (g.X + T - 1) / T;
+  const dim3 grid(g.Nz * ntx, a.ninst);
+  if (a.grids) k_solve<true, T><<<grid, kThreads, solve_smem_bytes_t<T>(g), st>>>(g, a);
+  else k_solve<false, T><<<grid, kThreads, solve_smem_bytes_t<T>(g), st>>>(g, a);
+}
+
+// the block tile of Grid::stile (8 or 16 kx columns; the same results)
 cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
-  const int ntx = (g.X + kTile - 1) / kTile;
-  if (a.grids) k_solve<true><<<dim3(g.Nz * ntx, a.ninst), kThreads, solve_smem_bytes(g), st>>>(g, a);
-  else k_solve<false><<<dim3(g.Nz * ntx, a.ninst), kThreads, solve_smem_bytes(g), st>>>(g, a);
+  if (g.stile == 8) launch_solve_t<8>(g, a, st);
+  else launch_solve_t<16>(g, a, st);
   return cudaGetLastError();
 }
 
 void prepare_recon_solve(int optin) {
   allow_max_smem(k_recon<false>, optin);
-  allow_max_smem(k_solve<false>, optin);
   allow_max_smem(k_recon<true>, optin);
-  allow_max_smem(k_solve<true>, optin);
+  allow_max_smem(k_solve<false, 16>, optin);
+  allow_max_smem(k_solve<true, 16>, optin);
+  allow_max_smem(k_solve<false, 8>, optin);
+  allow_max_smem(k_solve<true, 8>, optin);
 }
 
 }  // namespace chn
