@@ -157,6 +157,26 @@ __device__ __forceinline__ cpx cmul(cpx a, cpx b) {
   return r;
 }
 
+// (row, col) of a flat index i = row * W + col walked in steps of `step`
+// without a division per step: one division at the start, then a carry.
+struct FlatRC {
+  int r, c, dr, dc, W;
+  __device__ __forceinline__ FlatRC(int i0, int step, int W_) : W(W_) {
+    r = i0 / W;
+    c = i0 - r * W;
+    dr = step / W;
+    dc = step - dr * W;
+  }
+  __device__ __forceinline__ void next() {
+    c += dc;
+    r += dr;
+    if (c >= W) {
+      c -= W;
+      ++r;
+    }
+  }
+};
+
 // Uneven batches: a MULTI kernel takes its instance's grid (sizes and
 // tables) from a device array, staged once per block in shared memory; the
 // launch is sized for the largest grid (kernel argument g0) and blocks beyond

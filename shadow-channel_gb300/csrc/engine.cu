@@ -892,10 +892,26 @@ static GraphKey& add_opts(GraphKey& k, const FwdOpts& o) {
 // steps-left counter down and ends the loop after the last step.  The graph
 // is built once per working set and key (or taken from the working set's
 // graphs when the key matches); each sweep sets the counter and launches it.
+// CHN_SWEEP_GRAPHS=0 launches every step's kernels on the stream instead
+// (the same kernels and results; profilers that skip the kernel nodes of
+// graphs with conditional nodes then see every launch).
+static bool sweep_graphs_on() {
+  static const bool on = [] {
+    const char* v = getenv("CHN_SWEEP_GRAPHS");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
 template <typename F>
 static bool run_steps(Engine& e, Work& w, const GraphKey& key, int nsteps, F&& enqueue) {
   if (nsteps <= 0) return true;
   if (nsteps == 1) return enqueue();
+  if (!sweep_graphs_on()) {
+    for (int i = 0; i < nsteps; ++i)
+      if (!enqueue()) return false;
+    return true;
+  }
   Work::StepGraph* sg = nullptr;
   for (Work::StepGraph& x : w.graphs)
     if (x.key == key.s) sg = &x;

@@ -246,8 +246,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
       const int KW = d.KTz * 8;
       const size_t zstride = (size_t)((d.NZ + 7) / 8 * 8) * d.KSz / 2;  // words between digits
       uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
-      for (int i = threadIdx.x; i < d.NZ * KW; i += blockDim.x) {
-        const int n = i / KW, w = i - n * KW;
+      FlatRC rc(threadIdx.x, blockDim.x, KW);
+      for (int i = threadIdx.x; i < d.NZ * KW; i += blockDim.x, rc.next()) {
+        const int n = rc.r, w = rc.c;
         const int kk = g.tcZM[w];
         cpx v = {0.0, 0.0};
         if (kk >= 0 && n < nfb * g.X) v = Fin[n * Kk + kk];
@@ -274,7 +275,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
           if (row >= 2 * d.pzh || col >= nfb * g.X) continue;
           const int e = g.tcZE[row] + exz[col] - 1022 - 64;
           const bool im = row >= d.pzh;
-          const int m = im ? row - d.pzh : row, fl = col / g.X, x = col - fl * g.X;
+          const int m = im ? row - d.pzh : row;
+          int fl = 0, x = col;  // col = fl X + x, fl < kFB
+          while (x >= g.X) { x -= g.X; ++fl; }
           const bool counts = !(im && x == 0);
           const double vp = round_col(HE[r] + HO[r], LE[r] + LO[r], e, exz[col]);
           cpx& zp = Zb[((size_t)fl * g.pz + m) * g.X + x];
@@ -303,8 +306,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
     {
       uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
       const int npad = (ncx + 7) / 8 * 8, KW = d.KTx * 8, WE = d.KTxE * 8;
-      for (int i = threadIdx.x; i < npad * KW; i += blockDim.x) {
-        const int n = i / KW, w = i - n * KW;
+      FlatRC rc(threadIdx.x, blockDim.x, KW);
+      for (int i = threadIdx.x; i < npad * KW; i += blockDim.x, rc.next()) {
+        const int n = rc.r, w = rc.c;
         const int j = w < WE ? (w < d.nxE ? d.Rx * w : -1) : (w - WE < d.nxO ? 2 * (w - WE) + 1 : -1);
         cpx v = {0.0, 0.0};
         if (j >= 0 && n < ncx) v = Zb[(size_t)n * g.X + j];
@@ -327,7 +331,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
         for (int r = 0; r < 4; ++r) {
           const int xp = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
           if (xp >= d.pxh || col >= ncx) continue;
-          const int fl = col / g.pz, m = col - fl * g.pz;
+          int fl = 0, m = col;  // col = fl pz + m, fl < kFB
+          while (m >= g.pz) { m -= g.pz; ++fl; }
           const int e = g.tcXE[xp] + exx[col] - 1022 - 64;
           double* Pr = P + ((size_t)(f0 + fl) * g.Q + y) * plane + (size_t)m * g.px;
           const double vp = round_col(HE[r] + HO[r], LE[r] + LO[r], e, exx[col]);
@@ -463,11 +468,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
       for (int i = threadIdx.x; i < pb * exs; i += blockDim.x) exx3[i] = 0;
       __syncthreads();
       const int nc = min(pb, ncomp - q);
-      for (int i = threadIdx.x; i < g.pz * g.px; i += blockDim.x) {
+      FlatRC rc(threadIdx.x, blockDim.x, g.px);
+      for (int i = threadIdx.x; i < g.pz * g.px; i += blockDim.x, rc.next()) {
         double v[PB];
 #pragma unroll
         for (int cc = 0; cc < PB; ++cc) v[cc] = cc < nc ? split_product(mode, Pp, Pt, fs, i, q + cc) : 0.0;
-        const int row = i / g.px;
+        const int row = rc.r;
 #pragma unroll
         for (int cc = 0; cc < PB; ++cc) {
           if (cc >= nc) break;
@@ -478,8 +484,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
       }
       __syncthreads();
     }
-    for (int i = threadIdx.x; i < d.pzp * (d.KTx * 16); i += blockDim.x) {
-      const int n = i / (d.KTx * 16), k = i - n * (d.KTx * 16);
+    FlatRC rcx(threadIdx.x, blockDim.x, d.KTx * 16);
+    for (int i = threadIdx.x; i < d.pzp * (d.KTx * 16); i += blockDim.x, rcx.next()) {
+      const int n = rcx.r, k = rcx.c;
       const double v = (n < g.pz && k < g.px) ? stage[(size_t)n * g.px + k] : 0.0;
       digits_bf16(scaled56(v, exx[min(n, g.pz - 1)] - 1022), dig + (size_t)n * d.KSx + k, xstride);
     }
@@ -506,17 +513,21 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
     // ---- z stage inputs: columns kx, K = 2 pz (Re, Im of Y[zp][kx] interleaved)
     for (int i = threadIdx.x; i < g.X; i += blockDim.x) exz[i] = 0;
     __syncthreads();
-    for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x) {
-      const cpx v = Yb[i];
-      const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
-                        (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
-      if (e) atomicMax(&exz[i % g.X], e);
+    {
+      FlatRC rc(threadIdx.x, blockDim.x, g.X);
+      for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x, rc.next()) {
+        const cpx v = Yb[i];
+        const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
+                          (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
+        if (e) atomicMax(&exz[rc.c], e);
+      }
     }
     __syncthreads();
     {
       uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
-      for (int i = threadIdx.x; i < d.Xp * (d.KTz * 8); i += blockDim.x) {
-        const int n = i / (d.KTz * 8), zp = i - n * (d.KTz * 8);
+      FlatRC rc(threadIdx.x, blockDim.x, d.KTz * 8);
+      for (int i = threadIdx.x; i < d.Xp * (d.KTz * 8); i += blockDim.x, rc.next()) {
+        const int n = rc.r, zp = rc.c;
         const cpx v = (n < g.X && zp < g.pz) ? Yb[(size_t)zp * g.X + n] : cpx{0.0, 0.0};
         const int ex = exz[min(n, g.X - 1)] - 1022;
         digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSz) / 2 + zp, zstride / 2);
@@ -543,8 +554,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
     }
     __syncthreads();
     // ---- outputs (the (kk, kx) -> thread map is the same for every q)
-    for (int i = threadIdx.x; i < d.Kk * g.X; i += blockDim.x) {
-      const int kk = i / g.X, x = i - kk * g.X;
+    FlatRC rco(threadIdx.x, blockDim.x, g.X);
+    for (int i = threadIdx.x; i < d.Kk * g.X; i += blockDim.x, rco.next()) {
+      const int kk = rco.r, x = rco.c;
       const int z = kk < g.Nz / 2 ? kk : kk + 1;
       if (mode < 2) H[(((size_t)z * 5 + q) * g.Q + y) * g.X + x] = Fb[i];
       else assemble_stage(g, mode == 3, H, z, y, x, q, Fb[i]);

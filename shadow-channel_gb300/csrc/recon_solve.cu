@@ -511,6 +511,7 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
 template <int W, int DL, int DU>
 __device__ void band_solve_chain(const double* __restrict__ LU, const double* __restrict__ RD, int N, int par,
                                  double* b, int bstride) {
+#pragma unroll 4
   for (int i = par; i < N; i += 2) {
     if (i < 2) continue;
     const int j0 = DL - i / 2;
@@ -522,6 +523,7 @@ __device__ void band_solve_chain(const double* __restrict__ LU, const double* __
   }
   // back substitution: the last row of this parity first
   const int ilast = ((N - 1 - par) % 2 == 0) ? N - 1 : N - 2;
+#pragma unroll 4
   for (int i = ilast; i >= 0; i -= 2) {
     double acc = b[i * bstride];
     const int jm = min(DU, (N - i + 1) / 2 - 1);  // no terms for i > N - 3
@@ -874,28 +876,32 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     }
     __syncthreads();
   }
+  // the solved state of this tile (So) is still in ra, rb unless the
+  // adjoint's second quadrature overwrote them (they share its digit
+  // buffer); the results go to Fa, Fb (each element read and written by one
+  // thread)
   for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx || l < xfirst) continue;
     const int x = x0 + l;
     const size_t zx = (size_t)z * g.X + x;
-    cpx va, vb;
+    const cpx* ya = adj ? So + cidx(0, 0, x) : s.ra + l;
+    const cpx* yb = adj ? So + cidx(1, 0, x) : s.rb + l;
+    const int ys = adj ? g.X : kTile;
     if (r < g.D) {
       const double* E = g.exA + ((size_t)rk.aidx_next * g.Nz * g.X + zx) * g.D * 9;
-      va = band_matvec_row(E, 9, 4, 4, g.D, So + cidx(0, 0, x), g.X, r);
+      cpx va = band_matvec_row_t<9, 4, 4>(E, g.D, ya, ys, r);
       const cpx f = s.Fa[r * kTile + l];
       va.re += dt * rk.dnext * f.re;
       va.im += dt * rk.dnext * f.im;
-    } else {
-      va = So[cidx(0, r, x)];
+      s.Fa[r * kTile + l] = va;
     }
     const double* E = g.exB + ((size_t)rk.aidx_next * g.Nz * g.X + zx) * g.R * 5;
-    vb = band_matvec_row(E, 5, 2, 2, g.R, So + cidx(1, 0, x), g.X, r);
+    cpx vb = band_matvec_row_t<5, 2, 2>(E, g.R, yb, ys, r);
     const cpx f = s.Fb[r * kTile + l];
     vb.re += dt * rk.dnext * f.re;
     vb.im += dt * rk.dnext * f.im;
-    s.ra[r * kTile + l] = va;
-    s.rb[r * kTile + l] = vb;
+    s.Fb[r * kTile + l] = vb;
   }
   if (xfirst == 1 && threadIdx.x < 32) {
     const double* E = g.ex0 + (size_t)rk.aidx_next * g.R * 5;
@@ -920,8 +926,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
       Cc[cidx(0, r, x)] = ca[r];
       Cc[cidx(1, r, x)] = ca[g.R + r];
     } else {
-      Cc[cidx(0, r, x)] = s.ra[r * kTile + l];
-      Cc[cidx(1, r, x)] = s.rb[r * kTile + l];
+      Cc[cidx(0, r, x)] = r < g.D ? s.Fa[r * kTile + l] : So[cidx(0, r, x)];  // rows >= Ny-4 carried
+      Cc[cidx(1, r, x)] = s.Fb[r * kTile + l];
     }
   }
 }

@@ -7,9 +7,34 @@
 
 namespace chn {
 
-// out[i] = sum_j A[i][j] y[i + 2(j - dl)] over the valid band (channel/mvOps.c:198-220)
+// out[i] = sum_j A[i][j] y[i + 2(j - DL)] over the valid band (channel/mvOps.c:198-220),
+// band layout (width W, lower DL, upper DU) known at compile time: the band
+// loop unrolls with per-term predicates (the loads issue together), the
+// multiply-adds keep the ascending order
+template <int W, int DL, int DU>
+__device__ __forceinline__ cpx band_matvec_row_t(const double* __restrict__ A, int N, const cpx* y, int ystride,
+                                                 int i) {
+  int j0 = DL - i / 2;
+  if (j0 < 0) j0 = 0;
+  int j1 = (N - i + 1) / 2 + DL;
+  if (j1 > DL + DU + 1) j1 = DL + DU + 1;
+  double re = 0.0, im = 0.0;
+#pragma unroll
+  for (int j = 0; j < DL + DU + 1; ++j) {
+    if (j < j0 || j >= j1) continue;
+    const double a = __ldg(A + (size_t)i * W + j);
+    const cpx v = y[(i - 2 * (DL - j)) * ystride];
+    re = fma(a, v.re, re);
+    im = fma(a, v.im, im);
+  }
+  return cpx{re, im};
+}
+
+// the same for the two band layouts in use, chosen by the arguments
 __device__ __forceinline__ cpx band_matvec_row(const double* __restrict__ A, int w, int dl, int du, int N,
                                                const cpx* y, int ystride, int i) {
+  if (w == 9 && dl == 4 && du == 4) return band_matvec_row_t<9, 4, 4>(A, N, y, ystride, i);
+  if (w == 5 && dl == 2 && du == 2) return band_matvec_row_t<5, 2, 2>(A, N, y, ystride, i);
   int j0 = dl - i / 2;
   if (j0 < 0) j0 = 0;
   int j1 = (N - i + 1) / 2 + dl;
