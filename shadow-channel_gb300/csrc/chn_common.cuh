@@ -119,7 +119,7 @@ struct Grid {
   const int* tcXE;
   const int* tcZM;
   int tci;
-  int tcminb;  // blocks per SM the tensor-core inverse is compiled for (2 or 3; autotuned)
+  int tcminb;  // build of the tensor-core inverse (2..5: fields per pass, threads, blocks per SM; autotuned)
   // the same inverse on the fifth-generation tensor cores (phys_tc5.cu,
   // tcgen05.mma with tensor-memory accumulators): the two stages' digit
   // tables as stacked B operands in the K-major canonical layout; tc5 = 0:

@@ -206,7 +206,10 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   const char* tfp64 = getenv("CHN_TRANSFORMS_FP64");
   g.tci = (!(tfp64 && tfp64[0] == '1') && phys_tc_fits(g, optin)) ? 1 : 0;
   g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_fits(g, optin)) ? 1 : 0;
-  g.tcminb = 2;  // until the autotuner has timed both builds (3 blocks rarely fit the shared memory)
+  // the inverse's build (phys_tc.cu) until the autotuner has timed them;
+  // CHN_INVERSE_BUILD=2..5 fixes it (and skips that timing)
+  const char* ib = getenv("CHN_INVERSE_BUILD");
+  g.tcminb = (ib && ib[0] >= '2' && ib[0] <= '5' && ib[1] == 0) ? ib[0] - '0' : 2;
   // the solve's block tile: 16 until the autotuner has timed both;
   // CHN_SOLVE_TILE=8 or 16 fixes it (and skips that timing)
   const char* stl = getenv("CHN_SOLVE_TILE");
@@ -1031,14 +1034,18 @@ static bool autotune_transforms(Engine& e, Work& w) {
   std::vector<Cand> cands;
   const char* t5env = getenv("CHN_INVERSE_TC5");
   const bool t5forced = t5env && (t5env[0] == '0' || t5env[0] == '1');
+  const char* ibenv = getenv("CHN_INVERSE_BUILD");
+  const bool ibforced = ibenv && ibenv[0];
   if (g.tci && g.tcf) {
     // both transforms on the tensor cores: the FFT variants are unused; time
-    // the two register budgets of the mma.sync inverse and the tcgen05 one
+    // the builds of the mma.sync inverse and the tcgen05 one
     if (!(t5forced && g.tc5)) {
-      cands.push_back({g.split, g.tvar, 2, 0, 0.f});
-      cands.push_back({g.split, g.tvar, 3, 0, 0.f});
+      if (ibforced) cands.push_back({g.split, g.tvar, g.tcminb, 0, 0.f});
+      else
+        for (int b = 2; b <= 5; ++b) cands.push_back({g.split, g.tvar, b, 0, 0.f});
     }
-    if (g.t5Z && !(t5forced && !g.tc5) && !w.gdev) cands.push_back({g.split, g.tvar, 2, 1, 0.f});
+    if (g.t5Z && !(t5forced && !g.tc5) && !(ibforced && !t5forced) && !w.gdev)
+      cands.push_back({g.split, g.tvar, 2, 1, 0.f});
   } else {
     if (fused_transforms_fit(g, optin)) cands.push_back({0, 0, g.tcminb, 0, 0.f});
     for (int v = 0; v < split_variant_count(); ++v)
@@ -1117,7 +1124,7 @@ static bool autotune_transforms(Engine& e, Work& w) {
     if (tcv && c.tc5) {
       snprintf(buf, sizeof(buf), "\"tc_inverse_tcgen05\": %.4f, ", c.ms);
     } else if (tcv) {
-      snprintf(buf, sizeof(buf), "\"tc_inverse_minb%d\": %.4f, ", c.minb, c.ms);
+      snprintf(buf, sizeof(buf), "\"tc_inverse_f%d_b%d\": %.4f, ", c.minb <= 3 ? 2 : 1, c.minb, c.ms);
     } else if (c.split) {
       const TransformVariant v = split_variant(c.tvar);
       snprintf(buf, sizeof(buf), "\"split_nt%d_ch%d\": %.4f, ", v.nt, v.ch, c.ms);
@@ -1129,7 +1136,8 @@ static bool autotune_transforms(Engine& e, Work& w) {
   if (tcv && best->tc5) {
     snprintf(buf, sizeof(buf), "\"chosen\": \"tc_inverse_tcgen05\", \"instances\": %d}", nt);
   } else if (tcv) {
-    snprintf(buf, sizeof(buf), "\"chosen\": \"tc_inverse_minb%d\", \"instances\": %d}", best->minb, nt);
+    snprintf(buf, sizeof(buf), "\"chosen\": \"tc_inverse_f%d_b%d\", \"instances\": %d}", best->minb <= 3 ? 2 : 1,
+             best->minb, nt);
   } else if (best->split) {
     const TransformVariant v = split_variant(best->tvar);
     snprintf(buf, sizeof(buf), "\"chosen\": \"split_nt%d_ch%d\", \"instances\": %d}", v.nt, v.ch, nt);

@@ -169,19 +169,19 @@ bool build_fwd_tc_tables(const HostTables& h, std::vector<uint32_t>& xfrag, std:
 // shared-memory plan
 // ---------------------------------------------------------------------------
 
-__host__ __device__ inline size_t phys_tc_dbuf_bytes(const Grid& g) {
-  const PhysTcDims d = phys_tc_dims(g);
+__host__ __device__ inline size_t phys_tc_dbuf_bytes(const Grid& g, int fb) {
+  const PhysTcDims d = phys_tc_dims(g, fb);
   const size_t z = (size_t)kDig * ((d.NZ + 7) / 8 * 8) * d.KSz * 2, x = (size_t)kDig * ((d.NX + 7) / 8 * 8) * d.KSx * 2;
   return (z > x ? z : x + 0);
 }
 
-size_t phys_tc_smem_bytes(const Grid& g, bool with_cfl) {
-  const PhysTcDims d = phys_tc_dims(g);
+size_t phys_tc_smem_bytes(const Grid& g, bool with_cfl, int fb) {
+  const PhysTcDims d = phys_tc_dims(g, fb);
   size_t b = 0;
   b += (size_t)((d.NZ + 3) / 4 * 4) * sizeof(int);            // z-stage column exponents
   b += (size_t)((d.NX + 3) / 4 * 4) * sizeof(int);            // x-stage column exponents
-  b += (phys_tc_dbuf_bytes(g) + 15) / 16 * 16;                 // digits (z, then x)
-  b += (size_t)kFB * g.pz * g.X * sizeof(cpx);                 // Z intermediate
+  b += (phys_tc_dbuf_bytes(g, fb) + 15) / 16 * 16;             // digits (z, then x)
+  b += (size_t)fb * g.pz * g.X * sizeof(cpx);                  // Z intermediate
   (void)with_cfl;  // the CFL number is read back from the written fields
   return b;
 }
@@ -190,18 +190,19 @@ size_t phys_tc_smem_bytes(const Grid& g, bool with_cfl) {
 // kernel
 // ---------------------------------------------------------------------------
 
-template <bool MULTI, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid_constant__ Grid g0, PhysArgs a) {
+// FB fields per pass, NTHR threads, MINB blocks per SM (the register budget)
+template <bool MULTI, int MINB, int FB, int NTHR>
+__global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_constant__ Grid g0, PhysArgs a) {
   const int inst = blockIdx.y, y = blockIdx.x;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
   if (y >= g.Q) return;
   if (a.skip_blocked && blocked(a.status, a.sdiv, inst)) return;
-  const PhysTcDims d = phys_tc_dims(g);
+  const PhysTcDims d = phys_tc_dims(g, FB);
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* p = smem;
   int* exz = reinterpret_cast<int*>(p); p += (size_t)((d.NZ + 3) / 4 * 4) * sizeof(int);
   int* exx = reinterpret_cast<int*>(p); p += (size_t)((d.NX + 3) / 4 * 4) * sizeof(int);
-  uint16_t* dig = reinterpret_cast<uint16_t*>(p); p += (phys_tc_dbuf_bytes(g) + 15) / 16 * 16;
+  uint16_t* dig = reinterpret_cast<uint16_t*>(p); p += (phys_tc_dbuf_bytes(g, FB) + 15) / 16 * 16;
   cpx* Zb = reinterpret_cast<cpx*>(p);  // [fl][m][x]
 
   const cpx* __restrict__ U = a.U.at(inst);
@@ -216,8 +217,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
   bool nonfinite = false;
   for (int i = threadIdx.x; i < d.NZ; i += blockDim.x) exz[i] = 0;
   __syncthreads();
-  for (int f0 = 0; f0 < a.nfields; f0 += kFB) {
-    const int nfb = min(kFB, a.nfields - f0);
+  for (int f0 = 0; f0 < a.nfields; f0 += FB) {
+    const int nfb = min(FB, a.nfields - f0);
     // ---- z stage: columns n = fl * X + x.  The inputs are staged in the Z
     // buffer (free until the z stage writes it: X (Nz - 1) <= pz X values per
     // field); each thread keeps one column (consecutive threads: consecutive
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
           const int e = g.tcZE[row] + exz[col] - 1022 - 64;
           const bool im = row >= d.pzh;
           const int m = im ? row - d.pzh : row;
-          int fl = 0, x = col;  // col = fl X + x, fl < kFB
+          int fl = 0, x = col;  // col = fl X + x, fl < FB
           while (x >= g.X) { x -= g.X; ++fl; }
           const bool counts = !(im && x == 0);
           const double vp = round_col(HE[r] + HO[r], LE[r] + LO[r], e, exz[col]);
@@ -331,7 +332,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
         for (int r = 0; r < 4; ++r) {
           const int xp = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
           if (xp >= d.pxh || col >= ncx) continue;
-          int fl = 0, m = col;  // col = fl pz + m, fl < kFB
+          int fl = 0, m = col;  // col = fl pz + m, fl < FB
           while (m >= g.pz) { m -= g.pz; ++fl; }
           const int e = g.tcXE[xp] + exx[col] - 1022 - 64;
           double* Pr = P + ((size_t)(f0 + fl) * g.Q + y) * plane + (size_t)m * g.px;
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_phys_inverse_tc(const __grid
   if (a.cfl_check) {
     // block max of the CFL field (channel/pass1.c:116-138), from the written
     // velocity fields (this block's own stores)
-    __shared__ double red[kThreads];
+    __shared__ double red[NTHR];
     double mx = 0.0;
     const double* Pu = P + (size_t)y * plane;
     const size_t fs = (size_t)g.Q * plane;
@@ -588,31 +589,43 @@ cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaS
 
 bool phys_tc_fits(const Grid& g, int optin) {
   // the kernel's static shared memory (reduction, staged grid) is below 4 KB;
-  // the input staging keeps one thread per z-stage column
-  return kFB * g.X <= kThreads && phys_tc_smem_bytes(g, true) + 4096 <= (size_t)optin;
+  // the input staging keeps one thread per z-stage column (the widest build's
+  // plan; the one-field builds need less)
+  return kFB * g.X <= kThreads && phys_tc_smem_bytes(g, true, kFB) + 4096 <= (size_t)optin;
 }
 
-// Two builds of the kernel: for 2 blocks per SM (128 registers) and for 3
-// (80 registers, some spilled); Grid::tcminb selects (the autotuner times
-// both; the results are identical)
-cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st) {
-  const size_t sm = phys_tc_smem_bytes(g, a.cfl_check != 0);
+// Builds of the kernel (Grid::tcminb; the autotuner times them, the results
+// are identical): 2 = two fields per pass, 256 threads, 2 blocks per SM (128
+// registers); 3 = the same for 3 blocks (80 registers, some spilled); 4 / 5 =
+// one field per pass in 128-thread blocks, 4 / 5 blocks per SM (half the
+// shared memory, more independent blocks per SM)
+template <bool MULTI>
+static void launch_inverse_build(const Grid& g, const PhysArgs& a, cudaStream_t st) {
   const dim3 grid(g.Q, a.ninst);
-  if (g.tcminb == 3) {
-    if (a.grids) k_phys_inverse_tc<true, 3><<<grid, kThreads, sm, st>>>(g, a);
-    else k_phys_inverse_tc<false, 3><<<grid, kThreads, sm, st>>>(g, a);
-  } else {
-    if (a.grids) k_phys_inverse_tc<true, 2><<<grid, kThreads, sm, st>>>(g, a);
-    else k_phys_inverse_tc<false, 2><<<grid, kThreads, sm, st>>>(g, a);
+  const bool cfl = a.cfl_check != 0;
+  switch (g.tcminb) {
+    case 3: k_phys_inverse_tc<MULTI, 3, 2, 256><<<grid, 256, phys_tc_smem_bytes(g, cfl, 2), st>>>(g, a); break;
+    case 4: k_phys_inverse_tc<MULTI, 4, 1, 128><<<grid, 128, phys_tc_smem_bytes(g, cfl, 1), st>>>(g, a); break;
+    case 5: k_phys_inverse_tc<MULTI, 5, 1, 128><<<grid, 128, phys_tc_smem_bytes(g, cfl, 1), st>>>(g, a); break;
+    default: k_phys_inverse_tc<MULTI, 2, 2, 256><<<grid, 256, phys_tc_smem_bytes(g, cfl, 2), st>>>(g, a); break;
   }
+}
+
+cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st) {
+  if (a.grids) launch_inverse_build<true>(g, a, st);
+  else launch_inverse_build<false>(g, a, st);
   return cudaGetLastError();
 }
 
 void prepare_phys_tc(int optin) {
-  allow_max_smem(k_phys_inverse_tc<false, 2>, optin);
-  allow_max_smem(k_phys_inverse_tc<true, 2>, optin);
-  allow_max_smem(k_phys_inverse_tc<false, 3>, optin);
-  allow_max_smem(k_phys_inverse_tc<true, 3>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 2, 2, 256>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 3, 2, 256>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 3, 2, 256>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 4, 1, 128>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 5, 1, 128>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 5, 1, 128>, optin);
   allow_max_smem(k_products_tc<false, kPB>, optin);
   allow_max_smem(k_products_tc<true, kPB>, optin);
   allow_max_smem(k_products_tc<false, 1>, optin);

@@ -9,7 +9,7 @@
 
 namespace chn {
 
-static constexpr int kFB = 2;  // fields per pass of the mma.sync inverse
+static constexpr int kFB = 2;  // fields per pass of the mma.sync inverse (its widest build)
 
 // kept kz modes of even / odd padded index zp (kk < Nz/2: zp = kk; else
 // zp = kk + 1 + Nz/2, which runs over the odd Nz + 1 ... 3Nz/2 - 1); an odd
@@ -32,7 +32,8 @@ struct PhysTcDims {
   int MTz, MTx, KSz, KSx, NZ, NX;  // NZ = columns of the z stage, NX = of the x stage
 };
 
-__host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g) {
+// fb: fields per pass (the x stage has one column per (field, m))
+__host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g, int fb = kFB) {
   PhysTcDims d;
   d.Rz = g.pz % 2 ? 1 : 2;
   d.Rx = g.px % 2 ? 1 : 2;
@@ -50,8 +51,8 @@ __host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g) {
   d.MTx = (d.pxh + 15) / 16;
   d.KSz = d.KTz * 16 + 8;
   d.KSx = d.KTx * 16 + 8;
-  d.NZ = kFB * g.X;
-  d.NX = kFB * g.pz;  // the x stage: one column per (field, m)
+  d.NZ = fb * g.X;
+  d.NX = fb * g.pz;
   return d;
 }
 

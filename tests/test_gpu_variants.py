@@ -1,9 +1,16 @@
-"""The implicit solve's block tile (kx columns per block: 16 or 8), which
-the autotuner picks per batch, changes which columns share a block but no
-column's arithmetic: the batched sweeps give the same bits with either
-tile.  CHN_SOLVE_TILE fixes the tile at c_init / c_batch_init.  Grids:
-32x65x32 (16 kx columns: one tile of 16 or two of 8) and 48x97x48 (24
-columns: 16 + 8 or three of 8).
+"""Kernel variants the autotuner chooses among give the same bits.
+
+The implicit solve's block tile (kx columns per block: 16 or 8,
+CHN_SOLVE_TILE) changes which columns share a block, not any column's
+arithmetic.  The builds of the tensor-core inverse transform
+(CHN_INVERSE_BUILD: 2 = two fields per pass in 256-thread blocks at two
+blocks per SM, 3 = the same at three, 4 / 5 = one field per pass in
+128-thread blocks at four / five) change how the columns of a plane are
+grouped, not the digit sums or their rounding.  Each variant runs the
+batched forward (primal + 3 tangents, one forced) and the coupled adjoint,
+and the single-trajectory primal, and must reproduce the default's outputs
+bit for bit.  Grids: 32x65x32 (the benchmarked one) and 48x97x48 (24 kx
+columns: 16 + 8 or three tiles of 8 in the solve).
 """
 import ctypes
 import json
@@ -19,6 +26,7 @@ pytestmark = pytest.mark.gpu
 
 GRIDS = [(32, 65, 32, 2 * np.pi, np.pi, 3300.0, 2.0, 0.005, 3), (48, 97, 48, 2 * np.pi, np.pi, 3300.0, 2.0, 0.004, 2)]
 NSEG, NTAN = 2, 3
+KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_AUTOTUNE")
 
 
 @pytest.fixture(scope="module")
@@ -29,12 +37,11 @@ def cc():
     return c_channel
 
 
-def _sweeps(cc, args, tile):
-    old = os.environ.get("CHN_SOLVE_TILE")
-    if tile is None:
-        os.environ.pop("CHN_SOLVE_TILE", None)
-    else:
-        os.environ["CHN_SOLVE_TILE"] = str(tile)
+def _sweeps(cc, args, env):
+    old = {k: os.environ.get(k) for k in KNOBS}
+    for k in KNOBS:
+        os.environ.pop(k, None)
+    os.environ.update(env)
     try:
         n = args[-1]
         Nx, Ny, Nz = args[:3]
@@ -59,30 +66,44 @@ def _sweeps(cc, args, tile):
         finally:
             lib.c_batch_destroy()
         single = O.synthetic_state(Nx, Ny, Nz, seed=99)
-        cc.c_primal(0, single)   # the single-trajectory engine takes the tile of c_init
+        cc.c_primal(0, single)   # the single-trajectory engine takes the variants of c_init
         cc.c_destroy()
         return [C, IC, AC, np.stack(traj), single], report
     finally:
-        if old is None:
-            os.environ.pop("CHN_SOLVE_TILE", None)
-        else:
-            os.environ["CHN_SOLVE_TILE"] = old
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
 
 
-@pytest.mark.parametrize("gi", [0, 1])
-def test_solve_tiles_give_the_same_bits(cc, gi):
-    a, _ = _sweeps(cc, GRIDS[gi], 16)
-    b, _ = _sweeps(cc, GRIDS[gi], 8)
+def _same(a, b):
     for x, y in zip(a, b):
         assert np.array_equal(x.view(np.float64), y.view(np.float64))
 
 
-def test_autotuner_reports_the_solve_tile(cc):
-    res, report = _sweeps(cc, GRIDS[0], None)
+@pytest.mark.parametrize("gi", [0, 1])
+def test_solve_tiles_give_the_same_bits(cc, gi):
+    a, _ = _sweeps(cc, GRIDS[gi], {"CHN_SOLVE_TILE": "16"})
+    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_SOLVE_TILE": "8"})
+    _same(a, b)
+
+
+@pytest.mark.parametrize("build", ["3", "4", "5"])
+def test_inverse_builds_give_the_same_bits(cc, build):
+    a, _ = _sweeps(cc, GRIDS[0], {"CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
+    b, _ = _sweeps(cc, GRIDS[0], {"CHN_INVERSE_BUILD": build, "CHN_AUTOTUNE": "0"})
+    _same(a, b)
+
+
+def test_autotuner_reports_its_choices(cc):
+    res, report = _sweeps(cc, GRIDS[0], {})
     if "solve_chosen" not in report:
         pytest.skip("autotuner off (CHN_AUTOTUNE=0)")
     assert report["solve_chosen"] in ("tile16", "tile8")
     assert report["solve_tile16"] > 0 and report["solve_tile8"] > 0
-    ref, _ = _sweeps(cc, GRIDS[0], 16)
-    for x, y in zip(res, ref):
-        assert np.array_equal(x.view(np.float64), y.view(np.float64))
+    assert report["chosen"].startswith("tc_inverse_")
+    for b in ("f2_b2", "f2_b3", "f1_b4", "f1_b5"):
+        assert report["tc_inverse_" + b] > 0
+    ref, _ = _sweeps(cc, GRIDS[0], {"CHN_SOLVE_TILE": "16", "CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
+    _same(res, ref)
