@@ -209,7 +209,7 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   // the inverse's build (phys_tc.cu) until the autotuner has timed them;
   // CHN_INVERSE_BUILD=2..5 fixes it (and skips that timing)
   const char* ib = getenv("CHN_INVERSE_BUILD");
-  g.tcminb = (ib && ib[0] >= '2' && ib[0] <= '5' && ib[1] == 0) ? ib[0] - '0' : 2;
+  g.tcminb = (ib && ib[0] >= '2' && ib[0] <= '7' && ib[1] == 0) ? ib[0] - '0' : 2;
   // the solve's block tile: 16 until the autotuner has timed both;
   // CHN_SOLVE_TILE=8 or 16 fixes it (and skips that timing)
   const char* stl = getenv("CHN_SOLVE_TILE");
@@ -1018,6 +1018,19 @@ static bool collect_status(Engine& e, Work& w) {
 
 static std::string g_tune_report;
 
+// the builds of the tensor-core inverse (Grid::tcminb): fields per pass,
+// blocks per SM, compile-time sizes
+static const char* inverse_build_name(int b) {
+  switch (b) {
+    case 3: return "f2_b3";
+    case 4: return "f1_b4";
+    case 5: return "f1_b5";
+    case 6: return "f1_b4_fixed";
+    case 7: return "f2_b2_fixed";
+    default: return "f2_b2";
+  }
+}
+
 static bool autotune_transforms(Engine& e, Work& w) {
   const char* off = getenv("CHN_AUTOTUNE");
   if (off && off[0] == '0') return true;
@@ -1040,9 +1053,13 @@ static bool autotune_transforms(Engine& e, Work& w) {
     // both transforms on the tensor cores: the FFT variants are unused; time
     // the builds of the mma.sync inverse and the tcgen05 one
     if (!(t5forced && g.tc5)) {
-      if (ibforced) cands.push_back({g.split, g.tvar, g.tcminb, 0, 0.f});
-      else
+      if (ibforced) {
+        cands.push_back({g.split, g.tvar, g.tcminb, 0, 0.f});
+      } else {
         for (int b = 2; b <= 5; ++b) cands.push_back({g.split, g.tvar, b, 0, 0.f});
+        if (!w.gdev && phys_tc_specialised(g))
+          for (int b = 6; b <= 7; ++b) cands.push_back({g.split, g.tvar, b, 0, 0.f});
+      }
     }
     if (g.t5Z && !(t5forced && !g.tc5) && !(ibforced && !t5forced) && !w.gdev)
       cands.push_back({g.split, g.tvar, 2, 1, 0.f});
@@ -1124,7 +1141,7 @@ static bool autotune_transforms(Engine& e, Work& w) {
     if (tcv && c.tc5) {
       snprintf(buf, sizeof(buf), "\"tc_inverse_tcgen05\": %.4f, ", c.ms);
     } else if (tcv) {
-      snprintf(buf, sizeof(buf), "\"tc_inverse_f%d_b%d\": %.4f, ", c.minb <= 3 ? 2 : 1, c.minb, c.ms);
+      snprintf(buf, sizeof(buf), "\"tc_inverse_%s\": %.4f, ", inverse_build_name(c.minb), c.ms);
     } else if (c.split) {
       const TransformVariant v = split_variant(c.tvar);
       snprintf(buf, sizeof(buf), "\"split_nt%d_ch%d\": %.4f, ", v.nt, v.ch, c.ms);
@@ -1136,8 +1153,8 @@ static bool autotune_transforms(Engine& e, Work& w) {
   if (tcv && best->tc5) {
     snprintf(buf, sizeof(buf), "\"chosen\": \"tc_inverse_tcgen05\", \"instances\": %d}", nt);
   } else if (tcv) {
-    snprintf(buf, sizeof(buf), "\"chosen\": \"tc_inverse_f%d_b%d\", \"instances\": %d}", best->minb <= 3 ? 2 : 1,
-             best->minb, nt);
+    snprintf(buf, sizeof(buf), "\"chosen\": \"tc_inverse_%s\", \"instances\": %d}", inverse_build_name(best->minb),
+             nt);
   } else if (best->split) {
     const TransformVariant v = split_variant(best->tvar);
     snprintf(buf, sizeof(buf), "\"chosen\": \"split_nt%d_ch%d\", \"instances\": %d}", v.nt, v.ch, nt);

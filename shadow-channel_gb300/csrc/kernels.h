@@ -155,6 +155,8 @@ cudaError_t launch_phys_inverse(const Grid& g, const PhysArgs& a, cudaStream_t s
 // the inverse transforms as exact digit GEMMs on the tensor cores (fused, one block per plane)
 cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st);
 bool phys_tc_fits(const Grid& g, int optin);
+// the grid has compile-time-size builds of the tensor-core inverse (Grid::tcminb 6, 7)
+bool phys_tc_specialised(const Grid& g);
 // the inverse on tcgen05 (phys_tc5.cu): fits for nf fields; the error word
 // of its bounded waits (returned and cleared)
 cudaError_t launch_phys_inverse_tc5(const Grid& g, const PhysArgs& a, cudaStream_t st);

@@ -11,8 +11,11 @@ __device__ __forceinline__ bool blocked(const uint32_t* status, int sdiv, int in
 
 // spectral value of physical field f at (z, x) on plane y: f = 0..2 velocity,
 // 3 = wz, 4 = wx, 5 = wy (channel/pass1.c:58-104)
-__device__ __forceinline__ cpx field_value(const Grid& g, const cpx* __restrict__ U, int f, int z, int y, int x) {
-  auto at = [&](int c) { return U[(((size_t)z * 5 + c) * g.Q + y) * g.X + x]; };
+// (Q, X: the grid's plane count and kx columns, compile-time constants in
+// the specialised transform kernels)
+__device__ __forceinline__ cpx field_value_qx(const Grid& g, int Q, int X, const cpx* __restrict__ U, int f, int z,
+                                              int y, int x) {
+  auto at = [&](int c) { return U[(((size_t)z * 5 + c) * Q + y) * X + x]; };
   cpx r;
   if (f < 3) return at(f);
   const double kx = g.Kx[x], kz = g.Kz[z];
@@ -30,6 +33,10 @@ __device__ __forceinline__ cpx field_value(const Grid& g, const cpx* __restrict_
     r.im = kz * u.re - kx * w.re;
   }
   return r;
+}
+
+__device__ __forceinline__ cpx field_value(const Grid& g, const cpx* __restrict__ U, int f, int z, int y, int x) {
+  return field_value_qx(g, g.Q, g.X, U, f, z, y, x);
 }
 
 // padded spectral row zp -> unpadded kz index, or -1 for the zero band

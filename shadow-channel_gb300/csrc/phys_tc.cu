@@ -190,32 +190,57 @@ size_t phys_tc_smem_bytes(const Grid& g, bool with_cfl, int fb) {
 // kernel
 // ---------------------------------------------------------------------------
 
-// FB fields per pass, NTHR threads, MINB blocks per SM (the register budget)
-template <bool MULTI, int MINB, int FB, int NTHR>
+// The sizes a kernel reads: from the grid at run time, or compile-time
+// constants for the grids with a specialised build (the same arithmetic;
+// the loops over known extents unroll and the index arithmetic folds).
+struct InvSizesRT {  // read from the grid where used (no register copies)
+  const int &Nz, &X, &pz, &px, &Q;
+  __device__ explicit InvSizesRT(const Grid& g) : Nz(g.Nz), X(g.X), pz(g.pz), px(g.px), Q(g.Q) {}
+};
+template <int NZ, int XX, int QQ>
+struct InvSizesCT {
+  static constexpr int Nz = NZ, X = XX, pz = 3 * NZ / 2, px = 3 * XX, Q = QQ;
+  __device__ explicit InvSizesCT(const Grid&) {}
+};
+template <class S>
+__host__ __device__ inline bool sizes_match(const Grid& g) {
+  return g.Nz == S::Nz && g.X == S::X && g.pz == S::pz && g.px == S::px && g.Q == S::Q;
+}
+
+__host__ __device__ constexpr size_t phys_tc_dbuf_of(const PhysTcDims& d) {
+  return (size_t)kDig * ((d.NZ + 7) / 8 * 8) * d.KSz * 2 > (size_t)kDig * ((d.NX + 7) / 8 * 8) * d.KSx * 2
+             ? (size_t)kDig * ((d.NZ + 7) / 8 * 8) * d.KSz * 2
+             : (size_t)kDig * ((d.NX + 7) / 8 * 8) * d.KSx * 2;
+}
+
+// FB fields per pass, NTHR threads, MINB blocks per SM (the register
+// budget), S the sizes (InvSizesRT, or InvSizesCT for a specialised grid)
+template <bool MULTI, int MINB, int FB, int NTHR, class S>
 __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_constant__ Grid g0, PhysArgs a) {
   const int inst = blockIdx.y, y = blockIdx.x;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
-  if (y >= g.Q) return;
+  const S sz(g);
+  if (y >= sz.Q) return;
   if (a.skip_blocked && blocked(a.status, a.sdiv, inst)) return;
-  const PhysTcDims d = phys_tc_dims(g, FB);
+  const PhysTcDims d = phys_tc_dims_n(sz.Nz, sz.pz, sz.px, sz.X, FB);
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* p = smem;
   int* exz = reinterpret_cast<int*>(p); p += (size_t)((d.NZ + 3) / 4 * 4) * sizeof(int);
   int* exx = reinterpret_cast<int*>(p); p += (size_t)((d.NX + 3) / 4 * 4) * sizeof(int);
-  uint16_t* dig = reinterpret_cast<uint16_t*>(p); p += (phys_tc_dbuf_bytes(g, FB) + 15) / 16 * 16;
+  uint16_t* dig = reinterpret_cast<uint16_t*>(p); p += (phys_tc_dbuf_of(d) + 15) / 16 * 16;
   cpx* Zb = reinterpret_cast<cpx*>(p);  // [fl][m][x]
 
   const cpx* __restrict__ U = a.U.at(inst);
   double* __restrict__ P = a.P.at(inst);
   if (a.pslot.stride) P += (long long)a.pslot.slot() * a.pslot.stride;
-  const size_t plane = (size_t)g.pz * g.px;
+  const size_t plane = (size_t)sz.pz * sz.px;
   const uint4* __restrict__ Az = reinterpret_cast<const uint4*>(g.tcZ);
   const uint4* __restrict__ Ax = reinterpret_cast<const uint4*>(g.tcX);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
-  const int nwarp = blockDim.x >> 5;
-  const int Kk = g.Nz - 1;  // kept kz rows
+  constexpr int nwarp = NTHR >> 5;
+  const int Kk = sz.Nz - 1;  // kept kz rows
   bool nonfinite = false;
-  for (int i = threadIdx.x; i < d.NZ; i += blockDim.x) exz[i] = 0;
+  for (int i = threadIdx.x; i < d.NZ; i += NTHR) exz[i] = 0;
   __syncthreads();
   for (int f0 = 0; f0 < a.nfields; f0 += FB) {
     const int nfb = min(FB, a.nfields - f0);
@@ -225,15 +250,15 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
     // x, coalesced loads) and its exponent maximum.  The x stage's column
     // exponents are cleared here and gathered by the z stage's epilogue.
     cpx* Fin = Zb;  // [n][kk]
-    for (int i = threadIdx.x; i < d.NX; i += blockDim.x) exx[i] = 0;
+    for (int i = threadIdx.x; i < d.NX; i += NTHR) exx[i] = 0;
     {
-      const int ncol = nfb * g.X, per = blockDim.x / ncol;
+      const int ncol = nfb * sz.X, per = NTHR / ncol;
       if ((int)threadIdx.x < per * ncol) {
-        const int n = threadIdx.x % ncol, fl = n / g.X, x = n - fl * g.X;
+        const int n = threadIdx.x % ncol, fl = n / sz.X, x = n - fl * sz.X;
         int emax = 0;
         for (int kk = threadIdx.x / ncol; kk < Kk; kk += per) {
-          const int z = kk < g.Nz / 2 ? kk : kk + 1;
-          const cpx v = field_value(g, U, f0 + fl, z, y, x);
+          const int z = kk < sz.Nz / 2 ? kk : kk + 1;
+          const cpx v = field_value_qx(g, sz.Q, sz.X, U, f0 + fl, z, y, x);
           Fin[(size_t)n * Kk + kk] = v;
           emax = max(emax, max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
                                (int)((__double_as_longlong(v.im) >> 52) & 0x7FF)));
@@ -247,12 +272,12 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
       const int KW = d.KTz * 8;
       const size_t zstride = (size_t)((d.NZ + 7) / 8 * 8) * d.KSz / 2;  // words between digits
       uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
-      FlatRC rc(threadIdx.x, blockDim.x, KW);
-      for (int i = threadIdx.x; i < d.NZ * KW; i += blockDim.x, rc.next()) {
+      FlatRC rc(threadIdx.x, NTHR, KW);
+      for (int i = threadIdx.x; i < d.NZ * KW; i += NTHR, rc.next()) {
         const int n = rc.r, w = rc.c;
         const int kk = g.tcZM[w];
         cpx v = {0.0, 0.0};
-        if (kk >= 0 && n < nfb * g.X) v = Fin[n * Kk + kk];
+        if (kk >= 0 && n < nfb * sz.X) v = Fin[n * Kk + kk];
         const int ex = exz[n] - 1022;
         digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSz) / 2 + w, zstride);
       }
@@ -262,7 +287,7 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
       // rows Re Z[m], Im Z[m] for m < pzh; E + O -> Z[m], E - O -> Z[m + pzh];
       // the exponent of each value into its x-stage column (fl, m) (not the
       // imaginary part of the kx = 0 bin, which c2r ignores)
-      const int NT = (nfb * g.X + 7) / 8;
+      const int NT = (nfb * sz.X + 7) / 8;
       const size_t dstride = (size_t)((d.NZ + 7) / 8 * 8) * d.KSz;  // bf16 between digits
       for (int item = warp; item < d.MTz * NT; item += nwarp) {
         const int mt = item / NT, nt = item - mt * NT;
@@ -273,26 +298,26 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int row = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
-          if (row >= 2 * d.pzh || col >= nfb * g.X) continue;
+          if (row >= 2 * d.pzh || col >= nfb * sz.X) continue;
           const int e = g.tcZE[row] + exz[col] - 1022 - 64;
           const bool im = row >= d.pzh;
           const int m = im ? row - d.pzh : row;
           int fl = 0, x = col;  // col = fl X + x, fl < FB
-          while (x >= g.X) { x -= g.X; ++fl; }
+          while (x >= sz.X) { x -= sz.X; ++fl; }
           const bool counts = !(im && x == 0);
           const double vp = round_col(HE[r] + HO[r], LE[r] + LO[r], e, exz[col]);
-          cpx& zp = Zb[((size_t)fl * g.pz + m) * g.X + x];
+          cpx& zp = Zb[((size_t)fl * sz.pz + m) * sz.X + x];
           if (im) zp.im = vp;
           else zp.re = vp;
           const int ep = (int)((__double_as_longlong(vp) >> 52) & 0x7FF);
-          if (counts && ep) atomicMax(&exx[fl * g.pz + m], ep);
+          if (counts && ep) atomicMax(&exx[fl * sz.pz + m], ep);
           if (d.Rz == 2) {
             const double vm = round_col(HE[r] - HO[r], LE[r] - LO[r], e, exz[col]);
-            cpx& zm = Zb[((size_t)fl * g.pz + m + d.pzh) * g.X + x];
+            cpx& zm = Zb[((size_t)fl * sz.pz + m + d.pzh) * sz.X + x];
             if (im) zm.im = vm;
             else zm.re = vm;
             const int em = (int)((__double_as_longlong(vm) >> 52) & 0x7FF);
-            if (counts && em) atomicMax(&exx[fl * g.pz + m + d.pzh], em);
+            if (counts && em) atomicMax(&exx[fl * sz.pz + m + d.pzh], em);
           }
         }
       }
@@ -301,18 +326,18 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
     // ---- x stage, both fields: columns n = fl * pz + m, K words: Re, Im of
     // Z[m][j] for the even j, then the odd j (Im of j = 0 unused).  The z
     // stage's column exponents are cleared for the next pass.
-    const int ncx = nfb * g.pz;
+    const int ncx = nfb * sz.pz;
     const size_t xstride = (size_t)((d.NX + 7) / 8 * 8) * d.KSx;
-    for (int i = threadIdx.x; i < d.NZ; i += blockDim.x) exz[i] = 0;
+    for (int i = threadIdx.x; i < d.NZ; i += NTHR) exz[i] = 0;
     {
       uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
       const int npad = (ncx + 7) / 8 * 8, KW = d.KTx * 8, WE = d.KTxE * 8;
-      FlatRC rc(threadIdx.x, blockDim.x, KW);
-      for (int i = threadIdx.x; i < npad * KW; i += blockDim.x, rc.next()) {
+      FlatRC rc(threadIdx.x, NTHR, KW);
+      for (int i = threadIdx.x; i < npad * KW; i += NTHR, rc.next()) {
         const int n = rc.r, w = rc.c;
         const int j = w < WE ? (w < d.nxE ? d.Rx * w : -1) : (w - WE < d.nxO ? 2 * (w - WE) + 1 : -1);
         cpx v = {0.0, 0.0};
-        if (j >= 0 && n < ncx) v = Zb[(size_t)n * g.X + j];
+        if (j >= 0 && n < ncx) v = Zb[(size_t)n * sz.X + j];
         if (j == 0) v.im = 0.0;
         const int ex = exx[min(n, ncx - 1)] - 1022;
         digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSx) / 2 + w, xstride / 2);
@@ -333,9 +358,9 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
           const int xp = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
           if (xp >= d.pxh || col >= ncx) continue;
           int fl = 0, m = col;  // col = fl pz + m, fl < FB
-          while (m >= g.pz) { m -= g.pz; ++fl; }
+          while (m >= sz.pz) { m -= sz.pz; ++fl; }
           const int e = g.tcXE[xp] + exx[col] - 1022 - 64;
-          double* Pr = P + ((size_t)(f0 + fl) * g.Q + y) * plane + (size_t)m * g.px;
+          double* Pr = P + ((size_t)(f0 + fl) * sz.Q + y) * plane + (size_t)m * sz.px;
           const double vp = round_col(HE[r] + HO[r], LE[r] + LO[r], e, exx[col]);
           Pr[xp] = vp;
           nonfinite |= !finite_bits(vp);
@@ -356,13 +381,13 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
     __shared__ double red[NTHR];
     double mx = 0.0;
     const double* Pu = P + (size_t)y * plane;
-    const size_t fs = (size_t)g.Q * plane;
+    const size_t fs = (size_t)sz.Q * plane;
     const double c2 = g.cfl2[y];
-    for (int i = threadIdx.x; i < g.pz * g.px; i += blockDim.x)
+    for (int i = threadIdx.x; i < sz.pz * sz.px; i += NTHR)
       mx = fmax(mx, fabs(Pu[i]) * g.cfl1 + fabs(Pu[fs + i]) * c2 + fabs(Pu[2 * fs + i]) * g.cfl3);
     red[threadIdx.x] = mx;
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    for (int w = NTHR / 2; w > 0; w >>= 1) {
       if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
       __syncthreads();
     }
@@ -603,29 +628,64 @@ template <bool MULTI>
 static void launch_inverse_build(const Grid& g, const PhysArgs& a, cudaStream_t st) {
   const dim3 grid(g.Q, a.ninst);
   const bool cfl = a.cfl_check != 0;
+  const size_t s2 = phys_tc_smem_bytes(g, cfl, 2), s1 = phys_tc_smem_bytes(g, cfl, 1);
+  using RT = InvSizesRT;
   switch (g.tcminb) {
-    case 3: k_phys_inverse_tc<MULTI, 3, 2, 256><<<grid, 256, phys_tc_smem_bytes(g, cfl, 2), st>>>(g, a); break;
-    case 4: k_phys_inverse_tc<MULTI, 4, 1, 128><<<grid, 128, phys_tc_smem_bytes(g, cfl, 1), st>>>(g, a); break;
-    case 5: k_phys_inverse_tc<MULTI, 5, 1, 128><<<grid, 128, phys_tc_smem_bytes(g, cfl, 1), st>>>(g, a); break;
-    default: k_phys_inverse_tc<MULTI, 2, 2, 256><<<grid, 256, phys_tc_smem_bytes(g, cfl, 2), st>>>(g, a); break;
+    case 3: k_phys_inverse_tc<MULTI, 3, 2, 256, RT><<<grid, 256, s2, st>>>(g, a); break;
+    case 4: k_phys_inverse_tc<MULTI, 4, 1, 128, RT><<<grid, 128, s1, st>>>(g, a); break;
+    case 5: k_phys_inverse_tc<MULTI, 5, 1, 128, RT><<<grid, 128, s1, st>>>(g, a); break;
+    default: k_phys_inverse_tc<MULTI, 2, 2, 256, RT><<<grid, 256, s2, st>>>(g, a); break;
   }
 }
 
+// the specialised builds (6: build 4, 7: build 2 with compile-time sizes)
+// for the grids 32x65x32 and 16x33x16 of a single-grid batch
+using InvCT32 = InvSizesCT<32, 16, 97>;
+using InvCT16 = InvSizesCT<16, 8, 49>;
+
+bool phys_tc_specialised(const Grid& g) { return sizes_match<InvCT32>(g) || sizes_match<InvCT16>(g); }
+
+template <class S>
+static void launch_inverse_ct(const Grid& g, const PhysArgs& a, cudaStream_t st) {
+  const dim3 grid(g.Q, a.ninst);
+  const bool cfl = a.cfl_check != 0;
+  if (g.tcminb == 6)
+    k_phys_inverse_tc<false, 4, 1, 128, S><<<grid, 128, phys_tc_smem_bytes(g, cfl, 1), st>>>(g, a);
+  else
+    k_phys_inverse_tc<false, 2, 2, 256, S><<<grid, 256, phys_tc_smem_bytes(g, cfl, 2), st>>>(g, a);
+}
+
 cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st) {
-  if (a.grids) launch_inverse_build<true>(g, a, st);
-  else launch_inverse_build<false>(g, a, st);
+  if (a.grids) {
+    Grid gr = g;
+    if (gr.tcminb > 5) gr.tcminb = gr.tcminb == 6 ? 4 : 2;
+    launch_inverse_build<true>(gr, a, st);
+  } else if (g.tcminb > 5 && sizes_match<InvCT32>(g)) {
+    launch_inverse_ct<InvCT32>(g, a, st);
+  } else if (g.tcminb > 5 && sizes_match<InvCT16>(g)) {
+    launch_inverse_ct<InvCT16>(g, a, st);
+  } else {
+    Grid gr = g;
+    if (gr.tcminb > 5) gr.tcminb = gr.tcminb == 6 ? 4 : 2;
+    launch_inverse_build<false>(gr, a, st);
+  }
   return cudaGetLastError();
 }
 
 void prepare_phys_tc(int optin) {
-  allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256>, optin);
-  allow_max_smem(k_phys_inverse_tc<true, 2, 2, 256>, optin);
-  allow_max_smem(k_phys_inverse_tc<false, 3, 2, 256>, optin);
-  allow_max_smem(k_phys_inverse_tc<true, 3, 2, 256>, optin);
-  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128>, optin);
-  allow_max_smem(k_phys_inverse_tc<true, 4, 1, 128>, optin);
-  allow_max_smem(k_phys_inverse_tc<false, 5, 1, 128>, optin);
-  allow_max_smem(k_phys_inverse_tc<true, 5, 1, 128>, optin);
+  using RT = InvSizesRT;
+  allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, RT>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 2, 2, 256, RT>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 3, 2, 256, RT>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 3, 2, 256, RT>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128, RT>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 4, 1, 128, RT>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 5, 1, 128, RT>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 5, 1, 128, RT>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128, InvCT32>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, InvCT32>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128, InvCT16>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, InvCT16>, optin);
   allow_max_smem(k_products_tc<false, kPB>, optin);
   allow_max_smem(k_products_tc<true, kPB>, optin);
   allow_max_smem(k_products_tc<false, 1>, optin);

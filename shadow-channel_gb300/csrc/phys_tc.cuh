@@ -14,7 +14,7 @@ static constexpr int kFB = 2;  // fields per pass of the mma.sync inverse (its w
 // kept kz modes of even / odd padded index zp (kk < Nz/2: zp = kk; else
 // zp = kk + 1 + Nz/2, which runs over the odd Nz + 1 ... 3Nz/2 - 1); an odd
 // pz keeps all modes in one class
-__host__ __device__ inline void z_class_counts(int Nz, int pz, int& nE, int& nO) {
+__host__ __device__ constexpr void z_class_counts(int Nz, int pz, int& nE, int& nO) {
   if (pz % 2) {
     nE = Nz - 1;
     nO = 0;
@@ -32,17 +32,18 @@ struct PhysTcDims {
   int MTz, MTx, KSz, KSx, NZ, NX;  // NZ = columns of the z stage, NX = of the x stage
 };
 
-// fb: fields per pass (the x stage has one column per (field, m))
-__host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g, int fb = kFB) {
-  PhysTcDims d;
-  d.Rz = g.pz % 2 ? 1 : 2;
-  d.Rx = g.px % 2 ? 1 : 2;
-  d.pzh = g.pz / d.Rz;
-  d.pxh = g.px / d.Rx;
-  int nzE, nzO;
-  z_class_counts(g.Nz, g.pz, nzE, nzO);
-  d.nxE = (g.X + d.Rx - 1) / d.Rx;
-  d.nxO = g.X - d.nxE;
+// from the sizes (a constant expression for compile-time sizes); fb: fields
+// per pass (the x stage has one column per (field, m))
+__host__ __device__ constexpr PhysTcDims phys_tc_dims_n(int Nz, int pz, int px, int X, int fb) {
+  PhysTcDims d{};
+  d.Rz = pz % 2 ? 1 : 2;
+  d.Rx = px % 2 ? 1 : 2;
+  d.pzh = pz / d.Rz;
+  d.pxh = px / d.Rx;
+  int nzE = 0, nzO = 0;
+  z_class_counts(Nz, pz, nzE, nzO);
+  d.nxE = (X + d.Rx - 1) / d.Rx;
+  d.nxO = X - d.nxE;
   d.KTzE = (2 * nzE + 15) / 16;
   d.KTz = d.KTzE + (2 * nzO + 15) / 16;
   d.KTxE = (2 * d.nxE + 15) / 16;
@@ -51,9 +52,13 @@ __host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g, int fb = kFB) 
   d.MTx = (d.pxh + 15) / 16;
   d.KSz = d.KTz * 16 + 8;
   d.KSx = d.KTx * 16 + 8;
-  d.NZ = fb * g.X;
-  d.NX = fb * g.pz;
+  d.NZ = fb * X;
+  d.NX = fb * pz;
   return d;
+}
+
+__host__ __device__ inline PhysTcDims phys_tc_dims(const Grid& g, int fb = kFB) {
+  return phys_tc_dims_n(g.Nz, g.pz, g.px, g.X, fb);
 }
 
 // the two stages' matrices (rows x K words of Re, Im) and the z stage's

@@ -5,7 +5,8 @@ CHN_SOLVE_TILE) changes which columns share a block, not any column's
 arithmetic.  The builds of the tensor-core inverse transform
 (CHN_INVERSE_BUILD: 2 = two fields per pass in 256-thread blocks at two
 blocks per SM, 3 = the same at three, 4 / 5 = one field per pass in
-128-thread blocks at four / five) change how the columns of a plane are
+128-thread blocks at four / five, 6 / 7 = builds 4 / 2 compiled for the
+sizes of 32x65x32 and 16x33x16) change how the columns of a plane are
 grouped, not the digit sums or their rounding.  Each variant runs the
 batched forward (primal + 3 tangents, one forced) and the coupled adjoint,
 and the single-trajectory primal, and must reproduce the default's outputs
@@ -24,7 +25,8 @@ from conftest import has_gpu
 
 pytestmark = pytest.mark.gpu
 
-GRIDS = [(32, 65, 32, 2 * np.pi, np.pi, 3300.0, 2.0, 0.005, 3), (48, 97, 48, 2 * np.pi, np.pi, 3300.0, 2.0, 0.004, 2)]
+GRIDS = [(32, 65, 32, 2 * np.pi, np.pi, 3300.0, 2.0, 0.005, 3), (48, 97, 48, 2 * np.pi, np.pi, 3300.0, 2.0, 0.004, 2),
+         (16, 33, 16, 2 * np.pi, np.pi, 2000.0, 2.0, 0.01, 3)]
 NSEG, NTAN = 2, 3
 KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_AUTOTUNE")
 
@@ -89,10 +91,10 @@ def test_solve_tiles_give_the_same_bits(cc, gi):
     _same(a, b)
 
 
-@pytest.mark.parametrize("build", ["3", "4", "5"])
-def test_inverse_builds_give_the_same_bits(cc, build):
-    a, _ = _sweeps(cc, GRIDS[0], {"CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
-    b, _ = _sweeps(cc, GRIDS[0], {"CHN_INVERSE_BUILD": build, "CHN_AUTOTUNE": "0"})
+@pytest.mark.parametrize("gi,build", [(0, "3"), (0, "4"), (0, "5"), (0, "6"), (0, "7"), (2, "4"), (2, "6"), (2, "7")])
+def test_inverse_builds_give_the_same_bits(cc, gi, build):
+    a, _ = _sweeps(cc, GRIDS[gi], {"CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
+    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_INVERSE_BUILD": build, "CHN_AUTOTUNE": "0"})
     _same(a, b)
 
 
@@ -103,7 +105,7 @@ def test_autotuner_reports_its_choices(cc):
     assert report["solve_chosen"] in ("tile16", "tile8")
     assert report["solve_tile16"] > 0 and report["solve_tile8"] > 0
     assert report["chosen"].startswith("tc_inverse_")
-    for b in ("f2_b2", "f2_b3", "f1_b4", "f1_b5"):
+    for b in ("f2_b2", "f2_b3", "f1_b4", "f1_b5", "f1_b4_fixed", "f2_b2_fixed"):
         assert report["tc_inverse_" + b] > 0
     ref, _ = _sweeps(cc, GRIDS[0], {"CHN_SOLVE_TILE": "16", "CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
     _same(res, ref)
