@@ -136,6 +136,9 @@ struct Grid {
   const uint32_t* tcFZ;
   const int* tcFZE;
   int tcf;
+  // kernels that run their build compiled for the grid's sizes (32x65x32,
+  // 16x33x16): FIXED_* bits of sizes.cuh (autotuned; the same results)
+  int fixed;
 };
 
 __host__ __device__ inline size_t coef_size(const Grid& g) { return (size_t)g.Nz * 2 * g.R * g.X; }

@@ -26,6 +26,7 @@
 #include "chn_common.cuh"
 #include "fft.cuh"
 #include "kernels.h"
+#include "sizes.cuh"
 #include "setup.h"
 
 namespace chn {
@@ -208,6 +209,9 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_fits(g, optin)) ? 1 : 0;
   // the inverse's build (phys_tc.cu) until the autotuner has timed them;
   // CHN_INVERSE_BUILD=2..5 fixes it (and skips that timing)
+  // the kernels' builds compiled for the grid's sizes (autotuned)
+  const char* fx = getenv("CHN_FIXED_SIZES");
+  g.fixed = (fx && fx[0] == '1') ? (FIXED_PRODUCTS | FIXED_RECON | FIXED_SOLVE) : 0;
   const char* ib = getenv("CHN_INVERSE_BUILD");
   g.tcminb = (ib && ib[0] >= '2' && ib[0] <= '7' && ib[1] == 0) ? ib[0] - '0' : 2;
   // the solve's block tile: 16 until the autotuner has timed both;
@@ -1232,6 +1236,107 @@ static bool autotune_solve(Engine& e, Work& w) {
   return true;
 }
 
+// autotuner, the builds compiled for the grid's sizes (sizes.cuh; the
+// same results): for the product kernels (one batched substage's tangent
+// and adjoint products), the reconstruction (tangents) and the implicit
+// solve (a tangent solve into scratch), each timed against its run-time-
+// size build and kept where faster (Grid::fixed).  CHN_FIXED_SIZES=0 / 1
+// fixes all three off / on.
+static bool autotune_fixed(Engine& e, Work& w) {
+  const char* off = getenv("CHN_AUTOTUNE");
+  const char* forced = getenv("CHN_FIXED_SIZES");
+  Grid& g = e.T.g;
+  if ((off && off[0] == '0') || (forced && forced[0]) || w.gdev || !phys_tc_specialised(g)) return true;
+  const int nt = w.nseg * (w.ntan > 0 ? w.ntan : 1);
+  ProdArgs f{};
+  f.Pp = cbd(w.Pp, w.psz);
+  f.pdiv = w.ntan > 0 ? w.ntan : 1;
+  f.Pt = cbd(w.Pt, w.psz);
+  f.H = mb(w.Ut, w.usz);
+  f.ninst = nt;
+  f.sdiv = 1;
+  f.tmp = w.Zt;
+  f.tmp_inst = w.zt_inst;
+  ProdArgs b = f;
+  b.pdiv = 1;
+  b.Pt = cbd(w.Pl, w.psz);
+  b.H = mb(w.Up, w.usz);
+  b.ninst = w.nseg;
+  ReconArgs r{};
+  r.ninst = nt;
+  r.C = cb(w.St, w.csz);
+  r.slot = noslot();
+  r.U = mb(w.Ut, w.usz);
+  r.sdiv = 1;
+  SolveArgs sa{};
+  sa.H = cb(w.Ut, w.usz);
+  sa.Hprev = cb(nullptr, 0);
+  sa.Cc = mb(w.io, w.csz);  // scratch: no state of the working set is touched
+  sa.Sout = mb(w.io, w.csz);
+  sa.T = mb(nullptr, 0);
+  sa.tdiv = 1;
+  sa.slot = noslot();
+  sa.k = 1;
+  sa.mean_mode = MEAN_TAN_HOMOG;
+  sa.mdiv = w.ntan > 0 ? w.ntan : 1;
+  sa.ninst = nt;
+  sa.sdiv = w.ntan > 0 ? w.ntan : 1;
+  struct Part {
+    int bit;
+    const char* name;
+    int launches;
+  };
+  const Part parts[3] = {{FIXED_PRODUCTS, "products", 2}, {FIXED_RECON, "recon", 1}, {FIXED_SOLVE, "solve", 1}};
+  auto enqueue = [&](int bit) -> bool {
+    if (bit == FIXED_PRODUCTS)
+      return launch_products_fwd(g, f, e.st) == cudaSuccess && launch_products_adj(g, b, e.st) == cudaSuccess;
+    if (bit == FIXED_RECON) return launch_recon(g, r, e.st) == cudaSuccess;
+    return launch_solve(g, sa, e.st) == cudaSuccess;
+  };
+  cudaEvent_t t0, t1;
+  CK(cudaEventCreate(&t0));
+  CK(cudaEventCreate(&t1));
+  const int saved = g.fixed;
+  bool ok = true;
+  std::string rep;
+  char buf[160];
+  for (const Part& pt : parts) {
+    float ms[2] = {0.f, 0.f};
+    for (int c = 0; c < 2 && ok; ++c) {
+      g.fixed = c ? (g.fixed | pt.bit) : (g.fixed & ~pt.bit);
+      ok = enqueue(pt.bit);  // warm-up
+      ok = ok && cudaEventRecord(t0, e.st) == cudaSuccess;
+      for (int k = 0; k < 3 && ok; ++k) ok = enqueue(pt.bit);
+      ok = ok && cudaEventRecord(t1, e.st) == cudaSuccess && cudaEventSynchronize(t1) == cudaSuccess;
+      if (ok) cudaEventElapsedTime(&ms[c], t0, t1);
+      ms[c] /= 3;
+    }
+    if (!ok) break;
+    g_launches += 8 * pt.launches;
+    g.fixed = ms[1] < ms[0] ? (g.fixed | pt.bit) : (g.fixed & ~pt.bit);
+    snprintf(buf, sizeof(buf), "\"%s_runtime_sizes\": %.4f, \"%s_fixed_sizes\": %.4f, \"%s_sizes\": \"%s\"", pt.name,
+             ms[0], pt.name, ms[1], pt.name, (g.fixed & pt.bit) ? "fixed" : "runtime");
+    if (!rep.empty()) rep += ", ";
+    rep += buf;
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (!ok) {
+    g.fixed = saved;
+    set_error(-1, "fixed-size autotuner: %s", cudaGetErrorString(cudaGetLastError()));
+    return false;
+  }
+  if (g_tune_report.size() > 1 && g_tune_report.back() == '}') {
+    g_tune_report.pop_back();
+    g_tune_report += ", ";
+  } else {
+    g_tune_report = "{";
+  }
+  g_tune_report += rep;
+  g_tune_report += "}";
+  return true;
+}
+
 static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
   NvtxRange nvtx_op("op_primal");
   const size_t csz = w.csz;
@@ -1950,7 +2055,8 @@ int c_batch_init_steps(int nseg, int ntan, int couple, int nsteps) {
   }
   e.have_batch = true;
   g_tune_report.clear();
-  if (!autotune_transforms(e, e.batch) || !autotune_solve(e, e.batch)) return g_status;
+  if (!autotune_transforms(e, e.batch) || !autotune_solve(e, e.batch) || !autotune_fixed(e, e.batch))
+    return g_status;
   g_status = 0;
   return 0;
 }
@@ -2336,7 +2442,8 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
   m->e.batch.gdev = m->gdev;
   m->e.have_batch = true;
   g_tune_report.clear();
-  if (!autotune_transforms(m->e, m->e.batch) || !autotune_solve(m->e, m->e.batch)) {
+  if (!autotune_transforms(m->e, m->e.batch) || !autotune_solve(m->e, m->e.batch) ||
+      !autotune_fixed(m->e, m->e.batch)) {
     const int rc = g_status ? g_status : -1;
     c_multi_destroy();
     return rc;

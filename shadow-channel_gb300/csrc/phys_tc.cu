@@ -24,6 +24,7 @@
 // CFL check and status bits as k_phys_inverse.
 #include <cmath>
 #include <cstdlib>
+#include <type_traits>
 #include <vector>
 
 #include "chn_common.cuh"
@@ -31,6 +32,7 @@
 #include "phys_common.cuh"
 #include "setup.h"
 #include "phys_tc.cuh"
+#include "sizes.cuh"
 #include "tc_common.cuh"
 
 namespace chn {
@@ -190,23 +192,6 @@ size_t phys_tc_smem_bytes(const Grid& g, bool with_cfl, int fb) {
 // kernel
 // ---------------------------------------------------------------------------
 
-// The sizes a kernel reads: from the grid at run time, or compile-time
-// constants for the grids with a specialised build (the same arithmetic;
-// the loops over known extents unroll and the index arithmetic folds).
-struct InvSizesRT {  // read from the grid where used (no register copies)
-  const int &Nz, &X, &pz, &px, &Q;
-  __device__ explicit InvSizesRT(const Grid& g) : Nz(g.Nz), X(g.X), pz(g.pz), px(g.px), Q(g.Q) {}
-};
-template <int NZ, int XX, int QQ>
-struct InvSizesCT {
-  static constexpr int Nz = NZ, X = XX, pz = 3 * NZ / 2, px = 3 * XX, Q = QQ;
-  __device__ explicit InvSizesCT(const Grid&) {}
-};
-template <class S>
-__host__ __device__ inline bool sizes_match(const Grid& g) {
-  return g.Nz == S::Nz && g.X == S::X && g.pz == S::pz && g.px == S::px && g.Q == S::Q;
-}
-
 __host__ __device__ constexpr size_t phys_tc_dbuf_of(const PhysTcDims& d) {
   return (size_t)kDig * ((d.NZ + 7) / 8 * 8) * d.KSz * 2 > (size_t)kDig * ((d.NX + 7) / 8 * 8) * d.KSx * 2
              ? (size_t)kDig * ((d.NZ + 7) / 8 * 8) * d.KSz * 2
@@ -214,15 +199,15 @@ __host__ __device__ constexpr size_t phys_tc_dbuf_of(const PhysTcDims& d) {
 }
 
 // FB fields per pass, NTHR threads, MINB blocks per SM (the register
-// budget), S the sizes (InvSizesRT, or InvSizesCT for a specialised grid)
+// budget), S the sizes (SizesRT, or SizesCT for a specialised grid)
 template <bool MULTI, int MINB, int FB, int NTHR, class S>
 __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_constant__ Grid g0, PhysArgs a) {
   const int inst = blockIdx.y, y = blockIdx.x;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
-  const S sz(g);
-  if (y >= sz.Q) return;
+  const S gsz(g);
+  if (y >= gsz.Q()) return;
   if (a.skip_blocked && blocked(a.status, a.sdiv, inst)) return;
-  const PhysTcDims d = phys_tc_dims_n(sz.Nz, sz.pz, sz.px, sz.X, FB);
+  const PhysTcDims d = phys_tc_dims_n(gsz.Nz(), gsz.pz(), gsz.px(), gsz.X(), FB);
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* p = smem;
   int* exz = reinterpret_cast<int*>(p); p += (size_t)((d.NZ + 3) / 4 * 4) * sizeof(int);
@@ -233,12 +218,12 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
   const cpx* __restrict__ U = a.U.at(inst);
   double* __restrict__ P = a.P.at(inst);
   if (a.pslot.stride) P += (long long)a.pslot.slot() * a.pslot.stride;
-  const size_t plane = (size_t)sz.pz * sz.px;
+  const size_t plane = (size_t)gsz.pz() * gsz.px();
   const uint4* __restrict__ Az = reinterpret_cast<const uint4*>(g.tcZ);
   const uint4* __restrict__ Ax = reinterpret_cast<const uint4*>(g.tcX);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
   constexpr int nwarp = NTHR >> 5;
-  const int Kk = sz.Nz - 1;  // kept kz rows
+  const int Kk = gsz.Nz() - 1;  // kept kz rows
   bool nonfinite = false;
   for (int i = threadIdx.x; i < d.NZ; i += NTHR) exz[i] = 0;
   __syncthreads();
@@ -252,13 +237,13 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
     cpx* Fin = Zb;  // [n][kk]
     for (int i = threadIdx.x; i < d.NX; i += NTHR) exx[i] = 0;
     {
-      const int ncol = nfb * sz.X, per = NTHR / ncol;
+      const int ncol = nfb * gsz.X(), per = NTHR / ncol;
       if ((int)threadIdx.x < per * ncol) {
-        const int n = threadIdx.x % ncol, fl = n / sz.X, x = n - fl * sz.X;
+        const int n = threadIdx.x % ncol, fl = n / gsz.X(), x = n - fl * gsz.X();
         int emax = 0;
         for (int kk = threadIdx.x / ncol; kk < Kk; kk += per) {
-          const int z = kk < sz.Nz / 2 ? kk : kk + 1;
-          const cpx v = field_value_qx(g, sz.Q, sz.X, U, f0 + fl, z, y, x);
+          const int z = kk < gsz.Nz() / 2 ? kk : kk + 1;
+          const cpx v = field_value_qx(g, gsz.Q(), gsz.X(), U, f0 + fl, z, y, x);
           Fin[(size_t)n * Kk + kk] = v;
           emax = max(emax, max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
                                (int)((__double_as_longlong(v.im) >> 52) & 0x7FF)));
@@ -277,7 +262,7 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
         const int n = rc.r, w = rc.c;
         const int kk = g.tcZM[w];
         cpx v = {0.0, 0.0};
-        if (kk >= 0 && n < nfb * sz.X) v = Fin[n * Kk + kk];
+        if (kk >= 0 && n < nfb * gsz.X()) v = Fin[n * Kk + kk];
         const int ex = exz[n] - 1022;
         digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSz) / 2 + w, zstride);
       }
@@ -287,7 +272,7 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
       // rows Re Z[m], Im Z[m] for m < pzh; E + O -> Z[m], E - O -> Z[m + pzh];
       // the exponent of each value into its x-stage column (fl, m) (not the
       // imaginary part of the kx = 0 bin, which c2r ignores)
-      const int NT = (nfb * sz.X + 7) / 8;
+      const int NT = (nfb * gsz.X() + 7) / 8;
       const size_t dstride = (size_t)((d.NZ + 7) / 8 * 8) * d.KSz;  // bf16 between digits
       for (int item = warp; item < d.MTz * NT; item += nwarp) {
         const int mt = item / NT, nt = item - mt * NT;
@@ -298,26 +283,26 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int row = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
-          if (row >= 2 * d.pzh || col >= nfb * sz.X) continue;
+          if (row >= 2 * d.pzh || col >= nfb * gsz.X()) continue;
           const int e = g.tcZE[row] + exz[col] - 1022 - 64;
           const bool im = row >= d.pzh;
           const int m = im ? row - d.pzh : row;
           int fl = 0, x = col;  // col = fl X + x, fl < FB
-          while (x >= sz.X) { x -= sz.X; ++fl; }
+          while (x >= gsz.X()) { x -= gsz.X(); ++fl; }
           const bool counts = !(im && x == 0);
           const double vp = round_col(HE[r] + HO[r], LE[r] + LO[r], e, exz[col]);
-          cpx& zp = Zb[((size_t)fl * sz.pz + m) * sz.X + x];
+          cpx& zp = Zb[((size_t)fl * gsz.pz() + m) * gsz.X() + x];
           if (im) zp.im = vp;
           else zp.re = vp;
           const int ep = (int)((__double_as_longlong(vp) >> 52) & 0x7FF);
-          if (counts && ep) atomicMax(&exx[fl * sz.pz + m], ep);
+          if (counts && ep) atomicMax(&exx[fl * gsz.pz() + m], ep);
           if (d.Rz == 2) {
             const double vm = round_col(HE[r] - HO[r], LE[r] - LO[r], e, exz[col]);
-            cpx& zm = Zb[((size_t)fl * sz.pz + m + d.pzh) * sz.X + x];
+            cpx& zm = Zb[((size_t)fl * gsz.pz() + m + d.pzh) * gsz.X() + x];
             if (im) zm.im = vm;
             else zm.re = vm;
             const int em = (int)((__double_as_longlong(vm) >> 52) & 0x7FF);
-            if (counts && em) atomicMax(&exx[fl * sz.pz + m + d.pzh], em);
+            if (counts && em) atomicMax(&exx[fl * gsz.pz() + m + d.pzh], em);
           }
         }
       }
@@ -326,7 +311,7 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
     // ---- x stage, both fields: columns n = fl * pz + m, K words: Re, Im of
     // Z[m][j] for the even j, then the odd j (Im of j = 0 unused).  The z
     // stage's column exponents are cleared for the next pass.
-    const int ncx = nfb * sz.pz;
+    const int ncx = nfb * gsz.pz();
     const size_t xstride = (size_t)((d.NX + 7) / 8 * 8) * d.KSx;
     for (int i = threadIdx.x; i < d.NZ; i += NTHR) exz[i] = 0;
     {
@@ -337,7 +322,7 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
         const int n = rc.r, w = rc.c;
         const int j = w < WE ? (w < d.nxE ? d.Rx * w : -1) : (w - WE < d.nxO ? 2 * (w - WE) + 1 : -1);
         cpx v = {0.0, 0.0};
-        if (j >= 0 && n < ncx) v = Zb[(size_t)n * sz.X + j];
+        if (j >= 0 && n < ncx) v = Zb[(size_t)n * gsz.X() + j];
         if (j == 0) v.im = 0.0;
         const int ex = exx[min(n, ncx - 1)] - 1022;
         digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSx) / 2 + w, xstride / 2);
@@ -358,9 +343,9 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
           const int xp = mt * 16 + gq + 8 * (r >> 1), col = nt * 8 + 2 * t + (r & 1);
           if (xp >= d.pxh || col >= ncx) continue;
           int fl = 0, m = col;  // col = fl pz + m, fl < FB
-          while (m >= sz.pz) { m -= sz.pz; ++fl; }
+          while (m >= gsz.pz()) { m -= gsz.pz(); ++fl; }
           const int e = g.tcXE[xp] + exx[col] - 1022 - 64;
-          double* Pr = P + ((size_t)(f0 + fl) * sz.Q + y) * plane + (size_t)m * sz.px;
+          double* Pr = P + ((size_t)(f0 + fl) * gsz.Q() + y) * plane + (size_t)m * gsz.px();
           const double vp = round_col(HE[r] + HO[r], LE[r] + LO[r], e, exx[col]);
           Pr[xp] = vp;
           nonfinite |= !finite_bits(vp);
@@ -381,9 +366,9 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
     __shared__ double red[NTHR];
     double mx = 0.0;
     const double* Pu = P + (size_t)y * plane;
-    const size_t fs = (size_t)sz.Q * plane;
+    const size_t fs = (size_t)gsz.Q() * plane;
     const double c2 = g.cfl2[y];
-    for (int i = threadIdx.x; i < sz.pz * sz.px; i += NTHR)
+    for (int i = threadIdx.x; i < gsz.pz() * gsz.px(); i += NTHR)
       mx = fmax(mx, fabs(Pu[i]) * g.cfl1 + fabs(Pu[fs + i]) * c2 + fabs(Pu[2 * fs + i]) * g.cfl3);
     red[threadIdx.x] = mx;
     __syncthreads();
@@ -411,19 +396,21 @@ struct FwdTcDims {
   int KTx, KTz, MTx, MTz, KSx, KSz, pzp, Xp, Kk;
 };
 
-__host__ __device__ inline FwdTcDims fwd_tc_dims(const Grid& g) {
-  FwdTcDims d;
-  d.Kk = g.Nz - 1;
-  d.KTx = (g.px + 15) / 16;
-  d.KTz = (2 * g.pz + 15) / 16;
-  d.MTx = (2 * g.X + 15) / 16;
+__host__ __device__ constexpr FwdTcDims fwd_tc_dims_n(int Nz, int X, int pz, int px) {
+  FwdTcDims d{};
+  d.Kk = Nz - 1;
+  d.KTx = (px + 15) / 16;
+  d.KTz = (2 * pz + 15) / 16;
+  d.MTx = (2 * X + 15) / 16;
   d.MTz = (2 * d.Kk + 15) / 16;
   d.KSx = d.KTx * 16 + 8;
   d.KSz = d.KTz * 16 + 8;
-  d.pzp = (g.pz + 7) / 8 * 8;
-  d.Xp = (g.X + 7) / 8 * 8;
+  d.pzp = (pz + 7) / 8 * 8;
+  d.Xp = (X + 7) / 8 * 8;
   return d;
 }
+
+__host__ __device__ inline FwdTcDims fwd_tc_dims(const Grid& g) { return fwd_tc_dims_n(g.Nz, g.X, g.pz, g.px); }
 
 // pb product planes per pass: kPB for the forward modes (0, 1), one for the
 // adjoint modes (2, 3), whose six transforms per plane run faster with the
@@ -450,27 +437,29 @@ size_t fwd_tc_smem_bytes(const Grid& g, int pb) {
 // modes 0/1 write H slots 0..2, modes 2/3 fold each component into the
 // output slots (assemble_stage).  Same outputs as k_products_fwd /
 // k_products_adj.
-template <bool MULTI, int PB>
+// S: the sizes (SizesRT, or SizesCT for a specialised grid)
+template <bool MULTI, int PB, class S>
 __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_constant__ Grid g0, ProdArgs a, int mode) {
   const int inst = blockIdx.y, y = blockIdx.x;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
-  if (y >= g.Q) return;
+  const S gsz(g);
+  if (y >= gsz.Q()) return;
   if (blocked(a.status, a.sdiv, inst)) return;
-  const FwdTcDims d = fwd_tc_dims(g);
+  const FwdTcDims d = fwd_tc_dims_n(gsz.Nz(), gsz.X(), gsz.pz(), gsz.px());
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* p = smem;
-  const int exs = (g.pz + 3) / 4 * 4, pb = PB;
+  const int exs = (gsz.pz() + 3) / 4 * 4, pb = PB;
   int* exx3 = reinterpret_cast<int*>(p); p += (size_t)pb * exs * sizeof(int);  // [c][zp]
-  int* exz = reinterpret_cast<int*>(p); p += (size_t)((g.X + 3) / 4 * 4) * sizeof(int);
+  int* exz = reinterpret_cast<int*>(p); p += (size_t)((gsz.X() + 3) / 4 * 4) * sizeof(int);
   uint16_t* dig = reinterpret_cast<uint16_t*>(p);
   {
     const size_t dx = (size_t)kDig * d.pzp * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
     p += ((dx > dz ? dx : dz) + 15) / 16 * 16;
   }
   double* stage3 = reinterpret_cast<double*>(p);  // [c][zp][xp] products; Y [zp][kx] (cpx) over plane c
-  p += ((size_t)pb * g.pz * g.px * sizeof(double) + 15) / 16 * 16;
+  p += ((size_t)pb * gsz.pz() * gsz.px() * sizeof(double) + 15) / 16 * 16;
   cpx* Fb = reinterpret_cast<cpx*>(p);  // [kk][kx]
-  const size_t plane = (size_t)g.pz * g.px, fs = (size_t)g.Q * plane;
+  const size_t plane = (size_t)gsz.pz() * gsz.px(), fs = (size_t)gsz.Q() * plane;
   const double* __restrict__ Pp = a.Pp.base + (long long)(inst / a.pdiv) * a.Pp.stride + (size_t)y * plane +
                                   (a.pslot.stride ? (long long)a.pslot.slot() * a.pslot.stride : 0LL);
   const double* __restrict__ Pt = a.Pt.base ? a.Pt.at(inst) + (size_t)y * plane : nullptr;
@@ -480,7 +469,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
   const int* __restrict__ AxE = mode == 3 ? g.tcFXUE : g.tcFXE;
   const uint4* __restrict__ Az = reinterpret_cast<const uint4*>(g.tcFZ);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
-  const int nwarp = blockDim.x >> 5;
+  constexpr int nwarp = kThreads >> 5;
   const int ncomp = mode >= 2 ? 6 : 3;
   const size_t xstride = (size_t)d.pzp * d.KSx, zstride = (size_t)d.Xp * d.KSz;  // bf16 between digits
   for (int q = 0; q < ncomp; ++q) {
@@ -491,11 +480,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
     if (c == 0) {
       // ---- products of components q .. q+2 (each field loaded once per
       // point), row exponents (one column per zp)
-      for (int i = threadIdx.x; i < pb * exs; i += blockDim.x) exx3[i] = 0;
+      for (int i = threadIdx.x; i < pb * exs; i += kThreads) exx3[i] = 0;
       __syncthreads();
       const int nc = min(pb, ncomp - q);
-      FlatRC rc(threadIdx.x, blockDim.x, g.px);
-      for (int i = threadIdx.x; i < g.pz * g.px; i += blockDim.x, rc.next()) {
+      FlatRC rc(threadIdx.x, kThreads, gsz.px());
+      auto point = [&](int i) {
         double v[PB];
 #pragma unroll
         for (int cc = 0; cc < PB; ++cc) v[cc] = cc < nc ? split_product(mode, Pp, Pt, fs, i, q + cc) : 0.0;
@@ -507,14 +496,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
           const int e = (int)((__double_as_longlong(v[cc]) >> 52) & 0x7FF);
           if (e) atomicMax(&exx3[cc * exs + row], e);
         }
+      };
+      if constexpr (std::is_same<S, SizesRT>::value) {
+        for (int i = threadIdx.x; i < gsz.pz() * gsz.px(); i += kThreads, rc.next()) point(i);
+      } else {
+#pragma unroll 3
+        for (int i = threadIdx.x; i < gsz.pz() * gsz.px(); i += kThreads, rc.next()) point(i);
       }
       __syncthreads();
     }
-    FlatRC rcx(threadIdx.x, blockDim.x, d.KTx * 16);
-    for (int i = threadIdx.x; i < d.pzp * (d.KTx * 16); i += blockDim.x, rcx.next()) {
+    FlatRC rcx(threadIdx.x, kThreads, d.KTx * 16);
+    for (int i = threadIdx.x; i < d.pzp * (d.KTx * 16); i += kThreads, rcx.next()) {
       const int n = rcx.r, k = rcx.c;
-      const double v = (n < g.pz && k < g.px) ? stage[(size_t)n * g.px + k] : 0.0;
-      digits_bf16(scaled56(v, exx[min(n, g.pz - 1)] - 1022), dig + (size_t)n * d.KSx + k, xstride);
+      const double v = (n < gsz.pz() && k < gsz.px()) ? stage[(size_t)n * gsz.px() + k] : 0.0;
+      digits_bf16(scaled56(v, exx[min(n, gsz.pz() - 1)] - 1022), dig + (size_t)n * d.KSx + k, xstride);
     }
     __syncthreads();
     // ---- x stage: rows 2kx (+1), columns zp; Y into the staging region
@@ -527,9 +522,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int row = mt * 16 + gq + 8 * (r >> 1), zp = nt * 8 + 2 * t + (r & 1);
-          if (row >= 2 * g.X || zp >= g.pz) continue;
+          if (row >= 2 * gsz.X() || zp >= gsz.pz()) continue;
           const double v = round_col(Hh[r], Ll[r], AxE[row] + exx[zp] - 1022 - 64, exx[zp]);
-          cpx& yv = Yb[(size_t)zp * g.X + (row >> 1)];
+          cpx& yv = Yb[(size_t)zp * gsz.X() + (row >> 1)];
           if (row & 1) yv.im = v;
           else yv.re = v;
         }
@@ -537,11 +532,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
     }
     __syncthreads();
     // ---- z stage inputs: columns kx, K = 2 pz (Re, Im of Y[zp][kx] interleaved)
-    for (int i = threadIdx.x; i < g.X; i += blockDim.x) exz[i] = 0;
+    for (int i = threadIdx.x; i < gsz.X(); i += kThreads) exz[i] = 0;
     __syncthreads();
     {
-      FlatRC rc(threadIdx.x, blockDim.x, g.X);
-      for (int i = threadIdx.x; i < g.pz * g.X; i += blockDim.x, rc.next()) {
+      FlatRC rc(threadIdx.x, kThreads, gsz.X());
+      for (int i = threadIdx.x; i < gsz.pz() * gsz.X(); i += kThreads, rc.next()) {
         const cpx v = Yb[i];
         const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
                           (int)((__double_as_longlong(v.im) >> 52) & 0x7FF));
@@ -551,11 +546,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
     __syncthreads();
     {
       uint32_t* dw = reinterpret_cast<uint32_t*>(dig);
-      FlatRC rc(threadIdx.x, blockDim.x, d.KTz * 8);
-      for (int i = threadIdx.x; i < d.Xp * (d.KTz * 8); i += blockDim.x, rc.next()) {
+      FlatRC rc(threadIdx.x, kThreads, d.KTz * 8);
+      for (int i = threadIdx.x; i < d.Xp * (d.KTz * 8); i += kThreads, rc.next()) {
         const int n = rc.r, zp = rc.c;
-        const cpx v = (n < g.X && zp < g.pz) ? Yb[(size_t)zp * g.X + n] : cpx{0.0, 0.0};
-        const int ex = exz[min(n, g.X - 1)] - 1022;
+        const cpx v = (n < gsz.X() && zp < gsz.pz()) ? Yb[(size_t)zp * gsz.X() + n] : cpx{0.0, 0.0};
+        const int ex = exz[min(n, gsz.X() - 1)] - 1022;
         digits_pair_bf16(scaled56(v.re, ex), scaled56(v.im, ex), dw + ((size_t)n * d.KSz) / 2 + zp, zstride / 2);
       }
     }
@@ -570,9 +565,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int row = mt * 16 + gq + 8 * (r >> 1), kx = nt * 8 + 2 * t + (r & 1);
-          if (row >= 2 * d.Kk || kx >= g.X) continue;
+          if (row >= 2 * d.Kk || kx >= gsz.X()) continue;
           const double v = round_col(Hh[r], Ll[r], g.tcFZE[row] + exz[kx] - 1022 - 64, exz[kx]);
-          cpx& fv = Fb[(size_t)(row >> 1) * g.X + kx];
+          cpx& fv = Fb[(size_t)(row >> 1) * gsz.X() + kx];
           if (row & 1) fv.im = v;
           else fv.re = v;
         }
@@ -580,11 +575,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
     }
     __syncthreads();
     // ---- outputs (the (kk, kx) -> thread map is the same for every q)
-    FlatRC rco(threadIdx.x, blockDim.x, g.X);
-    for (int i = threadIdx.x; i < d.Kk * g.X; i += blockDim.x, rco.next()) {
+    FlatRC rco(threadIdx.x, kThreads, gsz.X());
+    for (int i = threadIdx.x; i < d.Kk * gsz.X(); i += kThreads, rco.next()) {
       const int kk = rco.r, x = rco.c;
-      const int z = kk < g.Nz / 2 ? kk : kk + 1;
-      if (mode < 2) H[(((size_t)z * 5 + q) * g.Q + y) * g.X + x] = Fb[i];
+      const int z = kk < gsz.Nz() / 2 ? kk : kk + 1;
+      if (mode < 2) H[(((size_t)z * 5 + q) * gsz.Q() + y) * gsz.X() + x] = Fb[i];
       else assemble_stage(g, mode == 3, H, z, y, x, q, Fb[i]);
     }
     __syncthreads();
@@ -599,16 +594,27 @@ bool fwd_tc_fits(const Grid& g, int optin) {
   return 2 * (fwd_tc_smem_bytes(g, kPB) + 4096) <= (size_t)optin + 4096;
 }
 
-cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
+template <class S>
+static void launch_products_sizes(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
   const size_t sm = fwd_tc_smem_bytes(g, products_per_pass(mode));
   const dim3 grid(g.Q, a.ninst);
+  constexpr bool M = std::is_same<S, SizesRT>::value;  // only the run-time sizes serve uneven batches
   if (products_per_pass(mode) == kPB) {
-    if (a.grids) k_products_tc<true, kPB><<<grid, kThreads, sm, st>>>(g, a, mode);
-    else k_products_tc<false, kPB><<<grid, kThreads, sm, st>>>(g, a, mode);
+    if (M && a.grids) k_products_tc<true, kPB, SizesRT><<<grid, kThreads, sm, st>>>(g, a, mode);
+    else k_products_tc<false, kPB, S><<<grid, kThreads, sm, st>>>(g, a, mode);
   } else {
-    if (a.grids) k_products_tc<true, 1><<<grid, kThreads, sm, st>>>(g, a, mode);
-    else k_products_tc<false, 1><<<grid, kThreads, sm, st>>>(g, a, mode);
+    if (M && a.grids) k_products_tc<true, 1, SizesRT><<<grid, kThreads, sm, st>>>(g, a, mode);
+    else k_products_tc<false, 1, S><<<grid, kThreads, sm, st>>>(g, a, mode);
   }
+}
+
+// Grid::fixed & FIXED_PRODUCTS: the build compiled for the grid's sizes
+// (32x65x32, 16x33x16; single-grid batches), else the run-time sizes
+cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
+  const bool fx = (g.fixed & FIXED_PRODUCTS) && !a.grids;
+  if (fx && sizes_match<Sizes32>(g)) launch_products_sizes<Sizes32>(g, a, mode, st);
+  else if (fx && sizes_match<Sizes16>(g)) launch_products_sizes<Sizes16>(g, a, mode, st);
+  else launch_products_sizes<SizesRT>(g, a, mode, st);
   return cudaGetLastError();
 }
 
@@ -629,7 +635,7 @@ static void launch_inverse_build(const Grid& g, const PhysArgs& a, cudaStream_t 
   const dim3 grid(g.Q, a.ninst);
   const bool cfl = a.cfl_check != 0;
   const size_t s2 = phys_tc_smem_bytes(g, cfl, 2), s1 = phys_tc_smem_bytes(g, cfl, 1);
-  using RT = InvSizesRT;
+  using RT = SizesRT;
   switch (g.tcminb) {
     case 3: k_phys_inverse_tc<MULTI, 3, 2, 256, RT><<<grid, 256, s2, st>>>(g, a); break;
     case 4: k_phys_inverse_tc<MULTI, 4, 1, 128, RT><<<grid, 128, s1, st>>>(g, a); break;
@@ -638,12 +644,10 @@ static void launch_inverse_build(const Grid& g, const PhysArgs& a, cudaStream_t 
   }
 }
 
-// the specialised builds (6: build 4, 7: build 2 with compile-time sizes)
-// for the grids 32x65x32 and 16x33x16 of a single-grid batch
-using InvCT32 = InvSizesCT<32, 16, 97>;
-using InvCT16 = InvSizesCT<16, 8, 49>;
+// the specialised inverse builds (6: build 4, 7: build 2 with compile-time
+// sizes) for the grids of a single-grid batch with Sizes32 / Sizes16 sizes
 
-bool phys_tc_specialised(const Grid& g) { return sizes_match<InvCT32>(g) || sizes_match<InvCT16>(g); }
+bool phys_tc_specialised(const Grid& g) { return sizes_match<Sizes32>(g) || sizes_match<Sizes16>(g); }
 
 template <class S>
 static void launch_inverse_ct(const Grid& g, const PhysArgs& a, cudaStream_t st) {
@@ -660,10 +664,10 @@ cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_
     Grid gr = g;
     if (gr.tcminb > 5) gr.tcminb = gr.tcminb == 6 ? 4 : 2;
     launch_inverse_build<true>(gr, a, st);
-  } else if (g.tcminb > 5 && sizes_match<InvCT32>(g)) {
-    launch_inverse_ct<InvCT32>(g, a, st);
-  } else if (g.tcminb > 5 && sizes_match<InvCT16>(g)) {
-    launch_inverse_ct<InvCT16>(g, a, st);
+  } else if (g.tcminb > 5 && sizes_match<Sizes32>(g)) {
+    launch_inverse_ct<Sizes32>(g, a, st);
+  } else if (g.tcminb > 5 && sizes_match<Sizes16>(g)) {
+    launch_inverse_ct<Sizes16>(g, a, st);
   } else {
     Grid gr = g;
     if (gr.tcminb > 5) gr.tcminb = gr.tcminb == 6 ? 4 : 2;
@@ -673,7 +677,7 @@ cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_
 }
 
 void prepare_phys_tc(int optin) {
-  using RT = InvSizesRT;
+  using RT = SizesRT;
   allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, RT>, optin);
   allow_max_smem(k_phys_inverse_tc<true, 2, 2, 256, RT>, optin);
   allow_max_smem(k_phys_inverse_tc<false, 3, 2, 256, RT>, optin);
@@ -682,14 +686,18 @@ void prepare_phys_tc(int optin) {
   allow_max_smem(k_phys_inverse_tc<true, 4, 1, 128, RT>, optin);
   allow_max_smem(k_phys_inverse_tc<false, 5, 1, 128, RT>, optin);
   allow_max_smem(k_phys_inverse_tc<true, 5, 1, 128, RT>, optin);
-  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128, InvCT32>, optin);
-  allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, InvCT32>, optin);
-  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128, InvCT16>, optin);
-  allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, InvCT16>, optin);
-  allow_max_smem(k_products_tc<false, kPB>, optin);
-  allow_max_smem(k_products_tc<true, kPB>, optin);
-  allow_max_smem(k_products_tc<false, 1>, optin);
-  allow_max_smem(k_products_tc<true, 1>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128, Sizes32>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, Sizes32>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128, Sizes16>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, Sizes16>, optin);
+  allow_max_smem(k_products_tc<false, kPB, RT>, optin);
+  allow_max_smem(k_products_tc<true, kPB, RT>, optin);
+  allow_max_smem(k_products_tc<false, 1, RT>, optin);
+  allow_max_smem(k_products_tc<true, 1, RT>, optin);
+  allow_max_smem(k_products_tc<false, kPB, Sizes32>, optin);
+  allow_max_smem(k_products_tc<false, 1, Sizes32>, optin);
+  allow_max_smem(k_products_tc<false, kPB, Sizes16>, optin);
+  allow_max_smem(k_products_tc<false, 1, Sizes16>, optin);
 }
 
 }  // namespace chn

@@ -16,6 +16,7 @@
 #include "chn_common.cuh"
 #include "kernels.h"
 #include "solve_common.cuh"
+#include "sizes.cuh"
 #include "tc_common.cuh"
 
 namespace chn {
@@ -386,23 +387,23 @@ __device__ void quad_rhs(const Grid& g, const cpx* __restrict__ H, int z, int x0
 // of the FP64 version's parity-combined inputs), times the digit tables of
 // the weighted transposes; one FP64 rounding per contraction.
 //   Fa = Qpw P - K2 Qw Hy [+ Qppw Sa],   Fb = Rw G [+ Rpw Sb]
-template <int kTile>
-__device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int x0, int nx, bool adj,
+template <int kTile, class S>
+__device__ void quad_rhs_tc(const Grid& g, const S& gsz, const cpx* __restrict__ H, int z, int x0, int nx, bool adj,
                             SolveSmem& s) {
   constexpr int NC = 2 * kTile;  // digit columns: Re, Im of each kx column
-  const int KT = (g.Q + 15) / 16, MTw = (g.R + 15) / 16;
-  const size_t KS = solve_tc_kstride(g);
+  const int KT = (gsz.Q() + 15) / 16, MTw = (gsz.R() + 15) / 16;
+  const size_t KS = (size_t)((gsz.Q() + 15) / 16) * 16 + 8;  // solve_tc_kstride
   uint16_t* dig = reinterpret_cast<uint16_t*>(s.hc);             // [7][NC][KS]
   int* exc = reinterpret_cast<int*>(dig + (size_t)kDig * NC * KS);  // [kTile]
   const double kz = g.Kz[z];
-  const size_t cs = (size_t)g.Q * g.X;
+  const size_t cs = (size_t)gsz.Q() * gsz.X();
   const cpx* Hz_ = H + (size_t)z * 5 * cs;  // slot c at Hz_ + c*cs + y*X + x
   // input q: 0 P = i(kx Hx + kz Hz), 1 Hy, 2 Sa = -i(kz Sx - kx Sz), 3 G = i(kz Hx - kx Hz),
   // 4 Sb = i(kz Sz + kx Sx); weight table: Qpw 1, Qw 0, Qppw 2, Rw 3, Rpw 4
   auto input = [&](int q, int y, int col) -> cpx {
     const int x = x0 + col;
     const double kx = g.Kx[x];
-    const cpx* b = Hz_ + (size_t)y * g.X + x;
+    const cpx* b = Hz_ + (size_t)y * gsz.X() + x;
     switch (q) {
       case 0: { const cpx hx = b[cs], hz = b[0];
                 return cpx{-kx * hx.im - kz * hz.im, kx * hx.re + kz * hz.re}; }
@@ -424,12 +425,12 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
     const int q = adj ? iq : qs[iq];
     const int w = q == 0 ? 1 : (q == 1 ? 0 : q);
     const bool toA = q < 3;
-    const int N = toA ? g.D : g.R;
+    const int N = toA ? gsz.D() : gsz.R();
     cpx* F = toA ? s.Fa : s.Fb;
     const bool first = (q == 0 || q == 3);
-    for (int i = threadIdx.x; i < kTile; i += blockDim.x) exc[i] = 0;
+    for (int i = threadIdx.x; i < kTile; i += kThreads) exc[i] = 0;
     __syncthreads();
-    if (KT <= kQuadRegs && blockDim.x == 16 * kTile) {
+    if (KT <= kQuadRegs && kThreads == 16 * kTile) {
       // thread t holds column t % kTile, planes t / kTile + 16 k (k < KT):
       // its inputs stay in registers from the exponent maximum to the digits
       const int col = threadIdx.x % kTile, y0 = threadIdx.x / kTile;
@@ -438,7 +439,7 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
 #pragma unroll
       for (int k = 0; k < kQuadRegs; ++k) {
         const int y = y0 + 16 * k;
-        vin[k] = (k < KT && y < g.Q && col < nx) ? input(q, y, col) : cpx{0.0, 0.0};
+        vin[k] = (k < KT && y < gsz.Q() && col < nx) ? input(q, y, col) : cpx{0.0, 0.0};
         emax = max(emax, max((int)((__double_as_longlong(vin[k].re) >> 52) & 0x7FF),
                              (int)((__double_as_longlong(vin[k].im) >> 52) & 0x7FF)));
       }
@@ -453,7 +454,7 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
         digits_bf16(scaled56(vin[k].im, ex), dig + (size_t)(2 * col + 1) * KS + y, NC * KS);
       }
     } else {
-      for (int i = threadIdx.x; i < g.Q * kTile; i += blockDim.x) {
+      for (int i = threadIdx.x; i < gsz.Q() * kTile; i += kThreads) {
         const int y = i / kTile, col = i - y * kTile;
         if (col >= nx) continue;
         const cpx v = input(q, y, col);
@@ -462,9 +463,9 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
         if (e) atomicMax(&exc[col], e);
       }
       __syncthreads();
-      for (int i = threadIdx.x; i < KT * 16 * kTile; i += blockDim.x) {
+      for (int i = threadIdx.x; i < KT * 16 * kTile; i += kThreads) {
         const int y = i / kTile, col = i - y * kTile;
-        const cpx v = (y < g.Q && col < nx) ? input(q, y, col) : cpx{0.0, 0.0};
+        const cpx v = (y < gsz.Q() && col < nx) ? input(q, y, col) : cpx{0.0, 0.0};
         const int ex = exc[col] - 1022;
         digits_bf16(scaled56(v.re, ex), dig + (size_t)(2 * col) * KS + y, NC * KS);
         digits_bf16(scaled56(v.im, ex), dig + (size_t)(2 * col + 1) * KS + y, NC * KS);
@@ -472,7 +473,7 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
     }
     __syncthreads();
     const int MTn = (N + 15) / 16;
-    for (int item = warp; item < MTn * NT; item += blockDim.x >> 5) {
+    for (int item = warp; item < MTn * NT; item += kThreads >> 5) {
       const int mt = item / NT, nt = item - mt * NT;
       const int col = nt * 4 + t, n = nt * 8 + gq;
       const int ecol = exc[min(col, kTile - 1)] - 1022;
@@ -482,14 +483,14 @@ __device__ void quad_rhs_tc(const Grid& g, const cpx* __restrict__ H, int z, int
       for (int rr = 0; rr < 2; ++rr) {
         const int row = mt * 16 + gq + 8 * rr;
         if (row >= N || col >= nx) continue;
-        const int e = g.tcWE[(size_t)w * g.R + row] + ecol - 64;
+        const int e = g.tcWE[(size_t)w * gsz.R() + row] + ecol - 64;
         const cpx val = {round_col(Hh[2 * rr], Ll[2 * rr], e, ecol + 1022),
                          round_col(Hh[2 * rr + 1], Ll[2 * rr + 1], e, ecol + 1022)};
         cpx& f = F[row * kTile + col];
         if (first) {
           f = val;
         } else if (q == 1) {
-          const double k2 = g.K2[(size_t)z * g.X + x0 + col];
+          const double k2 = g.K2[(size_t)z * gsz.X() + x0 + col];
           f.re = fma(-k2, val.re, f.re);
           f.im = fma(-k2, val.im, f.im);
         } else {
@@ -537,16 +538,18 @@ __device__ void band_solve_chain(const double* __restrict__ LU, const double* __
 
 
 
-template <bool MULTI, int kTile>
+// S: the sizes (SizesRT, or SizesCT for a specialised grid)
+template <bool MULTI, int kTile, class S>
 __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ Grid g0, SolveArgs a) {
   const int ntx = (g0.X + kTile - 1) / kTile;
   const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
   const int inst = blockIdx.y;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
-  if (z >= g.Nz || tx * kTile >= g.X) return;
+  const S gsz(g);
+  if (z >= gsz.Nz() || tx * kTile >= gsz.X()) return;
   if (blocked(a.status, a.sdiv, inst)) return;
   const int x0 = tx * kTile;
-  const int nx = min(kTile, g.X - x0);
+  const int nx = min(kTile, gsz.X() - x0);
   const size_t csz = coef_size(g);
   cpx* __restrict__ Cc = a.Cc.at(inst);
   cpx* __restrict__ So = a.Sout.at(inst);
@@ -558,11 +561,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   }
   int mean_mode = a.mean_mode;
   if (mean_mode == MEAN_TAN_HOMOG && ((a.forced_mask >> (inst % a.mdiv)) & 1u)) mean_mode = MEAN_TAN_FORCED;
-  auto cidx = [&](int v, int r, int x) { return (((size_t)z * 2 + v) * g.R + r) * g.X + x; };
-  if (z == g.Nz / 2) {
+  auto cidx = [&](int v, int r, int x) { return (((size_t)z * 2 + v) * gsz.R() + r) * gsz.X() + x; };
+  if (z == gsz.Nz() / 2) {
     // the Nz/2 line is zeroed every substage and never stored (channel/channel.c:460-467)
-    for (int i = threadIdx.x; i < 2 * g.R * nx; i += blockDim.x) {
-      const int v = i / (g.R * nx), r = (i / nx) % g.R, x = x0 + i % nx;
+    for (int i = threadIdx.x; i < 2 * gsz.R() * nx; i += kThreads) {
+      const int v = i / (gsz.R() * nx), r = (i / nx) % gsz.R(), x = x0 + i % nx;
       Cc[cidx(v, r, x)] = cpx{0.0, 0.0};
       So[cidx(v, r, x)] = cpx{0.0, 0.0};
     }
@@ -573,7 +576,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   const RKc rk = rk_coeffs(a.k, a.adjoint);
   const bool adj = a.adjoint != 0;
   const cpx* __restrict__ H = a.H.at(inst);
-  if (g.tc) quad_rhs_tc<kTile>(g, H, z, x0, nx, adj, s);
+  if (g.tc) quad_rhs_tc<kTile>(g, gsz, H, z, x0, nx, adj, s);
   else quad_rhs<kTile>(g, H, z, x0, nx, adj, s);
   const double dt = g.dt;
   const int xfirst = (z == 0 && x0 == 0) ? 1 : 0;  // the mean mode has its own system
@@ -599,40 +602,40 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     // C += dt Mass^-1 F MC[3n+1] with F_alpha = -re^2 Dv, F_beta = re^2 (Rps + K2 Rs)
     __syncthreads();
     const cpx* x1 = xk + csz;
-    for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+    for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
       const int r = i / kTile, l = i - r * kTile;
       if (l >= nx || l < xfirst) continue;
       const int x = x0 + l;
-      const double k2 = g.K2[(size_t)z * g.X + x];
-      if (r < g.D) {
-        const cpx v = visc_v_row(g, k2, x1 + cidx(0, 0, x), g.X, r);
+      const double k2 = g.K2[(size_t)z * gsz.X() + x];
+      if (r < gsz.D()) {
+        const cpx v = visc_v_row(g, k2, x1 + cidx(0, 0, x), gsz.X(), r);
         s.ra[r * kTile + l] = cpx{-re2 * v.re, -re2 * v.im};
       }
-      const cpx w = visc_g_row(g, k2, x1 + cidx(1, 0, x), g.X, r);
+      const cpx w = visc_g_row(g, k2, x1 + cidx(1, 0, x), gsz.X(), r);
       s.rb[r * kTile + l] = cpx{re2 * w.re, re2 * w.im};
     }
     __syncthreads();
     if (threadIdx.x < 8 * kTile) {  // mass matrices: the b = 0 factors
       const int l = (threadIdx.x % (4 * kTile)) / 4, ch = 4 * (threadIdx.x / (4 * kTile)) + threadIdx.x % 4;
       if (l < nx && l >= xfirst) {
-        const size_t zx = (size_t)z * g.X + x0 + l;
+        const size_t zx = (size_t)z * gsz.X() + x0 + l;
         const int par = ch & 1, part = (ch >> 1) & 1;
         if (ch < 4)
-          band_solve_chain<9, 4, 4>(g.luA + ((size_t)2 * g.Nz * g.X + zx) * g.D * 9,
-                                    g.rdA + ((size_t)2 * g.Nz * g.X + zx) * g.D, g.D, par,
+          band_solve_chain<9, 4, 4>(g.luA + ((size_t)2 * gsz.Nz() * gsz.X() + zx) * gsz.D() * 9,
+                                    g.rdA + ((size_t)2 * gsz.Nz() * gsz.X() + zx) * gsz.D(), gsz.D(), par,
                                     reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
         else
-          band_solve_chain<5, 2, 2>(g.luB + ((size_t)2 * g.Nz * g.X + zx) * g.R * 5,
-                                    g.rdB + ((size_t)2 * g.Nz * g.X + zx) * g.R, g.R, par,
+          band_solve_chain<5, 2, 2>(g.luB + ((size_t)2 * gsz.Nz() * gsz.X() + zx) * gsz.R() * 5,
+                                    g.rdB + ((size_t)2 * gsz.Nz() * gsz.X() + zx) * gsz.R(), gsz.R(), par,
                                     reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
       }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+    for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
       const int r = i / kTile, l = i - r * kTile;
       if (l >= nx || l < xfirst) continue;
       const int x = x0 + l;
-      if (r < g.D) {
+      if (r < gsz.D()) {
         const cpx f = s.ra[r * kTile + l];
         Cc[cidx(0, r, x)].re += dt * f.re;
         Cc[cidx(0, r, x)].im += dt * f.im;
@@ -644,16 +647,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     __syncthreads();
   }
   // right-hand sides (channel/project.c:60-81, 125-130, 143-163, 202-207)
-  for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+  for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx || l < xfirst) continue;
     const int x = x0 + l;
-    const size_t zx = (size_t)z * g.X + x;
+    const size_t zx = (size_t)z * gsz.X() + x;
     cpx va, vb;
-    if (r < g.D) {
+    if (r < gsz.D()) {
       if (a.k == 0) {
-        const double* E = g.exA + ((size_t)rk.aidx0 * g.Nz * g.X + zx) * g.D * 9;
-        va = band_matvec_row(E, 9, 4, 4, g.D, Cc + cidx(0, 0, x), g.X, r);
+        const double* E = g.exA + ((size_t)rk.aidx0 * gsz.Nz() * gsz.X() + zx) * gsz.D() * 9;
+        va = band_matvec_row(E, 9, 4, 4, gsz.D(), Cc + cidx(0, 0, x), gsz.X(), r);
       } else {
         va = Cc[cidx(0, r, x)];
       }
@@ -662,8 +665,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
       va.im += dt * rk.c * f.im;
       if (fkind == 3) {
         const double k2 = g.K2[zx];
-        const cpx d0 = visc_v_row(g, k2, xk + cidx(0, 0, x), g.X, r);
-        const cpx d1 = visc_v_row(g, k2, xk + csz + cidx(0, 0, x), g.X, r);
+        const cpx d0 = visc_v_row(g, k2, xk + cidx(0, 0, x), gsz.X(), r);
+        const cpx d1 = visc_v_row(g, k2, xk + csz + cidx(0, 0, x), gsz.X(), r);
         va.re -= re2 * dt * ak * d0.re;
         va.im -= re2 * dt * ak * d0.im;
         va.re -= re2 * dt * rk.b * d1.re;
@@ -673,8 +676,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
       va = Cc[cidx(0, r, x)];  // alpha rows >= Ny-4 ride along unchanged
     }
     if (a.k == 0) {
-      const double* E = g.exB + ((size_t)rk.aidx0 * g.Nz * g.X + zx) * g.R * 5;
-      vb = band_matvec_row(E, 5, 2, 2, g.R, Cc + cidx(1, 0, x), g.X, r);
+      const double* E = g.exB + ((size_t)rk.aidx0 * gsz.Nz() * gsz.X() + zx) * gsz.R() * 5;
+      vb = band_matvec_row(E, 5, 2, 2, gsz.R(), Cc + cidx(1, 0, x), gsz.X(), r);
     } else {
       vb = Cc[cidx(1, r, x)];
     }
@@ -683,8 +686,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     vb.im += dt * rk.c * f.im;
     if (fkind == 3) {  // beta: D = -(Rps + K2 Rs)
       const double k2 = g.K2[zx];
-      const cpx d0 = visc_g_row(g, k2, xk + cidx(1, 0, x), g.X, r);
-      const cpx d1 = visc_g_row(g, k2, xk + csz + cidx(1, 0, x), g.X, r);
+      const cpx d0 = visc_g_row(g, k2, xk + cidx(1, 0, x), gsz.X(), r);
+      const cpx d1 = visc_g_row(g, k2, xk + csz + cidx(1, 0, x), gsz.X(), r);
       vb.re += re2 * dt * ak * d0.re;
       vb.im += re2 * dt * ak * d0.im;
       vb.re += re2 * dt * rk.b * d1.re;
@@ -701,15 +704,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     const int l = (threadIdx.x % (4 * kTile)) / 4, ch = 4 * (threadIdx.x / (4 * kTile)) + threadIdx.x % 4;
     if (l < nx && l >= xfirst) {
       const int x = x0 + l;
-      const size_t zx = (size_t)z * g.X + x;
+      const size_t zx = (size_t)z * gsz.X() + x;
       const int par = ch & 1, part = (ch >> 1) & 1;
       if (ch < 4) {
-        const size_t sys = (size_t)rk.bidx * g.Nz * g.X + zx;
-        band_solve_chain<9, 4, 4>(g.luA + sys * g.D * 9, g.rdA + sys * g.D, g.D, par,
+        const size_t sys = (size_t)rk.bidx * gsz.Nz() * gsz.X() + zx;
+        band_solve_chain<9, 4, 4>(g.luA + sys * gsz.D() * 9, g.rdA + sys * gsz.D(), gsz.D(), par,
                                   reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
       } else {
-        const size_t sys = (size_t)rk.bidx * g.Nz * g.X + zx;
-        band_solve_chain<5, 2, 2>(g.luB + sys * g.R * 5, g.rdB + sys * g.R, g.R, par,
+        const size_t sys = (size_t)rk.bidx * gsz.Nz() * gsz.X() + zx;
+        band_solve_chain<5, 2, 2>(g.luB + sys * gsz.R() * 5, g.rdB + sys * gsz.R(), gsz.R(), par,
                                   reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
       }
     }
@@ -718,29 +721,29 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   // mean mode (channel/project0.c, increproject0.c, adjproject0.c), warp 0
   if (xfirst == 1 && threadIdx.x < 32) {
     double* fa = s.m0;                 // [R]
-    double* fb = s.m0 + g.R;           // [R]
-    cpx* ca = reinterpret_cast<cpx*>(s.m0 + 2 * g.R);  // [R]
-    cpx* cb = ca + g.R;                                // [R]
+    double* fb = s.m0 + gsz.R();           // [R]
+    cpx* ca = reinterpret_cast<cpx*>(s.m0 + 2 * gsz.R());  // [R]
+    cpx* cb = ca + gsz.R();                                // [R]
     const int lane = threadIdx.x;
-    const size_t cs = (size_t)g.Q * g.X;
+    const size_t cs = (size_t)gsz.Q() * gsz.X();
     const cpx* H0 = H;  // z = 0, x = 0
     if (fkind == 2 && a.k == 0) {
       // tangent_forcing0.c:31-41 on MC[3n+1], Rs^-1, IC += dt f (increproject0.c:45-90)
       const cpx* x1 = xk + csz;
-      for (int i = lane; i < g.R; i += 32) {
-        const cpx p = band_matvec_row(g.Rps, 5, 2, 2, g.R, x1 + cidx(0, 0, 0), g.X, i);
-        const cpx q = band_matvec_row(g.Rps, 5, 2, 2, g.R, x1 + cidx(1, 0, 0), g.X, i);
+      for (int i = lane; i < gsz.R(); i += 32) {
+        const cpx p = band_matvec_row(g.Rps, 5, 2, 2, gsz.R(), x1 + cidx(0, 0, 0), gsz.X(), i);
+        const cpx q = band_matvec_row(g.Rps, 5, 2, 2, gsz.R(), x1 + cidx(1, 0, 0), gsz.X(), i);
         ca[i] = cpx{re2 * p.re, re2 * p.im};
         cb[i] = cpx{re2 * q.re, re2 * q.im};
       }
       __syncwarp();
       if (lane < 8) {
         const int par = lane & 1, part = (lane >> 1) & 1;
-        band_solve_chain<5, 2, 2>(g.lu0 + (size_t)2 * g.R * 5, g.rd0 + (size_t)2 * g.R, g.R, par,
+        band_solve_chain<5, 2, 2>(g.lu0 + (size_t)2 * gsz.R() * 5, g.rd0 + (size_t)2 * gsz.R(), gsz.R(), par,
                                   reinterpret_cast<double*>(lane < 4 ? ca : cb) + part, 2);
       }
       __syncwarp();
-      for (int i = lane; i < g.R; i += 32) {
+      for (int i = lane; i < gsz.R(); i += 32) {
         Cc[cidx(0, i, 0)].re += dt * ca[i].re;
         Cc[cidx(0, i, 0)].im += dt * ca[i].im;
         Cc[cidx(1, i, 0)].re += dt * cb[i].re;
@@ -748,25 +751,25 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
       }
       __syncwarp();
     }
-    for (int i = lane; i < g.R; i += 32) {
+    for (int i = lane; i < gsz.R(); i += 32) {
       double sa = 0.0, sb = 0.0;
-      for (int y = 0; y < g.Q; ++y) {
-        const double rw = __ldg(g.Wr + (size_t)i * g.Q + y);
-        sa = fma(rw, H0[1 * cs + (size_t)y * g.X].re, sa);
-        sb = fma(rw, H0[0 * cs + (size_t)y * g.X].re, sb);
+      for (int y = 0; y < gsz.Q(); ++y) {
+        const double rw = __ldg(g.Wr + (size_t)i * gsz.Q() + y);
+        sa = fma(rw, H0[1 * cs + (size_t)y * gsz.X()].re, sa);
+        sb = fma(rw, H0[0 * cs + (size_t)y * gsz.X()].re, sb);
         if (adj) {
-          const double rpw = __ldg(g.Wrp + (size_t)i * g.Q + y);
-          sa = fma(rpw, H0[4 * cs + (size_t)y * g.X].re, sa);
-          sb = fma(-rpw, H0[3 * cs + (size_t)y * g.X].re, sb);
+          const double rpw = __ldg(g.Wrp + (size_t)i * gsz.Q() + y);
+          sa = fma(rpw, H0[4 * cs + (size_t)y * gsz.X()].re, sa);
+          sb = fma(-rpw, H0[3 * cs + (size_t)y * gsz.X()].re, sb);
         }
       }
       fa[i] = sa;
       fb[i] = sb;
       cpx va, vb;
       if (a.k == 0) {
-        const double* E = g.ex0 + (size_t)rk.aidx0 * g.R * 5;
-        va = band_matvec_row(E, 5, 2, 2, g.R, Cc + cidx(0, 0, 0), g.X, i);
-        vb = band_matvec_row(E, 5, 2, 2, g.R, Cc + cidx(1, 0, 0), g.X, i);
+        const double* E = g.ex0 + (size_t)rk.aidx0 * gsz.R() * 5;
+        va = band_matvec_row(E, 5, 2, 2, gsz.R(), Cc + cidx(0, 0, 0), gsz.X(), i);
+        vb = band_matvec_row(E, 5, 2, 2, gsz.R(), Cc + cidx(1, 0, 0), gsz.X(), i);
       } else {
         va = Cc[cidx(0, i, 0)];
         vb = Cc[cidx(1, i, 0)];
@@ -776,11 +779,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
       if (fkind == 3) {
         // D0 = -Rps; the implicit term acts on the primal's solved mean flow
         // before its flux correction: MC[3n+k+1] - 0.5 flux_t add
-        const cpx p0 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + cidx(0, 0, 0), g.X, i);
-        cpx p1 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + csz + cidx(0, 0, 0), g.X, i);
+        const cpx p0 = band_matvec_row(g.Rps, 5, 2, 2, gsz.R(), xk + cidx(0, 0, 0), gsz.X(), i);
+        cpx p1 = band_matvec_row(g.Rps, 5, 2, 2, gsz.R(), xk + csz + cidx(0, 0, 0), gsz.X(), i);
         p1.re -= 0.5 * ft1 * rps_row_real(g, g.add0, i);
-        const cpx q0 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + cidx(1, 0, 0), g.X, i);
-        const cpx q1 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + csz + cidx(1, 0, 0), g.X, i);
+        const cpx q0 = band_matvec_row(g.Rps, 5, 2, 2, gsz.R(), xk + cidx(1, 0, 0), gsz.X(), i);
+        const cpx q1 = band_matvec_row(g.Rps, 5, 2, 2, gsz.R(), xk + csz + cidx(1, 0, 0), gsz.X(), i);
         va.re += re2 * dt * ak * p0.re;
         va.im += re2 * dt * ak * p0.im;
         va.re += re2 * dt * rk.b * p1.re;
@@ -797,25 +800,25 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     if (lane < 8) {
       const int par = lane & 1, part = (lane >> 1) & 1;
       cpx* vec = (lane < 4) ? ca : cb;
-      band_solve_chain<5, 2, 2>(g.lu0 + (size_t)rk.bidx * g.R * 5, g.rd0 + (size_t)rk.bidx * g.R, g.R, par,
+      band_solve_chain<5, 2, 2>(g.lu0 + (size_t)rk.bidx * gsz.R() * 5, g.rd0 + (size_t)rk.bidx * gsz.R(), gsz.R(), par,
                                 reinterpret_cast<double*>(vec) + part, 2);
     }
     __syncwarp();
     // constant mass flux: a += 0.5 * flux_t * add (channel/project0.c:153-168)
     double part = 0.0;
-    for (int i = lane; i < g.R; i += 32) part = fma(g.rwsum[i], ca[i].re, part);
+    for (int i = lane; i < gsz.R(); i += 32) part = fma(g.rwsum[i], ca[i].re, part);
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     double flux_t;
     if (mean_mode == MEAN_PRIMAL) flux_t = g.flux - part;
     else if (mean_mode == MEAN_TAN_FORCED) flux_t = 2.0 - part;
     else flux_t = -part;
-    const double* add = g.add0 + (size_t)(adj ? 1 + rk.bidx : 0) * g.R;
+    const double* add = g.add0 + (size_t)(adj ? 1 + rk.bidx : 0) * gsz.R();
     if (mean_mode == MEAN_PRIMAL && a.Fts && Tst && lane == 0)
       a.Fts[(long long)(inst / a.tdiv) * a.fts_stride + tslot] = flux_t;
     __syncwarp();
-    for (int i = lane; i < g.R; i += 32) ca[i].re = ca[i].re + flux_t * add[i] * 0.5;
+    for (int i = lane; i < gsz.R(); i += 32) ca[i].re = ca[i].re + flux_t * add[i] * 0.5;
     __syncwarp();
-    for (int i = lane; i < g.R; i += 32) {
+    for (int i = lane; i < gsz.R(); i += 32) {
       So[cidx(0, i, 0)] = ca[i];
       So[cidx(1, i, 0)] = cb[i];
       if (Tst) {
@@ -825,7 +828,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     }
   }
   // state rows: alpha from the solve (rows >= Ny-4 carried), beta from the solve
-  for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+  for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx || l < xfirst) continue;
     const int x = x0 + l;
@@ -840,7 +843,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   __syncthreads();
   if (a.k == 2) {
     // the carried array is the state after the last substage
-    for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+    for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
       const int r = i / kTile, l = i - r * kTile;
       if (l >= nx) continue;
       const int x = x0 + l;
@@ -854,24 +857,24 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   //  channel/adjproject.c:393-549)
   if (adj) {
     __syncthreads();
-    if (g.tc) quad_rhs_tc<kTile>(g, a.Hprev.at(inst), z, x0, nx, true, s);
+    if (g.tc) quad_rhs_tc<kTile>(g, gsz, a.Hprev.at(inst), z, x0, nx, true, s);
     else quad_rhs<kTile>(g, a.Hprev.at(inst), z, x0, nx, true, s);
     if (xfirst == 1 && threadIdx.x < 32) {
       // mean mode fa/fb from the previous-stage terms (channel/adjproject0.c:254-294)
       const cpx* H0 = a.Hprev.at(inst);
-      const size_t cs = (size_t)g.Q * g.X;
-      for (int i = threadIdx.x; i < g.R; i += 32) {
+      const size_t cs = (size_t)gsz.Q() * gsz.X();
+      for (int i = threadIdx.x; i < gsz.R(); i += 32) {
         double sa = 0.0, sb = 0.0;
-        for (int y = 0; y < g.Q; ++y) {
-          const double rw = __ldg(g.Wr + (size_t)i * g.Q + y);
-          const double rpw = __ldg(g.Wrp + (size_t)i * g.Q + y);
-          sa = fma(rw, H0[1 * cs + (size_t)y * g.X].re, sa);
-          sa = fma(rpw, H0[4 * cs + (size_t)y * g.X].re, sa);
-          sb = fma(rw, H0[0 * cs + (size_t)y * g.X].re, sb);
-          sb = fma(-rpw, H0[3 * cs + (size_t)y * g.X].re, sb);
+        for (int y = 0; y < gsz.Q(); ++y) {
+          const double rw = __ldg(g.Wr + (size_t)i * gsz.Q() + y);
+          const double rpw = __ldg(g.Wrp + (size_t)i * gsz.Q() + y);
+          sa = fma(rw, H0[1 * cs + (size_t)y * gsz.X()].re, sa);
+          sa = fma(rpw, H0[4 * cs + (size_t)y * gsz.X()].re, sa);
+          sb = fma(rw, H0[0 * cs + (size_t)y * gsz.X()].re, sb);
+          sb = fma(-rpw, H0[3 * cs + (size_t)y * gsz.X()].re, sb);
         }
         s.m0[i] = sa;
-        s.m0[g.R + i] = sb;
+        s.m0[gsz.R() + i] = sb;
       }
     }
     __syncthreads();
@@ -880,81 +883,94 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   // adjoint's second quadrature overwrote them (they share its digit
   // buffer); the results go to Fa, Fb (each element read and written by one
   // thread)
-  for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+  for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx || l < xfirst) continue;
     const int x = x0 + l;
-    const size_t zx = (size_t)z * g.X + x;
+    const size_t zx = (size_t)z * gsz.X() + x;
     const cpx* ya = adj ? So + cidx(0, 0, x) : s.ra + l;
     const cpx* yb = adj ? So + cidx(1, 0, x) : s.rb + l;
-    const int ys = adj ? g.X : kTile;
-    if (r < g.D) {
-      const double* E = g.exA + ((size_t)rk.aidx_next * g.Nz * g.X + zx) * g.D * 9;
-      cpx va = band_matvec_row_t<9, 4, 4>(E, g.D, ya, ys, r);
+    const int ys = adj ? gsz.X() : kTile;
+    if (r < gsz.D()) {
+      const double* E = g.exA + ((size_t)rk.aidx_next * gsz.Nz() * gsz.X() + zx) * gsz.D() * 9;
+      cpx va = band_matvec_row_t<9, 4, 4>(E, gsz.D(), ya, ys, r);
       const cpx f = s.Fa[r * kTile + l];
       va.re += dt * rk.dnext * f.re;
       va.im += dt * rk.dnext * f.im;
       s.Fa[r * kTile + l] = va;
     }
-    const double* E = g.exB + ((size_t)rk.aidx_next * g.Nz * g.X + zx) * g.R * 5;
-    cpx vb = band_matvec_row_t<5, 2, 2>(E, g.R, yb, ys, r);
+    const double* E = g.exB + ((size_t)rk.aidx_next * gsz.Nz() * gsz.X() + zx) * gsz.R() * 5;
+    cpx vb = band_matvec_row_t<5, 2, 2>(E, gsz.R(), yb, ys, r);
     const cpx f = s.Fb[r * kTile + l];
     vb.re += dt * rk.dnext * f.re;
     vb.im += dt * rk.dnext * f.im;
     s.Fb[r * kTile + l] = vb;
   }
   if (xfirst == 1 && threadIdx.x < 32) {
-    const double* E = g.ex0 + (size_t)rk.aidx_next * g.R * 5;
-    cpx* ca = reinterpret_cast<cpx*>(s.m0 + 2 * g.R);
-    cpx* cb = ca + g.R;
-    for (int i = threadIdx.x; i < g.R; i += 32) {
-      cpx va = band_matvec_row(E, 5, 2, 2, g.R, So + cidx(0, 0, 0), g.X, i);
-      cpx vb = band_matvec_row(E, 5, 2, 2, g.R, So + cidx(1, 0, 0), g.X, i);
+    const double* E = g.ex0 + (size_t)rk.aidx_next * gsz.R() * 5;
+    cpx* ca = reinterpret_cast<cpx*>(s.m0 + 2 * gsz.R());
+    cpx* cb = ca + gsz.R();
+    for (int i = threadIdx.x; i < gsz.R(); i += 32) {
+      cpx va = band_matvec_row(E, 5, 2, 2, gsz.R(), So + cidx(0, 0, 0), gsz.X(), i);
+      cpx vb = band_matvec_row(E, 5, 2, 2, gsz.R(), So + cidx(1, 0, 0), gsz.X(), i);
       va.re += dt * rk.dnext * s.m0[i];
-      vb.re += dt * rk.dnext * s.m0[g.R + i];
+      vb.re += dt * rk.dnext * s.m0[gsz.R() + i];
       ca[i] = va;
       cb[i] = vb;
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+  for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx) continue;
     const int x = x0 + l;
     if (l < xfirst) {
-      const cpx* ca = reinterpret_cast<const cpx*>(s.m0 + 2 * g.R);
+      const cpx* ca = reinterpret_cast<const cpx*>(s.m0 + 2 * gsz.R());
       Cc[cidx(0, r, x)] = ca[r];
-      Cc[cidx(1, r, x)] = ca[g.R + r];
+      Cc[cidx(1, r, x)] = ca[gsz.R() + r];
     } else {
-      Cc[cidx(0, r, x)] = r < g.D ? s.Fa[r * kTile + l] : So[cidx(0, r, x)];  // rows >= Ny-4 carried
+      Cc[cidx(0, r, x)] = r < gsz.D() ? s.Fa[r * kTile + l] : So[cidx(0, r, x)];  // rows >= Ny-4 carried
       Cc[cidx(1, r, x)] = s.Fb[r * kTile + l];
     }
   }
 }
 
-template <int T>
+template <int T, class S>
 static void launch_solve_t(const Grid& g, const SolveArgs& a, cudaStream_t st) {
   const int ntx = (g.X + T - 1) / T;
   const dim3 grid(g.Nz * ntx, a.ninst);
-  if (a.grids) k_solve<true, T><<<grid, kThreads, solve_smem_bytes_t<T>(g), st>>>(g, a);
-  else k_solve<false, T><<<grid, kThreads, solve_smem_bytes_t<T>(g), st>>>(g, a);
+  if (a.grids) k_solve<true, T, SizesRT><<<grid, kThreads, solve_smem_bytes_t<T>(g), st>>>(g, a);
+  else k_solve<false, T, S><<<grid, kThreads, solve_smem_bytes_t<T>(g), st>>>(g, a);
 }
 
-// the block tile of Grid::stile (8 or 16 kx columns; the same results)
+template <class S>
+static void launch_solve_s(const Grid& g, const SolveArgs& a, cudaStream_t st) {
+  if (g.stile == 8) launch_solve_t<8, S>(g, a, st);
+  else launch_solve_t<16, S>(g, a, st);
+}
+
+// the block tile of Grid::stile (8 or 16 kx columns; the same results), the
+// build compiled for the grid's sizes where Grid::fixed & FIXED_SOLVE
 cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st) {
   if (a.ninst <= 0) return cudaSuccess;
-  if (g.stile == 8) launch_solve_t<8>(g, a, st);
-  else launch_solve_t<16>(g, a, st);
+  const bool fx = (g.fixed & FIXED_SOLVE) && !a.grids;
+  if (fx && sizes_match<Sizes32>(g)) launch_solve_s<Sizes32>(g, a, st);
+  else if (fx && sizes_match<Sizes16>(g)) launch_solve_s<Sizes16>(g, a, st);
+  else launch_solve_s<SizesRT>(g, a, st);
   return cudaGetLastError();
 }
 
 void prepare_recon_solve(int optin) {
   allow_max_smem(k_recon<false>, optin);
   allow_max_smem(k_recon<true>, optin);
-  allow_max_smem(k_solve<false, 16>, optin);
-  allow_max_smem(k_solve<true, 16>, optin);
-  allow_max_smem(k_solve<false, 8>, optin);
-  allow_max_smem(k_solve<true, 8>, optin);
+  allow_max_smem(k_solve<false, 16, SizesRT>, optin);
+  allow_max_smem(k_solve<true, 16, SizesRT>, optin);
+  allow_max_smem(k_solve<false, 8, SizesRT>, optin);
+  allow_max_smem(k_solve<true, 8, SizesRT>, optin);
+  allow_max_smem(k_solve<false, 16, Sizes32>, optin);
+  allow_max_smem(k_solve<false, 8, Sizes32>, optin);
+  allow_max_smem(k_solve<false, 16, Sizes16>, optin);
+  allow_max_smem(k_solve<false, 8, Sizes16>, optin);
 }
 
 }  // namespace chn

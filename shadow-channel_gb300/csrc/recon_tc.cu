@@ -30,6 +30,7 @@
 #include "kernels.h"
 #include "setup.h"
 #include "tc_common.cuh"
+#include "sizes.cuh"
 
 namespace chn {
 
@@ -143,18 +144,20 @@ size_t recon_tc_smem_bytes(const Grid& g) {
   return (size_t)2 * kDig * 32 * recon_tc_kstride(KT) * sizeof(uint16_t) + 2 * kTile * sizeof(int);
 }
 
-template <bool MULTI>
+// S: the sizes (SizesRT, or SizesCT for a specialised grid)
+template <bool MULTI, class S>
 __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant__ Grid g0, ReconArgs a) {
   const int ntx = (g0.X + kTile - 1) / kTile;
   const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
   const int inst = blockIdx.y;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
-  if (z >= g.Nz || tx * kTile >= g.X) return;
-  if (z == g.Nz / 2) return;  // never read (channel/pass1.c:51-85 skips it)
+  const S gsz(g);
+  if (z >= gsz.Nz() || tx * kTile >= gsz.X()) return;
+  if (z == gsz.Nz() / 2) return;  // never read (channel/pass1.c:51-85 skips it)
   if (a.status != nullptr && (a.status[inst / a.sdiv] & ST_CFL) != 0) return;
   const int x0 = tx * kTile;
-  const int nx = min(kTile, g.X - x0);
-  const int KT = (g.R + 15) / 16, KS = recon_tc_kstride(KT), MT = (g.Q + 15) / 16;
+  const int nx = min(kTile, gsz.X() - x0);
+  const int KT = (gsz.R() + 15) / 16, KS = recon_tc_kstride(KT), MT = (gsz.Q() + 15) / 16;
   const bool meancol = (z == 0 && x0 == 0);  // column 0 of this tile is the mean mode
   extern __shared__ __align__(16) unsigned char smem[];
   uint16_t* dig = reinterpret_cast<uint16_t*>(smem);  // [cls][digit][n 32][KS]
@@ -162,15 +165,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
   const cpx* __restrict__ C = a.C.at(inst);
   if (a.slot.stride) C += (long long)a.slot.slot() * a.slot.stride;
   auto cval = [&](int cls, int j, int col) -> cpx {
-    const int K = cls == 0 ? g.D : g.R;
+    const int K = cls == 0 ? gsz.D() : gsz.R();
     if (j >= K || col >= nx || (meancol && col == 0)) return cpx{0.0, 0.0};
-    return C[(((size_t)z * 2 + cls) * g.R + j) * g.X + x0 + col];
+    return C[(((size_t)z * 2 + cls) * gsz.R() + j) * gsz.X() + x0 + col];
   };
   // column exponents: |c| < 2^exc over the column's real and imaginary parts
-  for (int i = threadIdx.x; i < 2 * kTile; i += blockDim.x) exc[i] = 0;
+  for (int i = threadIdx.x; i < 2 * kTile; i += kThreads) exc[i] = 0;
   __syncthreads();
   const int nent = 2 * (KT * 16) * kTile;
-  if (KT <= kReconRegs && blockDim.x == 16 * kTile) {
+  if (KT <= kReconRegs && kThreads == 16 * kTile) {
     // thread t holds column t % kTile, rows t / kTile + 16 k of both classes:
     // its coefficients stay in registers from the exponent maxima to the digits
     const int col = threadIdx.x % kTile, j0 = threadIdx.x / kTile;
@@ -200,7 +203,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
       }
     }
   } else {
-    for (int i = threadIdx.x; i < nent; i += blockDim.x) {
+    for (int i = threadIdx.x; i < nent; i += kThreads) {
       const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
       const cpx v = cval(cls, j, col);
       const int e1 = (int)((__double_as_longlong(v.re) >> 52) & 0x7FF);
@@ -209,7 +212,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
       if (e) atomicMax(&exc[cls * kTile + col], e);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nent; i += blockDim.x) {
+    for (int i = threadIdx.x; i < nent; i += kThreads) {
       const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
       const cpx v = cval(cls, j, col);
       const int ex = exc[cls * kTile + col] - 1022;
@@ -224,16 +227,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
   const int NT = (2 * nx + 7) / 8;  // n-tiles of 8 real columns (4 complex)
   const uint4* __restrict__ A = reinterpret_cast<const uint4*>(g.tcA);
   cpx* __restrict__ U = a.U.at(inst);
-  const size_t cs = (size_t)g.Q * g.X;
+  const size_t cs = (size_t)gsz.Q() * gsz.X();
   const int order[5] = {0, 1, 3, 2, 4};
-  for (int item = warp; item < MT * NT; item += blockDim.x >> 5) {
+  for (int item = warp; item < MT * NT; item += kThreads >> 5) {
     const int mt = item / NT, nt = item - mt * NT;
     const int col = nt * 4 + t;  // this thread's complex column
     const int n = nt * 8 + gq;   // the B-fragment column this thread loads
     cpx held[2];                 // Q' alpha, then Q'' alpha, at rows gq and gq + 8
     for (int ob = 0; ob < 5; ++ob) {
       const int b = order[ob], cls = b < 3 ? 0 : 1;
-      const int KTb = ((cls == 0 ? g.D : g.R) + 15) / 16;
+      const int KTb = ((cls == 0 ? gsz.D() : gsz.R()) + 15) / 16;
       const int ecol = exc[cls * kTile + col] - 1022;
       long long H[4], L[4];
       tc_tile_pf(A + (size_t)b * MT * KT * kDig * 32, mt, KT, KTb, dig + (size_t)cls * kDig * 32 * KS, KS,
@@ -241,13 +244,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
 #pragma unroll
       for (int rr = 0; rr < 2; ++rr) {
         const int y = mt * 16 + gq + 8 * rr;
-        if (y >= g.Q || col >= nx || (meancol && col == 0)) continue;
-        const int e = g.tcE[(size_t)b * g.Q + y] + ecol - 64;
+        if (y >= gsz.Q() || col >= nx || (meancol && col == 0)) continue;
+        const int e = g.tcE[(size_t)b * gsz.Q() + y] + ecol - 64;
         const cpx val = {round_col(H[2 * rr], L[2 * rr], e, ecol + 1022),
                          round_col(H[2 * rr + 1], L[2 * rr + 1], e, ecol + 1022)};
         const int x = x0 + col;
-        cpx* out = U + ((size_t)z * 5 * g.Q + y) * g.X + x;
-        const double ax = g.kxK2[(size_t)z * g.X + x], az = g.kzK2[(size_t)z * g.X + x];
+        cpx* out = U + ((size_t)z * 5 * gsz.Q() + y) * gsz.X() + x;
+        const double ax = g.kxK2[(size_t)z * gsz.X() + x], az = g.kzK2[(size_t)z * gsz.X() + x];
         if (b == 0) {
           out[cs] = val;  // v = Q alpha
         } else if (b == 1 || b == 2) {
@@ -268,17 +271,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
   if (meancol) {
     // (kx, kz) = (0, 0): u = R a, du = R' a, v = 0, w = R b, dw = R' b
     // (channel/initAlphaBeta2.c:25-68), direct FP64
-    for (int y = threadIdx.x; y < g.Q; y += blockDim.x) {
+    for (int y = threadIdx.x; y < gsz.Q(); y += kThreads) {
       double ur = 0, ui = 0, dur = 0, dui = 0, wr = 0, wi = 0, dwr = 0, dwi = 0;
-      for (int j = 0; j < g.R; ++j) {
-        const double r = __ldg(g.Br + (size_t)y * g.R + j), rp = __ldg(g.Brp + (size_t)y * g.R + j);
-        const cpx al = C[((size_t)0 * g.R + j) * g.X], be = C[((size_t)1 * g.R + j) * g.X];
+      for (int j = 0; j < gsz.R(); ++j) {
+        const double r = __ldg(g.Br + (size_t)y * gsz.R() + j), rp = __ldg(g.Brp + (size_t)y * gsz.R() + j);
+        const cpx al = C[((size_t)0 * gsz.R() + j) * gsz.X()], be = C[((size_t)1 * gsz.R() + j) * gsz.X()];
         ur = fma(r, al.re, ur); ui = fma(r, al.im, ui);
         dur = fma(rp, al.re, dur); dui = fma(rp, al.im, dui);
         wr = fma(r, be.re, wr); wi = fma(r, be.im, wi);
         dwr = fma(rp, be.re, dwr); dwi = fma(rp, be.im, dwi);
       }
-      cpx* out = U + (size_t)y * g.X;
+      cpx* out = U + (size_t)y * gsz.X();
       out[0] = cpx{ur, ui};
       out[cs] = cpx{0.0, 0.0};
       out[2 * cs] = cpx{wr, wi};
@@ -288,17 +291,28 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
   }
 }
 
-cudaError_t launch_recon_tc(const Grid& g, const ReconArgs& a, cudaStream_t st) {
+template <class S>
+static void launch_recon_sizes(const Grid& g, const ReconArgs& a, cudaStream_t st) {
   const int ntx = (g.X + kTile - 1) / kTile;
   const size_t sm = recon_tc_smem_bytes(g);
-  if (a.grids) k_recon_tc<true><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
-  else k_recon_tc<false><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
+  if (a.grids) k_recon_tc<true, SizesRT><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
+  else k_recon_tc<false, S><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
+}
+
+// Grid::fixed & FIXED_RECON: the build compiled for the grid's sizes
+cudaError_t launch_recon_tc(const Grid& g, const ReconArgs& a, cudaStream_t st) {
+  const bool fx = (g.fixed & FIXED_RECON) && !a.grids;
+  if (fx && sizes_match<Sizes32>(g)) launch_recon_sizes<Sizes32>(g, a, st);
+  else if (fx && sizes_match<Sizes16>(g)) launch_recon_sizes<Sizes16>(g, a, st);
+  else launch_recon_sizes<SizesRT>(g, a, st);
   return cudaGetLastError();
 }
 
 void prepare_recon_tc(int optin) {
-  allow_max_smem(k_recon_tc<false>, optin);
-  allow_max_smem(k_recon_tc<true>, optin);
+  allow_max_smem(k_recon_tc<false, SizesRT>, optin);
+  allow_max_smem(k_recon_tc<true, SizesRT>, optin);
+  allow_max_smem(k_recon_tc<false, Sizes32>, optin);
+  allow_max_smem(k_recon_tc<false, Sizes16>, optin);
 }
 
 }  // namespace chn

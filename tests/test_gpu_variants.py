@@ -7,7 +7,9 @@ arithmetic.  The builds of the tensor-core inverse transform
 blocks per SM, 3 = the same at three, 4 / 5 = one field per pass in
 128-thread blocks at four / five, 6 / 7 = builds 4 / 2 compiled for the
 sizes of 32x65x32 and 16x33x16) change how the columns of a plane are
-grouped, not the digit sums or their rounding.  Each variant runs the
+grouped, not the digit sums or their rounding; nor do the builds of the
+products, reconstruction and solve kernels compiled for those sizes
+(CHN_FIXED_SIZES=1).  Each variant runs the
 batched forward (primal + 3 tangents, one forced) and the coupled adjoint,
 and the single-trajectory primal, and must reproduce the default's outputs
 bit for bit.  Grids: 32x65x32 (the benchmarked one) and 48x97x48 (24 kx
@@ -28,7 +30,7 @@ pytestmark = pytest.mark.gpu
 GRIDS = [(32, 65, 32, 2 * np.pi, np.pi, 3300.0, 2.0, 0.005, 3), (48, 97, 48, 2 * np.pi, np.pi, 3300.0, 2.0, 0.004, 2),
          (16, 33, 16, 2 * np.pi, np.pi, 2000.0, 2.0, 0.01, 3)]
 NSEG, NTAN = 2, 3
-KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_AUTOTUNE")
+KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_FIXED_SIZES", "CHN_AUTOTUNE")
 
 
 @pytest.fixture(scope="module")
@@ -98,6 +100,13 @@ def test_inverse_builds_give_the_same_bits(cc, gi, build):
     _same(a, b)
 
 
+@pytest.mark.parametrize("gi", [0, 2])
+def test_fixed_size_builds_give_the_same_bits(cc, gi):
+    a, _ = _sweeps(cc, GRIDS[gi], {"CHN_FIXED_SIZES": "0", "CHN_AUTOTUNE": "0"})
+    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_FIXED_SIZES": "1", "CHN_AUTOTUNE": "0"})
+    _same(a, b)
+
+
 def test_autotuner_reports_its_choices(cc):
     res, report = _sweeps(cc, GRIDS[0], {})
     if "solve_chosen" not in report:
@@ -107,5 +116,7 @@ def test_autotuner_reports_its_choices(cc):
     assert report["chosen"].startswith("tc_inverse_")
     for b in ("f2_b2", "f2_b3", "f1_b4", "f1_b5", "f1_b4_fixed", "f2_b2_fixed"):
         assert report["tc_inverse_" + b] > 0
+    for part in ("products", "recon", "solve"):
+        assert report[part + "_sizes"] in ("runtime", "fixed") and report[part + "_fixed_sizes"] > 0
     ref, _ = _sweeps(cc, GRIDS[0], {"CHN_SOLVE_TILE": "16", "CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
     _same(res, ref)
