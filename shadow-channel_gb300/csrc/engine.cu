@@ -207,13 +207,18 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   const char* tfp64 = getenv("CHN_TRANSFORMS_FP64");
   g.tci = (!(tfp64 && tfp64[0] == '1') && phys_tc_fits(g, optin)) ? 1 : 0;
   g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_fits(g, optin)) ? 1 : 0;
-  // the inverse's build (phys_tc.cu) until the autotuner has timed them;
-  // CHN_INVERSE_BUILD=2..5 fixes it (and skips that timing)
-  // the kernels' builds compiled for the grid's sizes (autotuned)
+  // the kernels' builds compiled for the grid's sizes where it has them
+  // (a batch's autotuner then times both); CHN_FIXED_SIZES=0 / 1 fixes it
+  const bool spec = phys_tc_specialised(g);
   const char* fx = getenv("CHN_FIXED_SIZES");
-  g.fixed = (fx && fx[0] == '1') ? (FIXED_PRODUCTS | FIXED_RECON | FIXED_SOLVE) : 0;
+  const bool fixed_on = (fx && fx[0]) ? fx[0] == '1' : spec;
+  g.fixed = fixed_on ? (FIXED_PRODUCTS | FIXED_RECON | FIXED_SOLVE) : 0;
+  // the inverse's build (phys_tc.cu) until a batch's autotuner has timed
+  // them: two fields per pass (the single trajectory's plane count gives a
+  // block per plane), compiled for the grid's sizes where it has them;
+  // CHN_INVERSE_BUILD=2..7 fixes it (and skips that timing)
   const char* ib = getenv("CHN_INVERSE_BUILD");
-  g.tcminb = (ib && ib[0] >= '2' && ib[0] <= '7' && ib[1] == 0) ? ib[0] - '0' : 2;
+  g.tcminb = (ib && ib[0] >= '2' && ib[0] <= '7' && ib[1] == 0) ? ib[0] - '0' : (spec ? 7 : 2);
   // the solve's block tile: 16 until the autotuner has timed both;
   // CHN_SOLVE_TILE=8 or 16 fixes it (and skips that timing)
   const char* stl = getenv("CHN_SOLVE_TILE");
