@@ -235,11 +235,11 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 
 // exact (H, L) of seven FP32 level sums (levels at lv[0..6])
 __device__ __forceinline__ void fold7(const float (&lv)[kDig], long long& H, long long& L) {
-  long long v[kDig];
+  int v[kDig];
 #pragma unroll
-  for (int l = 0; l < kDig; ++l) v[l] = (long long)__float2int_rn(lv[l]);
-  H = (v[0] << 16) + (v[1] << 8) + v[2];
-  L = (v[3] << 24) + (v[4] << 16) + (v[5] << 8) + v[6];
+  for (int l = 0; l < kDig; ++l) v[l] = __float2int_rn(lv[l]);
+  H = (long long)v[2] + (long long)v[1] * 256LL + (long long)v[0] * 65536LL;
+  L = (long long)v[6] + (long long)v[5] * 256LL + (long long)v[4] * 65536LL + (long long)v[3] * 16777216LL;
 }
 
 // One stage's MMAs over the k-tiles [k0, k1): data digits (A, blocks of

@@ -137,14 +137,21 @@ __device__ __forceinline__ void digits_pair_bf16(long long xr, long long xi, uin
     out[(size_t)q * stride] = __byte_perm(__float_as_uint(fr[q]), __float_as_uint(fi[q]), 0x7632);
 }
 
-// the exact level sums of one mma accumulator element as (H, L): the sum is
-// (H 2^32 + L) 2^(e_row + e_col - 64) for operands scaled to 56-bit integers
-__device__ __forceinline__ void fold_levels(const float (&acc)[kDig][4], int r, long long& H, long long& L) {
-  long long lv[kDig];
+// the exact level sums of one mma accumulator element added to (H, L): the
+// sum is (H 2^32 + L) 2^(e_row + e_col - 64) for operands scaled to 56-bit
+// integers.  Each level enters as a 32 x 32 -> 64-bit multiply-add onto the
+// running 64-bit sum (exact integer arithmetic: the order does not matter).
+__device__ __forceinline__ void fold_levels_add(const float (&acc)[kDig][4], int r, long long& H, long long& L) {
+  int lv[kDig];
 #pragma unroll
-  for (int l = 0; l < kDig; ++l) lv[l] = (long long)__float2int_rn(acc[l][r]);
-  H = (lv[0] << 16) + (lv[1] << 8) + lv[2];
-  L = (lv[3] << 24) + (lv[4] << 16) + (lv[5] << 8) + lv[6];
+  for (int l = 0; l < kDig; ++l) lv[l] = __float2int_rn(acc[l][r]);
+  H += (long long)lv[2];
+  H += (long long)lv[1] * 256LL;
+  H += (long long)lv[0] * 65536LL;
+  L += (long long)lv[6];
+  L += (long long)lv[5] * 256LL;
+  L += (long long)lv[4] * 65536LL;
+  L += (long long)lv[3] * 16777216LL;
 }
 
 // One exact digit GEMM tile of a fixed table A (fragment order
@@ -180,12 +187,7 @@ __device__ __forceinline__ void tc_tile_range(const uint4* __restrict__ A, int m
       }
     }
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      long long h, l;
-      fold_levels(acc, r, h, l);
-      H[r] += h;
-      L[r] += l;
-    }
+    for (int r = 0; r < 4; ++r) fold_levels_add(acc, r, H[r], L[r]);
   }
 }
 
@@ -234,12 +236,7 @@ __device__ __forceinline__ void tc_tile_pf(const uint4* __restrict__ A, int mt, 
       for (int i = 0; i < kDig; ++i) af[i] = an[i];
     }
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      long long h, l;
-      fold_levels(acc, r, h, l);
-      H[r] += h;
-      L[r] += l;
-    }
+    for (int r = 0; r < 4; ++r) fold_levels_add(acc, r, H[r], L[r]);
   }
 }
 
