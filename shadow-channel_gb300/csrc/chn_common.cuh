@@ -136,6 +136,7 @@ struct Grid {
   const uint32_t* tcFZ;
   const int* tcFZE;
   int tcf;
+  int adjpb;  // product planes per pass of the adjoint product modes (1 or 3; autotuned)
   // kernels that run their build compiled for the grid's sizes (32x65x32,
   // 16x33x16): FIXED_* bits of sizes.cuh (autotuned; the same results)
   int fixed;

@@ -219,6 +219,10 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   // CHN_INVERSE_BUILD=2..7 fixes it (and skips that timing)
   const char* ib = getenv("CHN_INVERSE_BUILD");
   g.tcminb = (ib && ib[0] >= '2' && ib[0] <= '7' && ib[1] == 0) ? ib[0] - '0' : (spec ? 7 : 2);
+  // the adjoint products' planes per pass: 1 until the autotuner has timed
+  // 1 and 3; CHN_ADJ_PRODUCTS_PER_PASS=1 or 3 fixes it
+  const char* apb = getenv("CHN_ADJ_PRODUCTS_PER_PASS");
+  g.adjpb = (apb && apb[0] == '3') ? 3 : 1;
   // the solve's block tile: 16 until the autotuner has timed both;
   // CHN_SOLVE_TILE=8 or 16 fixes it (and skips that timing)
   const char* stl = getenv("CHN_SOLVE_TILE");
@@ -1246,12 +1250,16 @@ static bool autotune_solve(Engine& e, Work& w) {
 // and adjoint products), the reconstruction (tangents) and the implicit
 // solve (a tangent solve into scratch), each timed against its run-time-
 // size build and kept where faster (Grid::fixed).  CHN_FIXED_SIZES=0 / 1
-// fixes all three off / on.
+// fixes all three off / on.  Then the adjoint products' planes per pass,
+// 1 or 3 (Grid::adjpb; CHN_ADJ_PRODUCTS_PER_PASS fixes it).
 static bool autotune_fixed(Engine& e, Work& w) {
   const char* off = getenv("CHN_AUTOTUNE");
   const char* forced = getenv("CHN_FIXED_SIZES");
   Grid& g = e.T.g;
-  if ((off && off[0] == '0') || (forced && forced[0]) || w.gdev || !phys_tc_specialised(g)) return true;
+  const char* apb = getenv("CHN_ADJ_PRODUCTS_PER_PASS");
+  const bool do_fixed = !(forced && forced[0]) && !w.gdev && phys_tc_specialised(g);
+  const bool do_pb = g.tcf && !(apb && apb[0]) && !w.gdev;
+  if ((off && off[0] == '0') || !(do_fixed || do_pb)) return true;
   const int nt = w.nseg * (w.ntan > 0 ? w.ntan : 1);
   ProdArgs f{};
   f.Pp = cbd(w.Pp, w.psz);
@@ -1306,6 +1314,7 @@ static bool autotune_fixed(Engine& e, Work& w) {
   std::string rep;
   char buf[160];
   for (const Part& pt : parts) {
+    if (!do_fixed) break;
     float ms[2] = {0.f, 0.f};
     for (int c = 0; c < 2 && ok; ++c) {
       g.fixed = c ? (g.fixed | pt.bit) : (g.fixed & ~pt.bit);
@@ -1323,6 +1332,31 @@ static bool autotune_fixed(Engine& e, Work& w) {
              ms[0], pt.name, ms[1], pt.name, (g.fixed & pt.bit) ? "fixed" : "runtime");
     if (!rep.empty()) rep += ", ";
     rep += buf;
+  }
+  // the adjoint products' planes per pass (its own switch)
+  if (ok && do_pb) {
+    const int saved_pb = g.adjpb;
+    float ms[2] = {0.f, 0.f};
+    const int pbs[2] = {1, 3};
+    for (int c = 0; c < 2 && ok; ++c) {
+      g.adjpb = pbs[c];
+      ok = launch_products_adj(g, b, e.st) == cudaSuccess;  // warm-up
+      ok = ok && cudaEventRecord(t0, e.st) == cudaSuccess;
+      for (int k = 0; k < 3 && ok; ++k) ok = launch_products_adj(g, b, e.st) == cudaSuccess;
+      ok = ok && cudaEventRecord(t1, e.st) == cudaSuccess && cudaEventSynchronize(t1) == cudaSuccess;
+      if (ok) cudaEventElapsedTime(&ms[c], t0, t1);
+      ms[c] /= 3;
+    }
+    if (ok) {
+      g_launches += 8;
+      g.adjpb = ms[1] < ms[0] ? 3 : 1;
+      snprintf(buf, sizeof(buf), "\"adjoint_products_pb1\": %.4f, \"adjoint_products_pb3\": %.4f, "
+               "\"adjoint_products_per_pass\": %d", ms[0], ms[1], g.adjpb);
+      if (!rep.empty()) rep += ", ";
+      rep += buf;
+    } else {
+      g.adjpb = saved_pb;
+    }
   }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
@@ -2430,6 +2464,7 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
     gs[i].tci = gmax.tci;
     gs[i].tcf = gmax.tcf;
     gs[i].tcminb = gmax.tcminb;
+    gs[i].adjpb = gmax.adjpb;
   }
   if (cudaMalloc(&m->gdev, sizeof(Grid) * n) != cudaSuccess ||
       cudaMemcpy(m->gdev, gs.data(), sizeof(Grid) * n, cudaMemcpyHostToDevice) != cudaSuccess) {

@@ -412,10 +412,11 @@ __host__ __device__ constexpr FwdTcDims fwd_tc_dims_n(int Nz, int X, int pz, int
 
 __host__ __device__ inline FwdTcDims fwd_tc_dims(const Grid& g) { return fwd_tc_dims_n(g.Nz, g.X, g.pz, g.px); }
 
-// pb product planes per pass: kPB for the forward modes (0, 1), one for the
-// adjoint modes (2, 3), whose six transforms per plane run faster with the
-// L1 space the smaller footprint leaves to the tables
-inline int products_per_pass(int mode) { return mode >= 2 ? 1 : kPB; }
+// pb product planes per pass: kPB for the forward modes (0, 1); for the
+// adjoint modes (2, 3, six products) Grid::adjpb: kPB (each field loaded
+// once per three products) or one (a smaller footprint leaves L1 to the
+// tables), as the autotuner finds faster
+inline int products_per_pass(const Grid& g, int mode) { return mode >= 2 && g.adjpb != kPB ? 1 : kPB; }
 
 size_t fwd_tc_smem_bytes(const Grid& g, int pb) {
   const FwdTcDims d = fwd_tc_dims(g);
@@ -596,10 +597,10 @@ bool fwd_tc_fits(const Grid& g, int optin) {
 
 template <class S>
 static void launch_products_sizes(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
-  const size_t sm = fwd_tc_smem_bytes(g, products_per_pass(mode));
+  const size_t sm = fwd_tc_smem_bytes(g, products_per_pass(g, mode));
   const dim3 grid(g.Q, a.ninst);
   constexpr bool M = std::is_same<S, SizesRT>::value;  // only the run-time sizes serve uneven batches
-  if (products_per_pass(mode) == kPB) {
+  if (products_per_pass(g, mode) == kPB) {
     if (M && a.grids) k_products_tc<true, kPB, SizesRT><<<grid, kThreads, sm, st>>>(g, a, mode);
     else k_products_tc<false, kPB, S><<<grid, kThreads, sm, st>>>(g, a, mode);
   } else {

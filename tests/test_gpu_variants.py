@@ -9,9 +9,10 @@ blocks per SM, 3 = the same at three, 4 / 5 = one field per pass in
 sizes of 32x65x32 and 16x33x16) change how the columns of a plane are
 grouped, not the digit sums or their rounding; nor do the builds of the
 products, reconstruction and solve kernels compiled for those sizes
-(CHN_FIXED_SIZES=1).  Each variant runs the
-batched forward (primal + 3 tangents, one forced) and the coupled adjoint,
-and the single-trajectory primal, and must reproduce the default's outputs
+(CHN_FIXED_SIZES=1), nor the adjoint products' planes per pass (1 or 3,
+CHN_ADJ_PRODUCTS_PER_PASS; the reference adjoint and the exact one).  Each variant runs the
+batched forward (primal + 3 tangents, one forced), the coupled adjoint
+and the exact adjoint, and the single-trajectory primal, and must reproduce the default's outputs
 bit for bit.  Grids: 32x65x32 (the benchmarked one) and 48x97x48 (24 kx
 columns: 16 + 8 or three tiles of 8 in the solve).
 """
@@ -30,7 +31,7 @@ pytestmark = pytest.mark.gpu
 GRIDS = [(32, 65, 32, 2 * np.pi, np.pi, 3300.0, 2.0, 0.005, 3), (48, 97, 48, 2 * np.pi, np.pi, 3300.0, 2.0, 0.004, 2),
          (16, 33, 16, 2 * np.pi, np.pi, 2000.0, 2.0, 0.01, 3)]
 NSEG, NTAN = 2, 3
-KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_FIXED_SIZES", "CHN_AUTOTUNE")
+KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_FIXED_SIZES", "CHN_ADJ_PRODUCTS_PER_PASS", "CHN_AUTOTUNE")
 
 
 @pytest.fixture(scope="module")
@@ -60,7 +61,9 @@ def _sweeps(cc, args, env):
         try:
             inh = (ctypes.c_int * NTAN)(0, 0, 1)
             assert lib.c_batch_forward(0, n, C.ctypes.data, IC.ctypes.data, inh) == 0, cc.c_last_error_message()
+            AX = AC.copy()
             assert lib.c_batch_adjoint(n, 0, AC.ctypes.data, 1.0) == 0, cc.c_last_error_message()
+            assert lib.c_batch_adjoint_exact(n, 0, AX.ctypes.data) == 0, cc.c_last_error_message()
             out = np.zeros(C[0].shape, np.complex128)
             traj = []
             for s in range(NSEG):
@@ -72,7 +75,7 @@ def _sweeps(cc, args, env):
         single = O.synthetic_state(Nx, Ny, Nz, seed=99)
         cc.c_primal(0, single)   # the single-trajectory engine takes the variants of c_init
         cc.c_destroy()
-        return [C, IC, AC, np.stack(traj), single], report
+        return [C, IC, AC, AX, np.stack(traj), single], report
     finally:
         for k, v in old.items():
             if v is None:
@@ -107,6 +110,13 @@ def test_fixed_size_builds_give_the_same_bits(cc, gi):
     _same(a, b)
 
 
+@pytest.mark.parametrize("gi", [0, 2])
+def test_adjoint_products_per_pass_give_the_same_bits(cc, gi):
+    a, _ = _sweeps(cc, GRIDS[gi], {"CHN_ADJ_PRODUCTS_PER_PASS": "1", "CHN_AUTOTUNE": "0"})
+    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_ADJ_PRODUCTS_PER_PASS": "3", "CHN_AUTOTUNE": "0"})
+    _same(a, b)
+
+
 def test_autotuner_reports_its_choices(cc):
     res, report = _sweeps(cc, GRIDS[0], {})
     if "solve_chosen" not in report:
@@ -118,5 +128,6 @@ def test_autotuner_reports_its_choices(cc):
         assert report["tc_inverse_" + b] > 0
     for part in ("products", "recon", "solve"):
         assert report[part + "_sizes"] in ("runtime", "fixed") and report[part + "_fixed_sizes"] > 0
+    assert report["adjoint_products_per_pass"] in (1, 3)
     ref, _ = _sweeps(cc, GRIDS[0], {"CHN_SOLVE_TILE": "16", "CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
     _same(res, ref)
