@@ -206,7 +206,9 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   // inverse transforms on the tensor cores unless CHN_TRANSFORMS_FP64=1 (or they do not fit)
   const char* tfp64 = getenv("CHN_TRANSFORMS_FP64");
   g.tci = (!(tfp64 && tfp64[0] == '1') && phys_tc_fits(g, optin)) ? 1 : 0;
-  g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_fits(g, optin)) ? 1 : 0;
+  g.fwdpb = 3;
+  g.fxch = 8;
+  g.tcf = (!(tfp64 && tfp64[0] == '1') && fwd_tc_plan(g, optin, g.fwdpb, g.fxch)) ? 1 : 0;
   // the kernels' builds compiled for the grid's sizes where it has them
   // (a batch's autotuner then times both); CHN_FIXED_SIZES=0 / 1 fixes it
   const bool spec = phys_tc_specialised(g);
@@ -2450,7 +2452,7 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
   const char* force = getenv("CHN_SPLIT_TRANSFORMS");
   gmax.split = (!fused_transforms_fit(gmax, optin) || (force && force[0] == '1')) ? 1 : 0;
   if (!phys_tc_fits(gmax, optin)) gmax.tci = 0;
-  if (!fwd_tc_fits(gmax, optin)) gmax.tcf = 0;
+  if (!fwd_tc_plan(gmax, optin, gmax.fwdpb, gmax.fxch)) gmax.tcf = 0;
   if (solve_smem_bytes(gmax) > (size_t)optin) {
     set_error(1, "c_multi_init: the largest grid needs more shared memory than the device has");
     c_multi_destroy();
@@ -2465,6 +2467,8 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
     gs[i].tcf = gmax.tcf;
     gs[i].tcminb = gmax.tcminb;
     gs[i].adjpb = gmax.adjpb;
+    gs[i].fwdpb = gmax.fwdpb;
+    gs[i].fxch = gmax.fxch;
   }
   if (cudaMalloc(&m->gdev, sizeof(Grid) * n) != cudaSuccess ||
       cudaMemcpy(m->gdev, gs.data(), sizeof(Grid) * n, cudaMemcpyHostToDevice) != cudaSuccess) {

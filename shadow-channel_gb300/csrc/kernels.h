@@ -165,6 +165,8 @@ int tc5_take_error();
 // products + forward transforms as digit GEMMs (mode 0 primal, 1 tangent, 2 adjoint, 3 exact transpose)
 cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st);
 bool fwd_tc_fits(const Grid& g, int optin);
+// the forward products' shared-memory plan (planes per pass, x-stage columns per chunk)
+bool fwd_tc_plan(const Grid& g, int optin, int& pb, int& xch);
 cudaError_t launch_products_fwd(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_products_adj(const Grid& g, const ProdArgs& a, cudaStream_t st);
 cudaError_t launch_solve(const Grid& g, const SolveArgs& a, cudaStream_t st);

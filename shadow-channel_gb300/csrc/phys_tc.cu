@@ -416,11 +416,15 @@ __host__ __device__ inline FwdTcDims fwd_tc_dims(const Grid& g) { return fwd_tc_
 // adjoint modes (2, 3, six products) Grid::adjpb: kPB (each field loaded
 // once per three products) or one (a smaller footprint leaves L1 to the
 // tables), as the autotuner finds faster
-inline int products_per_pass(const Grid& g, int mode) { return mode >= 2 && g.adjpb != kPB ? 1 : kPB; }
+inline int products_per_pass(const Grid& g, int mode) {
+  if (mode < 2) return g.fwdpb;
+  return g.adjpb == kPB && g.fwdpb == kPB ? kPB : 1;
+}
 
-size_t fwd_tc_smem_bytes(const Grid& g, int pb) {
+// xch: x-stage columns (padded zp rows) digitised per chunk
+size_t fwd_tc_smem_bytes(const Grid& g, int pb, int xch) {
   const FwdTcDims d = fwd_tc_dims(g);
-  const size_t dx = (size_t)kDig * d.pzp * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
+  const size_t dx = (size_t)kDig * xch * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
   // kPB product planes (Y of the component in flight overlays its own plane:
   // pz X complex values <= pz px doubles)
   const size_t stage = (size_t)pb * g.pz * g.px * sizeof(double);
@@ -453,8 +457,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
   int* exx3 = reinterpret_cast<int*>(p); p += (size_t)pb * exs * sizeof(int);  // [c][zp]
   int* exz = reinterpret_cast<int*>(p); p += (size_t)((gsz.X() + 3) / 4 * 4) * sizeof(int);
   uint16_t* dig = reinterpret_cast<uint16_t*>(p);
+  // x-stage columns per chunk: all of them in the fixed-size builds, else
+  // the plan's (Grid::fxch, a multiple of 8)
+  int XCH = d.pzp;
+  if constexpr (std::is_same<S, SizesRT>::value) XCH = min(g.fxch, d.pzp);
   {
-    const size_t dx = (size_t)kDig * d.pzp * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
+    const size_t dx = (size_t)kDig * XCH * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
     p += ((dx > dz ? dx : dz) + 15) / 16 * 16;
   }
   double* stage3 = reinterpret_cast<double*>(p);  // [c][zp][xp] products; Y [zp][kx] (cpx) over plane c
@@ -472,7 +480,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
   constexpr int nwarp = kThreads >> 5;
   const int ncomp = mode >= 2 ? 6 : 3;
-  const size_t xstride = (size_t)d.pzp * d.KSx, zstride = (size_t)d.Xp * d.KSz;  // bf16 between digits
+  const size_t xstride = (size_t)XCH * d.KSx, zstride = (size_t)d.Xp * d.KSz;  // bf16 between digits
   for (int q = 0; q < ncomp; ++q) {
     const int c = q % pb;
     double* stage = stage3 + (size_t)c * plane;
@@ -506,23 +514,26 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
       }
       __syncthreads();
     }
-    FlatRC rcx(threadIdx.x, kThreads, d.KTx * 16);
-    for (int i = threadIdx.x; i < d.pzp * (d.KTx * 16); i += kThreads, rcx.next()) {
-      const int n = rcx.r, k = rcx.c;
-      const double v = (n < gsz.pz() && k < gsz.px()) ? stage[(size_t)n * gsz.px() + k] : 0.0;
-      digits_bf16(scaled56(v, exx[min(n, gsz.pz() - 1)] - 1022), dig + (size_t)n * d.KSx + k, xstride);
-    }
-    __syncthreads();
-    // ---- x stage: rows 2kx (+1), columns zp; Y into the staging region
-    {
-      const int NT = d.pzp / 8;
+    // ---- x stage: rows 2kx (+1), columns zp, in chunks of XCH columns; Y
+    // into the staging region (Y row zp lies below stage row zp, 16 X < 8 px
+    // bytes per row, so a chunk's outputs only cover rows already digitised)
+    for (int zc = 0; zc < d.pzp; zc += XCH) {
+      const int nch = min(XCH, d.pzp - zc);
+      FlatRC rcx(threadIdx.x, kThreads, d.KTx * 16);
+      for (int i = threadIdx.x; i < nch * (d.KTx * 16); i += kThreads, rcx.next()) {
+        const int n = zc + rcx.r, k = rcx.c;
+        const double v = (n < gsz.pz() && k < gsz.px()) ? stage[(size_t)n * gsz.px() + k] : 0.0;
+        digits_bf16(scaled56(v, exx[min(n, gsz.pz() - 1)] - 1022), dig + (size_t)rcx.r * d.KSx + k, xstride);
+      }
+      __syncthreads();
+      const int NT = nch / 8;
       for (int item = warp; item < d.MTx * NT; item += nwarp) {
         const int mt = item / NT, nt = item - mt * NT;
         long long Hh[4], Ll[4];
         tc_tile(Ax, mt, d.KTx, dig, d.KSx, xstride, nt * 8 + gq, lane, t, Hh, Ll);
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-          const int row = mt * 16 + gq + 8 * (r >> 1), zp = nt * 8 + 2 * t + (r & 1);
+          const int row = mt * 16 + gq + 8 * (r >> 1), zp = zc + nt * 8 + 2 * t + (r & 1);
           if (row >= 2 * gsz.X() || zp >= gsz.pz()) continue;
           const double v = round_col(Hh[r], Ll[r], AxE[row] + exx[zp] - 1022 - 64, exx[zp]);
           cpx& yv = Yb[(size_t)zp * gsz.X() + (row >> 1)];
@@ -530,8 +541,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
           else yv.re = v;
         }
       }
+      __syncthreads();
     }
-    __syncthreads();
     // ---- z stage inputs: columns kx, K = 2 pz (Re, Im of Y[zp][kx] interleaved)
     for (int i = threadIdx.x; i < gsz.X(); i += kThreads) exz[i] = 0;
     __syncthreads();
@@ -587,17 +598,34 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
   }
 }
 
-// Used where two blocks fit an SM (up to 32x65x32): at 48x97x48 a block
-// needs 149 KB, one per SM, and the FFT kernels (two per SM) are faster,
-// also for an uneven batch, whose every instance runs at the largest
-// grid's shared memory.
+// The forward products' shared-memory plan: product planes per pass of the
+// forward modes (kPB, else one) and x-stage columns per chunk (the widest
+// multiple of 8), the first that lets two blocks share an SM; false if none
+// does (the FFT kernels then run).  48x97x48: one plane per pass, chunks of
+// 24 columns, 111 KB per block.
+bool fwd_tc_plan(const Grid& g, int optin, int& pb, int& xch) {
+  const FwdTcDims d = fwd_tc_dims(g);
+  const int pbs[2] = {kPB, 1};
+  for (int p : pbs)
+    for (int c = d.pzp; c >= 8; c -= 8)
+      if (2 * (fwd_tc_smem_bytes(g, p, c) + 4096) <= (size_t)optin + 4096) {
+        pb = p;
+        xch = c;
+        return true;
+      }
+  return false;
+}
+
 bool fwd_tc_fits(const Grid& g, int optin) {
-  return 2 * (fwd_tc_smem_bytes(g, kPB) + 4096) <= (size_t)optin + 4096;
+  int pb = 0, xch = 0;
+  return fwd_tc_plan(g, optin, pb, xch);
 }
 
 template <class S>
 static void launch_products_sizes(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
-  const size_t sm = fwd_tc_smem_bytes(g, products_per_pass(g, mode));
+  const FwdTcDims d = fwd_tc_dims(g);
+  const int xch = std::is_same<S, SizesRT>::value ? (g.fxch < d.pzp ? g.fxch : d.pzp) : d.pzp;
+  const size_t sm = fwd_tc_smem_bytes(g, products_per_pass(g, mode), xch);
   const dim3 grid(g.Q, a.ninst);
   constexpr bool M = std::is_same<S, SizesRT>::value;  // only the run-time sizes serve uneven batches
   if (products_per_pass(g, mode) == kPB) {
@@ -612,7 +640,7 @@ static void launch_products_sizes(const Grid& g, const ProdArgs& a, int mode, cu
 // Grid::fixed & FIXED_PRODUCTS: the build compiled for the grid's sizes
 // (32x65x32, 16x33x16; single-grid batches), else the run-time sizes
 cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
-  const bool fx = (g.fixed & FIXED_PRODUCTS) && !a.grids;
+  const bool fx = (g.fixed & FIXED_PRODUCTS) && !a.grids && g.fxch >= fwd_tc_dims(g).pzp;
   if (fx && sizes_match<Sizes32>(g)) launch_products_sizes<Sizes32>(g, a, mode, st);
   else if (fx && sizes_match<Sizes16>(g)) launch_products_sizes<Sizes16>(g, a, mode, st);
   else launch_products_sizes<SizesRT>(g, a, mode, st);
