@@ -372,7 +372,10 @@ __global__ void __launch_bounds__(NTHR, MINB) k_phys_inverse_tc(const __grid_con
       mx = fmax(mx, fabs(Pu[i]) * g.cfl1 + fabs(Pu[fs + i]) * c2 + fabs(Pu[2 * fs + i]) * g.cfl3);
     red[threadIdx.x] = mx;
     __syncthreads();
-    for (int w = NTHR / 2; w > 0; w >>= 1) {
+    constexpr int P2 = NTHR >= 256 ? 256 : (NTHR >= 128 ? 128 : 64);  // largest power of 2 <= NTHR
+    if (P2 < NTHR && threadIdx.x < NTHR - P2) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + P2]);
+    if (P2 < NTHR) __syncthreads();
+    for (int w = P2 / 2; w > 0; w >>= 1) {
       if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
       __syncthreads();
     }
@@ -655,10 +658,14 @@ bool phys_tc_fits(const Grid& g, int optin) {
 }
 
 // Builds of the kernel (Grid::tcminb; the autotuner times them, the results
-// are identical): 2 = two fields per pass, 256 threads, 2 blocks per SM (128
-// registers); 3 = the same for 3 blocks (80 registers, some spilled); 4 / 5 =
-// one field per pass in 128-thread blocks, 4 / 5 blocks per SM (half the
-// shared memory, more independent blocks per SM)
+// are identical): fields per pass, threads, blocks per SM (the register
+// budget) and the sizes, run-time (RT) or compiled for the grid (CT):
+//   2: 2 fields, 256 threads, 2 blocks, RT   3: the same at 3 blocks
+//   4: 1 field, 128 threads, 4 blocks, RT    5: the same at 5 blocks
+//   6: build 4, CT                           7: build 2, CT
+//   8: 1 field, 192 threads, 3 blocks, RT    9: build 8, CT
+// One field per pass halves the shared memory; 192 threads give the z
+// stage's six output tiles of a field one warp each.
 template <bool MULTI>
 static void launch_inverse_build(const Grid& g, const PhysArgs& a, cudaStream_t st) {
   const dim3 grid(g.Q, a.ninst);
@@ -669,14 +676,16 @@ static void launch_inverse_build(const Grid& g, const PhysArgs& a, cudaStream_t 
     case 3: k_phys_inverse_tc<MULTI, 3, 2, 256, RT><<<grid, 256, s2, st>>>(g, a); break;
     case 4: k_phys_inverse_tc<MULTI, 4, 1, 128, RT><<<grid, 128, s1, st>>>(g, a); break;
     case 5: k_phys_inverse_tc<MULTI, 5, 1, 128, RT><<<grid, 128, s1, st>>>(g, a); break;
+    case 8: k_phys_inverse_tc<MULTI, 3, 1, 192, RT><<<grid, 192, s1, st>>>(g, a); break;
     default: k_phys_inverse_tc<MULTI, 2, 2, 256, RT><<<grid, 256, s2, st>>>(g, a); break;
   }
 }
 
-// the specialised inverse builds (6: build 4, 7: build 2 with compile-time
-// sizes) for the grids of a single-grid batch with Sizes32 / Sizes16 sizes
-
 bool phys_tc_specialised(const Grid& g) { return sizes_match<Sizes32>(g) || sizes_match<Sizes16>(g); }
+
+// the run-time-size build a compile-time one stands for
+static int inverse_rt_build(int b) { return b == 6 ? 4 : (b == 7 ? 2 : (b == 9 ? 8 : b)); }
+static bool inverse_ct_build(int b) { return b == 6 || b == 7 || b == 9; }
 
 template <class S>
 static void launch_inverse_ct(const Grid& g, const PhysArgs& a, cudaStream_t st) {
@@ -684,23 +693,23 @@ static void launch_inverse_ct(const Grid& g, const PhysArgs& a, cudaStream_t st)
   const bool cfl = a.cfl_check != 0;
   if (g.tcminb == 6)
     k_phys_inverse_tc<false, 4, 1, 128, S><<<grid, 128, phys_tc_smem_bytes(g, cfl, 1), st>>>(g, a);
+  else if (g.tcminb == 9)
+    k_phys_inverse_tc<false, 3, 1, 192, S><<<grid, 192, phys_tc_smem_bytes(g, cfl, 1), st>>>(g, a);
   else
     k_phys_inverse_tc<false, 2, 2, 256, S><<<grid, 256, phys_tc_smem_bytes(g, cfl, 2), st>>>(g, a);
 }
 
 cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st) {
-  if (a.grids) {
-    Grid gr = g;
-    if (gr.tcminb > 5) gr.tcminb = gr.tcminb == 6 ? 4 : 2;
-    launch_inverse_build<true>(gr, a, st);
-  } else if (g.tcminb > 5 && sizes_match<Sizes32>(g)) {
+  const bool ct = inverse_ct_build(g.tcminb) && !a.grids;
+  if (ct && sizes_match<Sizes32>(g)) {
     launch_inverse_ct<Sizes32>(g, a, st);
-  } else if (g.tcminb > 5 && sizes_match<Sizes16>(g)) {
+  } else if (ct && sizes_match<Sizes16>(g)) {
     launch_inverse_ct<Sizes16>(g, a, st);
   } else {
     Grid gr = g;
-    if (gr.tcminb > 5) gr.tcminb = gr.tcminb == 6 ? 4 : 2;
-    launch_inverse_build<false>(gr, a, st);
+    gr.tcminb = inverse_rt_build(g.tcminb);
+    if (a.grids) launch_inverse_build<true>(gr, a, st);
+    else launch_inverse_build<false>(gr, a, st);
   }
   return cudaGetLastError();
 }
@@ -718,6 +727,10 @@ void prepare_phys_tc(int optin) {
   allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128, Sizes32>, optin);
   allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, Sizes32>, optin);
   allow_max_smem(k_phys_inverse_tc<false, 4, 1, 128, Sizes16>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 3, 1, 192, RT>, optin);
+  allow_max_smem(k_phys_inverse_tc<true, 3, 1, 192, RT>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 3, 1, 192, Sizes32>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 3, 1, 192, Sizes16>, optin);
   allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, Sizes16>, optin);
   allow_max_smem(k_products_tc<false, kPB, RT>, optin);
   allow_max_smem(k_products_tc<true, kPB, RT>, optin);

@@ -6,7 +6,8 @@ arithmetic.  The builds of the tensor-core inverse transform
 (CHN_INVERSE_BUILD: 2 = two fields per pass in 256-thread blocks at two
 blocks per SM, 3 = the same at three, 4 / 5 = one field per pass in
 128-thread blocks at four / five, 6 / 7 = builds 4 / 2 compiled for the
-sizes of 32x65x32 and 16x33x16) change how the columns of a plane are
+sizes of 32x65x32 and 16x33x16, 8 / 9 = one field per pass in 192-thread
+blocks at three, run-time / compiled sizes) change how the columns of a plane are
 grouped, not the digit sums or their rounding; nor do the builds of the
 products, reconstruction and solve kernels compiled for those sizes
 (CHN_FIXED_SIZES=1), nor the adjoint products' planes per pass (1 or 3,
@@ -96,7 +97,8 @@ def test_solve_tiles_give_the_same_bits(cc, gi):
     _same(a, b)
 
 
-@pytest.mark.parametrize("gi,build", [(0, "3"), (0, "4"), (0, "5"), (0, "6"), (0, "7"), (2, "4"), (2, "6"), (2, "7")])
+@pytest.mark.parametrize("gi,build", [(0, "3"), (0, "4"), (0, "5"), (0, "6"), (0, "7"), (0, "8"), (0, "9"),
+                                      (2, "4"), (2, "6"), (2, "7"), (2, "9")])
 def test_inverse_builds_give_the_same_bits(cc, gi, build):
     a, _ = _sweeps(cc, GRIDS[gi], {"CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
     b, _ = _sweeps(cc, GRIDS[gi], {"CHN_INVERSE_BUILD": build, "CHN_AUTOTUNE": "0"})
@@ -124,7 +126,7 @@ def test_autotuner_reports_its_choices(cc):
     assert report["solve_chosen"] in ("tile16", "tile8")
     assert report["solve_tile16"] > 0 and report["solve_tile8"] > 0
     assert report["chosen"].startswith("tc_inverse_")
-    for b in ("f2_b2", "f2_b3", "f1_b4", "f1_b5", "f1_b4_fixed", "f2_b2_fixed"):
+    for b in ("f2_b2", "f2_b3", "f1_b4", "f1_b5", "f1_b4_fixed", "f2_b2_fixed", "f1_t192_b3", "f1_t192_b3_fixed"):
         assert report["tc_inverse_" + b] > 0
     for part in ("products", "recon", "solve"):
         assert report[part + "_sizes"] in ("runtime", "fixed") and report[part + "_fixed_sizes"] > 0
