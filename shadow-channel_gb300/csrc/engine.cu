@@ -220,7 +220,8 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   // block per plane), compiled for the grid's sizes where it has them;
   // CHN_INVERSE_BUILD=2..7 fixes it (and skips that timing)
   const char* ib = getenv("CHN_INVERSE_BUILD");
-  g.tcminb = (ib && ib[0] >= '2' && ib[0] <= '9' && ib[1] == 0) ? ib[0] - '0' : (spec ? 7 : 2);
+  const int ibv = ib ? atoi(ib) : 0;
+  g.tcminb = (ibv >= 2 && ibv <= 12) ? ibv : (spec ? 7 : 2);
   // the adjoint products' planes per pass: 1 until the autotuner has timed
   // 1 and 3; CHN_ADJ_PRODUCTS_PER_PASS=1 or 3 fixes it
   const char* apb = getenv("CHN_ADJ_PRODUCTS_PER_PASS");
@@ -1044,6 +1045,9 @@ static const char* inverse_build_name(int b) {
     case 7: return "f2_b2_fixed";
     case 8: return "f1_t192_b3";
     case 9: return "f1_t192_b3_fixed";
+    case 10: return "f1_b5_fixed";
+    case 11: return "f1_t192_b4_fixed";
+    case 12: return "f1_t256_b3_fixed";
     default: return "f2_b2";
   }
 }
@@ -1073,7 +1077,7 @@ static bool autotune_transforms(Engine& e, Work& w) {
       if (ibforced) {
         cands.push_back({g.split, g.tvar, g.tcminb, 0, 0.f});
       } else {
-        const int rt[5] = {2, 3, 4, 5, 8}, ct[3] = {6, 7, 9};
+        const int rt[5] = {2, 3, 4, 5, 8}, ct[6] = {6, 7, 9, 10, 11, 12};
         for (int b : rt) cands.push_back({g.split, g.tvar, b, 0, 0.f});
         if (!w.gdev && phys_tc_specialised(g))
           for (int b : ct) cands.push_back({g.split, g.tvar, b, 0, 0.f});

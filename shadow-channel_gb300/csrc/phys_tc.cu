@@ -664,8 +664,11 @@ bool phys_tc_fits(const Grid& g, int optin) {
 //   4: 1 field, 128 threads, 4 blocks, RT    5: the same at 5 blocks
 //   6: build 4, CT                           7: build 2, CT
 //   8: 1 field, 192 threads, 3 blocks, RT    9: build 8, CT
+//  10: 1 field, 128 threads, 5 blocks, CT   11: 192 threads, 4 blocks, CT
+//  12: 1 field, 256 threads, 3 blocks, CT
 // One field per pass halves the shared memory; 192 threads give the z
-// stage's six output tiles of a field one warp each.
+// stage's six output tiles of a field one warp each; the compiled sizes
+// need fewer registers (96 at 5 blocks of 128 threads without spills).
 template <bool MULTI>
 static void launch_inverse_build(const Grid& g, const PhysArgs& a, cudaStream_t st) {
   const dim3 grid(g.Q, a.ninst);
@@ -684,19 +687,30 @@ static void launch_inverse_build(const Grid& g, const PhysArgs& a, cudaStream_t 
 bool phys_tc_specialised(const Grid& g) { return sizes_match<Sizes32>(g) || sizes_match<Sizes16>(g); }
 
 // the run-time-size build a compile-time one stands for
-static int inverse_rt_build(int b) { return b == 6 ? 4 : (b == 7 ? 2 : (b == 9 ? 8 : b)); }
-static bool inverse_ct_build(int b) { return b == 6 || b == 7 || b == 9; }
+static int inverse_rt_build(int b) {
+  switch (b) {
+    case 6: return 4;
+    case 7: return 2;
+    case 9: case 11: case 12: return 8;
+    case 10: return 5;
+    default: return b;
+  }
+}
+static bool inverse_ct_build(int b) { return b == 6 || b == 7 || b >= 9; }
 
 template <class S>
 static void launch_inverse_ct(const Grid& g, const PhysArgs& a, cudaStream_t st) {
   const dim3 grid(g.Q, a.ninst);
   const bool cfl = a.cfl_check != 0;
-  if (g.tcminb == 6)
-    k_phys_inverse_tc<false, 4, 1, 128, S><<<grid, 128, phys_tc_smem_bytes(g, cfl, 1), st>>>(g, a);
-  else if (g.tcminb == 9)
-    k_phys_inverse_tc<false, 3, 1, 192, S><<<grid, 192, phys_tc_smem_bytes(g, cfl, 1), st>>>(g, a);
-  else
-    k_phys_inverse_tc<false, 2, 2, 256, S><<<grid, 256, phys_tc_smem_bytes(g, cfl, 2), st>>>(g, a);
+  const size_t s1 = phys_tc_smem_bytes(g, cfl, 1);
+  switch (g.tcminb) {
+    case 6: k_phys_inverse_tc<false, 4, 1, 128, S><<<grid, 128, s1, st>>>(g, a); break;
+    case 9: k_phys_inverse_tc<false, 3, 1, 192, S><<<grid, 192, s1, st>>>(g, a); break;
+    case 10: k_phys_inverse_tc<false, 5, 1, 128, S><<<grid, 128, s1, st>>>(g, a); break;
+    case 11: k_phys_inverse_tc<false, 4, 1, 192, S><<<grid, 192, s1, st>>>(g, a); break;
+    case 12: k_phys_inverse_tc<false, 3, 1, 256, S><<<grid, 256, s1, st>>>(g, a); break;
+    default: k_phys_inverse_tc<false, 2, 2, 256, S><<<grid, 256, phys_tc_smem_bytes(g, cfl, 2), st>>>(g, a); break;
+  }
 }
 
 cudaError_t launch_phys_inverse_tc(const Grid& g, const PhysArgs& a, cudaStream_t st) {
@@ -731,6 +745,12 @@ void prepare_phys_tc(int optin) {
   allow_max_smem(k_phys_inverse_tc<true, 3, 1, 192, RT>, optin);
   allow_max_smem(k_phys_inverse_tc<false, 3, 1, 192, Sizes32>, optin);
   allow_max_smem(k_phys_inverse_tc<false, 3, 1, 192, Sizes16>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 5, 1, 128, Sizes32>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 192, Sizes32>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 3, 1, 256, Sizes32>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 5, 1, 128, Sizes16>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 4, 1, 192, Sizes16>, optin);
+  allow_max_smem(k_phys_inverse_tc<false, 3, 1, 256, Sizes16>, optin);
   allow_max_smem(k_phys_inverse_tc<false, 2, 2, 256, Sizes16>, optin);
   allow_max_smem(k_products_tc<false, kPB, RT>, optin);
   allow_max_smem(k_products_tc<true, kPB, RT>, optin);

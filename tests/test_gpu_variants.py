@@ -7,7 +7,9 @@ arithmetic.  The builds of the tensor-core inverse transform
 blocks per SM, 3 = the same at three, 4 / 5 = one field per pass in
 128-thread blocks at four / five, 6 / 7 = builds 4 / 2 compiled for the
 sizes of 32x65x32 and 16x33x16, 8 / 9 = one field per pass in 192-thread
-blocks at three, run-time / compiled sizes) change how the columns of a plane are
+blocks at three, run-time / compiled sizes, 10 / 11 / 12 = one field per
+pass compiled for the sizes in 128 / 192 / 256-thread blocks at five / four
+/ three) change how the columns of a plane are
 grouped, not the digit sums or their rounding; nor do the builds of the
 products, reconstruction and solve kernels compiled for those sizes
 (CHN_FIXED_SIZES=1), nor the adjoint products' planes per pass (1 or 3,
@@ -98,7 +100,8 @@ def test_solve_tiles_give_the_same_bits(cc, gi):
 
 
 @pytest.mark.parametrize("gi,build", [(0, "3"), (0, "4"), (0, "5"), (0, "6"), (0, "7"), (0, "8"), (0, "9"),
-                                      (2, "4"), (2, "6"), (2, "7"), (2, "9")])
+                                      (0, "10"), (0, "11"), (0, "12"), (2, "4"), (2, "6"), (2, "7"), (2, "9"),
+                                      (2, "12")])
 def test_inverse_builds_give_the_same_bits(cc, gi, build):
     a, _ = _sweeps(cc, GRIDS[gi], {"CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
     b, _ = _sweeps(cc, GRIDS[gi], {"CHN_INVERSE_BUILD": build, "CHN_AUTOTUNE": "0"})
