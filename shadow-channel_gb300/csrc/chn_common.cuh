@@ -104,9 +104,11 @@ struct Grid {
   const uint32_t* tcWT;
   const int* tcWTE;
   int tc;
-  // kx columns per block of the implicit solve (16 or 8; the autotuner's
-  // choice, the same results either way)
+  // kx columns per block of the implicit solve (16 or 8) and its threads
+  // (256, or 128 with 8 columns: 4 blocks per SM); the autotuner's choice,
+  // the same results either way
   int stile;
+  int sthr;
   // inverse transforms as DFT GEMMs on the tensor cores (phys_tc.cu), each
   // stage split radix-2 into even and odd modes where its length is even:
   // the z stage's matrix [2 pz / 2][even | odd modes (Re, Im)] and the x

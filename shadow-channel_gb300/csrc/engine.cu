@@ -228,8 +228,9 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   g.adjpb = (apb && apb[0] == '3') ? 3 : 1;
   // the solve's block tile: 16 until the autotuner has timed both;
   // CHN_SOLVE_TILE=8 or 16 fixes it (and skips that timing)
-  const char* stl = getenv("CHN_SOLVE_TILE");
+  const char* stl = getenv("CHN_SOLVE_TILE");  // 16, 8 or 8/128 (8 columns, 128 threads)
   g.stile = (stl && atoi(stl) == 8) ? 8 : 16;
+  g.sthr = (g.stile == 8 && stl && strstr(stl, "/128")) ? 128 : 256;
   // the inverse on tcgen05 where it fits: a candidate of the autotuner
   // (bit-identical results); CHN_INVERSE_TC5=1 forces it, =0 leaves it out
   const char* t5 = getenv("CHN_INVERSE_TC5");
@@ -1215,15 +1216,16 @@ static bool autotune_solve(Engine& e, Work& w) {
   sa.mdiv = w.ntan > 0 ? w.ntan : 1;
   sa.ninst = nt;
   sa.sdiv = w.ntan > 0 ? w.ntan : 1;
-  const int tiles[2] = {16, 8};
-  float ms[2] = {0.f, 0.f};
+  const int tiles[3] = {16, 8, 8}, thr[3] = {256, 256, 128};
+  float ms[3] = {0.f, 0.f, 0.f};
   cudaEvent_t t0, t1;
   CK(cudaEventCreate(&t0));
   CK(cudaEventCreate(&t1));
-  const int saved = g.stile;
+  const int saved = g.stile, saved_thr = g.sthr;
   bool ok = true;
-  for (int c = 0; c < 2 && ok; ++c) {
+  for (int c = 0; c < 3 && ok; ++c) {
     g.stile = tiles[c];
+    g.sthr = thr[c];
     ok = launch_solve(g, sa, e.st) == cudaSuccess;  // warm-up
     ok = ok && cudaEventRecord(t0, e.st) == cudaSuccess;
     for (int r = 0; r < 3 && ok; ++r) ok = launch_solve(g, sa, e.st) == cudaSuccess;
@@ -1233,16 +1235,22 @@ static bool autotune_solve(Engine& e, Work& w) {
   }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
-  g_launches += ok ? 8 : 0;
+  g_launches += ok ? 12 : 0;
   if (!ok) {
     g.stile = saved;
+    g.sthr = saved_thr;
     set_error(-1, "solve autotuner: %s", cudaGetErrorString(cudaGetLastError()));
     return false;
   }
-  g.stile = ms[1] < ms[0] ? 8 : 16;
-  char buf[160];
-  snprintf(buf, sizeof(buf), "\"solve_tile16\": %.4f, \"solve_tile8\": %.4f, \"solve_chosen\": \"tile%d\"", ms[0],
-           ms[1], g.stile);
+  int best = 0;
+  for (int c = 1; c < 3; ++c)
+    if (ms[c] < ms[best]) best = c;
+  g.stile = tiles[best];
+  g.sthr = thr[best];
+  char buf[200];
+  snprintf(buf, sizeof(buf),
+           "\"solve_tile16\": %.4f, \"solve_tile8\": %.4f, \"solve_tile8_t128\": %.4f, \"solve_chosen\": \"%s\"",
+           ms[0], ms[1], ms[2], best == 0 ? "tile16" : (best == 1 ? "tile8" : "tile8_t128"));
   if (g_tune_report.size() > 1 && g_tune_report.back() == '}') {
     g_tune_report.pop_back();
     g_tune_report += ", ";
@@ -2473,6 +2481,8 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
     gs[i].tci = gmax.tci;
     gs[i].tcf = gmax.tcf;
     gs[i].tcminb = gmax.tcminb;
+    gs[i].stile = gmax.stile;
+    gs[i].sthr = gmax.sthr;
     gs[i].adjpb = gmax.adjpb;
     gs[i].fwdpb = gmax.fwdpb;
     gs[i].fxch = gmax.fxch;

@@ -225,9 +225,10 @@ struct SolveSmem {
 // [7][2 kTile columns][KS] bf16 + kTile exponents
 __host__ __device__ inline size_t solve_tc_kstride(const Grid& g) { return (size_t)((g.Q + 15) / 16) * 16 + 8; }
 
+// the FP64 quadrature's parity-combined inputs only where it runs (g.tc = 0)
 template <int kTile>
 __host__ __device__ inline size_t solve_hc_elems(const Grid& g) {
-  size_t hc = (size_t)g.Qh * kTile * 6, r = 2 * (size_t)g.R * kTile;
+  size_t hc = g.tc ? 0 : (size_t)g.Qh * kTile * 6, r = 2 * (size_t)g.R * kTile;
   const size_t tc =
       ((size_t)kDig * 2 * kTile * solve_tc_kstride(g) * 2 + kTile * sizeof(int) + sizeof(cpx) - 1) / sizeof(cpx);
   if (r > hc) hc = r;
@@ -387,7 +388,7 @@ __device__ void quad_rhs(const Grid& g, const cpx* __restrict__ H, int z, int x0
 // of the FP64 version's parity-combined inputs), times the digit tables of
 // the weighted transposes; one FP64 rounding per contraction.
 //   Fa = Qpw P - K2 Qw Hy [+ Qppw Sa],   Fb = Rw G [+ Rpw Sb]
-template <int kTile, class S>
+template <int kTile, int NTHR, class S>
 __device__ void quad_rhs_tc(const Grid& g, const S& gsz, const cpx* __restrict__ H, int z, int x0, int nx, bool adj,
                             SolveSmem& s) {
   constexpr int NC = 2 * kTile;  // digit columns: Re, Im of each kx column
@@ -428,9 +429,9 @@ __device__ void quad_rhs_tc(const Grid& g, const S& gsz, const cpx* __restrict__
     const int N = toA ? gsz.D() : gsz.R();
     cpx* F = toA ? s.Fa : s.Fb;
     const bool first = (q == 0 || q == 3);
-    for (int i = threadIdx.x; i < kTile; i += kThreads) exc[i] = 0;
+    for (int i = threadIdx.x; i < kTile; i += NTHR) exc[i] = 0;
     __syncthreads();
-    if (KT <= kQuadRegs && kThreads == 16 * kTile) {
+    if (KT <= kQuadRegs && NTHR == 16 * kTile) {
       // thread t holds column t % kTile, planes t / kTile + 16 k (k < KT):
       // its inputs stay in registers from the exponent maximum to the digits
       const int col = threadIdx.x % kTile, y0 = threadIdx.x / kTile;
@@ -454,7 +455,7 @@ __device__ void quad_rhs_tc(const Grid& g, const S& gsz, const cpx* __restrict__
         digits_bf16(scaled56(vin[k].im, ex), dig + (size_t)(2 * col + 1) * KS + y, NC * KS);
       }
     } else {
-      for (int i = threadIdx.x; i < gsz.Q() * kTile; i += kThreads) {
+      for (int i = threadIdx.x; i < gsz.Q() * kTile; i += NTHR) {
         const int y = i / kTile, col = i - y * kTile;
         if (col >= nx) continue;
         const cpx v = input(q, y, col);
@@ -463,7 +464,7 @@ __device__ void quad_rhs_tc(const Grid& g, const S& gsz, const cpx* __restrict__
         if (e) atomicMax(&exc[col], e);
       }
       __syncthreads();
-      for (int i = threadIdx.x; i < KT * 16 * kTile; i += kThreads) {
+      for (int i = threadIdx.x; i < KT * 16 * kTile; i += NTHR) {
         const int y = i / kTile, col = i - y * kTile;
         const cpx v = (y < gsz.Q() && col < nx) ? input(q, y, col) : cpx{0.0, 0.0};
         const int ex = exc[col] - 1022;
@@ -473,7 +474,7 @@ __device__ void quad_rhs_tc(const Grid& g, const S& gsz, const cpx* __restrict__
     }
     __syncthreads();
     const int MTn = (N + 15) / 16;
-    for (int item = warp; item < MTn * NT; item += kThreads >> 5) {
+    for (int item = warp; item < MTn * NT; item += NTHR >> 5) {
       const int mt = item / NT, nt = item - mt * NT;
       const int col = nt * 4 + t, n = nt * 8 + gq;
       const int ecol = exc[min(col, kTile - 1)] - 1022;
@@ -538,9 +539,10 @@ __device__ void band_solve_chain(const double* __restrict__ LU, const double* __
 
 
 
-// S: the sizes (SizesRT, or SizesCT for a specialised grid)
-template <bool MULTI, int kTile, class S>
-__global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ Grid g0, SolveArgs a) {
+// S: the sizes (SizesRT, or SizesCT for a specialised grid); NTHR threads
+// (256, or 128 with the 8-column tile), MINB blocks per SM
+template <bool MULTI, int kTile, class S, int NTHR = kThreads, int MINB = 2>
+__global__ void __launch_bounds__(NTHR, MINB) k_solve(const __grid_constant__ Grid g0, SolveArgs a) {
   const int ntx = (g0.X + kTile - 1) / kTile;
   const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
   const int inst = blockIdx.y;
@@ -564,7 +566,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   auto cidx = [&](int v, int r, int x) { return (((size_t)z * 2 + v) * gsz.R() + r) * gsz.X() + x; };
   if (z == gsz.Nz() / 2) {
     // the Nz/2 line is zeroed every substage and never stored (channel/channel.c:460-467)
-    for (int i = threadIdx.x; i < 2 * gsz.R() * nx; i += kThreads) {
+    for (int i = threadIdx.x; i < 2 * gsz.R() * nx; i += NTHR) {
       const int v = i / (gsz.R() * nx), r = (i / nx) % gsz.R(), x = x0 + i % nx;
       Cc[cidx(v, r, x)] = cpx{0.0, 0.0};
       So[cidx(v, r, x)] = cpx{0.0, 0.0};
@@ -576,7 +578,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   const RKc rk = rk_coeffs(a.k, a.adjoint);
   const bool adj = a.adjoint != 0;
   const cpx* __restrict__ H = a.H.at(inst);
-  if (g.tc) quad_rhs_tc<kTile>(g, gsz, H, z, x0, nx, adj, s);
+  if (g.tc) quad_rhs_tc<kTile, NTHR>(g, gsz, H, z, x0, nx, adj, s);
   else quad_rhs<kTile>(g, H, z, x0, nx, adj, s);
   const double dt = g.dt;
   const int xfirst = (z == 0 && x0 == 0) ? 1 : 0;  // the mean mode has its own system
@@ -602,7 +604,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     // C += dt Mass^-1 F MC[3n+1] with F_alpha = -re^2 Dv, F_beta = re^2 (Rps + K2 Rs)
     __syncthreads();
     const cpx* x1 = xk + csz;
-    for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
+    for (int i = threadIdx.x; i < gsz.R() * kTile; i += NTHR) {
       const int r = i / kTile, l = i - r * kTile;
       if (l >= nx || l < xfirst) continue;
       const int x = x0 + l;
@@ -631,7 +633,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
       }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
+    for (int i = threadIdx.x; i < gsz.R() * kTile; i += NTHR) {
       const int r = i / kTile, l = i - r * kTile;
       if (l >= nx || l < xfirst) continue;
       const int x = x0 + l;
@@ -647,7 +649,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     __syncthreads();
   }
   // right-hand sides (channel/project.c:60-81, 125-130, 143-163, 202-207)
-  for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
+  for (int i = threadIdx.x; i < gsz.R() * kTile; i += NTHR) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx || l < xfirst) continue;
     const int x = x0 + l;
@@ -828,7 +830,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     }
   }
   // state rows: alpha from the solve (rows >= Ny-4 carried), beta from the solve
-  for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
+  for (int i = threadIdx.x; i < gsz.R() * kTile; i += NTHR) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx || l < xfirst) continue;
     const int x = x0 + l;
@@ -843,7 +845,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   __syncthreads();
   if (a.k == 2) {
     // the carried array is the state after the last substage
-    for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
+    for (int i = threadIdx.x; i < gsz.R() * kTile; i += NTHR) {
       const int r = i / kTile, l = i - r * kTile;
       if (l >= nx) continue;
       const int x = x0 + l;
@@ -857,7 +859,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   //  channel/adjproject.c:393-549)
   if (adj) {
     __syncthreads();
-    if (g.tc) quad_rhs_tc<kTile>(g, gsz, a.Hprev.at(inst), z, x0, nx, true, s);
+    if (g.tc) quad_rhs_tc<kTile, NTHR>(g, gsz, a.Hprev.at(inst), z, x0, nx, true, s);
     else quad_rhs<kTile>(g, a.Hprev.at(inst), z, x0, nx, true, s);
     if (xfirst == 1 && threadIdx.x < 32) {
       // mean mode fa/fb from the previous-stage terms (channel/adjproject0.c:254-294)
@@ -883,7 +885,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   // adjoint's second quadrature overwrote them (they share its digit
   // buffer); the results go to Fa, Fb (each element read and written by one
   // thread)
-  for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
+  for (int i = threadIdx.x; i < gsz.R() * kTile; i += NTHR) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx || l < xfirst) continue;
     const int x = x0 + l;
@@ -920,7 +922,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < gsz.R() * kTile; i += kThreads) {
+  for (int i = threadIdx.x; i < gsz.R() * kTile; i += NTHR) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx) continue;
     const int x = x0 + l;
@@ -935,17 +937,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const __grid_constant__ G
   }
 }
 
-template <int T, class S>
+template <int T, class S, int NTHR = kThreads, int MINB = 2>
 static void launch_solve_t(const Grid& g, const SolveArgs& a, cudaStream_t st) {
   const int ntx = (g.X + T - 1) / T;
   const dim3 grid(g.Nz * ntx, a.ninst);
-  if (a.grids) k_solve<true, T, SizesRT><<<grid, kThreads, solve_smem_bytes_t<T>(g), st>>>(g, a);
-  else k_solve<false, T, S><<<grid, kThreads, solve_smem_bytes_t<T>(g), st>>>(g, a);
+  if (a.grids) k_solve<true, T, SizesRT, NTHR, MINB><<<grid, NTHR, solve_smem_bytes_t<T>(g), st>>>(g, a);
+  else k_solve<false, T, S, NTHR, MINB><<<grid, NTHR, solve_smem_bytes_t<T>(g), st>>>(g, a);
 }
 
+// Grid::stile 16 or 8 columns in 256-thread blocks, or 8 columns in
+// 128-thread blocks at 4 per SM (Grid::sthr 128)
 template <class S>
 static void launch_solve_s(const Grid& g, const SolveArgs& a, cudaStream_t st) {
-  if (g.stile == 8) launch_solve_t<8, S>(g, a, st);
+  if (g.stile == 8 && g.sthr == 128) launch_solve_t<8, S, 128, 4>(g, a, st);
+  else if (g.stile == 8) launch_solve_t<8, S>(g, a, st);
   else launch_solve_t<16, S>(g, a, st);
 }
 
@@ -971,6 +976,10 @@ void prepare_recon_solve(int optin) {
   allow_max_smem(k_solve<false, 8, Sizes32>, optin);
   allow_max_smem(k_solve<false, 16, Sizes16>, optin);
   allow_max_smem(k_solve<false, 8, Sizes16>, optin);
+  allow_max_smem(k_solve<false, 8, SizesRT, 128, 4>, optin);
+  allow_max_smem(k_solve<true, 8, SizesRT, 128, 4>, optin);
+  allow_max_smem(k_solve<false, 8, Sizes32, 128, 4>, optin);
+  allow_max_smem(k_solve<false, 8, Sizes16, 128, 4>, optin);
 }
 
 }  // namespace chn

@@ -1,8 +1,8 @@
 """Kernel variants the autotuner chooses among give the same bits.
 
-The implicit solve's block tile (kx columns per block: 16 or 8,
-CHN_SOLVE_TILE) changes which columns share a block, not any column's
-arithmetic.  The builds of the tensor-core inverse transform
+The implicit solve's block tile (kx columns per block: 16 or 8, and 8 in
+128-thread blocks; CHN_SOLVE_TILE=16, 8, 8/128) changes which columns share
+a block, not any column's arithmetic.  The builds of the tensor-core inverse transform
 (CHN_INVERSE_BUILD: 2 = two fields per pass in 256-thread blocks at two
 blocks per SM, 3 = the same at three, 4 / 5 = one field per pass in
 128-thread blocks at four / five, 6 / 7 = builds 4 / 2 compiled for the
@@ -92,10 +92,10 @@ def _same(a, b):
         assert np.array_equal(x.view(np.float64), y.view(np.float64))
 
 
-@pytest.mark.parametrize("gi", [0, 1])
-def test_solve_tiles_give_the_same_bits(cc, gi):
+@pytest.mark.parametrize("gi,tile", [(0, "8"), (0, "8/128"), (1, "8"), (1, "8/128"), (2, "8/128")])
+def test_solve_tiles_give_the_same_bits(cc, gi, tile):
     a, _ = _sweeps(cc, GRIDS[gi], {"CHN_SOLVE_TILE": "16"})
-    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_SOLVE_TILE": "8"})
+    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_SOLVE_TILE": tile})
     _same(a, b)
 
 
@@ -126,7 +126,7 @@ def test_autotuner_reports_its_choices(cc):
     res, report = _sweeps(cc, GRIDS[0], {})
     if "solve_chosen" not in report:
         pytest.skip("autotuner off (CHN_AUTOTUNE=0)")
-    assert report["solve_chosen"] in ("tile16", "tile8")
+    assert report["solve_chosen"] in ("tile16", "tile8", "tile8_t128")
     assert report["solve_tile16"] > 0 and report["solve_tile8"] > 0
     assert report["chosen"].startswith("tc_inverse_")
     for b in ("f2_b2", "f2_b3", "f1_b4", "f1_b5", "f1_b4_fixed", "f2_b2_fixed", "f1_t192_b3", "f1_t192_b3_fixed"):
