@@ -231,6 +231,10 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   const char* stl = getenv("CHN_SOLVE_TILE");  // 16, 8 or 8/128 (8 columns, 128 threads)
   g.stile = (stl && atoi(stl) == 8) ? 8 : 16;
   g.sthr = (g.stile == 8 && stl && strstr(stl, "/128")) ? 128 : 256;
+  // the tensor-core reconstruction's tile: 16 columns until the autotuner
+  // has timed 16 and 8 (128-thread blocks); CHN_RECON_TILE fixes it
+  const char* rtl = getenv("CHN_RECON_TILE");
+  g.rtile = (rtl && atoi(rtl) == 8) ? 8 : 16;
   // the inverse on tcgen05 where it fits: a candidate of the autotuner
   // (bit-identical results); CHN_INVERSE_TC5=1 forces it, =0 leaves it out
   const char* t5 = getenv("CHN_INVERSE_TC5");
@@ -1268,7 +1272,8 @@ static bool autotune_solve(Engine& e, Work& w) {
 // solve (a tangent solve into scratch), each timed against its run-time-
 // size build and kept where faster (Grid::fixed).  CHN_FIXED_SIZES=0 / 1
 // fixes all three off / on.  Then the adjoint products' planes per pass,
-// 1 or 3 (Grid::adjpb; CHN_ADJ_PRODUCTS_PER_PASS fixes it).
+// 1 or 3 (Grid::adjpb; CHN_ADJ_PRODUCTS_PER_PASS fixes it), and the
+// reconstruction's tile, 16 or 8 columns (Grid::rtile; CHN_RECON_TILE).
 static bool autotune_fixed(Engine& e, Work& w) {
   const char* off = getenv("CHN_AUTOTUNE");
   const char* forced = getenv("CHN_FIXED_SIZES");
@@ -1276,7 +1281,9 @@ static bool autotune_fixed(Engine& e, Work& w) {
   const char* apb = getenv("CHN_ADJ_PRODUCTS_PER_PASS");
   const bool do_fixed = !(forced && forced[0]) && !w.gdev && phys_tc_specialised(g);
   const bool do_pb = g.tcf && !(apb && apb[0]) && !w.gdev;
-  if ((off && off[0] == '0') || !(do_fixed || do_pb)) return true;
+  const char* rtl = getenv("CHN_RECON_TILE");
+  const bool do_rt = g.tc && !(rtl && rtl[0]) && !w.gdev;
+  if ((off && off[0] == '0') || !(do_fixed || do_pb || do_rt)) return true;
   const int nt = w.nseg * (w.ntan > 0 ? w.ntan : 1);
   ProdArgs f{};
   f.Pp = cbd(w.Pp, w.psz);
@@ -1373,6 +1380,31 @@ static bool autotune_fixed(Engine& e, Work& w) {
       rep += buf;
     } else {
       g.adjpb = saved_pb;
+    }
+  }
+  // the reconstruction's tile (16 columns in 256 threads or 8 in 128)
+  if (ok && do_rt) {
+    const int saved_t = g.rtile;
+    float ms[2] = {0.f, 0.f};
+    const int tiles[2] = {16, 8};
+    for (int c = 0; c < 2 && ok; ++c) {
+      g.rtile = tiles[c];
+      ok = enqueue(FIXED_RECON);  // warm-up
+      ok = ok && cudaEventRecord(t0, e.st) == cudaSuccess;
+      for (int k = 0; k < 3 && ok; ++k) ok = enqueue(FIXED_RECON);
+      ok = ok && cudaEventRecord(t1, e.st) == cudaSuccess && cudaEventSynchronize(t1) == cudaSuccess;
+      if (ok) cudaEventElapsedTime(&ms[c], t0, t1);
+      ms[c] /= 3;
+    }
+    if (ok) {
+      g_launches += 8;
+      g.rtile = ms[1] < ms[0] ? 8 : 16;
+      snprintf(buf, sizeof(buf), "\"recon_tile16\": %.4f, \"recon_tile8\": %.4f, \"recon_tile\": %d", ms[0], ms[1],
+               g.rtile);
+      if (!rep.empty()) rep += ", ";
+      rep += buf;
+    } else {
+      g.rtile = saved_t;
     }
   }
   cudaEventDestroy(t0);

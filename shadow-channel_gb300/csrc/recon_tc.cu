@@ -139,29 +139,33 @@ bool build_adj_tc_tables(const HostTables& h, std::vector<uint32_t>& btfrag, std
 
 __host__ __device__ inline int recon_tc_kstride(int KT) { return KT * 16 + 8; }  // bf16 per digit row (padded)
 
-size_t recon_tc_smem_bytes(const Grid& g) {
+// tile: kx columns per block (16 or 8)
+size_t recon_tc_smem_bytes(const Grid& g, int tile) {
   const int KT = (g.R + 15) / 16;
-  return (size_t)2 * kDig * 32 * recon_tc_kstride(KT) * sizeof(uint16_t) + 2 * kTile * sizeof(int);
+  return (size_t)2 * kDig * (2 * tile) * recon_tc_kstride(KT) * sizeof(uint16_t) + 2 * tile * sizeof(int);
 }
 
-// S: the sizes (SizesRT, or SizesCT for a specialised grid)
-template <bool MULTI, class S>
-__global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant__ Grid g0, ReconArgs a) {
-  const int ntx = (g0.X + kTile - 1) / kTile;
+size_t recon_tc_smem_bytes(const Grid& g) { return recon_tc_smem_bytes(g, kTile); }
+
+// S: the sizes (SizesRT, or SizesCT for a specialised grid); TILE kx
+// columns per block (2 TILE real digit columns) in NTHR = 16 TILE threads
+template <bool MULTI, class S, int TILE = kTile, int NTHR = kThreads, int MINB = 2>
+__global__ void __launch_bounds__(NTHR, MINB) k_recon_tc(const __grid_constant__ Grid g0, ReconArgs a) {
+  const int ntx = (g0.X + TILE - 1) / TILE;
   const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
   const int inst = blockIdx.y;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
   const S gsz(g);
-  if (z >= gsz.Nz() || tx * kTile >= gsz.X()) return;
+  if (z >= gsz.Nz() || tx * TILE >= gsz.X()) return;
   if (z == gsz.Nz() / 2) return;  // never read (channel/pass1.c:51-85 skips it)
   if (a.status != nullptr && (a.status[inst / a.sdiv] & ST_CFL) != 0) return;
-  const int x0 = tx * kTile;
-  const int nx = min(kTile, gsz.X() - x0);
+  const int x0 = tx * TILE;
+  const int nx = min(TILE, gsz.X() - x0);
   const int KT = (gsz.R() + 15) / 16, KS = recon_tc_kstride(KT), MT = (gsz.Q() + 15) / 16;
   const bool meancol = (z == 0 && x0 == 0);  // column 0 of this tile is the mean mode
   extern __shared__ __align__(16) unsigned char smem[];
-  uint16_t* dig = reinterpret_cast<uint16_t*>(smem);  // [cls][digit][n 32][KS]
-  int* exc = reinterpret_cast<int*>(smem + (size_t)2 * kDig * 32 * KS * sizeof(uint16_t));  // [cls][16]
+  uint16_t* dig = reinterpret_cast<uint16_t*>(smem);  // [cls][digit][n 2 TILE][KS]
+  int* exc = reinterpret_cast<int*>(smem + (size_t)2 * kDig * (2 * TILE) * KS * sizeof(uint16_t));  // [cls][TILE]
   const cpx* __restrict__ C = a.C.at(inst);
   if (a.slot.stride) C += (long long)a.slot.slot() * a.slot.stride;
   auto cval = [&](int cls, int j, int col) -> cpx {
@@ -170,13 +174,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
     return C[(((size_t)z * 2 + cls) * gsz.R() + j) * gsz.X() + x0 + col];
   };
   // column exponents: |c| < 2^exc over the column's real and imaginary parts
-  for (int i = threadIdx.x; i < 2 * kTile; i += kThreads) exc[i] = 0;
+  for (int i = threadIdx.x; i < 2 * TILE; i += NTHR) exc[i] = 0;
   __syncthreads();
-  const int nent = 2 * (KT * 16) * kTile;
-  if (KT <= kReconRegs && kThreads == 16 * kTile) {
-    // thread t holds column t % kTile, rows t / kTile + 16 k of both classes:
+  const int nent = 2 * (KT * 16) * TILE;
+  if (KT <= kReconRegs && NTHR == 16 * TILE) {
+    // thread t holds column t % TILE, rows t / TILE + 16 k of both classes:
     // its coefficients stay in registers from the exponent maxima to the digits
-    const int col = threadIdx.x % kTile, j0 = threadIdx.x / kTile;
+    const int col = threadIdx.x % TILE, j0 = threadIdx.x / TILE;
     cpx vin[2][kReconRegs];
     int emax[2] = {0, 0};
 #pragma unroll
@@ -189,36 +193,36 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
       }
 #pragma unroll
     for (int cls = 0; cls < 2; ++cls)
-      if (emax[cls]) atomicMax(&exc[cls * kTile + col], emax[cls]);
+      if (emax[cls]) atomicMax(&exc[cls * TILE + col], emax[cls]);
     __syncthreads();
 #pragma unroll
     for (int cls = 0; cls < 2; ++cls) {
-      const int ex = exc[cls * kTile + col] - 1022;
+      const int ex = exc[cls * TILE + col] - 1022;
 #pragma unroll
       for (int k = 0; k < kReconRegs; ++k) {
         if (k >= KT) break;
-        for (int p = 0; p < 2; ++p)  // digit q of column n at dig[((cls * 7 + q) * 32 + n) * KS + j]
+        for (int p = 0; p < 2; ++p)  // digit q of column n at dig[((cls * 7 + q) * 2 TILE + n) * KS + j]
           digits_bf16(scaled56(p ? vin[cls][k].im : vin[cls][k].re, ex),
-                      dig + ((size_t)cls * kDig * 32 + 2 * col + p) * KS + j0 + 16 * k, (size_t)32 * KS);
+                      dig + ((size_t)cls * kDig * (2 * TILE) + 2 * col + p) * KS + j0 + 16 * k, (size_t)(2 * TILE) * KS);
       }
     }
   } else {
-    for (int i = threadIdx.x; i < nent; i += kThreads) {
-      const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
+    for (int i = threadIdx.x; i < nent; i += NTHR) {
+      const int cls = i / ((KT * 16) * TILE), r = i - cls * (KT * 16) * TILE, j = r / TILE, col = r - j * TILE;
       const cpx v = cval(cls, j, col);
       const int e1 = (int)((__double_as_longlong(v.re) >> 52) & 0x7FF);
       const int e2 = (int)((__double_as_longlong(v.im) >> 52) & 0x7FF);
       const int e = max(e1, e2);
-      if (e) atomicMax(&exc[cls * kTile + col], e);
+      if (e) atomicMax(&exc[cls * TILE + col], e);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nent; i += kThreads) {
-      const int cls = i / ((KT * 16) * kTile), r = i - cls * (KT * 16) * kTile, j = r / kTile, col = r - j * kTile;
+    for (int i = threadIdx.x; i < nent; i += NTHR) {
+      const int cls = i / ((KT * 16) * TILE), r = i - cls * (KT * 16) * TILE, j = r / TILE, col = r - j * TILE;
       const cpx v = cval(cls, j, col);
-      const int ex = exc[cls * kTile + col] - 1022;
-      for (int p = 0; p < 2; ++p)  // digit q of column n at dig[((cls * 7 + q) * 32 + n) * KS + j]
-        digits_bf16(scaled56(p ? v.im : v.re, ex), dig + ((size_t)cls * kDig * 32 + 2 * col + p) * KS + j,
-                    (size_t)32 * KS);
+      const int ex = exc[cls * TILE + col] - 1022;
+      for (int p = 0; p < 2; ++p)  // digit q of column n at dig[((cls * 7 + q) * 2 TILE + n) * KS + j]
+        digits_bf16(scaled56(p ? v.im : v.re, ex), dig + ((size_t)cls * kDig * (2 * TILE) + 2 * col + p) * KS + j,
+                    (size_t)(2 * TILE) * KS);
     }
   }
   __syncthreads();
@@ -229,7 +233,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
   cpx* __restrict__ U = a.U.at(inst);
   const size_t cs = (size_t)gsz.Q() * gsz.X();
   const int order[5] = {0, 1, 3, 2, 4};
-  for (int item = warp; item < MT * NT; item += kThreads >> 5) {
+  for (int item = warp; item < MT * NT; item += NTHR >> 5) {
     const int mt = item / NT, nt = item - mt * NT;
     const int col = nt * 4 + t;  // this thread's complex column
     const int n = nt * 8 + gq;   // the B-fragment column this thread loads
@@ -237,10 +241,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
     for (int ob = 0; ob < 5; ++ob) {
       const int b = order[ob], cls = b < 3 ? 0 : 1;
       const int KTb = ((cls == 0 ? gsz.D() : gsz.R()) + 15) / 16;
-      const int ecol = exc[cls * kTile + col] - 1022;
+      const int ecol = exc[cls * TILE + col] - 1022;
       long long H[4], L[4];
-      tc_tile_pf(A + (size_t)b * MT * KT * kDig * 32, mt, KT, KTb, dig + (size_t)cls * kDig * 32 * KS, KS,
-                 (size_t)32 * KS, n, lane, t, H, L);
+      tc_tile_pf(A + (size_t)b * MT * KT * kDig * 32, mt, KT, KTb, dig + (size_t)cls * kDig * (2 * TILE) * KS, KS,
+                 (size_t)(2 * TILE) * KS, n, lane, t, H, L);
 #pragma unroll
       for (int rr = 0; rr < 2; ++rr) {
         const int y = mt * 16 + gq + 8 * rr;
@@ -271,7 +275,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
   if (meancol) {
     // (kx, kz) = (0, 0): u = R a, du = R' a, v = 0, w = R b, dw = R' b
     // (channel/initAlphaBeta2.c:25-68), direct FP64
-    for (int y = threadIdx.x; y < gsz.Q(); y += kThreads) {
+    for (int y = threadIdx.x; y < gsz.Q(); y += NTHR) {
       double ur = 0, ui = 0, dur = 0, dui = 0, wr = 0, wi = 0, dwr = 0, dwi = 0;
       for (int j = 0; j < gsz.R(); ++j) {
         const double r = __ldg(g.Br + (size_t)y * gsz.R() + j), rp = __ldg(g.Brp + (size_t)y * gsz.R() + j);
@@ -291,8 +295,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_recon_tc(const __grid_constant_
   }
 }
 
+// Grid::rtile 16: 16-column tiles in 256-thread blocks; 8: 8-column tiles
+// in 128-thread blocks at 4 per SM (single-grid batches)
 template <class S>
 static void launch_recon_sizes(const Grid& g, const ReconArgs& a, cudaStream_t st) {
+  if (g.rtile == 8 && !a.grids) {
+    const int ntx = (g.X + 7) / 8;
+    k_recon_tc<false, S, 8, 128, 4><<<dim3(g.Nz * ntx, a.ninst), 128, recon_tc_smem_bytes(g, 8), st>>>(g, a);
+    return;
+  }
   const int ntx = (g.X + kTile - 1) / kTile;
   const size_t sm = recon_tc_smem_bytes(g);
   if (a.grids) k_recon_tc<true, SizesRT><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
@@ -313,6 +324,9 @@ void prepare_recon_tc(int optin) {
   allow_max_smem(k_recon_tc<true, SizesRT>, optin);
   allow_max_smem(k_recon_tc<false, Sizes32>, optin);
   allow_max_smem(k_recon_tc<false, Sizes16>, optin);
+  allow_max_smem(k_recon_tc<false, SizesRT, 8, 128, 4>, optin);
+  allow_max_smem(k_recon_tc<false, Sizes32, 8, 128, 4>, optin);
+  allow_max_smem(k_recon_tc<false, Sizes16, 8, 128, 4>, optin);
 }
 
 }  // namespace chn
