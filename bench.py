@@ -187,10 +187,10 @@ def segment_step_flops(g):
 
 # ncu DRAM bytes (read + write) of one instance of a 24-instance launch at
 # 32x65x32 (traffic grows with the instance count; the ncu capture of the
-# 8-segment bench case): k_phys_inverse_tc 298.3 MB (95.3 read + 203.0
-# write), k_products_tc tangent mode 388.0 MB (343.6 + 44.5)
-PHYS_TRAFFIC_PER_INSTANCE_32 = 298.3e6 / 24
-PROD_TRAFFIC_PER_INSTANCE_32 = 388.0e6 / 24
+# 8-segment bench case): k_phys_inverse_tc 306.1 MB (97.2 read + 208.9
+# write), k_products_tc tangent mode 387.9 MB (343.6 + 44.3)
+PHYS_TRAFFIC_PER_INSTANCE_32 = 306.1e6 / 24
+PROD_TRAFFIC_PER_INSTANCE_32 = 387.9e6 / 24
 
 
 def products_fwd_flops(ninst, g):
