@@ -109,7 +109,8 @@ struct Grid {
   // the same results either way
   int stile;
   int sthr;
-  int rtile;  // kx columns per block of the tensor-core reconstruction (16, or 8 in 128-thread blocks; autotuned)
+  int rbuild;  // tensor-core reconstruction: 0 = 16 columns, 256 threads; 1 = 8 columns, 128 threads;
+               // 2 = 16 columns at 3 blocks per SM (autotuned)
   // inverse transforms as DFT GEMMs on the tensor cores (phys_tc.cu), each
   // stage split radix-2 into even and odd modes where its length is even:
   // the z stage's matrix [2 pz / 2][even | odd modes (Re, Im)] and the x

@@ -231,10 +231,10 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   const char* stl = getenv("CHN_SOLVE_TILE");  // 16, 8 or 8/128 (8 columns, 128 threads)
   g.stile = (stl && atoi(stl) == 8) ? 8 : 16;
   g.sthr = (g.stile == 8 && stl && strstr(stl, "/128")) ? 128 : 256;
-  // the tensor-core reconstruction's tile: 16 columns until the autotuner
-  // has timed 16 and 8 (128-thread blocks); CHN_RECON_TILE fixes it
-  const char* rtl = getenv("CHN_RECON_TILE");
-  g.rtile = (rtl && atoi(rtl) == 8) ? 8 : 16;
+  // the tensor-core reconstruction's build (recon_tc.cu): 0 until the
+  // autotuner has timed 0, 1, 2; CHN_RECON_BUILD fixes it
+  const char* rbe = getenv("CHN_RECON_BUILD");
+  g.rbuild = (rbe && rbe[0] >= '0' && rbe[0] <= '2' && rbe[1] == 0) ? rbe[0] - '0' : 0;
   // the inverse on tcgen05 where it fits: a candidate of the autotuner
   // (bit-identical results); CHN_INVERSE_TC5=1 forces it, =0 leaves it out
   const char* t5 = getenv("CHN_INVERSE_TC5");
@@ -1273,7 +1273,7 @@ static bool autotune_solve(Engine& e, Work& w) {
 // size build and kept where faster (Grid::fixed).  CHN_FIXED_SIZES=0 / 1
 // fixes all three off / on.  Then the adjoint products' planes per pass,
 // 1 or 3 (Grid::adjpb; CHN_ADJ_PRODUCTS_PER_PASS fixes it), and the
-// reconstruction's tile, 16 or 8 columns (Grid::rtile; CHN_RECON_TILE).
+// reconstruction's build, tile and blocks per SM (Grid::rbuild; CHN_RECON_BUILD).
 static bool autotune_fixed(Engine& e, Work& w) {
   const char* off = getenv("CHN_AUTOTUNE");
   const char* forced = getenv("CHN_FIXED_SIZES");
@@ -1281,8 +1281,8 @@ static bool autotune_fixed(Engine& e, Work& w) {
   const char* apb = getenv("CHN_ADJ_PRODUCTS_PER_PASS");
   const bool do_fixed = !(forced && forced[0]) && !w.gdev && phys_tc_specialised(g);
   const bool do_pb = g.tcf && !(apb && apb[0]) && !w.gdev;
-  const char* rtl = getenv("CHN_RECON_TILE");
-  const bool do_rt = g.tc && !(rtl && rtl[0]) && !w.gdev;
+  const char* rbe = getenv("CHN_RECON_BUILD");
+  const bool do_rt = g.tc && !(rbe && rbe[0]) && !w.gdev;
   if ((off && off[0] == '0') || !(do_fixed || do_pb || do_rt)) return true;
   const int nt = w.nseg * (w.ntan > 0 ? w.ntan : 1);
   ProdArgs f{};
@@ -1382,13 +1382,12 @@ static bool autotune_fixed(Engine& e, Work& w) {
       g.adjpb = saved_pb;
     }
   }
-  // the reconstruction's tile (16 columns in 256 threads or 8 in 128)
+  // the reconstruction's build (tile, threads, blocks per SM)
   if (ok && do_rt) {
-    const int saved_t = g.rtile;
-    float ms[2] = {0.f, 0.f};
-    const int tiles[2] = {16, 8};
-    for (int c = 0; c < 2 && ok; ++c) {
-      g.rtile = tiles[c];
+    const int saved_t = g.rbuild;
+    float ms[3] = {0.f, 0.f, 0.f};
+    for (int c = 0; c < 3 && ok; ++c) {
+      g.rbuild = c;
       ok = enqueue(FIXED_RECON);  // warm-up
       ok = ok && cudaEventRecord(t0, e.st) == cudaSuccess;
       for (int k = 0; k < 3 && ok; ++k) ok = enqueue(FIXED_RECON);
@@ -1397,14 +1396,17 @@ static bool autotune_fixed(Engine& e, Work& w) {
       ms[c] /= 3;
     }
     if (ok) {
-      g_launches += 8;
-      g.rtile = ms[1] < ms[0] ? 8 : 16;
-      snprintf(buf, sizeof(buf), "\"recon_tile16\": %.4f, \"recon_tile8\": %.4f, \"recon_tile\": %d", ms[0], ms[1],
-               g.rtile);
+      g_launches += 12;
+      int best = 0;
+      for (int c = 1; c < 3; ++c)
+        if (ms[c] < ms[best]) best = c;
+      g.rbuild = best;
+      snprintf(buf, sizeof(buf), "\"recon_b0\": %.4f, \"recon_b1\": %.4f, \"recon_b2\": %.4f, \"recon_build\": %d",
+               ms[0], ms[1], ms[2], g.rbuild);
       if (!rep.empty()) rep += ", ";
       rep += buf;
     } else {
-      g.rtile = saved_t;
+      g.rbuild = saved_t;
     }
   }
   cudaEventDestroy(t0);

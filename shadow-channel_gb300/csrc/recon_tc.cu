@@ -243,8 +243,12 @@ __global__ void __launch_bounds__(NTHR, MINB) k_recon_tc(const __grid_constant__
       const int KTb = ((cls == 0 ? gsz.D() : gsz.R()) + 15) / 16;
       const int ecol = exc[cls * TILE + col] - 1022;
       long long H[4], L[4];
-      tc_tile_pf(A + (size_t)b * MT * KT * kDig * 32, mt, KT, KTb, dig + (size_t)cls * kDig * (2 * TILE) * KS, KS,
-                 (size_t)(2 * TILE) * KS, n, lane, t, H, L);
+      if constexpr (MINB > 2)
+        tc_tile_range(A + (size_t)b * MT * KT * kDig * 32, mt, KT, 0, KTb, dig + (size_t)cls * kDig * (2 * TILE) * KS,
+                      KS, (size_t)(2 * TILE) * KS, n, lane, t, H, L);
+      else
+        tc_tile_pf(A + (size_t)b * MT * KT * kDig * 32, mt, KT, KTb, dig + (size_t)cls * kDig * (2 * TILE) * KS, KS,
+                   (size_t)(2 * TILE) * KS, n, lane, t, H, L);
 #pragma unroll
       for (int rr = 0; rr < 2; ++rr) {
         const int y = mt * 16 + gq + 8 * rr;
@@ -295,13 +299,20 @@ __global__ void __launch_bounds__(NTHR, MINB) k_recon_tc(const __grid_constant__
   }
 }
 
-// Grid::rtile 16: 16-column tiles in 256-thread blocks; 8: 8-column tiles
-// in 128-thread blocks at 4 per SM (single-grid batches)
+// Grid::rbuild (single-grid batches) 0: 16-column tiles in 256-thread
+// blocks at 2 per SM; 1: 8-column tiles in 128-thread blocks at 4; 2:
+// 16-column tiles at 3 per SM, the table fragments loaded without prefetch
+// (80 registers)
 template <class S>
 static void launch_recon_sizes(const Grid& g, const ReconArgs& a, cudaStream_t st) {
-  if (g.rtile == 8 && !a.grids) {
+  if (g.rbuild == 1 && !a.grids) {
     const int ntx = (g.X + 7) / 8;
     k_recon_tc<false, S, 8, 128, 4><<<dim3(g.Nz * ntx, a.ninst), 128, recon_tc_smem_bytes(g, 8), st>>>(g, a);
+    return;
+  }
+  if (g.rbuild == 2 && !a.grids) {
+    const int ntx = (g.X + kTile - 1) / kTile;
+    k_recon_tc<false, S, 16, 256, 3><<<dim3(g.Nz * ntx, a.ninst), 256, recon_tc_smem_bytes(g), st>>>(g, a);
     return;
   }
   const int ntx = (g.X + kTile - 1) / kTile;
@@ -324,6 +335,9 @@ void prepare_recon_tc(int optin) {
   allow_max_smem(k_recon_tc<true, SizesRT>, optin);
   allow_max_smem(k_recon_tc<false, Sizes32>, optin);
   allow_max_smem(k_recon_tc<false, Sizes16>, optin);
+  allow_max_smem(k_recon_tc<false, SizesRT, 16, 256, 3>, optin);
+  allow_max_smem(k_recon_tc<false, Sizes32, 16, 256, 3>, optin);
+  allow_max_smem(k_recon_tc<false, Sizes16, 16, 256, 3>, optin);
   allow_max_smem(k_recon_tc<false, SizesRT, 8, 128, 4>, optin);
   allow_max_smem(k_recon_tc<false, Sizes32, 8, 128, 4>, optin);
   allow_max_smem(k_recon_tc<false, Sizes16, 8, 128, 4>, optin);

@@ -14,8 +14,9 @@ grouped, not the digit sums or their rounding; nor do the builds of the
 products, reconstruction and solve kernels compiled for those sizes
 (CHN_FIXED_SIZES=1), nor the adjoint products' planes per pass (1 or 3,
 CHN_ADJ_PRODUCTS_PER_PASS; the reference adjoint and the exact one), nor
-the reconstruction's tile (16 columns in 256-thread blocks or 8 in 128,
-CHN_RECON_TILE).  Each variant runs the
+the reconstruction's build (CHN_RECON_BUILD: 0 = 16 columns in 256-thread
+blocks at two per SM, 1 = 8 columns in 128-thread blocks at four, 2 = 16
+columns at three without the table prefetch).  Each variant runs the
 batched forward (primal + 3 tangents, one forced), the coupled adjoint
 and the exact adjoint, and the single-trajectory primal, and must reproduce the default's outputs
 bit for bit.  Grids: 32x65x32 (the benchmarked one) and 48x97x48 (24 kx
@@ -36,7 +37,7 @@ pytestmark = pytest.mark.gpu
 GRIDS = [(32, 65, 32, 2 * np.pi, np.pi, 3300.0, 2.0, 0.005, 3), (48, 97, 48, 2 * np.pi, np.pi, 3300.0, 2.0, 0.004, 2),
          (16, 33, 16, 2 * np.pi, np.pi, 2000.0, 2.0, 0.01, 3)]
 NSEG, NTAN = 2, 3
-KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_FIXED_SIZES", "CHN_ADJ_PRODUCTS_PER_PASS", "CHN_RECON_TILE",
+KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_FIXED_SIZES", "CHN_ADJ_PRODUCTS_PER_PASS", "CHN_RECON_BUILD",
          "CHN_AUTOTUNE")
 
 
@@ -125,10 +126,11 @@ def test_adjoint_products_per_pass_give_the_same_bits(cc, gi):
     _same(a, b)
 
 
-@pytest.mark.parametrize("gi,fixed", [(0, "1"), (0, "0"), (2, "1")])
-def test_recon_tiles_give_the_same_bits(cc, gi, fixed):
-    a, _ = _sweeps(cc, GRIDS[gi], {"CHN_RECON_TILE": "16", "CHN_AUTOTUNE": "0"})
-    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_RECON_TILE": "8", "CHN_FIXED_SIZES": fixed, "CHN_AUTOTUNE": "0"})
+@pytest.mark.parametrize("gi,build,fixed", [(0, "1", "1"), (0, "1", "0"), (2, "1", "1"), (0, "2", "1"), (0, "2", "0"),
+                                            (2, "2", "1")])
+def test_recon_builds_give_the_same_bits(cc, gi, build, fixed):
+    a, _ = _sweeps(cc, GRIDS[gi], {"CHN_RECON_BUILD": "0", "CHN_AUTOTUNE": "0"})
+    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_RECON_BUILD": build, "CHN_FIXED_SIZES": fixed, "CHN_AUTOTUNE": "0"})
     _same(a, b)
 
 
@@ -144,6 +146,6 @@ def test_autotuner_reports_its_choices(cc):
     for part in ("products", "recon", "solve"):
         assert report[part + "_sizes"] in ("runtime", "fixed") and report[part + "_fixed_sizes"] > 0
     assert report["adjoint_products_per_pass"] in (1, 3)
-    assert report["recon_tile"] in (8, 16)
+    assert report["recon_build"] in (0, 1, 2)
     ref, _ = _sweeps(cc, GRIDS[0], {"CHN_SOLVE_TILE": "16", "CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
     _same(res, ref)
