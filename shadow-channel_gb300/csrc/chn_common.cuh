@@ -143,6 +143,8 @@ struct Grid {
   int fwdpb;  // product planes per pass of the forward modes (3, or 1 where 3 leave no room for two blocks)
   int fxch;   // x-stage columns per chunk of the forward products (a multiple of 8; all where they fit)
   int adjpb;  // product planes per pass of the adjoint product modes (1 or 3; autotuned)
+  int prodb;  // products build: 0 = the plan above, 1 = two planes per pass at 3 blocks per SM
+              // (single-grid batches; autotuned)
   // kernels that run their build compiled for the grid's sizes (32x65x32,
   // 16x33x16): FIXED_* bits of sizes.cuh (autotuned; the same results)
   int fixed;

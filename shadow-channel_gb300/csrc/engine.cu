@@ -226,6 +226,10 @@ static bool build_device_tables(DevTables& T, int Nx, int Ny, int Nz, double Lx,
   // 1 and 3; CHN_ADJ_PRODUCTS_PER_PASS=1 or 3 fixes it
   const char* apb = getenv("CHN_ADJ_PRODUCTS_PER_PASS");
   g.adjpb = (apb && apb[0] == '3') ? 3 : 1;
+  // the products' build (phys_tc.cu): 0 until the autotuner has timed 0 and
+  // 1 (two planes per pass at 3 blocks per SM); CHN_PRODUCTS_BUILD fixes it
+  const char* pbe = getenv("CHN_PRODUCTS_BUILD");
+  g.prodb = (pbe && pbe[0] == '1' && pbe[1] == 0) ? 1 : 0;
   // the solve's block tile: 16 until the autotuner has timed both;
   // CHN_SOLVE_TILE=8 or 16 fixes it (and skips that timing)
   const char* stl = getenv("CHN_SOLVE_TILE");  // 16, 8 or 8/128 (8 columns, 128 threads)
@@ -1280,7 +1284,7 @@ static bool autotune_fixed(Engine& e, Work& w) {
   Grid& g = e.T.g;
   const char* apb = getenv("CHN_ADJ_PRODUCTS_PER_PASS");
   const bool do_fixed = !(forced && forced[0]) && !w.gdev && phys_tc_specialised(g);
-  const bool do_pb = g.tcf && !(apb && apb[0]) && !w.gdev;
+  const bool do_pb = g.tcf && !w.gdev;  // the adjoint planes per pass, the products' build
   const char* rbe = getenv("CHN_RECON_BUILD");
   const bool do_rt = g.tc && !(rbe && rbe[0]) && !w.gdev;
   if ((off && off[0] == '0') || !(do_fixed || do_pb || do_rt)) return true;
@@ -1358,7 +1362,7 @@ static bool autotune_fixed(Engine& e, Work& w) {
     rep += buf;
   }
   // the adjoint products' planes per pass (its own switch)
-  if (ok && do_pb) {
+  if (ok && do_pb && !(apb && apb[0])) {
     const int saved_pb = g.adjpb;
     float ms[2] = {0.f, 0.f};
     const int pbs[2] = {1, 3};
@@ -1380,6 +1384,32 @@ static bool autotune_fixed(Engine& e, Work& w) {
       rep += buf;
     } else {
       g.adjpb = saved_pb;
+    }
+  }
+  // the products' build: three planes per pass at 2 blocks per SM (the
+  // plan) against two planes at 3 blocks
+  const char* pbe = getenv("CHN_PRODUCTS_BUILD");
+  if (ok && g.tcf && !w.gdev && !(pbe && pbe[0])) {
+    const int saved_b = g.prodb;
+    float ms[2] = {0.f, 0.f};
+    for (int c = 0; c < 2 && ok; ++c) {
+      g.prodb = c;
+      ok = enqueue(FIXED_PRODUCTS);  // warm-up
+      ok = ok && cudaEventRecord(t0, e.st) == cudaSuccess;
+      for (int k = 0; k < 3 && ok; ++k) ok = enqueue(FIXED_PRODUCTS);
+      ok = ok && cudaEventRecord(t1, e.st) == cudaSuccess && cudaEventSynchronize(t1) == cudaSuccess;
+      if (ok) cudaEventElapsedTime(&ms[c], t0, t1);
+      ms[c] /= 3;
+    }
+    if (ok) {
+      g_launches += 16;
+      g.prodb = ms[1] < ms[0] ? 1 : 0;
+      snprintf(buf, sizeof(buf), "\"products_b0\": %.4f, \"products_b1\": %.4f, \"products_build\": %d", ms[0], ms[1],
+               g.prodb);
+      if (!rep.empty()) rep += ", ";
+      rep += buf;
+    } else {
+      g.prodb = saved_b;
     }
   }
   // the reconstruction's build (tile, threads, blocks per SM)
@@ -2520,6 +2550,7 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
     gs[i].adjpb = gmax.adjpb;
     gs[i].fwdpb = gmax.fwdpb;
     gs[i].fxch = gmax.fxch;
+    gs[i].prodb = 0;  // uneven batches keep the plan's build
   }
   if (cudaMalloc(&m->gdev, sizeof(Grid) * n) != cudaSuccess ||
       cudaMemcpy(m->gdev, gs.data(), sizeof(Grid) * n, cudaMemcpyHostToDevice) != cudaSuccess) {

@@ -415,6 +415,24 @@ __host__ __device__ constexpr FwdTcDims fwd_tc_dims_n(int Nz, int X, int pz, int
 
 __host__ __device__ inline FwdTcDims fwd_tc_dims(const Grid& g) { return fwd_tc_dims_n(g.Nz, g.X, g.pz, g.px); }
 
+// shared memory of a products block: pb product planes, x-stage digits of
+// xch columns (a chunk), z-stage digits, exponents, the z-stage outputs
+__host__ __device__ constexpr size_t fwd_tc_smem_n(int Nz, int X, int pz, int px, int pb, int xch) {
+  const FwdTcDims d = fwd_tc_dims_n(Nz, X, pz, px);
+  const size_t dx = (size_t)kDig * xch * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
+  return (size_t)(pb * ((pz + 3) / 4 * 4) + (X + 3) / 4 * 4) * sizeof(int) + ((dx > dz ? dx : dz) + 15) / 16 * 16 +
+         ((size_t)pb * pz * px * sizeof(double) + 15) / 16 * 16 + (size_t)d.Kk * X * sizeof(cpx);
+}
+
+// the widest x-stage chunk (a multiple of 8 columns) with which minb blocks
+// of pb planes share an SM's 228 KB (1 KB reserved per block); 8 if none
+__host__ __device__ constexpr int fwd_tc_xch_n(int Nz, int X, int pz, int px, int pb, int minb) {
+  const int pzp = (pz + 7) / 8 * 8;
+  for (int c = pzp; c > 8; c -= 8)
+    if ((size_t)minb * (fwd_tc_smem_n(Nz, X, pz, px, pb, c) + 1024 + 1024) <= 233472) return c;
+  return 8;
+}
+
 // pb product planes per pass: kPB for the forward modes (0, 1); for the
 // adjoint modes (2, 3, six products) Grid::adjpb: kPB (each field loaded
 // once per three products) or one (a smaller footprint leaves L1 to the
@@ -425,18 +443,7 @@ inline int products_per_pass(const Grid& g, int mode) {
 }
 
 // xch: x-stage columns (padded zp rows) digitised per chunk
-size_t fwd_tc_smem_bytes(const Grid& g, int pb, int xch) {
-  const FwdTcDims d = fwd_tc_dims(g);
-  const size_t dx = (size_t)kDig * xch * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
-  // kPB product planes (Y of the component in flight overlays its own plane:
-  // pz X complex values <= pz px doubles)
-  const size_t stage = (size_t)pb * g.pz * g.px * sizeof(double);
-  size_t b = (size_t)(pb * ((g.pz + 3) / 4 * 4) + (g.X + 3) / 4 * 4) * sizeof(int);
-  b += ((dx > dz ? dx : dz) + 15) / 16 * 16;
-  b += (stage + 15) / 16 * 16;
-  b += (size_t)d.Kk * g.X * sizeof(cpx);
-  return b;
-}
+size_t fwd_tc_smem_bytes(const Grid& g, int pb, int xch) { return fwd_tc_smem_n(g.Nz, g.X, g.pz, g.px, pb, xch); }
 
 // The products of one plane (mode 0 primal, 1 tangent, 2 adjoint S and T,
 // 3 the exact transpose; split_product) and their forward transforms as
@@ -445,9 +452,11 @@ size_t fwd_tc_smem_bytes(const Grid& g, int pb, int xch) {
 // modes 0/1 write H slots 0..2, modes 2/3 fold each component into the
 // output slots (assemble_stage).  Same outputs as k_products_fwd /
 // k_products_adj.
-// S: the sizes (SizesRT, or SizesCT for a specialised grid)
-template <bool MULTI, int PB, class S>
-__global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_constant__ Grid g0, ProdArgs a, int mode) {
+// S: the sizes (SizesRT, or SizesCT for a specialised grid); MINB blocks
+// per SM (the register budget; with MINB > 2 the x stage runs in the chunks
+// that let MINB blocks share an SM)
+template <bool MULTI, int PB, class S, int MINB = 2>
+__global__ void __launch_bounds__(kThreads, MINB) k_products_tc(const __grid_constant__ Grid g0, ProdArgs a, int mode) {
   const int inst = blockIdx.y, y = blockIdx.x;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
   const S gsz(g);
@@ -463,7 +472,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_products_tc(const __grid_consta
   // x-stage columns per chunk: all of them in the fixed-size builds, else
   // the plan's (Grid::fxch, a multiple of 8)
   int XCH = d.pzp;
-  if constexpr (std::is_same<S, SizesRT>::value) XCH = min(g.fxch, d.pzp);
+  if constexpr (MINB > 2) XCH = fwd_tc_xch_n(gsz.Nz(), gsz.X(), gsz.pz(), gsz.px(), PB, MINB);
+  else if constexpr (std::is_same<S, SizesRT>::value) XCH = min(g.fxch, d.pzp);
   {
     const size_t dx = (size_t)kDig * XCH * d.KSx * 2, dz = (size_t)kDig * d.Xp * d.KSz * 2;
     p += ((dx > dz ? dx : dz) + 15) / 16 * 16;
@@ -640,9 +650,25 @@ static void launch_products_sizes(const Grid& g, const ProdArgs& a, int mode, cu
   }
 }
 
+// Grid::prodb 1 (single-grid batches): two product planes per pass at 3
+// blocks per SM (80 registers), the x stage in the chunks that fit
+template <class S>
+static void launch_products_b3(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
+  const dim3 grid(g.Q, a.ninst);
+  const size_t sm = fwd_tc_smem_bytes(g, 2, fwd_tc_xch_n(g.Nz, g.X, g.pz, g.px, 2, 3));
+  k_products_tc<false, 2, S, 3><<<grid, kThreads, sm, st>>>(g, a, mode);
+}
+
 // Grid::fixed & FIXED_PRODUCTS: the build compiled for the grid's sizes
 // (32x65x32, 16x33x16; single-grid batches), else the run-time sizes
 cudaError_t launch_products_tc(const Grid& g, const ProdArgs& a, int mode, cudaStream_t st) {
+  if (g.prodb == 1 && !a.grids) {
+    const bool fx = (g.fixed & FIXED_PRODUCTS) != 0;
+    if (fx && sizes_match<Sizes32>(g)) launch_products_b3<Sizes32>(g, a, mode, st);
+    else if (fx && sizes_match<Sizes16>(g)) launch_products_b3<Sizes16>(g, a, mode, st);
+    else launch_products_b3<SizesRT>(g, a, mode, st);
+    return cudaGetLastError();
+  }
   const bool fx = (g.fixed & FIXED_PRODUCTS) && !a.grids && g.fxch >= fwd_tc_dims(g).pzp;
   if (fx && sizes_match<Sizes32>(g)) launch_products_sizes<Sizes32>(g, a, mode, st);
   else if (fx && sizes_match<Sizes16>(g)) launch_products_sizes<Sizes16>(g, a, mode, st);
@@ -757,6 +783,9 @@ void prepare_phys_tc(int optin) {
   allow_max_smem(k_products_tc<false, 1, RT>, optin);
   allow_max_smem(k_products_tc<true, 1, RT>, optin);
   allow_max_smem(k_products_tc<false, kPB, Sizes32>, optin);
+  allow_max_smem(k_products_tc<false, 2, SizesRT, 3>, optin);
+  allow_max_smem(k_products_tc<false, 2, Sizes32, 3>, optin);
+  allow_max_smem(k_products_tc<false, 2, Sizes16, 3>, optin);
   allow_max_smem(k_products_tc<false, 1, Sizes32>, optin);
   allow_max_smem(k_products_tc<false, kPB, Sizes16>, optin);
   allow_max_smem(k_products_tc<false, 1, Sizes16>, optin);

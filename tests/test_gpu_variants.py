@@ -16,7 +16,9 @@ products, reconstruction and solve kernels compiled for those sizes
 CHN_ADJ_PRODUCTS_PER_PASS; the reference adjoint and the exact one), nor
 the reconstruction's build (CHN_RECON_BUILD: 0 = 16 columns in 256-thread
 blocks at two per SM, 1 = 8 columns in 128-thread blocks at four, 2 = 16
-columns at three without the table prefetch).  Each variant runs the
+columns at three without the table prefetch), nor the products' build
+(CHN_PRODUCTS_BUILD: 1 = two product planes per pass at three blocks per
+SM).  Each variant runs the
 batched forward (primal + 3 tangents, one forced), the coupled adjoint
 and the exact adjoint, and the single-trajectory primal, and must reproduce the default's outputs
 bit for bit.  Grids: 32x65x32 (the benchmarked one) and 48x97x48 (24 kx
@@ -38,7 +40,7 @@ GRIDS = [(32, 65, 32, 2 * np.pi, np.pi, 3300.0, 2.0, 0.005, 3), (48, 97, 48, 2 *
          (16, 33, 16, 2 * np.pi, np.pi, 2000.0, 2.0, 0.01, 3)]
 NSEG, NTAN = 2, 3
 KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_FIXED_SIZES", "CHN_ADJ_PRODUCTS_PER_PASS", "CHN_RECON_BUILD",
-         "CHN_AUTOTUNE")
+         "CHN_PRODUCTS_BUILD", "CHN_AUTOTUNE")
 
 
 @pytest.fixture(scope="module")
@@ -134,6 +136,13 @@ def test_recon_builds_give_the_same_bits(cc, gi, build, fixed):
     _same(a, b)
 
 
+@pytest.mark.parametrize("gi,fixed", [(0, "1"), (0, "0"), (2, "1")])
+def test_products_builds_give_the_same_bits(cc, gi, fixed):
+    a, _ = _sweeps(cc, GRIDS[gi], {"CHN_PRODUCTS_BUILD": "0", "CHN_AUTOTUNE": "0"})
+    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_PRODUCTS_BUILD": "1", "CHN_FIXED_SIZES": fixed, "CHN_AUTOTUNE": "0"})
+    _same(a, b)
+
+
 def test_autotuner_reports_its_choices(cc):
     res, report = _sweeps(cc, GRIDS[0], {})
     if "solve_chosen" not in report:
@@ -147,5 +156,6 @@ def test_autotuner_reports_its_choices(cc):
         assert report[part + "_sizes"] in ("runtime", "fixed") and report[part + "_fixed_sizes"] > 0
     assert report["adjoint_products_per_pass"] in (1, 3)
     assert report["recon_build"] in (0, 1, 2)
+    assert report["products_build"] in (0, 1)
     ref, _ = _sweeps(cc, GRIDS[0], {"CHN_SOLVE_TILE": "16", "CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
     _same(res, ref)
