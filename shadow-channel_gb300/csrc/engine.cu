@@ -1457,6 +1457,31 @@ static bool autotune_fixed(Engine& e, Work& w) {
   return true;
 }
 
+// The autotuners' timing inputs: the working set's spectral planes,
+// physical fields and tangent coefficients filled with a seeded pattern
+// before the timings (fill) and cleared again after them, so a batch starts
+// from the zeroed buffers it would have had without tuning.
+static bool tune_inputs(Engine& e, Work& w, bool fill) {
+  const size_t nt = (size_t)w.nseg * (w.ntan > 0 ? w.ntan : 1);
+  struct Buf {
+    double* p;
+    size_t n;
+  };
+  const Buf bufs[6] = {{reinterpret_cast<double*>(w.Ut), 2 * nt * w.usz},
+                       {reinterpret_cast<double*>(w.Up), 2 * (size_t)w.nseg * w.usz},
+                       {reinterpret_cast<double*>(w.St), 2 * nt * w.csz},
+                       {w.Pp, (size_t)w.nseg * w.psz},
+                       {w.Pt, nt * w.psz},
+                       {w.Pl, (size_t)w.nseg * w.psz}};
+  uint32_t seed = 0x9E3779B9u;
+  for (const Buf& b : bufs) {
+    if (!b.p) continue;
+    if (fill) LK(launch_fill_pattern(b.p, b.n, seed++, e.st));
+    else CK(cudaMemsetAsync(b.p, 0, b.n * sizeof(double), e.st));
+  }
+  return true;
+}
+
 static bool op_primal(Engine& e, Work& w, int ru, const cpx* C) {
   NvtxRange nvtx_op("op_primal");
   const size_t csz = w.csz;
@@ -2175,7 +2200,8 @@ int c_batch_init_steps(int nseg, int ntan, int couple, int nsteps) {
   }
   e.have_batch = true;
   g_tune_report.clear();
-  if (!autotune_transforms(e, e.batch) || !autotune_solve(e, e.batch) || !autotune_fixed(e, e.batch))
+  if (!tune_inputs(e, e.batch, true) || !autotune_transforms(e, e.batch) || !autotune_solve(e, e.batch) ||
+      !autotune_fixed(e, e.batch) || !tune_inputs(e, e.batch, false))
     return g_status;
   g_status = 0;
   return 0;
@@ -2568,8 +2594,8 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
   m->e.batch.gdev = m->gdev;
   m->e.have_batch = true;
   g_tune_report.clear();
-  if (!autotune_transforms(m->e, m->e.batch) || !autotune_solve(m->e, m->e.batch) ||
-      !autotune_fixed(m->e, m->e.batch)) {
+  if (!tune_inputs(m->e, m->e.batch, true) || !autotune_transforms(m->e, m->e.batch) ||
+      !autotune_solve(m->e, m->e.batch) || !autotune_fixed(m->e, m->e.batch) || !tune_inputs(m->e, m->e.batch, false)) {
     const int rc = g_status ? g_status : -1;
     c_multi_destroy();
     return rc;

@@ -222,6 +222,8 @@ cudaError_t launch_step_advance(int* ctr, int delta, cudaStream_t st);
 // a multi-step sweep as one graph launch: the steps-left counter, and the
 // while node's per-iteration kernel that counts it down and sets its condition
 cudaError_t launch_loop_set(int* ctr, int n, cudaStream_t st);
+// a seeded pattern of finite doubles (the autotuner's timing inputs)
+cudaError_t launch_fill_pattern(double* p, size_t n, uint32_t seed, cudaStream_t st);
 cudaError_t launch_loop_next(int* ctr, cudaGraphConditionalHandle h, cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
 // pipe throughput probes: kind 0 DFMA, 1 DADD, 2 DMMA (m8n8k4 f64), 3 FFMA

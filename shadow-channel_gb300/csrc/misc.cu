@@ -347,6 +347,28 @@ cudaError_t launch_loop_next(int* ctr, cudaGraphConditionalHandle h, cudaStream_
   return cudaGetLastError();
 }
 
+// A seeded pattern of finite doubles with exponents spread over 2^-6 .. 2^1
+// (both signs), written where the autotuner times kernels: zeros would take
+// the kernels' zero shortcuts (no exponents to gather, no rounding) and time
+// a lighter workload than the real one.
+__global__ void k_fill_pattern(double* p, size_t n, uint32_t seed) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    uint32_t h = (uint32_t)i * 2654435761u ^ seed;
+    h ^= h >> 15;
+    h *= 2246822519u;
+    h ^= h >> 13;
+    const double m = 0.5 + (double)(h & 0xFFFFFu) * (1.0 / 2097152.0);  // [0.5, 1)
+    const int k = (int)((h >> 20) & 7u) - 6;
+    p[i] = ((h >> 31) ? -m : m) * ldexp(1.0, k);
+  }
+}
+
+cudaError_t launch_fill_pattern(double* p, size_t n, uint32_t seed, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_fill_pattern<<<1216, 256, 0, st>>>(p, n, seed);
+  return cudaGetLastError();
+}
+
 // FP64 fused multiply-add throughput probe: 8 independent chains per thread,
 // registers only; out gets one value per thread so nothing is optimised away.
 __global__ void k_fp64_probe(double* out, int iters, double a, double b) {
