@@ -187,10 +187,11 @@ def segment_step_flops(g):
 
 # ncu DRAM bytes (read + write) of one instance of a 24-instance launch at
 # 32x65x32 (traffic grows with the instance count; the ncu capture of the
-# 8-segment bench case): k_phys_inverse_tc 306.1 MB (97.2 read + 208.9
-# write), k_products_tc tangent mode 387.9 MB (343.6 + 44.3)
+# 8-segment bench case): k_phys_inverse_tc 306.1 MB (97.0 read + 209.1
+# write), k_products_tc tangent mode 458.3 MB (411.7 + 46.7; two product
+# planes per pass, the third product's fields loaded again)
 PHYS_TRAFFIC_PER_INSTANCE_32 = 306.1e6 / 24
-PROD_TRAFFIC_PER_INSTANCE_32 = 387.9e6 / 24
+PROD_TRAFFIC_PER_INSTANCE_32 = 458.3e6 / 24
 
 
 def products_fwd_flops(ninst, g):
