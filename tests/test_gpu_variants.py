@@ -21,8 +21,9 @@ columns at three without the table prefetch), nor the products' build
 SM).  Each variant runs the
 batched forward (primal + 3 tangents, one forced), the coupled adjoint
 and the exact adjoint, and the single-trajectory primal, and must reproduce the default's outputs
-bit for bit.  Grids: 32x65x32 (the benchmarked one) and 48x97x48 (24 kx
-columns: 16 + 8 or three tiles of 8 in the solve).
+bit for bit.  Grids: 32x65x32 (the benchmarked one), 16x33x16 (both with
+compiled-size builds) and 48x97x48 (run-time sizes; 24 kx columns: 16 + 8
+or three tiles of 8 in the solve).
 """
 import ctypes
 import json
@@ -107,7 +108,7 @@ def test_solve_tiles_give_the_same_bits(cc, gi, tile):
 
 @pytest.mark.parametrize("gi,build", [(0, "3"), (0, "4"), (0, "5"), (0, "6"), (0, "7"), (0, "8"), (0, "9"),
                                       (0, "10"), (0, "11"), (0, "12"), (2, "4"), (2, "6"), (2, "7"), (2, "9"),
-                                      (2, "12")])
+                                      (2, "12"), (1, "4"), (1, "8")])
 def test_inverse_builds_give_the_same_bits(cc, gi, build):
     a, _ = _sweeps(cc, GRIDS[gi], {"CHN_INVERSE_BUILD": "2", "CHN_AUTOTUNE": "0"})
     b, _ = _sweeps(cc, GRIDS[gi], {"CHN_INVERSE_BUILD": build, "CHN_AUTOTUNE": "0"})
@@ -129,14 +130,14 @@ def test_adjoint_products_per_pass_give_the_same_bits(cc, gi):
 
 
 @pytest.mark.parametrize("gi,build,fixed", [(0, "1", "1"), (0, "1", "0"), (2, "1", "1"), (0, "2", "1"), (0, "2", "0"),
-                                            (2, "2", "1")])
+                                            (2, "2", "1"), (1, "1", "0"), (1, "2", "0")])
 def test_recon_builds_give_the_same_bits(cc, gi, build, fixed):
     a, _ = _sweeps(cc, GRIDS[gi], {"CHN_RECON_BUILD": "0", "CHN_AUTOTUNE": "0"})
     b, _ = _sweeps(cc, GRIDS[gi], {"CHN_RECON_BUILD": build, "CHN_FIXED_SIZES": fixed, "CHN_AUTOTUNE": "0"})
     _same(a, b)
 
 
-@pytest.mark.parametrize("gi,fixed", [(0, "1"), (0, "0"), (2, "1")])
+@pytest.mark.parametrize("gi,fixed", [(0, "1"), (0, "0"), (2, "1"), (1, "0")])
 def test_products_builds_give_the_same_bits(cc, gi, fixed):
     a, _ = _sweeps(cc, GRIDS[gi], {"CHN_PRODUCTS_BUILD": "0", "CHN_AUTOTUNE": "0"})
     b, _ = _sweeps(cc, GRIDS[gi], {"CHN_PRODUCTS_BUILD": "1", "CHN_FIXED_SIZES": fixed, "CHN_AUTOTUNE": "0"})
