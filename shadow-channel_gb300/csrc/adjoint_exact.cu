@@ -20,6 +20,7 @@
 // physical fields to u_in_bar.
 #include "chn_common.cuh"
 #include "kernels.h"
+#include "sizes.cuh"
 #include "solve_common.cuh"
 #include "tc_common.cuh"
 
@@ -243,10 +244,10 @@ static constexpr int kTRegs = 8;  // plane inputs a thread keeps in registers (Q
 // table b (row-major [rows][Q] digits: [b][ceil(R/16)][KT][7][32][4], row
 // exponents TE[b * R + row]) with the per-column plane inputs in(y, col)
 // (Re and Im as two GEMM columns sharing the column exponent)
-template <typename In, typename Comb>
-__device__ void contract_planes_tc(const Grid& g, const uint4* __restrict__ T, const int* __restrict__ TE, int b,
-                                   int N, int nx, In input, Comb comb, uint16_t* dig, int* exc) {
-  const int KT = (g.Q + 15) / 16, MTw = (g.R + 15) / 16;
+template <class S, typename In, typename Comb>
+__device__ void contract_planes_tc(const Grid& g, const S& gsz, const uint4* __restrict__ T, const int* __restrict__ TE,
+                                   int b, int N, int nx, In input, Comb comb, uint16_t* dig, int* exc) {
+  const int KT = (gsz.Q() + 15) / 16, MTw = (gsz.R() + 15) / 16;
   const size_t KS = (size_t)KT * 16 + 8;
   for (int i = threadIdx.x; i < kTile; i += blockDim.x) exc[i] = 0;
   __syncthreads();
@@ -257,7 +258,7 @@ __device__ void contract_planes_tc(const Grid& g, const uint4* __restrict__ T, c
 #pragma unroll
     for (int k = 0; k < kTRegs; ++k) {
       const int y = y0 + 16 * k;
-      vin[k] = (k < KT && y < g.Q && col < nx) ? input(y, col) : cpx{0.0, 0.0};
+      vin[k] = (k < KT && y < gsz.Q() && col < nx) ? input(y, col) : cpx{0.0, 0.0};
       emax = max(emax, max((int)((__double_as_longlong(vin[k].re) >> 52) & 0x7FF),
                            (int)((__double_as_longlong(vin[k].im) >> 52) & 0x7FF)));
     }
@@ -272,7 +273,7 @@ __device__ void contract_planes_tc(const Grid& g, const uint4* __restrict__ T, c
       digits_bf16(scaled56(vin[k].im, ex), dig + (size_t)(2 * col + 1) * KS + y, 32 * KS);
     }
   } else {
-    for (int i = threadIdx.x; i < g.Q * kTile; i += blockDim.x) {
+    for (int i = threadIdx.x; i < gsz.Q() * kTile; i += blockDim.x) {
       const int y = i / kTile, col = i - y * kTile;
       if (col >= nx) continue;
       const cpx v = input(y, col);
@@ -283,7 +284,7 @@ __device__ void contract_planes_tc(const Grid& g, const uint4* __restrict__ T, c
     __syncthreads();
     for (int i = threadIdx.x; i < KT * 16 * kTile; i += blockDim.x) {
       const int y = i / kTile, col = i - y * kTile;
-      const cpx v = (y < g.Q && col < nx) ? input(y, col) : cpx{0.0, 0.0};
+      const cpx v = (y < gsz.Q() && col < nx) ? input(y, col) : cpx{0.0, 0.0};
       const int ex = exc[col] - 1022;
       digits_bf16(scaled56(v.re, ex), dig + (size_t)(2 * col) * KS + y, 32 * KS);
       digits_bf16(scaled56(v.im, ex), dig + (size_t)(2 * col + 1) * KS + y, 32 * KS);
@@ -302,7 +303,7 @@ __device__ void contract_planes_tc(const Grid& g, const uint4* __restrict__ T, c
     for (int rr = 0; rr < 2; ++rr) {
       const int row = mt * 16 + gq + 8 * rr;
       if (row >= N || col >= nx) continue;
-      const int e = TE[(size_t)b * g.R + row] + ecol - 64;
+      const int e = TE[(size_t)b * gsz.R() + row] + ecol - 64;
       const cpx val = {round_col(Hh[2 * rr], Ll[2 * rr], e, ecol + 1022),
                        round_col(Hh[2 * rr + 1], Ll[2 * rr + 1], e, ecol + 1022)};
       comb(row, col, val);
@@ -313,25 +314,26 @@ __device__ void contract_planes_tc(const Grid& g, const uint4* __restrict__ T, c
 
 // Recon^T (as recon_T_tile) with its five contractions on the tensor cores
 // (the mean column, col < xfirst, gets zeros: it has its own rows)
-__device__ void recon_T_tc(const Grid& g, const cpx* __restrict__ Ub, int z, int x0, int nx, int xfirst,
+template <class S>
+__device__ void recon_T_tc(const Grid& g, const S& gsz, const cpx* __restrict__ Ub, int z, int x0, int nx, int xfirst,
                            SolveTSmem& s) {
-  const size_t cs = (size_t)g.Q * g.X;
+  const size_t cs = (size_t)gsz.Q() * gsz.X();
   const cpx* Uz = Ub + (size_t)z * 5 * cs;
   uint16_t* dig = reinterpret_cast<uint16_t*>(s.hc);
-  int* exc = reinterpret_cast<int*>(dig + (size_t)kDig * 32 * ((size_t)(g.Q + 15) / 16 * 16 + 8));
+  int* exc = reinterpret_cast<int*>(dig + (size_t)kDig * 32 * ((size_t)(gsz.Q() + 15) / 16 * 16 + 8));
   const uint4* T = reinterpret_cast<const uint4*>(g.tcBT);
-  auto at = [&](int c, int y, int col) { return Uz[(size_t)c * cs + (size_t)y * g.X + x0 + col]; };
+  auto at = [&](int c, int y, int col) { return Uz[(size_t)c * cs + (size_t)y * gsz.X() + x0 + col]; };
   auto axz = [&](int col, double& ax, double& az) {
-    ax = g.kxK2[(size_t)z * g.X + x0 + col];
-    az = g.kzK2[(size_t)z * g.X + x0 + col];
+    ax = g.kxK2[(size_t)z * gsz.X() + x0 + col];
+    az = g.kzK2[(size_t)z * gsz.X() + x0 + col];
   };
   // alpha_bar = Q^T v_bar - Q'^T Xp_bar + Q''^T dx_bar -> s.Fa
   contract_planes_tc(
-      g, T, g.tcBTE, 0, g.D, nx,
+      g, gsz, T, g.tcBTE, 0, gsz.D(), nx,
       [&](int y, int col) { return col < xfirst ? cpx{0.0, 0.0} : at(1, y, col); },
       [&](int row, int col, cpx v) { s.Fa[row * kTile + col] = v; }, dig, exc);
   contract_planes_tc(
-      g, T, g.tcBTE, 1, g.D, nx,
+      g, gsz, T, g.tcBTE, 1, gsz.D(), nx,
       [&](int y, int col) {
         if (col < xfirst) return cpx{0.0, 0.0};
         double ax, az;
@@ -346,7 +348,7 @@ __device__ void recon_T_tc(const Grid& g, const cpx* __restrict__ Ub, int z, int
       },
       dig, exc);
   contract_planes_tc(
-      g, T, g.tcBTE, 2, g.D, nx,
+      g, gsz, T, g.tcBTE, 2, gsz.D(), nx,
       [&](int y, int col) {
         if (col < xfirst) return cpx{0.0, 0.0};
         double ax, az;
@@ -362,7 +364,7 @@ __device__ void recon_T_tc(const Grid& g, const cpx* __restrict__ Ub, int z, int
       dig, exc);
   // beta_bar = R^T Zp_bar + R'^T dz_bar -> s.Fb
   contract_planes_tc(
-      g, T, g.tcBTE, 3, g.R, nx,
+      g, gsz, T, g.tcBTE, 3, gsz.R(), nx,
       [&](int y, int col) {
         if (col < xfirst) return cpx{0.0, 0.0};
         double ax, az;
@@ -372,7 +374,7 @@ __device__ void recon_T_tc(const Grid& g, const cpx* __restrict__ Ub, int z, int
       },
       [&](int row, int col, cpx v) { s.Fb[row * kTile + col] = v; }, dig, exc);
   contract_planes_tc(
-      g, T, g.tcBTE, 4, g.R, nx,
+      g, gsz, T, g.tcBTE, 4, gsz.R(), nx,
       [&](int y, int col) {
         if (col < xfirst) return cpx{0.0, 0.0};
         double ax, az;
@@ -410,17 +412,18 @@ __device__ __forceinline__ void recon_T_mean_row(const Grid& g, const cpx* __res
 // per plane y the contractions over the modes pa = Qpw^T Fa, qa = Qw^T Fa,
 // rb = Rw^T Fb as GEMMs (rows: planes), then the combination of the FP64
 // loop in k_solve_T (the mean column keeps that loop)
-__device__ void quad_T_tc(const Grid& g, int z, int x0, int nx, int xfirst, SolveTSmem& s, cpx* __restrict__ Hb) {
-  const int KTr = (g.R + 15) / 16, MTq = (g.Q + 15) / 16;
+template <class S>
+__device__ void quad_T_tc(const Grid& g, const S& gsz, int z, int x0, int nx, int xfirst, SolveTSmem& s, cpx* __restrict__ Hb) {
+  const int KTr = (gsz.R() + 15) / 16, MTq = (gsz.Q() + 15) / 16;
   const size_t KS = (size_t)KTr * 16 + 8;
   uint16_t* dA = reinterpret_cast<uint16_t*>(s.hc);             // [7][32][KS] digits of Fa
   uint16_t* dB = dA + (size_t)kDig * 32 * KS;                    // digits of Fb
   int* exa = reinterpret_cast<int*>(dB + (size_t)kDig * 32 * KS);  // [2][kTile] column exponents
   for (int i = threadIdx.x; i < 2 * kTile; i += blockDim.x) exa[i] = 0;
   __syncthreads();
-  for (int i = threadIdx.x; i < (g.D + g.R) * kTile; i += blockDim.x) {
-    const bool fb = i >= g.D * kTile;
-    const int j = fb ? i - g.D * kTile : i, row = j / kTile, col = j - row * kTile;
+  for (int i = threadIdx.x; i < (gsz.D() + gsz.R()) * kTile; i += blockDim.x) {
+    const bool fb = i >= gsz.D() * kTile;
+    const int j = fb ? i - gsz.D() * kTile : i, row = j / kTile, col = j - row * kTile;
     if (col >= nx || col < xfirst) continue;
     const cpx v = (fb ? s.Fb : s.Fa)[row * kTile + col];
     const int e = max((int)((__double_as_longlong(v.re) >> 52) & 0x7FF),
@@ -431,7 +434,7 @@ __device__ void quad_T_tc(const Grid& g, int z, int x0, int nx, int xfirst, Solv
   for (int i = threadIdx.x; i < 2 * KTr * 16 * kTile; i += blockDim.x) {
     const bool fb = i >= KTr * 16 * kTile;
     const int j = fb ? i - KTr * 16 * kTile : i, row = j / kTile, col = j - row * kTile;
-    const int N = fb ? g.R : g.D;
+    const int N = fb ? gsz.R() : gsz.D();
     const cpx v = (row < N && col < nx && col >= xfirst) ? (fb ? s.Fb : s.Fa)[row * kTile + col] : cpx{0.0, 0.0};
     const int ex = exa[(fb ? kTile : 0) + col] - 1022;
     uint16_t* d = fb ? dB : dA;
@@ -442,7 +445,7 @@ __device__ void quad_T_tc(const Grid& g, int z, int x0, int nx, int xfirst, Solv
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
   const int NT = (2 * nx + 7) / 8;
   const uint4* __restrict__ W = reinterpret_cast<const uint4*>(g.tcWT);
-  const size_t cs = (size_t)g.Q * g.X;
+  const size_t cs = (size_t)gsz.Q() * gsz.X();
   const double kz = g.Kz[z];
   for (int item = warp; item < MTq * NT; item += blockDim.x >> 5) {
     const int mt = item / NT, nt = item - mt * NT;
@@ -456,16 +459,16 @@ __device__ void quad_T_tc(const Grid& g, int z, int x0, int nx, int xfirst, Solv
       tc_tile(W + (size_t)b * MTq * KTr * kDig * 32, mt, KTr, d, KS, (size_t)32 * KS, n, lane, t, Hh, Ll);
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
-        const int y = min(mt * 16 + gq + 8 * (r >> 1), g.Q - 1);
-        v[b][r] = round_col(Hh[r], Ll[r], g.tcWTE[(size_t)b * g.Q + y] + ecol - 64, ecol + 1022);
+        const int y = min(mt * 16 + gq + 8 * (r >> 1), gsz.Q() - 1);
+        v[b][r] = round_col(Hh[r], Ll[r], g.tcWTE[(size_t)b * gsz.Q() + y] + ecol - 64, ecol + 1022);
       }
     }
 #pragma unroll
     for (int rr = 0; rr < 2; ++rr) {
       const int y = mt * 16 + gq + 8 * rr;
-      if (y >= g.Q || col >= nx || col < xfirst) continue;
+      if (y >= gsz.Q() || col >= nx || col < xfirst) continue;
       const int x = x0 + col;
-      const double kx = g.Kx[x], k2 = g.K2[(size_t)z * g.X + x];
+      const double kx = g.Kx[x], k2 = g.K2[(size_t)z * gsz.X() + x];
       const double scl = x == 0 ? g.norm : 0.5 * g.norm;
       const cpx pa = {v[0][2 * rr], v[0][2 * rr + 1]}, qa = {v[1][2 * rr], v[1][2 * rr + 1]};
       const cpx rb = {v[2][2 * rr], v[2][2 * rr + 1]};
@@ -476,7 +479,7 @@ __device__ void quad_T_tc(const Grid& g, int z, int x0, int nx, int xfirst, Solv
       hz.im = scl * (kx * rb.re - kz * pa.re);
       hy.re = -scl * k2 * qa.re;
       hy.im = -scl * k2 * qa.im;
-      cpx* out = Hb + ((size_t)z * 5 * g.Q + y) * g.X + x;
+      cpx* out = Hb + ((size_t)z * 5 * gsz.Q() + y) * gsz.X() + x;
       out[0] = hz;
       out[cs] = hx;
       out[2 * cs] = hy;
@@ -484,23 +487,25 @@ __device__ void quad_T_tc(const Grid& g, int z, int x0, int nx, int xfirst, Solv
   }
 }
 
-template <bool MULTI>
+// S: the sizes (SizesRT, or SizesCT for a specialised grid)
+template <bool MULTI, class S>
 __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__ Grid g0, SolveTArgs a) {
   const int ntx = (g0.X + kTile - 1) / kTile;
   const int z = blockIdx.x / ntx, tx = blockIdx.x - z * ntx;
   const int inst = blockIdx.y;
   CHN_INSTANCE_GRID(g0, a.grids, inst);
-  if (z >= g.Nz || tx * kTile >= g.X) return;
+  const S gsz(g);
+  if (z >= gsz.Nz() || tx * kTile >= gsz.X()) return;
   if (blocked_t(a.status, a.sdiv, inst)) return;
   const int x0 = tx * kTile;
-  const int nx = min(kTile, g.X - x0);
+  const int nx = min(kTile, gsz.X() - x0);
   cpx* __restrict__ Cc = a.Cc.at(inst);
-  auto cidx = [&](int v, int r, int x) { return (((size_t)z * 2 + v) * g.R + r) * g.X + x; };
-  if (z == g.Nz / 2) {
+  auto cidx = [&](int v, int r, int x) { return (((size_t)z * 2 + v) * gsz.R() + r) * gsz.X() + x; };
+  if (z == gsz.Nz() / 2) {
     // the tangent zeroes this line every substage (channel/channel.c:460-467)
     if (!a.final_only)
-      for (int i = threadIdx.x; i < 2 * g.R * nx; i += blockDim.x) {
-        const int v = i / (g.R * nx), r = (i / nx) % g.R, x = x0 + i % nx;
+      for (int i = threadIdx.x; i < 2 * gsz.R() * nx; i += blockDim.x) {
+        const int v = i / (gsz.R() * nx), r = (i / nx) % gsz.R(), x = x0 + i % nx;
         Cc[cidx(v, r, x)] = cpx{0.0, 0.0};
       }
     return;
@@ -509,15 +514,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
   SolveTSmem s = carve_solveT(g, smem);
   const cpx* __restrict__ Ub = a.Ub.at(inst);
   const int xfirst = (z == 0 && x0 == 0) ? 1 : 0;
-  if (g.tc) recon_T_tc(g, Ub, z, x0, nx, xfirst, s);
+  if (g.tc) recon_T_tc(g, gsz, Ub, z, x0, nx, xfirst, s);
   else recon_T_tile(g, Ub, z, x0, nx, xfirst, s);
   if (a.final_only) {
     // the sweep's start state: IU = Recon(IC), so IC_bar += Recon^T(IU_bar)
-    for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+    for (int i = threadIdx.x; i < gsz.R() * kTile; i += blockDim.x) {
       const int r = i / kTile, l = i - r * kTile;
       if (l >= nx || l < xfirst) continue;
       const int x = x0 + l;
-      if (r < g.D) {
+      if (r < gsz.D()) {
         const cpx f = s.Fa[r * kTile + l];
         Cc[cidx(0, r, x)].re += f.re;
         Cc[cidx(0, r, x)].im += f.im;
@@ -527,7 +532,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
       Cc[cidx(1, r, x)].im += f.im;
     }
     if (xfirst == 1)
-      for (int i = threadIdx.x; i < g.R; i += blockDim.x) {
+      for (int i = threadIdx.x; i < gsz.R(); i += blockDim.x) {
         cpx ma, mb;
         recon_T_mean_row(g, Ub, i, ma, mb);
         Cc[cidx(0, i, 0)].re += ma.re;
@@ -545,18 +550,18 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
   const int bidx = k;
   const int aidx_next = (k == 0) ? 1 : 0;  // a[1] = -1/2, a[2] = 1/3
   // x_bar = Recon^T part + E_{k+1}^T c_out_bar (or c_out_bar); F_bar = dt d_{k+1} c_out_bar
-  for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+  for (int i = threadIdx.x; i < gsz.R() * kTile; i += blockDim.x) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx || l < xfirst) continue;
     const int x = x0 + l;
-    const size_t zx = (size_t)z * g.X + x;
+    const size_t zx = (size_t)z * gsz.X() + x;
     cpx xa, xb;
-    if (r < g.D) {
+    if (r < gsz.D()) {
       const cpx rec = s.Fa[r * kTile + l];
       const cpx co = Cc[cidx(0, r, x)];
       if (k < 2) {
-        const double* E = g.exA + ((size_t)aidx_next * g.Nz * g.X + zx) * g.D * 9;
-        xa = band_matvecT_row(E, 9, 4, 4, g.D, Cc + cidx(0, 0, x), g.X, r);
+        const double* E = g.exA + ((size_t)aidx_next * gsz.Nz() * gsz.X() + zx) * gsz.D() * 9;
+        xa = band_matvecT_row(E, 9, 4, 4, gsz.D(), Cc + cidx(0, 0, x), gsz.X(), r);
         s.Fa[r * kTile + l] = cpx{dt * dnext * co.re, dt * dnext * co.im};
       } else {
         xa = co;
@@ -571,8 +576,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
       const cpx rec = s.Fb[r * kTile + l];
       const cpx co = Cc[cidx(1, r, x)];
       if (k < 2) {
-        const double* E = g.exB + ((size_t)aidx_next * g.Nz * g.X + zx) * g.R * 5;
-        xb = band_matvecT_row(E, 5, 2, 2, g.R, Cc + cidx(1, 0, x), g.X, r);
+        const double* E = g.exB + ((size_t)aidx_next * gsz.Nz() * gsz.X() + zx) * gsz.R() * 5;
+        xb = band_matvecT_row(E, 5, 2, 2, gsz.R(), Cc + cidx(1, 0, x), gsz.X(), r);
         s.Fb[r * kTile + l] = cpx{dt * dnext * co.re, dt * dnext * co.im};
       } else {
         xb = co;
@@ -591,15 +596,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
     // ones: a warp holds one system (no divergence between the two bands)
     const int l = (threadIdx.x % (4 * kTile)) / 4, ch = 4 * (threadIdx.x / (4 * kTile)) + threadIdx.x % 4;
     if (l < nx && l >= xfirst) {
-      const size_t zx = (size_t)z * g.X + x0 + l;
+      const size_t zx = (size_t)z * gsz.X() + x0 + l;
       const int par = ch & 1, part = (ch >> 1) & 1;
       if (ch < 4)
-        band_solveT_chain<9, 4, 4>(g.luA + ((size_t)bidx * g.Nz * g.X + zx) * g.D * 9,
-                                   g.rdA + ((size_t)bidx * g.Nz * g.X + zx) * g.D, g.D, par,
+        band_solveT_chain<9, 4, 4>(g.luA + ((size_t)bidx * gsz.Nz() * gsz.X() + zx) * gsz.D() * 9,
+                                   g.rdA + ((size_t)bidx * gsz.Nz() * gsz.X() + zx) * gsz.D(), gsz.D(), par,
                                    reinterpret_cast<double*>(s.ra + l) + part, 2 * kTile);
       else
-        band_solveT_chain<5, 2, 2>(g.luB + ((size_t)bidx * g.Nz * g.X + zx) * g.R * 5,
-                                   g.rdB + ((size_t)bidx * g.Nz * g.X + zx) * g.R, g.R, par,
+        band_solveT_chain<5, 2, 2>(g.luB + ((size_t)bidx * gsz.Nz() * gsz.X() + zx) * gsz.R() * 5,
+                                   g.rdB + ((size_t)bidx * gsz.Nz() * gsz.X() + zx) * gsz.R(), gsz.R(), par,
                                    reinterpret_cast<double*>(s.rb + l) + part, 2 * kTile);
     }
   }
@@ -617,59 +622,59 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
     xk = a.Xf + (long long)inst * a.xstride + (long long)xs * a.xslot.stride;
     if (a.Ftr) ft1 = a.Ftr[(long long)inst * a.ftr_stride + xs + 1];
     const size_t csz = coef_size(g);
-    for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+    for (int i = threadIdx.x; i < gsz.R() * kTile; i += blockDim.x) {
       const int r = i / kTile, l = i - r * kTile;
       if (l >= nx || l < xfirst) continue;
       const int x = x0 + l;
-      const double k2 = g.K2[(size_t)z * g.X + x];
-      if (r < g.D) {
-        const cpx d0 = visc_v_row(g, k2, xk + cidx(0, 0, x), g.X, r);
-        const cpx d1 = visc_v_row(g, k2, xk + csz + cidx(0, 0, x), g.X, r);
+      const double k2 = g.K2[(size_t)z * gsz.X() + x];
+      if (r < gsz.D()) {
+        const cpx d0 = visc_v_row(g, k2, xk + cidx(0, 0, x), gsz.X(), r);
+        const cpx d1 = visc_v_row(g, k2, xk + csz + cidx(0, 0, x), gsz.X(), r);
         const cpx c2 = s.ra[r * kTile + l];
         gpart -= re2 * dt * (c2.re * (akf * d0.re + bkf * d1.re) + c2.im * (akf * d0.im + bkf * d1.im));
       }
-      const cpx d0 = visc_g_row(g, k2, xk + cidx(1, 0, x), g.X, r);
-      const cpx d1 = visc_g_row(g, k2, xk + csz + cidx(1, 0, x), g.X, r);
+      const cpx d0 = visc_g_row(g, k2, xk + cidx(1, 0, x), gsz.X(), r);
+      const cpx d1 = visc_g_row(g, k2, xk + csz + cidx(1, 0, x), gsz.X(), r);
       const cpx c2 = s.rb[r * kTile + l];
       gpart += re2 * dt * (c2.re * (akf * d0.re + bkf * d1.re) + c2.im * (akf * d0.im + bkf * d1.im));
     }
   }
   // F_bar += dt c_k c2_bar; c_in_bar = E_0^T c2_bar (k == 0) or c2_bar
-  for (int i = threadIdx.x; i < g.R * kTile; i += blockDim.x) {
+  for (int i = threadIdx.x; i < gsz.R() * kTile; i += blockDim.x) {
     const int r = i / kTile, l = i - r * kTile;
     if (l >= nx || l < xfirst) continue;
     const int x = x0 + l;
-    const size_t zx = (size_t)z * g.X + x;
-    if (r < g.D) {
+    const size_t zx = (size_t)z * gsz.X() + x;
+    if (r < gsz.D()) {
       const cpx c2 = s.ra[r * kTile + l];
       s.Fa[r * kTile + l].re += dt * ck * c2.re;
       s.Fa[r * kTile + l].im += dt * ck * c2.im;
-      Cc[cidx(0, r, x)] = k == 0 ? band_matvecT_row(g.exA + zx * g.D * 9, 9, 4, 4, g.D, s.ra + l, kTile, r) : c2;
+      Cc[cidx(0, r, x)] = k == 0 ? band_matvecT_row(g.exA + zx * gsz.D() * 9, 9, 4, 4, gsz.D(), s.ra + l, kTile, r) : c2;
     } else {
       Cc[cidx(0, r, x)] = s.ra[r * kTile + l];
     }
     const cpx c2 = s.rb[r * kTile + l];
     s.Fb[r * kTile + l].re += dt * ck * c2.re;
     s.Fb[r * kTile + l].im += dt * ck * c2.im;
-    Cc[cidx(1, r, x)] = k == 0 ? band_matvecT_row(g.exB + zx * g.R * 5, 5, 2, 2, g.R, s.rb + l, kTile, r) : c2;
+    Cc[cidx(1, r, x)] = k == 0 ? band_matvecT_row(g.exB + zx * gsz.R() * 5, 5, 2, 2, gsz.R(), s.rb + l, kTile, r) : c2;
   }
   // mean mode (transpose of channel/increproject0.c with the homogeneous
   // flux correction), warp 0
   if (xfirst == 1 && threadIdx.x < 32) {
     double* fa = s.m0;
-    double* fb = s.m0 + g.R;
-    cpx* ca = reinterpret_cast<cpx*>(s.m0 + 2 * g.R);
-    cpx* cb = ca + g.R;
+    double* fb = s.m0 + gsz.R();
+    cpx* ca = reinterpret_cast<cpx*>(s.m0 + 2 * gsz.R());
+    cpx* cb = ca + gsz.R();
     const int lane = threadIdx.x;
-    const double* Enext = g.ex0 + (size_t)aidx_next * g.R * 5;
-    for (int i = lane; i < g.R; i += 32) {
+    const double* Enext = g.ex0 + (size_t)aidx_next * gsz.R() * 5;
+    for (int i = lane; i < gsz.R(); i += 32) {
       cpx ma, mb;
       recon_T_mean_row(g, Ub, i, ma, mb);
       const cpx coa = Cc[cidx(0, i, 0)], cob = Cc[cidx(1, i, 0)];
       cpx xa, xb;
       if (k < 2) {
-        xa = band_matvecT_row(Enext, 5, 2, 2, g.R, Cc + cidx(0, 0, 0), g.X, i);
-        xb = band_matvecT_row(Enext, 5, 2, 2, g.R, Cc + cidx(1, 0, 0), g.X, i);
+        xa = band_matvecT_row(Enext, 5, 2, 2, gsz.R(), Cc + cidx(0, 0, 0), gsz.X(), i);
+        xb = band_matvecT_row(Enext, 5, 2, 2, gsz.R(), Cc + cidx(1, 0, 0), gsz.X(), i);
         fa[i] = dt * dnext * coa.re;  // the mean right-hand side is real
         fb[i] = dt * dnext * cob.re;
       } else {
@@ -685,17 +690,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
     // flux correction x = xs - 0.5 add (rwsum . xs.re), transposed:
     // xs_bar.re = x_bar.re - 0.5 rwsum (add . x_bar.re)
     double part = 0.0;
-    for (int i = lane; i < g.R; i += 32) part = fma(g.add0[i], ca[i].re, part);
+    for (int i = lane; i < gsz.R(); i += 32) part = fma(g.add0[i], ca[i].re, part);
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     // the forced tangent adds 0.5 * 2.0 * add to this line's real part
     // (channel/increproject0.c:209-214): its cotangent is <add, x_bar.re>
     if (want_g && lane == 0) a.gacc[(long long)inst * a.gstride] += part;
     __syncwarp();
-    for (int i = lane; i < g.R; i += 32) ca[i].re = fma(-0.5 * part, g.rwsum[i], ca[i].re);
+    for (int i = lane; i < gsz.R(); i += 32) ca[i].re = fma(-0.5 * part, g.rwsum[i], ca[i].re);
     __syncwarp();
     if (lane < 8) {
       const int par = lane & 1, pt = (lane >> 1) & 1;
-      band_solveT_chain<5, 2, 2>(g.lu0 + (size_t)bidx * g.R * 5, g.rd0 + (size_t)bidx * g.R, g.R, par,
+      band_solveT_chain<5, 2, 2>(g.lu0 + (size_t)bidx * gsz.R() * 5, g.rd0 + (size_t)bidx * gsz.R(), gsz.R(), par,
                                  reinterpret_cast<double*>(lane < 4 ? ca : cb) + pt, 2);
     }
     __syncwarp();
@@ -704,23 +709,23 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
       // before its flux correction, MC[3n + k + 1] - 0.5 flux_t add
       const size_t csz = coef_size(g);
       double mp = 0.0;
-      for (int i = lane; i < g.R; i += 32) {
-        const cpx p0 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + cidx(0, 0, 0), g.X, i);
-        cpx p1 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + csz + cidx(0, 0, 0), g.X, i);
+      for (int i = lane; i < gsz.R(); i += 32) {
+        const cpx p0 = band_matvec_row(g.Rps, 5, 2, 2, gsz.R(), xk + cidx(0, 0, 0), gsz.X(), i);
+        cpx p1 = band_matvec_row(g.Rps, 5, 2, 2, gsz.R(), xk + csz + cidx(0, 0, 0), gsz.X(), i);
         p1.re -= 0.5 * ft1 * rps_row_real(g, g.add0, i);
-        const cpx q0 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + cidx(1, 0, 0), g.X, i);
-        const cpx q1 = band_matvec_row(g.Rps, 5, 2, 2, g.R, xk + csz + cidx(1, 0, 0), g.X, i);
+        const cpx q0 = band_matvec_row(g.Rps, 5, 2, 2, gsz.R(), xk + cidx(1, 0, 0), gsz.X(), i);
+        const cpx q1 = band_matvec_row(g.Rps, 5, 2, 2, gsz.R(), xk + csz + cidx(1, 0, 0), gsz.X(), i);
         mp += re2 * dt * (ca[i].re * (akf * p0.re + bkf * p1.re) + ca[i].im * (akf * p0.im + bkf * p1.im));
         mp += re2 * dt * (cb[i].re * (akf * q0.re + bkf * q1.re) + cb[i].im * (akf * q0.im + bkf * q1.im));
       }
       gpart += mp;  // lane partials; the block reduction below adds every thread's
     }
-    for (int i = lane; i < g.R; i += 32) {
+    for (int i = lane; i < gsz.R(); i += 32) {
       fa[i] = fma(dt * ck, ca[i].re, fa[i]);
       fb[i] = fma(dt * ck, cb[i].re, fb[i]);
       if (k == 0) {
-        Cc[cidx(0, i, 0)] = band_matvecT_row(g.ex0, 5, 2, 2, g.R, ca, 1, i);
-        Cc[cidx(1, i, 0)] = band_matvecT_row(g.ex0, 5, 2, 2, g.R, cb, 1, i);
+        Cc[cidx(0, i, 0)] = band_matvecT_row(g.ex0, 5, 2, 2, gsz.R(), ca, 1, i);
+        Cc[cidx(1, i, 0)] = band_matvecT_row(g.ex0, 5, 2, 2, gsz.R(), cb, 1, i);
       } else {
         Cc[cidx(0, i, 0)] = ca[i];
         Cc[cidx(1, i, 0)] = cb[i];
@@ -749,47 +754,47 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
   // halved off the kx = 0 column (the transpose of the real-to-complex x
   // transform).  Plane pairs (y, -y) share the sums: weights of even type
   // (Qw, Rw) give E + O / E - O, of odd type (Qpw) E + O / O - E.
-  if (g.tc) quad_T_tc(g, z, x0, nx, xfirst, s, a.Hb.at(inst));
+  if (g.tc) quad_T_tc(g, gsz, z, x0, nx, xfirst, s, a.Hb.at(inst));
   const int lx = threadIdx.x % kTile, grp = threadIdx.x / kTile, ngrp = blockDim.x / kTile;
   if (lx >= nx) return;
   if (g.tc && lx >= xfirst) return;  // the tensor cores took every column but the mean one
   const int x = x0 + lx;
   const bool mean = (z == 0 && x == 0);
-  const double kx = g.Kx[x], kz = g.Kz[z], k2 = g.K2[(size_t)z * g.X + x];
+  const double kx = g.Kx[x], kz = g.Kz[z], k2 = g.K2[(size_t)z * gsz.X() + x];
   const double scl = x == 0 ? g.norm : 0.5 * g.norm;
   cpx* __restrict__ Hb = a.Hb.at(inst);
-  const size_t cs = (size_t)g.Q * g.X;
-  for (int yp = grp; yp < g.Qh; yp += ngrp) {
-    const int y1 = yp, y2 = g.Q - 1 - yp;
+  const size_t cs = (size_t)gsz.Q() * gsz.X();
+  for (int yp = grp; yp < gsz.Qh(); yp += ngrp) {
+    const int y1 = yp, y2 = gsz.Q() - 1 - yp;
     // E/O sums over even/odd rows: [0] Qpw^T Fa, [1] Qw^T Fa, [2] Rw^T Fb
     double er[3] = {0, 0, 0}, ei[3] = {0, 0, 0}, orr[3] = {0, 0, 0}, oi[3] = {0, 0, 0};
     if (!mean) {
       int i = 0;
-      for (; i + 1 < g.D; i += 2) {
+      for (; i + 1 < gsz.D(); i += 2) {
         const cpx f0 = s.Fa[i * kTile + lx], f1 = s.Fa[(i + 1) * kTile + lx];
-        cfma_t(__ldg(g.Wqp + (size_t)i * g.Q + yp), f0, er[0], ei[0]);
-        cfma_t(__ldg(g.Wqp + (size_t)(i + 1) * g.Q + yp), f1, orr[0], oi[0]);
-        cfma_t(__ldg(g.Wq + (size_t)i * g.Q + yp), f0, er[1], ei[1]);
-        cfma_t(__ldg(g.Wq + (size_t)(i + 1) * g.Q + yp), f1, orr[1], oi[1]);
+        cfma_t(__ldg(g.Wqp + (size_t)i * gsz.Q() + yp), f0, er[0], ei[0]);
+        cfma_t(__ldg(g.Wqp + (size_t)(i + 1) * gsz.Q() + yp), f1, orr[0], oi[0]);
+        cfma_t(__ldg(g.Wq + (size_t)i * gsz.Q() + yp), f0, er[1], ei[1]);
+        cfma_t(__ldg(g.Wq + (size_t)(i + 1) * gsz.Q() + yp), f1, orr[1], oi[1]);
       }
-      if (i < g.D) {
+      if (i < gsz.D()) {
         const cpx f0 = s.Fa[i * kTile + lx];
-        cfma_t(__ldg(g.Wqp + (size_t)i * g.Q + yp), f0, er[0], ei[0]);
-        cfma_t(__ldg(g.Wq + (size_t)i * g.Q + yp), f0, er[1], ei[1]);
+        cfma_t(__ldg(g.Wqp + (size_t)i * gsz.Q() + yp), f0, er[0], ei[0]);
+        cfma_t(__ldg(g.Wq + (size_t)i * gsz.Q() + yp), f0, er[1], ei[1]);
       }
       i = 0;
-      for (; i + 1 < g.R; i += 2) {
+      for (; i + 1 < gsz.R(); i += 2) {
         const cpx f0 = s.Fb[i * kTile + lx], f1 = s.Fb[(i + 1) * kTile + lx];
-        cfma_t(__ldg(g.Wr + (size_t)i * g.Q + yp), f0, er[2], ei[2]);
-        cfma_t(__ldg(g.Wr + (size_t)(i + 1) * g.Q + yp), f1, orr[2], oi[2]);
+        cfma_t(__ldg(g.Wr + (size_t)i * gsz.Q() + yp), f0, er[2], ei[2]);
+        cfma_t(__ldg(g.Wr + (size_t)(i + 1) * gsz.Q() + yp), f1, orr[2], oi[2]);
       }
-      if (i < g.R) cfma_t(__ldg(g.Wr + (size_t)i * g.Q + yp), s.Fb[i * kTile + lx], er[2], ei[2]);
+      if (i < gsz.R()) cfma_t(__ldg(g.Wr + (size_t)i * gsz.Q() + yp), s.Fb[i * kTile + lx], er[2], ei[2]);
     } else {
       const double* fa = s.m0;
-      const double* fb = s.m0 + g.R;
+      const double* fb = s.m0 + gsz.R();
       // [0] Rw^T fa, [2] Rw^T fb (real)
-      for (int i = 0; i < g.R; ++i) {
-        const double w = __ldg(g.Wr + (size_t)i * g.Q + yp);
+      for (int i = 0; i < gsz.R(); ++i) {
+        const double w = __ldg(g.Wr + (size_t)i * gsz.Q() + yp);
         if (i & 1) {
           orr[0] = fma(w, fa[i], orr[0]);
           orr[2] = fma(w, fb[i], orr[2]);
@@ -823,7 +828,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve_T(const __grid_constant__
         hy.re = -scl * k2 * qa.re;
         hy.im = -scl * k2 * qa.im;
       }
-      cpx* out = Hb + ((size_t)z * 5 * g.Q + y) * g.X + x;
+      cpx* out = Hb + ((size_t)z * 5 * gsz.Q() + y) * gsz.X() + x;
       out[0] = hz;
       out[cs] = hx;
       out[2 * cs] = hy;
@@ -862,14 +867,19 @@ cudaError_t launch_solve_T(const Grid& g, const SolveTArgs& a, cudaStream_t st) 
   if (a.ninst <= 0) return cudaSuccess;
   const int ntx = (g.X + kTile - 1) / kTile;
   const size_t sm = solveT_smem_bytes(g);
-  if (a.grids) k_solve_T<true><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
-  else k_solve_T<false><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
+  const bool fx = (g.fixed & FIXED_SOLVE) && !a.grids;  // the solve's fixed-size choice covers its transpose
+  if (a.grids) k_solve_T<true, SizesRT><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
+  else if (fx && sizes_match<Sizes32>(g)) k_solve_T<false, Sizes32><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
+  else if (fx && sizes_match<Sizes16>(g)) k_solve_T<false, Sizes16><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
+  else k_solve_T<false, SizesRT><<<dim3(g.Nz * ntx, a.ninst), kThreads, sm, st>>>(g, a);
   return cudaGetLastError();
 }
 
 void prepare_solve_T(int optin) {
-  allow_max_smem(k_solve_T<false>, optin);
-  allow_max_smem(k_solve_T<true>, optin);
+  allow_max_smem(k_solve_T<false, SizesRT>, optin);
+  allow_max_smem(k_solve_T<true, SizesRT>, optin);
+  allow_max_smem(k_solve_T<false, Sizes32>, optin);
+  allow_max_smem(k_solve_T<false, Sizes16>, optin);
 }
 
 }  // namespace chn

@@ -11,8 +11,8 @@ blocks at three, run-time / compiled sizes, 10 / 11 / 12 = one field per
 pass compiled for the sizes in 128 / 192 / 256-thread blocks at five / four
 / three) change how the columns of a plane are
 grouped, not the digit sums or their rounding; nor do the builds of the
-products, reconstruction and solve kernels compiled for those sizes
-(CHN_FIXED_SIZES=1), nor the adjoint products' planes per pass (1 or 3,
+products, reconstruction and solve kernels (and the exact adjoint's
+transposed solve) compiled for those sizes (CHN_FIXED_SIZES=1), nor the adjoint products' planes per pass (1 or 3,
 CHN_ADJ_PRODUCTS_PER_PASS; the reference adjoint and the exact one), nor
 the reconstruction's build (CHN_RECON_BUILD: 0 = 16 columns in 256-thread
 blocks at two per SM, 1 = 8 columns in 128-thread blocks at four, 2 = 16
