@@ -430,6 +430,11 @@ struct Engine {
   Work batch;      // c_batch_*
   bool have_batch = false;
   cudaStream_t st = nullptr;
+  // a second stream and the events that fork and join the concurrent
+  // branches of a substage (chains_concurrent)
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool conc = true;  // CHN_CONCURRENT_CHAINS at creation
   int nsteps = 0;
   std::vector<double> qy, qw;
   cpx* host_mc = nullptr;   // pinned mirrors for c_getsoln / c_getincresoln
@@ -438,6 +443,47 @@ struct Engine {
 };
 
 static Engine* E = nullptr;
+
+static bool engine_streams_create(Engine& e) {
+  const char* v = getenv("CHN_CONCURRENT_CHAINS");
+  e.conc = !(v && v[0] == '0');
+  if (cudaStreamCreateWithFlags(&e.st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&e.st2, cudaStreamNonBlocking) != cudaSuccess)
+    return false;
+  for (cudaEvent_t& v : e.ev)
+    if (cudaEventCreateWithFlags(&v, cudaEventDisableTiming) != cudaSuccess) return false;
+  return true;
+}
+
+static void engine_streams_destroy(Engine& e) {
+  for (cudaEvent_t& v : e.ev)
+    if (v) cudaEventDestroy(v);
+  for (cudaEvent_t& v : e.ev) v = nullptr;
+  if (e.st2) cudaStreamDestroy(e.st2);
+  if (e.st) cudaStreamDestroy(e.st);
+  e.st2 = e.st = nullptr;
+}
+
+// Independent chains of a substage (the primal's and the tangents' kernels
+// of a forward substage, the reference adjoint's two product passes) run as
+// concurrent branches: on st and st2 outside a graph, as parallel branches
+// of the captured step inside one, joined by events where one reads what
+// the other writes and at the end of the substage, so each fills the other's
+// last waves.  Only where the kernels share no scratch (the one-block-per-
+// plane tensor-core transforms; the split and FFT passes share Work::Zt).
+// The arithmetic is the same either way.  CHN_CONCURRENT_CHAINS=0 (read at
+// c_init / c_multi_init) keeps one stream.
+static bool chains_concurrent(const Engine& e) {
+  const Grid& g = e.T.g;
+  return e.conc && e.st2 && g.tci && g.tcf && !g.split && !g.tc5;
+}
+
+// st2 waits for what st has enqueued so far (fork), or the reverse (join)
+static bool fork_to(Engine& e, cudaStream_t from, cudaStream_t to, int ev) {
+  CK(cudaEventRecord(e.ev[ev], from));
+  CK(cudaStreamWaitEvent(to, e.ev[ev], 0));
+  return true;
+}
 
 // sizes and shorthands
 static inline Batch<const cpx> cb(const cpx* p, long long s) { return Batch<const cpx>{p, s}; }
@@ -467,7 +513,11 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
   cudaStream_t st = e.st;
   const int nt = w.nseg * w.ntan;
   const bool use_cache = o.cache && w.Pc != nullptr;
+  // the tangents' chain on its own branch where the primal advances beside it
+  const bool conc = o.tangents && o.adv_primal && chains_concurrent(e);
+  cudaStream_t stt = conc ? e.st2 : st;
   for (int k = 0; k < 3; ++k) {
+    if (conc && !fork_to(e, st, stt, 0)) return false;
     // where this substage's primal physical fields live
     Batch<const double> Pprim = cbd(w.Pp, w.psz);
     SlotRef pslot = noslot();
@@ -502,7 +552,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
       rt.U = mb(w.Ut, w.usz);
       rt.status = w.status;
       rt.sdiv = w.ntan;
-      LK(launch_recon(g, rt, st));
+      LK(launch_recon(g, rt, stt));
     }
     if (need_primal_fields) {
       PhysArgs pp{};
@@ -520,6 +570,7 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
       pp.cfl_check = k == 0;  // channel/pass1.c:117
       pp.skip_blocked = 1;
       LK(launch_phys_inverse(g, pp, st));
+      if (conc) CK(cudaEventRecord(e.ev[1], st));  // the tangents' products read these fields
     }
     if (o.tangents) {
       PhysArgs pt{};
@@ -534,10 +585,10 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
       pt.status = w.status;
       pt.sdiv = w.ntan;
       pt.skip_blocked = 1;
-      LK(launch_phys_inverse(g, pt, st));
+      LK(launch_phys_inverse(g, pt, stt));
       if (k == 0 && w.Pv)
         LK(launch_cache_velocity(g, w.Pt, w.psz, w.ntan, w.couple, w.Pv, w.vstride, w.vslot, w.step, 0, w.status,
-                                 w.nseg, st));
+                                 w.nseg, stt));
       ProdArgs ap{};
       ap.grids = w.gdev;
       ap.tmp = w.Zt;
@@ -550,7 +601,8 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
       ap.ninst = nt;
       ap.status = w.status;
       ap.sdiv = w.ntan;
-      LK(launch_products_fwd(g, ap, st));
+      if (conc) CK(cudaStreamWaitEvent(stt, e.ev[1], 0));
+      LK(launch_products_fwd(g, ap, stt));
     }
     if (o.adv_primal) {
       ProdArgs ap{};
@@ -590,6 +642,8 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
       sa.Fts = w.Ft;
       sa.fts_stride = 3 * (long long)w.nsteps + 1;
       LK(launch_solve(g, sa, st));
+      // a tangent Re forcing reads the primal states and fluxes this solve stores
+      if (conc && (o.re2_mask | o.re3_mask) && !fork_to(e, st, stt, 2)) return false;
     }
     if (o.tangents) {
       SolveArgs sa{};
@@ -620,8 +674,9 @@ static bool enqueue_forward_step(Engine& e, Work& w, const FwdOpts& o) {
         sa.Ftr = w.Ft;
         sa.ftr_stride = 3 * (long long)w.nsteps + 1;
       }
-      LK(launch_solve(g, sa, st));
+      LK(launch_solve(g, sa, stt));
     }
+    if (conc && !fork_to(e, stt, st, 3)) return false;  // join
   }
   LK(launch_step_advance(w.step, +1, st));
   return true;
@@ -767,12 +822,16 @@ static bool enqueue_adjoint_step(Engine& e, Work& w, double strength_dt, bool ca
     a.Pp = Pcur;
     a.pslot = scur;
     a.H = mb(w.Up, w.usz);
+    // the two passes read the same adjoint fields and write apart: branches
+    const bool conc = k < 2 && chains_concurrent(e);
+    if (conc && !fork_to(e, st, e.st2, 0)) return false;
     LK(launch_products_adj(g, a, st));
     if (k < 2) {
       a.Pp = Pprv;
       a.pslot = sprv;
       a.H = mb(w.Uprev, w.usz);
-      LK(launch_products_adj(g, a, st));
+      LK(launch_products_adj(g, a, conc ? e.st2 : st));
+      if (conc && !fork_to(e, e.st2, st, 3)) return false;  // join
     }
     SolveArgs s{};
     s.grids = w.gdev;
@@ -1883,14 +1942,15 @@ int c_init(int Nx, int Ny, int Nz, double Lx, double Lz, double Re, double flux,
     return 1;
   }
   Engine* e = new Engine();
-  if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess) {
+  if (!engine_streams_create(*e)) {
     set_error(-1, "no CUDA device available");
+    engine_streams_destroy(*e);
     delete e;
     return 1;
   }
   if (!build_device_tables(e->T, Nx, Ny, Nz, Lx, Lz, Re, flux, dt)) {
     e->T.release();
-    cudaStreamDestroy(e->st);
+    engine_streams_destroy(*e);
     delete e;
     return 1;
   }
@@ -1900,7 +1960,7 @@ int c_init(int Nx, int Ny, int Nz, double Lx, double Lz, double Re, double flux,
   if (!e->single.create(e->T.g, 1, 1, nsteps, 0)) {
     e->single.release();
     e->T.release();
-    cudaStreamDestroy(e->st);
+    engine_streams_destroy(*e);
     delete e;
     return 1;
   }
@@ -1919,7 +1979,7 @@ void c_destroy(void) {
   if (E->host_mc) cudaFreeHost(E->host_mc);
   if (E->host_mic) cudaFreeHost(E->host_mic);
   E->T.release();
-  cudaStreamDestroy(E->st);
+  engine_streams_destroy(*E);
   delete E;
   E = nullptr;
 }
@@ -2458,8 +2518,7 @@ struct Multi {
     tabs.clear();
     if (gdev) cudaFree(gdev);
     gdev = nullptr;
-    if (e.st) cudaStreamDestroy(e.st);
-    e.st = nullptr;
+    engine_streams_destroy(e);
   }
 };
 static Multi* MX = nullptr;
@@ -2518,7 +2577,7 @@ int c_multi_init(int n, const int* Nx, const int* Ny, const int* Nz, const doubl
   }
   Multi* m = new Multi();
   MX = m;
-  if (cudaStreamCreateWithFlags(&m->e.st, cudaStreamNonBlocking) != cudaSuccess) {
+  if (!engine_streams_create(m->e)) {
     set_error(-1, "no CUDA device available");
     c_multi_destroy();
     return -1;

@@ -18,7 +18,9 @@ the reconstruction's build (CHN_RECON_BUILD: 0 = 16 columns in 256-thread
 blocks at two per SM, 1 = 8 columns in 128-thread blocks at four, 2 = 16
 columns at three without the table prefetch), nor the products' build
 (CHN_PRODUCTS_BUILD: 1 = two product planes per pass at three blocks per
-SM).  Each variant runs the
+SM), nor the concurrent branches of a substage (CHN_CONCURRENT_CHAINS: the
+primal and tangent chains of a forward substage and the adjoint's two
+product passes on two streams, or one).  Each variant runs the
 batched forward (primal + 3 tangents, one forced), the coupled adjoint
 and the exact adjoint, and the single-trajectory primal, and must reproduce the default's outputs
 bit for bit.  Grids: 32x65x32 (the benchmarked one), 16x33x16 (both with
@@ -41,7 +43,7 @@ GRIDS = [(32, 65, 32, 2 * np.pi, np.pi, 3300.0, 2.0, 0.005, 3), (48, 97, 48, 2 *
          (16, 33, 16, 2 * np.pi, np.pi, 2000.0, 2.0, 0.01, 3)]
 NSEG, NTAN = 2, 3
 KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_FIXED_SIZES", "CHN_ADJ_PRODUCTS_PER_PASS", "CHN_RECON_BUILD",
-         "CHN_PRODUCTS_BUILD", "CHN_AUTOTUNE")
+         "CHN_PRODUCTS_BUILD", "CHN_AUTOTUNE", "CHN_CONCURRENT_CHAINS")
 
 
 @pytest.fixture(scope="module")
@@ -141,6 +143,13 @@ def test_recon_builds_give_the_same_bits(cc, gi, build, fixed):
 def test_products_builds_give_the_same_bits(cc, gi, fixed):
     a, _ = _sweeps(cc, GRIDS[gi], {"CHN_PRODUCTS_BUILD": "0", "CHN_AUTOTUNE": "0"})
     b, _ = _sweeps(cc, GRIDS[gi], {"CHN_PRODUCTS_BUILD": "1", "CHN_FIXED_SIZES": fixed, "CHN_AUTOTUNE": "0"})
+    _same(a, b)
+
+
+@pytest.mark.parametrize("gi", [0, 1, 2])
+def test_concurrent_chains_give_the_same_bits(cc, gi):
+    a, _ = _sweeps(cc, GRIDS[gi], {"CHN_CONCURRENT_CHAINS": "0", "CHN_AUTOTUNE": "0"})
+    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_CONCURRENT_CHAINS": "1", "CHN_AUTOTUNE": "0"})
     _same(a, b)
 
 
