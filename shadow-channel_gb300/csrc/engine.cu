@@ -478,6 +478,13 @@ static bool chains_concurrent(const Engine& e) {
   return e.conc && e.st2 && g.tci && g.tcf && !g.split && !g.tc5;
 }
 
+// both streams drained: before the engine's arrays are released (a failed
+// enqueue can leave a branch on st2 that never joined st)
+static void engine_sync(Engine& e) {
+  if (e.st) cudaStreamSynchronize(e.st);
+  if (e.st2) cudaStreamSynchronize(e.st2);
+}
+
 // st2 waits for what st has enqueued so far (fork), or the reverse (join)
 static bool fork_to(Engine& e, cudaStream_t from, cudaStream_t to, int ev) {
   CK(cudaEventRecord(e.ev[ev], from));
@@ -1973,7 +1980,7 @@ int c_init(int Nx, int Ny, int Nz, double Lx, double Lz, double Re, double flux,
 
 void c_destroy(void) {
   if (!E) return;
-  cudaStreamSynchronize(E->st);
+  engine_sync(*E);
   E->single.release();
   if (E->have_batch) E->batch.release();
   if (E->host_mc) cudaFreeHost(E->host_mc);
@@ -2250,7 +2257,7 @@ int c_batch_init_steps(int nseg, int ntan, int couple, int nsteps) {
   }
   Engine& e = *E;
   if (e.have_batch) {
-    cudaStreamSynchronize(e.st);
+    engine_sync(e);
     e.batch.release();
     e.have_batch = false;
   }
@@ -2269,7 +2276,7 @@ int c_batch_init_steps(int nseg, int ntan, int couple, int nsteps) {
 
 int c_batch_destroy(void) {
   if (!E || !E->have_batch) return 0;
-  cudaStreamSynchronize(E->st);
+  engine_sync(*E);
   E->batch.release();
   E->have_batch = false;
   return 0;
@@ -2512,7 +2519,7 @@ struct Multi {
   std::vector<size_t> off;     // packed offsets
   Grid* gdev = nullptr;
   void release() {
-    if (e.st) cudaStreamSynchronize(e.st);
+    engine_sync(e);
     if (e.have_batch) e.batch.release();
     for (DevTables& t : tabs) t.release();
     tabs.clear();
