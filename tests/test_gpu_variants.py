@@ -43,7 +43,7 @@ GRIDS = [(32, 65, 32, 2 * np.pi, np.pi, 3300.0, 2.0, 0.005, 3), (48, 97, 48, 2 *
          (16, 33, 16, 2 * np.pi, np.pi, 2000.0, 2.0, 0.01, 3)]
 NSEG, NTAN = 2, 3
 KNOBS = ("CHN_SOLVE_TILE", "CHN_INVERSE_BUILD", "CHN_FIXED_SIZES", "CHN_ADJ_PRODUCTS_PER_PASS", "CHN_RECON_BUILD",
-         "CHN_PRODUCTS_BUILD", "CHN_AUTOTUNE", "CHN_CONCURRENT_CHAINS")
+         "CHN_PRODUCTS_BUILD", "CHN_AUTOTUNE", "CHN_CONCURRENT_CHAINS", "CHN_NO_FIELD_CACHE")
 
 
 @pytest.fixture(scope="module")
@@ -146,10 +146,13 @@ def test_products_builds_give_the_same_bits(cc, gi, fixed):
     _same(a, b)
 
 
-@pytest.mark.parametrize("gi", [0, 1, 2])
-def test_concurrent_chains_give_the_same_bits(cc, gi):
-    a, _ = _sweeps(cc, GRIDS[gi], {"CHN_CONCURRENT_CHAINS": "0", "CHN_AUTOTUNE": "0"})
-    b, _ = _sweeps(cc, GRIDS[gi], {"CHN_CONCURRENT_CHAINS": "1", "CHN_AUTOTUNE": "0"})
+@pytest.mark.parametrize("gi,cache", [(0, "1"), (1, "1"), (2, "1"), (0, "0"), (2, "0")])
+def test_concurrent_chains_give_the_same_bits(cc, gi, cache):
+    """with and without the primal field cache (without it the primal's
+    fields share one buffer across substages, read by both branches)"""
+    env = {"CHN_AUTOTUNE": "0", "CHN_NO_FIELD_CACHE": "1" if cache == "0" else "0"}
+    a, _ = _sweeps(cc, GRIDS[gi], {**env, "CHN_CONCURRENT_CHAINS": "0"})
+    b, _ = _sweeps(cc, GRIDS[gi], {**env, "CHN_CONCURRENT_CHAINS": "1"})
     _same(a, b)
 
 
